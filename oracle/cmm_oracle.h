@@ -1,0 +1,171 @@
+/*
+ * cmm_oracle.h -- CPU restatement (plain C99 + OpenMP, FP64) of the
+ * characteristic-mapping-method time step of Arcadia197/cmm-turbulence.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the parity checker for the
+ * CUDA product in cmm-turbulence_gb300/.  Only tests/, __graft_entry__.smoke()
+ * and bench.py's cpu_baseline / --impl reference legs may load it.  The
+ * product never links, loads or falls back to it.
+ *
+ * Every routine restates the reference's arithmetic in the reference's
+ * memory layout (planar Hermite planes [f, f_x, f_y, f_xy], row-major
+ * iY*NX+iX) and cites the reference file:line it follows.  Paths are
+ * relative to the reference project's Cuda-CMM/ directory.
+ *
+ * Parity pin: the reference's own golden Debug_globals / Mesure /
+ * Monitoring_data files (tests/euler2D_init_fields, tests/euler2D_one_step,
+ * tests/euler2D_11b_4nodes_reference_remapping) are reproduced by this
+ * oracle; see tests/test_oracle_golden.py.  The reference's FFT is cuFFT
+ * (closed); this oracle uses its own mixed-radix FFT (og_fft.c), so FFT
+ * rounding differs at the 1e-16 level.
+ */
+#ifndef CMM_ORACLE_H
+#define CMM_ORACLE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Grid metadata: src/grid/cmm-grid2d.h:25-39, ctor src/grid/cmm-grid2d.cu:20-52. */
+typedef struct {
+    int NX, NY, NX_fft;
+    long N, Nfft;
+    double hx, hy;
+    double bounds[4];
+} og_grid;
+
+void og_grid_fill(og_grid* g, int NX, int NY, const double* bounds);
+
+/* ---------------- Hermite helpers (src/numerical/cmm-hermite.cu) ---------------- */
+double og_hermite_interpolate_2D(const double* H, double x, double y, const og_grid* g);
+double og_hermite_interpolate_dx_2D(const double* H, double x, double y, const og_grid* g);
+double og_hermite_interpolate_dy_2D(const double* H, double x, double y, const og_grid* g);
+void og_hermite_interpolate_grad_2D(const double* H, const double* x, double* u, const og_grid* g, int n_l);
+void og_diffeo_interpolate_2D(const double* Hx, const double* Hy, double x, double y,
+                              double* x2, double* y2, const og_grid* g);
+double og_diffeo_grad_2D(const double* Hx, const double* Hy, double x, double y, const og_grid* g);
+
+/* ---------------- time stepping (src/numerical/cmm-timestep.cu) ---------------- */
+double og_get_L_coefficient(const double* t, double t_next, int loop_ctr, int i_point, int l_order);
+
+/* ---------------- kernels restated as loops ---------------- */
+/* k_init_diffeo: src/simulation/cmm-simulation-kernel.cu:27-41 */
+void og_init_diffeo(double* ChiX, double* ChiY, const og_grid* g);
+/* advect_using_stream_hermite + k_advect_using_stream_hermite (direction -1):
+ * src/simulation/cmm-simulation-host.cu:64-104, src/simulation/cmm-simulation-kernel.cu:207-298.
+ * L1/L12 are the Lagrange coefficients, c1/cx/cy/cxy the footpoint weights. */
+void og_advect_map(const double* ChiX, const double* ChiY, double* ChiX_new, double* ChiY_new,
+                   const double* psi, const og_grid* gmap, const og_grid* gpsi,
+                   double dt, double ep, int time_integration_num, int map_update_order_num,
+                   int l_order, const double* L1, const double* L12,
+                   const double* c1, const double* cx, const double* cy, const double* cxy);
+/* footpoint weights: src/simulation/cmm-simulation-host.cu:76-90 */
+void og_map_update_coefficients(int map_update_order_num, double ep,
+                                double* c1, double* cx, double* cy, double* cxy);
+/* incompressibility_check: src/simulation/cmm-simulation-host.cu:44-50 +
+ * k_incompressibility_check src/simulation/cmm-simulation-kernel.cu:159-173 */
+double og_incompressibility_check(const og_grid* gcheck, const og_grid* gmap,
+                                  const double* ChiX, const double* ChiY);
+/* k_h_sample_map_compact / k_apply_map_compact: src/simulation/cmm-simulation-kernel.cu:302-340 */
+void og_sample_map_compact(const double* ChiX, const double* ChiY, double* x_y,
+                           const og_grid* gmap, const og_grid* g);
+void og_apply_map_compact(const double* ChiX, const double* ChiY, double* x_y,
+                          const og_grid* gmap, const og_grid* g);
+/* d_init_vorticity "4_nodes": src/simulation/cmm-init.cu:45-52 */
+double og_init_vorticity(double x, double y, int ic_num);
+/* k_apply_map_and_sample_from_hermite: src/simulation/cmm-simulation-kernel.cu:402-461 */
+void og_apply_map_and_sample_from_hermite(const double* ChiX, const double* ChiY, double* fs,
+                                          const double* H, const og_grid* gmap, const og_grid* gvort,
+                                          const og_grid* gfine, int molly_stencil, int padd_inline_fft);
+
+/* ---------------- spectral (src/numerical/cmm-fft.cu) ---------------- */
+/* complex arrays are interleaved (re, im) doubles, length 2*Nfft */
+void og_fft_d2z(const og_grid* g, const double* in, double* out_c);
+void og_fft_z2d(const og_grid* g, const double* in_c, double* out);
+void og_normalize_h(double* F, const og_grid* g);
+void og_fft_grid_move(const double* in_c, double* out_c, const og_grid* gout, const og_grid* gin);
+void og_fft_cut_off_scale_h(double* W, const og_grid* g, double freq);
+void og_fft_iLap_h(const double* in_c, double* out_c, const og_grid* g);
+void og_fft_dx_h(const double* in_c, double* out_c, const og_grid* g);
+void og_fft_dy_h(const double* in_c, double* out_c, const og_grid* g);
+/* fourier_hermite: src/numerical/cmm-fft.cu:398-429; out has 4*N doubles */
+void og_fourier_hermite(const og_grid* g, const double* in_c, double* out4);
+
+/* ---------------- the Euler-2D driver (src/simulation/cmm-euler2d.cu) ---------------- */
+typedef struct {
+    int num;                      /* particles in the set */
+    double tau;                   /* only tau == 0 (fluid tracers) is restated */
+    int time_integration_num;     /* 10, 20, 30, 40 */
+    double init_time;
+} og_particle_set;
+
+typedef struct {
+    int grid_coarse, grid_fine, grid_psi, grid_vort;
+    double bounds[4];
+    double dt;
+    int time_integration_num;     /* map advection scheme (30 = RK3) */
+    int lagrange_order;           /* after particle / override adjustment */
+    int lagrange_init_higher_order;
+    int map_update_order_num;     /* 0 = 2nd, 1 = 4th, 2 = 6th */
+    double map_epsilon;
+    double incomp_threshold;
+    int skip_remapping;
+    int molly_stencil;
+    double freq_cut_psi;
+    int initial_condition_num;    /* 0 = 4_nodes */
+    int initial_discrete;
+    int initial_discrete_grid;
+    int max_maps;                 /* stack capacity (cpu_map_num) */
+    int n_particle_sets;
+    og_particle_set psets[8];
+} og_settings;
+
+typedef struct og_state og_state;
+
+og_state* og_create(const og_settings* s);
+void og_destroy(og_state* st);
+/* discrete IC values (NxN row-major) -- Hermite form is built internally
+ * (src/simulation/cmm-euler2d.cu:325-344) */
+int og_set_discrete_initial(og_state* st, const double* values);
+/* particle initial positions (interleaved x,y) for set i */
+int og_set_particles(og_state* st, int i_set, const double* pos);
+/* initial state + Lagrange history (src/simulation/cmm-euler2d.cu:495-619) */
+int og_init(og_state* st);
+/* one loop iteration (src/simulation/cmm-euler2d.cu:750-897); dt_now from the
+ * caller (compute_next_timestep). Returns 0 ok, 1 stack saturated (loop stops). */
+int og_step(og_state* st, double dt_now, double* e_inc, int* remapped);
+
+/* state access (reference layouts) */
+double og_time(const og_state* st);
+int og_map_count(const og_state* st);
+int og_loop_ctr(const og_state* st);
+int og_old_ctr(const og_state* st);
+const double* og_chix(const og_state* st);        /* 4*Nc */
+const double* og_chiy(const og_state* st);
+const double* og_psi(const og_state* st);         /* L*4*Npsi, level 0 first */
+const double* og_vort_coarse(const og_state* st); /* Nc */
+const double* og_vort_fine(const og_state* st);   /* 4*Nf */
+const double* og_particles(const og_state* st, int i_set);
+const og_grid* og_grid_of(const og_state* st, int which); /* 0 coarse,1 fine,2 psi,3 vort */
+
+/* diagnostics: src/numerical/cmm-mesure.cu:30-89, cmm-simulation-host.cu:668-680 */
+double og_energy_H(const og_state* st);
+double og_enstrophy(const og_state* st);
+double og_palinstrophy(const og_state* st);
+double og_max_vorticity(const og_state* st);
+/* debug globals (src/numerical/cmm-mesure.cu:217-249): grid form uses hx*hy, raw form /N */
+void og_stats_grid(const double* v, const og_grid* g, double* out4);
+void og_stats_raw(const double* v, long n, double* out4);
+/* ψ_x, ψ_y at particle positions (k_h_sample_points_dxdy, cmm-simulation-kernel.cu:138-155) */
+void og_sample_points_dxdy(const og_state* st, const double* pos, double* out, int num);
+
+/* particle advection on an explicit ψ history (src/numerical/cmm-particles.cu:119-276) */
+void og_particle_advect(int num, double dt, double* pos, const double* psi, const og_grid* g,
+                        int time_integration_num, int l_order, const double* Lp12);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

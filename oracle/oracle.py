@@ -1,0 +1,224 @@
+"""ctypes wrapper of the CPU parity oracle (liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: loaded by tests/, __graft_entry__.smoke() and the
+CPU-baseline legs of bench.py, never by the product.  The C sources restate
+the reference's algorithm (see cmm_oracle.h for the citations).
+
+`EulerOracle` drives og_init / og_step with the reference's host-side loop
+logic (src/simulation/cmm-euler2d.cu:750-960: compute_next_timestep,
+final-time clipping, save instants) so tests can compare with the golden
+monitoring files the reference writes.
+"""
+import ctypes as C
+import math
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+
+def build(force=False):
+    """Compile liboracle.so with the committed Makefile (gcc + OpenMP)."""
+    srcs = [os.path.join(HERE, f) for f in ("og_hermite.c", "og_fft.c", "og_euler.c", "cmm_oracle.h")]
+    if not force and os.path.exists(LIB_PATH):
+        if os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(s) for s in srcs):
+            return LIB_PATH
+    subprocess.run(["make", "-s", "-C", HERE, "-B", "liboracle.so"], check=True)
+    return LIB_PATH
+
+
+class OgGrid(C.Structure):
+    _fields_ = [("NX", C.c_int), ("NY", C.c_int), ("NX_fft", C.c_int),
+                ("N", C.c_long), ("Nfft", C.c_long),
+                ("hx", C.c_double), ("hy", C.c_double), ("bounds", C.c_double * 4)]
+
+
+class OgParticleSet(C.Structure):
+    _fields_ = [("num", C.c_int), ("tau", C.c_double), ("time_integration_num", C.c_int),
+                ("init_time", C.c_double)]
+
+
+class OgSettings(C.Structure):
+    _fields_ = [("grid_coarse", C.c_int), ("grid_fine", C.c_int), ("grid_psi", C.c_int),
+                ("grid_vort", C.c_int), ("bounds", C.c_double * 4), ("dt", C.c_double),
+                ("time_integration_num", C.c_int), ("lagrange_order", C.c_int),
+                ("lagrange_init_higher_order", C.c_int), ("map_update_order_num", C.c_int),
+                ("map_epsilon", C.c_double), ("incomp_threshold", C.c_double),
+                ("skip_remapping", C.c_int), ("molly_stencil", C.c_int),
+                ("freq_cut_psi", C.c_double), ("initial_condition_num", C.c_int),
+                ("initial_discrete", C.c_int), ("initial_discrete_grid", C.c_int),
+                ("max_maps", C.c_int), ("n_particle_sets", C.c_int),
+                ("psets", OgParticleSet * 8)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        dp = C.POINTER(C.c_double)
+        L.og_create.restype = C.c_void_p
+        L.og_create.argtypes = [C.POINTER(OgSettings)]
+        L.og_destroy.argtypes = [C.c_void_p]
+        L.og_init.argtypes = [C.c_void_p]
+        L.og_step.argtypes = [C.c_void_p, C.c_double, dp, C.POINTER(C.c_int)]
+        L.og_set_particles.argtypes = [C.c_void_p, C.c_int, dp]
+        L.og_set_discrete_initial.argtypes = [C.c_void_p, dp]
+        for name in ("og_chix", "og_chiy", "og_psi", "og_vort_coarse", "og_vort_fine"):
+            getattr(L, name).restype = dp
+            getattr(L, name).argtypes = [C.c_void_p]
+        L.og_particles.restype = dp
+        L.og_particles.argtypes = [C.c_void_p, C.c_int]
+        L.og_grid_of.restype = C.POINTER(OgGrid)
+        L.og_grid_of.argtypes = [C.c_void_p, C.c_int]
+        for name in ("og_time", "og_energy_H", "og_enstrophy", "og_palinstrophy", "og_max_vorticity"):
+            getattr(L, name).restype = C.c_double
+            getattr(L, name).argtypes = [C.c_void_p]
+        for name in ("og_map_count", "og_loop_ctr", "og_old_ctr"):
+            getattr(L, name).restype = C.c_int
+            getattr(L, name).argtypes = [C.c_void_p]
+        L.og_sample_points_dxdy.argtypes = [C.c_void_p, dp, dp, C.c_int]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def stats_grid(v, hx, hy):
+    """Debug-globals grid form (src/numerical/cmm-mesure.cu:217-232)."""
+    v = np.asarray(v, dtype=np.float64)
+    return [float(v.min()), float(v.max()), hx * hy * max(0.0, float(v.max())), hx * hy * float(v.sum())]
+
+
+def stats_raw(v):
+    """Debug-globals raw-array form (src/numerical/cmm-mesure.cu:234-249)."""
+    v = np.asarray(v, dtype=np.float64)
+    n = v.size
+    return [float(v.min()), float(v.max()), max(0.0, float(v.max())) / n, float(v.sum()) / n]
+
+
+class EulerOracle:
+    """CPU restatement of one Euler-2D run, configured from a `Settings` object
+    (cmm-turbulence_gb300 host-side settings mirror) or a plain dict."""
+
+    def __init__(self, cfg):
+        self.cfg = cfg
+        L = lib()
+        s = OgSettings()
+        s.grid_coarse, s.grid_fine = cfg["grid_coarse"], cfg["grid_fine"]
+        s.grid_psi, s.grid_vort = cfg["grid_psi"], cfg["grid_vort"]
+        for i in range(4):
+            s.bounds[i] = cfg["bounds"][i]
+        s.dt = cfg["dt"]
+        s.time_integration_num = cfg["time_integration_num"]
+        s.lagrange_order = cfg["lagrange_order"]
+        s.lagrange_init_higher_order = int(cfg["lagrange_init_higher_order"])
+        s.map_update_order_num = cfg["map_update_order_num"]
+        s.map_epsilon = cfg["map_epsilon"]
+        s.incomp_threshold = cfg["incomp_threshold"]
+        s.skip_remapping = int(cfg["skip_remapping"])
+        s.molly_stencil = cfg["molly_stencil"]
+        s.freq_cut_psi = cfg["freq_cut_psi"]
+        s.initial_condition_num = cfg["initial_condition_num"]
+        s.initial_discrete = int(cfg.get("initial_discrete", 0))
+        s.initial_discrete_grid = cfg.get("initial_discrete_grid", 1)
+        s.max_maps = cfg["max_maps"]
+        psets = cfg.get("particles", [])
+        s.n_particle_sets = len(psets)
+        for i, p in enumerate(psets):
+            s.psets[i].num = p["num"]
+            s.psets[i].tau = p["tau"]
+            s.psets[i].time_integration_num = p["time_integration_num"]
+            s.psets[i].init_time = p["init_time"]
+        self._s = s
+        self.h = L.og_create(C.byref(s))
+        self.L = L
+
+    def close(self):
+        if self.h:
+            self.L.og_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def grid(self, which):
+        g = self.L.og_grid_of(self.h, which).contents
+        return g
+
+    def set_discrete_initial(self, values):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        self.L.og_set_discrete_initial(self.h, _dp(v))
+
+    def set_particles(self, i, pos):
+        p = np.ascontiguousarray(pos, dtype=np.float64)
+        self.L.og_set_particles(self.h, i, _dp(p))
+
+    def init(self):
+        self.L.og_init(self.h)
+
+    def step(self, dt_now):
+        e = C.c_double()
+        r = C.c_int()
+        rc = self.L.og_step(self.h, dt_now, C.byref(e), C.byref(r))
+        return rc, e.value, bool(r.value)
+
+    def _arr(self, fn, n):
+        return np.ctypeslib.as_array(fn(self.h), shape=(n,)).copy()
+
+    def chix(self):
+        return self._arr(self.L.og_chix, 4 * self.grid(0).N)
+
+    def chiy(self):
+        return self._arr(self.L.og_chiy, 4 * self.grid(0).N)
+
+    def psi(self, levels=1):
+        return self._arr(self.L.og_psi, 4 * self.grid(2).N * levels)
+
+    def vort(self):
+        return self._arr(self.L.og_vort_coarse, self.grid(0).N)
+
+    def vort_fine(self):
+        return self._arr(self.L.og_vort_fine, 4 * self.grid(1).N)
+
+    def particles(self, i):
+        n = self.cfg["particles"][i]["num"]
+        return np.ctypeslib.as_array(self.L.og_particles(self.h, i), shape=(2 * n,)).copy()
+
+    def particle_velocity(self, i):
+        pos = self.particles(i)
+        out = np.empty_like(pos)
+        self.L.og_sample_points_dxdy(self.h, _dp(pos), _dp(out), len(pos) // 2)
+        return out
+
+    def time(self):
+        return self.L.og_time(self.h)
+
+    def map_count(self):
+        return self.L.og_map_count(self.h)
+
+    def loop_ctr(self):
+        return self.L.og_loop_ctr(self.h)
+
+    def old_ctr(self):
+        return self.L.og_old_ctr(self.h)
+
+    def energy(self):
+        return self.L.og_energy_H(self.h)
+
+    def enstrophy(self):
+        return self.L.og_enstrophy(self.h)
+
+    def palinstrophy(self):
+        return self.L.og_palinstrophy(self.h)
+
+    def max_vorticity(self):
+        return self.L.og_max_vorticity(self.h)

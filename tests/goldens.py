@@ -1,0 +1,158 @@
+"""Golden-fixture helpers shared by the CPU (oracle) and GPU (product) tests.
+
+`reference_goldens.json` holds the reference's own golden monitoring series
+(see tests/golden/make_golden.py).  `DebugRecorder` produces the same series
+from any simulation state using the reference's writer semantics
+(src/ui/cmm-io.cu:295-437 for which variables are written,
+src/numerical/cmm-mesure.cu:217-249 for the statistics).
+"""
+import json
+import os
+
+import numpy as np
+
+from refloop import save_instant
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_G = None
+
+
+def goldens():
+    global _G
+    if _G is None:
+        with open(os.path.join(HERE, "golden", "reference_goldens.json")) as f:
+            _G = json.load(f)
+    return _G
+
+
+def stats_grid(v, hx, hy):
+    v = np.asarray(v, dtype=np.float64)
+    return [float(v.min()), float(v.max()), hx * hy * max(0.0, float(v.max())), hx * hy * float(v.sum())]
+
+
+def stats_raw(v):
+    v = np.asarray(v, dtype=np.float64)
+    return [float(v.min()), float(v.max()), max(0.0, float(v.max())) / v.size, float(v.sum()) / v.size]
+
+
+def _has(var, *keys):
+    return any(k in var for k in keys)
+
+
+class DebugRecorder:
+    """Collects Debug_globals / Mesure / monitoring series like the reference
+    writes them at verbose=4.  `state` must provide grid(k) -> (N, hx, hy),
+    chix(), chiy(), psi(), vort(), particles(i), particle_velocity(i),
+    energy(), enstrophy(), palinstrophy(), max_vorticity()."""
+
+    def __init__(self, settings, state):
+        self.s = settings
+        self.st = state
+        self.series = {}
+
+    def _app(self, key, vals):
+        self.series.setdefault(key, []).extend(vals)
+
+    def _stat(self, name, vals):
+        for suf, v in zip(("Min", "Max", "Avg", "L2"), vals):
+            self._app("Debug_globals/%s_%s" % (name, suf), [v])
+
+    def on_save(self, t_now, dt_now):
+        s, st = self.s, self.st
+        dt = s.dt
+        var = ""
+        fire = False
+        for r in s.save_comp:
+            if save_instant([r], t_now, dt_now, dt):
+                fire = True
+                var += r.var
+        if fire:
+            all_ = "All" in var
+            gc, gp = st.grid(0), st.grid(2)
+            if _has(var, "Vorticity", "W", "Stream", "Psi", "Map", "Chi", "Velocity", "U", "Dist", "F") or all_:
+                self._app("Debug_globals/Time_s", [t_now])
+                saved_any = True
+            else:
+                saved_any = False
+            if _has(var, "Vorticity", "W") or all_:
+                self._stat("Vorticity_W_coarse", stats_grid(st.vort(), gc[1], gc[2]))
+            if _has(var, "Dist", "F") or all_:
+                self._stat("Distribution_coarse", stats_grid(st.vort(), gc[1], gc[2]))
+            psi = None
+            if _has(var, "Stream", "Psi") or all_:
+                psi = st.psi()
+                self._stat("Stream_function_Psi_psi", stats_grid(psi[:gp[0]], gp[1], gp[2]))
+            if _has(var, "Stream_H", "Psi_H") or all_:
+                psi = st.psi() if psi is None else psi
+                self._stat("Stream_function_Psi_H_psi", stats_raw(psi[:4 * gp[0]]))
+            if _has(var, "Velocity", "U") or all_:
+                psi = st.psi() if psi is None else psi
+                self._stat("Velocity_UX_psi", stats_grid(psi[gp[0]:2 * gp[0]], gp[1], gp[2]))
+                self._stat("Velocity_UY_psi", stats_grid(psi[2 * gp[0]:3 * gp[0]], gp[1], gp[2]))
+            if _has(var, "Map_b", "Chi_b") or all_:
+                self._stat("Map_ChiX_coarse", stats_grid(st.chix()[:gc[0]], gc[1], gc[2]))
+                self._stat("Map_ChiY_coarse", stats_grid(st.chiy()[:gc[0]], gc[1], gc[2]))
+            if _has(var, "Map_H", "Chi_H") or all_:
+                self._stat("Map_ChiX_H_coarse", stats_raw(st.chix()))
+                self._stat("Map_ChiY_H_coarse", stats_raw(st.chiy()))
+            if "PartA_" in var or all_:
+                if not saved_any:
+                    self._app("Debug_globals/Time_s", [t_now])
+            for i, p in enumerate(s.particles_advected):
+                if ("PartA_%02d" % (i + 1)) in var or all_:
+                    self._stat("Particles_advected_pos_P%02d" % (i + 1), stats_raw(st.particles(i)))
+                if ("PartA_Vel_%02d" % (i + 1)) in var or all_:
+                    if p.tau == 0:
+                        self._stat("Particles_advected_vel_U%02d" % (i + 1), stats_raw(st.particle_velocity(i)))
+        # compute_conservation_targets (cmm-simulation-host.cu:615-698)
+        if save_instant(s.save_comp, t_now, dt_now, dt, need_conv=True):
+            self._app("Mesure/Time_s", [t_now])
+            self._app("Mesure/Energy", [st.energy()])
+            self._app("Mesure/Enstrophy", [st.enstrophy()])
+            self._app("Mesure/Palinstrophy", [st.palinstrophy()])
+            self._app("Mesure/Max_vorticity", [st.max_vorticity()])
+
+    def on_step(self, loop_ctr, t, e_inc, gap, maps):
+        self._app("Time_s", [t])
+        self._app("Error_incompressibility", [e_inc])
+        self._app("Map_gaps", [float(gap)])
+        self._app("Map_counter", [float(maps)])
+
+
+def compare_series(ours, gold, keys, rtol):
+    """Return list of (key, worst scaled error) and failures.  Each golden value
+    g is compared to ours o as |o-g| <= rtol*scale, scale being the magnitude of
+    the data the statistic summarises (so sums of zero-mean fields compare on
+    the magnitude of their terms, not on their near-zero total)."""
+    worst = []
+    fails = []
+    for k in keys:
+        if k not in gold:
+            continue
+        g = np.asarray(gold[k], dtype=np.float64)
+        o = np.asarray(ours.get(k, []), dtype=np.float64)
+        if o.shape != g.shape:
+            fails.append((k, "length %d vs golden %d" % (o.size, g.size)))
+            continue
+        base = k.rsplit("_", 1)[0] if k.startswith("Debug_globals/") else k
+        if k.startswith("Debug_globals/") and k.rsplit("_", 1)[-1] in ("Min", "Max", "Avg", "L2"):
+            mn = np.abs(np.asarray(gold.get(base + "_Min", g)))
+            mx = np.abs(np.asarray(gold.get(base + "_Max", g)))
+            mag = np.maximum(mn, mx)
+            if k.endswith("_L2") or k.endswith("_Avg"):
+                # grid form multiplies by hx*hy*N ~ area; raw form divides by N
+                area_scale = np.maximum(np.abs(g), mag * (4 * np.pi ** 2 if "Particles" not in k and "_H_" not in k else 1.0))
+                scale = np.maximum(area_scale, 1e-300)
+            else:
+                scale = np.maximum(mag, 1e-300)
+        elif k == "Error_incompressibility":
+            # |1 - det grad X| with det ~ 1: the error is absolute on the scale of det
+            scale = np.ones_like(g)
+        else:
+            scale = np.maximum(np.abs(g), 1e-300)
+        err = np.abs(o - g) / scale
+        e = float(err.max()) if err.size else 0.0
+        worst.append((k, e))
+        if not np.all(err <= rtol):
+            fails.append((k, e))
+    return worst, fails

@@ -1,0 +1,58 @@
+"""Adapter giving the CPU oracle the state interface used by goldens.DebugRecorder
+and refloop.run_reference_loop (test infrastructure)."""
+import numpy as np
+
+import oracle as O
+
+
+class OracleRun:
+    def __init__(self, settings, particle_init=None):
+        self.s = settings
+        self.o = O.EulerOracle(settings.oracle_config())
+        self.particle_init = particle_init or {}
+
+    # stepper interface
+    def init(self):
+        for i, pos in self.particle_init.items():
+            self.o.set_particles(i, pos)
+        self.o.init()
+
+    def step(self, dt_now):
+        rc, e, r = self.o.step(dt_now)
+        gap = (self.o.loop_ctr() - 1) - self.o.old_ctr()
+        return rc, e, r, gap, self.o.map_count()
+
+    # state interface
+    def grid(self, k):
+        g = self.o.grid(k)
+        return (g.N, g.hx, g.hy)
+
+    def chix(self):
+        return self.o.chix()
+
+    def chiy(self):
+        return self.o.chiy()
+
+    def psi(self):
+        return self.o.psi()
+
+    def vort(self):
+        return self.o.vort()
+
+    def particles(self, i):
+        return self.o.particles(i)
+
+    def particle_velocity(self, i):
+        return self.o.particle_velocity(i)
+
+    def energy(self):
+        return self.o.energy()
+
+    def enstrophy(self):
+        return self.o.enstrophy()
+
+    def palinstrophy(self):
+        return self.o.palinstrophy()
+
+    def max_vorticity(self):
+        return self.o.max_vorticity()

@@ -1,0 +1,341 @@
+"""Benchmark of the CMM time step on one GB300 (and the CPU reference arm).
+
+Workload (the metric's configuration): 2D Euler decaying turbulence, map grid
+512^2, fine / vorticity grid 2048^2, psi grid 1024^2, dt = 1/256, random-phase
+initial vorticity with energy spectrum E(k) ~ k^4 exp(-(k/8)^2) normalised to
+unit enstrophy (Z = 1/2 hx hy sum w^2), map stack up to 200 sub-maps
+(mem_RAM_CPU_remaps=3356), 10^6 RK3 tracer particles.  One "step" is one
+iteration of the reference loop (map advection, incompressibility check,
+remap when needed, psi solve, coarse vorticity, particles, monitors).
+
+  python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  `value` is steps/s with the state resident in HBM,
+timed with CUDA events on the library's stream; `e2e` is the same metric
+through the C-ABI with the initial vorticity uploaded from pinned host memory,
+the initialisation, and every step's monitoring record plus the final psi
+read back to the host inside the timed region.  `--impl reference` times the
+CPU implementation of the same step (the FP64 OpenMP oracle restating the
+reference algorithm) on the host cores.
+"""
+import argparse
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+TWO_PI = 6.283185307179586
+WORKLOAD = dict(grid_coarse=512, grid_fine=2048, grid_psi=1024, grid_vort=2048, steps_per_sec=256,
+                mem_RAM_CPU_remaps=3356, particles=1000000, seed=0, k0=8.0)
+METRIC = "steps/s (512² map, 2048² fine): chosen vs plain FP64 at ≤1e-4 enstrophy err"
+
+
+def initial_vorticity(n=2048, seed=0, k0=8.0):
+    """Random-phase field with E(k) ~ k^4 exp(-(k/k0)^2), unit enstrophy."""
+    rng = np.random.default_rng(seed)
+    kx = np.fft.rfftfreq(n, 1.0 / n)
+    ky = np.fft.fftfreq(n, 1.0 / n)
+    k = np.sqrt(kx[None, :] ** 2 + ky[:, None] ** 2)
+    ek = k ** 4 * np.exp(-(k / k0) ** 2)
+    amp = np.zeros_like(k)
+    nz = k > 0
+    amp[nz] = np.sqrt(k[nz] ** 2 * ek[nz] / (2 * np.pi * k[nz]))   # |w_k|^2 ~ k^2 E(k) / (2 pi k)
+    phase = rng.uniform(0.0, 2 * np.pi, size=k.shape)
+    w = np.fft.irfft2(amp * np.exp(1j * phase), s=(n, n))
+    h = TWO_PI / n
+    z = 0.5 * h * h * np.sum(w * w)
+    return np.ascontiguousarray(w / np.sqrt(z))
+
+
+def sim_args(workspace, precision="fp64", particles=WORKLOAD["particles"]):
+    w = WORKLOAD
+    return ["workspace=%s/" % workspace, "sim_name=bench", "simulation_type=cmm_euler_2d",
+            "grid_coarse=%d" % w["grid_coarse"], "grid_fine=%d" % w["grid_fine"], "grid_psi=%d" % w["grid_psi"],
+            "grid_vort=%d" % w["grid_vort"], "set_dt_by_steps=1", "steps_per_sec=%d" % w["steps_per_sec"],
+            "final_time=10", "initial_condition=4_nodes", "initial_discrete=1",
+            "initial_discrete_grid=%d" % w["grid_fine"], "time_integration=RK3", "map_update_order=4th",
+            "map_epsilon=0.001", "incomp_threshold=0.0001", "skip_remapping=0", "molly_stencil=0",
+            "freq_cut_psi=128", "lagrange_init_higher_order=1", "mem_RAM_CPU_remaps=%d" % w["mem_RAM_CPU_remaps"],
+            "save_computational_num=0", "save_sample_num=0", "save_zoom_num=0", "forward_map=0", "verbose=0",
+            "precision=%s" % precision, "particles_advected_num=1"], \
+           ["{num=%d,tau=0,seed=0,time_integration=RK3,init_name=uniform,init_time=0,init_vel=0,"
+            "init_param_1=3.141592653589793,init_param_2=3.141592653589793,init_param_3=6.283185307179586,"
+            "init_param_4=6.283185307179586}" % particles]
+
+
+def write_param_file(path, args, records):
+    """The reference's param-file format, so the record list can follow particles_advected_num."""
+    lines = ["CMM Parameter file", "param_version\t=\t3", ""]
+    for a in args:
+        k, v = a.split("=", 1)
+        lines.append("%s\t=\t%s" % (k, v))
+    for r in records:
+        lines.append("particles_advected\t=\t%s" % r)
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                      "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.splitlines()[0].split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        if shutil.which("nvidia-smi"):
+            self._t = threading.Thread(target=self._run, daemon=True)
+            self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = sorted(float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit())
+        mx = max(float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 5 + i and s[5 + i] == "Active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------------- roofline bookkeeping
+def advect_model(w, L=3, nfoot=8):
+    """Algorithmic bytes and FP64 flops of one map-advection launch (per time step)."""
+    Nc, Np = w["grid_coarse"] ** 2, w["grid_psi"] ** 2
+    bytes_ = 8 * (8 * Nc + 4 * L * Np + 8 * Nc)      # read map + psi levels, write new map
+    flops = nfoot * (304 + 304 + 176 + 120 + 30) * Nc + 128 * Nc
+    return bytes_, flops
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+FP64_PEAK_TFLOPS = 1.20   # FP64 FMA throughput measured on this machine's GB300 (profiles/fp64_fma_probe.md)
+
+
+def cpu_oracle_steps(n_steps, ic, threads, particles=100000):
+    """Time n_steps of the CPU oracle on the C2 workload (after its initialisation)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    import oracle as O
+    w = WORKLOAD
+    cfg = dict(grid_coarse=w["grid_coarse"], grid_fine=w["grid_fine"], grid_psi=w["grid_psi"],
+               grid_vort=w["grid_vort"], bounds=[0, TWO_PI, 0, TWO_PI], dt=1.0 / w["steps_per_sec"],
+               time_integration_num=30, lagrange_order=3, lagrange_init_higher_order=1, map_update_order_num=1,
+               map_epsilon=1e-3, incomp_threshold=1e-4, skip_remapping=0, molly_stencil=0, freq_cut_psi=128.0,
+               initial_condition_num=0, initial_discrete=1, initial_discrete_grid=w["grid_fine"],
+               max_maps=200, particles=[dict(num=particles, tau=0.0, time_integration_num=30, init_time=0.0)])
+    o = O.EulerOracle(cfg)
+    o.set_discrete_initial(ic)
+    rng = np.random.default_rng(0)
+    o.set_particles(0, rng.uniform(0, TWO_PI, 2 * particles))
+    o.init()
+    t0 = time.perf_counter()
+    for _ in range(n_steps):
+        o.step(cfg["dt"])
+    dt = time.perf_counter() - t0
+    o.close()
+    return n_steps / dt, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    ic = initial_vorticity(WORKLOAD["grid_fine"], WORKLOAD["seed"], WORKLOAD["k0"])
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    steps = max(1, args.steps)
+    sps, secs = cpu_oracle_steps(steps + args.warmup, ic, threads, particles=WORKLOAD["particles"])
+    # the timed figure covers warmup + steps; all are full steps of the same workload
+    line = {"impl": "reference", "metric": METRIC, "value": sps, "unit": "steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / sps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "euler2d-turbulence coarse512 fine2048 psi1024 dt1/256 1e6 tracers",
+                       "form": "plain FP64 (CPU restatement of the reference algorithm)"},
+            "cpu_baseline": {"value": sps, "unit": "steps/s", "cores": threads, "kind": "port",
+                             "sample": "%d full steps of the workload after the Lagrange initialisation, %.1f s"
+                                       % (steps + args.warmup, secs)},
+            "e2e": {"value": sps, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import __graft_entry__ as ge
+    ge.build()
+    m = ge.package()
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    ic = initial_vorticity(WORKLOAD["grid_fine"], WORKLOAD["seed"], WORKLOAD["k0"])
+    work = tempfile.mkdtemp(prefix="cmm_bench_")
+    cli, recs = sim_args(work, args.precision)
+    pf = os.path.join(work, "params.txt")
+    write_param_file(pf, cli, recs)
+
+    stream = torch.cuda.Stream()
+    sim = m.Simulation(["param_file=" + pf], stream=stream.cuda_stream)
+    sim.set_initial_discrete(ic)
+    sim.init()
+    for _ in range(args.warmup):
+        sim.step(1)
+
+    # ---- value: K steps, state resident in HBM, CUDA events on the library stream
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    l0 = sim.scalar("kernel_launches")
+    maps0 = sim.scalar("map_counter")
+    with ClockSampler() as clocks:
+        e0.record(stream)
+        for _ in range(args.steps):
+            sim.step(1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+        ms = float(t.item())
+    launches = int(sim.scalar("kernel_launches") - l0)
+    remaps = int(sim.scalar("map_counter") - maps0)
+    ms_per_step = ms / args.steps
+    value = world * args.steps / (ms / 1000.0)
+
+    # ---- profiled pass: per-phase CUDA-event times of the same steps
+    sim.set_profiling(True)
+    prof_steps = max(3, min(args.steps, 20))
+    for _ in range(prof_steps):
+        sim.step(1)
+    phases = {}
+    for ph in ("advect", "incomp", "remap", "psi", "coarse", "particles", "save"):
+        n = sim.scalar("prof_%s_count" % ph)
+        phases[ph] = {"ms_total": sim.scalar("prof_%s_ms" % ph), "launches": int(n)}
+    sim.close()
+
+    # ---- e2e through the C-ABI with host buffers
+    ic_pinned = torch.from_numpy(ic).pin_memory()
+    stream2 = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim2 = m.Simulation(["param_file=" + pf], stream=stream2.cuda_stream)
+    sim2.set_initial_discrete(ic_pinned.numpy())
+    sim2.init()
+    d2h = 0
+    for _ in range(args.steps):
+        sim2.step(1)
+        sim2.scalar("e_inc")          # the step's monitoring record (read back inside the step)
+        d2h += 8
+    psi = sim2.field("Stream_function_Psi_H_psi")
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    d2h += psi.nbytes
+    sim2.close()
+    e2e = world * args.steps / e2e_s
+
+    # ---- roofline of the dominant kernel (map advection, FP64)
+    adv = phases["advect"]
+    adv_ms = adv["ms_total"] / max(1, adv["launches"])
+    bytes_, flops = advect_model(WORKLOAD)
+    peak, peak_kind = load_peaks()
+    achieved = bytes_ / (adv_ms / 1000.0) / 1e9
+    roof = {"kernel": "k_advect (FP64 GALS map advection)", "bound": "hbm", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "peak_source": "of " + peak_kind, "traffic": None,
+            "ms_per_launch": adv_ms,
+            "fp64": {"achieved_tflops": flops / (adv_ms / 1000.0) / 1e12, "peak_tflops": FP64_PEAK_TFLOPS,
+                     "frac": flops / (adv_ms / 1000.0) / 1e12 / FP64_PEAK_TFLOPS,
+                     "note": "the plain FP64 form is bound by GB300's FP64 issue rate, not HBM"}}
+
+    # ---- CPU baseline (oracle) on a bounded sample, rank 0 only
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        n = 3
+        sps, secs = cpu_oracle_steps(n, ic, threads, particles=WORKLOAD["particles"])
+        cpu = {"value": sps, "unit": "steps/s", "cores": threads, "kind": "port",
+               "sample": "%d full workload steps after the oracle's Lagrange initialisation (%.1f s)" % (n, secs)}
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "euler2d-turbulence coarse512 fine2048 psi1024 dt1/256 1e6 tracers",
+                       "form": "plain FP64" if args.precision == "fp64" else args.precision,
+                       "remaps_in_timed_region": remaps,
+                       "l2": "working set per step > 129 MB L2 (psi levels 100 MB + fine vorticity 134 MB)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "clocks": clocks.summary(), "gpu_launches": launches,
+            "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": ic.nbytes / args.steps,
+                    "d2h_bytes_per_step": d2h / args.steps,
+                    "includes": "IC upload + init + every step + final psi readback"},
+            "roofline": roof, "phases_ms_per_step": {k: v["ms_total"] / max(1, v["launches"]) for k, v in phases.items()},
+            "cpu_baseline": cpu}
+    print(json.dumps(line))
+    shutil.rmtree(work, ignore_errors=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

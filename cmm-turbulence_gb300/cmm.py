@@ -1,0 +1,235 @@
+"""Python binding of libcmm_gb300.so (the C-ABI of include/cmm_abi.h) via ctypes.
+
+This is the reference-facing host API used by tests, smoke() and bench.py:
+`Simulation(argv)` mirrors the reference executable's COMMAND=VALUE /
+param_file interface, and the module-level kernel functions mirror its host
+functions on caller-owned device buffers.  There is no CPU fallback: loading
+fails loudly when the CUDA library has not been built.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libcmm_gb300.so")
+CLI_PATH = os.path.join(HERE, "lib", "SimulationCuda2d.out")
+
+CMM_OK = 0
+CMM_ERR_PARAM = -1
+CMM_ERR_IO = -2
+CMM_ERR_CUDA = -3
+CMM_ERR_SATURATED = -4
+CMM_ERR_STATE = -5
+CMM_ERR_UNSUPPORTED = -6
+CMM_ERR_NOT_FOUND = -7
+
+# every entry point declared in include/cmm_abi.h
+EXPORTS = [
+    "cmm_last_error", "cmm_version", "cmm_create", "cmm_set_stream", "cmm_set_initial_discrete", "cmm_init",
+    "cmm_step", "cmm_run", "cmm_get_field", "cmm_field_bytes", "cmm_get_scalar", "cmm_set_profiling",
+    "cmm_settings_text",
+    "cmm_file_name", "cmm_destroy", "cmm_advect_map", "cmm_incomp_max", "cmm_compose_stack", "cmm_sample_vort",
+    "cmm_poisson_create", "cmm_poisson_hermite", "cmm_poisson_destroy", "cmm_particles_advect", "cmm_diagnostics",
+]
+
+
+class CmmError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("cmm error %d: %s" % (code, msg))
+        self.code = code
+
+
+class CmmGrid(C.Structure):
+    _fields_ = [("NX", C.c_int), ("NY", C.c_int), ("bounds", C.c_double * 4)]
+
+
+def grid(n, bounds=(0.0, 6.283185307179586, 0.0, 6.283185307179586)):
+    g = CmmGrid()
+    g.NX = g.NY = int(n)
+    for i in range(4):
+        g.bounds[i] = float(bounds[i])
+    return g
+
+
+_lib = None
+
+
+def lib():
+    """Load libcmm_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libcmm_gb300.so is missing: run __graft_entry__.build() (nvcc, sm_103a)")
+    L = C.CDLL(LIB_PATH)
+    vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.c_int
+    L.cmm_last_error.restype = C.c_char_p
+    L.cmm_version.restype = C.c_char_p
+    L.cmm_create.argtypes = [ip, C.POINTER(C.c_char_p), C.POINTER(vp)]
+    L.cmm_set_stream.argtypes = [vp, vp]
+    L.cmm_set_initial_discrete.argtypes = [vp, dp, C.c_size_t]
+    L.cmm_init.argtypes = [vp]
+    L.cmm_step.argtypes = [vp, ip]
+    L.cmm_run.argtypes = [vp]
+    L.cmm_get_field.argtypes = [vp, C.c_char_p, vp, C.c_size_t]
+    L.cmm_field_bytes.argtypes = [vp, C.c_char_p]
+    L.cmm_field_bytes.restype = C.c_size_t
+    L.cmm_get_scalar.argtypes = [vp, C.c_char_p, dp]
+    L.cmm_set_profiling.argtypes = [vp, ip]
+    L.cmm_settings_text.argtypes = [vp, C.c_char_p, C.c_size_t]
+    L.cmm_file_name.argtypes = [vp, C.c_char_p, C.c_size_t]
+    L.cmm_destroy.argtypes = [vp]
+    gp = C.POINTER(CmmGrid)
+    L.cmm_advect_map.argtypes = [gp, gp, vp, vp, vp, vp, C.POINTER(vp), ip, dp, dp, C.c_double, C.c_double, ip, ip, vp]
+    L.cmm_incomp_max.argtypes = [gp, gp, vp, vp, vp, vp]
+    L.cmm_compose_stack.argtypes = [gp, gp, vp, vp, vp, ip, ip, vp, gp, vp, vp]
+    L.cmm_sample_vort.argtypes = [gp, gp, gp, vp, vp, vp, ip, vp, vp]
+    L.cmm_poisson_create.argtypes = [gp, gp, C.c_double, vp, C.POINTER(vp)]
+    L.cmm_poisson_hermite.argtypes = [vp, vp, vp]
+    L.cmm_poisson_destroy.argtypes = [vp]
+    L.cmm_particles_advect.argtypes = [gp, vp, ip, C.POINTER(vp), ip, dp, C.c_double, ip, vp]
+    L.cmm_diagnostics.argtypes = [gp, vp, gp, vp, dp, vp]
+    _lib = L
+    return L
+
+
+def last_error():
+    return lib().cmm_last_error().decode()
+
+
+def check(rc, allow=()):
+    if rc < 0 and rc not in allow:
+        raise CmmError(rc, last_error())
+    return rc
+
+
+def _dptr(a):
+    """Device or host pointer of a numpy array / torch tensor / int."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+def _darr(vals):
+    arr = (C.c_double * max(1, len(vals)))(*[float(v) for v in vals])
+    return arr
+
+
+class Simulation:
+    """One CMM run configured like `SimulationCuda2d.out [param_file=F] [KEY=VALUE ...]`."""
+
+    def __init__(self, argv, stream=None):
+        L = lib()
+        args = ["cmm"] + [str(a) for a in argv]
+        arr = (C.c_char_p * len(args))(*[a.encode() for a in args])
+        h = C.c_void_p()
+        check(L.cmm_create(len(args), arr, C.byref(h)))
+        self.h = h
+        self.L = L
+        if stream is not None:
+            check(L.cmm_set_stream(self.h, C.c_void_p(stream)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cmm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_initial_discrete(self, values):
+        import numpy as np
+        v = np.ascontiguousarray(values, dtype=np.float64).ravel()
+        check(self.L.cmm_set_initial_discrete(self.h, v.ctypes.data_as(C.POINTER(C.c_double)), v.size))
+
+    def init(self):
+        return check(self.L.cmm_init(self.h))
+
+    def step(self, n=1):
+        return check(self.L.cmm_step(self.h, int(n)), allow=(CMM_ERR_SATURATED,))
+
+    def run(self):
+        return check(self.L.cmm_run(self.h), allow=(CMM_ERR_SATURATED,))
+
+    def field(self, name):
+        import numpy as np
+        nb = self.L.cmm_field_bytes(self.h, name.encode())
+        if nb == 0 and name != "Map_stack":
+            raise CmmError(CMM_ERR_NOT_FOUND, "unknown field " + name)
+        out = np.empty(nb // 8, dtype=np.float64)
+        check(self.L.cmm_get_field(self.h, name.encode(), out.ctypes.data_as(C.c_void_p), nb))
+        return out
+
+    def scalar(self, name):
+        v = C.c_double()
+        check(self.L.cmm_get_scalar(self.h, name.encode(), C.byref(v)))
+        return v.value
+
+    def set_profiling(self, on=True):
+        check(self.L.cmm_set_profiling(self.h, 1 if on else 0))
+
+    def settings_text(self):
+        n = self.L.cmm_settings_text(self.h, None, 0)
+        buf = C.create_string_buffer(n + 1)
+        self.L.cmm_settings_text(self.h, buf, n + 1)
+        return buf.value.decode()
+
+    def file_name(self):
+        buf = C.create_string_buffer(4096)
+        self.L.cmm_file_name(self.h, buf, 4096)
+        return buf.value.decode()
+
+
+# ---------------------------------------------------------------- kernel API
+def advect_map(gm, gp, chix, chiy, chix_out, chiy_out, psi_levels, L1, L12, dt, eps, ti=30, order=1, stream=None):
+    levels = (C.c_void_p * len(psi_levels))(*[_dptr(p) for p in psi_levels])
+    return check(lib().cmm_advect_map(C.byref(gm), C.byref(gp), _dptr(chix), _dptr(chiy), _dptr(chix_out),
+                                      _dptr(chiy_out), levels, len(psi_levels), _darr(L1), _darr(L12), dt, eps, ti,
+                                      order, stream))
+
+
+def incomp_max(gcheck, gm, chix, chiy, d_result, stream=None):
+    return check(lib().cmm_incomp_max(C.byref(gcheck), C.byref(gm), _dptr(chix), _dptr(chiy), _dptr(d_result), stream))
+
+
+def compose_stack(gm, gt, chix, chiy, stack, n_maps, ic_num, out, discrete=None, gd=None, stream=None):
+    return check(lib().cmm_compose_stack(C.byref(gm), C.byref(gt), _dptr(chix), _dptr(chiy), _dptr(stack), n_maps,
+                                         ic_num, _dptr(discrete), C.byref(gd) if gd is not None else None,
+                                         _dptr(out), stream))
+
+
+def sample_vort(gm, gout, gf, chix, chiy, w_fine, out, molly=0, stream=None):
+    return check(lib().cmm_sample_vort(C.byref(gm), C.byref(gout), C.byref(gf), _dptr(chix), _dptr(chiy),
+                                       _dptr(w_fine), molly, _dptr(out), stream))
+
+
+class Poisson:
+    def __init__(self, gv, gp, freq, stream=None):
+        self.h = C.c_void_p()
+        check(lib().cmm_poisson_create(C.byref(gv), C.byref(gp), freq, stream, C.byref(self.h)))
+
+    def __call__(self, vort, psi_out):
+        return check(lib().cmm_poisson_hermite(self.h, _dptr(vort), _dptr(psi_out)))
+
+    def close(self):
+        if self.h:
+            lib().cmm_poisson_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+def particles_advect(gp, pos, num, psi_levels, Lp12, dt, ti=30, stream=None):
+    levels = (C.c_void_p * len(psi_levels))(*[_dptr(p) for p in psi_levels])
+    return check(lib().cmm_particles_advect(C.byref(gp), _dptr(pos), num, levels, len(psi_levels), _darr(Lp12), dt,
+                                            ti, stream))
+
+
+def diagnostics(gp, psi, gc, vort, stream=None):
+    out = (C.c_double * 3)()
+    check(lib().cmm_diagnostics(C.byref(gp), _dptr(psi), C.byref(gc), _dptr(vort), out, stream))
+    return list(out)

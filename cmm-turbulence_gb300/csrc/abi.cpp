@@ -1,0 +1,361 @@
+// abi.cpp -- extern "C" entry points declared in include/cmm_abi.h.
+#include "../../include/cmm_abi.h"
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "kernels.hpp"
+#include "settings.hpp"
+#include "sim.hpp"
+
+struct cmm_ctx {
+    cmm::Settings settings;
+    cmm::EulerSim* sim = nullptr;
+    cudaStream_t stream = nullptr;
+    std::vector<double> discrete;
+};
+
+struct cmm_poisson {
+    cmm::Grid gv, gp;
+    double freq = 0;
+    cudaStream_t stream = nullptr;
+    cmm::FftPlans pv, pp;
+    double2* spec = nullptr;
+    double2* spec4 = nullptr;
+};
+
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg)
+{
+    g_err = msg;
+    return code;
+}
+
+int cuda_rc(cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return CMM_OK;
+    return fail(CMM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bool to_grid(const cmm_grid* g, cmm::Grid* out)
+{
+    if (!g || g->NX <= 0 || g->NY <= 0 || !(g->bounds[1] > g->bounds[0]) || !(g->bounds[3] > g->bounds[2])) return false;
+    *out = cmm::make_grid(g->NX, g->NY, g->bounds);
+    return true;
+}
+
+int copy_text(const std::string& t, char* buf, size_t cap)
+{
+    if (buf && cap > 0) {
+        size_t n = t.size() < cap - 1 ? t.size() : cap - 1;
+        memcpy(buf, t.data(), n);
+        buf[n] = 0;
+    }
+    return (int)t.size();
+}
+
+int sim_rc(cmm::EulerSim* sim, int rc)
+{
+    if (rc < 0) g_err = sim->err;
+    return rc;
+}
+}  // namespace
+
+extern "C" {
+
+const char* cmm_last_error(void) { return g_err.c_str(); }
+const char* cmm_version(void) { return "cmm-gb300 0.1 (sm_103a, FP64 plain form)"; }
+
+int cmm_create(int argc, const char* const* argv, cmm_ctx** out)
+{
+    if (!out) return fail(CMM_ERR_PARAM, "out is NULL");
+    *out = nullptr;
+    cmm_ctx* c = new (std::nothrow) cmm_ctx();
+    if (!c) return fail(CMM_ERR_PARAM, "out of host memory");
+    if (!c->settings.apply_cli(argc, argv)) {
+        std::string e = c->settings.error;
+        delete c;
+        return fail(e.find("parameter file") != std::string::npos ? CMM_ERR_IO : CMM_ERR_PARAM, e);
+    }
+    c->settings.file_name = c->settings.derived_file_name();
+    *out = c;
+    g_err.clear();
+    return CMM_OK;
+}
+
+int cmm_set_stream(cmm_ctx* c, void* stream)
+{
+    if (!c) return fail(CMM_ERR_PARAM, "ctx is NULL");
+    if (c->sim) return fail(CMM_ERR_STATE, "cmm_set_stream after cmm_init");
+    c->stream = static_cast<cudaStream_t>(stream);
+    return CMM_OK;
+}
+
+int cmm_set_initial_discrete(cmm_ctx* c, const double* v, size_t n)
+{
+    if (!c || !v) return fail(CMM_ERR_PARAM, "NULL argument");
+    if (c->sim) return fail(CMM_ERR_STATE, "cmm_set_initial_discrete after cmm_init");
+    size_t need = (size_t)c->settings.initial_discrete_grid * c->settings.initial_discrete_grid;
+    if (n != need) return fail(CMM_ERR_PARAM, "discrete initial condition needs initial_discrete_grid^2 values");
+    c->discrete.assign(v, v + n);
+    return CMM_OK;
+}
+
+int cmm_init(cmm_ctx* c)
+{
+    if (!c) return fail(CMM_ERR_PARAM, "ctx is NULL");
+    if (c->sim) return fail(CMM_ERR_STATE, "cmm_init called twice");
+    c->sim = new (std::nothrow) cmm::EulerSim(c->settings);
+    if (!c->sim) return fail(CMM_ERR_PARAM, "out of host memory");
+    if (c->stream) c->sim->set_stream(c->stream);
+    if (!c->discrete.empty()) {
+        int rc = c->sim->set_initial_discrete(c->discrete.data(), c->discrete.size());
+        if (rc) return sim_rc(c->sim, rc);
+    }
+    int rc = c->sim->init();
+    c->discrete.clear();
+    return sim_rc(c->sim, rc);
+}
+
+int cmm_step(cmm_ctx* c, int n)
+{
+    if (!c || !c->sim) return fail(CMM_ERR_STATE, "cmm_step before cmm_init");
+    for (int i = 0; i < n; ++i) {
+        int rc = c->sim->step_once();
+        if (rc != 0) return sim_rc(c->sim, rc);
+    }
+    return CMM_OK;
+}
+
+int cmm_run(cmm_ctx* c)
+{
+    if (!c || !c->sim) return fail(CMM_ERR_STATE, "cmm_run before cmm_init");
+    int status = CMM_OK;
+    while (true) {
+        int rc = c->sim->step_once();
+        if (rc == 1) break;
+        if (rc == CMM_ERR_SATURATED) { status = rc; g_err = "map stack saturated"; break; }
+        if (rc < 0) return sim_rc(c->sim, rc);
+    }
+    int rc = c->sim->finish();
+    if (rc) return sim_rc(c->sim, rc);
+    return status;
+}
+
+int cmm_get_field(cmm_ctx* c, const char* name, void* dst, size_t bytes)
+{
+    if (!c || !c->sim || !name || !dst) return fail(CMM_ERR_STATE, "cmm_get_field needs an initialised ctx, a name and a buffer");
+    return sim_rc(c->sim, c->sim->get_field(name, dst, bytes));
+}
+
+size_t cmm_field_bytes(cmm_ctx* c, const char* name)
+{
+    if (!c || !c->sim || !name) return 0;
+    return c->sim->field_bytes(name);
+}
+
+int cmm_get_scalar(cmm_ctx* c, const char* name, double* out)
+{
+    if (!c || !name || !out) return fail(CMM_ERR_PARAM, "NULL argument");
+    if (!c->sim) {
+        std::string n = name;
+        if (n == "dt") { *out = c->settings.dt(); return CMM_OK; }
+        if (n == "lagrange_order") { *out = c->settings.effective_lagrange_order(); return CMM_OK; }
+        if (n == "stack_capacity") { *out = c->settings.cpu_map_num(); return CMM_OK; }
+        return fail(CMM_ERR_STATE, "scalar needs cmm_init");
+    }
+    return sim_rc(c->sim, c->sim->get_scalar(name, out));
+}
+
+int cmm_set_profiling(cmm_ctx* c, int on)
+{
+    if (!c || !c->sim) return fail(CMM_ERR_STATE, "cmm_set_profiling needs an initialised ctx");
+    c->sim->set_profiling(on != 0);
+    return CMM_OK;
+}
+
+int cmm_settings_text(cmm_ctx* c, char* buf, size_t cap)
+{
+    if (!c) return fail(CMM_ERR_PARAM, "ctx is NULL");
+    return copy_text(c->sim ? c->sim->s.param_text() : c->settings.param_text(), buf, cap);
+}
+
+int cmm_file_name(cmm_ctx* c, char* buf, size_t cap)
+{
+    if (!c) return fail(CMM_ERR_PARAM, "ctx is NULL");
+    return copy_text(c->settings.derived_file_name(), buf, cap);
+}
+
+int cmm_destroy(cmm_ctx* c)
+{
+    if (!c) return CMM_OK;
+    delete c->sim;
+    delete c;
+    return CMM_OK;
+}
+
+// ---------------------------------------------------------------- kernel API
+int cmm_advect_map(const cmm_grid* grid_map, const cmm_grid* grid_psi, const double* chix, const double* chiy,
+                   double* chix_out, double* chiy_out, const double* const* psi_levels, int l_order,
+                   const double* L1, const double* L12, double dt, double map_epsilon, int time_integration_num,
+                   int map_update_order_num, void* stream)
+{
+    cmm::AdvectArgs a{};
+    if (!to_grid(grid_map, &a.gm) || !to_grid(grid_psi, &a.gp)) return fail(CMM_ERR_PARAM, "bad grid");
+    if (!chix || !chiy || !chix_out || !chiy_out || !psi_levels || !L1 || !L12) return fail(CMM_ERR_PARAM, "NULL pointer");
+    if (l_order < 1 || l_order > cmm::kMaxLagrange) return fail(CMM_ERR_PARAM, "l_order must be 1..4");
+    if (map_update_order_num < 0 || map_update_order_num > 2) return fail(CMM_ERR_PARAM, "map_update_order_num must be 0..2");
+    if (time_integration_num != 10 && time_integration_num != 21 && time_integration_num != 30)
+        return fail(CMM_ERR_UNSUPPORTED, "time_integration_num must be 10, 21 or 30");
+    if (time_integration_num == 30 && l_order < 3) return fail(CMM_ERR_PARAM, "RK3 needs l_order >= 3");
+    a.ChiX = chix; a.ChiY = chiy; a.outX = chix_out; a.outY = chiy_out;
+    for (int l = 0; l < l_order; ++l) {
+        if (!psi_levels[l]) return fail(CMM_ERR_PARAM, "NULL psi level");
+        a.psi[l] = psi_levels[l];
+        a.L1[l] = L1[l];
+        a.L12[l] = L12[l];
+    }
+    cmm::map_update_coefficients(map_update_order_num, map_epsilon, a.coef, &a.nfoot);
+    a.dt = dt; a.ep = map_epsilon; a.time_integration_num = time_integration_num; a.l_order = l_order;
+    return cuda_rc(cmm::launch_advect(a, static_cast<cudaStream_t>(stream)), "cmm_advect_map");
+}
+
+int cmm_incomp_max(const cmm_grid* grid_check, const cmm_grid* grid_map, const double* chix, const double* chiy,
+                   double* d_result, void* stream)
+{
+    cmm::Grid gc, gm;
+    if (!to_grid(grid_check, &gc) || !to_grid(grid_map, &gm)) return fail(CMM_ERR_PARAM, "bad grid");
+    if (!chix || !chiy || !d_result) return fail(CMM_ERR_PARAM, "NULL pointer");
+    return cuda_rc(cmm::launch_incomp(gc, gm, chix, chiy, d_result, static_cast<cudaStream_t>(stream)), "cmm_incomp_max");
+}
+
+int cmm_compose_stack(const cmm_grid* grid_map, const cmm_grid* grid_target, const double* chix, const double* chiy,
+                      const double* stack, int n_maps, int ic_num, const double* discrete,
+                      const cmm_grid* grid_discrete, double* out, void* stream)
+{
+    cmm::Grid gm, gt;
+    if (!to_grid(grid_map, &gm) || !to_grid(grid_target, &gt)) return fail(CMM_ERR_PARAM, "bad grid");
+    if (!chix || !chiy || !out || n_maps < 0 || (n_maps > 0 && !stack)) return fail(CMM_ERR_PARAM, "bad pointer / map count");
+    cmm::InitSource src{};
+    if (discrete) {
+        if (!to_grid(grid_discrete, &src.gd)) return fail(CMM_ERR_PARAM, "bad discrete grid");
+        src.kind = 3;
+        src.discrete = discrete;
+    } else {
+        if (ic_num < 0 || ic_num > 11 || ic_num == 7 || ic_num == 8 || ic_num == 11)
+            return fail(CMM_ERR_UNSUPPORTED, "ic_num not available in the kernel API (needs tables or parameters)");
+        src.kind = 0;
+        src.ic_num = ic_num;
+    }
+    return cuda_rc(cmm::launch_compose_sample(gm, gt, chix, chiy, stack, n_maps, src, out, static_cast<cudaStream_t>(stream)),
+                   "cmm_compose_stack");
+}
+
+int cmm_sample_vort(const cmm_grid* grid_map, const cmm_grid* grid_out, const cmm_grid* grid_fine, const double* chix,
+                    const double* chiy, const double* w_fine, int molly_stencil, double* out, void* stream)
+{
+    cmm::Grid gm, go, gf;
+    if (!to_grid(grid_map, &gm) || !to_grid(grid_out, &go) || !to_grid(grid_fine, &gf)) return fail(CMM_ERR_PARAM, "bad grid");
+    if (!chix || !chiy || !w_fine || !out) return fail(CMM_ERR_PARAM, "NULL pointer");
+    if (molly_stencil != 0 && molly_stencil != 4 && molly_stencil != 8) return fail(CMM_ERR_PARAM, "molly_stencil must be 0, 4 or 8");
+    return cuda_rc(cmm::launch_sample_vort(gm, go, gf, chix, chiy, w_fine, molly_stencil, out, go.NX,
+                                           static_cast<cudaStream_t>(stream)), "cmm_sample_vort");
+}
+
+int cmm_poisson_create(const cmm_grid* grid_vort, const cmm_grid* grid_psi, double freq_cut_psi, void* stream,
+                       cmm_poisson** out)
+{
+    if (!out) return fail(CMM_ERR_PARAM, "out is NULL");
+    *out = nullptr;
+    cmm_poisson* p = new (std::nothrow) cmm_poisson();
+    if (!p) return fail(CMM_ERR_PARAM, "out of host memory");
+    if (!to_grid(grid_vort, &p->gv) || !to_grid(grid_psi, &p->gp)) { delete p; return fail(CMM_ERR_PARAM, "bad grid"); }
+    p->freq = freq_cut_psi;
+    p->stream = static_cast<cudaStream_t>(stream);
+    if (!cmm::make_plans(p->pv, p->gv, p->stream) || !cmm::make_plans(p->pp, p->gp, p->stream)) {
+        cmm_poisson_destroy(p);
+        return fail(CMM_ERR_CUDA, "cuFFT plan creation failed");
+    }
+    long long cmax = p->gv.Nfft > p->gp.Nfft ? p->gv.Nfft : p->gp.Nfft;
+    if (cudaMalloc((void**)&p->spec, sizeof(double2) * (size_t)cmax) != cudaSuccess ||
+        cudaMalloc((void**)&p->spec4, sizeof(double2) * 4 * (size_t)p->gp.Nfft) != cudaSuccess) {
+        cmm_poisson_destroy(p);
+        return fail(CMM_ERR_CUDA, "cudaMalloc failed");
+    }
+    *out = p;
+    return CMM_OK;
+}
+
+int cmm_poisson_hermite(cmm_poisson* p, const double* vort, double* psi_out)
+{
+    if (!p || !vort || !psi_out) return fail(CMM_ERR_PARAM, "NULL argument");
+    if (cufftExecD2Z(p->pv.d2z, const_cast<double*>(vort), reinterpret_cast<cufftDoubleComplex*>(p->spec)) != CUFFT_SUCCESS)
+        return fail(CMM_ERR_CUDA, "cuFFT D2Z failed");
+    int rc = cuda_rc(cmm::launch_spec_psi(p->spec, p->gv, p->gp, p->freq, p->spec4, p->stream), "spec_psi");
+    if (rc) return rc;
+    if (cufftExecZ2D(p->pp.z2d4, reinterpret_cast<cufftDoubleComplex*>(p->spec4), psi_out) != CUFFT_SUCCESS)
+        return fail(CMM_ERR_CUDA, "cuFFT Z2D failed");
+    return CMM_OK;
+}
+
+int cmm_poisson_destroy(cmm_poisson* p)
+{
+    if (!p) return CMM_OK;
+    cmm::destroy_plans(p->pv);
+    cmm::destroy_plans(p->pp);
+    if (p->spec) cudaFree(p->spec);
+    if (p->spec4) cudaFree(p->spec4);
+    delete p;
+    return CMM_OK;
+}
+
+int cmm_particles_advect(const cmm_grid* grid_psi, double* pos, int num, const double* const* psi_levels, int l_order,
+                         const double* Lp12, double dt, int time_integration_num, void* stream)
+{
+    cmm::ParticleArgs a{};
+    if (!to_grid(grid_psi, &a.gp)) return fail(CMM_ERR_PARAM, "bad grid");
+    if (num < 0 || (num > 0 && (!pos || !psi_levels || !Lp12))) return fail(CMM_ERR_PARAM, "bad arguments");
+    if (l_order < 1 || l_order > cmm::kMaxLagrange) return fail(CMM_ERR_PARAM, "l_order must be 1..4");
+    int need = time_integration_num == 30 ? 3 : time_integration_num == 20 ? 2 : 2;
+    if (l_order < need) return fail(CMM_ERR_PARAM, "too few psi levels for this scheme");
+    a.pos = pos; a.num = num;
+    for (int l = 0; l < l_order; ++l) { a.psi[l] = psi_levels[l]; a.Lp12[l] = Lp12[l]; }
+    a.dt = dt; a.time_integration_num = time_integration_num; a.l_order = l_order;
+    cudaError_t e = cmm::launch_particles(a, static_cast<cudaStream_t>(stream));
+    if (e == cudaErrorInvalidValue) return fail(CMM_ERR_UNSUPPORTED, "particle scheme not built (10, 20, 30 are)");
+    return cuda_rc(e, "cmm_particles_advect");
+}
+
+int cmm_diagnostics(const cmm_grid* grid_psi, const double* psi, const cmm_grid* grid_coarse, const double* vort,
+                    double* out3, void* stream)
+{
+    cmm::Grid gp, gc;
+    if (!to_grid(grid_psi, &gp) || !to_grid(grid_coarse, &gc)) return fail(CMM_ERR_PARAM, "bad grid");
+    if (!psi || !vort || !out3) return fail(CMM_ERR_PARAM, "NULL pointer");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    double* scratch = nullptr;
+    int rc = cuda_rc(cudaMalloc((void**)&scratch, sizeof(double) * (3 * cmm::kReduceBlocks + 8)), "cudaMalloc");
+    if (rc) return rc;
+    double* res = scratch + 3 * cmm::kReduceBlocks;
+    cudaError_t e = cmm::launch_sumsq(psi + gp.N, 2 * gp.N, scratch, res, s);
+    if (e == cudaSuccess) e = cmm::launch_sumsq(vort, gc.N, scratch, res + 1, s);
+    if (e == cudaSuccess) e = cmm::launch_stats(vort, gc.N, 1, scratch, res + 4, s);
+    double h[8] = {0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, res, sizeof(double) * 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(scratch);
+    if (e != cudaSuccess) return cuda_rc(e, "cmm_diagnostics");
+    out3[0] = 0.5 * gp.hx * gp.hy * h[0];
+    out3[1] = 0.5 * gc.hx * gc.hy * h[1];
+    double w_max = h[5] > 0 ? h[5] : 0.0, w_min = h[4] < 0 ? h[4] : 0.0;
+    out3[2] = w_max > -w_min ? w_max : -w_min;
+    return CMM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,355 @@
+// aux_kernels.cu -- tracer particles, spectral operators of the Poisson /
+// Hermite solve, and deterministic reductions (FP64, sm_103a).
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include "kernels.hpp"
+
+namespace cmm {
+
+// ---------------------------------------------------------------------------
+// tracer particles (Particle_advect, src/numerical/cmm-particles.cu:119-276);
+// psi[0] holds t_{n+1}, psi[1] holds t_n
+// ---------------------------------------------------------------------------
+template <int L, int TI>
+__global__ void __launch_bounds__(256) k_particles(const ParticleArgs a)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.num) return;
+    double px = a.pos[2 * i], py = a.pos[2 * i + 1];
+    const double* lv1[1] = {a.psi[1]};
+    const double* lv0[1] = {a.psi[0]};
+    const double dt = a.dt;
+    double ux[L], uy[L], k1x[1], k1y[1];
+    velocity_levels<1>(lv1, a.gp, px, py, k1x, k1y);
+    if (TI == 10) {
+        px += dt * k1x[0];
+        py += dt * k1y[0];
+    } else if (TI == 20) {
+        double k2x[1], k2y[1];
+        velocity_levels<1>(lv0, a.gp, px + dt * k1x[0], py + dt * k1y[0], k2x, k2y);
+        px += dt * (k1x[0] + k2x[0]) / 2;
+        py += dt * (k1y[0] + k2y[0]) / 2;
+    } else {  // RK3
+        velocity_levels<L>(a.psi, a.gp, px + dt * k1x[0] / 2.0, py + dt * k1y[0] / 2.0, ux, uy);
+        double k2x = a.Lp12[0] * ux[0], k2y = a.Lp12[0] * uy[0];
+#pragma unroll
+        for (int l = 1; l < L; ++l) { k2x = fma(a.Lp12[l], ux[l], k2x); k2y = fma(a.Lp12[l], uy[l], k2y); }
+        double k3x[1], k3y[1];
+        velocity_levels<1>(lv0, a.gp, px - dt * k1x[0] + 2 * dt * k2x, py - dt * k1y[0] + 2 * dt * k2y, k3x, k3y);
+        px += dt * (k1x[0] + 4 * k2x + k3x[0]) / 6.0;
+        py += dt * (k1y[0] + 4 * k2y + k3y[0]) / 6.0;
+    }
+    a.pos[2 * i] = wrap(px, a.gp.b0, a.gp.Wx);
+    a.pos[2 * i + 1] = wrap(py, a.gp.b2, a.gp.Wy);
+}
+
+cudaError_t launch_particles(const ParticleArgs& a, cudaStream_t s)
+{
+    if (a.num <= 0) return cudaSuccess;
+    int threads = 256;
+    unsigned blocks = (unsigned)((a.num + threads - 1) / threads);
+    int L = a.l_order;
+    if (a.time_integration_num == 10) k_particles<1, 10><<<blocks, threads, 0, s>>>(a);
+    else if (a.time_integration_num == 20) k_particles<1, 20><<<blocks, threads, 0, s>>>(a);
+    else if (a.time_integration_num == 30 && L == 3) k_particles<3, 30><<<blocks, threads, 0, s>>>(a);
+    else if (a.time_integration_num == 30 && L == 4) k_particles<4, 30><<<blocks, threads, 0, s>>>(a);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+__global__ void k_particle_rescale(double* pos, int num, double p0, double p1, double p2, double p3, Grid g)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= num) return;
+    double x = p0 + p2 * (pos[2 * i] - 0.5);
+    double y = p1 + p3 * (pos[2 * i + 1] - 0.5);
+    pos[2 * i] = wrap(x, g.b0, g.Wx);
+    pos[2 * i + 1] = wrap(y, g.b2, g.Wy);
+}
+
+cudaError_t launch_particle_rescale(double* pos, int num, const double* p4, const Grid& g, cudaStream_t s)
+{
+    if (num <= 0) return cudaSuccess;
+    k_particle_rescale<<<(num + 255) / 256, 256, 0, s>>>(pos, num, p4[0], p4[1], p4[2], p4[3], g);
+    return cudaGetLastError();
+}
+
+// deterministic particle layouts (k_part_init_circle / _uniform_grid / _sine_sheets,
+// src/simulation/cmm-init.cu:394-451): mode 2 circle, 3 uniform grid, 4 sine sheet
+__global__ void k_particle_layout(double* pos, int num, int mode, double p0, double p1, double p2, double p3, Grid g)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= num) return;
+    double x, y;
+    if (mode == 2) {
+        x = p0 + p2 * cos(i / (double)num * kTwoPi);
+        y = p1 + p3 * sin(i / (double)num * kTwoPi);
+    } else if (mode == 3) {
+        int len = (int)ceil(sqrt((double)num));
+        x = p0 + p2 * (-1 + 2 * (i % len) / (double)len);
+        y = p1 + p3 * (-1 + 2 * (i / len) / (double)len);
+    } else {
+        x = i / (double)num * kTwoPi + p0;
+        y = sin(i / (double)num * kTwoPi) / 2.0 + p1;
+    }
+    pos[2 * i] = wrap(x, g.b0, g.Wx);
+    pos[2 * i + 1] = wrap(y, g.b2, g.Wy);
+}
+
+cudaError_t launch_particle_layout(double* pos, int num, int mode, const double* p4, const Grid& g, cudaStream_t s)
+{
+    if (num <= 0) return cudaSuccess;
+    k_particle_layout<<<(num + 255) / 256, 256, 0, s>>>(pos, num, mode, p4[0], p4[1], p4[2], p4[3], g);
+    return cudaGetLastError();
+}
+
+__global__ void k_sample_points_dxdy(Grid gp, const double* __restrict__ psi, const double* __restrict__ pos,
+                                     double* __restrict__ out, int num)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= num) return;
+    double x = pos[2 * i], y = pos[2 * i + 1];
+    if (x > gp.b0 && x < gp.b1 && y > gp.b2 && y < gp.b3) {
+        Cell c = locate(gp, x, y);
+        Corners q = load_corners(psi, gp.N, c);
+        double gx, gy;
+        hermite_grad(q, value_weights(c.tx, gp.hx), value_weights(c.ty, gp.hy), slope_weights(c.tx, gp.ihx),
+                     slope_weights(c.ty, gp.ihy), gx, gy);
+        out[2 * i] = gx;
+        out[2 * i + 1] = gy;
+    } else {
+        out[2 * i] = out[2 * i + 1] = __longlong_as_double(0x7ff8000000000000ll);
+    }
+}
+
+cudaError_t launch_sample_points_dxdy(const Grid& gp, const double* psi, const double* pos, double* out, int num,
+                                      cudaStream_t s)
+{
+    if (num <= 0) return cudaSuccess;
+    k_sample_points_dxdy<<<(num + 255) / 256, 256, 0, s>>>(gp, psi, pos, out, num);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// spectral operators on D2Z half spectra [NY][NX/2+1]
+// (src/numerical/cmm-fft.cu:55-78 iLap, :147-187 dx/dy, :267-286 cut-off,
+//  :294-323 grid move, :326-339 normalise, :398-429 fourier_hermite)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void hermite_spectra(double2 P, double kx, double ky, long long idx, long long nf,
+                                                double2* __restrict__ out4)
+{
+    double2 Px = make_double2(-P.y * kx, P.x * kx);
+    double2 Py = make_double2(-P.y * ky, P.x * ky);
+    double2 Pxy = make_double2(-Py.y * kx, Py.x * kx);
+    out4[idx] = P;
+    out4[nf + idx] = Px;
+    out4[2 * nf + idx] = Py;
+    out4[3 * nf + idx] = Pxy;
+}
+
+__global__ void k_spec_hermite(const double2* __restrict__ F, Grid g, double2* __restrict__ out4)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= g.Nfft) return;
+    int iX = (int)(i % g.NX_fft), iY = (int)(i / g.NX_fft);
+    double2 f = F[i];
+    double2 P = make_double2(f.x / (double)g.N, f.y / (double)g.N);
+    double kx = g.kfx * (iX - (iX > g.NX / 2) * g.NX);
+    double ky = g.kfy * (iY - (iY > g.NY / 2) * g.NY);
+    hermite_spectra(P, kx, ky, i, g.Nfft, out4);
+}
+
+cudaError_t launch_spec_hermite(const double2* F, const Grid& g, double2* out4, cudaStream_t s)
+{
+    k_spec_hermite<<<(unsigned)((g.Nfft + 255) / 256), 256, 0, s>>>(F, g, out4);
+    return cudaGetLastError();
+}
+
+__global__ void k_spec_psi(const double2* __restrict__ Fv, Grid gv, Grid gp, double freq, double2* __restrict__ out4)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= gp.Nfft) return;
+    int iXc = (int)(i % gp.NX_fft), iYc = (int)(i / gp.NX_fft);
+    double2 P = make_double2(0.0, 0.0);
+    // grid move (zero pad or truncate) from the vorticity grid spectrum
+    bool outside = (iXc + (iXc > gp.NX / 2.0) * (gp.NX - 2 * iXc) > gv.NX / 2.0) ||
+                   (iYc + (iYc > gp.NY / 2.0) * (gp.NY - 2 * iYc) > gv.NY / 2.0);
+    if (!outside) {
+        int iXs = iXc + (iXc > gp.NX / 2.0) * (gv.NX - gp.NX);
+        int iYs = iYc + (iYc > gp.NY / 2.0) * (gv.NY - gp.NY);
+        double2 f = Fv[(long long)iYs * gv.NX_fft + iXs];
+        P = make_double2(f.x / (double)gv.N, f.y / (double)gv.N);
+    }
+    // circular low-pass, also removes the mean mode
+    int fX = iXc + (iXc > gp.NX / 2.0) * (gp.NX - 2 * iXc);
+    int fY = iYc + (iYc > gp.NY / 2.0) * (gp.NY - 2 * iYc);
+    if ((double)(fX * fX + fY * fY) > freq * freq || i == 0) P = make_double2(0.0, 0.0);
+    double kx = gp.kfx * (iXc - (iXc > gp.NX / 2) * gp.NX);
+    double ky = gp.kfy * (iYc - (iYc > gp.NY / 2) * gp.NY);
+    // inverse Laplacian
+    if (iXc == 0 && iYc == 0) P = make_double2(0.0, 0.0);
+    else {
+        double k2 = kx * kx + ky * ky;
+        P = make_double2(-P.x / k2, -P.y / k2);
+    }
+    hermite_spectra(P, kx, ky, i, gp.Nfft, out4);
+}
+
+cudaError_t launch_spec_psi(const double2* Fv, const Grid& gv, const Grid& gp, double freq, double2* out4,
+                            cudaStream_t s)
+{
+    k_spec_psi<<<(unsigned)((gp.Nfft + 255) / 256), 256, 0, s>>>(Fv, gv, gp, freq, out4);
+    return cudaGetLastError();
+}
+
+__global__ void k_spec_grad(const double2* __restrict__ F, Grid g, double2* __restrict__ out2)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= g.Nfft) return;
+    int iX = (int)(i % g.NX_fft), iY = (int)(i / g.NX_fft);
+    double2 f = F[i];
+    double2 P = make_double2(f.x / (double)g.N, f.y / (double)g.N);
+    double kx = g.kfx * (iX - (iX > g.NX / 2) * g.NX);
+    double ky = g.kfy * (iY - (iY > g.NY / 2) * g.NY);
+    out2[i] = make_double2(-P.y * kx, P.x * kx);
+    out2[g.Nfft + i] = make_double2(-P.y * ky, P.x * ky);
+}
+
+cudaError_t launch_spec_grad(const double2* F, const Grid& g, double2* out2, cudaStream_t s)
+{
+    k_spec_grad<<<(unsigned)((g.Nfft + 255) / 256), 256, 0, s>>>(F, g, out2);
+    return cudaGetLastError();
+}
+
+bool make_plans(FftPlans& p, const Grid& g, cudaStream_t s)
+{
+    int n[2] = {g.NY, g.NX};
+    p.g = g;
+    if (cufftPlanMany(&p.d2z, 2, n, nullptr, 1, 0, nullptr, 1, 0, CUFFT_D2Z, 1) != CUFFT_SUCCESS) return false;
+    if (cufftPlanMany(&p.z2d4, 2, n, nullptr, 1, 0, nullptr, 1, 0, CUFFT_Z2D, 4) != CUFFT_SUCCESS) return false;
+    if (cufftPlanMany(&p.z2d1, 2, n, nullptr, 1, 0, nullptr, 1, 0, CUFFT_Z2D, 1) != CUFFT_SUCCESS) return false;
+    cufftSetStream(p.d2z, s);
+    cufftSetStream(p.z2d4, s);
+    cufftSetStream(p.z2d1, s);
+    p.ok = true;
+    return true;
+}
+
+void destroy_plans(FftPlans& p)
+{
+    if (p.d2z) cufftDestroy(p.d2z);
+    if (p.z2d4) cufftDestroy(p.z2d4);
+    if (p.z2d1) cufftDestroy(p.z2d1);
+    p.d2z = p.z2d4 = p.z2d1 = 0;
+    p.ok = false;
+}
+
+// ---------------------------------------------------------------------------
+// deterministic two-pass reductions (fixed grid, fixed order)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_stats_partial(const double* __restrict__ v, long long n, long long stride,
+                                                       double* __restrict__ part)
+{
+    __shared__ double smin[256], smax[256], ssum[256];
+    double mn = __longlong_as_double(0x7ff0000000000000ll), mx = -mn, sm = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double x = v[i * stride];
+        mn = fmin(mn, x);
+        mx = fmax(mx, x);
+        sm += x;
+    }
+    smin[threadIdx.x] = mn; smax[threadIdx.x] = mx; ssum[threadIdx.x] = sm;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + o]);
+            smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + o]);
+            ssum[threadIdx.x] += ssum[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[3 * blockIdx.x] = smin[0];
+        part[3 * blockIdx.x + 1] = smax[0];
+        part[3 * blockIdx.x + 2] = ssum[0];
+    }
+}
+
+__global__ void k_stats_final(const double* __restrict__ part, int nb, double* __restrict__ out)
+{
+    __shared__ double smin[256], smax[256], ssum[256];
+    double mn = __longlong_as_double(0x7ff0000000000000ll), mx = -mn, sm = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        mn = fmin(mn, part[3 * b]);
+        mx = fmax(mx, part[3 * b + 1]);
+        sm += part[3 * b + 2];
+    }
+    smin[threadIdx.x] = mn; smax[threadIdx.x] = mx; ssum[threadIdx.x] = sm;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + o]);
+            smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + o]);
+            ssum[threadIdx.x] += ssum[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = smin[0];
+        out[1] = smax[0];
+        out[2] = fmax(0.0, smax[0]);
+        out[3] = ssum[0];
+    }
+}
+
+cudaError_t launch_stats(const double* v, long long n, long long stride, double* d_scratch, double* d_out,
+                         cudaStream_t s)
+{
+    long long need = (n + 255) / 256;
+    int nb = (int)(need < kReduceBlocks ? (need > 0 ? need : 1) : kReduceBlocks);
+    k_stats_partial<<<nb, 256, 0, s>>>(v, n, stride, d_scratch);
+    k_stats_final<<<1, 256, 0, s>>>(d_scratch, nb, d_out);
+    return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(256) k_sumsq_partial(const double* __restrict__ v, long long n,
+                                                       double* __restrict__ part)
+{
+    __shared__ double ssum[256];
+    double sm = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        sm = fma(v[i], v[i], sm);
+    ssum[threadIdx.x] = sm;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) ssum[threadIdx.x] += ssum[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = ssum[0];
+}
+
+__global__ void k_sum_final(const double* __restrict__ part, int nb, double* __restrict__ out)
+{
+    __shared__ double ssum[256];
+    double sm = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) sm += part[b];
+    ssum[threadIdx.x] = sm;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) ssum[threadIdx.x] += ssum[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = ssum[0];
+}
+
+cudaError_t launch_sumsq(const double* v, long long n, double* d_scratch, double* d_out, cudaStream_t s)
+{
+    long long need = (n + 255) / 256;
+    int nb = (int)(need < kReduceBlocks ? (need > 0 ? need : 1) : kReduceBlocks);
+    k_sumsq_partial<<<nb, 256, 0, s>>>(v, n, d_scratch);
+    k_sum_final<<<1, 256, 0, s>>>(d_scratch, nb, d_out);
+    return cudaGetLastError();
+}
+
+}  // namespace cmm

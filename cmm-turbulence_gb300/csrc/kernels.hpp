@@ -1,0 +1,116 @@
+// kernels.hpp -- host launchers of the sm_103a CMM kernels (FP64 plain form).
+// Every launcher is stream-ordered and returns the launch status.
+#pragma once
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include "cmm_common.cuh"
+
+namespace cmm {
+
+constexpr int kMaxLagrange = 4;
+constexpr int kMaxFoot = 12;
+
+// Map advection (advect_using_stream_hermite + k_advect_using_stream_hermite,
+// Cuda-CMM/src/simulation/cmm-simulation-host.cu:64-104,
+// src/simulation/cmm-simulation-kernel.cu:207-298), backward direction.
+struct AdvectArgs {
+    Grid gm, gp;
+    const double* ChiX;
+    const double* ChiY;
+    double* outX;
+    double* outY;
+    const double* psi[kMaxLagrange];     // psi[l]: Hermite level l (l=0 newest)
+    double L1[kMaxLagrange], L12[kMaxLagrange];
+    double coef[4][kMaxFoot];            // c1, cx, cy, cxy footpoint weights
+    double dt, ep;
+    int time_integration_num;            // 10 EulerExp, 21 RK2 (Heun), 30 RK3
+    int l_order;                         // Lagrange levels used (1..4)
+    int nfoot;                           // 4, 8 or 12 footpoints
+};
+
+void map_update_coefficients(int order_num, double ep, double coef[4][kMaxFoot], int* nfoot);
+
+cudaError_t launch_init_map(double* X, double* Y, const Grid& g, cudaStream_t s);
+cudaError_t launch_advect(const AdvectArgs& a, cudaStream_t s);
+// max |1 - det grad X| over the half-shifted check grid -> *d_result (double);
+// d_result is reset by the launcher
+cudaError_t launch_incomp(const Grid& gcheck, const Grid& gmap, const double* X, const double* Y,
+                          double* d_result, cudaStream_t s);
+
+// Initial-condition selector for sampling omega_0 (k_h_sample_from_init,
+// src/simulation/cmm-simulation-kernel.cu:342-373).
+struct InitSource {
+    int kind;                 // 0 analytic vorticity, 1 analytic passive scalar, 3 discrete Hermite
+    int ic_num;               // analytic initial-condition number
+    const double* discrete;   // Hermite planes of the discrete initial field
+    Grid gd;                  // its grid
+    const double* params;     // 10 initial_params (device)
+    const double* rand_table; // 1000 uniform(-1,1) values (device), gaussian_blobs
+};
+
+// omega_0( X_0( ... X_{n-1}( X_cur(x) ) ) ) on the target grid, fused over a
+// device-resident stack (translate_initial_condition_through_map_stack,
+// src/simulation/cmm-simulation-host.cu:112-128,299-327).
+// stack holds n maps, map i = [X planes (4N) | Y planes (4N)] at stack + i*8N.
+cudaError_t launch_compose_sample(const Grid& gm, const Grid& gt, const double* X, const double* Y,
+                                  const double* stack, int n_maps, const InitSource& src, double* out,
+                                  cudaStream_t s);
+
+// omega(x) = W_fine_H( X(x) ) on the output grid (k_apply_map_and_sample_from_hermite,
+// src/simulation/cmm-simulation-kernel.cu:402-461); out has row stride `ld`.
+cudaError_t launch_sample_vort(const Grid& gm, const Grid& gout, const Grid& gf, const double* X,
+                               const double* Y, const double* Wf, int molly, double* out, long long ld,
+                               cudaStream_t s);
+
+// tracer particles (Particle_advect, src/numerical/cmm-particles.cu:119-276)
+struct ParticleArgs {
+    Grid gp;
+    double* pos;
+    int num;
+    const double* psi[kMaxLagrange];
+    double Lp12[kMaxLagrange];
+    double dt;
+    int time_integration_num;   // 10, 20, 30
+    int l_order;
+};
+cudaError_t launch_particles(const ParticleArgs& a, cudaStream_t s);
+// U(0,1) -> frame and wrap (k_rescale, cmm-particles.cu:30-46)
+cudaError_t launch_particle_rescale(double* pos, int num, const double* p4, const Grid& g, cudaStream_t s);
+// circle / uniform grid / sine-sheet layouts (mode 2, 3, 4)
+cudaError_t launch_particle_layout(double* pos, int num, int mode, const double* p4, const Grid& g, cudaStream_t s);
+// psi_x, psi_y at particle positions (k_h_sample_points_dxdy, cmm-simulation-kernel.cu:138-155)
+cudaError_t launch_sample_points_dxdy(const Grid& gp, const double* psi, const double* pos, double* out, int num,
+                                      cudaStream_t s);
+
+// ---------------------------------------------------------------- spectral
+// cuFFT-based transforms plus fused spectral operators (src/numerical/cmm-fft.cu)
+struct FftPlans {
+    cufftHandle d2z = 0;        // real -> half spectrum
+    cufftHandle z2d4 = 0;       // batch of 4 half spectra -> 4 real planes
+    cufftHandle z2d1 = 0;       // single inverse
+    Grid g;
+    bool ok = false;
+};
+bool make_plans(FftPlans& p, const Grid& g, cudaStream_t s);
+void destroy_plans(FftPlans& p);
+
+// normalised spectrum -> 4 spectra [F, dx F, dy F, dxdy F] (fourier_hermite prep)
+cudaError_t launch_spec_hermite(const double2* F, const Grid& g, double2* out4, cudaStream_t s);
+// vort spectrum (raw D2Z) -> psi-grid 4 spectra: normalise, grid move, circular cut,
+// inverse Laplacian, derivatives (evaluate_stream_hermite, cmm-simulation-host.cu:333-375)
+cudaError_t launch_spec_psi(const double2* Fv, const Grid& gv, const Grid& gp, double freq, double2* out4,
+                            cudaStream_t s);
+// raw D2Z spectrum -> normalised (dx F, dy F) for the palinstrophy (cmm-mesure.cu:77-89)
+cudaError_t launch_spec_grad(const double2* F, const Grid& g, double2* out2, cudaStream_t s);
+
+// ---------------------------------------------------------------- reductions
+// min, max, max(0,max), sum over n values at stride `stride` (Debug_globals);
+// result -> d_out[4]; partial scratch of kReduceBlocks*4 doubles
+constexpr int kReduceBlocks = 304;
+cudaError_t launch_stats(const double* v, long long n, long long stride, double* d_scratch, double* d_out,
+                         cudaStream_t s);
+// sum of squares of n values (energy, enstrophy) -> d_out[0]
+cudaError_t launch_sumsq(const double* v, long long n, double* d_scratch, double* d_out, cudaStream_t s);
+
+}  // namespace cmm

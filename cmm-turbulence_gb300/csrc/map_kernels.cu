@@ -1,0 +1,408 @@
+// map_kernels.cu -- FP64 kernels of the CMM map: identity, GALS advection,
+// incompressibility check, stack composition with initial-condition sampling,
+// and sampling of the fine vorticity through the current map.
+#include <cuda_runtime.h>
+
+#include "kernels.hpp"
+
+namespace cmm {
+
+// ---------------------------------------------------------------------------
+// identity map (k_init_diffeo, src/simulation/cmm-simulation-kernel.cu:27-41)
+// ---------------------------------------------------------------------------
+__global__ void k_init_map(double* __restrict__ X, double* __restrict__ Y, Grid g)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= g.N) return;
+    int iX = (int)(i % g.NX), iY = (int)(i / g.NX);
+    X[i] = g.b0 + iX * g.hx;
+    Y[i] = g.b2 + iY * g.hy;
+    X[g.N + i] = 1.0; Y[2 * g.N + i] = 1.0;
+    X[2 * g.N + i] = 0.0; Y[g.N + i] = 0.0; X[3 * g.N + i] = 0.0; Y[3 * g.N + i] = 0.0;
+}
+
+cudaError_t launch_init_map(double* X, double* Y, const Grid& g, cudaStream_t s)
+{
+    int threads = 256;
+    long long blocks = (g.N + threads - 1) / threads;
+    k_init_map<<<(unsigned)blocks, threads, 0, s>>>(X, Y, g);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// GALS footpoint weights (src/simulation/cmm-simulation-host.cu:76-90)
+// ---------------------------------------------------------------------------
+void map_update_coefficients(int order_num, double ep, double coef[4][kMaxFoot], int* nfoot)
+{
+    double hc[3] = {0, 0, 0};
+    switch (order_num) {
+        case 2: hc[0] = 3.0 / 8.0; hc[1] = -3.0 / 20.0; hc[2] = 1.0 / 40.0; break;
+        case 1: hc[0] = 1.0 / 3.0; hc[1] = -1.0 / 12.0; break;
+        default: hc[0] = 1.0 / 4.0; break;
+    }
+    int n = 4 + 4 * (order_num < 0 ? 0 : order_num > 2 ? 2 : order_num);
+    for (int k = 0; k < kMaxFoot; ++k) {
+        int r = k / 4;
+        double sx = 1 - 2 * ((k / 2) % 2), sy = 1 - 2 * (((k + 1) / 2) % 2), sxy = 1 - 2 * (k % 2);
+        bool on = k < n;
+        coef[0][k] = on ? hc[r] : 0.0;
+        coef[1][k] = on ? hc[r] * sx / ep / double(r + 1) : 0.0;
+        coef[2][k] = on ? hc[r] * sy / ep / double(r + 1) : 0.0;
+        coef[3][k] = on ? hc[r] * sxy / ep / ep / double(r + 1) / double(r + 1) : 0.0;
+    }
+    *nfoot = n;
+}
+
+// ---------------------------------------------------------------------------
+// backward characteristic integrators on the Hermite stream function
+// (src/numerical/cmm-timestep.cu:35-45 euler_exp_b, :66-81 RK2_heun_b,
+//  :175-207 RK3_classical_b).  u = (psi_y, -psi_x).
+// ---------------------------------------------------------------------------
+template <int L, int TI>
+__device__ __forceinline__ void integrate_back(const AdvectArgs& a, double x, double y, double& xo, double& yo)
+{
+    double ux[L], uy[L];
+    velocity_levels<L>(a.psi, a.gp, x, y, ux, uy);
+    double k1x = a.L1[0] * ux[0], k1y = a.L1[0] * uy[0];
+#pragma unroll
+    for (int l = 1; l < L; ++l) { k1x = fma(a.L1[l], ux[l], k1x); k1y = fma(a.L1[l], uy[l], k1y); }
+    const double dt = a.dt;
+    if (TI == 10) {
+        xo = x - dt * k1x;
+        yo = y - dt * k1y;
+    } else if (TI == 21) {
+        double u2x[1], u2y[1];
+        velocity_levels<1>(a.psi, a.gp, x - dt * k1x, y - dt * k1y, u2x, u2y);
+        xo = x - dt * (k1x + u2x[0]) / 2;
+        yo = y - dt * (k1y + u2y[0]) / 2;
+    } else {  // 30: RK3
+        velocity_levels<L>(a.psi, a.gp, x - dt * k1x / 2.0, y - dt * k1y / 2.0, ux, uy);
+        double k2x = a.L12[0] * ux[0], k2y = a.L12[0] * uy[0];
+#pragma unroll
+        for (int l = 1; l < L; ++l) { k2x = fma(a.L12[l], ux[l], k2x); k2y = fma(a.L12[l], uy[l], k2y); }
+        double u3x[1], u3y[1];
+        velocity_levels<1>(a.psi, a.gp, x + dt * k1x - 2 * dt * k2x, y + dt * k1y - 2 * dt * k2y, u3x, u3y);
+        xo = x - dt * (k1x + 4 * k2x + u3x[0]) / 6.0;
+        yo = y - dt * (k1y + 4 * k2y + u3y[0]) / 6.0;
+    }
+}
+
+// One lane per (node, footpoint); LPN lanes per node (power of two >= nfoot).
+// Lanes 0..7 of each group combine the footpoints into the 8 output planes
+// [X, X_x, X_y, X_xy, Y, Y_x, Y_y, Y_xy] with the same sequential
+// multiply-add order as the reference's accumulation (:280-289).
+template <int L, int TI>
+__global__ void __launch_bounds__(256) k_advect(const AdvectArgs a, int lpn_log2)
+{
+    __shared__ double sc[4][kMaxFoot];
+    if (threadIdx.x < 4 * kMaxFoot) sc[threadIdx.x / kMaxFoot][threadIdx.x % kMaxFoot] =
+        a.coef[threadIdx.x / kMaxFoot][threadIdx.x % kMaxFoot];
+    __syncthreads();
+
+    const int lpn = 1 << lpn_log2;
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    long long node = t >> lpn_log2;
+    int k = (int)(t & (lpn - 1));
+    bool live = node < a.gm.N;
+    long long nd = live ? node : 0;
+    int iX = (int)(nd % a.gm.NX), iY = (int)(nd / a.gm.NX);
+
+    double xf = 0.0, yf = 0.0;
+    if (live && k < a.nfoot) {
+        double r = (double)((k >> 2) + 1) * a.ep;
+        double x = a.gm.b0 + iX * a.gm.hx + r * (1 - 2 * ((k >> 1) & 1));
+        double y = a.gm.b2 + iY * a.gm.hy + r * (1 - 2 * (((k + 1) >> 1) & 1));
+        double xb, yb;
+        integrate_back<L, TI>(a, x, y, xb, yb);
+        map_value(a.ChiX, a.ChiY, a.gm, xb, yb, xf, yf);
+    }
+    // gather the footpoints of this node in every lane of the group
+    const int comp = (k >> 2) & 1, plane = k & 3;
+    double acc = 0.0;
+    for (int kk = 0; kk < a.nfoot; ++kk) {
+        double vx = __shfl_sync(0xffffffffu, xf, kk, lpn);
+        double vy = __shfl_sync(0xffffffffu, yf, kk, lpn);
+        acc = fma(comp ? vy : vx, sc[plane][kk], acc);
+    }
+    if (live && k < 8) {
+        double* out = comp ? a.outY : a.outX;
+        out[plane * a.gm.N + node] = acc;
+    }
+}
+
+cudaError_t launch_advect(const AdvectArgs& a, cudaStream_t s)
+{
+    int lpn_log2 = a.nfoot <= 4 ? 3 : a.nfoot <= 8 ? 3 : 4;   // >= 8 lanes so lanes 0..7 can store
+    int lpn = 1 << lpn_log2;
+    long long total = a.gm.N * lpn;
+    int threads = 256;
+    unsigned blocks = (unsigned)((total + threads - 1) / threads);
+#define CMM_ADV(LL, TT) k_advect<LL, TT><<<blocks, threads, 0, s>>>(a, lpn_log2)
+    switch (a.time_integration_num * 10 + a.l_order) {
+        case 101: CMM_ADV(1, 10); break;
+        case 102: CMM_ADV(2, 10); break;
+        case 103: CMM_ADV(3, 10); break;
+        case 104: CMM_ADV(4, 10); break;
+        case 211: CMM_ADV(1, 21); break;
+        case 212: CMM_ADV(2, 21); break;
+        case 213: CMM_ADV(3, 21); break;
+        case 214: CMM_ADV(4, 21); break;
+        case 301: CMM_ADV(1, 30); break;
+        case 302: CMM_ADV(2, 30); break;
+        case 303: CMM_ADV(3, 30); break;
+        case 304: CMM_ADV(4, 30); break;
+        default: return cudaErrorInvalidValue;
+    }
+#undef CMM_ADV
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// incompressibility: max |1 - det grad X| over the check grid, points shifted
+// by half a check cell (k_incompressibility_check + thrust max,
+// src/simulation/cmm-simulation-kernel.cu:159-173, cmm-simulation-host.cu:44-50)
+// fused with a warp-shuffle max and one atomic per block.  |1-det| >= 0, so
+// the IEEE bit pattern orders like the value and atomicMax on it is exact.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_incomp(Grid gc, Grid gm, const double* __restrict__ X,
+                                                const double* __restrict__ Y, unsigned long long* result)
+{
+    __shared__ unsigned long long wmax[8];
+    unsigned long long best = 0ull;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < gc.N;
+         i += (long long)gridDim.x * blockDim.x) {
+        int iX = (int)(i % gc.NX), iY = (int)(i / gc.NX);
+        double x = gm.b0 + iX * gc.hx + 0.5 * gc.hx;
+        double y = gm.b2 + iY * gc.hy + 0.5 * gc.hy;
+        double d = fabs(1.0 - map_det(X, Y, gm, x, y));
+        unsigned long long b = (unsigned long long)__double_as_longlong(d);
+        best = b > best ? b : best;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long v = __shfl_xor_sync(0xffffffffu, best, o);
+        best = v > best ? v : best;
+    }
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = best;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long m = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = wmax[w] > m ? wmax[w] : m;
+        atomicMax(result, m);
+    }
+}
+
+cudaError_t launch_incomp(const Grid& gc, const Grid& gm, const double* X, const double* Y, double* d_result,
+                          cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(d_result, 0, sizeof(double), s);
+    if (e != cudaSuccess) return e;
+    int threads = 256;
+    long long need = (gc.N + threads - 1) / threads;
+    unsigned blocks = (unsigned)(need < 152 * 16 ? need : 152 * 16);
+    k_incomp<<<blocks, threads, 0, s>>>(gc, gm, X, Y, reinterpret_cast<unsigned long long*>(d_result));
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// analytic initial conditions (d_init_vorticity / d_init_scalar,
+// src/simulation/cmm-init.cu:30-241, 253-298)
+// ---------------------------------------------------------------------------
+__device__ double init_vorticity(double x, double y, int ic, const double* __restrict__ prm,
+                                 const double* __restrict__ rnd)
+{
+    const double PI = kTwoPi / 2;
+    switch (ic) {
+        case 0: {  // 4_nodes
+            x -= floor(x / kTwoPi) * kTwoPi;
+            y -= floor(y / kTwoPi) * kTwoPi;
+            return cos(x) + cos(y) + 0.6 * cos(2 * x) + 0.2 * cos(3 * x);
+        }
+        case 1: {  // quadropole
+            double r = 0;
+            for (int iy = -2; iy <= 2; iy++)
+                for (int ix = -2; ix <= 2; ix++) {
+                    double dx = x - PI / 2 + ix * 2 * PI, dy = y - PI / 2 + iy * 2 * PI;
+                    double A = 0.6258473, s = 0.5;
+                    double B = A / (s * s * s * s) * (dx * dy) * (dx * dx + dy * dy - 6 * s * s);
+                    double D = (dx * dx + dy * dy) / (2 * s * s);
+                    r += B * exp(-D);
+                }
+            return r;
+        }
+        case 2: {  // one_vortex
+            double sig = kTwoPi * 0.125;
+            return 1.0 / (kTwoPi * sig * sig) * exp(-((x - PI) * (x - PI) + (y - PI) * (y - PI)) / (2 * sig * sig));
+        }
+        case 3: case 4: {  // two_votices / three_vortices
+            double r = 0, LX = PI / 2, LY = PI / (2.0 * sqrt(2.0));
+            for (int iy = -1; iy <= 1; iy++)
+                for (int ix = -1; ix <= 1; ix++) {
+                    double xs = x + kTwoPi * ix, ys = y + kTwoPi * iy;
+                    double env = sin(0.5 * xs) * sin(0.5 * xs) * sin(0.5 * (ys + kTwoPi * iy)) * sin(0.5 * (ys + kTwoPi * iy));
+                    double e;
+                    if (ic == 3)
+                        e = exp(-((xs - PI) * (xs - PI) + (ys - 0.33 * kTwoPi) * (ys - 0.33 * kTwoPi)) * 5) +
+                            exp(-((xs - PI) * (xs - PI) + (ys - 0.67 * kTwoPi) * (ys - 0.67 * kTwoPi)) * 5);
+                    else
+                        e = exp(-((xs - PI - LX) * (xs - PI - LX) + (ys - PI) * (ys - PI)) * 5) +
+                            exp(-((xs - PI + LX) * (xs - PI + LX) + (ys - PI) * (ys - PI)) * 5) -
+                            exp(-((xs - PI + LX) * (xs - PI + LX) + (ys - PI - LY) * (ys - PI - LY)) * 5);
+                    r += env * e;
+                }
+            return r;
+        }
+        case 5:  // single_shear_layer
+            return (1 + 0.01 * cos(2 * x)) * exp(-50.0 * (y - PI) * (y - PI));
+        case 6: {  // tanh_shear_layer
+            double freq = 2, d = 14 * freq / kTwoPi;
+            double c = exp(-d * (y - PI)) + exp(d * (y - PI));
+            return 5.0 * (1 + 0.01 * cos(freq * x)) * 4 / c / c;
+        }
+        case 8: {  // gaussian_blobs (random offsets from a host-drawn table)
+            x -= floor(x / kTwoPi) * kTwoPi;
+            y -= floor(y / kTwoPi) * kTwoPi;
+            const int NB = 10, border = 2;
+            double sig = kTwoPi * 0.01, off = kTwoPi * 0.005, r = 0;
+            int dir = 1;
+            for (int mx = -border; mx < 2 * NB + border; mx++) {
+                for (int my = -border; my < 2 * NB + border; my++) {
+                    int bn = (int)((mx - floor(mx / (double)(NB * 2)) * NB * 2) +
+                                   (my - floor(my / (double)(NB * 2)) * NB * 2) * NB * 2);
+                    double ex = x - (mx + 0.5) * kTwoPi / (2 * NB) + rnd[bn] * off;
+                    double ey = y - (my + 0.5) * kTwoPi / (2 * NB) + rnd[bn + NB * NB * 4] * off;
+                    r += dir / (kTwoPi * sig * sig) * exp(-(ex * ex + ey * ey) / (2 * sig * sig));
+                    dir = -dir;
+                }
+                dir = -dir;
+            }
+            return r;
+        }
+        case 9: {  // shielded_vortex
+            double nu = 2e-1, xr = PI - x, yr = PI - y;
+            return 1 / (2 * nu * nu * nu) * (4 * nu - xr * xr - yr * yr) * exp(-(xr * xr + yr * yr) / (4 * nu));
+        }
+        case 10: {  // two_cosine
+            x -= floor(x / kTwoPi) * kTwoPi;
+            y -= floor(y / kTwoPi) * kTwoPi;
+            return cos(x) * cos(y);
+        }
+        case 11: {  // vortex_sheets
+            double d = 1 / sqrt(prm[0]);
+            double q = y - PI - sin(x) / 2.0;
+            return exp(-q * q / (2 * d * d)) / sqrt(2 * PI) / d;
+        }
+        default: return 0.0;
+    }
+}
+
+__device__ double init_scalar(double x, double y, int sn)
+{
+    const double PI = kTwoPi / 2;
+    switch (sn) {
+        case 0: {  // rectangle
+            x -= floor(x / kTwoPi) * kTwoPi;
+            y -= floor(y / kTwoPi) * kTwoPi;
+            return (x > PI - PI && x < PI + PI && y > PI / 2.0 - PI / 2.0 && y < PI / 2.0 + PI / 2.0) ? 1.0 : 0.0;
+        }
+        case 1: {  // gaussian
+            double v = PI / 4.0;
+            return 1.0 / (kTwoPi * v * v) * exp(-((x - PI) * (x - PI) / (2 * v * v) + (y - PI) * (y - PI) / (2 * v * v)));
+        }
+        case 2: {  // circular_ring
+            double r = PI / 2.0, w = r / 8.0, q = (x - PI) * (x - PI) + (y - PI) * (y - PI);
+            return (tanh(10.0 * (q - (r + w) * (r + w))) - tanh(10.0 * (q - (r - w) * (r - w)))) / 2.0;
+        }
+        default: return 0.0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// stack composition + initial-condition sampling, fused: every target point
+// chases its footpoint through the current map and all stacked maps in
+// registers, instead of one launch and one HBM round trip of (x, y) per map.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_compose_sample(Grid gm, Grid gt, const double* __restrict__ X,
+                                                        const double* __restrict__ Y,
+                                                        const double* __restrict__ stack, int n_maps,
+                                                        InitSource src, double* __restrict__ out)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= gt.N) return;
+    int iX = (int)(i % gt.NX), iY = (int)(i / gt.NX);
+    double x = gt.b0 + iX * gt.hx, y = gt.b2 + iY * gt.hy;
+    double xo, yo;
+    map_value(X, Y, gm, x, y, xo, yo);
+    x = wrap(xo, gm.b0, gm.Wx);
+    y = wrap(yo, gm.b2, gm.Wy);
+    for (int m = n_maps - 1; m >= 0; --m) {
+        const double* MX = stack + (long long)m * 8 * gm.N;
+        map_value(MX, MX + 4 * gm.N, gm, x, y, xo, yo);
+        x = wrap(xo, gm.b0, gm.Wx);
+        y = wrap(yo, gm.b2, gm.Wy);
+    }
+    double v;
+    if (src.kind == 3) v = interp_value(src.discrete, src.gd, x, y);
+    else if (src.kind == 1) v = init_scalar(x, y, src.ic_num);
+    else v = init_vorticity(x, y, src.ic_num, src.params, src.rand_table);
+    out[i] = v;
+}
+
+cudaError_t launch_compose_sample(const Grid& gm, const Grid& gt, const double* X, const double* Y,
+                                  const double* stack, int n_maps, const InitSource& src, double* out,
+                                  cudaStream_t s)
+{
+    int threads = 256;
+    unsigned blocks = (unsigned)((gt.N + threads - 1) / threads);
+    k_compose_sample<<<blocks, threads, 0, s>>>(gm, gt, X, Y, stack, n_maps, src, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// vorticity through the current map (k_apply_map_and_sample_from_hermite)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_sample_vort(Grid gm, Grid go, Grid gf, const double* __restrict__ X,
+                                                     const double* __restrict__ Y, const double* __restrict__ Wf,
+                                                     int molly, double* __restrict__ out, long long ld)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= go.N) return;
+    int iX = (int)(i % go.NX), iY = (int)(i / go.NX);
+    double x = gm.b0 + iX * go.hx, y = gm.b2 + iY * go.hy;
+    double x2, y2, v;
+    if (molly == 4) {
+        // reference stencil; its x offset term evaluates to zero (operator
+        // precedence of `i>>1+1`), kept for identical results
+        map_value(X, Y, gm, x, y, x2, y2);
+        v = interp_value(Wf, gf, x2, y2) / 3.0;
+        for (int m = 0; m < 4; ++m) {
+            double xs = x + go.hx / 2.0 * ((m >> 2) & 1) * (-1 + 2 * (m & 1));
+            double ys = y + go.hy / 2.0 * ((m >> 1) & 1) * (-1 + 2 * (m & 1));
+            map_value(X, Y, gm, xs, ys, x2, y2);
+            v += interp_value(Wf, gf, x2, y2) / 6.0;
+        }
+    } else if (molly == 8) {
+        v = 0.0;
+        for (int m = 0; m < 9; ++m) {
+            double xs = x + go.hx * (-1 + m % 3) / 2.0;
+            double ys = y + go.hy * (-1 + m / 3) / 2.0;
+            map_value(X, Y, gm, xs, ys, x2, y2);
+            // reference weights ((1 + m%3) & 1) * ((1 + m/3) & 1), kept for identical results
+            v += ((1 + (m % 3)) & 1) * ((1 + (m / 3)) & 1) * interp_value(Wf, gf, x2, y2) / 16.0;
+        }
+    } else {
+        map_value(X, Y, gm, x, y, x2, y2);
+        v = interp_value(Wf, gf, x2, y2);
+    }
+    out[(long long)iY * ld + iX] = v;
+}
+
+cudaError_t launch_sample_vort(const Grid& gm, const Grid& go, const Grid& gf, const double* X, const double* Y,
+                               const double* Wf, int molly, double* out, long long ld, cudaStream_t s)
+{
+    int threads = 256;
+    unsigned blocks = (unsigned)((go.N + threads - 1) / threads);
+    k_sample_vort<<<blocks, threads, 0, s>>>(gm, go, gf, X, Y, Wf, molly, out, ld);
+    return cudaGetLastError();
+}
+
+}  // namespace cmm

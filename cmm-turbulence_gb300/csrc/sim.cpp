@@ -1,0 +1,796 @@
+// sim.cpp -- see sim.hpp.  Host orchestration of one Euler-2D CMM run:
+// reference driver src/simulation/cmm-euler2d.cu:45-1099 and host layer
+// src/simulation/cmm-simulation-host.cu.
+#include "sim.hpp"
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <curand.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <random>
+
+namespace cmm {
+
+namespace {
+// get_L_coefficient (src/numerical/cmm-timestep.cu:474-484)
+double lagrange_coefficient(const double* t, double t_next, int loop_ctr, int i_point, int l_order)
+{
+    double c = 1;
+    for (int i_p = 0; i_p < l_order; ++i_p)
+        if (i_p != i_point) c *= (t_next - t[loop_ctr - i_p]) / (t[loop_ctr - i_point] - t[loop_ctr - i_p]);
+    return c;
+}
+
+bool has(const std::string& s, const char* k) { return s.find(k) != std::string::npos; }
+
+std::string two(int i)
+{
+    char b[16];
+    snprintf(b, sizeof(b), "%02d", i);
+    return b;
+}
+}  // namespace
+
+EulerSim::EulerSim(const Settings& st) : s(st) {}
+
+EulerSim::~EulerSim()
+{
+    set_profiling(false);
+    release();
+}
+
+const char* EulerSim::phase_name(int p)
+{
+    static const char* n[kNumPhases] = {"advect", "incomp", "remap", "psi", "coarse", "particles", "save"};
+    return p >= 0 && p < kNumPhases ? n[p] : "";
+}
+
+void EulerSim::set_profiling(bool on)
+{
+    if (on && !prof_) {
+        for (int p = 0; p < kNumPhases; ++p) {
+            cudaEventCreate(&ev_[p][0]);
+            cudaEventCreate(&ev_[p][1]);
+            prof_ms[p] = 0;
+            prof_count[p] = 0;
+        }
+    } else if (!on && prof_) {
+        for (int p = 0; p < kNumPhases; ++p) {
+            cudaEventDestroy(ev_[p][0]);
+            cudaEventDestroy(ev_[p][1]);
+        }
+    }
+    prof_ = on;
+}
+
+void EulerSim::ph_begin(int p)
+{
+    if (prof_) cudaEventRecord(ev_[p][0], stream);
+}
+
+void EulerSim::ph_end(int p)
+{
+    if (!prof_) return;
+    cudaEventRecord(ev_[p][1], stream);
+    ev_live_[p] = true;
+}
+
+void EulerSim::ph_collect()
+{
+    // one stream sync per profiled iteration; events of each phase timed once
+    if (!prof_) return;
+    cudaStreamSynchronize(stream);
+    for (int p = 0; p < kNumPhases; ++p) {
+        if (!ev_live_[p]) continue;
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, ev_[p][0], ev_[p][1]) == cudaSuccess) {
+            prof_ms[p] += ms;
+            prof_count[p] += 1;
+        }
+        ev_live_[p] = false;
+    }
+}
+
+int EulerSim::check(cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return kOk;
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return kErrCuda;
+}
+
+#define CMM_CUDA(call) do { int rc_ = check((call), #call); if (rc_) return rc_; } while (0)
+#define CMM_LAUNCH(k, call) do { kernel_launches += (k); int rc_ = check((call), #call); if (rc_) return rc_; } while (0)
+#define CMM_FFT(call) do { fft_calls++; if ((call) != CUFFT_SUCCESS) { err = std::string("cuFFT: ") + #call; return kErrCuda; } } while (0)
+
+double EulerSim::wall() const
+{
+    return std::chrono::duration_cast<std::chrono::microseconds>(std::chrono::steady_clock::now() - begin_).count() / 1e6;
+}
+
+int EulerSim::set_stream(cudaStream_t st)
+{
+    if (initialised_) { err = "set_stream after init"; return kErrState; }
+    stream = st;
+    own_stream_ = false;
+    return kOk;
+}
+
+int EulerSim::set_initial_discrete(const double* host, size_t n)
+{
+    if (initialised_) { err = "set_initial_discrete after init"; return kErrState; }
+    size_t need = (size_t)s.initial_discrete_grid * s.initial_discrete_grid;
+    if (n != need) { err = "discrete initial condition needs initial_discrete_grid^2 values"; return kErrParam; }
+    host_discrete_.assign(host, host + n);
+    return kOk;
+}
+
+int EulerSim::alloc()
+{
+    if (s.simulation_type != "cmm_euler_2d") { err = "only cmm_euler_2d is built in this context"; return kErrUnsupported; }
+    if (s.initial_condition_num < 0) { err = "unknown initial condition " + s.initial_condition; return kErrParam; }
+    if (s.initial_condition_num == 7 && !s.initial_discrete) {
+        err = "initial condition turbulence_gaussienne is not built (needs device cuRAND sequences)";
+        return kErrUnsupported;
+    }
+    if (s.time_integration_num != 10 && s.time_integration_num != 21 && s.time_integration_num != 30) {
+        err = "map time integration " + s.time_integration + " is not built (EulerExp, RK2/Heun, RK3 are)";
+        return kErrUnsupported;
+    }
+    if (s.map_update_order_num < 0) { err = "unknown map_update_order " + s.map_update_order; return kErrParam; }
+    if (s.forward_map) { err = "forward_map is not built"; return kErrUnsupported; }
+    if (s.restart_time != 0) { err = "restart from a saved map stack is not built"; return kErrUnsupported; }
+    if (s.grid_coarse <= 0 || s.grid_fine <= 0 || s.grid_psi <= 0 || s.grid_vort <= 0) { err = "grid sizes must be positive"; return kErrParam; }
+
+    dt = s.dt();
+    L = s.effective_lagrange_order();
+    if (L < 1 || L > kMaxLagrange) { err = "lagrange order out of range"; return kErrParam; }
+    if (L < 3 && s.time_integration_num == 30) { err = "RK3 needs lagrange order >= 3"; return kErrParam; }
+    s.lagrange_order = L;
+    s.file_name = s.derived_file_name();
+    max_maps = s.cpu_map_num();
+
+    const double* b = s.domain_bounds;
+    gc = make_grid(s.grid_coarse, s.grid_coarse, b);
+    gf = make_grid(s.grid_fine, s.grid_fine, b);
+    gp = make_grid(s.grid_psi, s.grid_psi, b);
+    gv = make_grid(s.grid_vort, s.grid_vort, b);
+    int nd = s.initial_discrete ? s.initial_discrete_grid : 1;
+    gd = make_grid(nd, nd, b);
+
+    if (!stream) {
+        CMM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        own_stream_ = true;
+    }
+    auto dalloc = [&](double** p, long long n) { return check(cudaMalloc((void**)p, sizeof(double) * (size_t)std::max(n, 1ll)), "cudaMalloc"); };
+    int rc;
+    if ((rc = dalloc(&ChiX, 4 * gc.N)) || (rc = dalloc(&ChiY, 4 * gc.N)) || (rc = dalloc(&ChiX_new, 4 * gc.N)) ||
+        (rc = dalloc(&ChiY_new, 4 * gc.N)) || (rc = dalloc(&vort, gc.N)) || (rc = dalloc(&wfine, 4 * gf.N)))
+        return rc;
+    for (int l = 0; l < L; ++l) if ((rc = dalloc(&psi[l], 4 * gp.N))) return rc;
+    if (s.initial_discrete && (rc = dalloc(&wdisc, 4 * gd.N))) return rc;
+    stack_cap_ = std::max(0, std::min(max_maps, 16));
+    if (stack_cap_ > 0 && (rc = dalloc(&stack, 8 * gc.N * stack_cap_))) return rc;
+    long long rmax = std::max({gf.N, gv.N, gd.N, gc.N, gp.N});
+    long long cmax = std::max({gf.Nfft, gv.Nfft, gd.Nfft, gc.Nfft, gp.Nfft});
+    if ((rc = dalloc(&real_buf_, rmax))) return rc;
+    CMM_CUDA(cudaMalloc((void**)&spec_, sizeof(double2) * (size_t)cmax));
+    CMM_CUDA(cudaMalloc((void**)&spec4_, sizeof(double2) * 4 * (size_t)cmax));
+    if ((rc = dalloc(&red_, 3 * kReduceBlocks)) || (rc = dalloc(&d_scal_, 16)) || (rc = dalloc(&d_params_, 10)) ||
+        (rc = dalloc(&d_rand_, 1000)))
+        return rc;
+    CMM_CUDA(cudaMallocHost((void**)&h_scal_, sizeof(double) * 16));
+    for (auto& p : s.particles_advected) {
+        double* d = nullptr;
+        if ((rc = dalloc(&d, 2ll * std::max(p.num, 1)))) return rc;
+        parts.push_back(d);
+    }
+    if (!make_plans(pf_, gf, stream) || !make_plans(pv_, gv, stream) || !make_plans(pp_, gp, stream) ||
+        !make_plans(pc_, gc, stream) || (s.initial_discrete && !make_plans(pd_, gd, stream))) {
+        err = "cuFFT plan creation failed";
+        return kErrCuda;
+    }
+    // random table for gaussian_blobs (cmm-euler2d.cu:348-354)
+    std::vector<double> rnd(1000);
+    std::mt19937_64 gen(0);
+    std::uniform_real_distribution<double> dist(-1.0, 1.0);
+    for (auto& v : rnd) v = dist(gen);
+    CMM_CUDA(cudaMemcpyAsync(d_rand_, rnd.data(), sizeof(double) * 1000, cudaMemcpyHostToDevice, stream));
+    CMM_CUDA(cudaMemcpyAsync(d_params_, s.initial_params, sizeof(double) * 10, cudaMemcpyHostToDevice, stream));
+    CMM_CUDA(cudaStreamSynchronize(stream));
+    return kOk;
+}
+
+void EulerSim::release()
+{
+    auto f = [](void* p) { if (p) cudaFree(p); };
+    f(ChiX); f(ChiY); f(ChiX_new); f(ChiY_new); f(vort); f(wfine); f(wdisc); f(stack);
+    for (int l = 0; l < kMaxLagrange; ++l) f(psi[l]);
+    f(real_buf_); f(spec_); f(spec4_); f(red_); f(d_scal_); f(d_params_); f(d_rand_);
+    for (auto p : parts) f(p);
+    parts.clear();
+    if (h_scal_) cudaFreeHost(h_scal_);
+    h_scal_ = nullptr;
+    destroy_plans(pf_); destroy_plans(pv_); destroy_plans(pp_); destroy_plans(pc_); destroy_plans(pd_);
+    ChiX = ChiY = ChiX_new = ChiY_new = vort = wfine = wdisc = stack = nullptr;
+    for (int l = 0; l < kMaxLagrange; ++l) psi[l] = nullptr;
+    real_buf_ = nullptr; spec_ = nullptr; spec4_ = nullptr; red_ = d_scal_ = d_params_ = d_rand_ = nullptr;
+    if (own_stream_ && stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+    own_stream_ = false;
+}
+
+// ---------------------------------------------------------------- phases
+int EulerSim::translate_ic()
+{
+    InitSource src{};
+    src.kind = s.initial_discrete ? 3 : 0;
+    src.ic_num = s.initial_condition_num;
+    src.discrete = wdisc;
+    src.gd = gd;
+    src.params = d_params_;
+    src.rand_table = d_rand_;
+    CMM_LAUNCH(1, launch_compose_sample(gc, gf, ChiX, ChiY, stack, n_maps_, src, real_buf_, stream));
+    CMM_FFT(cufftExecD2Z(pf_.d2z, real_buf_, reinterpret_cast<cufftDoubleComplex*>(spec_)));
+    CMM_LAUNCH(1, launch_spec_hermite(spec_, gf, spec4_, stream));
+    CMM_FFT(cufftExecZ2D(pf_.z2d4, reinterpret_cast<cufftDoubleComplex*>(spec4_), wfine));
+    return kOk;
+}
+
+int EulerSim::evaluate_stream()
+{
+    CMM_LAUNCH(1, launch_sample_vort(gc, gv, gf, ChiX, ChiY, wfine, s.molly_stencil, real_buf_, gv.NX, stream));
+    CMM_FFT(cufftExecD2Z(pv_.d2z, real_buf_, reinterpret_cast<cufftDoubleComplex*>(spec_)));
+    CMM_LAUNCH(1, launch_spec_psi(spec_, gv, gp, s.freq_cut_psi, spec4_, stream));
+    CMM_FFT(cufftExecZ2D(pp_.z2d4, reinterpret_cast<cufftDoubleComplex*>(spec4_), psi[0]));
+    return kOk;
+}
+
+int EulerSim::coarse_vort()
+{
+    CMM_LAUNCH(1, launch_sample_vort(gc, gc, gf, ChiX, ChiY, wfine, 0, vort, gc.NX, stream));
+    return kOk;
+}
+
+int EulerSim::advect(const double* t, const double* dtv, int lc, int ti_num, int l_order)
+{
+    AdvectArgs a{};
+    a.gm = gc; a.gp = gp;
+    a.ChiX = ChiX; a.ChiY = ChiY; a.outX = ChiX_new; a.outY = ChiY_new;
+    for (int l = 0; l < kMaxLagrange; ++l) a.psi[l] = psi[l];
+    int lcl = lc + l_order - 1;
+    for (int i = 0; i < l_order; ++i) {
+        a.L1[i] = lagrange_coefficient(t, t[lcl + 1], lcl, i, l_order);
+        a.L12[i] = lagrange_coefficient(t, t[lcl] + dtv[lcl + 1] / 2.0, lcl, i, l_order);
+    }
+    map_update_coefficients(s.map_update_order_num, s.map_epsilon, a.coef, &a.nfoot);
+    a.dt = dtv[lcl + 1];
+    a.ep = s.map_epsilon;
+    a.time_integration_num = ti_num;
+    a.l_order = l_order;
+    CMM_LAUNCH(1, launch_advect(a, stream));
+    std::swap(ChiX, ChiX_new);
+    std::swap(ChiY, ChiY_new);
+    return kOk;
+}
+
+int EulerSim::incomp(double* out)
+{
+    CMM_LAUNCH(1, launch_incomp(gf, gc, ChiX, ChiY, d_scal_, stream));
+    CMM_CUDA(cudaMemcpyAsync(h_scal_, d_scal_, sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CMM_CUDA(cudaStreamSynchronize(stream));
+    *out = h_scal_[0];
+    return kOk;
+}
+
+void EulerSim::rotate_psi(int n)
+{
+    // levels 0..n-1 move to 1..n, the buffer of level n becomes the new level 0
+    double* tmp = psi[n];
+    for (int j = n; j >= 1; --j) psi[j] = psi[j - 1];
+    psi[0] = tmp;
+}
+
+int EulerSim::push_stack()
+{
+    if (n_maps_ >= stack_cap_) {
+        int cap = std::min(max_maps, std::max(2 * stack_cap_, 16));
+        double* bigger = nullptr;
+        CMM_CUDA(cudaMalloc((void**)&bigger, sizeof(double) * 8 * (size_t)gc.N * cap));
+        if (stack && n_maps_ > 0)
+            CMM_CUDA(cudaMemcpyAsync(bigger, stack, sizeof(double) * 8 * (size_t)gc.N * n_maps_,
+                                     cudaMemcpyDeviceToDevice, stream));
+        CMM_CUDA(cudaStreamSynchronize(stream));
+        if (stack) cudaFree(stack);
+        stack = bigger;
+        stack_cap_ = cap;
+    }
+    double* slot = stack + (size_t)n_maps_ * 8 * gc.N;
+    CMM_CUDA(cudaMemcpyAsync(slot, ChiX, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToDevice, stream));
+    CMM_CUDA(cudaMemcpyAsync(slot + 4 * gc.N, ChiY, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToDevice, stream));
+    n_maps_++;
+    return kOk;
+}
+
+int EulerSim::init_particles()
+{
+    // init_particles (src/simulation/cmm-init.cu:311-389); bounds of the psi grid
+    for (size_t i = 0; i < s.particles_advected.size(); ++i) {
+        auto& p = s.particles_advected[i];
+        if (p.num <= 0) continue;
+        if (p.init_num == 0 || p.init_num == 1) {
+            curandGenerator_t g;
+            if (curandCreateGenerator(&g, CURAND_RNG_PSEUDO_DEFAULT) != CURAND_STATUS_SUCCESS) { err = "cuRAND create"; return kErrCuda; }
+            curandSetStream(g, stream);
+            curandSetPseudoRandomGeneratorSeed(g, p.seed);
+            curandStatus_t st = p.init_num == 0 ? curandGenerateUniformDouble(g, parts[i], 2 * (size_t)p.num)
+                                                : curandGenerateNormalDouble(g, parts[i], 2 * (size_t)p.num, 0.5, 1.0);
+            curandDestroyGenerator(g);
+            if (st != CURAND_STATUS_SUCCESS) { err = "cuRAND generate"; return kErrCuda; }
+            CMM_LAUNCH(1, launch_particle_rescale(parts[i], p.num, p.init_param, gp, stream));
+        } else if (p.init_num >= 2 && p.init_num <= 4) {
+            CMM_LAUNCH(1, launch_particle_layout(parts[i], p.num, p.init_num, p.init_param, gp, stream));
+        } else {
+            err = "unknown particle init_name " + p.init_name;
+            return kErrParam;
+        }
+        if (p.tau != 0)
+            log_.push("Particles set P" + two((int)i + 1) + " : inertial particles (tau != 0) are not advected by this build");
+    }
+    return kOk;
+}
+
+int EulerSim::advect_particles(int lcl)
+{
+    // particles_advect (src/numerical/cmm-particles.cu:63-87): L12 for
+    // t_n + dt/2 on the history ending at the new psi
+    double Lp12[kMaxLagrange] = {0, 0, 0, 0};
+    for (int i = 0; i < L; ++i)
+        Lp12[i] = lagrange_coefficient(t_vec_.data(), t_vec_[lcl] + dt_vec_[lcl + 1] / 2.0, lcl + 1, i, L);
+    for (size_t i = 0; i < s.particles_advected.size(); ++i) {
+        auto& p = s.particles_advected[i];
+        if (p.num <= 0 || p.tau != 0) continue;
+        if (!(t_vec_[lcl + 1] + 1e-5 * dt_vec_[lcl + 1] >= p.init_time)) continue;
+        ParticleArgs a{};
+        a.gp = gp; a.pos = parts[i]; a.num = p.num;
+        for (int l = 0; l < kMaxLagrange; ++l) a.psi[l] = psi[l];
+        for (int l = 0; l < kMaxLagrange; ++l) a.Lp12[l] = Lp12[l];
+        a.dt = dt_vec_[lcl + 1];
+        a.time_integration_num = p.time_integration_num;
+        a.l_order = L;
+        cudaError_t e = launch_particles(a, stream);
+        kernel_launches++;
+        if (e == cudaErrorInvalidValue) { err = "particle time integration " + p.time_integration + " is not built"; return kErrUnsupported; }
+        CMM_CUDA(e);
+    }
+    return kOk;
+}
+
+// ---------------------------------------------------------------- init
+int EulerSim::init()
+{
+    if (initialised_) { err = "init called twice"; return kErrState; }
+    begin_ = std::chrono::steady_clock::now();
+    int rc = alloc();
+    if (rc) return rc;
+    if (!create_directory_structure(s)) { err = "cannot create output folders under " + s.workspace; return kErrIO; }
+    log_.open(run_dir(s) + "/log.txt");
+    log_.quiet = s.verbose < 1;
+    if (s.verbose >= 1) {
+        log_.push("Solving = " + s.simulation_type);
+        log_.push("Initial condition = " + s.initial_condition);
+        log_.push("Iter max = " + std::to_string(s.iter_max()));
+        log_.push("Name of simulation = " + s.file_name);
+        log_.push("Map stack length = " + std::to_string(max_maps) + " (device resident)");
+    }
+    s.save_param_file(run_dir(s) + "/params.txt");
+
+    // discrete initial condition (cmm-euler2d.cu:325-344)
+    if (s.initial_discrete) {
+        if (host_discrete_.empty()) {
+            host_discrete_.resize((size_t)gd.N);
+            std::ifstream f(s.initial_discrete_location, std::ios::binary);
+            if (!f) { err = "unable to read discrete initial condition " + s.initial_discrete_location; return kErrIO; }
+            f.read(reinterpret_cast<char*>(host_discrete_.data()), sizeof(double) * gd.N);
+            if (f.gcount() != (std::streamsize)(sizeof(double) * gd.N)) { err = "discrete initial condition too short"; return kErrIO; }
+        }
+        CMM_CUDA(cudaMemcpyAsync(real_buf_, host_discrete_.data(), sizeof(double) * gd.N, cudaMemcpyHostToDevice, stream));
+        CMM_FFT(cufftExecD2Z(pd_.d2z, real_buf_, reinterpret_cast<cufftDoubleComplex*>(spec_)));
+        CMM_LAUNCH(1, launch_spec_hermite(spec_, gd, spec4_, stream));
+        CMM_FFT(cufftExecZ2D(pd_.z2d4, reinterpret_cast<cufftDoubleComplex*>(spec4_), wdisc));
+        CMM_CUDA(cudaStreamSynchronize(stream));   // host_discrete_ may be released by the caller
+    }
+
+    CMM_LAUNCH(1, launch_init_map(ChiX, ChiY, gc, stream));
+    if ((rc = translate_ic()) || (rc = evaluate_stream()) || (rc = coarse_vort())) return rc;
+
+    // Lagrange velocity history (cmm-euler2d.cu:520-619): alternate the
+    // direction of time and raise the scheme order EulerExp -> RK2 -> RK3
+    if (L > 1) {
+        double dt_now = dt * std::pow(-1.0, L);
+        double t_init[5] = {0, dt_now, 2 * dt_now, 3 * dt_now, 4 * dt_now};
+        double dt_init[5] = {dt_now, dt_now, dt_now, dt_now, dt_now};
+        for (int io = 1; io <= L; ++io) {
+            if (!s.lagrange_init_higher_order && io != L) {
+                for (int i = 0; i < 5; ++i) { dt_init[i] = -dt_init[i]; t_init[i] = -t_init[i]; }
+                continue;
+            }
+            int ti = 10, lo = 1;
+            if (s.lagrange_init_higher_order) {
+                ti = io == 1 ? 10 : io == 2 ? 21 : 30;
+                lo = io;
+                if (io == 4) { err = "Lagrange order 4 initialisation needs RK4 (not built)"; return kErrUnsupported; }
+            }
+            int nsteps = io - (io == L);
+            for (int k = 1; k <= nsteps; ++k) {
+                if ((rc = advect(t_init, dt_init, 0, ti, lo))) return rc;
+                double inc;
+                if ((rc = incomp(&inc))) return rc;
+                rotate_psi(nsteps);
+                if ((rc = evaluate_stream())) return rc;
+                if (s.verbose >= 2)
+                    log_.push("   Init step = " + std::to_string(k) + "/" + std::to_string(nsteps) + " \t IncompErr = " + to_str3(inc));
+            }
+            for (int i = 0; i < 5; ++i) { dt_init[i] = -dt_init[i]; t_init[i] = -t_init[i]; }
+            std::swap(psi[0], psi[nsteps]);
+            if (nsteps >= 3) std::swap(psi[1], psi[2]);
+            CMM_LAUNCH(1, launch_init_map(ChiX, ChiY, gc, stream));
+        }
+        CMM_LAUNCH(1, launch_init_map(ChiX, ChiY, gc, stream));
+    }
+    if ((rc = init_particles())) return rc;
+
+    t_vec_.assign((size_t)s.iter_max() + L + 8, 0.0);
+    dt_vec_.assign(t_vec_.size(), dt);
+    for (int i = 0; i < L; ++i) { t_vec_[i] = s.restart_time - (L - 1 - i) * dt; dt_vec_[i] = dt; }
+    loop_ctr_ = 0; old_ctr_ = 0; n_maps_ = 0;
+    initialised_ = true;
+
+    if ((rc = save_functions(s.restart_time, dt))) return rc;
+    double tc = wall();
+    append_f64(run_dir(s) + "/Monitoring_data/Time_c.data", &tc, 1);
+    if (s.verbose >= 1) log_.push("Simulation initialization finished \t C-Time = " + format_duration(tc));
+    return kOk;
+}
+
+// ---------------------------------------------------------------- loop
+double EulerSim::compute_next_timestep(double t) const
+{
+    // src/simulation/cmm-simulation-host.cu:1307-1374
+    double dt_now = dt, e = dt * 1e-5;
+    auto instant = [&](double start) {
+        if (t + e - start < 0 && t + e + dt - start > 0) dt_now = std::fmin(dt_now, start - t);
+    };
+    auto interval = [&](double start, double end, double step) {
+        double a = std::fmod(t + e - start, step), b2 = std::fmod(t + dt + e - start, step);
+        if ((a > b2 || (a < 0 && b2 > 0)) && t + dt + e >= start && t - e <= end)
+            dt_now = std::fmin(dt_now, step - std::fmod(t, step));
+    };
+    for (auto& p : s.particles_advected) instant(p.init_time);
+    for (auto& p : s.particles_forwarded) instant(p.init_time);
+    for (auto& r : s.save_computational) r.is_instant ? instant(r.time_start) : interval(r.time_start, r.time_end, r.time_step);
+    for (auto& r : s.save_sample) r.is_instant ? instant(r.time_start) : interval(r.time_start, r.time_end, r.time_step);
+    for (auto& r : s.save_zoom) r.is_instant ? instant(r.time_start) : interval(r.time_start, r.time_end, r.time_step);
+    return dt_now;
+}
+
+bool EulerSim::done() const
+{
+    if (!initialised_) return false;
+    int lcl = loop_ctr_ + L - 1;
+    return !(s.final_time - t_vec_[lcl] > dt * 1e-5 && loop_ctr_ < s.iter_max() && continue_);
+}
+
+int EulerSim::step_once()
+{
+    if (!initialised_) { err = "step before init"; return kErrState; }
+    if (done()) return 1;
+    int rc;
+    int lcl = loop_ctr_ + L - 1;
+    double t = t_vec_[lcl];
+    double dt_now = compute_next_timestep(t);
+    if (t + dt_now > s.final_time) dt_now = s.final_time - t;
+    t_vec_[lcl + 1] = t + dt_now;
+    dt_vec_[lcl + 1] = dt_now;
+
+    ph_begin(kPhAdvect);
+    if ((rc = advect(t_vec_.data(), dt_vec_.data(), loop_ctr_, s.time_integration_num, L))) return rc;
+    ph_end(kPhAdvect);
+    ph_begin(kPhIncomp);
+    if ((rc = incomp(&e_inc_))) return rc;
+    ph_end(kPhIncomp);
+    bool saturated = false;
+    if (e_inc_ > s.incomp_threshold && !s.skip_remapping) {
+        if (n_maps_ >= max_maps) {
+            if (s.verbose >= 0) log_.push("Stack Saturated : Exitting");
+            saturated = true;
+            continue_ = false;
+        } else {
+            if (s.verbose >= 2)
+                log_.push("Refining Map : Step = " + std::to_string(loop_ctr_) + " \t Maps = " + std::to_string(n_maps_ + 1) +
+                          " \t Gap = " + std::to_string(loop_ctr_ - old_ctr_));
+            old_ctr_ = loop_ctr_;
+            ph_begin(kPhRemap);
+            if ((rc = translate_ic())) return rc;
+            if ((rc = push_stack())) return rc;
+            CMM_LAUNCH(1, launch_init_map(ChiX, ChiY, gc, stream));
+            kernel_launches++;
+            ph_end(kPhRemap);
+        }
+    }
+    double gap = loop_ctr_ - old_ctr_, counter = n_maps_;
+    rotate_psi(L - 1);
+    ph_begin(kPhPsi);
+    if ((rc = evaluate_stream())) return rc;
+    ph_end(kPhPsi);
+    ph_begin(kPhCoarse);
+    if ((rc = coarse_vort())) return rc;
+    ph_end(kPhCoarse);
+    ph_begin(kPhParticles);
+    if ((rc = advect_particles(lcl))) return rc;
+    ph_end(kPhParticles);
+    ph_begin(kPhSave);
+    if ((rc = save_functions(t_vec_[lcl + 1], dt_now))) return rc;
+    ph_end(kPhSave);
+    ph_collect();
+    loop_ctr_++;
+    CMM_CUDA(cudaGetLastError());
+
+    std::string dir = run_dir(s) + "/Monitoring_data/";
+    append_f64(dir + "Time_s.data", &t_vec_[lcl + 1], 1);
+    append_f64(dir + "Error_incompressibility.data", &e_inc_, 1);
+    append_f64(dir + "Map_gaps.data", &gap, 1);
+    append_f64(dir + "Map_counter.data", &counter, 1);
+    double tc = wall();
+    if (s.verbose >= 2)
+        log_.push("Step = " + std::to_string(loop_ctr_) + " \t S-Time = " + to_str3(t_vec_[lcl + 1]) + "/" +
+                  to_str3(s.final_time) + " \t E-inc = " + to_str3(e_inc_) + " \t C-Time = " + format_duration(tc));
+    append_f64(dir + "Time_c.data", &tc, 1);
+    return saturated ? kErrSaturated : kOk;
+}
+
+int EulerSim::finish()
+{
+    if (!initialised_) { err = "finish before init"; return kErrState; }
+    if (finished_) return kOk;
+    int rc = save_functions(kTMax, dt);
+    if (rc) return rc;
+    CMM_CUDA(cudaStreamSynchronize(stream));
+    double tc = wall();
+    append_f64(run_dir(s) + "/Monitoring_data/Time_c.data", &tc, 1);
+    if (s.verbose >= 1) log_.push("Finished simulation \t Last Cuda Error = cudaSuccess \t C-Time = " + format_duration(tc));
+    finished_ = true;
+    return kOk;
+}
+
+// ---------------------------------------------------------------- saves
+static bool instant_fires(bool is_instant, double start, double end, double step, double t_now, double dt_now, double dt)
+{
+    // src/ui/cmm-io.cu:302-317
+    if (is_instant) return t_now - start + dt * 1e-5 < dt_now && t_now - start + dt * 1e-5 >= 0;
+    return (std::fmod(t_now - start + dt * 1e-5, step) < dt_now && t_now + dt * 1e-5 >= start && t_now - dt * 1e-5 <= end) ||
+           t_now == end;
+}
+
+int EulerSim::save_functions(double t_now, double dt_now)
+{
+    int rc;
+    if ((rc = write_time_step(t_now, dt_now))) return rc;
+    if ((rc = conservation(t_now, dt_now))) return rc;
+    return kOk;
+}
+
+int EulerSim::debug_globals(const std::string& name, const double* v, long long n, bool grid_form, const Grid& g)
+{
+    CMM_LAUNCH(2, launch_stats(v, n, 1, red_, d_scal_ + 8, stream));
+    CMM_CUDA(cudaMemcpyAsync(h_scal_ + 8, d_scal_ + 8, sizeof(double) * 4, cudaMemcpyDeviceToHost, stream));
+    CMM_CUDA(cudaStreamSynchronize(stream));
+    double m[4] = {h_scal_[8], h_scal_[9], 0, 0};
+    if (grid_form) { m[2] = g.hy * g.hx * h_scal_[10]; m[3] = g.hy * g.hx * h_scal_[11]; }
+    else { m[2] = h_scal_[10] / (double)n; m[3] = h_scal_[11] / (double)n; }
+    std::string base = run_dir(s) + "/Monitoring_data/Debug_globals/" + name;
+    const char* suf[4] = {"_Min", "_Max", "_Avg", "_L2"};
+    for (int i = 0; i < 4; ++i) append_f64(base + suf[i] + ".data", &m[i], 1);
+    return kOk;
+}
+
+int EulerSim::write_field(const std::string& sub, const std::string& name, const double* v, long long n)
+{
+    std::vector<double> h((size_t)n);
+    CMM_CUDA(cudaMemcpyAsync(h.data(), v, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
+    CMM_CUDA(cudaStreamSynchronize(stream));
+    if (!write_f64(run_dir(s) + sub + "/" + name + ".data", h.data(), (size_t)n)) { err = "cannot write " + name; return kErrIO; }
+    return kOk;
+}
+
+int EulerSim::write_time_step(double t_now, double dt_now)
+{
+    // writeTimeStep (src/ui/cmm-io.cu:295-437)
+    std::string var;
+    bool fire = false;
+    for (auto& r : s.save_computational)
+        if (instant_fires(r.is_instant, r.time_start, r.time_end, r.time_step, t_now, dt_now, dt)) { fire = true; var += r.var; }
+    if (!fire) return kOk;
+    std::string tname = std::abs(t_now - kTMax) < 1 ? "final" : to_str3(t_now);
+    bool all = has(var, "All");
+    bool dbg = s.verbose >= 4;
+    std::string sub = "/Time_data/Time_" + tname;
+    bool any = has(var, "Vorticity") || has(var, "W") || has(var, "Stream") || has(var, "Psi") || has(var, "Map") ||
+               has(var, "Chi") || has(var, "Velocity") || has(var, "U") || has(var, "Dist") || has(var, "F") || all;
+    std::string dbg_time = run_dir(s) + "/Monitoring_data/Debug_globals/Time_s.data";
+    if (any) {
+        make_dir(run_dir(s) + sub);
+        if (dbg) append_f64(dbg_time, &t_now, 1);
+    }
+    int rc;
+    auto var2d = [&](const std::string& name, const double* v, const Grid& g) {
+        return dbg ? debug_globals(name, v, g.N, true, g) : write_field(sub, name, v, g.N);
+    };
+    auto arr = [&](const std::string& sub2, const std::string& name, const double* v, long long n) {
+        return dbg ? debug_globals(name, v, n, false, gc) : write_field(sub2, name, v, n);
+    };
+    if (has(var, "Vorticity") || has(var, "W") || all) if ((rc = var2d("Vorticity_W_coarse", vort, gc))) return rc;
+    if (has(var, "Dist") || has(var, "F") || all) if ((rc = var2d("Distribution_coarse", vort, gc))) return rc;
+    if (has(var, "Stream") || has(var, "Psi") || all) if ((rc = var2d("Stream_function_Psi_psi", psi[0], gp))) return rc;
+    if (has(var, "Stream_H") || has(var, "Psi_H") || all)
+        if ((rc = arr(sub, "Stream_function_Psi_H_psi", psi[0], 4 * gp.N))) return rc;
+    if (has(var, "Velocity") || has(var, "U") || all) {
+        if ((rc = var2d("Velocity_UX_psi", psi[0] + gp.N, gp))) return rc;
+        if ((rc = var2d("Velocity_UY_psi", psi[0] + 2 * gp.N, gp))) return rc;
+    }
+    if (has(var, "Map_b") || has(var, "Chi_b") || all) {
+        if ((rc = var2d("Map_ChiX_coarse", ChiX, gc))) return rc;
+        if ((rc = var2d("Map_ChiY_coarse", ChiY, gc))) return rc;
+    }
+    if (has(var, "Map_H") || has(var, "Chi_H") || all) {
+        if ((rc = arr(sub, "Map_ChiX_H_coarse", ChiX, 4 * gc.N))) return rc;
+        if ((rc = arr(sub, "Map_ChiY_H_coarse", ChiY, 4 * gc.N))) return rc;
+    }
+    std::string psub = "/Particle_data/Time_" + tname;
+    if (has(var, "PartA_") || all) {
+        make_dir(run_dir(s) + psub);
+        if (!any && dbg) append_f64(dbg_time, &t_now, 1);
+    }
+    for (size_t i = 0; i < s.particles_advected.size(); ++i) {
+        auto& p = s.particles_advected[i];
+        if (p.tau != 0) continue;   // inertial sets are not advected by this build
+        std::string id = two((int)i + 1);
+        if (has(var, ("PartA_" + id).c_str()) || all)
+            if ((rc = arr(psub, "Particles_advected_pos_P" + id, parts[i], 2ll * p.num))) return rc;
+        if (has(var, ("PartA_Vel_" + id).c_str()) || all) {
+            CMM_LAUNCH(1, launch_sample_points_dxdy(gp, psi[0], parts[i], real_buf_, p.num, stream));
+            if ((rc = arr(psub, "Particles_advected_vel_U" + id, real_buf_, 2ll * p.num))) return rc;
+        }
+    }
+    return kOk;
+}
+
+int EulerSim::diagnostics(double* energy, double* enstrophy, double* palinstrophy, double* wmax)
+{
+    // Compute_Energy_H, Compute_Enstrophy, Compute_Palinstrophy, w max
+    // (src/numerical/cmm-mesure.cu:30-89, cmm-simulation-host.cu:668-673)
+    CMM_LAUNCH(2, launch_sumsq(psi[0] + gp.N, 2 * gp.N, red_, d_scal_ + 1, stream));
+    CMM_LAUNCH(2, launch_sumsq(vort, gc.N, red_, d_scal_ + 2, stream));
+    CMM_FFT(cufftExecD2Z(pc_.d2z, vort, reinterpret_cast<cufftDoubleComplex*>(spec_)));
+    CMM_LAUNCH(1, launch_spec_grad(spec_, gc, spec4_, stream));
+    CMM_FFT(cufftExecZ2D(pc_.z2d1, reinterpret_cast<cufftDoubleComplex*>(spec4_), real_buf_));
+    CMM_LAUNCH(2, launch_sumsq(real_buf_, gc.N, red_, d_scal_ + 3, stream));
+    CMM_FFT(cufftExecZ2D(pc_.z2d1, reinterpret_cast<cufftDoubleComplex*>(spec4_ + gc.Nfft), real_buf_));
+    CMM_LAUNCH(2, launch_sumsq(real_buf_, gc.N, red_, d_scal_ + 4, stream));
+    CMM_LAUNCH(2, launch_stats(vort, gc.N, 1, red_, d_scal_ + 8, stream));
+    CMM_CUDA(cudaMemcpyAsync(h_scal_, d_scal_, sizeof(double) * 12, cudaMemcpyDeviceToHost, stream));
+    CMM_CUDA(cudaStreamSynchronize(stream));
+    *energy = 0.5 * gp.hx * gp.hy * h_scal_[1];
+    *enstrophy = 0.5 * gc.hx * gc.hy * h_scal_[2];
+    *palinstrophy = 0.5 * gc.hx * gc.hy * h_scal_[3] + 0.5 * gc.hx * gc.hy * h_scal_[4];
+    double w_max = std::max(0.0, h_scal_[9]), w_min = std::min(0.0, h_scal_[8]);
+    *wmax = std::max(w_max, -w_min);
+    return kOk;
+}
+
+int EulerSim::conservation(double t_now, double dt_now)
+{
+    // compute_conservation_targets (src/simulation/cmm-simulation-host.cu:615-698)
+    bool fire = false;
+    for (auto& r : s.save_computational)
+        if (r.conv && instant_fires(r.is_instant, r.time_start, r.time_end, r.time_step, t_now, dt_now, dt)) fire = true;
+    if (!fire) return kOk;
+    double m[4];
+    int rc = diagnostics(&m[0], &m[1], &m[2], &m[3]);
+    if (rc) return rc;
+    std::string dir = run_dir(s) + "/Monitoring_data/Mesure/";
+    append_f64(dir + "Time_s.data", &t_now, 1);
+    append_f64(dir + "Energy.data", &m[0], 1);
+    append_f64(dir + "Enstrophy.data", &m[1], 1);
+    append_f64(dir + "Palinstrophy.data", &m[2], 1);
+    append_f64(dir + "Max_vorticity.data", &m[3], 1);
+    if (s.verbose >= 3)
+        log_.push("Computed coarse Cons : Energ = " + to_str_prec(m[0], 8) + " \t Enstr = " + to_str_prec(m[1], 8) +
+                  " \t Palinstr = " + to_str_prec(m[2], 8) + " \t Wmax = " + to_str_prec(m[3], 8));
+    return kOk;
+}
+
+// ---------------------------------------------------------------- fields
+size_t EulerSim::field_bytes(const std::string& n) const
+{
+    if (n == "Map_ChiX_H_coarse" || n == "Map_ChiY_H_coarse") return sizeof(double) * 4 * gc.N;
+    if (n == "Stream_function_Psi_H_psi") return sizeof(double) * 4 * gp.N;
+    if (n == "Stream_function_Psi_H_psi_all") return sizeof(double) * 4 * gp.N * L;
+    if (n == "Vorticity_W_coarse") return sizeof(double) * gc.N;
+    if (n == "Vorticity_W_fine_H") return sizeof(double) * 4 * gf.N;
+    if (n == "Map_stack") return sizeof(double) * 8 * gc.N * n_maps_;
+    for (size_t i = 0; i < s.particles_advected.size(); ++i) {
+        std::string id = two((int)i + 1);
+        if (n == "Particles_advected_pos_P" + id || n == "Particles_advected_vel_U" + id)
+            return sizeof(double) * 2 * s.particles_advected[i].num;
+    }
+    return 0;
+}
+
+int EulerSim::get_field(const std::string& n, void* dst, size_t bytes)
+{
+    if (!initialised_) { err = "get_field before init"; return kErrState; }
+    size_t need = field_bytes(n);
+    if (need == 0 && n != "Map_stack") { err = "unknown field " + n; return kErrNotFound; }
+    if (bytes != need) { err = "field " + n + " needs " + std::to_string(need) + " bytes"; return kErrParam; }
+    char* d = static_cast<char*>(dst);
+    auto cp = [&](const void* src, size_t b) { return check(cudaMemcpyAsync(d, src, b, cudaMemcpyDeviceToHost, stream), "get_field"); };
+    int rc = kOk;
+    if (n == "Map_ChiX_H_coarse") rc = cp(ChiX, bytes);
+    else if (n == "Map_ChiY_H_coarse") rc = cp(ChiY, bytes);
+    else if (n == "Stream_function_Psi_H_psi") rc = cp(psi[0], bytes);
+    else if (n == "Stream_function_Psi_H_psi_all") {
+        size_t lb = sizeof(double) * 4 * gp.N;
+        for (int l = 0; l < L && !rc; ++l) { rc = check(cudaMemcpyAsync(d + l * lb, psi[l], lb, cudaMemcpyDeviceToHost, stream), "get_field"); }
+    }
+    else if (n == "Vorticity_W_coarse") rc = cp(vort, bytes);
+    else if (n == "Vorticity_W_fine_H") rc = cp(wfine, bytes);
+    else if (n == "Map_stack") rc = bytes ? cp(stack, bytes) : kOk;
+    else {
+        for (size_t i = 0; i < s.particles_advected.size(); ++i) {
+            std::string id = two((int)i + 1);
+            if (n == "Particles_advected_pos_P" + id) rc = cp(parts[i], bytes);
+            else if (n == "Particles_advected_vel_U" + id) {
+                rc = check(launch_sample_points_dxdy(gp, psi[0], parts[i], real_buf_, s.particles_advected[i].num, stream), "dxdy");
+                if (!rc) rc = cp(real_buf_, bytes);
+            }
+        }
+    }
+    if (rc) return rc;
+    CMM_CUDA(cudaStreamSynchronize(stream));
+    return kOk;
+}
+
+int EulerSim::get_scalar(const std::string& n, double* out)
+{
+    if (n == "dt") { *out = dt; return kOk; }
+    if (n == "lagrange_order") { *out = L; return kOk; }
+    if (n == "stack_capacity") { *out = max_maps; return kOk; }
+    if (!initialised_) { err = "get_scalar before init"; return kErrState; }
+    if (n == "time") { *out = time(); return kOk; }
+    if (n == "e_inc") { *out = e_inc_; return kOk; }
+    if (n == "map_counter") { *out = n_maps_; return kOk; }
+    if (n == "map_gap") { *out = (loop_ctr_ - 1) - old_ctr_; return kOk; }
+    if (n == "loop_ctr") { *out = loop_ctr_; return kOk; }
+    if (n == "kernel_launches") { *out = (double)kernel_launches; return kOk; }
+    if (n == "fft_calls") { *out = (double)fft_calls; return kOk; }
+    for (int p = 0; p < kNumPhases; ++p) {
+        std::string base = std::string("prof_") + phase_name(p);
+        if (n == base + "_ms") { *out = prof_ms[p]; return kOk; }
+        if (n == base + "_count") { *out = (double)prof_count[p]; return kOk; }
+    }
+    double m[4];
+    if (n == "energy" || n == "enstrophy" || n == "palinstrophy" || n == "max_vorticity") {
+        int rc = diagnostics(&m[0], &m[1], &m[2], &m[3]);
+        if (rc) return rc;
+        *out = n == "energy" ? m[0] : n == "enstrophy" ? m[1] : n == "palinstrophy" ? m[2] : m[3];
+        return kOk;
+    }
+    err = "unknown scalar " + n;
+    return kErrNotFound;
+}
+
+}  // namespace cmm

@@ -1,0 +1,128 @@
+// sim.hpp -- the 2D Euler CMM simulation context on one GPU (FP64 plain form).
+//
+// Owns every device buffer; all work is ordered on one CUDA stream.  The only
+// host synchronisation per loop iteration is the 8-byte read of the
+// incompressibility error that decides the remap (the reference also blocks
+// there, src/simulation/cmm-simulation-host.cu:48-49).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <string>
+#include <vector>
+
+#include "io.hpp"
+#include "kernels.hpp"
+#include "settings.hpp"
+
+namespace cmm {
+
+// status codes shared with the C-ABI
+enum Status { kOk = 0, kErrParam = -1, kErrIO = -2, kErrCuda = -3, kErrSaturated = -4, kErrState = -5,
+              kErrUnsupported = -6, kErrNotFound = -7 };
+
+class EulerSim {
+public:
+    explicit EulerSim(const Settings& s);
+    ~EulerSim();
+
+    int set_stream(cudaStream_t s);
+    int set_initial_discrete(const double* host, size_t n);
+    int init();
+    // one loop iteration; returns 0, 1 (final time reached, nothing done),
+    // kErrSaturated (loop stopped after this iteration) or an error
+    int step_once();
+    int finish();       // final save + log line
+    bool done() const;
+
+    int get_field(const std::string& name, void* dst, size_t bytes);
+    size_t field_bytes(const std::string& name) const;
+    int get_scalar(const std::string& name, double* out);
+
+    Settings s;
+    std::string err;
+
+    // grids
+    Grid gc, gf, gp, gv, gd;
+    double dt = 0;
+    int L = 1;
+    int max_maps = 0;
+
+    // monitoring state
+    double time() const { return t_vec_.empty() ? 0.0 : t_vec_[loop_ctr_ + L - 1]; }
+    int loop_ctr() const { return loop_ctr_; }
+    int map_count() const { return n_maps_; }
+    double last_e_inc() const { return e_inc_; }
+
+    // device state (reference planar layouts)
+    double* ChiX = nullptr; double* ChiY = nullptr;
+    double* ChiX_new = nullptr; double* ChiY_new = nullptr;
+    double* psi[kMaxLagrange] = {nullptr, nullptr, nullptr, nullptr};
+    double* vort = nullptr;        // coarse vorticity
+    double* wfine = nullptr;       // fine vorticity Hermite (4 planes)
+    double* wdisc = nullptr;       // discrete initial vorticity Hermite (4 planes)
+    double* stack = nullptr;       // n maps, 8*Nc doubles each
+    std::vector<double*> parts;    // particle positions per set
+    cudaStream_t stream = nullptr;
+
+    // diagnostics (reference Mesure)
+    int diagnostics(double* energy, double* enstrophy, double* palinstrophy, double* wmax);
+
+    // per-phase CUDA-event timers (off by default) and launch counters
+    enum Phase { kPhAdvect = 0, kPhIncomp, kPhRemap, kPhPsi, kPhCoarse, kPhParticles, kPhSave, kNumPhases };
+    static const char* phase_name(int p);
+    void set_profiling(bool on);
+    double prof_ms[kNumPhases] = {0};
+    long long prof_count[kNumPhases] = {0};
+    long long kernel_launches = 0;    // launches of this library's kernels
+    long long fft_calls = 0;          // cuFFT executions
+
+private:
+    int alloc();
+    void release();
+    int translate_ic();
+    int evaluate_stream();
+    int coarse_vort();
+    int advect(const double* t, const double* dtv, int loop_ctr, int ti_num, int l_order);
+    int incomp(double* out);
+    int init_particles();
+    int advect_particles(int lcl);
+    int push_stack();
+    int save_functions(double t_now, double dt_now);
+    int write_time_step(double t_now, double dt_now);
+    int conservation(double t_now, double dt_now);
+    int debug_globals(const std::string& name, const double* v, long long n, bool grid_form, const Grid& g);
+    int write_field(const std::string& sub, const std::string& name, const double* v, long long n);
+    int write_monitors();
+    int check(cudaError_t e, const char* what);
+    double compute_next_timestep(double t) const;
+    void rotate_psi(int n);
+    double wall() const;
+
+    void ph_begin(int p);
+    void ph_end(int p);
+    void ph_collect();
+    bool prof_ = false;
+    cudaEvent_t ev_[kNumPhases][2] = {};
+    bool ev_live_[kNumPhases] = {};
+    bool own_stream_ = false;
+    bool initialised_ = false, finished_ = false, continue_ = true;
+    double* real_buf_ = nullptr;     // real scratch (largest grid)
+    double2* spec_ = nullptr;        // complex scratch (largest grid)
+    double2* spec4_ = nullptr;       // 4 complex spectra (largest grid)
+    double* red_ = nullptr;          // reduction partials
+    double* d_scal_ = nullptr;       // 8 device scalars
+    double* h_scal_ = nullptr;       // pinned mirror
+    double* d_params_ = nullptr;     // 10 initial params
+    double* d_rand_ = nullptr;       // 1000 random numbers (gaussian_blobs)
+    int stack_cap_ = 0;
+    FftPlans pf_, pv_, pp_, pc_, pd_;
+    std::vector<double> host_discrete_;
+    std::vector<double> t_vec_, dt_vec_;
+    int loop_ctr_ = 0, old_ctr_ = 0, n_maps_ = 0;
+    double e_inc_ = 0;
+    Logger log_;
+    std::chrono::steady_clock::time_point begin_;
+};
+
+}  // namespace cmm

@@ -1,0 +1,185 @@
+/*
+ * cmm_abi.h -- C-ABI of the GB300 (sm_103a) characteristic-mapping-method
+ * time-step library, libcmm_gb300.so.
+ *
+ * Two levels:
+ *  1. Context API: a drop-in for the reference driver cuda_euler_2d
+ *     (Cuda-CMM/src/simulation/cmm-euler2d.cu:45-1099) configured exactly like
+ *     the reference executable (src/main2d.cpp:66-105): presets, then every
+ *     param_file=F argument, then COMMAND=VALUE arguments.  It writes the
+ *     reference's output tree (data/<sim_name>_<ic>_C<c>_F<f>_t<1/dt>_T<T>/).
+ *  2. Kernel API on caller-owned device buffers in the reference's planar
+ *     Hermite layout ([f, f_x, f_y, f_xy] planes of N doubles, row-major
+ *     iY*NX+iX), each a drop-in for one host function of
+ *     src/simulation/cmm-simulation-host.h:23-77.
+ *
+ * Conventions: every function returns 0 on success or a negative CMM_ERR_*
+ * code; nothing calls exit().  cmm_last_error() describes the last failure of
+ * the calling thread.  All GPU work is ordered on the context stream (or on
+ * the stream argument of the kernel API); one context per host thread.
+ * No torch or CUDA runtime types appear in these signatures: streams are
+ * passed as void* (a cudaStream_t, NULL = legacy default stream).
+ */
+#ifndef CMM_ABI_H
+#define CMM_ABI_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CMM_OK 0
+#define CMM_ERR_PARAM (-1)      /* bad setting / argument (reference: error() -> exit) */
+#define CMM_ERR_IO (-2)         /* unreadable input file, unwritable output */
+#define CMM_ERR_CUDA (-3)       /* CUDA / cuFFT / cuRAND failure (reference: exit(0)) */
+#define CMM_ERR_SATURATED (-4)  /* map stack full; loop stopped (reference: "Stack Saturated") */
+#define CMM_ERR_STATE (-5)      /* call out of order (e.g. step before init) */
+#define CMM_ERR_UNSUPPORTED (-6)/* option of the reference not built in this library */
+#define CMM_ERR_NOT_FOUND (-7)  /* unknown field / scalar name */
+
+typedef struct cmm_ctx cmm_ctx;
+
+/* text of the last error of the calling thread ("" if none) */
+const char* cmm_last_error(void);
+/* library version string */
+const char* cmm_version(void);
+
+/* ---------------------------------------------------------------- context API */
+
+/* Parse settings like main() (src/main2d.cpp:73-89) and create a context.
+ * No GPU work happens here.  Replaces: SettingsCMM(argc,args) +
+ * load_param_file (src/ui/cmm-param.cu:149-229) + applyCommands
+ * (src/ui/settings.cu:334-343). */
+int cmm_create(int argc, const char* const* argv, cmm_ctx** out);
+
+/* Use this CUDA stream (cudaStream_t as void*) for all work of the context;
+ * must precede cmm_init.  Default: a stream owned by the context. */
+int cmm_set_stream(cmm_ctx* ctx, void* stream);
+
+/* Provide the discrete initial vorticity (n = initial_discrete_grid^2 values,
+ * row-major, host memory) instead of reading initial_discrete_location.
+ * Must precede cmm_init.  Replaces readTransferFromBinaryFile at
+ * src/simulation/cmm-euler2d.cu:329. */
+int cmm_set_initial_discrete(cmm_ctx* ctx, const double* host_values, size_t n);
+
+/* Allocate, build the initial state and the Lagrange velocity history, write
+ * the t=0 outputs.  Replaces cmm-euler2d.cu:129-737. */
+int cmm_init(cmm_ctx* ctx);
+
+/* Advance n loop iterations (each: map advection, incompressibility check,
+ * remap, psi solve, coarse vorticity, particles, saves, monitors).  Returns
+ * CMM_ERR_SATURATED when the map stack filled (the loop has stopped), and 1
+ * when the final time was reached before n iterations.  Replaces one pass of
+ * the loop at cmm-euler2d.cu:750-960. */
+int cmm_step(cmm_ctx* ctx, int n);
+
+/* Run to the final time and write the final outputs ("Finished simulation").
+ * Replaces cmm-euler2d.cu:750-1099. */
+int cmm_run(cmm_ctx* ctx);
+
+/* Copy a field to host memory, in the reference's layout.  Names follow the
+ * reference's output files: "Map_ChiX_H_coarse", "Map_ChiY_H_coarse" (4*Nc),
+ * "Stream_function_Psi_H_psi" (4*Npsi, newest level), "Stream_function_Psi_H_psi_all"
+ * (L*4*Npsi), "Vorticity_W_coarse" (Nc), "Vorticity_W_fine_H" (4*Nf),
+ * "Particles_advected_pos_PNN" (2*num), "Particles_advected_vel_UNN" (2*num).
+ * bytes must equal the field size. */
+int cmm_get_field(cmm_ctx* ctx, const char* name, void* host_dst, size_t bytes);
+/* Size in bytes of a field (0 if unknown). */
+size_t cmm_field_bytes(cmm_ctx* ctx, const char* name);
+
+/* Scalars: "time", "dt", "e_inc", "map_counter", "map_gap", "loop_ctr",
+ * "lagrange_order", "energy", "enstrophy", "palinstrophy", "max_vorticity",
+ * "stack_capacity".  Diagnostics are computed on request
+ * (src/numerical/cmm-mesure.cu:30-89). */
+int cmm_get_scalar(cmm_ctx* ctx, const char* name, double* out);
+
+/* Time each loop phase with CUDA events on the context stream (adds one
+ * stream synchronisation per iteration while on).  Totals are read back as
+ * scalars "prof_<phase>_ms" / "prof_<phase>_count" for the phases advect,
+ * incomp, remap, psi, coarse, particles, save; "kernel_launches" and
+ * "fft_calls" count this library's kernel launches and cuFFT executions.
+ * The reference has no counterpart (it only logs wall-clock C-Time,
+ * src/simulation/cmm-euler2d.cu:940-959). */
+int cmm_set_profiling(cmm_ctx* ctx, int on);
+
+/* Resolved settings as the reference's param-file text (cmm-param.cu:39-146)
+ * into buf (NUL-terminated, truncated to cap); returns the full length.
+ * Works without a GPU. */
+int cmm_settings_text(cmm_ctx* ctx, char* buf, size_t cap);
+/* Derived name of the output folder (cmm-euler2d.cu:81-83); works without a GPU. */
+int cmm_file_name(cmm_ctx* ctx, char* buf, size_t cap);
+
+int cmm_destroy(cmm_ctx* ctx);
+
+/* ---------------------------------------------------------------- kernel API */
+
+/* Periodic grid: NX x NY nodes on [bounds[0],bounds[1]) x [bounds[2],bounds[3]),
+ * spacing (bounds[1]-bounds[0])/NX.  Mirrors TCudaGrid2D
+ * (src/grid/cmm-grid2d.h:25-39). */
+typedef struct {
+    int NX, NY;
+    double bounds[4];
+} cmm_grid;
+
+/* Backward map advection by GALS footpoints.  Replaces
+ * advect_using_stream_hermite (src/simulation/cmm-simulation-host.cu:64-104)
+ * for direction -1.  psi_levels: l_order device pointers to Hermite levels
+ * (level 0 newest).  L1/L12: Lagrange coefficients for t_{n+1} and
+ * t_{n+1/2} (get_L_coefficient, src/numerical/cmm-timestep.cu:474-484).
+ * time_integration_num: 10 EulerExp, 21 RK2, 30 RK3; map_update_order_num:
+ * 0 2nd, 1 4th, 2 6th.  Writes the new map to chix_out / chiy_out. */
+int cmm_advect_map(const cmm_grid* grid_map, const cmm_grid* grid_psi, const double* chix, const double* chiy,
+                   double* chix_out, double* chiy_out, const double* const* psi_levels, int l_order,
+                   const double* L1, const double* L12, double dt, double map_epsilon, int time_integration_num,
+                   int map_update_order_num, void* stream);
+
+/* max |1 - det grad X| at half-shifted points of grid_check -> *d_result
+ * (one double in device memory).  Replaces incompressibility_check
+ * (src/simulation/cmm-simulation-host.cu:44-50). */
+int cmm_incomp_max(const cmm_grid* grid_check, const cmm_grid* grid_map, const double* chix, const double* chiy,
+                   double* d_result, void* stream);
+
+/* omega_0(X_0(...X_{n-1}(X_cur(x)))) on grid_target.  stack: n_maps maps
+ * contiguous in device memory, map i = [X planes | Y planes] at stack + i*8*Nc
+ * (i = 0 oldest).  ic_num: analytic initial-condition number (settings name table);
+ * when discrete != NULL the Hermite discrete field on grid_discrete is
+ * sampled instead.  Replaces apply_map_stack + k_h_sample_from_init
+ * (src/simulation/cmm-simulation-host.cu:112-128,299-316). */
+int cmm_compose_stack(const cmm_grid* grid_map, const cmm_grid* grid_target, const double* chix,
+                      const double* chiy, const double* stack, int n_maps, int ic_num,
+                      const double* discrete, const cmm_grid* grid_discrete, double* out, void* stream);
+
+/* omega(x) = W_fine(X(x)) on grid_out (molly_stencil 0, 4 or 8).  Replaces
+ * k_apply_map_and_sample_from_hermite (src/simulation/cmm-simulation-kernel.cu:402-461). */
+int cmm_sample_vort(const cmm_grid* grid_map, const cmm_grid* grid_out, const cmm_grid* grid_fine,
+                    const double* chix, const double* chiy, const double* w_fine, int molly_stencil, double* out,
+                    void* stream);
+
+/* Poisson / Hermite solve: vorticity samples on grid_vort -> Hermite stream
+ * function (4 planes) on grid_psi.  Replaces the FFT part of
+ * evaluate_stream_hermite (src/simulation/cmm-simulation-host.cu:349-374).
+ * Plans and workspace live in the opaque handle. */
+typedef struct cmm_poisson cmm_poisson;
+int cmm_poisson_create(const cmm_grid* grid_vort, const cmm_grid* grid_psi, double freq_cut_psi, void* stream,
+                       cmm_poisson** out);
+int cmm_poisson_hermite(cmm_poisson* p, const double* vort, double* psi_out);
+int cmm_poisson_destroy(cmm_poisson* p);
+
+/* Tracer particles (tau = 0).  Replaces particles_advect / Particle_advect
+ * (src/numerical/cmm-particles.cu:63-87,119-276).  pos: 2*num interleaved
+ * (x, y) in device memory; psi_levels[0] = t_{n+1}, [1] = t_n, ... */
+int cmm_particles_advect(const cmm_grid* grid_psi, double* pos, int num, const double* const* psi_levels,
+                         int l_order, const double* Lp12, double dt, int time_integration_num, void* stream);
+
+/* Energy (psi Hermite), enstrophy (coarse omega) and max |omega| -> host out[3].
+ * Replaces Compute_Energy_H / Compute_Enstrophy / the w_max reduction
+ * (src/numerical/cmm-mesure.cu:30-57, cmm-simulation-host.cu:668-673).
+ * Synchronises the stream. */
+int cmm_diagnostics(const cmm_grid* grid_psi, const double* psi, const cmm_grid* grid_coarse, const double* vort,
+                    double* out3, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

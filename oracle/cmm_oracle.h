@@ -73,6 +73,9 @@ void og_sample_map_compact(const double* ChiX, const double* ChiY, double* x_y,
                            const og_grid* gmap, const og_grid* g);
 void og_apply_map_compact(const double* ChiX, const double* ChiY, double* x_y,
                           const og_grid* gmap, const og_grid* g);
+/* stack composition + initial-condition sampling on gt (stack: n maps of [X|Y] planes) */
+void og_compose_sample(const double* ChiX, const double* ChiY, const double* stack, int n, const og_grid* gm,
+                       const og_grid* gt, int ic_num, const double* discrete, const og_grid* gd, double* out);
 /* d_init_vorticity "4_nodes": src/simulation/cmm-init.cu:45-52 */
 double og_init_vorticity(double x, double y, int ic_num);
 /* k_apply_map_and_sample_from_hermite: src/simulation/cmm-simulation-kernel.cu:402-461 */

@@ -357,6 +357,22 @@ int og_set_particles(og_state* st, int i, const double* pos)
     return 0;
 }
 
+/* apply_map_stack (direction -1) + k_h_sample_from_init: cmm-simulation-host.cu:112-128,
+ * cmm-simulation-kernel.cu:342-373; stack = n maps of [X planes | Y planes] */
+void og_compose_sample(const double* ChiX, const double* ChiY, const double* stack, int n, const og_grid* gm,
+                       const og_grid* gt, int ic_num, const double* discrete, const og_grid* gd, double* out)
+{
+    double* xy = (double*)xmalloc(sizeof(double) * 2 * gt->N);
+    og_sample_map_compact(ChiX, ChiY, xy, gm, gt);
+    for (int i = n - 1; i >= 0; i--)
+        og_apply_map_compact(stack + 8 * gm->N * (size_t)i, stack + 8 * gm->N * (size_t)i + 4 * gm->N, xy, gm, gt);
+    #pragma omp parallel for schedule(static)
+    for (long In = 0; In < gt->N; ++In)
+        out[In] = discrete ? og_hermite_interpolate_2D(discrete, xy[2 * In], xy[2 * In + 1], gd)
+                           : og_init_vorticity(xy[2 * In], xy[2 * In + 1], ic_num);
+    free(xy);
+}
+
 /* translate_initial_condition_through_map_stack: cmm-simulation-host.cu:299-327 */
 static void translate_ic(og_state* st)
 {

@@ -222,3 +222,110 @@ class EulerOracle:
 
     def max_vorticity(self):
         return self.L.og_max_vorticity(self.h)
+
+
+# ---------------------------------------------------------------- kernel-level restatements
+def make_grid(n, bounds=(0.0, 6.283185307179586, 0.0, 6.283185307179586)):
+    g = OgGrid()
+    L = lib()
+    b = (C.c_double * 4)(*bounds)
+    L.og_grid_fill(C.byref(g), int(n), int(n), b)
+    return g
+
+
+def _kernel_lib():
+    L = lib()
+    if not getattr(L, "_kernels_typed", False):
+        dp = C.POINTER(C.c_double)
+        gp = C.POINTER(OgGrid)
+        L.og_grid_fill.argtypes = [gp, C.c_int, C.c_int, dp]
+        L.og_advect_map.argtypes = [dp, dp, dp, dp, dp, gp, gp, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
+                                    dp, dp, dp, dp, dp, dp]
+        L.og_map_update_coefficients.argtypes = [C.c_int, C.c_double, dp, dp, dp, dp]
+        L.og_incompressibility_check.argtypes = [gp, gp, dp, dp]
+        L.og_incompressibility_check.restype = C.c_double
+        L.og_compose_sample.argtypes = [dp, dp, dp, C.c_int, gp, gp, C.c_int, dp, gp, dp]
+        L.og_apply_map_and_sample_from_hermite.argtypes = [dp, dp, dp, dp, gp, gp, gp, C.c_int, C.c_int]
+        L.og_particle_advect.argtypes = [C.c_int, C.c_double, dp, dp, gp, C.c_int, C.c_int, dp]
+        L.og_fft_d2z.argtypes = [gp, dp, dp]
+        L.og_fft_z2d.argtypes = [gp, dp, dp]
+        L.og_normalize_h.argtypes = [dp, gp]
+        L.og_fft_grid_move.argtypes = [dp, dp, gp, gp]
+        L.og_fft_cut_off_scale_h.argtypes = [dp, gp, C.c_double]
+        L.og_fft_iLap_h.argtypes = [dp, dp, gp]
+        L.og_fourier_hermite.argtypes = [gp, dp, dp]
+        L.og_get_L_coefficient.argtypes = [dp, C.c_double, C.c_int, C.c_int, C.c_int]
+        L.og_get_L_coefficient.restype = C.c_double
+        L._kernels_typed = True
+    return L
+
+
+def advect_map(chix, chiy, psi_levels, gm, gp, dt, ep, ti, order, L1, L12):
+    """og_advect_map on contiguous numpy inputs; psi_levels is a list of 4*Np arrays."""
+    L = _kernel_lib()
+    psi = np.ascontiguousarray(np.concatenate(psi_levels))
+    outx = np.empty_like(chix)
+    outy = np.empty_like(chiy)
+    c = [np.zeros(12) for _ in range(4)]
+    L.og_map_update_coefficients(order, ep, *[_dp(a) for a in c])
+    l1 = np.array(list(L1) + [0] * 4, dtype=np.float64)
+    l12 = np.array(list(L12) + [0] * 4, dtype=np.float64)
+    L.og_advect_map(_dp(chix), _dp(chiy), _dp(outx), _dp(outy), _dp(psi), C.byref(gm), C.byref(gp), dt, ep, ti, order,
+                    len(psi_levels), _dp(l1), _dp(l12), *[_dp(a) for a in c])
+    return outx, outy
+
+
+def incompressibility(gcheck, gm, chix, chiy):
+    return _kernel_lib().og_incompressibility_check(C.byref(gcheck), C.byref(gm), _dp(chix), _dp(chiy))
+
+
+def compose_sample(chix, chiy, stack, n, gm, gt, ic_num, discrete=None, gd=None):
+    L = _kernel_lib()
+    out = np.empty(gt.N, dtype=np.float64)
+    st = np.ascontiguousarray(stack if stack is not None else np.zeros(1))
+    L.og_compose_sample(_dp(chix), _dp(chiy), _dp(st), n, C.byref(gm), C.byref(gt), ic_num,
+                        _dp(discrete) if discrete is not None else None, C.byref(gd) if gd is not None else None,
+                        _dp(out))
+    return out
+
+
+def sample_vort(chix, chiy, w_fine, gm, gout, gf, molly=0):
+    L = _kernel_lib()
+    out = np.empty(gout.N, dtype=np.float64)
+    L.og_apply_map_and_sample_from_hermite(_dp(chix), _dp(chiy), _dp(out), _dp(w_fine), C.byref(gm), C.byref(gout),
+                                           C.byref(gf), molly, 0)
+    return out
+
+
+def particle_advect(pos, psi_levels, g, dt, ti, Lp12):
+    L = _kernel_lib()
+    p = np.ascontiguousarray(pos, dtype=np.float64).copy()
+    psi = np.ascontiguousarray(np.concatenate(psi_levels))
+    lp = np.array(list(Lp12) + [0] * 4, dtype=np.float64)
+    L.og_particle_advect(len(p) // 2, dt, _dp(p), _dp(psi), C.byref(g), ti, len(psi_levels), _dp(lp))
+    return p
+
+
+def poisson_hermite(vort, gv, gp, freq):
+    """evaluate_stream_hermite's FFT part on the CPU: vort samples -> 4 Hermite planes."""
+    L = _kernel_lib()
+    cv = np.empty(2 * gv.Nfft)
+    cp = np.empty(2 * max(gv.Nfft, gp.Nfft))
+    v = np.ascontiguousarray(vort, dtype=np.float64)
+    L.og_fft_d2z(C.byref(gv), _dp(v), _dp(cv))
+    L.og_normalize_h(_dp(cv), C.byref(gv))
+    if gv.NX != gp.NX:
+        L.og_fft_grid_move(_dp(cv), _dp(cp), C.byref(gp), C.byref(gv))
+    else:
+        cp[: 2 * gv.Nfft] = cv
+    L.og_fft_cut_off_scale_h(_dp(cp), C.byref(gp), freq)
+    c2 = np.empty_like(cp)
+    L.og_fft_iLap_h(_dp(cp), _dp(c2), C.byref(gp))
+    out = np.empty(4 * gp.N)
+    L.og_fourier_hermite(C.byref(gp), _dp(c2), _dp(out))
+    return out
+
+
+def lagrange(t, t_next, loop_ctr, i_point, l_order):
+    tt = np.ascontiguousarray(t, dtype=np.float64)
+    return _kernel_lib().og_get_L_coefficient(_dp(tt), t_next, loop_ctr, i_point, l_order)

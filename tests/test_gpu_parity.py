@@ -1,0 +1,243 @@
+"""GPU parity tests: the sm_103a kernels and the full loop, called through the
+C-ABI, against the CPU oracle (same inputs, FP64) and against the reference's
+own golden monitoring series.
+
+Tolerances (FP64; rounding order differs from the reference and the oracle):
+  * kernel outputs: relative L-infinity <= 1e-12 of the array's magnitude;
+  * maps are compared plane by plane in units of their conditioning
+    (map_err below: the slope planes are finite differences over epsilon);
+  * full runs: psi, omega and map fields within 1e-12 of the oracle after the
+    Lagrange initialisation and the first steps, and within 1e-10 after a
+    whole C1 run (64 steps incl. a remap);
+  * golden statistics: scaled error <= 1e-9 (the reference harness itself
+    allows 1e-10..1e-12 across GPUs, tests/test_functions.py:67-70);
+  * E_inc = |1 - det| is compared absolutely (<= 1e-10).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+import refloop
+from goldens import DebugRecorder, compare_series, goldens
+from product import cmm, read_monitoring
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TWO_PI = 6.283185307179586
+
+
+def rel_linf(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def map_err(a, b, eps=1e-3):
+    """Relative L-infinity of a Hermite map [X, X_x, X_y, X_xy] in units of its
+    conditioning: the GALS update forms the slope planes as finite differences
+    of footpoints over eps (X_x, X_y ~ sum c/eps * x_f, X_xy ~ sum c/eps^2 * x_f,
+    src/simulation/cmm-simulation-host.cu:84-89), so rounding of the footpoint
+    positions (relative to max|X|) is amplified by 1/eps and 1/eps^2 there."""
+    a = np.asarray(a, dtype=np.float64).reshape(4, -1)
+    b = np.asarray(b, dtype=np.float64).reshape(4, -1)
+    scale = max(np.max(np.abs(b[0])), 1e-300)
+    amp = (1.0, 1.0 / eps, 1.0 / eps, 1.0 / eps ** 2)
+    return max(float(np.max(np.abs(a[k] - b[k]))) / (scale * amp[k]) for k in range(4))
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+SMALL = dict(grid_coarse=32, grid_fine=128, grid_psi=64, grid_vort=128, bounds=[0, TWO_PI, 0, TWO_PI], dt=1.0 / 16,
+             time_integration_num=30, lagrange_order=3, lagrange_init_higher_order=1, map_update_order_num=1,
+             map_epsilon=1e-3, incomp_threshold=5e-4, skip_remapping=0, molly_stencil=0, freq_cut_psi=21.0,
+             initial_condition_num=0, max_maps=16, particles=[])
+
+
+@pytest.fixture(scope="module")
+def state():
+    """An oracle state with a deformed map, a 3-level psi history and one stacked map."""
+    o = O.EulerOracle(SMALL)
+    o.init()
+    stack = []
+    for _ in range(6):
+        rc, e, remapped = o.step(SMALL["dt"])
+    return o
+
+
+def test_advect_kernel_matches_oracle(state):
+    m = cmm()
+    o = state
+    gc, gp = o.grid(0), o.grid(2)
+    X, Y = o.chix(), o.chiy()
+    psi = o.psi(levels=3).reshape(3, -1)
+    t = np.array([0.0, 1 / 16, 2 / 16, 3 / 16])
+    L1 = [O.lagrange(t, t[3], 2, i, 3) for i in range(3)]
+    L12 = [O.lagrange(t, t[2] + 1 / 32, 2, i, 3) for i in range(3)]
+    for ti, lv, order in ((30, 3, 1), (21, 2, 1), (10, 1, 1), (30, 3, 0), (30, 3, 2)):
+        ox, oy = O.advect_map(X, Y, [psi[l] for l in range(lv)], gc, gp, 1 / 16, 1e-3, ti, order, L1[:lv], L12[:lv])
+        dX, dY = dev(X), dev(Y)
+        outx, outy = torch.empty_like(dX), torch.empty_like(dY)
+        levels = [dev(psi[l]) for l in range(lv)]
+        m.advect_map(m.grid(gc.NX), m.grid(gp.NX), dX, dY, outx, outy, levels, L1[:lv], L12[:lv], 1 / 16, 1e-3, ti, order)
+        assert map_err(host(outx), ox) < 1e-12, (ti, order)
+        assert map_err(host(outy), oy) < 1e-12, (ti, order)
+
+
+def test_incompressibility_kernel_matches_oracle(state):
+    m = cmm()
+    o = state
+    gc, gf = o.grid(0), o.grid(1)
+    ref = O.incompressibility(gf, gc, o.chix(), o.chiy())
+    res = torch.zeros(1, dtype=torch.float64, device="cuda")
+    m.incomp_max(m.grid(gf.NX), m.grid(gc.NX), dev(o.chix()), dev(o.chiy()), res)
+    assert abs(host(res)[0] - ref) < 1e-12
+    assert ref > 0
+
+
+def test_compose_and_sample_kernels_match_oracle(state):
+    m = cmm()
+    o = state
+    gc, gf = o.grid(0), o.grid(1)
+    X, Y = o.chix(), o.chiy()
+    # a two-map stack built from shifted copies of the current map
+    s1 = np.concatenate([X, Y])
+    X2 = X.copy(); X2[:gc.N] += 0.01 * np.sin(np.arange(gc.N))
+    s2 = np.concatenate([X2, Y])
+    stack = np.concatenate([s1, s2])
+    for n in (0, 1, 2):
+        ref = O.compose_sample(X, Y, stack, n, gc, gf, 0)
+        out = torch.empty(gf.N, dtype=torch.float64, device="cuda")
+        m.compose_stack(m.grid(gc.NX), m.grid(gf.NX), dev(X), dev(Y), dev(stack), n, 0, out)
+        assert rel_linf(host(out), ref) < 1e-12, n
+    wf = o.vort_fine()
+    for molly in (0, 4, 8):
+        ref = O.sample_vort(X, Y, wf, gc, gf, gf, molly)
+        out = torch.empty(gf.N, dtype=torch.float64, device="cuda")
+        m.sample_vort(m.grid(gc.NX), m.grid(gf.NX), m.grid(gf.NX), dev(X), dev(Y), dev(wf), out, molly)
+        assert rel_linf(host(out), ref) < 1e-12, molly
+
+
+def test_poisson_kernel_matches_oracle(state):
+    m = cmm()
+    o = state
+    gv, gp = o.grid(3), o.grid(2)
+    vort = O.sample_vort(o.chix(), o.chiy(), o.vort_fine(), o.grid(0), gv, o.grid(1), 0)
+    ref = O.poisson_hermite(vort, gv, gp, SMALL["freq_cut_psi"])
+    out = torch.empty(4 * gp.N, dtype=torch.float64, device="cuda")
+    p = m.Poisson(m.grid(gv.NX), m.grid(gp.NX), SMALL["freq_cut_psi"])
+    p(dev(vort), out)
+    got = host(out)
+    for k in range(4):
+        assert rel_linf(got[k * gp.N:(k + 1) * gp.N], ref[k * gp.N:(k + 1) * gp.N]) < 1e-12, k
+    p.close()
+
+
+def test_particle_kernel_matches_oracle(state):
+    m = cmm()
+    o = state
+    gp = o.grid(2)
+    psi = o.psi(levels=3).reshape(3, -1)
+    rng = np.random.default_rng(0)
+    pos = rng.uniform(0, TWO_PI, 2 * 777)
+    t = np.array([0.0, 1 / 16, 2 / 16, 3 / 16])
+    Lp12 = [O.lagrange(t, t[2] + 1 / 32, 3, i, 3) for i in range(3)]
+    for ti, lv in ((30, 3), (20, 2), (10, 2)):
+        ref = O.particle_advect(pos, [psi[l] for l in range(lv)], gp, 1 / 16, ti, Lp12[:lv])
+        d = dev(pos)
+        m.particles_advect(m.grid(gp.NX), d, 777, [dev(psi[l]) for l in range(lv)], Lp12[:lv], 1 / 16, ti)
+        assert rel_linf(host(d), ref) < 1e-12, ti
+
+
+def _c1_args(work, steps=None, final_time=1.0):
+    # C1: 4_nodes, coarse 128, fine = vort 512, psi 256, dt = 1/64, T = 1, remap at 1e-4
+    return ["workspace=%s/" % work, "sim_name=c1", "simulation_type=cmm_euler_2d", "initial_condition=4_nodes",
+            "grid_coarse=128", "grid_fine=512", "grid_vort=512", "grid_psi=256", "set_dt_by_steps=1",
+            "steps_per_sec=64", "final_time=%g" % final_time, "time_integration=RK3", "map_update_order=4th",
+            "map_epsilon=0.001", "incomp_threshold=0.0001", "skip_remapping=0", "molly_stencil=0",
+            "lagrange_init_higher_order=1", "lagrange_override=-1", "freq_cut_psi=128", "particles_advected_num=0",
+            "save_sample_num=0", "save_zoom_num=0", "forward_map=0", "mem_RAM_CPU_remaps=1000",
+            "save_computational_num=0", "verbose=0"]
+
+
+def _c1_oracle():
+    cfg = dict(grid_coarse=128, grid_fine=512, grid_psi=256, grid_vort=512, bounds=[0, TWO_PI, 0, TWO_PI],
+               dt=1.0 / 64, time_integration_num=30, lagrange_order=3, lagrange_init_higher_order=1,
+               map_update_order_num=1, map_epsilon=1e-3, incomp_threshold=1e-4, skip_remapping=0, molly_stencil=0,
+               freq_cut_psi=128.0, initial_condition_num=0, max_maps=int(1000 / (8 * 128 * 128 * 8 / 1e6)),
+               particles=[])
+    return O.EulerOracle(cfg)
+
+
+def test_c1_initial_state_and_first_steps_match_oracle(tmp_path):
+    m = cmm()
+    sim = m.Simulation(_c1_args(tmp_path))
+    sim.init()
+    o = _c1_oracle()
+    o.init()
+    psi_all = sim.field("Stream_function_Psi_H_psi_all")
+    assert rel_linf(psi_all, o.psi(levels=3)) < 1e-12
+    assert rel_linf(sim.field("Vorticity_W_fine_H"), o.vort_fine()) < 1e-12
+    for k in range(3):
+        sim.step(1)
+        _, e, _ = o.step(1.0 / 64)
+        assert abs(sim.scalar("e_inc") - e) < 1e-12
+    assert map_err(sim.field("Map_ChiX_H_coarse"), o.chix()) < 1e-12
+    assert map_err(sim.field("Map_ChiY_H_coarse"), o.chiy()) < 1e-12
+    for name, ref in (("Stream_function_Psi_H_psi", o.psi()), ("Vorticity_W_coarse", o.vort())):
+        assert rel_linf(sim.field(name), ref) < 1e-12, name
+
+
+def test_c1_full_run_matches_oracle_field_by_field(tmp_path):
+    m = cmm()
+    sim = m.Simulation(_c1_args(tmp_path))
+    sim.init()
+    o = _c1_oracle()
+    o.init()
+    maps_gpu, maps_cpu = [], []
+    while True:
+        rc = sim.step(1)
+        if rc == 1:
+            break
+        _, e, r = o.step(1.0 / 64)
+        assert abs(sim.scalar("e_inc") - e) < 1e-10
+        maps_gpu.append(int(sim.scalar("map_counter")))
+        maps_cpu.append(o.map_count())
+    assert len(maps_gpu) == 64
+    assert maps_gpu == maps_cpu and maps_gpu[-1] >= 1
+    assert map_err(sim.field("Map_ChiX_H_coarse"), o.chix()) < 1e-10
+    assert map_err(sim.field("Map_ChiY_H_coarse"), o.chiy()) < 1e-10
+    for name, ref in (("Stream_function_Psi_H_psi", o.psi()), ("Vorticity_W_coarse", o.vort()),
+                      ("Vorticity_W_fine_H", o.vort_fine())):
+        assert rel_linf(sim.field(name), ref) < 1e-10, name
+    for name, ref in (("energy", o.energy()), ("enstrophy", o.enstrophy()), ("palinstrophy", o.palinstrophy())):
+        assert abs(sim.scalar(name) - ref) <= 1e-11 * abs(ref), name
+
+
+@pytest.mark.parametrize("name", ["one_step", "remap_11b"])
+def test_reference_goldens_through_the_cli_interface(tmp_path, name):
+    """The product, configured by the reference's own param file, writes the
+    reference's monitoring files; they match the golden series, including the
+    fluid-particle statistics (cuRAND initial positions, RK3 tracers)."""
+    m = cmm()
+    g = goldens()[name]
+    pf = tmp_path / "params.txt"
+    pf.write_text(g["params_in"])
+    sim = m.Simulation(["param_file=%s" % pf, "workspace=%s/" % tmp_path])
+    sim.init()
+    sim.run()
+    run_dir = os.path.join(str(tmp_path), "data", sim.file_name())
+    ours = read_monitoring(run_dir)
+    keys = [k for k in g["files"] if "_256" not in k and "Scalar" not in k and "P02" not in k and "U02" not in k]
+    worst, fails = compare_series(ours, g["files"], keys, 1e-9)
+    assert not fails, fails
+    assert ours["Map_counter"] == g["files"]["Map_counter"]

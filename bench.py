@@ -200,6 +200,108 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def measure_form(m, torch, pf, ic, precision, args, world, clocks=None, profile=True):
+    """Init one simulation of the workload in `precision`, run W warm-up steps,
+    time exactly K steps with CUDA events on the library stream, then
+    (optionally) profile a few more steps phase by phase."""
+    stream = torch.cuda.Stream()
+    sim = m.Simulation(["param_file=" + pf, "precision=" + precision], stream=stream.cuda_stream)
+    sim.set_initial_discrete(ic)
+    sim.init()
+    for _ in range(args.warmup):
+        sim.step(1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    l0, maps0 = sim.scalar("kernel_launches"), sim.scalar("map_counter")
+    ctx = clocks if clocks is not None else ClockSampler()
+    with ctx:
+        e0.record(stream)
+        for _ in range(args.steps):
+            sim.step(1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+        ms = float(t.item())
+    out = {"ms": ms, "value": world * args.steps / (ms / 1000.0), "launches": int(sim.scalar("kernel_launches") - l0),
+           "remaps": int(sim.scalar("map_counter") - maps0), "time": sim.scalar("time"),
+           "enstrophy": sim.scalar("enstrophy"), "energy": sim.scalar("energy"),
+           "palinstrophy": sim.scalar("palinstrophy"), "maps": int(sim.scalar("map_counter"))}
+    if profile:
+        sim.set_profiling(True)
+        for _ in range(max(3, min(args.steps, 20))):
+            sim.step(1)
+        out["phases"] = {ph: {"ms_total": sim.scalar("prof_%s_ms" % ph), "launches": int(sim.scalar("prof_%s_count" % ph))}
+                         for ph in ("advect", "incomp", "remap", "psi", "coarse", "particles", "save")}
+    sim.close()
+    return out
+
+
+def full_run(m, torch, pf, ic, precision, every=64, final_time=10.0):
+    """Run the workload to its final time (T = 10, 2560 steps with every remap)
+    and record (t, enstrophy, energy, maps) every `every` steps (0.25 time units)."""
+    stream = torch.cuda.Stream()
+    sim = m.Simulation(["param_file=" + pf, "precision=" + precision, "final_time=%g" % final_time],
+                       stream=stream.cuda_stream)
+    sim.set_initial_discrete(ic)
+    sim.init()
+    rec = [(sim.scalar("time"), sim.scalar("enstrophy"), sim.scalar("energy"), 0)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    n = 0
+    steps_only = 0.0
+    while True:
+        ts = time.perf_counter()
+        rc = sim.step(1)
+        if rc == 1:
+            break
+        n += 1
+        if n % every == 0:
+            torch.cuda.synchronize()
+            steps_only += time.perf_counter() - ts
+            rec.append((sim.scalar("time"), sim.scalar("enstrophy"), sim.scalar("energy"), int(sim.scalar("map_counter"))))
+        else:
+            steps_only += time.perf_counter() - ts
+        if rc == m.CMM_ERR_SATURATED:
+            break
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    maps = int(sim.scalar("map_counter"))
+    sim.close()
+    return {"steps": n, "wall_s": wall, "steps_per_s": n / wall, "maps": maps, "series": rec}
+
+
+def run_t10(args):
+    """Both forms to T = 10: the metric's enstrophy error over the whole run."""
+    import __graft_entry__ as ge
+    ge.build()
+    m = ge.package()
+    import torch
+    ic = initial_vorticity(WORKLOAD["grid_fine"], WORKLOAD["seed"], WORKLOAD["k0"])
+    work = tempfile.mkdtemp(prefix="cmm_t10_")
+    cli, recs = sim_args(work, "mixed", particles=args.t10_particles)
+    pf = os.path.join(work, "params.txt")
+    write_param_file(pf, cli, recs)
+    mixed = full_run(m, torch, pf, ic, "mixed", final_time=args.t10_final)
+    plain = full_run(m, torch, pf, ic, "fp64", final_time=args.t10_final)
+    zs = [(a[0], abs(a[1] - b[1]) / abs(b[1]), abs(a[2] - b[2]) / abs(b[2]))
+          for a, b in zip(mixed["series"], plain["series"])]
+    out = {"validation": "chosen (mixed) vs plain FP64 over the whole run", "final_time": args.t10_final,
+           "workload": "euler2d-turbulence coarse512 fine2048 psi1024 dt1/256, %d tracers" % args.t10_particles,
+           "mixed": {k: mixed[k] for k in ("steps", "wall_s", "steps_per_s", "maps")},
+           "plain_fp64": {k: plain[k] for k in ("steps", "wall_s", "steps_per_s", "maps")},
+           "speedup": mixed["steps_per_s"] / plain["steps_per_s"],
+           "max_enstrophy_rel_err": max(z[1] for z in zs), "max_energy_rel_err": max(z[2] for z in zs),
+           "enstrophy_series": [(round(z[0], 4), z[1]) for z in zs]}
+    print(json.dumps(out))
+    shutil.rmtree(work, ignore_errors=True)
+
+
 def run_ours(args):
     import __graft_entry__ as ge
     ge.build()
@@ -219,54 +321,16 @@ def run_ours(args):
     pf = os.path.join(work, "params.txt")
     write_param_file(pf, cli, recs)
 
-    stream = torch.cuda.Stream()
-    sim = m.Simulation(["param_file=" + pf], stream=stream.cuda_stream)
-    sim.set_initial_discrete(ic)
-    sim.init()
-    for _ in range(args.warmup):
-        sim.step(1)
-
-    # ---- value: K steps, state resident in HBM, CUDA events on the library stream
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    l0 = sim.scalar("kernel_launches")
-    maps0 = sim.scalar("map_counter")
-    with ClockSampler() as clocks:
-        e0.record(stream)
-        for _ in range(args.steps):
-            sim.step(1)
-        e1.record(stream)
-        torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.barrier()
-        ms = float(t.item())
-    launches = int(sim.scalar("kernel_launches") - l0)
-    remaps = int(sim.scalar("map_counter") - maps0)
-    ms_per_step = ms / args.steps
-    value = world * args.steps / (ms / 1000.0)
-
-    # ---- profiled pass: per-phase CUDA-event times of the same steps
-    sim.set_profiling(True)
-    prof_steps = max(3, min(args.steps, 20))
-    for _ in range(prof_steps):
-        sim.step(1)
-    phases = {}
-    for ph in ("advect", "incomp", "remap", "psi", "coarse", "particles", "save"):
-        n = sim.scalar("prof_%s_count" % ph)
-        phases[ph] = {"ms_total": sim.scalar("prof_%s_ms" % ph), "launches": int(n)}
-    sim.close()
-
+    # ---- the chosen form: value, clocks, phases
+    clocks = ClockSampler()
+    chosen = measure_form(m, torch, pf, ic, args.precision, args, world, clocks=clocks)
+    # ---- plain FP64 over the same warm-up + K steps from the same state
+    plain = None
+    if args.precision != "fp64" and not args.no_plain:
+        plain = measure_form(m, torch, pf, ic, "fp64", args, world, profile=False)
     # ---- e2e through the C-ABI with host buffers
-    if args.no_e2e:
-        e2e, e2e_line = None, None
-    else:
-        e2e, e2e_line = _e2e(m, torch, ic, pf, args, world)
-    _report(args, world, rank, value, ms_per_step, launches, remaps, clocks, phases, e2e_line, ic)
+    e2e_line = None if args.no_e2e else _e2e(m, torch, ic, pf, args, world)
+    _report(args, world, rank, chosen, plain, clocks, e2e_line, ic)
     shutil.rmtree(work, ignore_errors=True)
 
 
@@ -275,7 +339,7 @@ def _e2e(m, torch, ic, pf, args, world):
     stream2 = torch.cuda.Stream()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    sim2 = m.Simulation(["param_file=" + pf], stream=stream2.cuda_stream)
+    sim2 = m.Simulation(["param_file=" + pf, "precision=" + args.precision], stream=stream2.cuda_stream)
     sim2.set_initial_discrete(ic_pinned.numpy())
     sim2.init()
     d2h = 0
@@ -289,26 +353,52 @@ def _e2e(m, torch, ic, pf, args, world):
     d2h += psi.nbytes
     sim2.close()
     e2e = world * args.steps / e2e_s
-    return e2e, {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": ic.nbytes / args.steps,
-                 "d2h_bytes_per_step": d2h / args.steps,
-                 "includes": "IC upload + init + every step + final psi readback"}
+    return {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": ic.nbytes / args.steps,
+            "d2h_bytes_per_step": d2h / args.steps,
+            "includes": "IC upload + init (Lagrange history) + every step + final psi readback"}
 
 
-def _report(args, world, rank, value, ms_per_step, launches, remaps, clocks, phases, e2e_line, ic):
-    # ---- roofline of the dominant kernel (map advection, FP64)
-    adv = phases["advect"]
-    adv_ms = adv["ms_total"] / max(1, adv["launches"])
-    bytes_, flops = advect_model(WORKLOAD)
+def phase_models(w, precision):
+    """Algorithmic (compulsory) HBM bytes of each loop phase per step, and the
+    FP64 flops of the plain advection (SURVEY 8d conventions)."""
+    Nc, Nf, Np, Nv, L = w["grid_coarse"] ** 2, w["grid_fine"] ** 2, w["grid_psi"] ** 2, w["grid_vort"] ** 2, 3
+    P = w["particles"]
+    if precision == "fp64":
+        b = {"advect": 8 * (16 * Nc + 4 * L * Np), "incomp": 8 * 8 * Nc,
+             "psi": 8 * (8 * Nc + 4 * Nf) + 8 * Nv + 2 * 16 * (Nv // 2 + 1) * w["grid_vort"] + 4 * 8 * Np,
+             "coarse": 8 * (8 * Nc + 4 * Nf) + 8 * Nc, "particles": 32 * P + 8 * 4 * L * Np}
+    else:
+        # FP32 map nodes 32 B, FP32 Hermite nodes 16 B
+        b = {"advect": 32 * 2 * Nc + 16 * L * Np, "incomp": 32 * Nc,
+             "psi": 32 * Nc + 16 * Nf + 4 * Nv + 2 * 8 * (Nv // 2 + 1) * w["grid_vort"] + 16 * Np,
+             "coarse": 32 * Nc + 16 * Nf + 8 * Nc, "particles": 32 * P + 16 * L * Np}
+    flops = 8 * (304 + 304 + 176 + 120 + 30) * Nc + 128 * Nc
+    return b, flops
+
+
+def _report(args, world, rank, chosen, plain, clocks, e2e_line, ic):
+    phases = chosen["phases"]
+    per = {k: v["ms_total"] / max(1, v["launches"]) for k, v in phases.items() if v["launches"]}
+    models, flops = phase_models(WORKLOAD, args.precision)
     peak, peak_kind = load_peaks()
-    achieved = bytes_ / (adv_ms / 1000.0) / 1e9
-    roof = {"kernel": "k_advect (FP64 GALS map advection)", "bound": "hbm", "achieved": achieved, "peak": peak,
+    # dominant phase of the step
+    dom = max((k for k in per if k in models), key=lambda k: per[k])
+    ms = per[dom]
+    achieved = models[dom] / (ms / 1000.0) / 1e9
+    kernels = {"advect": "k_advect (GALS map advection)", "incomp": "k_incomp (det grad X, max)",
+               "psi": "psi solve (k_sample + FFT + k_spec_psi)", "coarse": "k_sample (coarse omega)",
+               "particles": "k_particles (RK3 tracers)"}
+    roof = {"kernel": kernels.get(dom, dom), "phase": dom, "bound": "hbm", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "peak_source": "of " + peak_kind, "traffic": None,
-            "ms_per_launch": adv_ms,
-            "fp64": {"achieved_tflops": flops / (adv_ms / 1000.0) / 1e12, "peak_tflops": FP64_PEAK_TFLOPS,
-                     "frac": flops / (adv_ms / 1000.0) / 1e12 / FP64_PEAK_TFLOPS,
-                     "note": "the plain FP64 form is bound by GB300's FP64 issue rate, not HBM"}}
+            "ms_per_launch": ms, "algorithmic_bytes": models[dom],
+            "phases": {k: {"ms": per[k], "GBps": models[k] / (per[k] / 1000.0) / 1e9,
+                           "frac": models[k] / (per[k] / 1000.0) / 1e9 / peak} for k in per if k in models}}
+    if args.precision == "fp64":
+        adv = per.get("advect", 1.0)
+        roof["fp64"] = {"achieved_tflops": flops / (adv / 1000.0) / 1e12, "peak_tflops": FP64_PEAK_TFLOPS,
+                        "frac": flops / (adv / 1000.0) / 1e12 / FP64_PEAK_TFLOPS,
+                        "note": "the plain FP64 form is bound by GB300's FP64 issue rate, not HBM"}
 
-    # ---- CPU baseline (oracle) on a bounded sample, rank 0 only
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -318,17 +408,26 @@ def _report(args, world, rank, value, ms_per_step, launches, remaps, clocks, pha
                "sample": "%d full workload steps after the oracle's Lagrange initialisation (%.1f s)" % (n, secs)}
     if rank != 0:
         return
-    line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+    comparison = None
+    if plain is not None:
+        comparison = {"plain_fp64_value": plain["value"], "plain_fp64_ms_per_step": plain["ms"] / args.steps,
+                      "speedup_vs_plain_fp64": chosen["value"] / plain["value"],
+                      "time": chosen["time"], "maps_chosen": chosen["maps"], "maps_plain": plain["maps"],
+                      "enstrophy_rel_err": abs(chosen["enstrophy"] - plain["enstrophy"]) / abs(plain["enstrophy"]),
+                      "energy_rel_err": abs(chosen["energy"] - plain["energy"]) / abs(plain["energy"]),
+                      "palinstrophy_rel_err": abs(chosen["palinstrophy"] - plain["palinstrophy"]) / abs(plain["palinstrophy"])}
+    form = {"fp64": "plain FP64", "mixed": "mixed: FP32 displacement maps + FP32 Hermite psi/omega, FP64 "
+                                           "composition, FP64 det deviation, FP64 diagnostics"}.get(args.precision, args.precision)
+    line = {"metric": METRIC, "value": chosen["value"], "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": chosen["ms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": "synthetic",
             "config": {"workload": "euler2d-turbulence coarse512 fine2048 psi1024 dt1/256 1e6 tracers",
-                       "form": "plain FP64" if args.precision == "fp64" else args.precision,
-                       "remaps_in_timed_region": remaps,
-                       "l2": "working set per step > 129 MB L2 (psi levels 100 MB + fine vorticity 134 MB)",
+                       "form": form, "remaps_in_timed_region": chosen["remaps"],
+                       "l2": "working set per step > 129 MB L2 (psi levels, fine vorticity, map)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
-            "clocks": clocks.summary(), "gpu_launches": launches, "e2e": e2e_line,
-            "roofline": roof, "phases_ms_per_step": {k: v["ms_total"] / max(1, v["launches"]) for k, v in phases.items()},
-            "cpu_baseline": cpu}
+            "clocks": clocks.summary(), "gpu_launches": chosen["launches"], "e2e": e2e_line,
+            "vs_plain_fp64": comparison, "roofline": roof, "cpu_baseline": cpu}
     print(json.dumps(line))
 
 
@@ -338,12 +437,18 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--t10", action="store_true", help="run both forms to the final time and report the enstrophy error")
+    ap.add_argument("--t10-final", type=float, default=10.0)
+    ap.add_argument("--t10-particles", type=int, default=WORKLOAD["particles"])
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.t10:
+        run_t10(args)
     else:
         run_ours(args)
 

@@ -3,6 +3,7 @@
 // and sampling of the fine vorticity through the current map.
 #include <cuda_runtime.h>
 
+#include "init_conditions.cuh"
 #include "kernels.hpp"
 
 namespace cmm {
@@ -201,119 +202,6 @@ cudaError_t launch_incomp(const Grid& gc, const Grid& gm, const double* X, const
     unsigned blocks = (unsigned)(need < 152 * 16 ? need : 152 * 16);
     k_incomp<<<blocks, threads, 0, s>>>(gc, gm, X, Y, reinterpret_cast<unsigned long long*>(d_result));
     return cudaGetLastError();
-}
-
-// ---------------------------------------------------------------------------
-// analytic initial conditions (d_init_vorticity / d_init_scalar,
-// src/simulation/cmm-init.cu:30-241, 253-298)
-// ---------------------------------------------------------------------------
-__device__ double init_vorticity(double x, double y, int ic, const double* __restrict__ prm,
-                                 const double* __restrict__ rnd)
-{
-    const double PI = kTwoPi / 2;
-    switch (ic) {
-        case 0: {  // 4_nodes
-            x -= floor(x / kTwoPi) * kTwoPi;
-            y -= floor(y / kTwoPi) * kTwoPi;
-            return cos(x) + cos(y) + 0.6 * cos(2 * x) + 0.2 * cos(3 * x);
-        }
-        case 1: {  // quadropole
-            double r = 0;
-            for (int iy = -2; iy <= 2; iy++)
-                for (int ix = -2; ix <= 2; ix++) {
-                    double dx = x - PI / 2 + ix * 2 * PI, dy = y - PI / 2 + iy * 2 * PI;
-                    double A = 0.6258473, s = 0.5;
-                    double B = A / (s * s * s * s) * (dx * dy) * (dx * dx + dy * dy - 6 * s * s);
-                    double D = (dx * dx + dy * dy) / (2 * s * s);
-                    r += B * exp(-D);
-                }
-            return r;
-        }
-        case 2: {  // one_vortex
-            double sig = kTwoPi * 0.125;
-            return 1.0 / (kTwoPi * sig * sig) * exp(-((x - PI) * (x - PI) + (y - PI) * (y - PI)) / (2 * sig * sig));
-        }
-        case 3: case 4: {  // two_votices / three_vortices
-            double r = 0, LX = PI / 2, LY = PI / (2.0 * sqrt(2.0));
-            for (int iy = -1; iy <= 1; iy++)
-                for (int ix = -1; ix <= 1; ix++) {
-                    double xs = x + kTwoPi * ix, ys = y + kTwoPi * iy;
-                    double env = sin(0.5 * xs) * sin(0.5 * xs) * sin(0.5 * (ys + kTwoPi * iy)) * sin(0.5 * (ys + kTwoPi * iy));
-                    double e;
-                    if (ic == 3)
-                        e = exp(-((xs - PI) * (xs - PI) + (ys - 0.33 * kTwoPi) * (ys - 0.33 * kTwoPi)) * 5) +
-                            exp(-((xs - PI) * (xs - PI) + (ys - 0.67 * kTwoPi) * (ys - 0.67 * kTwoPi)) * 5);
-                    else
-                        e = exp(-((xs - PI - LX) * (xs - PI - LX) + (ys - PI) * (ys - PI)) * 5) +
-                            exp(-((xs - PI + LX) * (xs - PI + LX) + (ys - PI) * (ys - PI)) * 5) -
-                            exp(-((xs - PI + LX) * (xs - PI + LX) + (ys - PI - LY) * (ys - PI - LY)) * 5);
-                    r += env * e;
-                }
-            return r;
-        }
-        case 5:  // single_shear_layer
-            return (1 + 0.01 * cos(2 * x)) * exp(-50.0 * (y - PI) * (y - PI));
-        case 6: {  // tanh_shear_layer
-            double freq = 2, d = 14 * freq / kTwoPi;
-            double c = exp(-d * (y - PI)) + exp(d * (y - PI));
-            return 5.0 * (1 + 0.01 * cos(freq * x)) * 4 / c / c;
-        }
-        case 8: {  // gaussian_blobs (random offsets from a host-drawn table)
-            x -= floor(x / kTwoPi) * kTwoPi;
-            y -= floor(y / kTwoPi) * kTwoPi;
-            const int NB = 10, border = 2;
-            double sig = kTwoPi * 0.01, off = kTwoPi * 0.005, r = 0;
-            int dir = 1;
-            for (int mx = -border; mx < 2 * NB + border; mx++) {
-                for (int my = -border; my < 2 * NB + border; my++) {
-                    int bn = (int)((mx - floor(mx / (double)(NB * 2)) * NB * 2) +
-                                   (my - floor(my / (double)(NB * 2)) * NB * 2) * NB * 2);
-                    double ex = x - (mx + 0.5) * kTwoPi / (2 * NB) + rnd[bn] * off;
-                    double ey = y - (my + 0.5) * kTwoPi / (2 * NB) + rnd[bn + NB * NB * 4] * off;
-                    r += dir / (kTwoPi * sig * sig) * exp(-(ex * ex + ey * ey) / (2 * sig * sig));
-                    dir = -dir;
-                }
-                dir = -dir;
-            }
-            return r;
-        }
-        case 9: {  // shielded_vortex
-            double nu = 2e-1, xr = PI - x, yr = PI - y;
-            return 1 / (2 * nu * nu * nu) * (4 * nu - xr * xr - yr * yr) * exp(-(xr * xr + yr * yr) / (4 * nu));
-        }
-        case 10: {  // two_cosine
-            x -= floor(x / kTwoPi) * kTwoPi;
-            y -= floor(y / kTwoPi) * kTwoPi;
-            return cos(x) * cos(y);
-        }
-        case 11: {  // vortex_sheets
-            double d = 1 / sqrt(prm[0]);
-            double q = y - PI - sin(x) / 2.0;
-            return exp(-q * q / (2 * d * d)) / sqrt(2 * PI) / d;
-        }
-        default: return 0.0;
-    }
-}
-
-__device__ double init_scalar(double x, double y, int sn)
-{
-    const double PI = kTwoPi / 2;
-    switch (sn) {
-        case 0: {  // rectangle
-            x -= floor(x / kTwoPi) * kTwoPi;
-            y -= floor(y / kTwoPi) * kTwoPi;
-            return (x > PI - PI && x < PI + PI && y > PI / 2.0 - PI / 2.0 && y < PI / 2.0 + PI / 2.0) ? 1.0 : 0.0;
-        }
-        case 1: {  // gaussian
-            double v = PI / 4.0;
-            return 1.0 / (kTwoPi * v * v) * exp(-((x - PI) * (x - PI) / (2 * v * v) + (y - PI) * (y - PI) / (2 * v * v)));
-        }
-        case 2: {  // circular_ring
-            double r = PI / 2.0, w = r / 8.0, q = (x - PI) * (x - PI) + (y - PI) * (y - PI);
-            return (tanh(10.0 * (q - (r + w) * (r + w))) - tanh(10.0 * (q - (r - w) * (r - w)))) / 2.0;
-        }
-        default: return 0.0;
-    }
 }
 
 // ---------------------------------------------------------------------------

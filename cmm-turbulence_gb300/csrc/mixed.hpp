@@ -1,0 +1,52 @@
+// mixed.hpp -- launchers of the mixed-precision form (FP32 displacement maps,
+// FP32 Hermite stream function / fine vorticity, FP64 composition, FP64
+// determinant deviation and FP64 diagnostic sums).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "kernels.hpp"
+
+namespace cmm {
+
+// Map node layout: two float4 per node,
+//   a = (dX, dY, dX_x, dY_x), b = (dX_y, dY_y, dX_xy, dY_xy),  d = X - x, dX_x = X_x - 1, dY_y = Y_y - 1.
+struct AdvectMArgs {
+    Grid gm, gp;
+    const float4* map;      // 2*Nc float4
+    float4* out;            // 2*Nc float4
+    const float4* psiA;     // k1 field: sum_l L1[l] psi_l
+    const float4* psiB;     // k2 field of RK3: sum_l L12[l] psi_l
+    const float4* psi0;     // newest level
+    float coef[4][kMaxFoot];
+    float dt, ep;
+    int time_integration_num;   // 10, 21, 30
+    int nfoot;
+    int rp;                     // psi cells per map cell (Npsi / Nmap, integer)
+};
+
+cudaError_t launch_init_map_m(float4* map, const Grid& g, cudaStream_t s);
+// outA = sum_l cA[l] levels[l], outB likewise (outB may be null)
+cudaError_t launch_precombine(float4* const* levels, int L, const double* cA, const double* cB, long long n,
+                              float4* outA, float4* outB, cudaStream_t s);
+cudaError_t launch_advect_m(const AdvectMArgs& a, cudaStream_t s);
+// max |det grad X - 1| on the half-shifted check grid with r = Ncheck / Nmap points per cell and axis
+cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_result, cudaStream_t s);
+// omega_0 through current map + n stacked maps (n * 2*Nc float4), FP64 positions
+cudaError_t launch_compose_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
+                             const InitSource& src, double* out, cudaStream_t s);
+// W(x + d(x)) on grid go (Ngo multiple of Nmap, Nf multiple of Ngo); out_f or out_d
+cudaError_t launch_sample_m(const Grid& gm, const Grid& go, const Grid& gf, const float4* map, const float4* W,
+                            float* out_f, double* out_d, cudaStream_t s);
+cudaError_t launch_particles_m(const Grid& gp, double* pos, int num, const float4* psiA, const float4* psiB,
+                               const float4* psi0, double dt, int ti, cudaStream_t s);
+cudaError_t launch_spec_psi_f(const float2* Fv, const Grid& gv, const Grid& gp, double freq, float2* out4,
+                              cudaStream_t s);
+// 4 planes (float or double) -> float4 nodes
+cudaError_t launch_planes_to_float4(const float* planes, const double* planes_d, long long n, float4* out,
+                                    cudaStream_t s);
+cudaError_t launch_float4_to_planes(const float4* in, long long n, double* planes, cudaStream_t s);
+cudaError_t launch_map_to_planes(const float4* map, const Grid& g, double* X, double* Y, cudaStream_t s);
+// sum psi_x^2 + psi_y^2 (FP64 accumulation) -> out[0]
+cudaError_t launch_energy_m(const float4* psi, long long n, double* scratch, double* out, cudaStream_t s);
+
+}  // namespace cmm

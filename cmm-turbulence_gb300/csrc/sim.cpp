@@ -3,6 +3,8 @@
 // src/simulation/cmm-simulation-host.cu.
 #include "sim.hpp"
 
+#include "mixed.hpp"
+
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <curand.h>
@@ -152,6 +154,17 @@ int EulerSim::alloc()
     s.lagrange_order = L;
     s.file_name = s.derived_file_name();
     max_maps = s.cpu_map_num();
+    if (s.precision == "mixed") {
+        // the mixed kernels address every grid as integer multiples of the map grid
+        bool ratios = s.grid_psi % s.grid_coarse == 0 && s.grid_vort % s.grid_coarse == 0 &&
+                      s.grid_fine % s.grid_vort == 0 && s.grid_fine % s.grid_coarse == 0;
+        if (!ratios) { err = "precision=mixed needs psi, vort and fine grids that are integer multiples of the map grid"; return kErrUnsupported; }
+        if (s.molly_stencil != 0) { err = "precision=mixed does not build mollified sampling"; return kErrUnsupported; }
+        mixed_ = true;
+    } else if (s.precision != "fp64") {
+        err = "precision must be fp64 or mixed";
+        return kErrParam;
+    }
 
     const double* b = s.domain_bounds;
     gc = make_grid(s.grid_coarse, s.grid_coarse, b);
@@ -173,7 +186,7 @@ int EulerSim::alloc()
     for (int l = 0; l < L; ++l) if ((rc = dalloc(&psi[l], 4 * gp.N))) return rc;
     if (s.initial_discrete && (rc = dalloc(&wdisc, 4 * gd.N))) return rc;
     stack_cap_ = std::max(0, std::min(max_maps, 16));
-    if (stack_cap_ > 0 && (rc = dalloc(&stack, 8 * gc.N * stack_cap_))) return rc;
+    if (!mixed_ && stack_cap_ > 0 && (rc = dalloc(&stack, 8 * gc.N * stack_cap_))) return rc;
     long long rmax = std::max({gf.N, gv.N, gd.N, gc.N, gp.N});
     long long cmax = std::max({gf.Nfft, gv.Nfft, gd.Nfft, gc.Nfft, gp.Nfft});
     if ((rc = dalloc(&real_buf_, rmax))) return rc;
@@ -192,6 +205,27 @@ int EulerSim::alloc()
         !make_plans(pc_, gc, stream) || (s.initial_discrete && !make_plans(pd_, gd, stream))) {
         err = "cuFFT plan creation failed";
         return kErrCuda;
+    }
+    if (mixed_) {
+        auto falloc = [&](void** p, size_t bytes) { return check(cudaMalloc(p, std::max(bytes, (size_t)16)), "cudaMalloc"); };
+        size_t mapb = sizeof(float4) * 2 * (size_t)gc.N, psib = sizeof(float4) * (size_t)gp.N;
+        if ((rc = falloc((void**)&mapm_, mapb)) || (rc = falloc((void**)&mapm_new_, mapb)) ||
+            (rc = falloc((void**)&psiA_, psib)) || (rc = falloc((void**)&psiB_, psib)) ||
+            (rc = falloc((void**)&wfm_, sizeof(float4) * (size_t)gf.N)) ||
+            (rc = falloc((void**)&realf_, sizeof(float) * 4 * (size_t)std::max(gv.N, gp.N))) ||
+            (rc = falloc((void**)&specf_, sizeof(float2) * (size_t)gv.Nfft)) ||
+            (rc = falloc((void**)&spec4f_, sizeof(float2) * 4 * (size_t)gp.Nfft)))
+            return rc;
+        for (int l = 0; l < L; ++l) if ((rc = falloc((void**)&psim_[l], psib))) return rc;
+        if (stack_cap_ > 0 && (rc = falloc((void**)&stackm_, mapb * stack_cap_))) return rc;
+        int nv[2] = {gv.NY, gv.NX}, np[2] = {gp.NY, gp.NX};
+        if (cufftPlanMany(&r2c_v_, 2, nv, nullptr, 1, 0, nullptr, 1, 0, CUFFT_R2C, 1) != CUFFT_SUCCESS ||
+            cufftPlanMany(&c2r4_p_, 2, np, nullptr, 1, 0, nullptr, 1, 0, CUFFT_C2R, 4) != CUFFT_SUCCESS) {
+            err = "cuFFT FP32 plan creation failed";
+            return kErrCuda;
+        }
+        cufftSetStream(r2c_v_, stream);
+        cufftSetStream(c2r4_p_, stream);
     }
     // random table for gaussian_blobs (cmm-euler2d.cu:348-354)
     std::vector<double> rnd(1000);
@@ -212,6 +246,13 @@ void EulerSim::release()
     f(real_buf_); f(spec_); f(spec4_); f(red_); f(d_scal_); f(d_params_); f(d_rand_);
     for (auto p : parts) f(p);
     parts.clear();
+    f(mapm_); f(mapm_new_); f(psiA_); f(psiB_); f(wfm_); f(stackm_); f(realf_); f(specf_); f(spec4f_);
+    for (int l = 0; l < kMaxLagrange; ++l) { f(psim_[l]); psim_[l] = nullptr; }
+    mapm_ = mapm_new_ = psiA_ = psiB_ = wfm_ = stackm_ = nullptr;
+    realf_ = nullptr; specf_ = nullptr; spec4f_ = nullptr;
+    if (r2c_v_) cufftDestroy(r2c_v_);
+    if (c2r4_p_) cufftDestroy(c2r4_p_);
+    r2c_v_ = c2r4_p_ = 0;
     if (h_scal_) cudaFreeHost(h_scal_);
     h_scal_ = nullptr;
     destroy_plans(pf_); destroy_plans(pv_); destroy_plans(pp_); destroy_plans(pc_); destroy_plans(pd_);
@@ -233,15 +274,30 @@ int EulerSim::translate_ic()
     src.gd = gd;
     src.params = d_params_;
     src.rand_table = d_rand_;
-    CMM_LAUNCH(1, launch_compose_sample(gc, gf, ChiX, ChiY, stack, n_maps_, src, real_buf_, stream));
+    if (mixed_) {
+        // FP64 positions through the FP32 displacement stack, FP64 spectral
+        // Hermite construction, FP32 storage of the fine vorticity nodes
+        CMM_LAUNCH(1, launch_compose_m(gc, gf, mapm_, stackm_, n_maps_, src, real_buf_, stream));
+    } else {
+        CMM_LAUNCH(1, launch_compose_sample(gc, gf, ChiX, ChiY, stack, n_maps_, src, real_buf_, stream));
+    }
     CMM_FFT(cufftExecD2Z(pf_.d2z, real_buf_, reinterpret_cast<cufftDoubleComplex*>(spec_)));
     CMM_LAUNCH(1, launch_spec_hermite(spec_, gf, spec4_, stream));
     CMM_FFT(cufftExecZ2D(pf_.z2d4, reinterpret_cast<cufftDoubleComplex*>(spec4_), wfine));
+    if (mixed_) CMM_LAUNCH(1, launch_planes_to_float4(nullptr, wfine, gf.N, wfm_, stream));
     return kOk;
 }
 
 int EulerSim::evaluate_stream()
 {
+    if (mixed_) {
+        CMM_LAUNCH(1, launch_sample_m(gc, gv, gf, mapm_, wfm_, realf_, nullptr, stream));
+        CMM_FFT(cufftExecR2C(r2c_v_, realf_, reinterpret_cast<cufftComplex*>(specf_)));
+        CMM_LAUNCH(1, launch_spec_psi_f(specf_, gv, gp, s.freq_cut_psi, spec4f_, stream));
+        CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), realf_));
+        CMM_LAUNCH(1, launch_planes_to_float4(realf_, nullptr, gp.N, psim_[0], stream));
+        return kOk;
+    }
     CMM_LAUNCH(1, launch_sample_vort(gc, gv, gf, ChiX, ChiY, wfine, s.molly_stencil, real_buf_, gv.NX, stream));
     CMM_FFT(cufftExecD2Z(pv_.d2z, real_buf_, reinterpret_cast<cufftDoubleComplex*>(spec_)));
     CMM_LAUNCH(1, launch_spec_psi(spec_, gv, gp, s.freq_cut_psi, spec4_, stream));
@@ -251,12 +307,69 @@ int EulerSim::evaluate_stream()
 
 int EulerSim::coarse_vort()
 {
+    if (mixed_) {
+        CMM_LAUNCH(1, launch_sample_m(gc, gc, gf, mapm_, wfm_, nullptr, vort, stream));
+        return kOk;
+    }
     CMM_LAUNCH(1, launch_sample_vort(gc, gc, gf, ChiX, ChiY, wfine, 0, vort, gc.NX, stream));
+    return kOk;
+}
+
+int EulerSim::sync_fp64_views()
+{
+    // mixed form: rebuild the reference-layout FP64 views (map planes, psi
+    // levels, fine vorticity planes) used by the writers and cmm_get_field
+    if (!mixed_) return kOk;
+    CMM_LAUNCH(1, launch_map_to_planes(mapm_, gc, ChiX, ChiY, stream));
+    for (int l = 0; l < L; ++l) CMM_LAUNCH(1, launch_float4_to_planes(psim_[l], gp.N, psi[l], stream));
+    CMM_LAUNCH(1, launch_float4_to_planes(wfm_, gf.N, wfine, stream));
+    return kOk;
+}
+
+int EulerSim::reset_map()
+{
+    if (mixed_) CMM_LAUNCH(1, launch_init_map_m(mapm_, gc, stream));
+    else CMM_LAUNCH(1, launch_init_map(ChiX, ChiY, gc, stream));
+    return kOk;
+}
+
+void EulerSim::swap_levels(int a, int b)
+{
+    std::swap(psi[a], psi[b]);
+    std::swap(psim_[a], psim_[b]);
+}
+
+int EulerSim::advect_m(const double* t, const double* dtv, int lc, int ti_num, int l_order)
+{
+    int lcl = lc + l_order - 1;
+    double L1[kMaxLagrange] = {0, 0, 0, 0}, L12[kMaxLagrange] = {0, 0, 0, 0};
+    for (int i = 0; i < l_order; ++i) {
+        L1[i] = lagrange_coefficient(t, t[lcl + 1], lcl, i, l_order);
+        L12[i] = lagrange_coefficient(t, t[lcl] + dtv[lcl + 1] / 2.0, lcl, i, l_order);
+    }
+    // Lagrange extrapolation is linear in psi: combine the levels once per
+    // step, then every RK stage interpolates a single field
+    CMM_LAUNCH(1, launch_precombine(psim_, l_order, L1, ti_num == 30 ? L12 : nullptr, gp.N, psiA_,
+                                    ti_num == 30 ? psiB_ : nullptr, stream));
+    AdvectMArgs a{};
+    a.gm = gc; a.gp = gp;
+    a.map = mapm_; a.out = mapm_new_;
+    a.psiA = psiA_; a.psiB = psiB_; a.psi0 = psim_[0];
+    double coef[4][kMaxFoot];
+    map_update_coefficients(s.map_update_order_num, s.map_epsilon, coef, &a.nfoot);
+    for (int p = 0; p < 4; ++p) for (int k = 0; k < kMaxFoot; ++k) a.coef[p][k] = (float)coef[p][k];
+    a.dt = (float)dtv[lcl + 1];
+    a.ep = (float)s.map_epsilon;
+    a.time_integration_num = ti_num;
+    a.rp = gp.NX / gc.NX;
+    CMM_LAUNCH(1, launch_advect_m(a, stream));
+    std::swap(mapm_, mapm_new_);
     return kOk;
 }
 
 int EulerSim::advect(const double* t, const double* dtv, int lc, int ti_num, int l_order)
 {
+    if (mixed_) return advect_m(t, dtv, lc, ti_num, l_order);
     AdvectArgs a{};
     a.gm = gc; a.gp = gp;
     a.ChiX = ChiX; a.ChiY = ChiY; a.outX = ChiX_new; a.outY = ChiY_new;
@@ -279,7 +392,8 @@ int EulerSim::advect(const double* t, const double* dtv, int lc, int ti_num, int
 
 int EulerSim::incomp(double* out)
 {
-    CMM_LAUNCH(1, launch_incomp(gf, gc, ChiX, ChiY, d_scal_, stream));
+    if (mixed_) CMM_LAUNCH(1, launch_incomp_m(gc, gf.NX / gc.NX, mapm_, d_scal_, stream));
+    else CMM_LAUNCH(1, launch_incomp(gf, gc, ChiX, ChiY, d_scal_, stream));
     CMM_CUDA(cudaMemcpyAsync(h_scal_, d_scal_, sizeof(double), cudaMemcpyDeviceToHost, stream));
     CMM_CUDA(cudaStreamSynchronize(stream));
     *out = h_scal_[0];
@@ -292,10 +406,30 @@ void EulerSim::rotate_psi(int n)
     double* tmp = psi[n];
     for (int j = n; j >= 1; --j) psi[j] = psi[j - 1];
     psi[0] = tmp;
+    float4* tmf = psim_[n];
+    for (int j = n; j >= 1; --j) psim_[j] = psim_[j - 1];
+    psim_[0] = tmf;
 }
 
 int EulerSim::push_stack()
 {
+    if (mixed_) {
+        size_t mapb = sizeof(float4) * 2 * (size_t)gc.N;
+        if (n_maps_ >= stack_cap_) {
+            int cap = std::min(max_maps, std::max(2 * stack_cap_, 16));
+            float4* bigger = nullptr;
+            CMM_CUDA(cudaMalloc((void**)&bigger, mapb * cap));
+            if (stackm_ && n_maps_ > 0)
+                CMM_CUDA(cudaMemcpyAsync(bigger, stackm_, mapb * n_maps_, cudaMemcpyDeviceToDevice, stream));
+            CMM_CUDA(cudaStreamSynchronize(stream));
+            if (stackm_) cudaFree(stackm_);
+            stackm_ = bigger;
+            stack_cap_ = cap;
+        }
+        CMM_CUDA(cudaMemcpyAsync(stackm_ + 2 * (size_t)n_maps_ * gc.N, mapm_, mapb, cudaMemcpyDeviceToDevice, stream));
+        n_maps_++;
+        return kOk;
+    }
     if (n_maps_ >= stack_cap_) {
         int cap = std::min(max_maps, std::max(2 * stack_cap_, 16));
         double* bigger = nullptr;
@@ -350,10 +484,23 @@ int EulerSim::advect_particles(int lcl)
     double Lp12[kMaxLagrange] = {0, 0, 0, 0};
     for (int i = 0; i < L; ++i)
         Lp12[i] = lagrange_coefficient(t_vec_.data(), t_vec_[lcl] + dt_vec_[lcl + 1] / 2.0, lcl + 1, i, L);
+    bool combined = false;
     for (size_t i = 0; i < s.particles_advected.size(); ++i) {
         auto& p = s.particles_advected[i];
         if (p.num <= 0 || p.tau != 0) continue;
         if (!(t_vec_[lcl + 1] + 1e-5 * dt_vec_[lcl + 1] >= p.init_time)) continue;
+        if (mixed_) {
+            if (p.time_integration_num == 30 && !combined) {
+                CMM_LAUNCH(1, launch_precombine(psim_, L, Lp12, nullptr, gp.N, psiB_, nullptr, stream));
+                combined = true;
+            }
+            cudaError_t e = launch_particles_m(gp, parts[i], p.num, psim_[1], psiB_, psim_[0], dt_vec_[lcl + 1],
+                                               p.time_integration_num, stream);
+            kernel_launches++;
+            if (e == cudaErrorInvalidValue) { err = "particle time integration " + p.time_integration + " is not built"; return kErrUnsupported; }
+            CMM_CUDA(e);
+            continue;
+        }
         ParticleArgs a{};
         a.gp = gp; a.pos = parts[i]; a.num = p.num;
         for (int l = 0; l < kMaxLagrange; ++l) a.psi[l] = psi[l];
@@ -404,7 +551,7 @@ int EulerSim::init()
         CMM_CUDA(cudaStreamSynchronize(stream));   // host_discrete_ may be released by the caller
     }
 
-    CMM_LAUNCH(1, launch_init_map(ChiX, ChiY, gc, stream));
+    if ((rc = reset_map())) return rc;
     if ((rc = translate_ic()) || (rc = evaluate_stream()) || (rc = coarse_vort())) return rc;
 
     // Lagrange velocity history (cmm-euler2d.cu:520-619): alternate the
@@ -435,11 +582,11 @@ int EulerSim::init()
                     log_.push("   Init step = " + std::to_string(k) + "/" + std::to_string(nsteps) + " \t IncompErr = " + to_str3(inc));
             }
             for (int i = 0; i < 5; ++i) { dt_init[i] = -dt_init[i]; t_init[i] = -t_init[i]; }
-            std::swap(psi[0], psi[nsteps]);
-            if (nsteps >= 3) std::swap(psi[1], psi[2]);
-            CMM_LAUNCH(1, launch_init_map(ChiX, ChiY, gc, stream));
+            swap_levels(0, nsteps);
+            if (nsteps >= 3) swap_levels(1, 2);
+            if ((rc = reset_map())) return rc;
         }
-        CMM_LAUNCH(1, launch_init_map(ChiX, ChiY, gc, stream));
+        if ((rc = reset_map())) return rc;
     }
     if ((rc = init_particles())) return rc;
 
@@ -516,7 +663,7 @@ int EulerSim::step_once()
             ph_begin(kPhRemap);
             if ((rc = translate_ic())) return rc;
             if ((rc = push_stack())) return rc;
-            CMM_LAUNCH(1, launch_init_map(ChiX, ChiY, gc, stream));
+            if ((rc = reset_map())) return rc;
             kernel_launches++;
             ph_end(kPhRemap);
         }
@@ -614,6 +761,8 @@ int EulerSim::write_time_step(double t_now, double dt_now)
     for (auto& r : s.save_computational)
         if (instant_fires(r.is_instant, r.time_start, r.time_end, r.time_step, t_now, dt_now, dt)) { fire = true; var += r.var; }
     if (!fire) return kOk;
+    int rs = sync_fp64_views();
+    if (rs) return rs;
     std::string tname = std::abs(t_now - kTMax) < 1 ? "final" : to_str3(t_now);
     bool all = has(var, "All");
     bool dbg = s.verbose >= 4;
@@ -672,7 +821,8 @@ int EulerSim::diagnostics(double* energy, double* enstrophy, double* palinstroph
 {
     // Compute_Energy_H, Compute_Enstrophy, Compute_Palinstrophy, w max
     // (src/numerical/cmm-mesure.cu:30-89, cmm-simulation-host.cu:668-673)
-    CMM_LAUNCH(2, launch_sumsq(psi[0] + gp.N, 2 * gp.N, red_, d_scal_ + 1, stream));
+    if (mixed_) CMM_LAUNCH(2, launch_energy_m(psim_[0], gp.N, red_, d_scal_ + 1, stream));
+    else CMM_LAUNCH(2, launch_sumsq(psi[0] + gp.N, 2 * gp.N, red_, d_scal_ + 1, stream));
     CMM_LAUNCH(2, launch_sumsq(vort, gc.N, red_, d_scal_ + 2, stream));
     CMM_FFT(cufftExecD2Z(pc_.d2z, vort, reinterpret_cast<cufftDoubleComplex*>(spec_)));
     CMM_LAUNCH(1, launch_spec_grad(spec_, gc, spec4_, stream));
@@ -733,6 +883,8 @@ size_t EulerSim::field_bytes(const std::string& n) const
 int EulerSim::get_field(const std::string& n, void* dst, size_t bytes)
 {
     if (!initialised_) { err = "get_field before init"; return kErrState; }
+    int rs = sync_fp64_views();
+    if (rs) return rs;
     size_t need = field_bytes(n);
     if (need == 0 && n != "Map_stack") { err = "unknown field " + n; return kErrNotFound; }
     if (bytes != need) { err = "field " + n + " needs " + std::to_string(need) + " bytes"; return kErrParam; }

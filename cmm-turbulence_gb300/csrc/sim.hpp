@@ -84,6 +84,9 @@ private:
     int evaluate_stream();
     int coarse_vort();
     int advect(const double* t, const double* dtv, int loop_ctr, int ti_num, int l_order);
+    int advect_m(const double* t, const double* dtv, int loop_ctr, int ti_num, int l_order);
+    int reset_map();
+    void swap_levels(int a, int b);
     int incomp(double* out);
     int init_particles();
     int advect_particles(int lcl);
@@ -102,6 +105,21 @@ private:
     void ph_begin(int p);
     void ph_end(int p);
     void ph_collect();
+    int sync_fp64_views();   // mixed form: refresh the FP64 reference-layout copies
+
+    // mixed form (precision=mixed): FP32 displacement maps and FP32 Hermite nodes
+    bool mixed_ = false;
+    float4* mapm_ = nullptr;         // 2*Nc float4 (current map)
+    float4* mapm_new_ = nullptr;
+    float4* psim_[kMaxLagrange] = {nullptr, nullptr, nullptr, nullptr};
+    float4* psiA_ = nullptr;         // Lagrange combinations of the psi levels
+    float4* psiB_ = nullptr;
+    float4* wfm_ = nullptr;          // fine vorticity nodes
+    float4* stackm_ = nullptr;       // n maps, 2*Nc float4 each
+    float* realf_ = nullptr;         // FP32 real scratch (4 planes of the largest grid)
+    float2* specf_ = nullptr;        // FP32 complex scratch
+    float2* spec4f_ = nullptr;       // 4 FP32 spectra
+    cufftHandle r2c_v_ = 0, c2r4_p_ = 0;
     bool prof_ = false;
     cudaEvent_t ev_[kNumPhases][2] = {};
     bool ev_live_[kNumPhases] = {};

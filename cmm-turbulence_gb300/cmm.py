@@ -29,6 +29,7 @@ EXPORTS = [
     "cmm_settings_text",
     "cmm_file_name", "cmm_destroy", "cmm_advect_map", "cmm_incomp_max", "cmm_compose_stack", "cmm_sample_vort",
     "cmm_poisson_create", "cmm_poisson_hermite", "cmm_poisson_destroy", "cmm_particles_advect", "cmm_diagnostics",
+    "cmm_diagnostics_noalloc",
 ]
 
 
@@ -88,6 +89,7 @@ def lib():
     L.cmm_poisson_destroy.argtypes = [vp]
     L.cmm_particles_advect.argtypes = [gp, vp, ip, C.POINTER(vp), ip, dp, C.c_double, ip, vp]
     L.cmm_diagnostics.argtypes = [gp, vp, gp, vp, dp, vp]
+    L.cmm_diagnostics_noalloc.argtypes = [gp, vp, gp, vp, dp, vp]
     _lib = L
     return L
 
@@ -232,4 +234,12 @@ def particles_advect(gp, pos, num, psi_levels, Lp12, dt, ti=30, stream=None):
 def diagnostics(gp, psi, gc, vort, stream=None):
     out = (C.c_double * 3)()
     check(lib().cmm_diagnostics(C.byref(gp), _dptr(psi), C.byref(gc), _dptr(vort), out, stream))
+    return list(out)
+
+
+def diagnostics_noalloc(gp, psi, gc, vort, stream=None):
+    """cmm_diagnostics without device allocation (fixed in-library scratch;
+    serialise overlapping calls)."""
+    out = (C.c_double * 3)()
+    check(lib().cmm_diagnostics_noalloc(C.byref(gp), _dptr(psi), C.byref(gc), _dptr(vort), out, stream))
     return list(out)

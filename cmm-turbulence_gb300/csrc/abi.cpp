@@ -12,6 +12,10 @@
 #include "settings.hpp"
 #include "sim.hpp"
 
+namespace cmm {
+void set_last_error(const std::string& msg);
+}
+
 struct cmm_ctx {
     cmm::Settings settings;
     cmm::EulerSim* sim = nullptr;
@@ -66,6 +70,10 @@ int sim_rc(cmm::EulerSim* sim, int rc)
     return rc;
 }
 }  // namespace
+
+// lets entry points defined in other translation units report through
+// cmm_last_error
+void cmm::set_last_error(const std::string& msg) { g_err = msg; }
 
 extern "C" {
 

@@ -179,6 +179,21 @@ int cmm_particles_advect(const cmm_grid* grid_psi, double* pos, int num, const d
 int cmm_diagnostics(const cmm_grid* grid_psi, const double* psi, const cmm_grid* grid_coarse, const double* vort,
                     double* out3, void* stream);
 
+/* Same results as cmm_diagnostics (to rounding: the partial sums are grouped
+ * differently) without allocating device memory: no counterpart in the
+ * reference.  For callers that may not allocate, e.g. a host that reserves
+ * all device memory up front or a loop that cannot take cudaFree's implicit
+ * device-wide synchronisation.  The reduction scratch is a fixed array
+ * inside the library (about 393 KB per GPU, resident while the library is
+ * loaded), so 2*NX*NY of grid_psi and NX*NY of grid_coarse may each be at
+ * most 4194304 (2048^2 coarse, 1448^2 psi); larger grids -> CMM_ERR_PARAM.
+ * The first call on each device looks up the array's address (set-up, with
+ * that device current); later calls only launch.  Nothing in the scratch has
+ * to start at zero.  Calls that overlap -- other streams or host threads --
+ * race on the one array: serialise them.  Synchronises the stream. */
+int cmm_diagnostics_noalloc(const cmm_grid* grid_psi, const double* psi, const cmm_grid* grid_coarse,
+                            const double* vort, double* out3, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -131,14 +131,6 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- roofline bookkeeping
-def advect_model(w, L=3, nfoot=8):
-    """Algorithmic bytes and FP64 flops of one map-advection launch (per time step)."""
-    Nc, Np = w["grid_coarse"] ** 2, w["grid_psi"] ** 2
-    bytes_ = 8 * (8 * Nc + 4 * L * Np + 8 * Nc)      # read map + psi levels, write new map
-    flops = nfoot * (304 + 304 + 176 + 120 + 30) * Nc + 128 * Nc
-    return bytes_, flops
-
-
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -148,7 +140,34 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-FP64_PEAK_TFLOPS = 1.20   # FP64 FMA throughput measured on this machine's GB300 (profiles/fp64_fma_probe.md)
+FP64_PEAK_TFLOPS = 1.10   # GB300 FP64 rate: `python bench.py --fp64-peak` (cuBLAS DGEMM), profiles/fp64_peak.md
+
+# DRAM bytes (read + write) per launch of a phase's dominant kernel, from one
+# ncu capture of the workload (profiles/k_particles_m_c2.md, k_advect_fp64_c2.md)
+NCU_TRAFFIC = {("mixed", "particles"): 71.2e6, ("fp64", "advect"): 127.4e6}
+
+
+def measure_fp64_peak():
+    """FP64 throughput of a cuBLAS DGEMM (torch.matmul, float64, 8192^3,
+    2 N^3 flops, best of 5 after 2 warm-up runs, CUDA events)."""
+    import torch
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    best = None
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    tflops = 2.0 * n ** 3 / (best / 1000.0) / 1e12
+    print(json.dumps({"fp64_dgemm_tflops": tflops, "n": n, "best_ms": best, "how": "cuBLAS DGEMM via torch.matmul"}))
 
 
 def cpu_oracle_steps(n_steps, ic, threads, particles=100000):
@@ -201,15 +220,24 @@ def run_reference(args):
 
 
 def measure_form(m, torch, pf, ic, precision, args, world, clocks=None, profile=True):
-    """Init one simulation of the workload in `precision`, run W warm-up steps,
-    time exactly K steps with CUDA events on the library stream, then
-    (optionally) profile a few more steps phase by phase."""
+    """W warm-up steps on a throw-away instance, then a fresh simulation of the
+    workload in `precision`: its first K steps from t = 0 (with every remap
+    they trigger; K = 2560 is the whole T = 10 run) timed with CUDA events on
+    the library stream, then (optionally) a few more steps profiled phase by
+    phase."""
     stream = torch.cuda.Stream()
-    sim = m.Simulation(["param_file=" + pf, "precision=" + precision], stream=stream.cuda_stream)
+    over = ["param_file=" + pf, "precision=" + precision,
+            "final_time=%r" % ((args.steps + 32) / WORKLOAD["steps_per_sec"])]
+    if args.warmup > 0:
+        warm = m.Simulation(over, stream=stream.cuda_stream)
+        warm.set_initial_discrete(ic)
+        warm.init()
+        for _ in range(args.warmup):
+            warm.step(1)
+        warm.close()
+    sim = m.Simulation(over, stream=stream.cuda_stream)
     sim.set_initial_discrete(ic)
     sim.init()
-    for _ in range(args.warmup):
-        sim.step(1)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     if world > 1:
@@ -339,7 +367,8 @@ def _e2e(m, torch, ic, pf, args, world):
     stream2 = torch.cuda.Stream()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    sim2 = m.Simulation(["param_file=" + pf, "precision=" + args.precision], stream=stream2.cuda_stream)
+    sim2 = m.Simulation(["param_file=" + pf, "precision=" + args.precision,
+                         "final_time=%r" % ((args.steps + 32) / WORKLOAD["steps_per_sec"])], stream=stream2.cuda_stream)
     sim2.set_initial_discrete(ic_pinned.numpy())
     sim2.init()
     d2h = 0
@@ -358,22 +387,21 @@ def _e2e(m, torch, ic, pf, args, world):
             "includes": "IC upload + init (Lagrange history) + every step + final psi readback"}
 
 
+def roofline_model():
+    import importlib.util
+    path = os.path.join(ROOT, "cmm-turbulence_gb300", "roofline_model.py")
+    spec = importlib.util.spec_from_file_location("cmm_gb300_roofline_model", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def phase_models(w, precision):
-    """Algorithmic (compulsory) HBM bytes of each loop phase per step, and the
-    FP64 flops of the plain advection (SURVEY 8d conventions)."""
-    Nc, Nf, Np, Nv, L = w["grid_coarse"] ** 2, w["grid_fine"] ** 2, w["grid_psi"] ** 2, w["grid_vort"] ** 2, 3
-    P = w["particles"]
-    if precision == "fp64":
-        b = {"advect": 8 * (16 * Nc + 4 * L * Np), "incomp": 8 * 8 * Nc,
-             "psi": 8 * (8 * Nc + 4 * Nf) + 8 * Nv + 2 * 16 * (Nv // 2 + 1) * w["grid_vort"] + 4 * 8 * Np,
-             "coarse": 8 * (8 * Nc + 4 * Nf) + 8 * Nc, "particles": 32 * P + 8 * 4 * L * Np}
-    else:
-        # FP32 map nodes 32 B, FP32 Hermite nodes 16 B
-        b = {"advect": 32 * 2 * Nc + 16 * L * Np, "incomp": 32 * Nc,
-             "psi": 32 * Nc + 16 * Nf + 4 * Nv + 2 * 8 * (Nv // 2 + 1) * w["grid_vort"] + 16 * Np,
-             "coarse": 32 * Nc + 16 * Nf + 8 * Nc, "particles": 32 * P + 16 * L * Np}
-    flops = 8 * (304 + 304 + 176 + 120 + 30) * Nc + 128 * Nc
-    return b, flops
+    """Algorithmic (compulsory) HBM bytes of each loop phase per step (word 8
+    for the plain FP64 form, 4 for the FP32 nodes of the mixed form) and the
+    counted FLOPs of the advection."""
+    rm = roofline_model()
+    return rm.phase_bytes(w, 8 if precision == "fp64" else 4), rm.step_flops(w)["advect"]
 
 
 def _report(args, world, rank, chosen, plain, clocks, e2e_line, ic):
@@ -389,7 +417,8 @@ def _report(args, world, rank, chosen, plain, clocks, e2e_line, ic):
                "psi": "psi solve (k_sample + FFT + k_spec_psi)", "coarse": "k_sample (coarse omega)",
                "particles": "k_particles (RK3 tracers)"}
     roof = {"kernel": kernels.get(dom, dom), "phase": dom, "bound": "hbm", "achieved": achieved, "peak": peak,
-            "unit": "GB/s", "frac": achieved / peak, "peak_source": "of " + peak_kind, "traffic": None,
+            "unit": "GB/s", "frac": achieved / peak, "peak_source": "of " + peak_kind,
+            "traffic": NCU_TRAFFIC.get((args.precision, dom)),
             "ms_per_launch": ms, "algorithmic_bytes": models[dom],
             "phases": {k: {"ms": per[k], "GBps": models[k] / (per[k] / 1000.0) / 1e9,
                            "frac": models[k] / (per[k] / 1000.0) / 1e9 / peak} for k in per if k in models}}
@@ -434,7 +463,7 @@ def _report(args, world, rank, chosen, plain, clocks, e2e_line, ic):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=2560, help="timed steps from t = 0 (2560 = the whole T = 10 run)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
@@ -444,8 +473,11 @@ def main():
     ap.add_argument("--t10", action="store_true", help="run both forms to the final time and report the enstrophy error")
     ap.add_argument("--t10-final", type=float, default=10.0)
     ap.add_argument("--t10-particles", type=int, default=WORKLOAD["particles"])
+    ap.add_argument("--fp64-peak", action="store_true", help="measure the FP64 rate (cuBLAS DGEMM) and exit")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.fp64_peak:
+        measure_fp64_peak()
+    elif args.impl == "reference":
         run_reference(args)
     elif args.t10:
         run_t10(args)

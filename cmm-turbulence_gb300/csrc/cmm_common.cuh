@@ -12,7 +12,7 @@
 // The interpolants evaluate the same bicubic Hermite polynomial as the
 // reference (src/numerical/cmm-hermite.cu:239-271 basis, :30-86 contraction)
 // but in a separable order that needs fewer FP64 instructions: GB300 issues
-// FP64 at 1/58 of its FP32 rate, so every DFMA counts.  Divisions by the grid
+// FP64 at about 1/64 of its FP32 rate, so every DFMA counts.  Divisions by the grid
 // spacing are replaced by multiplications with its reciprocal.
 #pragma once
 #include <cuda_runtime.h>
@@ -32,6 +32,9 @@ struct Grid {
     double Lx, Ly;        // NX*hx, NY*hy: jump of a periodic map across the domain
     double Wx, Wy;        // bounds[1]-bounds[0], bounds[3]-bounds[2]: wrap length
     double kfx, kfy;      // 2*pi/(hx*NX), 2*pi/(hy*NY): spectral wavenumber factor
+    // FP32 copies for the mixed-precision kernels: converting a double in a
+    // kernel is an FP64-pipe instruction, which GB300 issues at 1/64 rate
+    float hxf, hyf, ihxf, ihyf, kfxf, kfyf;
 };
 
 inline Grid make_grid(int NX, int NY, const double* bounds)
@@ -49,6 +52,8 @@ inline Grid make_grid(int NX, int NY, const double* bounds)
     g.Lx = NX * g.hx; g.Ly = NY * g.hy;
     g.Wx = bounds[1] - bounds[0]; g.Wy = bounds[3] - bounds[2];
     g.kfx = kTwoPi / (g.hx * NX); g.kfy = kTwoPi / (g.hy * NY);
+    g.hxf = (float)g.hx; g.hyf = (float)g.hy; g.ihxf = (float)g.ihx; g.ihyf = (float)g.ihy;
+    g.kfxf = (float)g.kfx; g.kfyf = (float)g.kfy;
     return g;
 }
 

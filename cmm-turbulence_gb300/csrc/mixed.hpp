@@ -30,6 +30,7 @@ cudaError_t launch_precombine(float4* const* levels, int L, const double* cA, co
                               float4* outA, float4* outB, cudaStream_t s);
 cudaError_t launch_advect_m(const AdvectMArgs& a, cudaStream_t s);
 // max |det grad X - 1| on the half-shifted check grid with r = Ncheck / Nmap points per cell and axis
+// (r * Nmap^2 < 2^31)
 cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_result, cudaStream_t s);
 // omega_0 through current map + n stacked maps (n * 2*Nc float4), FP64 positions
 cudaError_t launch_compose_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
@@ -37,8 +38,11 @@ cudaError_t launch_compose_m(const Grid& gm, const Grid& gt, const float4* map, 
 // W(x + d(x)) on grid go (Ngo multiple of Nmap, Nf multiple of Ngo); out_f or out_d
 cudaError_t launch_sample_m(const Grid& gm, const Grid& go, const Grid& gf, const float4* map, const float4* W,
                             float* out_f, double* out_d, cudaStream_t s);
-cudaError_t launch_particles_m(const Grid& gp, double* pos, int num, const float4* psiA, const float4* psiB,
-                               const float4* psi0, double dt, int ti, cudaStream_t s);
+// tracers at 64-bit fixed-point positions P = (x - b0) / W * 2^64 (interleaved x, y)
+cudaError_t launch_particles_m(const Grid& gp, unsigned long long* pos, int num, const float4* psiA,
+                               const float4* psiB, const float4* psi0, double dt, int ti, cudaStream_t s);
+cudaError_t launch_pos_to_fix(const double* pos, int num, const Grid& g, unsigned long long* out, cudaStream_t s);
+cudaError_t launch_fix_to_pos(const unsigned long long* in, int num, const Grid& g, double* pos, cudaStream_t s);
 cudaError_t launch_spec_psi_f(const float2* Fv, const Grid& gv, const Grid& gp, double freq, float2* out4,
                               cudaStream_t s);
 // 4 planes (float or double) -> float4 nodes

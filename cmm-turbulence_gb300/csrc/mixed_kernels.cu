@@ -9,8 +9,11 @@
 // integer node + FP32 offset, corner values are taken relative to the node
 // (map) or to a cell corner (velocity), so the 1/eps and 1/eps^2 GALS stencil
 // only amplifies rounding of small quantities.  FP64 is kept in the remap-time
-// composition (positions accumulated in FP64 through the whole stack), in the
-// Jacobian-determinant deviation, and in the diagnostics' sums.
+// composition (positions accumulated in FP64 through the whole stack) and in
+// the diagnostics' sums; the Jacobian-determinant deviation is formed exactly
+// from FP32 slopes with error-free transformations (FP64-accurate), and tracer
+// positions are 64-bit fixed point.  No per-step kernel issues FP64
+// instructions: GB300 runs them at about 1/64 of the FP32 rate.
 #include <cuda_runtime.h>
 
 #include "init_conditions.cuh"
@@ -56,10 +59,9 @@ __device__ __forceinline__ int wrap_index(int i, int n)
     return r < 0 ? r + n : r;
 }
 
-// cell of the point (bx*h + ox, by*h + oy): integer base cell + FP32 offset
-__device__ __forceinline__ CellF locate_rel(const Grid& g, int bx, int by, float ox, float oy)
+// cell of the point (bx + qx, by + qy) in cell units: integer base cell + FP32 offset
+__device__ __forceinline__ CellF locate_q(const Grid& g, int bx, int by, float qx, float qy)
 {
-    float qx = ox * (float)g.ihx, qy = oy * (float)g.ihy;
     float fx = floorf(qx), fy = floorf(qy);
     CellF c;
     c.tx = qx - fx;
@@ -69,6 +71,12 @@ __device__ __forceinline__ CellF locate_rel(const Grid& g, int bx, int by, float
     c.i00 = iy0 * g.NX + ix0; c.i10 = iy0 * g.NX + ix1;
     c.i01 = iy1 * g.NX + ix0; c.i11 = iy1 * g.NX + ix1;
     return c;
+}
+
+// cell of the point (bx*h + ox, by*h + oy): integer base cell + FP32 offset in length units
+__device__ __forceinline__ CellF locate_rel(const Grid& g, int bx, int by, float ox, float oy)
+{
+    return locate_q(g, bx, by, ox * g.ihxf, oy * g.ihyf);
 }
 
 // cell of an absolute FP64 position; the fraction is rounded to FP32 once
@@ -130,8 +138,8 @@ __device__ __forceinline__ void velocity_f(const float4* __restrict__ P, const G
     q.c00 = __ldg(P + c.i00); q.c10 = __ldg(P + c.i10); q.c01 = __ldg(P + c.i01); q.c11 = __ldg(P + c.i11);
     float ref = q.c00.x;
     q.c00.x = 0.0f; q.c10.x -= ref; q.c01.x -= ref; q.c11.x -= ref;
-    W4f wx = value_weights_f(c.tx, (float)g.hx), wy = value_weights_f(c.ty, (float)g.hy);
-    W4f dx = slope_weights_f(c.tx, (float)g.ihx), dy = slope_weights_f(c.ty, (float)g.ihy);
+    W4f wx = value_weights_f(c.tx, g.hxf), wy = value_weights_f(c.ty, g.hyf);
+    W4f dx = slope_weights_f(c.tx, g.ihxf), dy = slope_weights_f(c.ty, g.ihyf);
     float gx, gy;
     herm_grad_f(q, wx, wy, dx, dy, gx, gy);
     ux = gy;
@@ -146,7 +154,7 @@ __device__ __forceinline__ void map_disp_f(const float4* __restrict__ M, const G
     float4 a10 = __ldg(M + 2 * c.i10), b10 = __ldg(M + 2 * c.i10 + 1);
     float4 a01 = __ldg(M + 2 * c.i01), b01 = __ldg(M + 2 * c.i01 + 1);
     float4 a11 = __ldg(M + 2 * c.i11), b11 = __ldg(M + 2 * c.i11 + 1);
-    W4f wx = value_weights_f(c.tx, (float)g.hx), wy = value_weights_f(c.ty, (float)g.hy);
+    W4f wx = value_weights_f(c.tx, g.hxf), wy = value_weights_f(c.ty, g.hyf);
     Q4 q;
     q.c00 = make_float4(a00.x - rx, a00.z, b00.x, b00.z);
     q.c10 = make_float4(a10.x - rx, a10.z, b10.x, b10.z);
@@ -219,8 +227,8 @@ __global__ void __launch_bounds__(256) k_advect_m(const AdvectMArgs a, int lpn_l
     long long node = t >> lpn_log2;
     int k = (int)(t & (lpn - 1));
     bool live = node < a.gm.N;
-    long long nd = live ? node : 0;
-    int iX = (int)(nd % a.gm.NX), iY = (int)(nd / a.gm.NX);
+    const int nd = live ? (int)node : 0;
+    const int iY = nd / a.gm.NX, iX = nd - iY * a.gm.NX;
     float4 n0 = __ldg(a.map + 2 * nd);     // (dX, dY, dX_x, dY_x) at the node
     float gX = 0.0f, gY = 0.0f;
     if (live && k < a.nfoot) {
@@ -284,22 +292,54 @@ cudaError_t launch_advect_m(const AdvectMArgs& a, cudaStream_t s)
 // incompressibility: one thread per (coarse cell, check row).  The slopes of
 // the displacement are interpolated in FP32; the deviation of the Jacobian
 // determinant  det - 1 = a + b + a*b - c*e  (a = dX_x, b = dY_y, c = dX_y,
-// e = dY_x) is formed and maximised in FP64.  Check points are the fine grid
-// shifted by half a fine cell (k_incompressibility_check), r = Nf / Nc per cell.
+// e = dY_x) is formed exactly from them with error-free transformations
+// (TwoSum, FMA TwoProduct) and kept as a normalised FP32 pair hi + lo, which
+// is as accurate as an FP64 evaluation (~1e-14 of |a|+|b|+|ab|+|ce|) but
+// needs no FP64 instruction.  Check points are the fine grid shifted by half
+// a fine cell (k_incompressibility_check), r = Nf / Nc per cell.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_incomp_m(Grid gm, int r, const float4* __restrict__ M,
+struct F2 { float hi, lo; };
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ F2 abs_det_deviation(float a, float b, float c, float e)
+{
+    float s, es, t, et, u, eu;
+    two_sum(a, b, s, es);
+    float p = __fmul_rn(a, b), ep = fmaf(a, b, -p);
+    float q = __fmul_rn(c, e), eq = fmaf(c, e, -q);
+    two_sum(p, -q, t, et);
+    two_sum(s, t, u, eu);
+    float lo = __fadd_rn(__fadd_rn(__fadd_rn(es, et), __fsub_rn(ep, eq)), eu);
+    F2 r;
+    r.hi = __fadd_rn(u, lo);
+    r.lo = __fsub_rn(lo, __fsub_rn(r.hi, u));
+    if (r.hi < 0.0f || (r.hi == 0.0f && r.lo < 0.0f)) { r.hi = -r.hi; r.lo = -r.lo; }
+    return r;
+}
+
+__device__ __forceinline__ bool f2_greater(const F2& x, const F2& y)
+{
+    return x.hi > y.hi || (x.hi == y.hi && x.lo > y.lo);
+}
+
+__global__ void __launch_bounds__(256) k_incomp_m(Grid gm, int r, float ir, const float4* __restrict__ M,
                                                   unsigned long long* result)
 {
-    __shared__ unsigned long long wmax[8];
-    unsigned long long best = 0ull;
-    long long total = gm.N * r;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        int sub_y = (int)(i % r);
-        long long cell = i / r;
-        int cx = (int)(cell % gm.NX), cy = (int)(cell / gm.NX);
+    __shared__ F2 wmax[8];
+    F2 best = {0.0f, 0.0f};
+    const int total = (int)gm.N * r;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        int cell = i / r, sub_y = i - cell * r;
+        int cy = cell / gm.NX, cx = cell - cy * gm.NX;
         int cx1 = cx + 1 == gm.NX ? 0 : cx + 1, cy1 = cy + 1 == gm.NY ? 0 : cy + 1;
-        long long i00 = (long long)cy * gm.NX + cx, i10 = (long long)cy * gm.NX + cx1;
-        long long i01 = (long long)cy1 * gm.NX + cx, i11 = (long long)cy1 * gm.NX + cx1;
+        int i00 = cy * gm.NX + cx, i10 = cy * gm.NX + cx1;
+        int i01 = cy1 * gm.NX + cx, i11 = cy1 * gm.NX + cx1;
         float4 a00 = __ldg(M + 2 * i00), b00 = __ldg(M + 2 * i00 + 1);
         float4 a10 = __ldg(M + 2 * i10), b10 = __ldg(M + 2 * i10 + 1);
         float4 a01 = __ldg(M + 2 * i01), b01 = __ldg(M + 2 * i01 + 1);
@@ -311,41 +351,43 @@ __global__ void __launch_bounds__(256) k_incomp_m(Grid gm, int r, const float4* 
         qX.c10 = make_float4(a10.x - a00.x, a10.z, b10.x, b10.z); qY.c10 = make_float4(a10.y - a00.y, a10.w, b10.y, b10.w);
         qX.c01 = make_float4(a01.x - a00.x, a01.z, b01.x, b01.z); qY.c01 = make_float4(a01.y - a00.y, a01.w, b01.y, b01.w);
         qX.c11 = make_float4(a11.x - a00.x, a11.z, b11.x, b11.z); qY.c11 = make_float4(a11.y - a00.y, a11.w, b11.y, b11.w);
-        float ty = ((float)sub_y + 0.5f) / (float)r;
-        W4f wy = value_weights_f(ty, (float)gm.hy), dy = slope_weights_f(ty, (float)gm.ihy);
+        float ty = ((float)sub_y + 0.5f) * ir;
+        W4f wy = value_weights_f(ty, gm.hyf), dy = slope_weights_f(ty, gm.ihyf);
         for (int sx = 0; sx < r; ++sx) {
-            float tx = ((float)sx + 0.5f) / (float)r;
-            W4f wx = value_weights_f(tx, (float)gm.hx), dx = slope_weights_f(tx, (float)gm.ihx);
+            float tx = ((float)sx + 0.5f) * ir;
+            W4f wx = value_weights_f(tx, gm.hxf), dx = slope_weights_f(tx, gm.ihxf);
             float Xx, Xy, Yx, Yy;
             herm_grad_f(qX, wx, wy, dx, dy, Xx, Xy);
             herm_grad_f(qY, wx, wy, dx, dy, Yx, Yy);
-            double A = Xx, B = Yy, Cc = Xy, E = Yx;
-            double dev = fabs(A + B + A * B - Cc * E);
-            unsigned long long bits = (unsigned long long)__double_as_longlong(dev);
-            best = bits > best ? bits : best;
+            F2 dev = abs_det_deviation(Xx, Yy, Xy, Yx);
+            if (f2_greater(dev, best)) best = dev;
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
-        unsigned long long v = __shfl_xor_sync(0xffffffffu, best, o);
-        best = v > best ? v : best;
+        F2 v;
+        v.hi = __shfl_xor_sync(0xffffffffu, best.hi, o);
+        v.lo = __shfl_xor_sync(0xffffffffu, best.lo, o);
+        if (f2_greater(v, best)) best = v;
     }
     if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = best;
     __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned long long m = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = wmax[w] > m ? wmax[w] : m;
-        atomicMax(result, m);
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+            if (f2_greater(wmax[w], best)) best = wmax[w];
+        double dev = (double)best.hi + (double)best.lo;   // non-negative: its bits order like its value
+        atomicMax(result, (unsigned long long)__double_as_longlong(dev));
     }
 }
 
 cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_result, cudaStream_t s)
 {
+    if (r <= 0 || gm.N * r > 0x7fffffffLL) return cudaErrorInvalidValue;
     cudaError_t e = cudaMemsetAsync(d_result, 0, sizeof(double), s);
     if (e != cudaSuccess) return e;
     long long total = gm.N * r;
     long long need = (total + 255) / 256;
     unsigned blocks = (unsigned)(need < 152 * 8 ? need : 152 * 8);
-    k_incomp_m<<<blocks, 256, 0, s>>>(gm, r, map, reinterpret_cast<unsigned long long*>(d_result));
+    k_incomp_m<<<blocks, 256, 0, s>>>(gm, r, 1.0f / (float)r, map, reinterpret_cast<unsigned long long*>(d_result));
     return cudaGetLastError();
 }
 
@@ -396,19 +438,19 @@ __global__ void __launch_bounds__(256) k_sample_m(Grid gm, Grid go, Grid gf, int
                                                   const float4* __restrict__ map, const float4* __restrict__ W,
                                                   T* __restrict__ out)
 {
-    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= go.N) return;
-    int iX = (int)(i % go.NX), iY = (int)(i / go.NX);
+    const int iX = blockIdx.x * blockDim.x + threadIdx.x, iY = blockIdx.y;
+    if (iX >= go.NX) return;
+    const long long i = (long long)iY * go.NX + iX;
     // position on the map grid: node (iX / ro) + fraction (iX % ro) / ro
     int mx = iX / ro, my = iY / ro;
-    float ox = (float)(iX - mx * ro) * (float)go.hx, oy = (float)(iY - my * ro) * (float)go.hy;
+    float ox = (float)(iX - mx * ro) * go.hxf, oy = (float)(iY - my * ro) * go.hyf;
     float dx, dy;
     map_disp_f(map, gm, locate_rel(gm, mx, my, ox, oy), 0.0f, 0.0f, dx, dy);
     // on the fine grid the output point is node iX * rf
     CellF c = locate_rel(gf, iX * rf, iY * rf, dx, dy);
     Q4 q;
     q.c00 = __ldg(W + c.i00); q.c10 = __ldg(W + c.i10); q.c01 = __ldg(W + c.i01); q.c11 = __ldg(W + c.i11);
-    float v = herm_value_f(q, value_weights_f(c.tx, (float)gf.hx), value_weights_f(c.ty, (float)gf.hy));
+    float v = herm_value_f(q, value_weights_f(c.tx, gf.hxf), value_weights_f(c.ty, gf.hyf));
     out[i] = (T)v;
 }
 
@@ -416,80 +458,160 @@ cudaError_t launch_sample_m(const Grid& gm, const Grid& go, const Grid& gf, cons
                             float* out_f, double* out_d, cudaStream_t s)
 {
     int ro = go.NX / gm.NX, rf = gf.NX / go.NX;
-    unsigned blocks = (unsigned)((go.N + 255) / 256);
+    if (go.NY > 65535) return cudaErrorInvalidValue;
+    dim3 blocks((unsigned)((go.NX + 255) / 256), (unsigned)go.NY);
     if (out_f) k_sample_m<float><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, map, W, out_f);
     else k_sample_m<double><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, map, W, out_d);
     return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
-// tracers: FP64 positions, FP32 velocities (psiA = level 1 = t_n, psiB =
-// Lagrange t_{n+1/2} combination, psi0 = t_{n+1})
+// tracers.  A coordinate is held as 64-bit fixed point, P = (x - b0) / W * 2^64
+// (mod 2^64), so the periodic wrap is unsigned overflow, the cell and its
+// fraction are integer operations (cell = hi64(P * N), fraction = top bits of
+// lo64(P * N)), and the stage positions are FP32 offsets from that cell.  The
+// RK displacement D (FP32, length units) is added as the exact fixed-point
+// number nearest D * 2^64 / W, the scale 2^32 / W carried as an FP32 pair;
+// positions therefore accumulate with 2^-64 resolution and no FP64 work.
+// Velocities are FP32 (psiA = level 1 = t_n, psiB = Lagrange t_{n+1/2}
+// combination, psi0 = t_{n+1}); stages as Particle_advect
+// (src/numerical/cmm-particles.cu:159-183).
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long fix_increment(float d, float2 sc)
+{
+    float sh = __fmul_rn(d, sc.x);
+    float sl = __fadd_rn(fmaf(d, sc.x, -sh), __fmul_rn(d, sc.y));   // d * 2^32 / W = sh + sl
+    float n = rintf(sh);
+    float r = __fadd_rn(__fsub_rn(sh, n), sl);                       // |r| <= 0.5 + 2^-20
+    unsigned long long hi = (unsigned long long)(long long)__float2int_rn(n);   // saturates beyond W / 2
+    unsigned long long lo = (unsigned long long)(long long)__float2int_rn(r * 2147483648.0f);
+    return (hi << 32) + (lo << 1);
+}
+
+__device__ __forceinline__ void fix_cell(unsigned long long P, int n, int& cell, float& frac)
+{
+    cell = (int)__umul64hi(P, (unsigned long long)n);
+    frac = (float)(unsigned)((P * (unsigned long long)n) >> 40) * 5.9604644775390625e-8f;   // 24 bits * 2^-24
+}
+
 template <int TI>
-__global__ void __launch_bounds__(256) k_particles_m(Grid gp, double* pos, int num, const float4* __restrict__ psiA,
-                                                     const float4* __restrict__ psiB, const float4* __restrict__ psi0,
-                                                     double dt)
+__global__ void __launch_bounds__(256) k_particles_m(Grid gp, ulonglong2* __restrict__ pos, int num,
+                                                     const float4* __restrict__ psiA, const float4* __restrict__ psiB,
+                                                     const float4* __restrict__ psi0, float dt, float2 scx, float2 scy)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= num) return;
-    double px = pos[2 * i], py = pos[2 * i + 1];
-    float k1x, k1y;
-    velocity_f(psiA, gp, locate_abs(gp, px, py), k1x, k1y);
+    ulonglong2 P = pos[i];
+    int bx, by;
+    float tx, ty;
+    fix_cell(P.x, gp.NX, bx, tx);
+    fix_cell(P.y, gp.NY, by, ty);
+    float k1x, k1y, Dx, Dy;
+    velocity_f(psiA, gp, locate_q(gp, bx, by, tx, ty), k1x, k1y);
     if (TI == 10) {
-        px += dt * k1x;
-        py += dt * k1y;
+        Dx = dt * k1x;
+        Dy = dt * k1y;
     } else if (TI == 20) {
         float k2x, k2y;
-        velocity_f(psi0, gp, locate_abs(gp, px + dt * k1x, py + dt * k1y), k2x, k2y);
-        px += dt * (double)(k1x + k2x) * 0.5;
-        py += dt * (double)(k1y + k2y) * 0.5;
+        velocity_f(psi0, gp, locate_q(gp, bx, by, fmaf(dt * k1x, gp.ihxf, tx), fmaf(dt * k1y, gp.ihyf, ty)), k2x, k2y);
+        Dx = dt * (k1x + k2x) * 0.5f;
+        Dy = dt * (k1y + k2y) * 0.5f;
     } else {
         float k2x, k2y, k3x, k3y;
-        velocity_f(psiB, gp, locate_abs(gp, px + 0.5 * dt * k1x, py + 0.5 * dt * k1y), k2x, k2y);
-        velocity_f(psi0, gp, locate_abs(gp, px - dt * k1x + 2.0 * dt * k2x, py - dt * k1y + 2.0 * dt * k2y), k3x, k3y);
-        px += dt * (double)(k1x + 4.0f * k2x + k3x) / 6.0;
-        py += dt * (double)(k1y + 4.0f * k2y + k3y) / 6.0;
+        velocity_f(psiB, gp, locate_q(gp, bx, by, fmaf(0.5f * dt * k1x, gp.ihxf, tx), fmaf(0.5f * dt * k1y, gp.ihyf, ty)),
+                   k2x, k2y);
+        velocity_f(psi0, gp,
+                   locate_q(gp, bx, by, fmaf(dt * fmaf(2.0f, k2x, -k1x), gp.ihxf, tx),
+                            fmaf(dt * fmaf(2.0f, k2y, -k1y), gp.ihyf, ty)),
+                   k3x, k3y);
+        Dx = dt * (k1x + 4.0f * k2x + k3x) * (1.0f / 6.0f);
+        Dy = dt * (k1y + 4.0f * k2y + k3y) * (1.0f / 6.0f);
     }
-    pos[2 * i] = wrap(px, gp.b0, gp.Wx);
-    pos[2 * i + 1] = wrap(py, gp.b2, gp.Wy);
+    P.x += fix_increment(Dx, scx);
+    P.y += fix_increment(Dy, scy);
+    pos[i] = P;
 }
 
-cudaError_t launch_particles_m(const Grid& gp, double* pos, int num, const float4* psiA, const float4* psiB,
-                               const float4* psi0, double dt, int ti, cudaStream_t s)
+static float2 fix_scale(double W)
+{
+    double c = 4294967296.0 / W;
+    float hi = (float)c;
+    return make_float2(hi, (float)(c - (double)hi));
+}
+
+cudaError_t launch_particles_m(const Grid& gp, unsigned long long* pos, int num, const float4* psiA,
+                               const float4* psiB, const float4* psi0, double dt, int ti, cudaStream_t s)
 {
     if (num <= 0) return cudaSuccess;
     unsigned blocks = (unsigned)((num + 255) / 256);
-    if (ti == 10) k_particles_m<10><<<blocks, 256, 0, s>>>(gp, pos, num, psiA, psiB, psi0, dt);
-    else if (ti == 20) k_particles_m<20><<<blocks, 256, 0, s>>>(gp, pos, num, psiA, psiB, psi0, dt);
-    else if (ti == 30) k_particles_m<30><<<blocks, 256, 0, s>>>(gp, pos, num, psiA, psiB, psi0, dt);
+    ulonglong2* P = reinterpret_cast<ulonglong2*>(pos);
+    float2 sx = fix_scale(gp.Wx), sy = fix_scale(gp.Wy);
+    float d = (float)dt;
+    if (ti == 10) k_particles_m<10><<<blocks, 256, 0, s>>>(gp, P, num, psiA, psiB, psi0, d, sx, sy);
+    else if (ti == 20) k_particles_m<20><<<blocks, 256, 0, s>>>(gp, P, num, psiA, psiB, psi0, d, sx, sy);
+    else if (ti == 30) k_particles_m<30><<<blocks, 256, 0, s>>>(gp, P, num, psiA, psiB, psi0, d, sx, sy);
     else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+// FP64 positions (reference layout, interleaved x, y) <-> fixed point
+__global__ void k_pos_to_fix(const double* __restrict__ pos, long long n2, Grid g, unsigned long long* __restrict__ out)
+{
+    long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (j >= n2) return;
+    const bool y = j & 1;
+    double t = (pos[j] - (y ? g.b2 : g.b0)) / (y ? g.Wy : g.Wx);
+    t -= floor(t);
+    double v = t * 18446744073709551616.0;
+    out[j] = v >= 18446744073709551616.0 ? 0ull : __double2ull_rn(v);
+}
+
+__global__ void k_fix_to_pos(const unsigned long long* __restrict__ in, long long n2, Grid g, double* __restrict__ pos)
+{
+    long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (j >= n2) return;
+    const bool y = j & 1;
+    pos[j] = (y ? g.b2 : g.b0) + __ull2double_rn(in[j]) * ((y ? g.Wy : g.Wx) * 5.42101086242752217e-20);
+}
+
+cudaError_t launch_pos_to_fix(const double* pos, int num, const Grid& g, unsigned long long* out, cudaStream_t s)
+{
+    long long n2 = 2LL * num;
+    if (n2 <= 0) return cudaSuccess;
+    k_pos_to_fix<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(pos, n2, g, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fix_to_pos(const unsigned long long* in, int num, const Grid& g, double* pos, cudaStream_t s)
+{
+    long long n2 = 2LL * num;
+    if (n2 <= 0) return cudaSuccess;
+    k_fix_to_pos<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(in, n2, g, pos);
     return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
 // FP32 spectral step of the psi solve and layout conversions
 // ---------------------------------------------------------------------------
-__global__ void k_spec_psi_f(const float2* __restrict__ Fv, Grid gv, Grid gp, float freq, float2* __restrict__ out4)
+// (integer forms of the reference's "index > N/2.0" tests: 2*index > N)
+__global__ void k_spec_psi_f(const float2* __restrict__ Fv, Grid gv, Grid gp, float freq, float inv_nv,
+                             float2* __restrict__ out4)
 {
-    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= gp.Nfft) return;
-    int iXc = (int)(i % gp.NX_fft), iYc = (int)(i / gp.NX_fft);
+    const int iXc = blockIdx.x * blockDim.x + threadIdx.x, iYc = blockIdx.y;
+    if (iXc >= gp.NX_fft) return;
+    const long long i = (long long)iYc * gp.NX_fft + iXc;
+    const bool hx = 2 * iXc > gp.NX, hy = 2 * iYc > gp.NY;
+    const int fX = hx ? gp.NX - iXc : iXc, fY = hy ? gp.NY - iYc : iYc;   // |frequency| on the psi grid
     float2 P = make_float2(0.f, 0.f);
-    bool outside = (iXc + (iXc > gp.NX / 2.0) * (gp.NX - 2 * iXc) > gv.NX / 2.0) ||
-                   (iYc + (iYc > gp.NY / 2.0) * (gp.NY - 2 * iYc) > gv.NY / 2.0);
-    if (!outside) {
-        int iXs = iXc + (iXc > gp.NX / 2.0) * (gv.NX - gp.NX);
-        int iYs = iYc + (iYc > gp.NY / 2.0) * (gv.NY - gp.NY);
+    if (!(2 * fX > gv.NX || 2 * fY > gv.NY)) {
+        int iXs = iXc + (hx ? gv.NX - gp.NX : 0);
+        int iYs = iYc + (hy ? gv.NY - gp.NY : 0);
         float2 f = Fv[(long long)iYs * gv.NX_fft + iXs];
-        float inv = (float)(1.0 / (double)gv.N);
-        P = make_float2(f.x * inv, f.y * inv);
+        P = make_float2(f.x * inv_nv, f.y * inv_nv);
     }
-    int fX = iXc + (iXc > gp.NX / 2.0) * (gp.NX - 2 * iXc);
-    int fY = iYc + (iYc > gp.NY / 2.0) * (gp.NY - 2 * iYc);
     if ((float)(fX * fX + fY * fY) > freq * freq || i == 0) P = make_float2(0.f, 0.f);
-    float kx = (float)(gp.kfx * (iXc - (iXc > gp.NX / 2) * gp.NX));
-    float ky = (float)(gp.kfy * (iYc - (iYc > gp.NY / 2) * gp.NY));
+    float kx = gp.kfxf * (float)(hx ? iXc - gp.NX : iXc);
+    float ky = gp.kfyf * (float)(hy ? iYc - gp.NY : iYc);
     if (iXc == 0 && iYc == 0) P = make_float2(0.f, 0.f);
     else {
         float ik2 = 1.0f / (kx * kx + ky * ky);
@@ -504,7 +626,9 @@ __global__ void k_spec_psi_f(const float2* __restrict__ Fv, Grid gv, Grid gp, fl
 
 cudaError_t launch_spec_psi_f(const float2* Fv, const Grid& gv, const Grid& gp, double freq, float2* out4, cudaStream_t s)
 {
-    k_spec_psi_f<<<(unsigned)((gp.Nfft + 255) / 256), 256, 0, s>>>(Fv, gv, gp, (float)freq, out4);
+    if (gp.NY > 65535) return cudaErrorInvalidValue;
+    dim3 blocks((unsigned)((gp.NX_fft + 255) / 256), (unsigned)gp.NY);
+    k_spec_psi_f<<<blocks, 256, 0, s>>>(Fv, gv, gp, (float)freq, (float)(1.0 / (double)gv.N), out4);
     return cudaGetLastError();
 }
 

@@ -217,6 +217,11 @@ int EulerSim::alloc()
             (rc = falloc((void**)&spec4f_, sizeof(float2) * 4 * (size_t)gp.Nfft)))
             return rc;
         for (int l = 0; l < L; ++l) if ((rc = falloc((void**)&psim_[l], psib))) return rc;
+        for (auto& p : s.particles_advected) {
+            unsigned long long* d = nullptr;
+            if ((rc = falloc((void**)&d, sizeof(unsigned long long) * 2 * (size_t)std::max(p.num, 1)))) return rc;
+            partfix_.push_back(d);
+        }
         if (stack_cap_ > 0 && (rc = falloc((void**)&stackm_, mapb * stack_cap_))) return rc;
         int nv[2] = {gv.NY, gv.NX}, np[2] = {gp.NY, gp.NX};
         if (cufftPlanMany(&r2c_v_, 2, nv, nullptr, 1, 0, nullptr, 1, 0, CUFFT_R2C, 1) != CUFFT_SUCCESS ||
@@ -246,6 +251,8 @@ void EulerSim::release()
     f(real_buf_); f(spec_); f(spec4_); f(red_); f(d_scal_); f(d_params_); f(d_rand_);
     for (auto p : parts) f(p);
     parts.clear();
+    for (auto p : partfix_) f(p);
+    partfix_.clear();
     f(mapm_); f(mapm_new_); f(psiA_); f(psiB_); f(wfm_); f(stackm_); f(realf_); f(specf_); f(spec4f_);
     for (int l = 0; l < kMaxLagrange; ++l) { f(psim_[l]); psim_[l] = nullptr; }
     mapm_ = mapm_new_ = psiA_ = psiB_ = wfm_ = stackm_ = nullptr;
@@ -323,6 +330,8 @@ int EulerSim::sync_fp64_views()
     CMM_LAUNCH(1, launch_map_to_planes(mapm_, gc, ChiX, ChiY, stream));
     for (int l = 0; l < L; ++l) CMM_LAUNCH(1, launch_float4_to_planes(psim_[l], gp.N, psi[l], stream));
     CMM_LAUNCH(1, launch_float4_to_planes(wfm_, gf.N, wfine, stream));
+    for (size_t i = 0; i < partfix_.size(); ++i)
+        CMM_LAUNCH(1, launch_fix_to_pos(partfix_[i], s.particles_advected[i].num, gp, parts[i], stream));
     return kOk;
 }
 
@@ -494,7 +503,7 @@ int EulerSim::advect_particles(int lcl)
                 CMM_LAUNCH(1, launch_precombine(psim_, L, Lp12, nullptr, gp.N, psiB_, nullptr, stream));
                 combined = true;
             }
-            cudaError_t e = launch_particles_m(gp, parts[i], p.num, psim_[1], psiB_, psim_[0], dt_vec_[lcl + 1],
+            cudaError_t e = launch_particles_m(gp, partfix_[i], p.num, psim_[1], psiB_, psim_[0], dt_vec_[lcl + 1],
                                                p.time_integration_num, stream);
             kernel_launches++;
             if (e == cudaErrorInvalidValue) { err = "particle time integration " + p.time_integration + " is not built"; return kErrUnsupported; }
@@ -589,6 +598,8 @@ int EulerSim::init()
         if ((rc = reset_map())) return rc;
     }
     if ((rc = init_particles())) return rc;
+    for (size_t i = 0; i < partfix_.size(); ++i)
+        CMM_LAUNCH(1, launch_pos_to_fix(parts[i], s.particles_advected[i].num, gp, partfix_[i], stream));
 
     t_vec_.assign((size_t)s.iter_max() + L + 8, 0.0);
     dt_vec_.assign(t_vec_.size(), dt);

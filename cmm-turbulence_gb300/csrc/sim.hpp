@@ -1,4 +1,5 @@
-// sim.hpp -- the 2D Euler CMM simulation context on one GPU (FP64 plain form).
+// sim.hpp -- the 2D Euler CMM simulation context on one GPU (plain FP64 and
+// mixed-precision forms).
 //
 // Owns every device buffer; all work is ordered on one CUDA stream.  The only
 // host synchronisation per loop iteration is the 8-byte read of the
@@ -116,6 +117,7 @@ private:
     float4* psiB_ = nullptr;
     float4* wfm_ = nullptr;          // fine vorticity nodes
     float4* stackm_ = nullptr;       // n maps, 2*Nc float4 each
+    std::vector<unsigned long long*> partfix_;   // tracer positions, 64-bit fixed point (x, y interleaved)
     float* realf_ = nullptr;         // FP32 real scratch (4 planes of the largest grid)
     float2* specf_ = nullptr;        // FP32 complex scratch
     float2* spec4f_ = nullptr;       // 4 FP32 spectra

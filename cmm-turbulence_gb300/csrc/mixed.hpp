@@ -32,9 +32,10 @@ cudaError_t launch_advect_m(const AdvectMArgs& a, cudaStream_t s);
 // max |det grad X - 1| on the half-shifted check grid with r = Ncheck / Nmap points per cell and axis
 // (r * Nmap^2 < 2^31)
 cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_result, cudaStream_t s);
-// omega_0 through current map + n stacked maps (n * 2*Nc float4), FP64 positions
+// omega_0 through current map + n stacked maps (n * 2*Nc float4), 64-bit fixed-point
+// positions; a discrete initial field (src.kind 3) is read from its FP32 Hermite nodes disc
 cudaError_t launch_compose_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
-                             const InitSource& src, double* out, cudaStream_t s);
+                             const InitSource& src, const float4* disc, double* out, cudaStream_t s);
 // W(x + d(x)) on grid go (Ngo multiple of Nmap, Nf multiple of Ngo); out_f or out_d
 cudaError_t launch_sample_m(const Grid& gm, const Grid& go, const Grid& gf, const float4* map, const float4* W,
                             float* out_f, double* out_d, cudaStream_t s);

@@ -55,6 +55,7 @@ struct CellF {
 
 __device__ __forceinline__ int wrap_index(int i, int n)
 {
+    if ((unsigned)i < (unsigned)n) return i;   // the common case: no integer division
     int r = i % n;
     return r < 0 ? r + n : r;
 }
@@ -328,10 +329,49 @@ __device__ __forceinline__ bool f2_greater(const F2& x, const F2& y)
     return x.hi > y.hi || (x.hi == y.hi && x.lo > y.lo);
 }
 
+// y-contraction of one Hermite column pair of a map component at fixed ty:
+// at each of the cell's two x-columns j, V_j = value, S_j = x-slope (both at
+// ty), DV_j / DS_j = their y-derivatives.  Corner value planes are taken
+// relative to f00 (slope weights sum to zero; values follow by adding f00).
+struct YCol { float V0, V1, S0, S1, DV0, DV1, DS0, DS1; };
+
+__device__ __forceinline__ YCol ycontract(float f00, float f10, float f01, float f11, float x00, float x10, float x01,
+                                          float x11, float y00, float y10, float y01, float y11, float z00, float z10,
+                                          float z01, float z11, const W4f& wy, const W4f& dy)
+{
+    // corners: (x0,y0) = 00, (x1,y0) = 10, (x0,y1) = 01, (x1,y1) = 11; x = f_x, y = f_y, z = f_xy
+    YCol c;
+    c.V0 = fmaf(wy.w3, y01, fmaf(wy.w2, y00, fmaf(wy.w1, f01, wy.w0 * f00)));
+    c.V1 = fmaf(wy.w3, y11, fmaf(wy.w2, y10, fmaf(wy.w1, f11, wy.w0 * f10)));
+    c.S0 = fmaf(wy.w3, z01, fmaf(wy.w2, z00, fmaf(wy.w1, x01, wy.w0 * x00)));
+    c.S1 = fmaf(wy.w3, z11, fmaf(wy.w2, z10, fmaf(wy.w1, x11, wy.w0 * x10)));
+    c.DV0 = fmaf(dy.w3, y01, fmaf(dy.w2, y00, fmaf(dy.w1, f01, dy.w0 * f00)));
+    c.DV1 = fmaf(dy.w3, y11, fmaf(dy.w2, y10, fmaf(dy.w1, f11, dy.w0 * f10)));
+    c.DS0 = fmaf(dy.w3, z01, fmaf(dy.w2, z00, fmaf(dy.w1, x01, dy.w0 * x00)));
+    c.DS1 = fmaf(dy.w3, z11, fmaf(dy.w2, z10, fmaf(dy.w1, x11, dy.w0 * x10)));
+    return c;
+}
+
+// gradient at tx from a y-contracted column pair (wx: value weights, dx: slope weights at tx)
+__device__ __forceinline__ void ycol_grad(const YCol& c, const W4f& wx, const W4f& dx, float& gx, float& gy)
+{
+    gx = fmaf(dx.w3, c.S1, fmaf(dx.w2, c.S0, fmaf(dx.w1, c.V1, dx.w0 * c.V0)));
+    gy = fmaf(wx.w3, c.DS1, fmaf(wx.w2, c.DS0, fmaf(wx.w1, c.DV1, wx.w0 * c.DV0)));
+}
+
+constexpr int kMaxCheckRatio = 32;   // check points per map cell and axis
+
 __global__ void __launch_bounds__(256) k_incomp_m(Grid gm, int r, float ir, const float4* __restrict__ M,
                                                   unsigned long long* result)
 {
+    __shared__ W4f sw[kMaxCheckRatio], sd[kMaxCheckRatio];   // x-weights of the r check columns
     __shared__ F2 wmax[8];
+    if ((int)threadIdx.x < r) {
+        float tx = ((float)threadIdx.x + 0.5f) * ir;
+        sw[threadIdx.x] = value_weights_f(tx, gm.hxf);
+        sd[threadIdx.x] = slope_weights_f(tx, gm.ihxf);
+    }
+    __syncthreads();
     F2 best = {0.0f, 0.0f};
     const int total = (int)gm.N * r;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
@@ -344,21 +384,17 @@ __global__ void __launch_bounds__(256) k_incomp_m(Grid gm, int r, float ir, cons
         float4 a10 = __ldg(M + 2 * i10), b10 = __ldg(M + 2 * i10 + 1);
         float4 a01 = __ldg(M + 2 * i01), b01 = __ldg(M + 2 * i01 + 1);
         float4 a11 = __ldg(M + 2 * i11), b11 = __ldg(M + 2 * i11 + 1);
-        // value planes relative to corner 00: slope weights sum to zero, so the
-        // gradient is unchanged and FP32 keeps the precision of the differences
-        Q4 qX, qY;
-        qX.c00 = make_float4(0.0f, a00.z, b00.x, b00.z); qY.c00 = make_float4(0.0f, a00.w, b00.y, b00.w);
-        qX.c10 = make_float4(a10.x - a00.x, a10.z, b10.x, b10.z); qY.c10 = make_float4(a10.y - a00.y, a10.w, b10.y, b10.w);
-        qX.c01 = make_float4(a01.x - a00.x, a01.z, b01.x, b01.z); qY.c01 = make_float4(a01.y - a00.y, a01.w, b01.y, b01.w);
-        qX.c11 = make_float4(a11.x - a00.x, a11.z, b11.x, b11.z); qY.c11 = make_float4(a11.y - a00.y, a11.w, b11.y, b11.w);
         float ty = ((float)sub_y + 0.5f) * ir;
         W4f wy = value_weights_f(ty, gm.hyf), dy = slope_weights_f(ty, gm.ihyf);
+        // X: f = a.x, f_x = a.z, f_y = b.x, f_xy = b.z;  Y: f = a.y, f_x = a.w, f_y = b.y, f_xy = b.w
+        YCol cX = ycontract(0.0f, a10.x - a00.x, a01.x - a00.x, a11.x - a00.x, a00.z, a10.z, a01.z, a11.z,
+                            b00.x, b10.x, b01.x, b11.x, b00.z, b10.z, b01.z, b11.z, wy, dy);
+        YCol cY = ycontract(0.0f, a10.y - a00.y, a01.y - a00.y, a11.y - a00.y, a00.w, a10.w, a01.w, a11.w,
+                            b00.y, b10.y, b01.y, b11.y, b00.w, b10.w, b01.w, b11.w, wy, dy);
         for (int sx = 0; sx < r; ++sx) {
-            float tx = ((float)sx + 0.5f) * ir;
-            W4f wx = value_weights_f(tx, gm.hxf), dx = slope_weights_f(tx, gm.ihxf);
             float Xx, Xy, Yx, Yy;
-            herm_grad_f(qX, wx, wy, dx, dy, Xx, Xy);
-            herm_grad_f(qY, wx, wy, dx, dy, Yx, Yy);
+            ycol_grad(cX, sw[sx], sd[sx], Xx, Xy);
+            ycol_grad(cY, sw[sx], sd[sx], Yx, Yy);
             F2 dev = abs_det_deviation(Xx, Yy, Xy, Yx);
             if (f2_greater(dev, best)) best = dev;
         }
@@ -381,7 +417,7 @@ __global__ void __launch_bounds__(256) k_incomp_m(Grid gm, int r, float ir, cons
 
 cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_result, cudaStream_t s)
 {
-    if (r <= 0 || gm.N * r > 0x7fffffffLL) return cudaErrorInvalidValue;
+    if (r <= 0 || r > kMaxCheckRatio || gm.N * r > 0x7fffffffLL) return cudaErrorInvalidValue;
     cudaError_t e = cudaMemsetAsync(d_result, 0, sizeof(double), s);
     if (e != cudaSuccess) return e;
     long long total = gm.N * r;
@@ -392,90 +428,13 @@ cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_
 }
 
 // ---------------------------------------------------------------------------
-// remap-time composition with FP64 positions: every target point is chased
-// through the current map and all stacked maps (x <- x + d(x)); the FP32
-// displacement is added to the FP64 position once per map
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_compose_m(Grid gm, Grid gt, const float4* __restrict__ map,
-                                                   const float4* __restrict__ stack, int n_maps, InitSource src,
-                                                   double* __restrict__ out)
-{
-    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= gt.N) return;
-    int iX = (int)(i % gt.NX), iY = (int)(i / gt.NX);
-    double x = gt.b0 + iX * gt.hx, y = gt.b2 + iY * gt.hy;
-    float dx, dy;
-    map_disp_f(map, gm, locate_abs(gm, x, y), 0.0f, 0.0f, dx, dy);
-    x += (double)dx;
-    y += (double)dy;
-    for (int m = n_maps - 1; m >= 0; --m) {
-        map_disp_f(stack + 2 * (long long)m * gm.N, gm, locate_abs(gm, x, y), 0.0f, 0.0f, dx, dy);
-        x += (double)dx;
-        y += (double)dy;
-    }
-    x = wrap(x, gm.b0, gm.Wx);
-    y = wrap(y, gm.b2, gm.Wy);
-    double v;
-    if (src.kind == 3) v = interp_value(src.discrete, src.gd, x, y);
-    else if (src.kind == 1) v = init_scalar(x, y, src.ic_num);
-    else v = init_vorticity(x, y, src.ic_num, src.params, src.rand_table);
-    out[i] = v;
-}
-
-cudaError_t launch_compose_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
-                             const InitSource& src, double* out, cudaStream_t s)
-{
-    k_compose_m<<<(unsigned)((gt.N + 255) / 256), 256, 0, s>>>(gm, gt, map, stack, n_maps, src, out);
-    return cudaGetLastError();
-}
-
-// ---------------------------------------------------------------------------
-// omega(x) = W(x + d(x)) on an output grid whose spacing divides the map's and
-// the fine grid's (integer ratios): positions are integer node + FP32 offset
-// ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(256) k_sample_m(Grid gm, Grid go, Grid gf, int ro, int rf,
-                                                  const float4* __restrict__ map, const float4* __restrict__ W,
-                                                  T* __restrict__ out)
-{
-    const int iX = blockIdx.x * blockDim.x + threadIdx.x, iY = blockIdx.y;
-    if (iX >= go.NX) return;
-    const long long i = (long long)iY * go.NX + iX;
-    // position on the map grid: node (iX / ro) + fraction (iX % ro) / ro
-    int mx = iX / ro, my = iY / ro;
-    float ox = (float)(iX - mx * ro) * go.hxf, oy = (float)(iY - my * ro) * go.hyf;
-    float dx, dy;
-    map_disp_f(map, gm, locate_rel(gm, mx, my, ox, oy), 0.0f, 0.0f, dx, dy);
-    // on the fine grid the output point is node iX * rf
-    CellF c = locate_rel(gf, iX * rf, iY * rf, dx, dy);
-    Q4 q;
-    q.c00 = __ldg(W + c.i00); q.c10 = __ldg(W + c.i10); q.c01 = __ldg(W + c.i01); q.c11 = __ldg(W + c.i11);
-    float v = herm_value_f(q, value_weights_f(c.tx, gf.hxf), value_weights_f(c.ty, gf.hyf));
-    out[i] = (T)v;
-}
-
-cudaError_t launch_sample_m(const Grid& gm, const Grid& go, const Grid& gf, const float4* map, const float4* W,
-                            float* out_f, double* out_d, cudaStream_t s)
-{
-    int ro = go.NX / gm.NX, rf = gf.NX / go.NX;
-    if (go.NY > 65535) return cudaErrorInvalidValue;
-    dim3 blocks((unsigned)((go.NX + 255) / 256), (unsigned)go.NY);
-    if (out_f) k_sample_m<float><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, map, W, out_f);
-    else k_sample_m<double><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, map, W, out_d);
-    return cudaGetLastError();
-}
-
-// ---------------------------------------------------------------------------
-// tracers.  A coordinate is held as 64-bit fixed point, P = (x - b0) / W * 2^64
+// 64-bit fixed-point positions: a coordinate is P = (x - b0) / W * 2^64
 // (mod 2^64), so the periodic wrap is unsigned overflow, the cell and its
 // fraction are integer operations (cell = hi64(P * N), fraction = top bits of
-// lo64(P * N)), and the stage positions are FP32 offsets from that cell.  The
-// RK displacement D (FP32, length units) is added as the exact fixed-point
-// number nearest D * 2^64 / W, the scale 2^32 / W carried as an FP32 pair;
-// positions therefore accumulate with 2^-64 resolution and no FP64 work.
-// Velocities are FP32 (psiA = level 1 = t_n, psiB = Lagrange t_{n+1/2}
-// combination, psi0 = t_{n+1}); stages as Particle_advect
-// (src/numerical/cmm-particles.cu:159-183).
+// lo64(P * N)), and a displacement D (FP32, length units) is added as the
+// exact fixed-point number nearest D * 2^64 / W, the scale 2^32 / W carried
+// as an FP32 pair.  Positions accumulate with 2^-64 resolution (finer than
+// FP64's 2^-53 relative) and no FP64 instruction.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned long long fix_increment(float d, float2 sc)
 {
@@ -494,6 +453,149 @@ __device__ __forceinline__ void fix_cell(unsigned long long P, int n, int& cell,
     frac = (float)(unsigned)((P * (unsigned long long)n) >> 40) * 5.9604644775390625e-8f;   // 24 bits * 2^-24
 }
 
+static float2 fix_scale(double W)
+{
+    double c = 4294967296.0 / W;
+    float hi = (float)c;
+    return make_float2(hi, (float)(c - (double)hi));
+}
+
+// floor(2^64 / n): the fixed-point spacing of an n-point grid
+static unsigned long long fix_step(int n)
+{
+    if (n <= 1) return 0ull;
+    if ((n & (n - 1)) == 0) {
+        int l = 0;
+        while ((1 << l) < n) ++l;
+        return 1ull << (64 - l);
+    }
+    return ~0ull / (unsigned long long)n;
+}
+
+// ---------------------------------------------------------------------------
+// remap-time composition: every target node is chased through the current
+// map and all stacked maps (x <- x + d(x)) at 64-bit fixed-point positions;
+// omega_0 is then evaluated there (a discrete initial field from its FP32
+// Hermite nodes, an analytic one with its FP64 formula).  Target, map and
+// discrete grids span the same domain.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_compose_m(Grid gm, Grid gt, unsigned long long stx, unsigned long long sty,
+                                                   float2 scx, float2 scy, const float4* __restrict__ map,
+                                                   const float4* __restrict__ stack, int n_maps, InitSource src,
+                                                   const float4* __restrict__ disc, double* __restrict__ out)
+{
+    const int iX = blockIdx.x * blockDim.x + threadIdx.x, iY = blockIdx.y;
+    if (iX >= gt.NX) return;
+    unsigned long long Px = (unsigned long long)iX * stx, Py = (unsigned long long)iY * sty;
+    int cx, cy;
+    float tx, ty, dx, dy;
+    fix_cell(Px, gm.NX, cx, tx);
+    fix_cell(Py, gm.NY, cy, ty);
+    map_disp_f(map, gm, locate_q(gm, cx, cy, tx, ty), 0.0f, 0.0f, dx, dy);
+    Px += fix_increment(dx, scx);
+    Py += fix_increment(dy, scy);
+    for (int m = n_maps - 1; m >= 0; --m) {
+        fix_cell(Px, gm.NX, cx, tx);
+        fix_cell(Py, gm.NY, cy, ty);
+        map_disp_f(stack + 2 * (long long)m * gm.N, gm, locate_q(gm, cx, cy, tx, ty), 0.0f, 0.0f, dx, dy);
+        Px += fix_increment(dx, scx);
+        Py += fix_increment(dy, scy);
+    }
+    double v;
+    if (src.kind == 3) {
+        fix_cell(Px, src.gd.NX, cx, tx);
+        fix_cell(Py, src.gd.NY, cy, ty);
+        CellF c = locate_q(src.gd, cx, cy, tx, ty);
+        Q4 q;
+        q.c00 = __ldg(disc + c.i00); q.c10 = __ldg(disc + c.i10); q.c01 = __ldg(disc + c.i01); q.c11 = __ldg(disc + c.i11);
+        v = herm_value_f(q, value_weights_f(c.tx, src.gd.hxf), value_weights_f(c.ty, src.gd.hyf));
+    } else {
+        double x = gm.b0 + __ull2double_rn(Px) * (gm.Wx * 5.42101086242752217e-20);
+        double y = gm.b2 + __ull2double_rn(Py) * (gm.Wy * 5.42101086242752217e-20);
+        v = src.kind == 1 ? init_scalar(x, y, src.ic_num) : init_vorticity(x, y, src.ic_num, src.params, src.rand_table);
+    }
+    out[(long long)iY * gt.NX + iX] = v;
+}
+
+cudaError_t launch_compose_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
+                             const InitSource& src, const float4* disc, double* out, cudaStream_t s)
+{
+    if (gt.b0 != gm.b0 || gt.b2 != gm.b2 || gt.Wx != gm.Wx || gt.Wy != gm.Wy || gt.NY > 65535) return cudaErrorInvalidValue;
+    if (src.kind == 3 && (!disc || src.gd.b0 != gm.b0 || src.gd.b2 != gm.b2 || src.gd.Wx != gm.Wx || src.gd.Wy != gm.Wy))
+        return cudaErrorInvalidValue;
+    dim3 blocks((unsigned)((gt.NX + 255) / 256), (unsigned)gt.NY);
+    k_compose_m<<<blocks, 256, 0, s>>>(gm, gt, fix_step(gt.NX), fix_step(gt.NY), fix_scale(gm.Wx), fix_scale(gm.Wy),
+                                       map, stack, n_maps, src, disc, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// omega(x) = W(x + d(x)) on an output grid whose spacing divides the map's and
+// the fine grid's (integer ratios ro = No / Nm, rf = Nf / No).  One thread per
+// (map cell, output row): the cell's map corners are loaded and contracted in
+// y once, then the ro output points of the cell in that row are evaluated
+// (x-weights from a table); positions are integer node + FP32 offset.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_sample_m(Grid gm, Grid go, Grid gf, int ro, int rf, float iro,
+                                                  const float4* __restrict__ map, const float4* __restrict__ W,
+                                                  T* __restrict__ out)
+{
+    __shared__ W4f swx[kMaxCheckRatio];
+    if ((int)threadIdx.x < ro) swx[threadIdx.x] = value_weights_f((float)threadIdx.x * iro, gm.hxf);
+    __syncthreads();
+    const int mx = blockIdx.x * blockDim.x + threadIdx.x, iY = blockIdx.y;
+    if (mx >= gm.NX) return;
+    const int my = iY / ro, sy = iY - my * ro;
+    const int mx1 = mx + 1 == gm.NX ? 0 : mx + 1, my1 = my + 1 == gm.NY ? 0 : my + 1;
+    const int i00 = my * gm.NX + mx, i10 = my * gm.NX + mx1, i01 = my1 * gm.NX + mx, i11 = my1 * gm.NX + mx1;
+    float4 a00 = __ldg(map + 2 * i00), b00 = __ldg(map + 2 * i00 + 1);
+    float4 a10 = __ldg(map + 2 * i10), b10 = __ldg(map + 2 * i10 + 1);
+    float4 a01 = __ldg(map + 2 * i01), b01 = __ldg(map + 2 * i01 + 1);
+    float4 a11 = __ldg(map + 2 * i11), b11 = __ldg(map + 2 * i11 + 1);
+    const W4f wy = value_weights_f((float)sy * iro, gm.hyf);
+    // y-contracted value (V) and x-slope (S) of each component at the two x-columns
+    const float VX0 = fmaf(wy.w3, b01.x, fmaf(wy.w2, b00.x, fmaf(wy.w1, a01.x, wy.w0 * a00.x)));
+    const float VX1 = fmaf(wy.w3, b11.x, fmaf(wy.w2, b10.x, fmaf(wy.w1, a11.x, wy.w0 * a10.x)));
+    const float SX0 = fmaf(wy.w3, b01.z, fmaf(wy.w2, b00.z, fmaf(wy.w1, a01.z, wy.w0 * a00.z)));
+    const float SX1 = fmaf(wy.w3, b11.z, fmaf(wy.w2, b10.z, fmaf(wy.w1, a11.z, wy.w0 * a10.z)));
+    const float VY0 = fmaf(wy.w3, b01.y, fmaf(wy.w2, b00.y, fmaf(wy.w1, a01.y, wy.w0 * a00.y)));
+    const float VY1 = fmaf(wy.w3, b11.y, fmaf(wy.w2, b10.y, fmaf(wy.w1, a11.y, wy.w0 * a10.y)));
+    const float SY0 = fmaf(wy.w3, b01.w, fmaf(wy.w2, b00.w, fmaf(wy.w1, a01.w, wy.w0 * a00.w)));
+    const float SY1 = fmaf(wy.w3, b11.w, fmaf(wy.w2, b10.w, fmaf(wy.w1, a11.w, wy.w0 * a10.w)));
+    T* row = out + (long long)iY * go.NX;
+    for (int k = 0; k < ro; ++k) {
+        const W4f w = swx[k];
+        float dx = fmaf(w.w3, SX1, fmaf(w.w2, SX0, fmaf(w.w1, VX1, w.w0 * VX0)));
+        float dy = fmaf(w.w3, SY1, fmaf(w.w2, SY0, fmaf(w.w1, VY1, w.w0 * VY0)));
+        const int iX = mx * ro + k;
+        // on the fine grid the output point is node iX * rf
+        CellF c = locate_rel(gf, iX * rf, iY * rf, dx, dy);
+        Q4 q;
+        q.c00 = __ldg(W + c.i00); q.c10 = __ldg(W + c.i10); q.c01 = __ldg(W + c.i01); q.c11 = __ldg(W + c.i11);
+        row[iX] = (T)herm_value_f(q, value_weights_f(c.tx, gf.hxf), value_weights_f(c.ty, gf.hyf));
+    }
+}
+
+cudaError_t launch_sample_m(const Grid& gm, const Grid& go, const Grid& gf, const float4* map, const float4* W,
+                            float* out_f, double* out_d, cudaStream_t s)
+{
+    int ro = go.NX / gm.NX, rf = gf.NX / go.NX;
+    if (ro < 1 || ro > kMaxCheckRatio || ro * gm.NX != go.NX || ro * gm.NY != go.NY || go.NY > 65535)
+        return cudaErrorInvalidValue;
+    dim3 blocks((unsigned)((gm.NX + 255) / 256), (unsigned)go.NY);
+    float iro = 1.0f / (float)ro;
+    if (out_f) k_sample_m<float><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out_f);
+    else k_sample_m<double><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out_d);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// tracers at 64-bit fixed-point positions (see fix_increment): the stage
+// positions are FP32 offsets from the start cell, velocities are FP32
+// (psiA = level 1 = t_n, psiB = Lagrange t_{n+1/2} combination, psi0 =
+// t_{n+1}); stages as Particle_advect (src/numerical/cmm-particles.cu:159-183).
+// ---------------------------------------------------------------------------
 template <int TI>
 __global__ void __launch_bounds__(256) k_particles_m(Grid gp, ulonglong2* __restrict__ pos, int num,
                                                      const float4* __restrict__ psiA, const float4* __restrict__ psiB,
@@ -530,13 +632,6 @@ __global__ void __launch_bounds__(256) k_particles_m(Grid gp, ulonglong2* __rest
     P.x += fix_increment(Dx, scx);
     P.y += fix_increment(Dy, scy);
     pos[i] = P;
-}
-
-static float2 fix_scale(double W)
-{
-    double c = 4294967296.0 / W;
-    float hi = (float)c;
-    return make_float2(hi, (float)(c - (double)hi));
 }
 
 cudaError_t launch_particles_m(const Grid& gp, unsigned long long* pos, int num, const float4* psiA,

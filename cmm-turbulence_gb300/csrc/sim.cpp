@@ -217,6 +217,7 @@ int EulerSim::alloc()
             (rc = falloc((void**)&spec4f_, sizeof(float2) * 4 * (size_t)gp.Nfft)))
             return rc;
         for (int l = 0; l < L; ++l) if ((rc = falloc((void**)&psim_[l], psib))) return rc;
+        if (s.initial_discrete && (rc = falloc((void**)&wdiscm_, sizeof(float4) * (size_t)gd.N))) return rc;
         for (auto& p : s.particles_advected) {
             unsigned long long* d = nullptr;
             if ((rc = falloc((void**)&d, sizeof(unsigned long long) * 2 * (size_t)std::max(p.num, 1)))) return rc;
@@ -253,6 +254,7 @@ void EulerSim::release()
     parts.clear();
     for (auto p : partfix_) f(p);
     partfix_.clear();
+    f(wdiscm_); wdiscm_ = nullptr;
     f(mapm_); f(mapm_new_); f(psiA_); f(psiB_); f(wfm_); f(stackm_); f(realf_); f(specf_); f(spec4f_);
     for (int l = 0; l < kMaxLagrange; ++l) { f(psim_[l]); psim_[l] = nullptr; }
     mapm_ = mapm_new_ = psiA_ = psiB_ = wfm_ = stackm_ = nullptr;
@@ -282,9 +284,9 @@ int EulerSim::translate_ic()
     src.params = d_params_;
     src.rand_table = d_rand_;
     if (mixed_) {
-        // FP64 positions through the FP32 displacement stack, FP64 spectral
-        // Hermite construction, FP32 storage of the fine vorticity nodes
-        CMM_LAUNCH(1, launch_compose_m(gc, gf, mapm_, stackm_, n_maps_, src, real_buf_, stream));
+        // fixed-point positions through the FP32 displacement stack, FP64
+        // spectral Hermite construction, FP32 storage of the fine vorticity nodes
+        CMM_LAUNCH(1, launch_compose_m(gc, gf, mapm_, stackm_, n_maps_, src, wdiscm_, real_buf_, stream));
     } else {
         CMM_LAUNCH(1, launch_compose_sample(gc, gf, ChiX, ChiY, stack, n_maps_, src, real_buf_, stream));
     }
@@ -557,6 +559,7 @@ int EulerSim::init()
         CMM_FFT(cufftExecD2Z(pd_.d2z, real_buf_, reinterpret_cast<cufftDoubleComplex*>(spec_)));
         CMM_LAUNCH(1, launch_spec_hermite(spec_, gd, spec4_, stream));
         CMM_FFT(cufftExecZ2D(pd_.z2d4, reinterpret_cast<cufftDoubleComplex*>(spec4_), wdisc));
+        if (mixed_) CMM_LAUNCH(1, launch_planes_to_float4(nullptr, wdisc, gd.N, wdiscm_, stream));
         CMM_CUDA(cudaStreamSynchronize(stream));   // host_discrete_ may be released by the caller
     }
 

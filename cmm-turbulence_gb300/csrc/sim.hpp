@@ -116,6 +116,7 @@ private:
     float4* psiA_ = nullptr;         // Lagrange combinations of the psi levels
     float4* psiB_ = nullptr;
     float4* wfm_ = nullptr;          // fine vorticity nodes
+    float4* wdiscm_ = nullptr;       // discrete initial vorticity nodes (FP32 Hermite)
     float4* stackm_ = nullptr;       // n maps, 2*Nc float4 each
     std::vector<unsigned long long*> partfix_;   // tracer positions, 64-bit fixed point (x, y interleaved)
     float* realf_ = nullptr;         // FP32 real scratch (4 planes of the largest grid)

@@ -123,6 +123,7 @@ typedef struct {
     int max_maps;                 /* stack capacity (cpu_map_num) */
     int n_particle_sets;
     og_particle_set psets[8];
+    int simulation_type_num;      /* 0 = cmm_euler_2d, 2 = cmm_vlasov_poisson_1d */
 } og_settings;
 
 typedef struct og_state og_state;
@@ -134,10 +135,12 @@ void og_destroy(og_state* st);
 int og_set_discrete_initial(og_state* st, const double* values);
 /* particle initial positions (interleaved x,y) for set i */
 int og_set_particles(og_state* st, int i_set, const double* pos);
-/* initial state + Lagrange history (src/simulation/cmm-euler2d.cu:495-619) */
+/* initial state + Lagrange history (src/simulation/cmm-euler2d.cu:495-619,
+ * src/simulation/cmm-vlasov1d.cu:516-656); -1 if the Vlasov potential rejects the grids */
 int og_init(og_state* st);
-/* one loop iteration (src/simulation/cmm-euler2d.cu:750-897); dt_now from the
- * caller (compute_next_timestep). Returns 0 ok, 1 stack saturated (loop stops). */
+/* one loop iteration (src/simulation/cmm-euler2d.cu:750-897, cmm-vlasov1d.cu:782-960);
+ * dt_now from the caller (compute_next_timestep). Returns 0 ok, 1 stack saturated
+ * (loop stops), 2 Vlasov incompressibility blow-up (cmm-vlasov1d.cu:838-840). */
 int og_step(og_state* st, double dt_now, double* e_inc, int* remapped);
 
 /* state access (reference layouts) */
@@ -161,6 +164,24 @@ double og_max_vorticity(const og_state* st);
 /* debug globals (src/numerical/cmm-mesure.cu:217-249): grid form uses hx*hy, raw form /N */
 void og_stats_grid(const double* v, const og_grid* g, double* out4);
 void og_stats_raw(const double* v, long n, double* out4);
+/* ---------------- Vlasov-Poisson (og_vlasov.c) ---------------- */
+/* d_init_distirbution_function: src/simulation/cmm-init.cu:457-493 */
+double og_init_distribution(double x, double v, int ic_num);
+/* integral_v with its output aliasing row 0 of f: cmm-simulation-kernel.cu:570-586 */
+void og_integral_v(const double* f, double* rho, int nx, int ny, double hy);
+/* h(v) of compute_periodification_function on grid g (NY values): cmm-simulation-host.cu:478-494,534-571 */
+void og_periodification(const og_grid* g, double* h);
+/* evaluate_potential_from_density_hermite: cmm-simulation-host.cu:385-415; -1 if unsupported grids */
+int og_vlasov_potential(const double* ChiX, const double* ChiY, const double* f_fine, const og_grid* gmap,
+                        const og_grid* gvort, const og_grid* gfine, const og_grid* gpsi, int molly, double* psi_out);
+/* out[9] = {Etot, Ekin, Epot, Mass, Momentum, Emode1..4}: cmm-simulation-host.cu:639-664 */
+void og_vlasov_mesure(const double* f_coarse, const og_grid* gc, const double* psi, const og_grid* gp, double* out);
+void og_vlasov_state_mesure(const og_state* st, double* out);
+/* stack composition + sampling of initial field var_num (0 vorticity, 2 distribution function) */
+void og_compose_sample_var(const double* ChiX, const double* ChiY, const double* stack, int n, const og_grid* gm,
+                           const og_grid* gt, int var_num, int ic_num, const double* discrete, const og_grid* gd,
+                           double* out);
+
 /* ψ_x, ψ_y at particle positions (k_h_sample_points_dxdy, cmm-simulation-kernel.cu:138-155) */
 void og_sample_points_dxdy(const og_state* st, const double* pos, double* out, int num);
 

@@ -359,8 +359,9 @@ int og_set_particles(og_state* st, int i, const double* pos)
 
 /* apply_map_stack (direction -1) + k_h_sample_from_init: cmm-simulation-host.cu:112-128,
  * cmm-simulation-kernel.cu:342-373; stack = n maps of [X planes | Y planes] */
-void og_compose_sample(const double* ChiX, const double* ChiY, const double* stack, int n, const og_grid* gm,
-                       const og_grid* gt, int ic_num, const double* discrete, const og_grid* gd, double* out)
+void og_compose_sample_var(const double* ChiX, const double* ChiY, const double* stack, int n, const og_grid* gm,
+                           const og_grid* gt, int var_num, int ic_num, const double* discrete, const og_grid* gd,
+                           double* out)
 {
     double* xy = (double*)xmalloc(sizeof(double) * 2 * gt->N);
     og_sample_map_compact(ChiX, ChiY, xy, gm, gt);
@@ -369,8 +370,15 @@ void og_compose_sample(const double* ChiX, const double* ChiY, const double* sta
     #pragma omp parallel for schedule(static)
     for (long In = 0; In < gt->N; ++In)
         out[In] = discrete ? og_hermite_interpolate_2D(discrete, xy[2 * In], xy[2 * In + 1], gd)
-                           : og_init_vorticity(xy[2 * In], xy[2 * In + 1], ic_num);
+                  : var_num == 2 ? og_init_distribution(xy[2 * In], xy[2 * In + 1], ic_num)
+                                 : og_init_vorticity(xy[2 * In], xy[2 * In + 1], ic_num);
     free(xy);
+}
+
+void og_compose_sample(const double* ChiX, const double* ChiY, const double* stack, int n, const og_grid* gm,
+                       const og_grid* gt, int ic_num, const double* discrete, const og_grid* gd, double* out)
+{
+    og_compose_sample_var(ChiX, ChiY, stack, n, gm, gt, 0, ic_num, discrete, gd, out);
 }
 
 /* translate_initial_condition_through_map_stack: cmm-simulation-host.cu:299-327 */
@@ -383,7 +391,9 @@ static void translate_ic(og_state* st)
     /* k_h_sample_from_init: cmm-simulation-kernel.cu:342-373 */
     #pragma omp parallel for schedule(static)
     for (long In = 0; In < gf->N; ++In) {
-        if (!st->s.initial_discrete)
+        if (!st->s.initial_discrete && st->s.simulation_type_num == 2)   /* ID_DIST_FUNC, cmm-vlasov1d.cu:538 */
+            st->rbuf[In] = og_init_distribution(st->xy[2 * In], st->xy[2 * In + 1], st->s.initial_condition_num);
+        else if (!st->s.initial_discrete)
             st->rbuf[In] = og_init_vorticity(st->xy[2 * In], st->xy[2 * In + 1], st->s.initial_condition_num);
         else
             st->rbuf[In] = og_hermite_interpolate_2D(st->vort_disc, st->xy[2 * In], st->xy[2 * In + 1], &st->gd);
@@ -393,10 +403,14 @@ static void translate_ic(og_state* st)
     og_fourier_hermite(gf, st->cbuf1, st->vort_fine);
 }
 
-/* evaluate_stream_hermite: cmm-simulation-host.cu:333-375 */
-static void evaluate_stream(og_state* st)
+/* evaluate_stream_hermite: cmm-simulation-host.cu:333-375 (Euler) or
+ * evaluate_potential_from_density_hermite (Vlasov, og_vlasov.c) */
+static int evaluate_stream(og_state* st)
 {
     og_grid* gv = &st->gv; og_grid* gp = &st->gp;
+    if (st->s.simulation_type_num == 2)
+        return og_vlasov_potential(st->ChiX, st->ChiY, st->vort_fine, &st->gc, gv, &st->gf, gp,
+                                   st->s.molly_stencil, st->psi);
     double* fs = (double*)xmalloc(sizeof(double) * gv->N);
     og_apply_map_and_sample_from_hermite(st->ChiX, st->ChiY, fs, st->vort_fine, &st->gc, gv, &st->gf,
                                          st->s.molly_stencil, 0);
@@ -408,6 +422,7 @@ static void evaluate_stream(og_state* st)
     og_fft_cut_off_scale_h(st->cbuf2, gp, st->s.freq_cut_psi);
     og_fft_iLap_h(st->cbuf2, st->cbuf1, gp);
     og_fourier_hermite(gp, st->cbuf1, st->psi);
+    return 0;
 }
 
 static void coarse_vort(og_state* st)
@@ -449,7 +464,7 @@ int og_init(og_state* st)
     og_init_diffeo(st->ChiX, st->ChiY, &st->gc);
     st->n_maps = 0;
     translate_ic(st);
-    evaluate_stream(st);
+    if (evaluate_stream(st)) return -1;
     coarse_vort(st);
     /* Lagrange history initialisation: src/simulation/cmm-euler2d.cu:520-619 */
     int Lo = s->lagrange_order;
@@ -478,7 +493,7 @@ int og_init(og_state* st)
                 advect(st, t_init, dt_init, 0, ti_num, l_now);
                 for (int i_l = 1; i_l <= n_steps; i_l++)
                     memcpy(st->psi + Np4 * (n_steps - i_l + 1), st->psi + Np4 * (n_steps - i_l), sizeof(double) * Np4);
-                evaluate_stream(st);
+                if (evaluate_stream(st)) return -1;
             }
             for (int i = 0; i < 5; i++) { dt_init[i] = -dt_init[i]; t_init[i] = -t_init[i]; }
             swap_levels(st, 0, n_steps);
@@ -503,6 +518,7 @@ int og_step(og_state* st, double dt_now, double* e_inc, int* remapped)
     advect(st, st->t_vec, st->dt_vec, st->loop_ctr, s->time_integration_num, Lo);
     double einc = og_incompressibility_check(&st->gf, &st->gc, st->ChiX, st->ChiY);
     *e_inc = einc; *remapped = 0;
+    if (s->simulation_type_num == 2 && (einc <= 0 || einc > 1e15)) return 2;
     int saturated = 0;
     if (einc > s->incomp_threshold && !s->skip_remapping) {
         if (st->n_maps >= s->max_maps) saturated = 1;
@@ -520,7 +536,7 @@ int og_step(og_state* st, double dt_now, double* e_inc, int* remapped)
     long Np4 = 4 * st->gp.N;
     for (int i_l = 1; i_l < Lo; i_l++)
         memcpy(st->psi + Np4 * (Lo - i_l), st->psi + Np4 * (Lo - i_l - 1), sizeof(double) * Np4);
-    evaluate_stream(st);
+    if (evaluate_stream(st)) return 2;
     coarse_vort(st);
     /* particles_advect: cmm-particles.cu:63-87 */
     double Lp12[4] = {0, 0, 0, 0};
@@ -623,4 +639,9 @@ void og_sample_points_dxdy(const og_state* st, const double* pos, double* out, i
             out[2 * i + 1] = og_hermite_interpolate_dy_2D(st->psi, x, y, g);
         } else out[2 * i] = out[2 * i + 1] = NAN;
     }
+}
+
+void og_vlasov_state_mesure(const og_state* st, double* out)
+{
+    og_vlasov_mesure(st->vort, &st->gc, st->psi, &st->gp, out);
 }

@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(HERE, "liboracle.so")
 
 def build(force=False):
     """Compile liboracle.so with the committed Makefile (gcc + OpenMP)."""
-    srcs = [os.path.join(HERE, f) for f in ("og_hermite.c", "og_fft.c", "og_euler.c", "cmm_oracle.h")]
+    srcs = [os.path.join(HERE, f) for f in ("og_hermite.c", "og_fft.c", "og_euler.c", "og_vlasov.c", "cmm_oracle.h")]
     if not force and os.path.exists(LIB_PATH):
         if os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(s) for s in srcs):
             return LIB_PATH
@@ -51,7 +51,7 @@ class OgSettings(C.Structure):
                 ("freq_cut_psi", C.c_double), ("initial_condition_num", C.c_int),
                 ("initial_discrete", C.c_int), ("initial_discrete_grid", C.c_int),
                 ("max_maps", C.c_int), ("n_particle_sets", C.c_int),
-                ("psets", OgParticleSet * 8)]
+                ("psets", OgParticleSet * 8), ("simulation_type_num", C.c_int)]
 
 
 _lib = None
@@ -84,6 +84,8 @@ def lib():
             getattr(L, name).restype = C.c_int
             getattr(L, name).argtypes = [C.c_void_p]
         L.og_sample_points_dxdy.argtypes = [C.c_void_p, dp, dp, C.c_int]
+        L.og_init.restype = C.c_int
+        L.og_vlasov_state_mesure.argtypes = [C.c_void_p, dp]
         _lib = L
     return _lib
 
@@ -131,6 +133,7 @@ class EulerOracle:
         s.initial_discrete = int(cfg.get("initial_discrete", 0))
         s.initial_discrete_grid = cfg.get("initial_discrete_grid", 1)
         s.max_maps = cfg["max_maps"]
+        s.simulation_type_num = int(cfg.get("simulation_type_num", 0))
         psets = cfg.get("particles", [])
         s.n_particle_sets = len(psets)
         for i, p in enumerate(psets):
@@ -163,7 +166,9 @@ class EulerOracle:
         self.L.og_set_particles(self.h, i, _dp(p))
 
     def init(self):
-        self.L.og_init(self.h)
+        rc = self.L.og_init(self.h)
+        if rc:
+            raise ValueError("oracle initialisation rejected the grids (vort grid finer than psi grid?)")
 
     def step(self, dt_now):
         e = C.c_double()
@@ -223,6 +228,14 @@ class EulerOracle:
     def max_vorticity(self):
         return self.L.og_max_vorticity(self.h)
 
+    def vlasov_mesure(self):
+        """{Etot, Ekin, Epot, Mass, Momentum, Emode1..4} of the current state
+        (Vlasov-Poisson conservation targets)."""
+        out = np.zeros(9)
+        self.L.og_vlasov_state_mesure(self.h, _dp(out))
+        keys = ("Etot", "Ekin", "Epot", "Mass", "Momentum", "Emode1", "Emode2", "Emode3", "Emode4")
+        return dict(zip(keys, out.tolist()))
+
 
 # ---------------------------------------------------------------- kernel-level restatements
 def make_grid(n, bounds=(0.0, 6.283185307179586, 0.0, 6.283185307179586)):
@@ -245,6 +258,12 @@ def _kernel_lib():
         L.og_incompressibility_check.argtypes = [gp, gp, dp, dp]
         L.og_incompressibility_check.restype = C.c_double
         L.og_compose_sample.argtypes = [dp, dp, dp, C.c_int, gp, gp, C.c_int, dp, gp, dp]
+        L.og_compose_sample_var.argtypes = [dp, dp, dp, C.c_int, gp, gp, C.c_int, C.c_int, dp, gp, dp]
+        L.og_vlasov_potential.argtypes = [dp, dp, dp, gp, gp, gp, gp, C.c_int, dp]
+        L.og_vlasov_potential.restype = C.c_int
+        L.og_vlasov_mesure.argtypes = [dp, gp, dp, gp, dp]
+        L.og_periodification.argtypes = [gp, dp]
+        L.og_integral_v.argtypes = [dp, dp, C.c_int, C.c_int, C.c_double]
         L.og_apply_map_and_sample_from_hermite.argtypes = [dp, dp, dp, dp, gp, gp, gp, C.c_int, C.c_int]
         L.og_particle_advect.argtypes = [C.c_int, C.c_double, dp, dp, gp, C.c_int, C.c_int, dp]
         L.og_fft_d2z.argtypes = [gp, dp, dp]
@@ -279,13 +298,39 @@ def incompressibility(gcheck, gm, chix, chiy):
     return _kernel_lib().og_incompressibility_check(C.byref(gcheck), C.byref(gm), _dp(chix), _dp(chiy))
 
 
-def compose_sample(chix, chiy, stack, n, gm, gt, ic_num, discrete=None, gd=None):
+def compose_sample(chix, chiy, stack, n, gm, gt, ic_num, discrete=None, gd=None, var_num=0):
     L = _kernel_lib()
     out = np.empty(gt.N, dtype=np.float64)
     st = np.ascontiguousarray(stack if stack is not None else np.zeros(1))
-    L.og_compose_sample(_dp(chix), _dp(chiy), _dp(st), n, C.byref(gm), C.byref(gt), ic_num,
-                        _dp(discrete) if discrete is not None else None, C.byref(gd) if gd is not None else None,
-                        _dp(out))
+    L.og_compose_sample_var(_dp(chix), _dp(chiy), _dp(st), n, C.byref(gm), C.byref(gt), var_num, ic_num,
+                            _dp(discrete) if discrete is not None else None, C.byref(gd) if gd is not None else None,
+                            _dp(out))
+    return out
+
+
+def vlasov_potential(chix, chiy, f_fine, gm, gv, gf, gp, molly=0):
+    """evaluate_potential_from_density_hermite on the CPU -> 4 Hermite planes of psi on gp."""
+    L = _kernel_lib()
+    out = np.empty(4 * gp.N)
+    rc = L.og_vlasov_potential(_dp(chix), _dp(chiy), _dp(f_fine), C.byref(gm), C.byref(gv), C.byref(gf),
+                               C.byref(gp), molly, _dp(out))
+    if rc:
+        raise ValueError("vort grid finer than psi grid, or psi grid not square")
+    return out
+
+
+def vlasov_mesure(f_coarse, gc, psi, gp):
+    L = _kernel_lib()
+    out = np.zeros(9)
+    L.og_vlasov_mesure(_dp(np.ascontiguousarray(f_coarse)), C.byref(gc), _dp(np.ascontiguousarray(psi)),
+                       C.byref(gp), _dp(out))
+    return out
+
+
+def periodification(gp):
+    L = _kernel_lib()
+    out = np.empty(gp.NY)
+    L.og_periodification(C.byref(gp), _dp(out))
     return out
 
 

@@ -4,8 +4,8 @@ The reference project (Arcadia197/cmm-turbulence) pins its CUDA code with
 golden monitoring files under Cuda-CMM/tests/*/data/reference-results_*/
 Monitoring_data (raw little-endian float64 appended once per save instant,
 written by src/ui/cmm-io.cu:508-534 and src/simulation/cmm-euler2d.cu:928-959).
-This script copies the numbers (not any source code) for the Euler tests whose
-path is in scope, together with each test's input parameter file, into
+This script copies the numbers (not any source code) for the Euler and
+Vlasov-Poisson tests whose path is in scope, together with each test's input parameter file, into
 tests/golden/reference_goldens.json so the tests never need the reference tree.
 
 Usage:  python tests/golden/make_golden.py /path/to/reference
@@ -29,6 +29,8 @@ TESTS = {
                  "tests/euler2D_one_step/params.txt"),
     "remap_11b": ("tests/euler2D_11b_4nodes_reference_remapping/data/reference-results_4_nodes_C256_F512_t32_T2",
                   "examples/euler2D/params-11b-4nodes-reference-remapping.txt"),
+    "vlasov_15": ("tests/vlasov1D_15_vp_landau_damping/data/reference-results_C256_F512_t1024_T0.2",
+                  "tests/vlasov1D_15_vp_landau_damping/params-15b-vp-landau-damping.txt"),
 }
 
 

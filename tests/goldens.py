@@ -105,7 +105,12 @@ class DebugRecorder:
                     if p.tau == 0:
                         self._stat("Particles_advected_vel_U%02d" % (i + 1), stats_raw(st.particle_velocity(i)))
         # compute_conservation_targets (cmm-simulation-host.cu:615-698)
-        if save_instant(s.save_comp, t_now, dt_now, dt, need_conv=True):
+        if save_instant(s.save_comp, t_now, dt_now, dt, need_conv=True) and s.simulation_type_num == 2:
+            m = st.vlasov_mesure()
+            self._app("Mesure/Time_s", [t_now])
+            for k in ("Etot", "Ekin", "Epot", "Mass", "Momentum", "Emode1", "Emode2", "Emode3", "Emode4"):
+                self._app("Mesure/" + k, [m[k]])
+        elif save_instant(s.save_comp, t_now, dt_now, dt, need_conv=True):
             self._app("Mesure/Time_s", [t_now])
             self._app("Mesure/Energy", [st.energy()])
             self._app("Mesure/Enstrophy", [st.enstrophy()])

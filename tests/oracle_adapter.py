@@ -56,3 +56,6 @@ class OracleRun:
 
     def max_vorticity(self):
         return self.o.max_vorticity()
+
+    def vlasov_mesure(self):
+        return self.o.vlasov_mesure()

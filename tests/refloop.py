@@ -15,6 +15,7 @@ Restates:
   next time step     src/simulation/cmm-simulation-host.cu:1307-1374
   save instants      src/ui/cmm-io.cu:300-317, cmm-simulation-host.cu:619-636
   loop               src/simulation/cmm-euler2d.cu:750-960
+  Vlasov driver      src/simulation/cmm-vlasov1d.cu:62-105 (bounds x pi, dt, iter_max)
 """
 import math
 
@@ -25,6 +26,7 @@ T_MAX = 10000.0
 IC_EULER = ["4_nodes", "quadropole", "one_vortex", "two_votices", "three_vortices", "single_shear_layer",
             "tanh_shear_layer", "turbulence_gaussienne", "gaussian_blobs", "shielded_vortex", "two_cosine",
             "vortex_sheets"]
+IC_VLASOV = ["landau_damping", "two_stream", "nonlin_landau_damping"]
 TI_MAP = {"EulerExp": (10, 1), "RK1": (10, 1), "Heun": (21, 2), "RK2": (21, 2), "AB2": (20, 2),
           "RK3": (30, 3), "RK4": (40, 4), "RK3Mod": (31, 3), "RK4Mod": (41, 4)}
 TI_PART = {"EulerExp": 10, "RK1": 10, "Heun": 20, "RK2": 20, "RK3": 30, "RK4": 40, "RK3Mod": 31, "RK4Mod": 41}
@@ -161,7 +163,12 @@ class Settings:
 
     @property
     def initial_condition_num(self):
-        return IC_EULER.index(self.initial_condition) if self.initial_condition in IC_EULER else -1
+        table = IC_VLASOV if self.simulation_type == "cmm_vlasov_poisson_1d" else IC_EULER
+        return table.index(self.initial_condition) if self.initial_condition in table else -1
+
+    @property
+    def simulation_type_num(self):
+        return 2 if self.simulation_type == "cmm_vlasov_poisson_1d" else 0
 
     def set_variable(self, line, delim):
         """settings.cu:347-436; returns the record-count code 0..5."""
@@ -241,6 +248,9 @@ class Settings:
 
     # ---- derived quantities of cmm-euler2d.cu:62-83 ----
     def finalize(self):
+        if self.simulation_type == "cmm_vlasov_poisson_1d":
+            # cmm-vlasov1d.cu:72: the Vlasov driver multiplies the bounds by pi
+            self.domain_bounds = [b * PI if i < 4 else b for i, b in enumerate(self.domain_bounds)]
         if self.set_dt_by_steps:
             self.dt = 1.0 / self.steps_per_sec
         else:
@@ -268,7 +278,7 @@ class Settings:
                     molly_stencil=self.molly_stencil, freq_cut_psi=self.freq_cut_psi,
                     initial_condition_num=self.initial_condition_num,
                     initial_discrete=self.initial_discrete, initial_discrete_grid=self.initial_discrete_grid,
-                    max_maps=self.cpu_map_num,
+                    max_maps=self.cpu_map_num, simulation_type_num=self.simulation_type_num,
                     particles=[dict(num=p.num, tau=p.tau, time_integration_num=p.time_integration_num,
                                     init_time=p.init_time) for p in self.particles_advected])
 
@@ -333,6 +343,8 @@ def run_reference_loop(s, stepper, on_save, on_step=None):
         if t + dt_now > s.final_time:
             dt_now = s.final_time - t
         rc, e_inc, remapped, gap, maps = stepper.step(dt_now)
+        if rc == 2:
+            raise RuntimeError("incompressibility error out of range: Vlasov run aborted (cmm-vlasov1d.cu:838-840)")
         if rc == 1:
             cont = False
         t_vec.append(t + dt_now)

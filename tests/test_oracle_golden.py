@@ -46,3 +46,68 @@ def test_oracle_matches_reference_remapping_11b():
     # the remap step (47) and map counter must agree exactly
     assert rec.series["Map_counter"] == g["files"]["Map_counter"]
     assert not fails, fails
+
+
+# ---------------------------------------------------------------- Vlasov-Poisson
+# The reference's Vlasov golden (tests/vlasov1D_15_vp_landau_damping) was
+# written by an older revision of the reference: its own parameter file puts
+# the vort grid (512) above the psi grid (256), which the current calc_phi
+# rejects (src/simulation/cmm-simulation-host.cu:457-460), and its psi has
+# Velocity_UY_psi_Max = 2.5*pi, i.e. psi_y = -v without the current
+# periodification (:534-571).  Only the t = 0 quantities that do not depend on
+# the potential (the sampled distribution, the identity map, Mass and Ekin) are
+# comparable; the oracle runs the golden case with grid_psi = 512 for them.
+VLASOV_T0_KEYS = ["Debug_globals/%s_%s" % (n, s)
+                  for n in ("Distribution_coarse", "Vorticity_W_coarse", "Map_ChiX_coarse", "Map_ChiY_coarse",
+                            "Map_ChiX_H_coarse", "Map_ChiY_H_coarse")
+                  for s in ("Min", "Max", "Avg", "L2")] + ["Mesure/Ekin", "Mesure/Mass"]
+
+
+def _vlasov_oracle(cli):
+    g = goldens()["vlasov_15"]
+    s = refloop.settings_from_param_text(g["params_in"], cli)
+    run = OracleRun(s)
+    rec = DebugRecorder(s, run)
+    refloop.run_reference_loop(s, run, rec.on_save, rec.on_step)
+    return rec, g, run
+
+
+def test_oracle_vlasov_rejects_the_goldens_own_grids():
+    g = goldens()["vlasov_15"]
+    s = refloop.settings_from_param_text(g["params_in"], ["final_time=0"])
+    assert s.grid_vort > s.grid_psi
+    with pytest.raises(ValueError):
+        OracleRun(s).init()
+
+
+def test_oracle_vlasov_initial_state_matches_reference_goldens():
+    rec, g, _ = _vlasov_oracle(["grid_psi=512", "final_time=0"])
+    first = {k: [rec.series[k][0]] for k in VLASOV_T0_KEYS if k in rec.series}
+    gold = {k: [g["files"][k][0]] for k in VLASOV_T0_KEYS}
+    worst, fails = compare_series(first, gold, VLASOV_T0_KEYS, RTOL)
+    assert len(worst) == len(VLASOV_T0_KEYS)
+    assert not fails, fails
+
+
+def test_oracle_vlasov_known_answers_at_t0():
+    """landau_damping, f0 = (1 + 0.05 cos(x/2)) exp(-v^2/2)/sqrt(2 pi) on
+    x in [0, 4 pi], v in [-2.5 pi, 2.5 pi]: rho - 1 = 0.05 cos(x/2), so
+    |psi_x| = |phi'| = 0.1 |sin(x/2)|, Epot = 0.5 * 0.01 * 2 pi = pi / 100,
+    |E_1| = 0.05, Ekin = 2 pi, Mass = 4 pi, Momentum = 0; in the centre of the
+    v range (|v| < 3) the periodified psi has psi_y = v, and psi is separable."""
+    import numpy as np
+    _, _, run = _vlasov_oracle(["grid_psi=512", "final_time=0"])
+    m = run.vlasov_mesure()
+    assert abs(m["Epot"] - np.pi / 100) < 1e-12
+    assert abs(m["Emode1"] - 0.05) < 1e-12 and max(m["Emode2"], m["Emode3"], m["Emode4"]) < 1e-12
+    assert abs(m["Ekin"] - 2 * np.pi) < 1e-11 and abs(m["Mass"] - 4 * np.pi) < 1e-11
+    assert abs(m["Momentum"]) < 1e-11
+    n, hx, hy = run.grid(2)
+    side = int(round(n ** 0.5))
+    psi = run.psi().reshape(4, side, side)
+    v = -2.5 * np.pi + hy * np.arange(side)
+    centre = np.abs(v) < 3.0      # the tanh bump is 1 to 1e-12 there (it leaves 1 near |v| = 4)
+    assert np.max(np.abs(psi[2][centre, :] - v[centre, None])) < 1e-10      # psi_y = v
+    # separable: psi_xy = 0 up to FFT rounding amplified by kx*ky (|psi| ~ 30, kx*ky <~ 1.3e4)
+    assert np.max(np.abs(psi[3])) < 1e-10
+    assert np.max(np.abs(psi[1] - psi[1][0:1, :])) < 1e-11                 # psi_x independent of v (to rounding x kx)

@@ -1,5 +1,5 @@
-// init_conditions.cuh -- analytic initial vorticity and passive-scalar fields
-// sampled by the remap-time composition kernels (header-only so every
+// init_conditions.cuh -- analytic initial vorticity, passive-scalar and
+// Vlasov distribution fields sampled by the remap-time composition kernels (header-only so every
 // translation unit that composes maps can inline them).
 #pragma once
 #include "cmm_common.cuh"
@@ -117,6 +117,41 @@ __device__ __forceinline__ double init_scalar(double x, double y, int sn)
         }
         default: return 0.0;
     }
+}
+
+// initial distribution function of the Vlasov-Poisson system
+// (d_init_distirbution_function, src/simulation/cmm-init.cu:457-493): x is
+// the periodic space coordinate, v the velocity
+__device__ __forceinline__ double init_distribution(double x, double v, int ic)
+{
+    const double PI = kTwoPi / 2;
+    switch (ic) {
+        case 0: {  // landau_damping
+            const double k = 0.5, eps = 5 * 1e-2;
+            return (1 + eps * cos(k * x)) * exp(-(v) * (v) * 0.5) / sqrt(2 * PI);
+        }
+        case 1: {  // two_stream
+            const double v0 = 3, k = 0.2, eps = 5 * 1e-2;
+            return 1 / (2 * sqrt(2 * PI)) * (1 + eps * cos(k * x)) *
+                   (exp(-(v - v0) * (v - v0) * 0.5) + exp(-(v + v0) * (v + v0) * 0.5));
+        }
+        case 2: {  // nonlin_landau_damping
+            const double k = 0.5, eps = 0.5;
+            return (1 + eps * cos(k * x)) * exp(-(v) * (v) * 0.5) / sqrt(2 * PI);
+        }
+        default: return 0.0;
+    }
+}
+
+// value of an initial field at (x, y) by source kind (0 vorticity, 1 passive
+// scalar, 2 distribution function; kind 3, a discrete field, is interpolated
+// by the caller)
+__device__ __forceinline__ double init_field(int kind, double x, double y, int ic, const double* __restrict__ prm,
+                                             const double* __restrict__ rnd)
+{
+    if (kind == 1) return init_scalar(x, y, ic);
+    if (kind == 2) return init_distribution(x, y, ic);
+    return init_vorticity(x, y, ic, prm, rnd);
 }
 
 }  // namespace cmm

@@ -41,7 +41,7 @@ cudaError_t launch_incomp(const Grid& gcheck, const Grid& gmap, const double* X,
 // Initial-condition selector for sampling omega_0 (k_h_sample_from_init,
 // src/simulation/cmm-simulation-kernel.cu:342-373).
 struct InitSource {
-    int kind;                 // 0 analytic vorticity, 1 analytic passive scalar, 3 discrete Hermite
+    int kind;                 // 0 analytic vorticity, 1 analytic passive scalar, 2 Vlasov distribution, 3 discrete Hermite
     int ic_num;               // analytic initial-condition number
     const double* discrete;   // Hermite planes of the discrete initial field
     Grid gd;                  // its grid

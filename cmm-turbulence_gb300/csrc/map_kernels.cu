@@ -230,8 +230,7 @@ __global__ void __launch_bounds__(256) k_compose_sample(Grid gm, Grid gt, const 
     }
     double v;
     if (src.kind == 3) v = interp_value(src.discrete, src.gd, x, y);
-    else if (src.kind == 1) v = init_scalar(x, y, src.ic_num);
-    else v = init_vorticity(x, y, src.ic_num, src.params, src.rand_table);
+    else v = init_field(src.kind, x, y, src.ic_num, src.params, src.rand_table);
     out[i] = v;
 }
 

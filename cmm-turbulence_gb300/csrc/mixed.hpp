@@ -17,6 +17,15 @@ struct AdvectMArgs {
     const float4* psiA;     // k1 field: sum_l L1[l] psi_l
     const float4* psiB;     // k2 field of RK3: sum_l L12[l] psi_l
     const float4* psi0;     // newest level
+    // separable stream function (Vlasov-Poisson): FP64 1D tables (f(i+1) - f(i), f'(i)) of
+    // the x-part of each combination and of h(v); tv != nullptr selects them (and FP64
+    // characteristics, coef64 / dt64 / ep64) over the nodes
+    const double2* tA;
+    const double2* tB;
+    const double2* t0;
+    const double2* tv;
+    double coef64[4][kMaxFoot];
+    double dt64, ep64;
     float coef[4][kMaxFoot];
     float dt, ep;
     int time_integration_num;   // 10, 21, 30
@@ -40,8 +49,11 @@ cudaError_t launch_compose_m(const Grid& gm, const Grid& gt, const float4* map, 
 cudaError_t launch_sample_m(const Grid& gm, const Grid& go, const Grid& gf, const float4* map, const float4* W,
                             float* out_f, double* out_d, cudaStream_t s);
 // tracers at 64-bit fixed-point positions P = (x - b0) / W * 2^64 (interleaved x, y)
+// (tA, tB, t0, tv: separable tables as in AdvectMArgs, used when tv != nullptr)
 cudaError_t launch_particles_m(const Grid& gp, unsigned long long* pos, int num, const float4* psiA,
-                               const float4* psiB, const float4* psi0, double dt, int ti, cudaStream_t s);
+                               const float4* psiB, const float4* psi0, double dt, int ti, cudaStream_t s,
+                               const double2* tA = nullptr, const double2* tB = nullptr,
+                               const double2* t0 = nullptr, const double2* tv = nullptr);
 cudaError_t launch_pos_to_fix(const double* pos, int num, const Grid& g, unsigned long long* out, cudaStream_t s);
 cudaError_t launch_fix_to_pos(const unsigned long long* in, int num, const Grid& g, double* pos, cudaStream_t s);
 cudaError_t launch_spec_psi_f(const float2* Fv, const Grid& gv, const Grid& gp, double freq, float2* out4,

@@ -61,16 +61,32 @@ __device__ __forceinline__ int wrap_index(int i, int n)
 }
 
 // cell of the point (bx + qx, by + qy) in cell units: integer base cell + FP32 offset
-__device__ __forceinline__ CellF locate_q(const Grid& g, int bx, int by, float qx, float qy)
+struct CellXY {
+    int ix0, iy0, ix1, iy1;
+    float tx, ty;
+};
+
+__device__ __forceinline__ CellXY locate_q_xy(const Grid& g, int bx, int by, float qx, float qy)
 {
     float fx = floorf(qx), fy = floorf(qy);
-    CellF c;
+    CellXY c;
     c.tx = qx - fx;
     c.ty = qy - fy;
-    int ix0 = wrap_index(bx + (int)fx, g.NX), iy0 = wrap_index(by + (int)fy, g.NY);
-    int ix1 = ix0 + 1 == g.NX ? 0 : ix0 + 1, iy1 = iy0 + 1 == g.NY ? 0 : iy0 + 1;
-    c.i00 = iy0 * g.NX + ix0; c.i10 = iy0 * g.NX + ix1;
-    c.i01 = iy1 * g.NX + ix0; c.i11 = iy1 * g.NX + ix1;
+    c.ix0 = wrap_index(bx + (int)fx, g.NX);
+    c.iy0 = wrap_index(by + (int)fy, g.NY);
+    c.ix1 = c.ix0 + 1 == g.NX ? 0 : c.ix0 + 1;
+    c.iy1 = c.iy0 + 1 == g.NY ? 0 : c.iy0 + 1;
+    return c;
+}
+
+__device__ __forceinline__ CellF locate_q(const Grid& g, int bx, int by, float qx, float qy)
+{
+    CellXY q = locate_q_xy(g, bx, by, qx, qy);
+    CellF c;
+    c.tx = q.tx;
+    c.ty = q.ty;
+    c.i00 = q.iy0 * g.NX + q.ix0; c.i10 = q.iy0 * g.NX + q.ix1;
+    c.i01 = q.iy1 * g.NX + q.ix0; c.i11 = q.iy1 * g.NX + q.ix1;
     return c;
 }
 
@@ -275,11 +291,140 @@ __global__ void __launch_bounds__(256) k_advect_m(const AdvectMArgs a, int lpn_l
     }
 }
 
+// ---------------------------------------------------------------------------
+// separable stream function psi = F(x) - h(v) (the Vlasov-Poisson potential):
+// characteristics in FP64.  The velocity u = (psi_y, -psi_x) = (-h'(v),
+// -F'(x)) is a pair of 1D cubic Hermite derivatives from FP64 tables
+// T[i] = (f(i+1) - f(i), f'(i)).  Vlasov characteristics move up to |v| dt
+// per step (0.2 at dt = 1/32), 60x the Euler displacement of the 2048^2
+// workload; FP32 velocities and offsets would put their rounding (~1e-7 of
+// the displacement) through the 1/eps^2 GALS stencil into the map's cross
+// derivative at the 1e-2 level, so footpoints, RK stages, the map
+// interpolation and the stencil sums are FP64 here, over the FP32 map nodes.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void locate64(int b, double q, int n, int& i0, int& i1, double& t)
+{
+    double fl = floor(q);
+    t = q - fl;
+    i0 = wrap_index(b + (int)fl, n);
+    i1 = i0 + 1 == n ? 0 : i0 + 1;
+}
+
+__device__ __forceinline__ double sep_slope64(const double2* __restrict__ T, int i0, int i1, double t, double ih)
+{
+    double s = 1.0 - t;
+    double2 a0 = __ldg(T + i0);
+    double s1 = __ldg(&T[i1].y);
+    return fma(6.0 * s * t * ih, a0.x, fma(s * fma(3.0, s, -2.0), a0.y, t * fma(3.0, t, -2.0) * s1));
+}
+
+__device__ __forceinline__ void velocity_sep64(const double2* __restrict__ TX, const double2* __restrict__ TV,
+                                               const Grid& g, int bx, int by, double qx, double qy, double& ux,
+                                               double& uy)
+{
+    int x0, x1, y0, y1;
+    double tx, ty;
+    locate64(bx, qx, g.NX, x0, x1, tx);
+    locate64(by, qy, g.NY, y0, y1, ty);
+    uy = -sep_slope64(TX, x0, x1, tx, g.ihx);
+    ux = -sep_slope64(TV, y0, y1, ty, g.ihy);
+}
+
+// FP64 interpolation of the FP32 displacement nodes, values taken relative to (rx, ry)
+__device__ __forceinline__ void map_disp64(const float4* __restrict__ M, const Grid& g, int bx, int by, double qx,
+                                           double qy, double rx, double ry, double& dxo, double& dyo)
+{
+    int x0, x1, y0, y1;
+    double tx, ty;
+    locate64(bx, qx, g.NX, x0, x1, tx);
+    locate64(by, qy, g.NY, y0, y1, ty);
+    const int i00 = y0 * g.NX + x0, i10 = y0 * g.NX + x1, i01 = y1 * g.NX + x0, i11 = y1 * g.NX + x1;
+    float4 a00 = __ldg(M + 2 * i00), b00 = __ldg(M + 2 * i00 + 1);
+    float4 a10 = __ldg(M + 2 * i10), b10 = __ldg(M + 2 * i10 + 1);
+    float4 a01 = __ldg(M + 2 * i01), b01 = __ldg(M + 2 * i01 + 1);
+    float4 a11 = __ldg(M + 2 * i11), b11 = __ldg(M + 2 * i11 + 1);
+    W4 wx = value_weights(tx, g.hx), wy = value_weights(ty, g.hy);
+    double s0, t0, s1, t1;
+    xrow(wx, a00.x - rx, a10.x - rx, a00.z, a10.z, b00.x, b10.x, b00.z, b10.z, s0, t0);
+    xrow(wx, a01.x - rx, a11.x - rx, a01.z, a11.z, b01.x, b11.x, b01.z, b11.z, s1, t1);
+    dxo = ycombine(wy, s0, s1, t0, t1);
+    xrow(wx, a00.y - ry, a10.y - ry, a00.w, a10.w, b00.y, b10.y, b00.w, b10.w, s0, t0);
+    xrow(wx, a01.y - ry, a11.y - ry, a01.w, a11.w, b01.y, b11.y, b01.w, b11.w, s1, t1);
+    dyo = ycombine(wy, s0, s1, t0, t1);
+}
+
+template <int TI>
+__global__ void __launch_bounds__(256) k_advect_sep(const AdvectMArgs a, int lpn_log2)
+{
+    __shared__ double sc[4][kMaxFoot];
+    if (threadIdx.x < 4 * kMaxFoot) sc[threadIdx.x / kMaxFoot][threadIdx.x % kMaxFoot] =
+        a.coef64[threadIdx.x / kMaxFoot][threadIdx.x % kMaxFoot];
+    __syncthreads();
+    const int lpn = 1 << lpn_log2;
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    long long node = t >> lpn_log2;
+    int k = (int)(t & (lpn - 1));
+    bool live = node < a.gm.N;
+    const int nd = live ? (int)node : 0;
+    const int iY = nd / a.gm.NX, iX = nd - iY * a.gm.NX;
+    float4 n0 = __ldg(a.map + 2 * nd);     // (dX, dY, dX_x, dY_x) at the node
+    double gX = 0.0, gY = 0.0;
+    if (live && k < a.nfoot) {
+        const double r = (double)((k >> 2) + 1) * a.ep64;
+        const double ex = r * (double)(1 - 2 * ((k >> 1) & 1));
+        const double ey = r * (double)(1 - 2 * (((k + 1) >> 1) & 1));
+        const int bx = iX * a.rp, by = iY * a.rp;
+        const double dt = a.dt64, ihx = a.gp.ihx, ihy = a.gp.ihy;
+        double k1x, k1y, Dx, Dy;
+        velocity_sep64(a.tA, a.tv, a.gp, bx, by, ex * ihx, ey * ihy, k1x, k1y);
+        if (TI == 10) {
+            Dx = dt * k1x;
+            Dy = dt * k1y;
+        } else if (TI == 21) {
+            double k2x, k2y;
+            velocity_sep64(a.t0, a.tv, a.gp, bx, by, (ex - dt * k1x) * ihx, (ey - dt * k1y) * ihy, k2x, k2y);
+            Dx = dt * (k1x + k2x) * 0.5;
+            Dy = dt * (k1y + k2y) * 0.5;
+        } else {
+            double k2x, k2y, k3x, k3y;
+            velocity_sep64(a.tB, a.tv, a.gp, bx, by, (ex - 0.5 * dt * k1x) * ihx, (ey - 0.5 * dt * k1y) * ihy, k2x, k2y);
+            velocity_sep64(a.t0, a.tv, a.gp, bx, by, (ex + dt * k1x - 2.0 * dt * k2x) * ihx,
+                           (ey + dt * k1y - 2.0 * dt * k2y) * ihy, k3x, k3y);
+            Dx = dt * (k1x + 4.0 * k2x + k3x) / 6.0;
+            Dy = dt * (k1y + 4.0 * k2y + k3y) / 6.0;
+        }
+        double mx, my;
+        map_disp64(a.map, a.gm, iX, iY, (ex - Dx) * a.gm.ihx, (ey - Dy) * a.gm.ihy, n0.x, n0.y, mx, my);
+        gX = mx - Dx;
+        gY = my - Dy;
+    }
+    const int comp = k & 1, plane = (k >> 1) & 3;
+    double acc = 0.0;
+    for (int kk = 0; kk < a.nfoot; ++kk) {
+        double vx = __shfl_sync(0xffffffffu, gX, kk, lpn);
+        double vy = __shfl_sync(0xffffffffu, gY, kk, lpn);
+        acc = fma(comp ? vy : vx, sc[plane][kk], acc);
+    }
+    if (live && k < 8) {
+        if (plane == 0) acc += comp ? (double)n0.y : (double)n0.x;
+        reinterpret_cast<float*>(a.out)[8 * node + k] = (float)acc;
+    }
+}
+
 cudaError_t launch_advect_m(const AdvectMArgs& a, cudaStream_t s)
 {
     int lpn_log2 = a.nfoot <= 8 ? 3 : 4;
     long long total = a.gm.N << lpn_log2;
     unsigned blocks = (unsigned)((total + 255) / 256);
+    if (a.tv) {
+        switch (a.time_integration_num) {
+            case 10: k_advect_sep<10><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
+            case 21: k_advect_sep<21><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
+            case 30: k_advect_sep<30><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
+            default: return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
+    }
     switch (a.time_integration_num) {
         case 10: k_advect_m<10><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
         case 21: k_advect_m<21><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
@@ -512,7 +657,7 @@ __global__ void __launch_bounds__(256) k_compose_m(Grid gm, Grid gt, unsigned lo
     } else {
         double x = gm.b0 + __ull2double_rn(Px) * (gm.Wx * 5.42101086242752217e-20);
         double y = gm.b2 + __ull2double_rn(Py) * (gm.Wy * 5.42101086242752217e-20);
-        v = src.kind == 1 ? init_scalar(x, y, src.ic_num) : init_vorticity(x, y, src.ic_num, src.params, src.rand_table);
+        v = init_field(src.kind, x, y, src.ic_num, src.params, src.rand_table);
     }
     out[(long long)iY * gt.NX + iX] = v;
 }
@@ -596,6 +741,8 @@ cudaError_t launch_sample_m(const Grid& gm, const Grid& go, const Grid& gf, cons
 // (psiA = level 1 = t_n, psiB = Lagrange t_{n+1/2} combination, psi0 =
 // t_{n+1}); stages as Particle_advect (src/numerical/cmm-particles.cu:159-183).
 // ---------------------------------------------------------------------------
+struct SepTables { const double2* tA; const double2* tB; const double2* t0; const double2* tv; };
+
 template <int TI>
 __global__ void __launch_bounds__(256) k_particles_m(Grid gp, ulonglong2* __restrict__ pos, int num,
                                                      const float4* __restrict__ psiA, const float4* __restrict__ psiB,
@@ -634,13 +781,58 @@ __global__ void __launch_bounds__(256) k_particles_m(Grid gp, ulonglong2* __rest
     pos[i] = P;
 }
 
+// tracers in a separable stream function: FP64 stages from the 1D tables
+template <int TI>
+__global__ void __launch_bounds__(256) k_particles_sep(Grid gp, ulonglong2* __restrict__ pos, int num, SepTables tb,
+                                                       double dt, float2 scx, float2 scy)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= num) return;
+    ulonglong2 P = pos[i];
+    int bx, by;
+    float txf, tyf;
+    fix_cell(P.x, gp.NX, bx, txf);
+    fix_cell(P.y, gp.NY, by, tyf);
+    const double tx = txf, ty = tyf;
+    double k1x, k1y, Dx, Dy;
+    velocity_sep64(tb.tA, tb.tv, gp, bx, by, tx, ty, k1x, k1y);
+    if (TI == 10) {
+        Dx = dt * k1x;
+        Dy = dt * k1y;
+    } else if (TI == 20) {
+        double k2x, k2y;
+        velocity_sep64(tb.t0, tb.tv, gp, bx, by, tx + dt * k1x * gp.ihx, ty + dt * k1y * gp.ihy, k2x, k2y);
+        Dx = dt * (k1x + k2x) * 0.5;
+        Dy = dt * (k1y + k2y) * 0.5;
+    } else {
+        double k2x, k2y, k3x, k3y;
+        velocity_sep64(tb.tB, tb.tv, gp, bx, by, tx + 0.5 * dt * k1x * gp.ihx, ty + 0.5 * dt * k1y * gp.ihy, k2x, k2y);
+        velocity_sep64(tb.t0, tb.tv, gp, bx, by, tx + dt * (2.0 * k2x - k1x) * gp.ihx,
+                       ty + dt * (2.0 * k2y - k1y) * gp.ihy, k3x, k3y);
+        Dx = dt * (k1x + 4.0 * k2x + k3x) / 6.0;
+        Dy = dt * (k1y + 4.0 * k2y + k3y) / 6.0;
+    }
+    P.x += fix_increment((float)Dx, scx);
+    P.y += fix_increment((float)Dy, scy);
+    pos[i] = P;
+}
+
 cudaError_t launch_particles_m(const Grid& gp, unsigned long long* pos, int num, const float4* psiA,
-                               const float4* psiB, const float4* psi0, double dt, int ti, cudaStream_t s)
+                               const float4* psiB, const float4* psi0, double dt, int ti, cudaStream_t s,
+                               const double2* tA, const double2* tB, const double2* t0, const double2* tv)
 {
     if (num <= 0) return cudaSuccess;
     unsigned blocks = (unsigned)((num + 255) / 256);
     ulonglong2* P = reinterpret_cast<ulonglong2*>(pos);
     float2 sx = fix_scale(gp.Wx), sy = fix_scale(gp.Wy);
+    if (tv) {
+        SepTables tb{tA, tB, t0, tv};
+        if (ti == 10) k_particles_sep<10><<<blocks, 256, 0, s>>>(gp, P, num, tb, dt, sx, sy);
+        else if (ti == 20) k_particles_sep<20><<<blocks, 256, 0, s>>>(gp, P, num, tb, dt, sx, sy);
+        else if (ti == 30) k_particles_sep<30><<<blocks, 256, 0, s>>>(gp, P, num, tb, dt, sx, sy);
+        else return cudaErrorInvalidValue;
+        return cudaGetLastError();
+    }
     float d = (float)dt;
     if (ti == 10) k_particles_m<10><<<blocks, 256, 0, s>>>(gp, P, num, psiA, psiB, psi0, d, sx, sy);
     else if (ti == 20) k_particles_m<20><<<blocks, 256, 0, s>>>(gp, P, num, psiA, psiB, psi0, d, sx, sy);

@@ -132,9 +132,13 @@ int EulerSim::set_initial_discrete(const double* host, size_t n)
 
 int EulerSim::alloc()
 {
-    if (s.simulation_type != "cmm_euler_2d") { err = "only cmm_euler_2d is built in this context"; return kErrUnsupported; }
+    if (s.simulation_type != "cmm_euler_2d" && s.simulation_type != "cmm_vlasov_poisson_1d") {
+        err = "unknown simulation_type " + s.simulation_type;
+        return kErrParam;
+    }
+    vlasov_ = s.simulation_type == "cmm_vlasov_poisson_1d";
     if (s.initial_condition_num < 0) { err = "unknown initial condition " + s.initial_condition; return kErrParam; }
-    if (s.initial_condition_num == 7 && !s.initial_discrete) {
+    if (!vlasov_ && s.initial_condition_num == 7 && !s.initial_discrete) {
         err = "initial condition turbulence_gaussienne is not built (needs device cuRAND sequences)";
         return kErrUnsupported;
     }
@@ -166,6 +170,15 @@ int EulerSim::alloc()
         return kErrParam;
     }
 
+    if (vlasov_) {
+        // the Vlasov driver states its domain in units of pi (cmm-vlasov1d.cu:72)
+        for (int i = 0; i < 4; ++i) s.domain_bounds[i] *= kTwoPi / 2;
+        if (s.grid_vort > s.grid_psi) {
+            // calc_phi's restriction (cmm-simulation-host.cu:457-460)
+            err = "vorticity grid should be smaller than phi_out grid (grid_vort > grid_psi)";
+            return kErrParam;
+        }
+    }
     const double* b = s.domain_bounds;
     gc = make_grid(s.grid_coarse, s.grid_coarse, b);
     gf = make_grid(s.grid_fine, s.grid_fine, b);
@@ -205,6 +218,18 @@ int EulerSim::alloc()
         !make_plans(pc_, gc, stream) || (s.initial_discrete && !make_plans(pd_, gd, stream))) {
         err = "cuFFT plan creation failed";
         return kErrCuda;
+    }
+    if (vlasov_) {
+        for (int l = 0; l < L; ++l) if ((rc = dalloc(&phi_lv_[l], 2 * (long long)gp.NX))) return rc;
+        long long nchunks = (gv.NY + kVlasovRowChunk - 1) / kVlasovRowChunk;
+        if ((rc = dalloc(&vl_h_, 2 * (long long)gp.NY)) || (rc = dalloc(&vl_rho_, gv.NX)) ||
+            (rc = dalloc(&vl_part_, nchunks * gv.NX)))
+            return rc;
+        int cn = std::max(gv.NX_fft, gp.NX_fft);
+        for (int k = 0; k < 3; ++k) CMM_CUDA(cudaMalloc((void**)&vl_c_[k], sizeof(double2) * cn));
+        if (mixed_)
+            for (int k = 0; k < 4; ++k) CMM_CUDA(cudaMalloc((void**)&vtab_[k], sizeof(double2) * std::max(gp.NX, gp.NY)));
+        if (!make_vlasov_plans(vp_, gv, gp, stream)) { err = "cuFFT 1D plan creation failed"; return kErrCuda; }
     }
     if (mixed_) {
         auto falloc = [&](void** p, size_t bytes) { return check(cudaMalloc(p, std::max(bytes, (size_t)16)), "cudaMalloc"); };
@@ -254,6 +279,12 @@ void EulerSim::release()
     parts.clear();
     for (auto p : partfix_) f(p);
     partfix_.clear();
+    for (int l = 0; l < kMaxLagrange; ++l) { f(phi_lv_[l]); phi_lv_[l] = nullptr; }
+    f(vl_h_); f(vl_rho_); f(vl_part_);
+    vl_h_ = vl_rho_ = vl_part_ = nullptr;
+    for (int k = 0; k < 3; ++k) { f(vl_c_[k]); vl_c_[k] = nullptr; }
+    for (int k = 0; k < 4; ++k) { f(vtab_[k]); vtab_[k] = nullptr; }
+    destroy_vlasov_plans(vp_);
     f(wdiscm_); wdiscm_ = nullptr;
     f(mapm_); f(mapm_new_); f(psiA_); f(psiB_); f(wfm_); f(stackm_); f(realf_); f(specf_); f(spec4f_);
     for (int l = 0; l < kMaxLagrange; ++l) { f(psim_[l]); psim_[l] = nullptr; }
@@ -277,7 +308,7 @@ void EulerSim::release()
 int EulerSim::translate_ic()
 {
     InitSource src{};
-    src.kind = s.initial_discrete ? 3 : 0;
+    src.kind = s.initial_discrete ? 3 : vlasov_ ? 2 : 0;   // ID_DIST_FUNC for Vlasov (cmm-vlasov1d.cu:538)
     src.ic_num = s.initial_condition_num;
     src.discrete = wdisc;
     src.gd = gd;
@@ -299,6 +330,7 @@ int EulerSim::translate_ic()
 
 int EulerSim::evaluate_stream()
 {
+    if (vlasov_) return evaluate_potential();
     if (mixed_) {
         CMM_LAUNCH(1, launch_sample_m(gc, gv, gf, mapm_, wfm_, realf_, nullptr, stream));
         CMM_FFT(cufftExecR2C(r2c_v_, realf_, reinterpret_cast<cufftComplex*>(specf_)));
@@ -334,6 +366,66 @@ int EulerSim::sync_fp64_views()
     CMM_LAUNCH(1, launch_float4_to_planes(wfm_, gf.N, wfine, stream));
     for (size_t i = 0; i < partfix_.size(); ++i)
         CMM_LAUNCH(1, launch_fix_to_pos(partfix_[i], s.particles_advected[i].num, gp, parts[i], stream));
+    if (vlasov_)   // psi levels are held as phi(x) and h(v): write their Hermite planes
+        for (int l = 0; l < L; ++l)
+            CMM_LAUNCH(1, launch_vlasov_assemble(phi_lv_[l], phi_lv_[l] + gp.NX, vl_h_, vl_h_ + gp.NY, gp, psi[l], stream));
+    return kOk;
+}
+
+// ---------------------------------------------------------------- Vlasov-Poisson
+int EulerSim::vlasov_setup_h()
+{
+    // compute_periodification_function (cmm-simulation-host.cu:534-571): the
+    // normalised bump, integrated twice in v by 1D spectra; h and h' on the psi grid
+    CMM_LAUNCH(1, launch_vlasov_bump(gp, real_buf_, stream));
+    CMM_FFT(cufftExecD2Z(vp_.d2z_p, real_buf_, vl_c_[0]));
+    CMM_LAUNCH(1, launch_vlasov_h_spec(vl_c_[0], gp, vl_c_[1], vl_c_[2], stream));
+    CMM_FFT(cufftExecZ2D(vp_.z2d_p, vl_c_[1], vl_h_));
+    CMM_FFT(cufftExecZ2D(vp_.z2d_p, vl_c_[2], vl_h_ + gp.NY));
+    if (mixed_) {
+        const double* lv[1] = {vl_h_};
+        double one[1] = {1.0};
+        CMM_LAUNCH(1, launch_vlasov_table(lv, one, 1, gp.NY, vtab_[3], stream));
+    }
+    return kOk;
+}
+
+int EulerSim::evaluate_potential()
+{
+    // evaluate_potential_from_density_hermite (cmm-simulation-host.cu:385-415):
+    // f on the vort grid, rho = int f dv - 1, phi from the 1D Poisson solve,
+    // psi = phi(x) - h(v) (its Hermite planes written directly, psi is separable)
+    if (mixed_) CMM_LAUNCH(1, launch_sample_m(gc, gv, gf, mapm_, wfm_, realf_, nullptr, stream));
+    else CMM_LAUNCH(1, launch_sample_vort(gc, gv, gf, ChiX, ChiY, wfine, s.molly_stencil, real_buf_, gv.NX, stream));
+    CMM_LAUNCH(2, launch_vlasov_rho(mixed_ ? nullptr : real_buf_, mixed_ ? realf_ : nullptr, gv, vl_part_, vl_rho_, stream));
+    CMM_FFT(cufftExecD2Z(vp_.d2z_v, vl_rho_, vl_c_[0]));
+    CMM_LAUNCH(1, launch_vlasov_phi_spec(vl_c_[0], gv, gp, vl_c_[1], vl_c_[2], stream));
+    double* phi = phi_lv_[0];
+    CMM_FFT(cufftExecZ2D(vp_.z2d_p, vl_c_[1], phi));
+    CMM_FFT(cufftExecZ2D(vp_.z2d_p, vl_c_[2], phi + gp.NX));
+    if (!mixed_) CMM_LAUNCH(1, launch_vlasov_assemble(phi, phi + gp.NX, vl_h_, vl_h_ + gp.NY, gp, psi[0], stream));
+    return kOk;
+}
+
+int EulerSim::vlasov_mesure(double* out)
+{
+    // Vlasov branch of compute_conservation_targets (cmm-simulation-host.cu:639-664),
+    // Compute_* of src/numerical/cmm-mesure.cu:97-202
+    CMM_LAUNCH(2, launch_vlasov_moments(vort, gc, red_, d_scal_, stream));
+    CMM_LAUNCH(2, launch_sumsq(phi_lv_[0] + gp.NX, gp.NX, red_, d_scal_ + 3, stream));
+    CMM_CUDA(cudaMemcpyAsync(real_buf_, phi_lv_[0] + gp.NX, sizeof(double) * gp.NX, cudaMemcpyDeviceToDevice, stream));
+    CMM_FFT(cufftExecD2Z(vp_.d2z_p, real_buf_, vl_c_[0]));
+    CMM_LAUNCH(1, launch_vlasov_modes(vl_c_[0], gp.NX, gp.NX_fft, d_scal_ + 4, stream));
+    CMM_CUDA(cudaMemcpyAsync(h_scal_, d_scal_, sizeof(double) * 8, cudaMemcpyDeviceToHost, stream));
+    CMM_CUDA(cudaStreamSynchronize(stream));
+    double ekin = 0.5 * gc.hy * gc.hx * h_scal_[2];
+    double epot = 0.5 * gp.hx * h_scal_[3];
+    out[0] = ekin + epot;
+    out[1] = ekin;
+    out[2] = epot;
+    out[3] = gc.hy * gc.hx * h_scal_[0];
+    out[4] = gc.hy * gc.hx * h_scal_[1];
+    for (int k = 0; k < 4; ++k) out[5 + k] = h_scal_[4 + k];
     return kOk;
 }
 
@@ -348,6 +440,7 @@ void EulerSim::swap_levels(int a, int b)
 {
     std::swap(psi[a], psi[b]);
     std::swap(psim_[a], psim_[b]);
+    std::swap(phi_lv_[a], phi_lv_[b]);
 }
 
 int EulerSim::advect_m(const double* t, const double* dtv, int lc, int ti_num, int l_order)
@@ -358,19 +451,32 @@ int EulerSim::advect_m(const double* t, const double* dtv, int lc, int ti_num, i
         L1[i] = lagrange_coefficient(t, t[lcl + 1], lcl, i, l_order);
         L12[i] = lagrange_coefficient(t, t[lcl] + dtv[lcl + 1] / 2.0, lcl, i, l_order);
     }
-    // Lagrange extrapolation is linear in psi: combine the levels once per
-    // step, then every RK stage interpolates a single field
-    CMM_LAUNCH(1, launch_precombine(psim_, l_order, L1, ti_num == 30 ? L12 : nullptr, gp.N, psiA_,
-                                    ti_num == 30 ? psiB_ : nullptr, stream));
     AdvectMArgs a{};
+    if (vlasov_) {
+        // separable psi: 1D tables of the combined phi levels (and the static h)
+        const double* lv[kMaxLagrange] = {phi_lv_[0], phi_lv_[1], phi_lv_[2], phi_lv_[3]};
+        double one[1] = {1.0};
+        CMM_LAUNCH(1, launch_vlasov_table(lv, L1, l_order, gp.NX, vtab_[0], stream));
+        if (ti_num == 30) CMM_LAUNCH(1, launch_vlasov_table(lv, L12, l_order, gp.NX, vtab_[1], stream));
+        CMM_LAUNCH(1, launch_vlasov_table(lv, one, 1, gp.NX, vtab_[2], stream));
+        a.tA = vtab_[0]; a.tB = vtab_[1]; a.t0 = vtab_[2]; a.tv = vtab_[3];
+    } else {
+        // Lagrange extrapolation is linear in psi: combine the levels once per
+        // step, then every RK stage interpolates a single field
+        CMM_LAUNCH(1, launch_precombine(psim_, l_order, L1, ti_num == 30 ? L12 : nullptr, gp.N, psiA_,
+                                        ti_num == 30 ? psiB_ : nullptr, stream));
+    }
     a.gm = gc; a.gp = gp;
     a.map = mapm_; a.out = mapm_new_;
     a.psiA = psiA_; a.psiB = psiB_; a.psi0 = psim_[0];
     double coef[4][kMaxFoot];
     map_update_coefficients(s.map_update_order_num, s.map_epsilon, coef, &a.nfoot);
-    for (int p = 0; p < 4; ++p) for (int k = 0; k < kMaxFoot; ++k) a.coef[p][k] = (float)coef[p][k];
+    for (int p = 0; p < 4; ++p)
+        for (int k = 0; k < kMaxFoot; ++k) { a.coef[p][k] = (float)coef[p][k]; a.coef64[p][k] = coef[p][k]; }
     a.dt = (float)dtv[lcl + 1];
     a.ep = (float)s.map_epsilon;
+    a.dt64 = dtv[lcl + 1];
+    a.ep64 = s.map_epsilon;
     a.time_integration_num = ti_num;
     a.rp = gp.NX / gc.NX;
     CMM_LAUNCH(1, launch_advect_m(a, stream));
@@ -420,6 +526,9 @@ void EulerSim::rotate_psi(int n)
     float4* tmf = psim_[n];
     for (int j = n; j >= 1; --j) psim_[j] = psim_[j - 1];
     psim_[0] = tmf;
+    double* tph = phi_lv_[n];
+    for (int j = n; j >= 1; --j) phi_lv_[j] = phi_lv_[j - 1];
+    phi_lv_[0] = tph;
 }
 
 int EulerSim::push_stack()
@@ -501,12 +610,24 @@ int EulerSim::advect_particles(int lcl)
         if (p.num <= 0 || p.tau != 0) continue;
         if (!(t_vec_[lcl + 1] + 1e-5 * dt_vec_[lcl + 1] >= p.init_time)) continue;
         if (mixed_) {
-            if (p.time_integration_num == 30 && !combined) {
+            if (!combined && vlasov_) {
+                // separable psi: tables of level 1 (t_n), the t_{n+1/2} combination and level 0
+                const double* lv[kMaxLagrange] = {phi_lv_[0], phi_lv_[1], phi_lv_[2], phi_lv_[3]};
+                const double* l1[1] = {phi_lv_[L > 1 ? 1 : 0]};
+                double one[1] = {1.0};
+                CMM_LAUNCH(1, launch_vlasov_table(l1, one, 1, gp.NX, vtab_[0], stream));
+                CMM_LAUNCH(1, launch_vlasov_table(lv, Lp12, L, gp.NX, vtab_[1], stream));
+                CMM_LAUNCH(1, launch_vlasov_table(lv, one, 1, gp.NX, vtab_[2], stream));
+                combined = true;
+            } else if (p.time_integration_num == 30 && !combined) {
                 CMM_LAUNCH(1, launch_precombine(psim_, L, Lp12, nullptr, gp.N, psiB_, nullptr, stream));
                 combined = true;
             }
-            cudaError_t e = launch_particles_m(gp, partfix_[i], p.num, psim_[1], psiB_, psim_[0], dt_vec_[lcl + 1],
-                                               p.time_integration_num, stream);
+            cudaError_t e = vlasov_
+                ? launch_particles_m(gp, partfix_[i], p.num, nullptr, nullptr, nullptr, dt_vec_[lcl + 1],
+                                     p.time_integration_num, stream, vtab_[0], vtab_[1], vtab_[2], vtab_[3])
+                : launch_particles_m(gp, partfix_[i], p.num, psim_[1], psiB_, psim_[0], dt_vec_[lcl + 1],
+                                     p.time_integration_num, stream);
             kernel_launches++;
             if (e == cudaErrorInvalidValue) { err = "particle time integration " + p.time_integration + " is not built"; return kErrUnsupported; }
             CMM_CUDA(e);
@@ -538,6 +659,7 @@ int EulerSim::init()
     log_.open(run_dir(s) + "/log.txt");
     log_.quiet = s.verbose < 1;
     if (s.verbose >= 1) {
+        if (vlasov_) log_.push(std::string("Starting Vlasov 1D simulation, initial condition ") + s.initial_condition);
         log_.push("Solving = " + s.simulation_type);
         log_.push("Initial condition = " + s.initial_condition);
         log_.push("Iter max = " + std::to_string(s.iter_max()));
@@ -564,6 +686,7 @@ int EulerSim::init()
     }
 
     if ((rc = reset_map())) return rc;
+    if (vlasov_ && (rc = vlasov_setup_h())) return rc;
     if ((rc = translate_ic()) || (rc = evaluate_stream()) || (rc = coarse_vort())) return rc;
 
     // Lagrange velocity history (cmm-euler2d.cu:520-619): alternate the
@@ -663,6 +786,13 @@ int EulerSim::step_once()
     ph_begin(kPhIncomp);
     if ((rc = incomp(&e_inc_))) return rc;
     ph_end(kPhIncomp);
+    if (vlasov_ && (e_inc_ <= 0 || e_inc_ > 1e15)) {
+        // the Vlasov driver aborts on a vanishing or exploding incompressibility error (cmm-vlasov1d.cu:838-840)
+        err = "incompressibility error out of range in the coarse grid (" + to_str3(e_inc_) + "): run aborted";
+        log_.push(err);
+        continue_ = false;
+        return kErrState;
+    }
     bool saturated = false;
     if (e_inc_ > s.incomp_threshold && !s.skip_remapping) {
         if (n_maps_ >= max_maps) {
@@ -862,10 +992,23 @@ int EulerSim::conservation(double t_now, double dt_now)
     for (auto& r : s.save_computational)
         if (r.conv && instant_fires(r.is_instant, r.time_start, r.time_end, r.time_step, t_now, dt_now, dt)) fire = true;
     if (!fire) return kOk;
+    std::string dir = run_dir(s) + "/Monitoring_data/Mesure/";
+    if (vlasov_) {
+        double v[9];
+        int rv = vlasov_mesure(v);
+        if (rv) return rv;
+        append_f64(dir + "Time_s.data", &t_now, 1);
+        const char* names[9] = {"Etot", "Ekin", "Epot", "Mass", "Momentum", "Emode1", "Emode2", "Emode3", "Emode4"};
+        for (int k = 0; k < 9; ++k) append_f64(dir + names[k] + ".data", &v[k], 1);
+        if (s.verbose >= 3)
+            log_.push("Computed coarse Cons : Etot = " + to_str_prec(v[0], 8) + " \t Momenta = " + to_str_prec(v[4], 8) +
+                      " \t Ekin = " + to_str_prec(v[1], 8) + " \t Epot = " + to_str_prec(v[2], 8) +
+                      " \t Mass = " + to_str_prec(v[3], 8));
+        return kOk;
+    }
     double m[4];
     int rc = diagnostics(&m[0], &m[1], &m[2], &m[3]);
     if (rc) return rc;
-    std::string dir = run_dir(s) + "/Monitoring_data/Mesure/";
     append_f64(dir + "Time_s.data", &t_now, 1);
     append_f64(dir + "Energy.data", &m[0], 1);
     append_f64(dir + "Enstrophy.data", &m[1], 1);
@@ -883,7 +1026,7 @@ size_t EulerSim::field_bytes(const std::string& n) const
     if (n == "Map_ChiX_H_coarse" || n == "Map_ChiY_H_coarse") return sizeof(double) * 4 * gc.N;
     if (n == "Stream_function_Psi_H_psi") return sizeof(double) * 4 * gp.N;
     if (n == "Stream_function_Psi_H_psi_all") return sizeof(double) * 4 * gp.N * L;
-    if (n == "Vorticity_W_coarse") return sizeof(double) * gc.N;
+    if (n == "Vorticity_W_coarse" || n == "Distribution_coarse") return sizeof(double) * gc.N;
     if (n == "Vorticity_W_fine_H") return sizeof(double) * 4 * gf.N;
     if (n == "Map_stack") return sizeof(double) * 8 * gc.N * n_maps_;
     for (size_t i = 0; i < s.particles_advected.size(); ++i) {
@@ -912,9 +1055,18 @@ int EulerSim::get_field(const std::string& n, void* dst, size_t bytes)
         size_t lb = sizeof(double) * 4 * gp.N;
         for (int l = 0; l < L && !rc; ++l) { rc = check(cudaMemcpyAsync(d + l * lb, psi[l], lb, cudaMemcpyDeviceToHost, stream), "get_field"); }
     }
-    else if (n == "Vorticity_W_coarse") rc = cp(vort, bytes);
+    else if (n == "Vorticity_W_coarse" || n == "Distribution_coarse") rc = cp(vort, bytes);
     else if (n == "Vorticity_W_fine_H") rc = cp(wfine, bytes);
-    else if (n == "Map_stack") rc = bytes ? cp(stack, bytes) : kOk;
+    else if (n == "Map_stack" && !mixed_) rc = bytes ? cp(stack, bytes) : kOk;
+    else if (n == "Map_stack") {
+        // FP32 displacement maps -> the reference's planar X | Y layout, one map at a time
+        size_t mb = sizeof(double) * 4 * gc.N;
+        for (int m = 0; m < n_maps_ && !rc; ++m) {
+            rc = check(launch_map_to_planes(stackm_ + 2 * (size_t)m * gc.N, gc, ChiX_new, ChiY_new, stream), "map_to_planes");
+            if (!rc) rc = check(cudaMemcpyAsync(d + 2 * m * mb, ChiX_new, mb, cudaMemcpyDeviceToHost, stream), "get_field");
+            if (!rc) rc = check(cudaMemcpyAsync(d + (2 * m + 1) * mb, ChiY_new, mb, cudaMemcpyDeviceToHost, stream), "get_field");
+        }
+    }
     else {
         for (size_t i = 0; i < s.particles_advected.size(); ++i) {
             std::string id = two((int)i + 1);
@@ -947,6 +1099,17 @@ int EulerSim::get_scalar(const std::string& n, double* out)
         std::string base = std::string("prof_") + phase_name(p);
         if (n == base + "_ms") { *out = prof_ms[p]; return kOk; }
         if (n == base + "_count") { *out = (double)prof_count[p]; return kOk; }
+    }
+    if (vlasov_) {
+        const char* names[9] = {"etot", "ekin", "epot", "mass", "momentum", "emode1", "emode2", "emode3", "emode4"};
+        for (int k = 0; k < 9; ++k)
+            if (n == names[k]) {
+                double v[9];
+                int rv = vlasov_mesure(v);
+                if (rv) return rv;
+                *out = v[k];
+                return kOk;
+            }
     }
     double m[4];
     if (n == "energy" || n == "enstrophy" || n == "palinstrophy" || n == "max_vorticity") {

@@ -15,6 +15,7 @@
 #include "io.hpp"
 #include "kernels.hpp"
 #include "settings.hpp"
+#include "vlasov.hpp"
 
 namespace cmm {
 
@@ -92,6 +93,9 @@ private:
     int init_particles();
     int advect_particles(int lcl);
     int push_stack();
+    int evaluate_potential();          // Vlasov-Poisson psi from the distribution function
+    int vlasov_setup_h();              // the periodification h(v), once per run
+    int vlasov_mesure(double* out9);   // Etot, Ekin, Epot, Mass, Momentum, Emode1..4
     int save_functions(double t_now, double dt_now);
     int write_time_step(double t_now, double dt_now);
     int conservation(double t_now, double dt_now);
@@ -119,6 +123,16 @@ private:
     float4* wdiscm_ = nullptr;       // discrete initial vorticity nodes (FP32 Hermite)
     float4* stackm_ = nullptr;       // n maps, 2*Nc float4 each
     std::vector<unsigned long long*> partfix_;   // tracer positions, 64-bit fixed point (x, y interleaved)
+
+    // Vlasov-Poisson (simulation_type cmm_vlasov_poisson_1d)
+    bool vlasov_ = false;
+    VlasovPlans vp_;
+    double* phi_lv_[kMaxLagrange] = {nullptr, nullptr, nullptr, nullptr};   // per psi level: phi (NX), phi' (NX)
+    double* vl_h_ = nullptr;         // h(v) (NY), h'(v) (NY) on the psi grid
+    double* vl_rho_ = nullptr;       // rho - 1 on the vort grid's x-nodes
+    double* vl_part_ = nullptr;      // v-integral partial sums
+    double2* vl_c_[3] = {nullptr, nullptr, nullptr};   // 1D spectra
+    double2* vtab_[4] = {nullptr, nullptr, nullptr, nullptr};  // mixed form: tables A, B, 0 (x) and h (v)
     float* realf_ = nullptr;         // FP32 real scratch (4 planes of the largest grid)
     float2* specf_ = nullptr;        // FP32 complex scratch
     float2* spec4f_ = nullptr;       // 4 FP32 spectra

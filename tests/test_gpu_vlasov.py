@@ -1,0 +1,169 @@
+"""GPU tests of the Vlasov-Poisson path (simulation_type=cmm_vlasov_poisson_1d).
+
+Plain FP64 against the CPU oracle step by step (same inputs, FP64; the
+oracle takes the reference's 2D FFT of the assembled psi, the product the
+equivalent 1D spectra of its separable parts), the mixed form against plain
+FP64, the analytic t = 0 answers of Landau damping, the reference golden's
+t = 0 rows through the reference's own parameter file, and the reference's
+rejection of a vort grid finer than the psi grid.
+
+Tolerances as in test_gpu_parity.py: maps and spectral Hermite fields in
+units of their conditioning (map_err, herm_err), distribution and
+diagnostics relative 1e-10 after a run with remaps; E_inc absolutely, in
+units of the map's conditioning (einc_tol).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import refloop
+from goldens import DebugRecorder, compare_series, goldens
+from product import cmm, read_monitoring
+from test_gpu_parity import herm_err, map_err, rel_linf
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+PI = np.pi
+CASES = {
+    # name: (initial condition, domain_bounds in units of pi)
+    "landau": ("landau_damping", "{0,4,-2.5,2.5}"),
+    "two_stream": ("two_stream", "{0,10,-2.5,2.5}"),
+}
+
+
+def _args(work, ic, bounds, precision="fp64", coarse=64, fine=128, psi=128, vort=128, sps=32, final_time=2.0,
+          threshold=1e-4):
+    return ["workspace=%s/" % work, "sim_name=vp", "simulation_type=cmm_vlasov_poisson_1d",
+            "initial_condition=%s" % ic, "domain_bounds=%s" % bounds, "grid_coarse=%d" % coarse,
+            "grid_fine=%d" % fine, "grid_vort=%d" % vort, "grid_psi=%d" % psi, "set_dt_by_steps=1",
+            "steps_per_sec=%d" % sps, "final_time=%g" % final_time, "time_integration=RK3", "map_update_order=4th",
+            "map_epsilon=0.001", "incomp_threshold=%r" % threshold, "skip_remapping=0", "molly_stencil=0",
+            "lagrange_init_higher_order=1", "freq_cut_psi=%d" % (psi // 2), "particles_advected_num=0",
+            "save_sample_num=0", "save_zoom_num=0", "forward_map=0", "mem_RAM_CPU_remaps=4000",
+            "save_computational_num=0", "verbose=0", "precision=%s" % precision]
+
+
+def einc_tol(max_x, h, eps=1e-3):
+    """E_inc = max |1 - det grad X| inherits the map's conditioning: the
+    X_xy plane carries footpoint rounding (relative to max|X|) times 1/eps^2,
+    and enters det scaled by the cell size h.  5 u max|X| h / eps^2 is 1.7e-10
+    for C1's Euler map and 8.5e-9 for the two-stream domain (10 pi)."""
+    return 5 * 1.1e-16 * max_x * h / eps ** 2
+
+
+def _oracle(args):
+    s = refloop.Settings()
+    for a in args:
+        s.set_variable(a, "=")
+    s.finalize()
+    return O.EulerOracle(s.oracle_config()), s
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_vlasov_plain_fp64_matches_oracle(tmp_path, case):
+    ic, bounds = CASES[case]
+    args = _args(tmp_path, ic, bounds)
+    m = cmm()
+    sim = m.Simulation(args)
+    sim.init()
+    o, s = _oracle(args)
+    o.init()
+    n = 128
+    psi0 = sim.field("Stream_function_Psi_H_psi_all").reshape(3, -1)
+    ref0 = o.psi(levels=3).reshape(3, -1)
+    for lvl in range(3):
+        assert herm_err(psi0[lvl], ref0[lvl], n) < 1e-12, lvl
+    maps_gpu, maps_cpu = [], []
+    b = s.domain_bounds
+    tol = einc_tol(max(abs(x) for x in b[:4]), (b[1] - b[0]) / s.grid_coarse)
+    while sim.step(1) != 1:
+        _, e, _ = o.step(s.dt)
+        assert abs(sim.scalar("e_inc") - e) < tol
+        maps_gpu.append(int(sim.scalar("map_counter")))
+        maps_cpu.append(o.map_count())
+    assert len(maps_gpu) == 64 and maps_gpu == maps_cpu and maps_gpu[-1] >= 2
+    assert map_err(sim.field("Map_ChiX_H_coarse"), o.chix()) < 1e-10
+    assert map_err(sim.field("Map_ChiY_H_coarse"), o.chiy()) < 1e-10
+    assert herm_err(sim.field("Vorticity_W_fine_H"), o.vort_fine(), 128) < 1e-10
+    assert herm_err(sim.field("Stream_function_Psi_H_psi"), o.psi(), n) < 1e-10
+    assert rel_linf(sim.field("Distribution_coarse"), o.vort()) < 1e-10
+    ref = o.vlasov_mesure()
+    for k in ("Etot", "Ekin", "Epot", "Mass", "Emode1"):
+        assert abs(sim.scalar(k.lower()) - ref[k]) <= 1e-10 * abs(ref[k]), k
+    assert abs(sim.scalar("momentum") - ref["Momentum"]) <= 1e-10 * ref["Mass"]
+    sim.close()
+
+
+def test_vlasov_known_answers_at_t0(tmp_path):
+    """Landau damping at t = 0: Epot = pi/100, |E_1| = 0.05, Ekin = 2 pi,
+    Mass = 4 pi (derivation in test_oracle_golden.py)."""
+    m = cmm()
+    sim = m.Simulation(_args(tmp_path, "landau_damping", "{0,4,-2.5,2.5}", coarse=128, fine=256, psi=256, vort=256))
+    sim.init()
+    assert abs(sim.scalar("epot") - PI / 100) < 1e-12
+    assert abs(sim.scalar("emode1") - 0.05) < 1e-12
+    assert abs(sim.scalar("ekin") - 2 * PI) < 1e-11 and abs(sim.scalar("mass") - 4 * PI) < 1e-11
+    psi = sim.field("Stream_function_Psi_H_psi").reshape(4, 256, 256)
+    v = -2.5 * PI + (5 * PI / 256) * np.arange(256)
+    centre = np.abs(v) < 3.0
+    # 1e-9: on 256 v-nodes the bump's tanh edges span a few points, and the
+    # spectral double integral of the bump is v there only to ~2e-10
+    assert np.max(np.abs(psi[2][centre, :] - v[centre, None])) < 1e-9
+    sim.close()
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_vlasov_mixed_matches_plain_fp64(tmp_path, case):
+    """Mixed form (FP32 displacement maps and distribution nodes, separable
+    psi from 1D FP32 tables, FP64 potential and diagnostics) against plain
+    FP64 over 64 steps with remaps."""
+    ic, bounds = CASES[case]
+    m = cmm()
+    res = {}
+    for prec in ("fp64", "mixed"):
+        sim = m.Simulation(_args(tmp_path, ic, bounds, precision=prec))
+        sim.init()
+        while sim.step(1) != 1:
+            pass
+        res[prec] = ({k: sim.scalar(k) for k in ("etot", "ekin", "epot", "mass", "emode1")},
+                     sim.field("Distribution_coarse"), int(sim.scalar("map_counter")))
+        sim.close()
+    (dp, fp, mp), (dm, fm, mm) = res["fp64"], res["mixed"]
+    for k in ("etot", "ekin", "mass"):
+        assert abs(dm[k] - dp[k]) <= 1e-6 * abs(dp[k]), (k, dm[k], dp[k])
+    for k in ("epot", "emode1"):
+        assert abs(dm[k] - dp[k]) <= 1e-4 * abs(dp[k]), (k, dm[k], dp[k])
+    assert np.max(np.abs(fm - fp)) <= 1e-5 * np.max(np.abs(fp))
+    assert abs(mm - mp) <= 1
+
+
+def test_vlasov_golden_initial_state_through_param_file(tmp_path):
+    """The reference's Vlasov parameter file with grid_psi raised to the vort
+    grid (the current reference rejects its own 256 < 512): the t = 0
+    monitoring rows that do not depend on the potential match the golden."""
+    m = cmm()
+    g = goldens()["vlasov_15"]
+    pf = tmp_path / "params.txt"
+    pf.write_text(g["params_in"])
+    sim = m.Simulation(["param_file=%s" % pf, "workspace=%s/" % tmp_path, "grid_psi=512", "final_time=0"])
+    sim.init()
+    sim.run()
+    import os
+    got = read_monitoring(os.path.join(str(tmp_path), "data", sim.file_name()))
+    sim.close()
+    from test_oracle_golden import RTOL, VLASOV_T0_KEYS
+    first = {k: [got[k][0]] for k in VLASOV_T0_KEYS if k in got}
+    gold = {k: [g["files"][k][0]] for k in VLASOV_T0_KEYS}
+    worst, fails = compare_series(first, gold, VLASOV_T0_KEYS, RTOL)
+    assert len(worst) == len(VLASOV_T0_KEYS)
+    assert not fails, fails
+
+
+def test_vlasov_rejects_vort_grid_finer_than_psi_grid(tmp_path):
+    m = cmm()
+    sim = m.Simulation(_args(tmp_path, "landau_damping", "{0,4,-2.5,2.5}", psi=64, vort=128))
+    with pytest.raises(m.CmmError) as e:
+        sim.init()
+    assert e.value.code == m.CMM_ERR_PARAM
+    sim.close()

@@ -304,6 +304,88 @@ def full_run(m, torch, pf, ic, precision, every=64, final_time=10.0):
     return {"steps": n, "wall_s": wall, "steps_per_s": n / wall, "maps": maps, "series": rec}
 
 
+VLASOV = dict(grid_coarse=256, grid_fine=1024, grid_vort=1024, grid_psi=1024, steps_per_sec=32, final_time=40.0,
+              bounds="{0,4,-2,2}", incomp_threshold=1e-4)
+
+
+def vlasov_initial(n):
+    """f0 = (1 + 0.01 cos(x/2)) v^2 exp(-v^2/2) / sqrt(2 pi) on the n x n nodes of
+    x in [0, 4 pi), v in [-2 pi, 2 pi) (row-major, v the row index)."""
+    x = 4 * np.pi / n * np.arange(n)
+    v = -2 * np.pi + 4 * np.pi / n * np.arange(n)
+    return np.ascontiguousarray((1 + 0.01 * np.cos(0.5 * x))[None, :] * (v * v * np.exp(-v * v / 2)
+                                                                        / np.sqrt(2 * np.pi))[:, None])
+
+
+def run_vlasov(args):
+    """The Vlasov-Poisson configuration in both forms over the whole run:
+    steps/s and the FP64 diagnostics (mass, L2 of f, energies) of the mixed
+    form against plain FP64."""
+    import __graft_entry__ as ge
+    ge.build()
+    m = ge.package()
+    import torch
+    w = VLASOV
+    work = tempfile.mkdtemp(prefix="cmm_vlasov_")
+    f0 = vlasov_initial(w["grid_fine"])
+    final = args.vlasov_final
+    out = {"validation": "Vlasov-Poisson, mixed vs plain FP64 over the whole run", "final_time": final,
+           "workload": "vlasov1d1v f0=(1+0.01cos(x/2)) v^2 exp(-v^2/2)/sqrt(2pi) coarse256 fine1024 psi1024 dt1/32"}
+    res = {}
+    for prec in ("mixed", "fp64"):
+        cli = ["workspace=%s/" % work, "sim_name=vp_%s" % prec, "simulation_type=cmm_vlasov_poisson_1d",
+               "domain_bounds=%s" % w["bounds"], "grid_coarse=%d" % w["grid_coarse"], "grid_fine=%d" % w["grid_fine"],
+               "grid_vort=%d" % w["grid_vort"], "grid_psi=%d" % w["grid_psi"], "set_dt_by_steps=1",
+               "steps_per_sec=%d" % w["steps_per_sec"], "final_time=%r" % final, "initial_condition=landau_damping",
+               "initial_discrete=1", "initial_discrete_grid=%d" % w["grid_fine"], "time_integration=RK3",
+               "map_update_order=4th", "map_epsilon=0.001", "incomp_threshold=%r" % w["incomp_threshold"],
+               "skip_remapping=0", "molly_stencil=0", "lagrange_init_higher_order=1", "mem_RAM_CPU_remaps=20000",
+               "particles_advected_num=0", "save_computational_num=0", "save_sample_num=0", "verbose=0",
+               "precision=%s" % prec]
+        stream = torch.cuda.Stream()
+        sim = m.Simulation(cli, stream=stream.cuda_stream)
+        sim.set_initial_discrete(f0)
+        sim.init()
+        hc = 4 * np.pi / w["grid_coarse"]
+
+        def diag():
+            f = sim.field("Distribution_coarse")
+            return {"t": sim.scalar("time"), "maps": int(sim.scalar("map_counter")), "mass": sim.scalar("mass"),
+                    "l2": float(hc * hc * np.sum(f * f)), "etot": sim.scalar("etot"), "ekin": sim.scalar("ekin"),
+                    "epot": sim.scalar("epot"), "emode1": sim.scalar("emode1")}
+
+        series = [diag()]
+        every = 5 * w["steps_per_sec"]
+        torch.cuda.synchronize()
+        wall = 0.0
+        n = 0
+        t0 = time.perf_counter()
+        while True:
+            rc = sim.step(1)
+            if rc == 1:
+                break
+            n += 1
+            if n % every == 0:
+                torch.cuda.synchronize()
+                wall += time.perf_counter() - t0
+                series.append(diag())
+                t0 = time.perf_counter()
+        torch.cuda.synchronize()
+        wall += time.perf_counter() - t0
+        res[prec] = dict(series[-1], steps=n, wall_s=wall, steps_per_s=n / wall, series=series)
+        sim.close()
+    keys = ("mass", "l2", "etot", "ekin", "epot", "emode1")
+    out["mixed"] = {k: v for k, v in res["mixed"].items() if k != "series"}
+    out["plain_fp64"] = {k: v for k, v in res["fp64"].items() if k != "series"}
+    out["speedup"] = res["mixed"]["steps_per_s"] / res["fp64"]["steps_per_s"]
+    out["rel_err"] = {k: abs(res["mixed"][k] - res["fp64"][k]) / abs(res["fp64"][k]) for k in keys}
+    out["rel_err_series"] = [dict({"t": round(a["t"], 3), "maps_mixed": a["maps"], "maps_plain": b["maps"]},
+                                  **{k: abs(a[k] - b[k]) / abs(b[k]) for k in keys})
+                             for a, b in zip(res["mixed"]["series"], res["fp64"]["series"])]
+    print(json.dumps(out))
+    shutil.rmtree(work, ignore_errors=True)
+
+
 def run_t10(args):
     """Both forms to T = 10: the metric's enstrophy error over the whole run."""
     import __graft_entry__ as ge
@@ -474,9 +556,13 @@ def main():
     ap.add_argument("--t10-final", type=float, default=10.0)
     ap.add_argument("--t10-particles", type=int, default=WORKLOAD["particles"])
     ap.add_argument("--fp64-peak", action="store_true", help="measure the FP64 rate (cuBLAS DGEMM) and exit")
+    ap.add_argument("--vlasov", action="store_true", help="run the Vlasov-Poisson configuration in both forms")
+    ap.add_argument("--vlasov-final", type=float, default=VLASOV["final_time"])
     args = ap.parse_args()
     if args.fp64_peak:
         measure_fp64_peak()
+    elif args.vlasov:
+        run_vlasov(args)
     elif args.impl == "reference":
         run_reference(args)
     elif args.t10:

@@ -29,7 +29,8 @@ EXPORTS = [
     "cmm_settings_text",
     "cmm_file_name", "cmm_destroy", "cmm_advect_map", "cmm_incomp_max", "cmm_compose_stack", "cmm_sample_vort",
     "cmm_poisson_create", "cmm_poisson_hermite", "cmm_poisson_destroy", "cmm_particles_advect", "cmm_diagnostics",
-    "cmm_diagnostics_noalloc",
+    "cmm_diagnostics_noalloc", "cmm_compose_stack_var", "cmm_vlasov_create", "cmm_vlasov_potential",
+    "cmm_vlasov_diagnostics", "cmm_vlasov_destroy",
 ]
 
 
@@ -90,6 +91,11 @@ def lib():
     L.cmm_particles_advect.argtypes = [gp, vp, ip, C.POINTER(vp), ip, dp, C.c_double, ip, vp]
     L.cmm_diagnostics.argtypes = [gp, vp, gp, vp, dp, vp]
     L.cmm_diagnostics_noalloc.argtypes = [gp, vp, gp, vp, dp, vp]
+    L.cmm_compose_stack_var.argtypes = [gp, gp, vp, vp, vp, ip, ip, ip, vp, gp, vp, vp]
+    L.cmm_vlasov_create.argtypes = [gp, gp, vp, C.POINTER(vp)]
+    L.cmm_vlasov_potential.argtypes = [vp, gp, gp, vp, vp, vp, ip, vp]
+    L.cmm_vlasov_diagnostics.argtypes = [vp, gp, vp, vp, dp]
+    L.cmm_vlasov_destroy.argtypes = [vp]
     _lib = L
     return L
 
@@ -243,3 +249,37 @@ def diagnostics_noalloc(gp, psi, gc, vort, stream=None):
     out = (C.c_double * 3)()
     check(lib().cmm_diagnostics_noalloc(C.byref(gp), _dptr(psi), C.byref(gc), _dptr(vort), out, stream))
     return list(out)
+
+
+def compose_stack_var(gm, gt, chix, chiy, stack, n_maps, var_num, ic_num, out, discrete=None, gd=None, stream=None):
+    """cmm_compose_stack_var: var_num 0 vorticity, 1 passive scalar, 2 Vlasov distribution."""
+    check(lib().cmm_compose_stack_var(C.byref(gm), C.byref(gt), _dptr(chix), _dptr(chiy), _dptr(stack), n_maps, var_num,
+                                      ic_num, _dptr(discrete), C.byref(gd) if gd is not None else None, _dptr(out),
+                                      stream))
+
+
+class VlasovPotential:
+    """cmm_vlasov_*: the Vlasov-Poisson potential and conservation targets on
+    caller-owned device buffers."""
+
+    def __init__(self, grid_vort, grid_psi, stream=None):
+        self.h = C.c_void_p()
+        self.gv, self.gp = grid_vort, grid_psi
+        check(lib().cmm_vlasov_create(C.byref(grid_vort), C.byref(grid_psi), stream, C.byref(self.h)))
+
+    def potential(self, gm, gf, chix, chiy, f_fine, psi_out, molly=0):
+        check(lib().cmm_vlasov_potential(self.h, C.byref(gm), C.byref(gf), _dptr(chix), _dptr(chiy), _dptr(f_fine),
+                                         molly, _dptr(psi_out)))
+
+    def diagnostics(self, gc, f_coarse, psi):
+        out = (C.c_double * 9)()
+        check(lib().cmm_vlasov_diagnostics(self.h, C.byref(gc), _dptr(f_coarse), _dptr(psi), out))
+        return list(out)
+
+    def close(self):
+        if self.h:
+            lib().cmm_vlasov_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

@@ -11,6 +11,7 @@
 #include "kernels.hpp"
 #include "settings.hpp"
 #include "sim.hpp"
+#include "vlasov.hpp"
 
 namespace cmm {
 void set_last_error(const std::string& msg);
@@ -30,6 +31,21 @@ struct cmm_poisson {
     cmm::FftPlans pv, pp;
     double2* spec = nullptr;
     double2* spec4 = nullptr;
+};
+
+struct cmm_vlasov {
+    cmm::Grid gv, gp;
+    cudaStream_t stream = nullptr;
+    cmm::VlasovPlans plans;
+    double* h = nullptr;       // h (NY), h' (NY)
+    double* fs = nullptr;      // f on the vort grid
+    double* rho = nullptr;
+    double* part = nullptr;
+    double* phi = nullptr;     // phi (NX), phi' (NX)
+    double* red = nullptr;
+    double* scal = nullptr;
+    double* row = nullptr;
+    double2* c[3] = {nullptr, nullptr, nullptr};
 };
 
 namespace {
@@ -78,7 +94,10 @@ void cmm::set_last_error(const std::string& msg) { g_err = msg; }
 extern "C" {
 
 const char* cmm_last_error(void) { return g_err.c_str(); }
-const char* cmm_version(void) { return "cmm-gb300 0.1 (sm_103a, FP64 plain form)"; }
+const char* cmm_version(void)
+{
+    return "cmm-gb300 0.2 (sm_103a; Euler 2D and Vlasov-Poisson 1D1V; plain FP64 and mixed forms)";
+}
 
 int cmm_create(int argc, const char* const* argv, cmm_ctx** out)
 {
@@ -263,6 +282,119 @@ int cmm_compose_stack(const cmm_grid* grid_map, const cmm_grid* grid_target, con
     }
     return cuda_rc(cmm::launch_compose_sample(gm, gt, chix, chiy, stack, n_maps, src, out, static_cast<cudaStream_t>(stream)),
                    "cmm_compose_stack");
+}
+
+int cmm_compose_stack_var(const cmm_grid* grid_map, const cmm_grid* grid_target, const double* chix,
+                          const double* chiy, const double* stack, int n_maps, int var_num, int ic_num,
+                          const double* discrete, const cmm_grid* grid_discrete, double* out, void* stream)
+{
+    if (var_num == 0 || discrete)
+        return cmm_compose_stack(grid_map, grid_target, chix, chiy, stack, n_maps, ic_num, discrete, grid_discrete, out,
+                                 stream);
+    cmm::Grid gm, gt;
+    if (!to_grid(grid_map, &gm) || !to_grid(grid_target, &gt)) return fail(CMM_ERR_PARAM, "bad grid");
+    if (!chix || !chiy || !out || n_maps < 0 || (n_maps > 0 && !stack)) return fail(CMM_ERR_PARAM, "bad pointer / map count");
+    if ((var_num == 1 && (ic_num < 0 || ic_num > 2)) || (var_num == 2 && (ic_num < 0 || ic_num > 2)) || var_num < 0 ||
+        var_num > 2)
+        return fail(CMM_ERR_PARAM, "var_num / ic_num out of range");
+    cmm::InitSource src{};
+    src.kind = var_num;
+    src.ic_num = ic_num;
+    return cuda_rc(cmm::launch_compose_sample(gm, gt, chix, chiy, stack, n_maps, src, out, static_cast<cudaStream_t>(stream)),
+                   "cmm_compose_stack_var");
+}
+
+int cmm_vlasov_create(const cmm_grid* grid_vort, const cmm_grid* grid_psi, void* stream, cmm_vlasov** out)
+{
+    if (!out) return fail(CMM_ERR_PARAM, "out is NULL");
+    *out = nullptr;
+    cmm_vlasov* p = new (std::nothrow) cmm_vlasov();
+    if (!p) return fail(CMM_ERR_PARAM, "out of host memory");
+    if (!to_grid(grid_vort, &p->gv) || !to_grid(grid_psi, &p->gp)) { delete p; return fail(CMM_ERR_PARAM, "bad grid"); }
+    if (p->gv.NX > p->gp.NX || p->gv.NY > p->gp.NY) { delete p; return fail(CMM_ERR_PARAM, "vort grid finer than psi grid"); }
+    if (p->gp.NX != p->gp.NY) { delete p; return fail(CMM_ERR_PARAM, "psi grid must be square"); }
+    p->stream = static_cast<cudaStream_t>(stream);
+    const int nchunks = (p->gv.NY + cmm::kVlasovRowChunk - 1) / cmm::kVlasovRowChunk;
+    const int cn = p->gv.NX_fft > p->gp.NX_fft ? p->gv.NX_fft : p->gp.NX_fft;
+    bool ok = cmm::make_vlasov_plans(p->plans, p->gv, p->gp, p->stream) &&
+              cudaMalloc((void**)&p->h, sizeof(double) * 2 * p->gp.NY) == cudaSuccess &&
+              cudaMalloc((void**)&p->fs, sizeof(double) * p->gv.N) == cudaSuccess &&
+              cudaMalloc((void**)&p->rho, sizeof(double) * p->gv.NX) == cudaSuccess &&
+              cudaMalloc((void**)&p->part, sizeof(double) * nchunks * p->gv.NX) == cudaSuccess &&
+              cudaMalloc((void**)&p->phi, sizeof(double) * 2 * p->gp.NX) == cudaSuccess &&
+              cudaMalloc((void**)&p->red, sizeof(double) * 3 * cmm::kReduceBlocks) == cudaSuccess &&
+              cudaMalloc((void**)&p->scal, sizeof(double) * 16) == cudaSuccess &&
+              cudaMalloc((void**)&p->row, sizeof(double) * (p->gp.NX > p->gp.NY ? p->gp.NX : p->gp.NY)) == cudaSuccess;
+    for (int k = 0; k < 3 && ok; ++k) ok = cudaMalloc((void**)&p->c[k], sizeof(double2) * cn) == cudaSuccess;
+    if (!ok) { cmm_vlasov_destroy(p); return fail(CMM_ERR_CUDA, "cuFFT plan or cudaMalloc failed"); }
+    // the periodification h(v) and h'(v) once
+    cudaError_t e = cmm::launch_vlasov_bump(p->gp, p->row, p->stream);
+    if (e == cudaSuccess && cufftExecD2Z(p->plans.d2z_p, p->row, reinterpret_cast<cufftDoubleComplex*>(p->c[0])) != CUFFT_SUCCESS)
+        e = cudaErrorUnknown;
+    if (e == cudaSuccess) e = cmm::launch_vlasov_h_spec(p->c[0], p->gp, p->c[1], p->c[2], p->stream);
+    if (e == cudaSuccess && (cufftExecZ2D(p->plans.z2d_p, reinterpret_cast<cufftDoubleComplex*>(p->c[1]), p->h) != CUFFT_SUCCESS ||
+                             cufftExecZ2D(p->plans.z2d_p, reinterpret_cast<cufftDoubleComplex*>(p->c[2]), p->h + p->gp.NY) != CUFFT_SUCCESS))
+        e = cudaErrorUnknown;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+    if (e != cudaSuccess) { cmm_vlasov_destroy(p); return cuda_rc(e, "cmm_vlasov_create"); }
+    *out = p;
+    return CMM_OK;
+}
+
+int cmm_vlasov_potential(cmm_vlasov* p, const cmm_grid* grid_map, const cmm_grid* grid_fine, const double* chix,
+                         const double* chiy, const double* f_fine_H, int molly_stencil, double* psi_out)
+{
+    if (!p || !chix || !chiy || !f_fine_H || !psi_out) return fail(CMM_ERR_PARAM, "NULL argument");
+    cmm::Grid gm, gf;
+    if (!to_grid(grid_map, &gm) || !to_grid(grid_fine, &gf)) return fail(CMM_ERR_PARAM, "bad grid");
+    if (molly_stencil != 0 && molly_stencil != 4 && molly_stencil != 8) return fail(CMM_ERR_PARAM, "molly_stencil must be 0, 4 or 8");
+    cudaStream_t s = p->stream;
+    cudaError_t e = cmm::launch_sample_vort(gm, p->gv, gf, chix, chiy, f_fine_H, molly_stencil, p->fs, p->gv.NX, s);
+    if (e == cudaSuccess) e = cmm::launch_vlasov_rho(p->fs, nullptr, p->gv, p->part, p->rho, s);
+    if (e == cudaSuccess && cufftExecD2Z(p->plans.d2z_v, p->rho, reinterpret_cast<cufftDoubleComplex*>(p->c[0])) != CUFFT_SUCCESS)
+        return fail(CMM_ERR_CUDA, "cuFFT D2Z failed");
+    if (e == cudaSuccess) e = cmm::launch_vlasov_phi_spec(p->c[0], p->gv, p->gp, p->c[1], p->c[2], s);
+    if (e == cudaSuccess && (cufftExecZ2D(p->plans.z2d_p, reinterpret_cast<cufftDoubleComplex*>(p->c[1]), p->phi) != CUFFT_SUCCESS ||
+                             cufftExecZ2D(p->plans.z2d_p, reinterpret_cast<cufftDoubleComplex*>(p->c[2]), p->phi + p->gp.NX) != CUFFT_SUCCESS))
+        return fail(CMM_ERR_CUDA, "cuFFT Z2D failed");
+    if (e == cudaSuccess) e = cmm::launch_vlasov_assemble(p->phi, p->phi + p->gp.NX, p->h, p->h + p->gp.NY, p->gp, psi_out, s);
+    return cuda_rc(e, "cmm_vlasov_potential");
+}
+
+int cmm_vlasov_diagnostics(cmm_vlasov* p, const cmm_grid* grid_coarse, const double* f_coarse, const double* psi,
+                           double* out9)
+{
+    if (!p || !f_coarse || !psi || !out9) return fail(CMM_ERR_PARAM, "NULL argument");
+    cmm::Grid gc;
+    if (!to_grid(grid_coarse, &gc)) return fail(CMM_ERR_PARAM, "bad grid");
+    const cmm::Grid& gp = p->gp;
+    cudaStream_t s = p->stream;
+    cudaError_t e = cmm::launch_vlasov_moments(f_coarse, gc, p->red, p->scal, s);
+    if (e == cudaSuccess) e = cmm::launch_sumsq(psi + gp.N, gp.NX, p->red, p->scal + 3, s);   // first row of psi_x
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p->row, psi + gp.N, sizeof(double) * gp.NX, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && cufftExecD2Z(p->plans.d2z_p, p->row, reinterpret_cast<cufftDoubleComplex*>(p->c[0])) != CUFFT_SUCCESS)
+        return fail(CMM_ERR_CUDA, "cuFFT D2Z failed");
+    if (e == cudaSuccess) e = cmm::launch_vlasov_modes(p->c[0], gp.NX, gp.NX_fft, p->scal + 4, s);
+    double h[8] = {0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, p->scal, sizeof(double) * 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_rc(e, "cmm_vlasov_diagnostics");
+    double ekin = 0.5 * gc.hy * gc.hx * h[2], epot = 0.5 * gp.hx * h[3];
+    out9[0] = ekin + epot; out9[1] = ekin; out9[2] = epot;
+    out9[3] = gc.hy * gc.hx * h[0]; out9[4] = gc.hy * gc.hx * h[1];
+    for (int k = 0; k < 4; ++k) out9[5 + k] = h[4 + k];
+    return CMM_OK;
+}
+
+int cmm_vlasov_destroy(cmm_vlasov* p)
+{
+    if (!p) return CMM_OK;
+    cmm::destroy_vlasov_plans(p->plans);
+    auto f = [](void* q) { if (q) cudaFree(q); };
+    f(p->h); f(p->fs); f(p->rho); f(p->part); f(p->phi); f(p->red); f(p->scal); f(p->row);
+    for (int k = 0; k < 3; ++k) f(p->c[k]);
+    delete p;
+    return CMM_OK;
 }
 
 int cmm_sample_vort(const cmm_grid* grid_map, const cmm_grid* grid_out, const cmm_grid* grid_fine, const double* chix,

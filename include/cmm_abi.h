@@ -3,8 +3,10 @@
  * time-step library, libcmm_gb300.so.
  *
  * Two levels:
- *  1. Context API: a drop-in for the reference driver cuda_euler_2d
- *     (Cuda-CMM/src/simulation/cmm-euler2d.cu:45-1099) configured exactly like
+ *  1. Context API: a drop-in for the reference drivers cuda_euler_2d
+ *     (Cuda-CMM/src/simulation/cmm-euler2d.cu:45-1099) and cuda_vlasov_1d
+ *     (src/simulation/cmm-vlasov1d.cu:48-1148, simulation_type
+ *     cmm_vlasov_poisson_1d), configured exactly like
  *     the reference executable (src/main2d.cpp:66-105): presets, then every
  *     param_file=F argument, then COMMAND=VALUE arguments.  It writes the
  *     reference's output tree (data/<sim_name>_<ic>_C<c>_F<f>_t<1/dt>_T<T>/).
@@ -81,7 +83,9 @@ int cmm_run(cmm_ctx* ctx);
 /* Copy a field to host memory, in the reference's layout.  Names follow the
  * reference's output files: "Map_ChiX_H_coarse", "Map_ChiY_H_coarse" (4*Nc),
  * "Stream_function_Psi_H_psi" (4*Npsi, newest level), "Stream_function_Psi_H_psi_all"
- * (L*4*Npsi), "Vorticity_W_coarse" (Nc), "Vorticity_W_fine_H" (4*Nf),
+ * (L*4*Npsi), "Vorticity_W_coarse" (Nc; for Vlasov-Poisson the distribution,
+ * also as "Distribution_coarse"), "Vorticity_W_fine_H" (4*Nf), "Map_stack"
+ * (n_maps * 8*Nc, oldest first),
  * "Particles_advected_pos_PNN" (2*num), "Particles_advected_vel_UNN" (2*num).
  * bytes must equal the field size. */
 int cmm_get_field(cmm_ctx* ctx, const char* name, void* host_dst, size_t bytes);
@@ -89,9 +93,10 @@ int cmm_get_field(cmm_ctx* ctx, const char* name, void* host_dst, size_t bytes);
 size_t cmm_field_bytes(cmm_ctx* ctx, const char* name);
 
 /* Scalars: "time", "dt", "e_inc", "map_counter", "map_gap", "loop_ctr",
- * "lagrange_order", "energy", "enstrophy", "palinstrophy", "max_vorticity",
- * "stack_capacity".  Diagnostics are computed on request
- * (src/numerical/cmm-mesure.cu:30-89). */
+ * "lagrange_order", "stack_capacity"; Euler: "energy", "enstrophy",
+ * "palinstrophy", "max_vorticity" (src/numerical/cmm-mesure.cu:30-89);
+ * Vlasov-Poisson: "etot", "ekin", "epot", "mass", "momentum", "emode1".."emode4"
+ * (src/numerical/cmm-mesure.cu:97-202).  Diagnostics are computed on request. */
 int cmm_get_scalar(cmm_ctx* ctx, const char* name, double* out);
 
 /* Time each loop phase with CUDA events on the context stream (adds one
@@ -150,6 +155,16 @@ int cmm_compose_stack(const cmm_grid* grid_map, const cmm_grid* grid_target, con
                       const double* chiy, const double* stack, int n_maps, int ic_num,
                       const double* discrete, const cmm_grid* grid_discrete, double* out, void* stream);
 
+/* As cmm_compose_stack for the initial field selected by var_num, the
+ * reference's last argument of translate_initial_condition_through_map_stack
+ * (cmm-simulation-host.cu:299-327; k_h_sample_from_init,
+ * cmm-simulation-kernel.cu:342-373): 0 vorticity, 1 passive scalar,
+ * 2 Vlasov distribution function (ic_num 0 landau_damping, 1 two_stream,
+ * 2 nonlin_landau_damping). */
+int cmm_compose_stack_var(const cmm_grid* grid_map, const cmm_grid* grid_target, const double* chix,
+                          const double* chiy, const double* stack, int n_maps, int var_num, int ic_num,
+                          const double* discrete, const cmm_grid* grid_discrete, double* out, void* stream);
+
 /* omega(x) = W_fine(X(x)) on grid_out (molly_stencil 0, 4 or 8).  Replaces
  * k_apply_map_and_sample_from_hermite (src/simulation/cmm-simulation-kernel.cu:402-461). */
 int cmm_sample_vort(const cmm_grid* grid_map, const cmm_grid* grid_out, const cmm_grid* grid_fine,
@@ -165,6 +180,25 @@ int cmm_poisson_create(const cmm_grid* grid_vort, const cmm_grid* grid_psi, doub
                        cmm_poisson** out);
 int cmm_poisson_hermite(cmm_poisson* p, const double* vort, double* psi_out);
 int cmm_poisson_destroy(cmm_poisson* p);
+
+/* Vlasov-Poisson potential.  Replaces evaluate_potential_from_density_hermite
+ * (src/simulation/cmm-simulation-host.cu:385-471,534-571): f = f_fine_H o X on
+ * grid_vort, rho = h_v sum_v f - 1, phi from the 1D Poisson solve on the x
+ * axis, psi = phi(x) - h(v) with h the periodification of the velocity, and
+ * psi's Hermite planes [psi, psi_x, psi_y, psi_xy] on grid_psi (4*Npsi
+ * doubles).  grid_vort may not be finer than grid_psi and grid_psi must be
+ * square (the reference's restrictions, CMM_ERR_PARAM).  h is built at
+ * creation (it depends on the grid only). */
+typedef struct cmm_vlasov cmm_vlasov;
+int cmm_vlasov_create(const cmm_grid* grid_vort, const cmm_grid* grid_psi, void* stream, cmm_vlasov** out);
+int cmm_vlasov_potential(cmm_vlasov* p, const cmm_grid* grid_map, const cmm_grid* grid_fine, const double* chix,
+                         const double* chiy, const double* f_fine_H, int molly_stencil, double* psi_out);
+/* Vlasov conservation targets (cmm-simulation-host.cu:639-664, cmm-mesure.cu:97-202):
+ * out9 = {Etot, Ekin, Epot, Mass, Momentum, |E_1|..|E_4|} from the coarse
+ * distribution f_coarse (grid_coarse) and psi (grid_psi).  Synchronises the stream. */
+int cmm_vlasov_diagnostics(cmm_vlasov* p, const cmm_grid* grid_coarse, const double* f_coarse, const double* psi,
+                           double* out9);
+int cmm_vlasov_destroy(cmm_vlasov* p);
 
 /* Tracer particles (tau = 0).  Replaces particles_advect / Particle_advect
  * (src/numerical/cmm-particles.cu:63-87,119-276).  pos: 2*num interleaved

@@ -104,6 +104,16 @@ cudaError_t launch_spec_psi(const double2* Fv, const Grid& gv, const Grid& gp, d
 // raw D2Z spectrum -> normalised (dx F, dy F) for the palinstrophy (cmm-mesure.cu:77-89)
 cudaError_t launch_spec_grad(const double2* F, const Grid& g, double2* out2, cudaStream_t s);
 
+// ---------------------------------------------------------------- sampled outputs
+// positions of the nodes of gt through the current map and n_maps stacked maps (wrapped)
+cudaError_t launch_compose_pos(const Grid& gm, const Grid& gt, const double* X, const double* Y, const double* stack,
+                               int n_maps, double* px, double* py, cudaStream_t s);
+// an initial field at n positions (src.kind 0 vorticity, 1 scalar, 2 distribution, 3 discrete)
+cudaError_t launch_eval_init(const double* px, const double* py, long long n, const InitSource& src, double* out,
+                             cudaStream_t s);
+// normalised spectral operator on a D2Z half spectrum: 0 Laplacian, 1 d/dx, 2 d/dy, 3 inverse Laplacian
+cudaError_t launch_spec_op(const double2* in, const Grid& g, int op, double2* out, cudaStream_t s);
+
 // ---------------------------------------------------------------- reductions
 // min, max, max(0,max), sum over n values at stride `stride` (Debug_globals);
 // result -> d_out[4]; partial scratch of kReduceBlocks*4 doubles

@@ -45,6 +45,9 @@ cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_
 // positions; a discrete initial field (src.kind 3) is read from its FP32 Hermite nodes disc
 cudaError_t launch_compose_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
                              const InitSource& src, const float4* disc, double* out, cudaStream_t s);
+// positions of the nodes of gt through the current map and the stack (fixed point), as FP64
+cudaError_t launch_compose_pos_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
+                                 double* px, double* py, cudaStream_t s);
 // W(x + d(x)) on grid go (Ngo multiple of Nmap, Nf multiple of Ngo); out_f or out_d
 cudaError_t launch_sample_m(const Grid& gm, const Grid& go, const Grid& gf, const float4* map, const float4* W,
                             float* out_f, double* out_d, cudaStream_t s);

@@ -674,6 +674,45 @@ cudaError_t launch_compose_m(const Grid& gm, const Grid& gt, const float4* map, 
     return cudaGetLastError();
 }
 
+// positions of the nodes of gt through the current map and the stack, at
+// fixed-point precision, returned as FP64 coordinates in [b0, b0 + W)
+__global__ void __launch_bounds__(256) k_compose_pos_m(Grid gm, Grid gt, unsigned long long stx, unsigned long long sty,
+                                                       float2 scx, float2 scy, const float4* __restrict__ map,
+                                                       const float4* __restrict__ stack, int n_maps,
+                                                       double* __restrict__ px, double* __restrict__ py)
+{
+    const int iX = blockIdx.x * blockDim.x + threadIdx.x, iY = blockIdx.y;
+    if (iX >= gt.NX) return;
+    unsigned long long Px = (unsigned long long)iX * stx, Py = (unsigned long long)iY * sty;
+    int cx, cy;
+    float tx, ty, dx, dy;
+    fix_cell(Px, gm.NX, cx, tx);
+    fix_cell(Py, gm.NY, cy, ty);
+    map_disp_f(map, gm, locate_q(gm, cx, cy, tx, ty), 0.0f, 0.0f, dx, dy);
+    Px += fix_increment(dx, scx);
+    Py += fix_increment(dy, scy);
+    for (int m = n_maps - 1; m >= 0; --m) {
+        fix_cell(Px, gm.NX, cx, tx);
+        fix_cell(Py, gm.NY, cy, ty);
+        map_disp_f(stack + 2 * (long long)m * gm.N, gm, locate_q(gm, cx, cy, tx, ty), 0.0f, 0.0f, dx, dy);
+        Px += fix_increment(dx, scx);
+        Py += fix_increment(dy, scy);
+    }
+    const long long i = (long long)iY * gt.NX + iX;
+    px[i] = gm.b0 + __ull2double_rn(Px) * (gm.Wx * 5.42101086242752217e-20);
+    py[i] = gm.b2 + __ull2double_rn(Py) * (gm.Wy * 5.42101086242752217e-20);
+}
+
+cudaError_t launch_compose_pos_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
+                                 double* px, double* py, cudaStream_t s)
+{
+    if (gt.b0 != gm.b0 || gt.b2 != gm.b2 || gt.Wx != gm.Wx || gt.Wy != gm.Wy || gt.NY > 65535) return cudaErrorInvalidValue;
+    dim3 blocks((unsigned)((gt.NX + 255) / 256), (unsigned)gt.NY);
+    k_compose_pos_m<<<blocks, 256, 0, s>>>(gm, gt, fix_step(gt.NX), fix_step(gt.NY), fix_scale(gm.Wx), fix_scale(gm.Wy),
+                                           map, stack, n_maps, px, py);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // omega(x) = W(x + d(x)) on an output grid whose spacing divides the map's and
 // the fine grid's (integer ratios ro = No / Nm, rf = Nf / No).  One thread per

@@ -286,6 +286,10 @@ void EulerSim::release()
     for (int k = 0; k < 4; ++k) { f(vtab_[k]); vtab_[k] = nullptr; }
     destroy_vlasov_plans(vp_);
     f(wdiscm_); wdiscm_ = nullptr;
+    for (auto& p : smp_) { f(p); p = nullptr; }
+    for (auto& p : smp_c_) { f(p); p = nullptr; }
+    destroy_plans(ps_);
+    smp_n_ = smp_plan_n_ = 0;
     f(mapm_); f(mapm_new_); f(psiA_); f(psiB_); f(wfm_); f(stackm_); f(realf_); f(specf_); f(spec4f_);
     for (int l = 0; l < kMaxLagrange; ++l) { f(psim_[l]); psim_[l] = nullptr; }
     mapm_ = mapm_new_ = psiA_ = psiB_ = wfm_ = stackm_ = nullptr;
@@ -871,6 +875,127 @@ int EulerSim::save_functions(double t_now, double dt_now)
     int rc;
     if ((rc = write_time_step(t_now, dt_now))) return rc;
     if ((rc = conservation(t_now, dt_now))) return rc;
+    if ((rc = sample_outputs(t_now, dt_now))) return rc;
+    return kOk;
+}
+
+int EulerSim::sample_outputs(double t_now, double dt_now)
+{
+    // sample_compute_and_write, backward-map part (src/simulation/cmm-simulation-host.cu:706-893):
+    // the full map on the sample grid, scalar and vorticity there, their spectral
+    // derivatives, psi and velocity, the sample-grid conservation values
+    if (vlasov_) return kOk;
+    for (auto& r : s.save_sample) {
+        if (r.grid <= 0 || !instant_fires(r.is_instant, r.time_start, r.time_end, r.time_step, t_now, dt_now, dt)) continue;
+        const int n = r.grid;
+        Grid gs = make_grid(n, n, s.domain_bounds);
+        if (n > smp_n_) {
+            auto f = [](void* p) { if (p) cudaFree(p); };
+            for (auto& p : smp_) { f(p); p = nullptr; }
+            for (auto& p : smp_c_) { f(p); p = nullptr; }
+            for (auto& p : smp_) CMM_CUDA(cudaMalloc((void**)&p, sizeof(double) * (size_t)gs.N));
+            for (auto& p : smp_c_) CMM_CUDA(cudaMalloc((void**)&p, sizeof(double2) * (size_t)gs.Nfft));
+            smp_n_ = n;
+        }
+        if (n != smp_plan_n_) {
+            destroy_plans(ps_);
+            smp_plan_n_ = 0;
+            if (!make_plans(ps_, gs, stream)) { err = "cuFFT plan creation failed (sample grid)"; return kErrCuda; }
+            smp_plan_n_ = n;
+        }
+        double *X = smp_[0], *Y = smp_[1], *S = smp_[2], *W = smp_[3], *P = smp_[4], *T = smp_[5];
+        double2 *F0 = smp_c_[0], *F1 = smp_c_[1];
+        const std::string ns = std::to_string(n), var = r.var;
+        const bool all = has(var, "All"), dbg = s.verbose >= 4;
+        const std::string tname = std::abs(t_now - kTMax) < 1 ? "final" : to_str3(t_now);
+        const std::string sub = "/Time_data/Time_" + tname, mdir = run_dir(s) + "/Monitoring_data/";
+        if (dbg) append_f64(mdir + "Debug_globals/Time_s_" + ns + ".data", &t_now, 1);
+        else make_dir(run_dir(s) + sub);
+        auto out = [&](const std::string& name, const double* v) {
+            return dbg ? debug_globals(name + "_" + ns, v, gs.N, true, gs) : write_field(sub, name + "_" + ns, v, gs.N);
+        };
+        auto sumsq = [&](const double* v, double* hv) {
+            int rc2 = check(launch_sumsq(v, gs.N, red_, d_scal_ + 12, stream), "sumsq");
+            kernel_launches += 2;
+            if (!rc2) rc2 = check(cudaMemcpyAsync(h_scal_ + 12, d_scal_ + 12, sizeof(double), cudaMemcpyDeviceToHost, stream), "copy");
+            if (!rc2) rc2 = check(cudaStreamSynchronize(stream), "sync");
+            *hv = h_scal_[12];
+            return rc2;
+        };
+        // spectral operator op of the field whose half spectrum is in F0 -> T (F1 is consumed)
+        auto spec = [&](int op, double* dst) {
+            int rc2 = check(launch_spec_op(F0, gs, op, F1, stream), "spec_op");
+            kernel_launches++;
+            if (!rc2 && cufftExecZ2D(ps_.z2d1, reinterpret_cast<cufftDoubleComplex*>(F1), dst) != CUFFT_SUCCESS) {
+                err = "cuFFT Z2D (sample grid)";
+                rc2 = kErrCuda;
+            }
+            fft_calls++;
+            return rc2;
+        };
+        int rc;
+        if (mixed_) CMM_LAUNCH(1, launch_compose_pos_m(gc, gs, mapm_, stackm_, n_maps_, X, Y, stream));
+        else CMM_LAUNCH(1, launch_compose_pos(gc, gs, ChiX, ChiY, stack, n_maps_, X, Y, stream));
+        if (has(var, "Map_b") || has(var, "Chi_b") || all) {
+            if ((rc = out("Map_ChiX", X)) || (rc = out("Map_ChiY", Y))) return rc;
+        }
+        InitSource src{};
+        src.params = d_params_;
+        src.rand_table = d_rand_;
+        if (has(var, "Scalar") || has(var, "Theta") || all) {
+            src.kind = 1;
+            src.ic_num = s.scalar_num;
+            CMM_LAUNCH(1, launch_eval_init(X, Y, gs.N, src, S, stream));
+            if ((rc = out("Scalar_Theta", S))) return rc;
+            // Compute_avg reduces with thrust::maximum: hx hy max(0, max theta) (cmm-mesure.cu:226-229)
+            CMM_LAUNCH(2, launch_stats(S, gs.N, 1, red_, d_scal_ + 8, stream));
+            CMM_CUDA(cudaMemcpyAsync(h_scal_ + 8, d_scal_ + 8, sizeof(double) * 4, cudaMemcpyDeviceToHost, stream));
+            CMM_CUDA(cudaStreamSynchronize(stream));
+            double si = gs.hx * gs.hy * h_scal_[10];
+            append_f64(mdir + "Mesure/Scalar_integral_" + ns + ".data", &si, 1);
+        }
+        src.kind = s.initial_discrete ? 3 : 0;
+        src.ic_num = s.initial_condition_num;
+        src.discrete = wdisc;
+        src.gd = gd;
+        CMM_LAUNCH(1, launch_eval_init(X, Y, gs.N, src, W, stream));
+        if (has(var, "Vorticity") || has(var, "W") || has(var, "F") || all)
+            if ((rc = out("Vorticity_W", W))) return rc;
+        double mes[4], a, b2;
+        if ((rc = sumsq(W, &a))) return rc;
+        mes[1] = 0.5 * gs.hx * gs.hy * a;
+        CMM_FFT(cufftExecD2Z(ps_.d2z, W, reinterpret_cast<cufftDoubleComplex*>(F0)));
+        if ((rc = spec(1, T)) || (rc = sumsq(T, &a))) return rc;
+        if (has(var, "Grad_W") || all) if ((rc = out("GradX_W", T))) return rc;
+        if ((rc = spec(2, T)) || (rc = sumsq(T, &b2))) return rc;
+        if (has(var, "Grad_W") || all) if ((rc = out("GradY_W", T))) return rc;
+        mes[2] = 0.5 * gs.hx * gs.hy * a + 0.5 * gs.hx * gs.hy * b2;
+        // both extremes are taken with Compute_max in the reference (cmm-simulation-host.cu:807-809)
+        CMM_LAUNCH(2, launch_stats(W, gs.N, 1, red_, d_scal_ + 8, stream));
+        CMM_CUDA(cudaMemcpyAsync(h_scal_ + 8, d_scal_ + 8, sizeof(double) * 4, cudaMemcpyDeviceToHost, stream));
+        CMM_CUDA(cudaStreamSynchronize(stream));
+        mes[3] = std::max(h_scal_[9], -h_scal_[9]);
+        if (has(var, "Laplacian_W") || all) {
+            if ((rc = spec(0, T)) || (rc = out("Laplacian_W", T))) return rc;
+        }
+        if ((rc = spec(3, P))) return rc;
+        if (has(var, "Stream") || has(var, "Psi") || all) if ((rc = out("Stream_function_Psi", P))) return rc;
+        CMM_FFT(cufftExecD2Z(ps_.d2z, P, reinterpret_cast<cufftDoubleComplex*>(F0)));
+        if ((rc = spec(1, T)) || (rc = sumsq(T, &a))) return rc;
+        if (has(var, "Velocity") || has(var, "U") || all) if ((rc = out("Velocity_UX", T))) return rc;
+        if ((rc = spec(2, T)) || (rc = sumsq(T, &b2))) return rc;
+        if (has(var, "Velocity") || has(var, "U") || all) if ((rc = out("Velocity_UY", T))) return rc;
+        mes[0] = 0.5 * gs.hx * gs.hy * a + 0.5 * gs.hx * gs.hy * b2;
+        append_f64(mdir + "Mesure/Time_s_" + ns + ".data", &t_now, 1);
+        append_f64(mdir + "Mesure/Energy_" + ns + ".data", &mes[0], 1);
+        append_f64(mdir + "Mesure/Enstrophy_" + ns + ".data", &mes[1], 1);
+        append_f64(mdir + "Mesure/Palinstrophy_" + ns + ".data", &mes[2], 1);
+        append_f64(mdir + "Mesure/Max_vorticity_" + ns + ".data", &mes[3], 1);
+        if (s.verbose >= 3)
+            log_.push("Processed sample data on grid " + ns + ", Cons : Energ = " + to_str_prec(mes[0], 8) +
+                      " \t Enstr = " + to_str_prec(mes[1], 8) + " \t Palinstr = " + to_str_prec(mes[2], 8) +
+                      " \t Wmax = " + to_str_prec(mes[3], 8));
+    }
     return kOk;
 }
 

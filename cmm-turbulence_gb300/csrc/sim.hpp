@@ -93,6 +93,7 @@ private:
     int init_particles();
     int advect_particles(int lcl);
     int push_stack();
+    int sample_outputs(double t_now, double dt_now);   // sampled outputs on user grids
     int evaluate_potential();          // Vlasov-Poisson psi from the distribution function
     int vlasov_setup_h();              // the periodification h(v), once per run
     int vlasov_mesure(double* out9);   // Etot, Ekin, Epot, Mass, Momentum, Emode1..4
@@ -123,6 +124,12 @@ private:
     float4* wdiscm_ = nullptr;       // discrete initial vorticity nodes (FP32 Hermite)
     float4* stackm_ = nullptr;       // n maps, 2*Nc float4 each
     std::vector<unsigned long long*> partfix_;   // tracer positions, 64-bit fixed point (x, y interleaved)
+
+    // sampled outputs: buffers and plans of the largest sample grid seen so far
+    int smp_n_ = 0, smp_plan_n_ = 0;
+    FftPlans ps_;
+    double* smp_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // X, Y, scalar, W, psi, work
+    double2* smp_c_[2] = {nullptr, nullptr};
 
     // Vlasov-Poisson (simulation_type cmm_vlasov_poisson_1d)
     bool vlasov_ = false;

@@ -182,6 +182,25 @@ void og_compose_sample_var(const double* ChiX, const double* ChiY, const double*
                            const og_grid* gt, int var_num, int ic_num, const double* discrete, const og_grid* gd,
                            double* out);
 
+/* ---------------- sampled outputs (og_sample.c) ---------------- */
+/* d_init_scalar: src/simulation/cmm-init.cu:253-298 */
+double og_init_scalar(double x, double y, int scalar_num);
+typedef struct {
+    const og_grid* gc;              /* map grid */
+    const double *ChiX, *ChiY;      /* current map */
+    const double *stackX, *stackY;  /* n_maps stacked maps, 4*Nc each */
+    int n_maps;
+    const double* discrete;         /* Hermite discrete initial vorticity or NULL */
+    const og_grid* gd;
+    int ic_num;
+} og_state_view;
+/* sample_compute_and_write, backward part (cmm-simulation-host.cu:706-893) on grid gs:
+ * out = 10 planes of gs->N: map X, map Y, scalar, W, Laplacian W, dW/dx, dW/dy, psi,
+ * dpsi/dx (Velocity_UX), dpsi/dy (Velocity_UY); mes = {Energy, Enstrophy,
+ * Palinstrophy, Max_vorticity, Scalar_integral} with the reference's quirks */
+void og_sample_fields(const og_state_view* st, const og_grid* gs, int scalar_num, double* out, double* mes);
+void og_state_sample(const og_state* st, int n_sample, int scalar_num, double* out, double* mes);
+
 /* ψ_x, ψ_y at particle positions (k_h_sample_points_dxdy, cmm-simulation-kernel.cu:138-155) */
 void og_sample_points_dxdy(const og_state* st, const double* pos, double* out, int num);
 

@@ -645,3 +645,18 @@ void og_vlasov_state_mesure(const og_state* st, double* out)
 {
     og_vlasov_mesure(st->vort, &st->gc, st->psi, &st->gp, out);
 }
+
+void og_state_sample(const og_state* st, int n_sample, int scalar_num, double* out, double* mes)
+{
+    og_grid gs;
+    og_grid_fill(&gs, n_sample, n_sample, st->gc.bounds);
+    og_state_view v;
+    v.gc = &st->gc;
+    v.ChiX = st->ChiX; v.ChiY = st->ChiY;
+    v.stackX = st->stackX; v.stackY = st->stackY;
+    v.n_maps = st->n_maps;
+    v.discrete = st->s.initial_discrete ? st->vort_disc : NULL;
+    v.gd = &st->gd;
+    v.ic_num = st->s.initial_condition_num;
+    og_sample_fields(&v, &gs, scalar_num, out, mes);
+}

@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(HERE, "liboracle.so")
 
 def build(force=False):
     """Compile liboracle.so with the committed Makefile (gcc + OpenMP)."""
-    srcs = [os.path.join(HERE, f) for f in ("og_hermite.c", "og_fft.c", "og_euler.c", "og_vlasov.c", "cmm_oracle.h")]
+    srcs = [os.path.join(HERE, f) for f in ("og_hermite.c", "og_fft.c", "og_euler.c", "og_vlasov.c", "og_sample.c", "cmm_oracle.h")]
     if not force and os.path.exists(LIB_PATH):
         if os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(s) for s in srcs):
             return LIB_PATH
@@ -85,6 +85,7 @@ def lib():
             getattr(L, name).argtypes = [C.c_void_p]
         L.og_sample_points_dxdy.argtypes = [C.c_void_p, dp, dp, C.c_int]
         L.og_init.restype = C.c_int
+        L.og_state_sample.argtypes = [C.c_void_p, C.c_int, C.c_int, dp, dp]
         L.og_vlasov_state_mesure.argtypes = [C.c_void_p, dp]
         _lib = L
     return _lib
@@ -227,6 +228,18 @@ class EulerOracle:
 
     def max_vorticity(self):
         return self.L.og_max_vorticity(self.h)
+
+    def sample(self, n, scalar_num):
+        """Sampled outputs on an n x n grid: dict of the ten planes and the five
+        conservation values (sample_compute_and_write, backward part)."""
+        out = np.zeros(10 * n * n)
+        mes = np.zeros(5)
+        self.L.og_state_sample(self.h, n, scalar_num, _dp(out), _dp(mes))
+        names = ("Map_ChiX", "Map_ChiY", "Scalar_Theta", "Vorticity_W", "Laplacian_W", "GradX_W", "GradY_W",
+                 "Stream_function_Psi", "Velocity_UX", "Velocity_UY")
+        planes = {k: out[i * n * n:(i + 1) * n * n].copy() for i, k in enumerate(names)}
+        return planes, dict(zip(("Energy", "Enstrophy", "Palinstrophy", "Max_vorticity", "Scalar_integral"),
+                                mes.tolist()))
 
     def vlasov_mesure(self):
         """{Etot, Ekin, Epot, Mass, Momentum, Emode1..4} of the current state

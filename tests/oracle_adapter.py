@@ -59,3 +59,6 @@ class OracleRun:
 
     def vlasov_mesure(self):
         return self.o.vlasov_mesure()
+
+    def sample(self, n, scalar_num):
+        return self.o.sample(n, scalar_num)

@@ -148,6 +148,7 @@ class Settings:
             PartRec("{num=100000,tau=0,seed=0,time_integration=RK3,init_name=sine_sheets,init_time=0,init_vel=0" + pi_s),
             PartRec("{num=100000,tau=0.1,seed=0,time_integration=RK3,init_name=uniform,init_time=0,init_vel=0" + pi_s)]
         self.particles_steps = -1
+        self.scalar_name = "rectangle"
 
     # settings.h:386-398 -- raises the Lagrange order, never lowers it
     def set_time_integration(self, v):
@@ -167,6 +168,11 @@ class Settings:
         return table.index(self.initial_condition) if self.initial_condition in table else -1
 
     @property
+    def scalar_num(self):
+        # settings.h:322-330
+        return {"rectangle": 0, "gaussian": 1, "circular_ring": 2}.get(self.scalar_name, -1)
+
+    @property
     def simulation_type_num(self):
         return 2 if self.simulation_type == "cmm_vlasov_poisson_1d" else 0
 
@@ -182,7 +188,7 @@ class Settings:
         bools = {"set_dt_by_steps", "save_map_stack", "initial_discrete", "lagrange_init_higher_order",
                  "skip_remapping", "forward_map"}
         strs = {"workspace", "simulation_type", "sim_name", "initial_condition", "initial_discrete_location",
-                "map_update_order"}
+                "map_update_order", "scalar_name"}
         if k in ints: setattr(self, k, int(v))
         elif k in floats: setattr(self, k, float(v))
         elif k in bools: setattr(self, k, _bool(v))

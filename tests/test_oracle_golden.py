@@ -28,11 +28,11 @@ def _run(name):
     run = OracleRun(s)
     rec = DebugRecorder(s, run)
     refloop.run_reference_loop(s, run, rec.on_save, rec.on_step)
-    keys = [k for k in g["files"] if "Particles" not in k and "_256" not in k and "Scalar" not in k]
+    keys = [k for k in g["files"] if "Particles" not in k]
     return rec, g, keys
 
 
-@pytest.mark.parametrize("name", ["init_comp", "init_conv", "one_step"])
+@pytest.mark.parametrize("name", ["init_comp", "init_conv", "init_sample", "one_step"])
 def test_oracle_matches_reference_goldens(name):
     rec, g, keys = _run(name)
     worst, fails = compare_series(rec.series, g["files"], keys, RTOL)

@@ -43,8 +43,12 @@ cudaError_t launch_advect_m(const AdvectMArgs& a, cudaStream_t s);
 cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_result, cudaStream_t s);
 // omega_0 through current map + n stacked maps (n * 2*Nc float4), 64-bit fixed-point
 // positions; a discrete initial field (src.kind 3) is read from its FP32 Hermite nodes disc
+// (out_f != nullptr: FP32 output instead of out)
 cudaError_t launch_compose_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
-                             const InitSource& src, const float4* disc, double* out, cudaStream_t s);
+                             const InitSource& src, const float4* disc, double* out, cudaStream_t s,
+                             float* out_f = nullptr);
+// FP32 Hermite spectra [F, i kx F, i ky F, -kx ky F] of an unnormalised R2C half spectrum
+cudaError_t launch_spec_hermite_f(const float2* F, const Grid& g, float2* out4, cudaStream_t s);
 // positions of the nodes of gt through the current map and the stack (fixed point), as FP64
 cudaError_t launch_compose_pos_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
                                  double* px, double* py, cudaStream_t s);

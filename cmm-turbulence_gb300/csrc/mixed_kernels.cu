@@ -624,10 +624,11 @@ static unsigned long long fix_step(int n)
 // Hermite nodes, an analytic one with its FP64 formula).  Target, map and
 // discrete grids span the same domain.
 // ---------------------------------------------------------------------------
+template <typename T>
 __global__ void __launch_bounds__(256) k_compose_m(Grid gm, Grid gt, unsigned long long stx, unsigned long long sty,
                                                    float2 scx, float2 scy, const float4* __restrict__ map,
                                                    const float4* __restrict__ stack, int n_maps, InitSource src,
-                                                   const float4* __restrict__ disc, double* __restrict__ out)
+                                                   const float4* __restrict__ disc, T* __restrict__ out)
 {
     const int iX = blockIdx.x * blockDim.x + threadIdx.x, iY = blockIdx.y;
     if (iX >= gt.NX) return;
@@ -659,18 +660,49 @@ __global__ void __launch_bounds__(256) k_compose_m(Grid gm, Grid gt, unsigned lo
         double y = gm.b2 + __ull2double_rn(Py) * (gm.Wy * 5.42101086242752217e-20);
         v = init_field(src.kind, x, y, src.ic_num, src.params, src.rand_table);
     }
-    out[(long long)iY * gt.NX + iX] = v;
+    out[(long long)iY * gt.NX + iX] = (T)v;
 }
 
 cudaError_t launch_compose_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
-                             const InitSource& src, const float4* disc, double* out, cudaStream_t s)
+                             const InitSource& src, const float4* disc, double* out, cudaStream_t s, float* out_f)
 {
     if (gt.b0 != gm.b0 || gt.b2 != gm.b2 || gt.Wx != gm.Wx || gt.Wy != gm.Wy || gt.NY > 65535) return cudaErrorInvalidValue;
     if (src.kind == 3 && (!disc || src.gd.b0 != gm.b0 || src.gd.b2 != gm.b2 || src.gd.Wx != gm.Wx || src.gd.Wy != gm.Wy))
         return cudaErrorInvalidValue;
     dim3 blocks((unsigned)((gt.NX + 255) / 256), (unsigned)gt.NY);
-    k_compose_m<<<blocks, 256, 0, s>>>(gm, gt, fix_step(gt.NX), fix_step(gt.NY), fix_scale(gm.Wx), fix_scale(gm.Wy),
-                                       map, stack, n_maps, src, disc, out);
+    if (out_f)
+        k_compose_m<float><<<blocks, 256, 0, s>>>(gm, gt, fix_step(gt.NX), fix_step(gt.NY), fix_scale(gm.Wx),
+                                                  fix_scale(gm.Wy), map, stack, n_maps, src, disc, out_f);
+    else
+        k_compose_m<double><<<blocks, 256, 0, s>>>(gm, gt, fix_step(gt.NX), fix_step(gt.NY), fix_scale(gm.Wx),
+                                                   fix_scale(gm.Wy), map, stack, n_maps, src, disc, out);
+    return cudaGetLastError();
+}
+
+// normalised half spectrum -> the four Hermite spectra [F, i kx F, i ky F, -kx ky F]
+// (fourier_hermite, src/numerical/cmm-fft.cu:398-429) in FP32
+__global__ void k_spec_hermite_f(const float2* __restrict__ F, Grid g, float inv_n, float2* __restrict__ out4)
+{
+    const int iX = blockIdx.x * blockDim.x + threadIdx.x, iY = blockIdx.y;
+    if (iX >= g.NX_fft) return;
+    const long long i = (long long)iY * g.NX_fft + iX;
+    float2 P = F[i];
+    P.x *= inv_n;
+    P.y *= inv_n;
+    const float kx = g.kfxf * (float)(2 * iX > g.NX ? iX - g.NX : iX);
+    const float ky = g.kfyf * (float)(2 * iY > g.NY ? iY - g.NY : iY);
+    const float2 Py = make_float2(-P.y * ky, P.x * ky);
+    out4[i] = P;
+    out4[g.Nfft + i] = make_float2(-P.y * kx, P.x * kx);
+    out4[2 * g.Nfft + i] = Py;
+    out4[3 * g.Nfft + i] = make_float2(-Py.y * kx, Py.x * kx);
+}
+
+cudaError_t launch_spec_hermite_f(const float2* F, const Grid& g, float2* out4, cudaStream_t s)
+{
+    if (g.NY > 65535) return cudaErrorInvalidValue;
+    dim3 blocks((unsigned)((g.NX_fft + 255) / 256), (unsigned)g.NY);
+    k_spec_hermite_f<<<blocks, 256, 0, s>>>(F, g, (float)(1.0 / (double)g.N), out4);
     return cudaGetLastError();
 }
 

@@ -237,9 +237,9 @@ int EulerSim::alloc()
         if ((rc = falloc((void**)&mapm_, mapb)) || (rc = falloc((void**)&mapm_new_, mapb)) ||
             (rc = falloc((void**)&psiA_, psib)) || (rc = falloc((void**)&psiB_, psib)) ||
             (rc = falloc((void**)&wfm_, sizeof(float4) * (size_t)gf.N)) ||
-            (rc = falloc((void**)&realf_, sizeof(float) * 4 * (size_t)std::max(gv.N, gp.N))) ||
-            (rc = falloc((void**)&specf_, sizeof(float2) * (size_t)gv.Nfft)) ||
-            (rc = falloc((void**)&spec4f_, sizeof(float2) * 4 * (size_t)gp.Nfft)))
+            (rc = falloc((void**)&realf_, sizeof(float) * 4 * (size_t)std::max({gv.N, gp.N, gf.N}))) ||
+            (rc = falloc((void**)&specf_, sizeof(float2) * (size_t)std::max(gv.Nfft, gf.Nfft))) ||
+            (rc = falloc((void**)&spec4f_, sizeof(float2) * 4 * (size_t)std::max(gp.Nfft, gf.Nfft))))
             return rc;
         for (int l = 0; l < L; ++l) if ((rc = falloc((void**)&psim_[l], psib))) return rc;
         if (s.initial_discrete && (rc = falloc((void**)&wdiscm_, sizeof(float4) * (size_t)gd.N))) return rc;
@@ -249,14 +249,18 @@ int EulerSim::alloc()
             partfix_.push_back(d);
         }
         if (stack_cap_ > 0 && (rc = falloc((void**)&stackm_, mapb * stack_cap_))) return rc;
-        int nv[2] = {gv.NY, gv.NX}, np[2] = {gp.NY, gp.NX};
+        int nv[2] = {gv.NY, gv.NX}, np[2] = {gp.NY, gp.NX}, nf[2] = {gf.NY, gf.NX};
         if (cufftPlanMany(&r2c_v_, 2, nv, nullptr, 1, 0, nullptr, 1, 0, CUFFT_R2C, 1) != CUFFT_SUCCESS ||
-            cufftPlanMany(&c2r4_p_, 2, np, nullptr, 1, 0, nullptr, 1, 0, CUFFT_C2R, 4) != CUFFT_SUCCESS) {
+            cufftPlanMany(&c2r4_p_, 2, np, nullptr, 1, 0, nullptr, 1, 0, CUFFT_C2R, 4) != CUFFT_SUCCESS ||
+            cufftPlanMany(&r2c_f_, 2, nf, nullptr, 1, 0, nullptr, 1, 0, CUFFT_R2C, 1) != CUFFT_SUCCESS ||
+            cufftPlanMany(&c2r4_f_, 2, nf, nullptr, 1, 0, nullptr, 1, 0, CUFFT_C2R, 4) != CUFFT_SUCCESS) {
             err = "cuFFT FP32 plan creation failed";
             return kErrCuda;
         }
         cufftSetStream(r2c_v_, stream);
         cufftSetStream(c2r4_p_, stream);
+        cufftSetStream(r2c_f_, stream);
+        cufftSetStream(c2r4_f_, stream);
     }
     // random table for gaussian_blobs (cmm-euler2d.cu:348-354)
     std::vector<double> rnd(1000);
@@ -296,6 +300,9 @@ void EulerSim::release()
     realf_ = nullptr; specf_ = nullptr; spec4f_ = nullptr;
     if (r2c_v_) cufftDestroy(r2c_v_);
     if (c2r4_p_) cufftDestroy(c2r4_p_);
+    if (r2c_f_) cufftDestroy(r2c_f_);
+    if (c2r4_f_) cufftDestroy(c2r4_f_);
+    r2c_v_ = c2r4_p_ = r2c_f_ = c2r4_f_ = 0;
     r2c_v_ = c2r4_p_ = 0;
     if (h_scal_) cudaFreeHost(h_scal_);
     h_scal_ = nullptr;
@@ -318,13 +325,20 @@ int EulerSim::translate_ic()
     src.gd = gd;
     src.params = d_params_;
     src.rand_table = d_rand_;
-    if (mixed_) {
-        // fixed-point positions through the FP32 displacement stack, FP64
-        // spectral Hermite construction, FP32 storage of the fine vorticity nodes
-        CMM_LAUNCH(1, launch_compose_m(gc, gf, mapm_, stackm_, n_maps_, src, wdiscm_, real_buf_, stream));
-    } else {
-        CMM_LAUNCH(1, launch_compose_sample(gc, gf, ChiX, ChiY, stack, n_maps_, src, real_buf_, stream));
+    if (mixed_ && !vlasov_) {
+        // fixed-point positions through the FP32 displacement stack, then the
+        // spectral Hermite planes in FP32, the precision of the nodes they are stored in
+        CMM_LAUNCH(1, launch_compose_m(gc, gf, mapm_, stackm_, n_maps_, src, wdiscm_, nullptr, stream, realf_));
+        CMM_FFT(cufftExecR2C(r2c_f_, realf_, reinterpret_cast<cufftComplex*>(specf_)));
+        CMM_LAUNCH(1, launch_spec_hermite_f(specf_, gf, spec4f_, stream));
+        CMM_FFT(cufftExecC2R(c2r4_f_, reinterpret_cast<cufftComplex*>(spec4f_), realf_));
+        CMM_LAUNCH(1, launch_planes_to_float4(realf_, nullptr, gf.N, wfm_, stream));
+        return kOk;
     }
+    // plain form, and the Vlasov mixed form: there the kinetic energy weights f by v^2 over the
+    // whole velocity range, where an FP32 transform's noise floor (~1e-7 of max f) would show
+    if (mixed_) CMM_LAUNCH(1, launch_compose_m(gc, gf, mapm_, stackm_, n_maps_, src, wdiscm_, real_buf_, stream));
+    else CMM_LAUNCH(1, launch_compose_sample(gc, gf, ChiX, ChiY, stack, n_maps_, src, real_buf_, stream));
     CMM_FFT(cufftExecD2Z(pf_.d2z, real_buf_, reinterpret_cast<cufftDoubleComplex*>(spec_)));
     CMM_LAUNCH(1, launch_spec_hermite(spec_, gf, spec4_, stream));
     CMM_FFT(cufftExecZ2D(pf_.z2d4, reinterpret_cast<cufftDoubleComplex*>(spec4_), wfine));

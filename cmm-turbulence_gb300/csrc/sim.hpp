@@ -143,7 +143,7 @@ private:
     float* realf_ = nullptr;         // FP32 real scratch (4 planes of the largest grid)
     float2* specf_ = nullptr;        // FP32 complex scratch
     float2* spec4f_ = nullptr;       // 4 FP32 spectra
-    cufftHandle r2c_v_ = 0, c2r4_p_ = 0;
+    cufftHandle r2c_v_ = 0, c2r4_p_ = 0, r2c_f_ = 0, c2r4_f_ = 0;
     bool prof_ = false;
     cudaEvent_t ev_[kNumPhases][2] = {};
     bool ev_live_[kNumPhases] = {};

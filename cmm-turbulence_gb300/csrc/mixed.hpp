@@ -37,6 +37,11 @@ cudaError_t launch_init_map_m(float4* map, const Grid& g, cudaStream_t s);
 // outA = sum_l cA[l] levels[l], outB likewise (outB may be null)
 cudaError_t launch_precombine(float4* const* levels, int L, const double* cA, const double* cB, long long n,
                               float4* outA, float4* outB, cudaStream_t s);
+// psi solve's last pass for 3 Lagrange levels: new level nodes (out0) from 4 FP32 planes and the
+// combinations c1, c2, c3 of the levels (new, l1, l2) -> o1, o2, o3 (same arithmetic as launch_precombine)
+cudaError_t launch_psi_nodes3(const float* planes, long long n, const float4* l1, const float4* l2, const double* c1,
+                              const double* c2, const double* c3, float4* out0, float4* o1, float4* o2, float4* o3,
+                              cudaStream_t s);
 cudaError_t launch_advect_m(const AdvectMArgs& a, cudaStream_t s);
 // max |det grad X - 1| on the half-shifted check grid with r = Ncheck / Nmap points per cell and axis
 // (r * Nmap^2 < 2^31)

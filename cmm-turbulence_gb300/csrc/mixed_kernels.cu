@@ -211,6 +211,45 @@ __global__ void k_precombine(const float4* __restrict__ p0, const float4* __rest
     if (outB) outB[i] = b;
 }
 
+// the psi solve's last pass for three Lagrange levels: the new level's four FP32
+// planes -> its nodes, and in the same pass three combinations of the levels
+// (new, 1, 2), accumulated in the order of k_precombine so the results are identical
+struct Combo3 { float c[3][3]; };
+
+__device__ __forceinline__ float4 combo(const float* c, const float4& v0, const float4& v1, const float4& v2)
+{
+    float4 a = make_float4(0, 0, 0, 0);
+    a.x = fmaf(c[0], v0.x, a.x); a.y = fmaf(c[0], v0.y, a.y); a.z = fmaf(c[0], v0.z, a.z); a.w = fmaf(c[0], v0.w, a.w);
+    a.x = fmaf(c[1], v1.x, a.x); a.y = fmaf(c[1], v1.y, a.y); a.z = fmaf(c[1], v1.z, a.z); a.w = fmaf(c[1], v1.w, a.w);
+    a.x = fmaf(c[2], v2.x, a.x); a.y = fmaf(c[2], v2.y, a.y); a.z = fmaf(c[2], v2.z, a.z); a.w = fmaf(c[2], v2.w, a.w);
+    return a;
+}
+
+__global__ void __launch_bounds__(256) k_psi_nodes3(const float* __restrict__ planes, long long n,
+                                                    const float4* __restrict__ l1, const float4* __restrict__ l2,
+                                                    Combo3 cm, float4* __restrict__ out0, float4* __restrict__ o1,
+                                                    float4* __restrict__ o2, float4* __restrict__ o3)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 v0 = make_float4(planes[i], planes[n + i], planes[2 * n + i], planes[3 * n + i]);
+    const float4 v1 = __ldg(l1 + i), v2 = __ldg(l2 + i);
+    out0[i] = v0;
+    o1[i] = combo(cm.c[0], v0, v1, v2);
+    o2[i] = combo(cm.c[1], v0, v1, v2);
+    o3[i] = combo(cm.c[2], v0, v1, v2);
+}
+
+cudaError_t launch_psi_nodes3(const float* planes, long long n, const float4* l1, const float4* l2, const double* c1,
+                              const double* c2, const double* c3, float4* out0, float4* o1, float4* o2, float4* o3,
+                              cudaStream_t s)
+{
+    Combo3 cm;
+    for (int l = 0; l < 3; ++l) { cm.c[0][l] = (float)c1[l]; cm.c[1][l] = (float)c2[l]; cm.c[2][l] = (float)c3[l]; }
+    k_psi_nodes3<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(planes, n, l1, l2, cm, out0, o1, o2, o3);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_precombine(float4* const* levels, int L, const double* cA, const double* cB, long long n,
                               float4* outA, float4* outB, cudaStream_t s)
 {

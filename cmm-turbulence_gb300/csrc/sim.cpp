@@ -236,6 +236,7 @@ int EulerSim::alloc()
         size_t mapb = sizeof(float4) * 2 * (size_t)gc.N, psib = sizeof(float4) * (size_t)gp.N;
         if ((rc = falloc((void**)&mapm_, mapb)) || (rc = falloc((void**)&mapm_new_, mapb)) ||
             (rc = falloc((void**)&psiA_, psib)) || (rc = falloc((void**)&psiB_, psib)) ||
+            (rc = falloc((void**)&psiP_, psib)) ||
             (rc = falloc((void**)&wfm_, sizeof(float4) * (size_t)gf.N)) ||
             (rc = falloc((void**)&realf_, sizeof(float) * 4 * (size_t)std::max({gv.N, gp.N, gf.N}))) ||
             (rc = falloc((void**)&specf_, sizeof(float2) * (size_t)std::max(gv.Nfft, gf.Nfft))) ||
@@ -294,7 +295,9 @@ void EulerSim::release()
     for (auto& p : smp_c_) { f(p); p = nullptr; }
     destroy_plans(ps_);
     smp_n_ = smp_plan_n_ = 0;
-    f(mapm_); f(mapm_new_); f(psiA_); f(psiB_); f(wfm_); f(stackm_); f(realf_); f(specf_); f(spec4f_);
+    f(mapm_); f(mapm_new_); f(psiA_); f(psiB_); f(psiP_); f(wfm_); f(stackm_); f(realf_); f(specf_); f(spec4f_);
+    psiP_ = nullptr;
+    fused_ = false;
     for (int l = 0; l < kMaxLagrange; ++l) { f(psim_[l]); psim_[l] = nullptr; }
     mapm_ = mapm_new_ = psiA_ = psiB_ = wfm_ = stackm_ = nullptr;
     realf_ = nullptr; specf_ = nullptr; spec4f_ = nullptr;
@@ -354,7 +357,27 @@ int EulerSim::evaluate_stream()
         CMM_FFT(cufftExecR2C(r2c_v_, realf_, reinterpret_cast<cufftComplex*>(specf_)));
         CMM_LAUNCH(1, launch_spec_psi_f(specf_, gv, gp, s.freq_cut_psi, spec4f_, stream));
         CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), realf_));
-        CMM_LAUNCH(1, launch_planes_to_float4(realf_, nullptr, gp.N, psim_[0], stream));
+        fused_ = false;
+        if (psi_lcl_ >= 0 && L == 3) {
+            // one pass writes the new level and the Lagrange combinations this step's
+            // tracers and the next step's advection will ask for (next dt predicted by
+            // compute_next_timestep; the users check the coefficients bitwise)
+            const int lcl = psi_lcl_;
+            const double* t = t_vec_.data();
+            const double tn = t[lcl + 1];
+            double dtn = compute_next_timestep(tn);
+            if (tn + dtn > s.final_time) dtn = s.final_time - tn;
+            for (int i = 0; i < L; ++i) {
+                fusedLp_[i] = lagrange_coefficient(t, t[lcl] + dt_vec_[lcl + 1] / 2.0, lcl + 1, i, L);
+                fusedL1_[i] = lagrange_coefficient(t, tn + dtn, lcl + 1, i, L);
+                fusedL12_[i] = lagrange_coefficient(t, tn + dtn / 2.0, lcl + 1, i, L);
+            }
+            CMM_LAUNCH(1, launch_psi_nodes3(realf_, gp.N, psim_[1], psim_[2], fusedLp_, fusedL1_, fusedL12_, psim_[0],
+                                            psiP_, psiA_, psiB_, stream));
+            fused_ = true;
+        } else {
+            CMM_LAUNCH(1, launch_planes_to_float4(realf_, nullptr, gp.N, psim_[0], stream));
+        }
         return kOk;
     }
     CMM_LAUNCH(1, launch_sample_vort(gc, gv, gf, ChiX, ChiY, wfine, s.molly_stencil, real_buf_, gv.NX, stream));
@@ -480,9 +503,14 @@ int EulerSim::advect_m(const double* t, const double* dtv, int lc, int ti_num, i
         a.tA = vtab_[0]; a.tB = vtab_[1]; a.t0 = vtab_[2]; a.tv = vtab_[3];
     } else {
         // Lagrange extrapolation is linear in psi: combine the levels once per
-        // step, then every RK stage interpolates a single field
-        CMM_LAUNCH(1, launch_precombine(psim_, l_order, L1, ti_num == 30 ? L12 : nullptr, gp.N, psiA_,
-                                        ti_num == 30 ? psiB_ : nullptr, stream));
+        // step, then every RK stage interpolates a single field (already done by
+        // the previous psi solve when its predicted coefficients are these)
+        bool have = fused_ && l_order == 3;
+        for (int i = 0; i < l_order && have; ++i)
+            have = L1[i] == fusedL1_[i] && (ti_num != 30 || L12[i] == fusedL12_[i]);
+        if (!have)
+            CMM_LAUNCH(1, launch_precombine(psim_, l_order, L1, ti_num == 30 ? L12 : nullptr, gp.N, psiA_,
+                                            ti_num == 30 ? psiB_ : nullptr, stream));
     }
     a.gm = gc; a.gp = gp;
     a.map = mapm_; a.out = mapm_new_;
@@ -638,13 +666,15 @@ int EulerSim::advect_particles(int lcl)
                 CMM_LAUNCH(1, launch_vlasov_table(lv, one, 1, gp.NX, vtab_[2], stream));
                 combined = true;
             } else if (p.time_integration_num == 30 && !combined) {
-                CMM_LAUNCH(1, launch_precombine(psim_, L, Lp12, nullptr, gp.N, psiB_, nullptr, stream));
+                bool have = fused_ && L == 3;
+                for (int k = 0; k < L && have; ++k) have = Lp12[k] == fusedLp_[k];
+                if (!have) CMM_LAUNCH(1, launch_precombine(psim_, L, Lp12, nullptr, gp.N, psiP_, nullptr, stream));
                 combined = true;
             }
             cudaError_t e = vlasov_
                 ? launch_particles_m(gp, partfix_[i], p.num, nullptr, nullptr, nullptr, dt_vec_[lcl + 1],
                                      p.time_integration_num, stream, vtab_[0], vtab_[1], vtab_[2], vtab_[3])
-                : launch_particles_m(gp, partfix_[i], p.num, psim_[1], psiB_, psim_[0], dt_vec_[lcl + 1],
+                : launch_particles_m(gp, partfix_[i], p.num, psim_[1], psiP_, psim_[0], dt_vec_[lcl + 1],
                                      p.time_integration_num, stream);
             kernel_launches++;
             if (e == cudaErrorInvalidValue) { err = "particle time integration " + p.time_integration + " is not built"; return kErrUnsupported; }
@@ -833,7 +863,10 @@ int EulerSim::step_once()
     double gap = loop_ctr_ - old_ctr_, counter = n_maps_;
     rotate_psi(L - 1);
     ph_begin(kPhPsi);
-    if ((rc = evaluate_stream())) return rc;
+    psi_lcl_ = lcl;
+    rc = evaluate_stream();
+    psi_lcl_ = -1;
+    if (rc) return rc;
     ph_end(kPhPsi);
     ph_begin(kPhCoarse);
     if ((rc = coarse_vort())) return rc;

@@ -120,6 +120,13 @@ private:
     float4* psim_[kMaxLagrange] = {nullptr, nullptr, nullptr, nullptr};
     float4* psiA_ = nullptr;         // Lagrange combinations of the psi levels
     float4* psiB_ = nullptr;
+    float4* psiP_ = nullptr;         // tracers' t_{n+1/2} combination
+    // combinations written by the psi solve's last pass (three levels): valid for the
+    // coefficients below; the next advection and this step's tracers check them bitwise
+    int psi_lcl_ = -1;
+    bool fused_ = false;
+    double fusedL1_[kMaxLagrange] = {0, 0, 0, 0}, fusedL12_[kMaxLagrange] = {0, 0, 0, 0},
+           fusedLp_[kMaxLagrange] = {0, 0, 0, 0};
     float4* wfm_ = nullptr;          // fine vorticity nodes
     float4* wdiscm_ = nullptr;       // discrete initial vorticity nodes (FP32 Hermite)
     float4* stackm_ = nullptr;       // n maps, 2*Nc float4 each

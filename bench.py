@@ -66,7 +66,7 @@ def sim_args(workspace, precision="fp64", particles=WORKLOAD["particles"]):
             "map_epsilon=0.001", "incomp_threshold=0.0001", "skip_remapping=0", "molly_stencil=0",
             "freq_cut_psi=128", "lagrange_init_higher_order=1", "mem_RAM_CPU_remaps=%d" % w["mem_RAM_CPU_remaps"],
             "save_computational_num=0", "save_sample_num=0", "save_zoom_num=0", "forward_map=0", "verbose=0",
-            "precision=%s" % precision, "particles_advected_num=1"], \
+            "save_map_stack=0", "precision=%s" % precision, "particles_advected_num=1"], \
            ["{num=%d,tau=0,seed=0,time_integration=RK3,init_name=uniform,init_time=0,init_vel=0,"
             "init_param_1=3.141592653589793,init_param_2=3.141592653589793,init_param_3=6.283185307179586,"
             "init_param_4=6.283185307179586}" % particles]
@@ -341,7 +341,7 @@ def run_vlasov(args):
                "map_update_order=4th", "map_epsilon=0.001", "incomp_threshold=%r" % w["incomp_threshold"],
                "skip_remapping=0", "molly_stencil=0", "lagrange_init_higher_order=1", "mem_RAM_CPU_remaps=20000",
                "particles_advected_num=0", "save_computational_num=0", "save_sample_num=0", "verbose=0",
-               "precision=%s" % prec]
+               "save_map_stack=0", "precision=%s" % prec]
         stream = torch.cuda.Stream()
         sim = m.Simulation(cli, stream=stream.cuda_stream)
         sim.set_initial_discrete(f0)

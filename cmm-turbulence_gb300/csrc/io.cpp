@@ -55,6 +55,24 @@ bool write_f64(const std::string& path, const double* v, size_t n)
     return w == n;
 }
 
+int read_f64(const std::string& path, double* v, size_t n)
+{
+    FILE* f = fopen(path.c_str(), "rb");
+    if (!f) return 1;
+    size_t r = fread(v, sizeof(double), n, f);
+    fclose(f);
+    return r == n ? 0 : 2;
+}
+
+int count_files_containing(const std::string& dir, const std::string& sub)
+{
+    std::error_code ec;
+    int n = 0;
+    for (std::filesystem::directory_iterator it(dir, ec), end; !ec && it != end; it.increment(ec))
+        if (it->is_regular_file(ec) && it->path().filename().string().find(sub) != std::string::npos) n++;
+    return n;
+}
+
 std::string to_str3(double v)
 {
     std::ostringstream os;
@@ -81,6 +99,16 @@ void Logger::open(const std::string& path)
 {
     if (f_) fclose(f_);
     f_ = fopen(path.c_str(), "a");
+}
+
+void Logger::start(const std::string& path, bool restart, const std::string& run_name)
+{
+    if (f_) fclose(f_);
+    f_ = fopen(path.c_str(), restart ? "a" : "w");
+    if (!f_) return;
+    if (restart) fputs("\nContinuing simulation\n\n", f_);
+    else fprintf(f_, "%s\n", run_name.c_str());
+    fflush(f_);
 }
 
 void Logger::push(const std::string& msg)

@@ -75,6 +75,7 @@ cudaError_t launch_planes_to_float4(const float* planes, const double* planes_d,
                                     cudaStream_t s);
 cudaError_t launch_float4_to_planes(const float4* in, long long n, double* planes, cudaStream_t s);
 cudaError_t launch_map_to_planes(const float4* map, const Grid& g, double* X, double* Y, cudaStream_t s);
+cudaError_t launch_planes_to_map(const double* X, const double* Y, const Grid& g, float4* map, cudaStream_t s);
 // sum psi_x^2 + psi_y^2 (FP64 accumulation) -> out[0]
 cudaError_t launch_energy_m(const float4* psi, long long n, double* scratch, double* out, cudaStream_t s);
 

@@ -1080,6 +1080,24 @@ cudaError_t launch_map_to_planes(const float4* map, const Grid& g, double* X, do
     return cudaGetLastError();
 }
 
+// reference planar map X, Y -> displacement map (a stored map read back at a restart)
+__global__ void k_planes_to_map(const double* __restrict__ X, const double* __restrict__ Y, Grid g, float4* __restrict__ M)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= g.N) return;
+    int iX = (int)(i % g.NX), iY = (int)(i / g.NX);
+    M[2 * i] = make_float4((float)(X[i] - (g.b0 + iX * g.hx)), (float)(Y[i] - (g.b2 + iY * g.hy)),
+                           (float)(X[g.N + i] - 1.0), (float)Y[g.N + i]);
+    M[2 * i + 1] = make_float4((float)X[2 * g.N + i], (float)(Y[2 * g.N + i] - 1.0), (float)X[3 * g.N + i],
+                               (float)Y[3 * g.N + i]);
+}
+
+cudaError_t launch_planes_to_map(const double* X, const double* Y, const Grid& g, float4* map, cudaStream_t s)
+{
+    k_planes_to_map<<<(unsigned)((g.N + 255) / 256), 256, 0, s>>>(X, Y, g, map);
+    return cudaGetLastError();
+}
+
 // sum of psi_x^2 + psi_y^2 over an FP32 Hermite level, accumulated in FP64 (energy)
 __global__ void __launch_bounds__(256) k_energy_partial(const float4* __restrict__ P, long long n, double* part)
 {

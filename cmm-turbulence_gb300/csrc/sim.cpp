@@ -14,6 +14,7 @@
 #include <cstring>
 #include <fstream>
 #include <random>
+#include <sstream>
 
 namespace cmm {
 
@@ -148,7 +149,6 @@ int EulerSim::alloc()
     }
     if (s.map_update_order_num < 0) { err = "unknown map_update_order " + s.map_update_order; return kErrParam; }
     if (s.forward_map) { err = "forward_map is not built"; return kErrUnsupported; }
-    if (s.restart_time != 0) { err = "restart from a saved map stack is not built"; return kErrUnsupported; }
     if (s.grid_coarse <= 0 || s.grid_fine <= 0 || s.grid_psi <= 0 || s.grid_vort <= 0) { err = "grid sizes must be positive"; return kErrParam; }
 
     dt = s.dt();
@@ -577,41 +577,172 @@ void EulerSim::rotate_psi(int n)
     phi_lv_[0] = tph;
 }
 
+int EulerSim::reserve_stack(int n)
+{
+    // the sub-map stack stays in HBM: grow it geometrically, up to the capacity
+    // mem_RAM_CPU_remaps allows
+    if (n <= stack_cap_) return kOk;
+    int cap = std::min(max_maps, std::max({2 * stack_cap_, 16, n}));
+    const size_t mapb = mixed_ ? sizeof(float4) * 2 * (size_t)gc.N : sizeof(double) * 8 * (size_t)gc.N;
+    void* bigger = nullptr;
+    CMM_CUDA(cudaMalloc(&bigger, mapb * cap));
+    void* old = mixed_ ? (void*)stackm_ : (void*)stack;
+    if (old && n_maps_ > 0) CMM_CUDA(cudaMemcpyAsync(bigger, old, mapb * n_maps_, cudaMemcpyDeviceToDevice, stream));
+    CMM_CUDA(cudaStreamSynchronize(stream));
+    if (old) cudaFree(old);
+    if (mixed_) stackm_ = (float4*)bigger;
+    else stack = (double*)bigger;
+    stack_cap_ = cap;
+    return kOk;
+}
+
 int EulerSim::push_stack()
 {
+    int rc;
+    if ((rc = reserve_stack(n_maps_ + 1))) return rc;
     if (mixed_) {
         size_t mapb = sizeof(float4) * 2 * (size_t)gc.N;
-        if (n_maps_ >= stack_cap_) {
-            int cap = std::min(max_maps, std::max(2 * stack_cap_, 16));
-            float4* bigger = nullptr;
-            CMM_CUDA(cudaMalloc((void**)&bigger, mapb * cap));
-            if (stackm_ && n_maps_ > 0)
-                CMM_CUDA(cudaMemcpyAsync(bigger, stackm_, mapb * n_maps_, cudaMemcpyDeviceToDevice, stream));
-            CMM_CUDA(cudaStreamSynchronize(stream));
-            if (stackm_) cudaFree(stackm_);
-            stackm_ = bigger;
-            stack_cap_ = cap;
-        }
         CMM_CUDA(cudaMemcpyAsync(stackm_ + 2 * (size_t)n_maps_ * gc.N, mapm_, mapb, cudaMemcpyDeviceToDevice, stream));
         n_maps_++;
         return kOk;
-    }
-    if (n_maps_ >= stack_cap_) {
-        int cap = std::min(max_maps, std::max(2 * stack_cap_, 16));
-        double* bigger = nullptr;
-        CMM_CUDA(cudaMalloc((void**)&bigger, sizeof(double) * 8 * (size_t)gc.N * cap));
-        if (stack && n_maps_ > 0)
-            CMM_CUDA(cudaMemcpyAsync(bigger, stack, sizeof(double) * 8 * (size_t)gc.N * n_maps_,
-                                     cudaMemcpyDeviceToDevice, stream));
-        CMM_CUDA(cudaStreamSynchronize(stream));
-        if (stack) cudaFree(stack);
-        stack = bigger;
-        stack_cap_ = cap;
     }
     double* slot = stack + (size_t)n_maps_ * 8 * gc.N;
     CMM_CUDA(cudaMemcpyAsync(slot, ChiX, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToDevice, stream));
     CMM_CUDA(cudaMemcpyAsync(slot + 4 * gc.N, ChiY, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToDevice, stream));
     n_maps_++;
+    return kOk;
+}
+
+// ---------------------------------------------------------------- MapStack folder
+static std::string two_digits(int i) { return (i < 10 ? "0" : "") + std::to_string(i); }
+
+int EulerSim::write_map_stack(int map_num)
+{
+    // writeMapStack (src/ui/cmm-io.cu:611-635): one backward map in the reference's planar
+    // FP64 layout under MapStack/Map_Chi{X,Y}_H_<n|coarse>.data, and psi for the restart.
+    // The reference stores psi level 0 under every Stream_function_Psi_H_psi_<l> name
+    // (l = 1..L-1, it passes Psi.Dev_var for each); a restart then starts with a flat
+    // psi history.  Kept as is: the reference's restart goldens depend on it.
+    const std::string dir = run_dir(s) + "/MapStack";
+    if (!make_dir(dir)) { err = "cannot create " + dir; return kErrIO; }
+    const std::string name = map_num < 0 ? std::string("coarse") : std::to_string(map_num);
+    if (mixed_) CMM_LAUNCH(1, launch_map_to_planes(mapm_, gc, ChiX, ChiY, stream));
+    std::vector<double> h((size_t)8 * gc.N);
+    CMM_CUDA(cudaMemcpyAsync(h.data(), ChiX, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToHost, stream));
+    CMM_CUDA(cudaMemcpyAsync(h.data() + 4 * gc.N, ChiY, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToHost, stream));
+    const double* p0 = psi[0];
+    if (mixed_ && vlasov_)
+        CMM_LAUNCH(1, launch_vlasov_assemble(phi_lv_[0], phi_lv_[0] + gp.NX, vl_h_, vl_h_ + gp.NY, gp, psi[0], stream));
+    else if (mixed_)
+        CMM_LAUNCH(1, launch_float4_to_planes(psim_[0], gp.N, psi[0], stream));
+    std::vector<double> hp(L > 1 ? (size_t)4 * gp.N : 0);
+    if (L > 1) CMM_CUDA(cudaMemcpyAsync(hp.data(), p0, sizeof(double) * 4 * gp.N, cudaMemcpyDeviceToHost, stream));
+    CMM_CUDA(cudaStreamSynchronize(stream));
+    bool ok = write_f64(dir + "/Map_ChiX_H_" + name + ".data", h.data(), (size_t)4 * gc.N) &&
+              write_f64(dir + "/Map_ChiY_H_" + name + ".data", h.data() + 4 * gc.N, (size_t)4 * gc.N);
+    for (int l = 1; l < L && ok; ++l)
+        ok = write_f64(dir + "/Stream_function_Psi_H_psi_" + std::to_string(l) + ".data", hp.data(), (size_t)4 * gp.N);
+    if (!ok) { err = "cannot write the map stack under " + dir; return kErrIO; }
+    return kOk;
+}
+
+int EulerSim::write_particles_state()
+{
+    // writeParticlesState (src/ui/cmm-io.cu:638-657): positions of every advected set
+    const std::string dir = run_dir(s) + "/MapStack";
+    if (!make_dir(dir)) { err = "cannot create " + dir; return kErrIO; }
+    for (size_t i = 0; i < s.particles_advected.size(); ++i) {
+        const int num = s.particles_advected[i].num;
+        if (num <= 0) continue;
+        if (mixed_) CMM_LAUNCH(1, launch_fix_to_pos(partfix_[i], num, gp, parts[i], stream));
+        std::vector<double> h((size_t)2 * num);
+        CMM_CUDA(cudaMemcpyAsync(h.data(), parts[i], sizeof(double) * 2 * num, cudaMemcpyDeviceToHost, stream));
+        CMM_CUDA(cudaStreamSynchronize(stream));
+        if (!write_f64(dir + "/Particles_advected_pos_P" + two_digits((int)i + 1) + ".data", h.data(), h.size())) {
+            err = "cannot write particle state under " + dir;
+            return kErrIO;
+        }
+    }
+    return kOk;
+}
+
+int EulerSim::restart_from_map_stack()
+{
+    // readMapStack (src/simulation/cmm-simulation-host.cu:1256-1302) and the rest of the
+    // restart branch (src/simulation/cmm-euler2d.cu:634-685): every stored sub-map onto the
+    // stack (their count: files named *Map_ChiX_H* minus the active map's), the initial
+    // condition translated through them with the identity as the active map, then the
+    // stored active map and psi levels 1..L-1; psi level 0 and the coarse vorticity are
+    // computed from those, and the particle positions are read back.  Missing or short
+    // files are reported together (the reference logs them and exits).
+    const std::string dir = s.restart_location.empty() ? run_dir(s) + "/MapStack" : s.restart_location;
+    if (s.verbose >= 2) log_.push("Initializing by loading previous state");
+    std::string msg;
+    auto read = [&](const std::string& file, double* dst, size_t n) {
+        int r = read_f64(dir + "/" + file, dst, n);
+        if (r == 1) msg += "Failed to read in " + file + " at location " + dir + "\n";
+        if (r == 2) msg += "File " + dir + "/" + file + " holds fewer than " + std::to_string(n) + " values\n";
+        return r == 0;
+    };
+    const int n = count_files_containing(dir, "Map_ChiX_H") - 1;
+    if (n > max_maps) {
+        err = "the map stack at " + dir + " holds " + std::to_string(n) + " maps, more than mem_RAM_CPU_remaps allows (" +
+              std::to_string(max_maps) + ")";
+        return kErrParam;
+    }
+    int rc;
+    if (n > 0 && (rc = reserve_stack(n))) return rc;
+    const size_t nc4 = (size_t)4 * gc.N, np4 = (size_t)4 * gp.N;
+    std::vector<double> h(2 * nc4);
+    auto upload_map = [&](double* X, double* Y, float4* M) -> int {
+        // host planes -> the device map (FP64 planes, or a displacement map in the mixed form)
+        double* dX = mixed_ ? ChiX_new : X;
+        double* dY = mixed_ ? ChiY_new : Y;
+        CMM_CUDA(cudaMemcpyAsync(dX, h.data(), sizeof(double) * nc4, cudaMemcpyHostToDevice, stream));
+        CMM_CUDA(cudaMemcpyAsync(dY, h.data() + nc4, sizeof(double) * nc4, cudaMemcpyHostToDevice, stream));
+        if (mixed_) CMM_LAUNCH(1, launch_planes_to_map(dX, dY, gc, M, stream));
+        CMM_CUDA(cudaStreamSynchronize(stream));
+        return kOk;
+    };
+    for (int i = 0; i < n; ++i) {
+        bool ok = read("Map_ChiX_H_" + std::to_string(i) + ".data", h.data(), nc4);
+        ok = read("Map_ChiY_H_" + std::to_string(i) + ".data", h.data() + nc4, nc4) && ok;
+        if (!ok) continue;
+        if (mixed_) rc = upload_map(nullptr, nullptr, stackm_ + 2 * (size_t)i * gc.N);
+        else rc = upload_map(stack + (size_t)i * 8 * gc.N, stack + (size_t)i * 8 * gc.N + nc4, nullptr);
+        if (rc) return rc;
+    }
+    n_maps_ = std::max(n, 0);
+    if (!msg.empty()) { log_.push(msg + "Exitting .."); err = msg; return kErrIO; }
+    if (s.verbose >= 2) log_.push("Loaded " + std::to_string(n_maps_) + " maps to map stack");
+
+    if ((rc = reset_map()) || (rc = translate_ic())) return rc;
+    bool ok = read("Map_ChiX_H_coarse.data", h.data(), nc4);
+    ok = read("Map_ChiY_H_coarse.data", h.data() + nc4, nc4) && ok;
+    if (ok && (rc = upload_map(ChiX, ChiY, mapm_))) return rc;
+    std::vector<double> hp(np4);
+    for (int l = 1; l < L; ++l) {
+        if (!read("Stream_function_Psi_H_psi_" + std::to_string(l) + ".data", hp.data(), np4)) continue;
+        CMM_CUDA(cudaMemcpyAsync(psi[l], hp.data(), sizeof(double) * np4, cudaMemcpyHostToDevice, stream));
+        if (mixed_ && !vlasov_) CMM_LAUNCH(1, launch_planes_to_float4(nullptr, psi[l], gp.N, psim_[l], stream));
+        if (vlasov_) CMM_LAUNCH(1, launch_vlasov_phi_from_psi(psi[l], vl_h_, gp, phi_lv_[l], stream));
+        CMM_CUDA(cudaStreamSynchronize(stream));
+    }
+    if (!msg.empty()) { log_.push(msg + "Exitting .."); err = msg; return kErrIO; }
+    if ((rc = evaluate_stream()) || (rc = coarse_vort())) return rc;
+
+    // readParticlesState (src/ui/cmm-io.cu:659-688)
+    for (size_t i = 0; i < s.particles_advected.size(); ++i) {
+        const int num = s.particles_advected[i].num;
+        if (num <= 0) continue;
+        std::vector<double> pos((size_t)2 * num);
+        if (!read("Particles_advected_pos_P" + two_digits((int)i + 1) + ".data", pos.data(), pos.size())) continue;
+        CMM_CUDA(cudaMemcpyAsync(parts[i], pos.data(), sizeof(double) * pos.size(), cudaMemcpyHostToDevice, stream));
+        if (mixed_) CMM_LAUNCH(1, launch_pos_to_fix(parts[i], num, gp, partfix_[i], stream));
+        CMM_CUDA(cudaStreamSynchronize(stream));
+    }
+    if (!msg.empty()) { log_.push(msg + "Exitting .."); err = msg; return kErrIO; }
+    if (!s.particles_advected.empty() && s.verbose >= 2) log_.push("Loaded data for particle sets");
     return kOk;
 }
 
@@ -704,7 +835,7 @@ int EulerSim::init()
     int rc = alloc();
     if (rc) return rc;
     if (!create_directory_structure(s)) { err = "cannot create output folders under " + s.workspace; return kErrIO; }
-    log_.open(run_dir(s) + "/log.txt");
+    log_.start(run_dir(s) + "/log.txt", s.restart_time != 0, s.file_name);
     log_.quiet = s.verbose < 1;
     if (s.verbose >= 1) {
         if (vlasov_) log_.push(std::string("Starting Vlasov 1D simulation, initial condition ") + s.initial_condition);
@@ -735,11 +866,16 @@ int EulerSim::init()
 
     if ((rc = reset_map())) return rc;
     if (vlasov_ && (rc = vlasov_setup_h())) return rc;
-    if ((rc = translate_ic()) || (rc = evaluate_stream()) || (rc = coarse_vort())) return rc;
+    const bool restart = s.restart_time != 0;
+    if (restart) {
+        if ((rc = restart_from_map_stack())) return rc;
+    } else if ((rc = translate_ic()) || (rc = evaluate_stream()) || (rc = coarse_vort())) {
+        return rc;
+    }
 
     // Lagrange velocity history (cmm-euler2d.cu:520-619): alternate the
     // direction of time and raise the scheme order EulerExp -> RK2 -> RK3
-    if (L > 1) {
+    if (L > 1 && !restart) {
         double dt_now = dt * std::pow(-1.0, L);
         double t_init[5] = {0, dt_now, 2 * dt_now, 3 * dt_now, 4 * dt_now};
         double dt_init[5] = {dt_now, dt_now, dt_now, dt_now, dt_now};
@@ -771,14 +907,17 @@ int EulerSim::init()
         }
         if ((rc = reset_map())) return rc;
     }
-    if ((rc = init_particles())) return rc;
-    for (size_t i = 0; i < partfix_.size(); ++i)
-        CMM_LAUNCH(1, launch_pos_to_fix(parts[i], s.particles_advected[i].num, gp, partfix_[i], stream));
+    if (!restart) {
+        if ((rc = init_particles())) return rc;
+        for (size_t i = 0; i < partfix_.size(); ++i)
+            CMM_LAUNCH(1, launch_pos_to_fix(parts[i], s.particles_advected[i].num, gp, partfix_[i], stream));
+    }
 
     t_vec_.assign((size_t)s.iter_max() + L + 8, 0.0);
     dt_vec_.assign(t_vec_.size(), dt);
     for (int i = 0; i < L; ++i) { t_vec_[i] = s.restart_time - (L - 1 - i) * dt; dt_vec_[i] = dt; }
-    loop_ctr_ = 0; old_ctr_ = 0; n_maps_ = 0;
+    loop_ctr_ = 0; old_ctr_ = 0;
+    if (!restart) n_maps_ = 0;   // a restart keeps the sub-maps it loaded
     initialised_ = true;
 
     if ((rc = save_functions(s.restart_time, dt))) return rc;
@@ -854,6 +993,7 @@ int EulerSim::step_once()
             old_ctr_ = loop_ctr_;
             ph_begin(kPhRemap);
             if ((rc = translate_ic())) return rc;
+            if (s.save_map_stack && (rc = write_map_stack(n_maps_))) return rc;
             if ((rc = push_stack())) return rc;
             if ((rc = reset_map())) return rc;
             kernel_launches++;
@@ -900,6 +1040,17 @@ int EulerSim::finish()
     if (finished_) return kOk;
     int rc = save_functions(kTMax, dt);
     if (rc) return rc;
+    if (s.save_map_stack) {
+        // cmm-euler2d.cu:1033-1051: the active map, psi and the particle state
+        if (s.verbose >= 2) {
+            std::ostringstream os;
+            os.precision(16);
+            os << "Saving last Map of MapStack : Maps = " << n_maps_ << " \t Total size = "
+               << (n_maps_ + 1) * (8.0 * gc.N * 8 / 1e6) << "mb \t S-time = " << time();
+            log_.push(os.str());
+        }
+        if ((rc = write_map_stack(-1)) || (rc = write_particles_state())) return rc;
+    }
     CMM_CUDA(cudaStreamSynchronize(stream));
     double tc = wall();
     append_f64(run_dir(s) + "/Monitoring_data/Time_c.data", &tc, 1);

@@ -93,6 +93,12 @@ private:
     int init_particles();
     int advect_particles(int lcl);
     int push_stack();
+    int reserve_stack(int n);          // device stack capacity for n sub-maps
+    // MapStack folder (writeMapStack / writeParticlesState / readMapStack, cmm-io.cu:611-688,
+    // cmm-simulation-host.cu:1256-1302): map_num >= 0 a stacked sub-map, -1 the active map
+    int write_map_stack(int map_num);
+    int write_particles_state();
+    int restart_from_map_stack();      // the restart branch of init (cmm-euler2d.cu:634-685)
     int sample_outputs(double t_now, double dt_now);   // sampled outputs on user grids
     int evaluate_potential();          // Vlasov-Poisson psi from the distribution function
     int vlasov_setup_h();              // the periodification h(v), once per run

@@ -46,6 +46,8 @@ cudaError_t launch_vlasov_h_spec(const double2* sig_hat, const Grid& gp, double2
 // Hermite planes of psi = phi(x) - h(v) on the psi grid (plain form)
 cudaError_t launch_vlasov_assemble(const double* phi, const double* dphi, const double* h, const double* dh,
                                    const Grid& gp, double* psi4, cudaStream_t s);
+// phi(x), phi'(x) (2 x NX) of Hermite planes of psi = phi(x) - h(v): row 0 of psi plus h(v_0), row 0 of psi_x
+cudaError_t launch_vlasov_phi_from_psi(const double* psi4, const double* h, const Grid& gp, double* phi, cudaStream_t s);
 // sums of f, f v and f v^2 over the coarse grid (v = b2 + iY hy) -> out3 (device)
 cudaError_t launch_vlasov_moments(const double* f, const Grid& gc, double* partial, double* out3, cudaStream_t s);
 // 1D Hermite table of a Lagrange combination c_l of phi levels: table[i] =

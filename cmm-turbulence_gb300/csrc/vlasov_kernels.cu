@@ -193,6 +193,23 @@ cudaError_t launch_vlasov_assemble(const double* phi, const double* dphi, const 
     return cudaGetLastError();
 }
 
+// phi, phi' of a separable psi's Hermite planes (a psi level read back at a restart):
+// row 0 of psi + h(v_0) and row 0 of psi_x
+__global__ void k_vlasov_phi_from_psi(const double* __restrict__ psi4, const double* __restrict__ h, Grid gp,
+                                      double* __restrict__ phi)
+{
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ix >= gp.NX) return;
+    phi[ix] = psi4[ix] + h[0];
+    phi[gp.NX + ix] = psi4[gp.N + ix];
+}
+
+cudaError_t launch_vlasov_phi_from_psi(const double* psi4, const double* h, const Grid& gp, double* phi, cudaStream_t s)
+{
+    k_vlasov_phi_from_psi<<<(unsigned)((gp.NX + 255) / 256), 256, 0, s>>>(psi4, h, gp, phi);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------- diagnostics
 __global__ void __launch_bounds__(256) k_vlasov_moments_partial(const double* __restrict__ f, Grid gc,
                                                                 double* __restrict__ partial)

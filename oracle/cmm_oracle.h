@@ -142,6 +142,13 @@ int og_init(og_state* st);
  * dt_now from the caller (compute_next_timestep). Returns 0 ok, 1 stack saturated
  * (loop stops), 2 Vlasov incompressibility blow-up (cmm-vlasov1d.cu:838-840). */
 int og_step(og_state* st, double dt_now, double* e_inc, int* remapped);
+/* in place of og_init: restart from a stored map stack (n sub-maps, each 4*Nc X planes in
+ * stackX and 4*Nc Y planes in stackY), the stored active map and psi levels 1..L-1
+ * (src/simulation/cmm-simulation-host.cu:1256-1302, src/simulation/cmm-euler2d.cu:634-715) */
+int og_restart(og_state* st, double restart_time, int n_maps, const double* stackX, const double* stackY,
+               const double* chix, const double* chiy, const double* psi_prev);
+const double* og_stack_x(const og_state* st);     /* n_maps x 4*Nc */
+const double* og_stack_y(const og_state* st);
 
 /* state access (reference layouts) */
 double og_time(const og_state* st);

@@ -507,6 +507,40 @@ int og_init(og_state* st)
     return 0;
 }
 
+/* Restart from a stored map stack instead of og_init: readMapStack
+ * (src/simulation/cmm-simulation-host.cu:1256-1302) and the restart branch of the driver
+ * (src/simulation/cmm-euler2d.cu:634-685, clock :711-715).  The n stored sub-maps become the
+ * stack and the initial condition is translated through them with the identity as the active
+ * map; then the stored active map and psi levels 1..L-1 are put in place, psi level 0 and the
+ * coarse vorticity are computed from them, and the clock starts at restart_time.  Particle
+ * positions are set beforehand with og_set_particles.  Returns -1 when n exceeds the stack. */
+int og_restart(og_state* st, double restart_time, int n_maps, const double* stackX, const double* stackY,
+               const double* chix, const double* chiy, const double* psi_prev)
+{
+    og_settings* s = &st->s;
+    long Nc4 = 4 * st->gc.N, Np4 = 4 * st->gp.N;
+    int Lo = s->lagrange_order;
+    if (n_maps < 0 || n_maps > s->max_maps) return -1;
+    if (n_maps > 0) {
+        memcpy(st->stackX, stackX, sizeof(double) * Nc4 * (size_t)n_maps);
+        memcpy(st->stackY, stackY, sizeof(double) * Nc4 * (size_t)n_maps);
+    }
+    st->n_maps = n_maps;
+    og_init_diffeo(st->ChiX, st->ChiY, &st->gc);
+    translate_ic(st);
+    memcpy(st->ChiX, chix, sizeof(double) * Nc4);
+    memcpy(st->ChiY, chiy, sizeof(double) * Nc4);
+    for (int l = 1; l < Lo; ++l) memcpy(st->psi + Np4 * l, psi_prev + Np4 * (l - 1), sizeof(double) * Np4);
+    if (evaluate_stream(st)) return -1;
+    coarse_vort(st);
+    for (int i = 0; i < Lo; i++) { st->t_vec[i] = restart_time - (Lo - 1 - i) * s->dt; st->dt_vec[i] = s->dt; }
+    st->loop_ctr = 0; st->old_ctr = 0;
+    return 0;
+}
+
+const double* og_stack_x(const og_state* st) { return st->stackX; }
+const double* og_stack_y(const og_state* st) { return st->stackY; }
+
 int og_step(og_state* st, double dt_now, double* e_inc, int* remapped)
 {
     og_settings* s = &st->s;

@@ -87,6 +87,11 @@ def lib():
         L.og_init.restype = C.c_int
         L.og_state_sample.argtypes = [C.c_void_p, C.c_int, C.c_int, dp, dp]
         L.og_vlasov_state_mesure.argtypes = [C.c_void_p, dp]
+        L.og_restart.argtypes = [C.c_void_p, C.c_double, C.c_int, dp, dp, dp, dp, dp]
+        L.og_restart.restype = C.c_int
+        for name in ("og_stack_x", "og_stack_y"):
+            getattr(L, name).restype = dp
+            getattr(L, name).argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -171,6 +176,41 @@ class EulerOracle:
         if rc:
             raise ValueError("oracle initialisation rejected the grids (vort grid finer than psi grid?)")
 
+    def restart(self, restart_time, files):
+        """In place of init(): restart from a stored map stack given as the file
+        contents of a MapStack folder (read_map_stack_dir / map_stack_files);
+        readMapStack, src/simulation/cmm-simulation-host.cu:1256-1302."""
+        nc4 = 4 * self.grid(0).N
+        np4 = 4 * self.grid(2).N
+        Lo = self.cfg["lagrange_order"]
+        n = sum(1 for k in files if "Map_ChiX_H" in k) - 1
+        sx = np.zeros(max(n, 1) * nc4)
+        sy = np.zeros(max(n, 1) * nc4)
+        for i in range(n):
+            sx[i * nc4:(i + 1) * nc4] = files["Map_ChiX_H_%d" % i]
+            sy[i * nc4:(i + 1) * nc4] = files["Map_ChiY_H_%d" % i]
+        chix = np.ascontiguousarray(files["Map_ChiX_H_coarse"], dtype=np.float64)
+        chiy = np.ascontiguousarray(files["Map_ChiY_H_coarse"], dtype=np.float64)
+        prev = np.zeros(max(Lo - 1, 1) * np4)
+        for l in range(1, Lo):
+            prev[(l - 1) * np4:l * np4] = files["Stream_function_Psi_H_psi_%d" % l]
+        for i, p in enumerate(self.cfg.get("particles", [])):
+            self.set_particles(i, files["Particles_advected_pos_P%02d" % (i + 1)])
+        rc = self.L.og_restart(self.h, restart_time, n, _dp(sx), _dp(sy), _dp(chix), _dp(chiy), _dp(prev))
+        if rc:
+            raise ValueError("oracle restart rejected the stored map stack (%d maps, capacity %d)"
+                             % (n, self.cfg["max_maps"]))
+        return n
+
+    def map_stack(self):
+        """(X planes, Y planes) of the stacked sub-maps, shape (n, 4*Nc) each."""
+        n, nc4 = self.map_count(), 4 * self.grid(0).N
+        if n == 0:
+            return np.zeros((0, nc4)), np.zeros((0, nc4))
+        x = np.ctypeslib.as_array(self.L.og_stack_x(self.h), shape=(n * nc4,)).copy()
+        y = np.ctypeslib.as_array(self.L.og_stack_y(self.h), shape=(n * nc4,)).copy()
+        return x.reshape(n, nc4), y.reshape(n, nc4)
+
     def step(self, dt_now):
         e = C.c_double()
         r = C.c_int()
@@ -248,6 +288,38 @@ class EulerOracle:
         self.L.og_vlasov_state_mesure(self.h, _dp(out))
         keys = ("Etot", "Ekin", "Epot", "Mass", "Momentum", "Emode1", "Emode2", "Emode3", "Emode4")
         return dict(zip(keys, out.tolist()))
+
+
+# ---------------------------------------------------------------- MapStack folder
+def map_stack_files(o):
+    """The files writeMapStack / writeParticlesState leave in the MapStack folder at
+    the end of a run (src/ui/cmm-io.cu:611-657; src/simulation/cmm-euler2d.cu:1033-1051):
+    every stacked sub-map (Map_ChiX_H_<i>, Map_ChiY_H_<i>, 4*Nc planar doubles), the
+    active map (..._H_coarse) and Stream_function_Psi_H_psi_<l> for l = 1..L-1 -- each
+    of them a copy of psi level 0, as the reference writes Psi.Dev_var for every l
+    (src/ui/cmm-io.cu:631-633) -- and the tracer positions Particles_advected_pos_P<ii>."""
+    files = {}
+    sx, sy = o.map_stack()
+    for i in range(sx.shape[0]):
+        files["Map_ChiX_H_%d" % i] = sx[i]
+        files["Map_ChiY_H_%d" % i] = sy[i]
+    files["Map_ChiX_H_coarse"] = o.chix()
+    files["Map_ChiY_H_coarse"] = o.chiy()
+    p0 = o.psi(1)
+    for l in range(1, o.cfg["lagrange_order"]):
+        files["Stream_function_Psi_H_psi_%d" % l] = p0
+    for i in range(len(o.cfg.get("particles", []))):
+        files["Particles_advected_pos_P%02d" % (i + 1)] = o.particles(i)
+    return files
+
+
+def read_map_stack_dir(path):
+    """{name: float64 array} of the .data files of a MapStack folder."""
+    out = {}
+    for fn in sorted(os.listdir(path)):
+        if fn.endswith(".data"):
+            out[fn[:-len(".data")]] = np.fromfile(os.path.join(path, fn), dtype=np.float64)
+    return out
 
 
 # ---------------------------------------------------------------- kernel-level restatements

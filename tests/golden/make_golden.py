@@ -29,6 +29,10 @@ TESTS = {
                  "tests/euler2D_one_step/params.txt"),
     "remap_11b": ("tests/euler2D_11b_4nodes_reference_remapping/data/reference-results_4_nodes_C256_F512_t32_T2",
                   "examples/euler2D/params-11b-4nodes-reference-remapping.txt"),
+    # restart: params-1 runs to t = 1 writing its MapStack, params-2 restarts from it to t = 2;
+    # the goldens are those of the restarted run
+    "restart_remap": ("tests/euler2D_remap/data/reference-results_4_nodes_C256_F512_t32_T2",
+                      "tests/euler2D_remap/params-2.txt", "tests/euler2D_remap/params-1.txt"),
     "vlasov_15": ("tests/vlasov1D_15_vp_landau_damping/data/reference-results_C256_F512_t1024_T0.2",
                   "tests/vlasov1D_15_vp_landau_damping/params-15b-vp-landau-damping.txt"),
 }
@@ -44,9 +48,11 @@ def read_f64(path):
 def main(ref_root):
     base = os.path.join(ref_root, "Cuda-CMM")
     out = {}
-    for name, (res_dir, param_file) in TESTS.items():
+    for name, (res_dir, param_file, *pre) in TESTS.items():
         rdir = os.path.join(base, res_dir, "Monitoring_data")
         entry = {"params_in": open(os.path.join(base, param_file)).read(), "files": {}}
+        if pre:
+            entry["params_pre"] = open(os.path.join(base, pre[0])).read()
         for root, _, files in os.walk(rdir):
             for fn in sorted(files):
                 if not fn.endswith(".data") or fn.endswith("_Hash.data") or fn == "Time_c.data":

@@ -6,16 +6,23 @@ import oracle as O
 
 
 class OracleRun:
-    def __init__(self, settings, particle_init=None):
+    def __init__(self, settings, particle_init=None, restart_files=None):
         self.s = settings
         self.o = O.EulerOracle(settings.oracle_config())
         self.particle_init = particle_init or {}
+        self.restart_files = restart_files
+        self.loaded_maps = None
 
     # stepper interface
     def init(self):
         for i, pos in self.particle_init.items():
             self.o.set_particles(i, pos)
-        self.o.init()
+        if self.s.restart_time != 0:
+            # the restart branch of the driver reads the stored state instead of
+            # building the Lagrange history (cmm-euler2d.cu:520-685)
+            self.loaded_maps = self.o.restart(self.s.restart_time, self.restart_files)
+        else:
+            self.o.init()
 
     def step(self, dt_now):
         rc, e, r = self.o.step(dt_now)

@@ -18,6 +18,7 @@ import pytest
 import refloop
 from goldens import DebugRecorder, compare_series, goldens
 from oracle_adapter import OracleRun
+import oracle as O
 
 RTOL = 1e-9
 
@@ -44,6 +45,29 @@ def test_oracle_matches_reference_remapping_11b():
     rec, g, keys = _run("remap_11b")
     worst, fails = compare_series(rec.series, g["files"], keys, RTOL)
     # the remap step (47) and map counter must agree exactly
+    assert rec.series["Map_counter"] == g["files"]["Map_counter"]
+    assert not fails, fails
+
+
+def test_oracle_matches_reference_restart():
+    """The reference's restart test (tests/euler2D_remap): params-1 runs to t = 1 with
+    save_map_stack=1, params-2 restarts from its MapStack folder and runs on to t = 2;
+    the goldens are the restarted run's.  The restarted run starts with psi levels
+    1..L-1 all equal to psi(1), because writeMapStack stores level 0 under every level's
+    name (src/ui/cmm-io.cu:631-633); the goldens pin that behaviour."""
+    g = goldens()["restart_remap"]
+    s1 = refloop.settings_from_param_text(g["params_pre"])
+    pre = OracleRun(s1)
+    refloop.run_reference_loop(s1, pre, lambda t, dt: None)
+    files = O.map_stack_files(pre.o)
+    s2 = refloop.settings_from_param_text(g["params_in"])
+    run = OracleRun(s2, restart_files=files)
+    rec = DebugRecorder(s2, run)
+    refloop.run_reference_loop(s2, run, rec.on_save, rec.on_step)
+    assert run.loaded_maps == 3      # the golden's log: "Loaded 3 maps to map stack"
+    keys = [k for k in g["files"] if "Particles" not in k]
+    worst, fails = compare_series(rec.series, g["files"], keys, RTOL)
+    assert len(worst) >= 40
     assert rec.series["Map_counter"] == g["files"]["Map_counter"]
     assert not fails, fails
 

@@ -8,53 +8,208 @@
 namespace cmm {
 
 // ---------------------------------------------------------------------------
-// tracer particles (Particle_advect, src/numerical/cmm-particles.cu:119-276);
-// psi[0] holds t_{n+1}, psi[1] holds t_n
+// tracer and inertial particles (Particle_advect, src/numerical/cmm-particles.cu:119-276;
+// Particle_advect_inertia, :280-551).  psi[0] holds t_{n+1}, psi[1] t_n, psi[2] t_{n-1};
+// Lp12 combines the L levels to t_{n+1/2}.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ void part_level(const ParticleArgs& a, int l, double x, double y, double& ux, double& uy)
+{
+    const double* lv[1] = {a.psi[l]};
+    double u1[1], v1[1];
+    velocity_levels<1>(lv, a.gp, x, y, u1, v1);
+    ux = u1[0];
+    uy = v1[0];
+}
+
+template <int L>
+__device__ __forceinline__ void part_half(const ParticleArgs& a, double x, double y, double& kx, double& ky)
+{
+    double ux[L], uy[L];
+    velocity_levels<L>(a.psi, a.gp, x, y, ux, uy);
+    kx = a.Lp12[0] * ux[0];
+    ky = a.Lp12[0] * uy[0];
+#pragma unroll
+    for (int l = 1; l < L; ++l) { kx = fma(a.Lp12[l], ux[l], kx); ky = fma(a.Lp12[l], uy[l], ky); }
+}
+
 template <int L, int TI>
 __global__ void __launch_bounds__(256) k_particles(const ParticleArgs a)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.num) return;
     double px = a.pos[2 * i], py = a.pos[2 * i + 1];
-    const double* lv1[1] = {a.psi[1]};
-    const double* lv0[1] = {a.psi[0]};
     const double dt = a.dt;
-    double ux[L], uy[L], k1x[1], k1y[1];
-    velocity_levels<1>(lv1, a.gp, px, py, k1x, k1y);
+    double k1x, k1y, k2x, k2y, k3x, k3y, k4x, k4y;
+    part_level(a, 1, px, py, k1x, k1y);
     if (TI == 10) {
-        px += dt * k1x[0];
-        py += dt * k1y[0];
+        px += dt * k1x;
+        py += dt * k1y;
     } else if (TI == 20) {
-        double k2x[1], k2y[1];
-        velocity_levels<1>(lv0, a.gp, px + dt * k1x[0], py + dt * k1y[0], k2x, k2y);
-        px += dt * (k1x[0] + k2x[0]) / 2;
-        py += dt * (k1y[0] + k2y[0]) / 2;
-    } else {  // RK3
-        velocity_levels<L>(a.psi, a.gp, px + dt * k1x[0] / 2.0, py + dt * k1y[0] / 2.0, ux, uy);
-        double k2x = a.Lp12[0] * ux[0], k2y = a.Lp12[0] * uy[0];
-#pragma unroll
-        for (int l = 1; l < L; ++l) { k2x = fma(a.Lp12[l], ux[l], k2x); k2y = fma(a.Lp12[l], uy[l], k2y); }
-        double k3x[1], k3y[1];
-        velocity_levels<1>(lv0, a.gp, px - dt * k1x[0] + 2 * dt * k2x, py - dt * k1y[0] + 2 * dt * k2y, k3x, k3y);
-        px += dt * (k1x[0] + 4 * k2x + k3x[0]) / 6.0;
-        py += dt * (k1y[0] + 4 * k2y + k3y[0]) / 6.0;
+        part_level(a, 0, px + dt * k1x, py + dt * k1y, k2x, k2y);
+        px += dt * (k1x + k2x) / 2;
+        py += dt * (k1y + k2y) / 2;
+    } else if (TI == 30) {
+        part_half<L>(a, px + dt * k1x / 2.0, py + dt * k1y / 2.0, k2x, k2y);
+        part_level(a, 0, px - dt * k1x + 2 * dt * k2x, py - dt * k1y + 2 * dt * k2y, k3x, k3y);
+        px += dt * (k1x + 4 * k2x + k3x) / 6.0;
+        py += dt * (k1y + 4 * k2y + k3y) / 6.0;
+    } else if (TI == 40) {
+        part_half<L>(a, px + dt * k1x / 2.0, py + dt * k1y / 2.0, k2x, k2y);
+        part_half<L>(a, px + dt * k2x / 2.0, py + dt * k2y / 2.0, k3x, k3y);
+        part_level(a, 0, px + dt * k3x, py + dt * k3y, k4x, k4y);
+        px += dt * (k1x + 2 * k2x + 2 * k3x + k4x) / 6.0;
+        py += dt * (k1y + 2 * k2y + 2 * k3y + k4y) / 6.0;
+    } else if (TI == 31) {
+        part_level(a, 0, px + dt * k1x, py + dt * k1y, k2x, k2y);
+        part_level(a, 2, px + dt * (k1x - 2 * k2x), py + dt * (k1y - 2 * k2y), k3x, k3y);
+        px += dt * (8 * k1x + 5 * k2x - k3x) / 12.0;
+        py += dt * (8 * k1y + 5 * k2y - k3y) / 12.0;
+    } else {   // 41
+        part_level(a, 0, px + dt * k1x, py + dt * k1y, k2x, k2y);
+        part_half<L>(a, px + dt / 8.0 * (3 * k1x + k2x), py + dt / 8.0 * (3 * k1y + k2y), k3x, k3y);
+        part_level(a, 0, px + dt / 3.0 * (-k2x + 4 * k3x), py + dt / 3.0 * (-k2y + 4 * k3y), k4x, k4y);
+        px += dt * (2 * k1x - k2x + 8 * k3x + 3 * k4x) / 12.0;
+        py += dt * (2 * k1y - k2y + 8 * k3y + 3 * k4y) / 12.0;
     }
     a.pos[2 * i] = wrap(px, a.gp.b0, a.gp.Wx);
     a.pos[2 * i + 1] = wrap(py, a.gp.b2, a.gp.Wy);
 }
 
+// inertial particles: dx/dt = v, dv/dt = -(v - u(x, t)) / tau.  Each stage s has a position
+// increment xs (a velocity) and an acceleration as = -(vs - u(x + ..., t_s)) / tau.
+template <int L, int TI>
+__global__ void __launch_bounds__(256) k_particles_inertia(const ParticleArgs a)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.num) return;
+    const double px = a.pos[2 * i], py = a.pos[2 * i + 1];
+    const double vx = a.vel[2 * i], vy = a.vel[2 * i + 1];
+    const double dt = a.dt, tau = a.tau;
+    double ux, uy, nx, ny, nvx, nvy;
+    auto acc = [&](double sx, double sy, double& ax, double& ay) { ax = -(sx - ux) / tau; ay = -(sy - uy) / tau; };
+    part_level(a, 1, px, py, ux, uy);
+    double a1x, a1y;
+    acc(vx, vy, a1x, a1y);
+    if (TI == 10) {
+        nx = px + dt * vx;
+        ny = py + dt * vy;
+        nvx = vx - dt * (vx - ux) / tau;
+        nvy = vy - dt * (vy - uy) / tau;
+    } else if (TI == 20) {
+        const double x2x = vx + dt * a1x, x2y = vy + dt * a1y;
+        double a2x, a2y;
+        part_level(a, 0, px + dt * vx, py + dt * vy, ux, uy);
+        acc(x2x, x2y, a2x, a2y);
+        nx = px + dt / 2.0 * (vx + x2x);
+        ny = py + dt / 2.0 * (vy + x2y);
+        nvx = vx + dt / 2.0 * (a1x + a2x);
+        nvy = vy + dt / 2.0 * (a1y + a2y);
+    } else if (TI == 30) {
+        const double x2x = vx + dt / 2.0 * a1x, x2y = vy + dt / 2.0 * a1y;
+        double a2x, a2y, a3x, a3y;
+        part_half<L>(a, px + dt / 2.0 * vx, py + dt / 2.0 * vy, ux, uy);
+        acc(x2x, x2y, a2x, a2y);
+        const double x3x = vx + dt * (-a1x + 2 * a2x), x3y = vy + dt * (-a1y + 2 * a2y);
+        part_level(a, 0, px + dt * (-vx + 2 * x2x), py + dt * (-vy + 2 * x2y), ux, uy);
+        acc(x3x, x3y, a3x, a3y);
+        nx = px + dt / 6.0 * (vx + 4 * x2x + x3x);
+        ny = py + dt / 6.0 * (vy + 4 * x2y + x3y);
+        nvx = vx + dt / 6.0 * (a1x + 4 * a2x + a3x);
+        nvy = vy + dt / 6.0 * (a1y + 4 * a2y + a3y);
+    } else if (TI == 40) {
+        const double x2x = vx + dt / 2.0 * a1x, x2y = vy + dt / 2.0 * a1y;
+        double a2x, a2y, a3x, a3y, a4x, a4y;
+        part_half<L>(a, px + dt / 2.0 * vx, py + dt / 2.0 * vy, ux, uy);
+        acc(x2x, x2y, a2x, a2y);
+        const double x3x = vx + dt / 2.0 * a2x, x3y = vy + dt / 2.0 * a2y;
+        part_half<L>(a, px + dt / 2.0 * x2x, py + dt / 2.0 * x2y, ux, uy);
+        acc(x3x, x3y, a3x, a3y);
+        const double x4x = vx + dt * a3x, x4y = vy + dt * a3y;
+        part_level(a, 0, px + dt * x3x, py + dt * x3y, ux, uy);
+        acc(x4x, x4y, a4x, a4y);
+        nx = px + dt / 6.0 * (vx + 2 * x2x + 2 * x3x + x4x);
+        ny = py + dt / 6.0 * (vy + 2 * x2y + 2 * x3y + x4y);
+        nvx = vx + dt / 6.0 * (a1x + 2 * a2x + 2 * a3x + a4x);
+        nvy = vy + dt / 6.0 * (a1y + 2 * a2y + 2 * a3y + a4y);
+    } else if (TI == 31) {
+        const double x2x = vx + dt * a1x, x2y = vy + dt * a1y;
+        double a2x, a2y, a3x, a3y;
+        part_level(a, 0, px + dt * vx, py + dt * vy, ux, uy);
+        acc(x2x, x2y, a2x, a2y);
+        const double x3x = vx + dt * (a1x - 2 * a2x), x3y = vy + dt * (a1y - 2 * a2y);
+        part_level(a, 2, px + dt * (vx - 2 * x2x), py + dt * (vy - 2 * x2y), ux, uy);
+        acc(x3x, x3y, a3x, a3y);
+        nx = px + dt / 12.0 * (8 * vx + 5 * x2x - x3x);
+        ny = py + dt / 12.0 * (8 * vy + 5 * x2y - x3y);
+        nvx = vx + dt / 12.0 * (8 * a1x + 5 * a2x - a3x);
+        nvy = vy + dt / 12.0 * (8 * a1y + 5 * a2y - a3y);
+    } else {   // 41
+        const double x2x = vx + dt * a1x, x2y = vy + dt * a1y;
+        double a2x, a2y, a3x, a3y, a4x, a4y;
+        part_level(a, 0, px + dt * vx, py + dt * vy, ux, uy);
+        acc(x2x, x2y, a2x, a2y);
+        const double x3x = vx + dt / 8.0 * (3 * a1x + a2x), x3y = vy + dt / 8.0 * (3 * a1y + a2y);
+        part_half<L>(a, px + dt / 8.0 * (3 * vx + x2x), py + dt / 8.0 * (3 * vy + x2y), ux, uy);
+        acc(x3x, x3y, a3x, a3y);
+        const double x4x = vx + dt / 3.0 * (-a2x + 4 * a3x), x4y = vy + dt / 3.0 * (-a2y + 4 * a3y);
+        part_level(a, 0, px + dt / 3.0 * (-x2x + 4 * x3x), py + dt / 3.0 * (-x2y + 4 * x3y), ux, uy);
+        acc(x4x, x4y, a4x, a4y);
+        nx = px + dt / 12.0 * (2 * vx - x2x + 8 * x3x + 3 * x4x);
+        ny = py + dt / 12.0 * (2 * vy - x2y + 8 * x3y + 3 * x4y);
+        nvx = vx + dt / 12.0 * (2 * a1x - a2x + 8 * a3x + 3 * a4x);
+        nvy = vy + dt / 12.0 * (2 * a1y - a2y + 8 * a3y + 3 * a4y);
+    }
+    a.pos[2 * i] = wrap(nx, a.gp.b0, a.gp.Wx);
+    a.pos[2 * i + 1] = wrap(ny, a.gp.b2, a.gp.Wy);
+    a.vel[2 * i] = nvx;
+    a.vel[2 * i + 1] = nvy;
+}
+
 cudaError_t launch_particles(const ParticleArgs& a, cudaStream_t s)
 {
     if (a.num <= 0) return cudaSuccess;
-    int threads = 256;
-    unsigned blocks = (unsigned)((a.num + threads - 1) / threads);
-    int L = a.l_order;
-    if (a.time_integration_num == 10) k_particles<1, 10><<<blocks, threads, 0, s>>>(a);
-    else if (a.time_integration_num == 20) k_particles<1, 20><<<blocks, threads, 0, s>>>(a);
-    else if (a.time_integration_num == 30 && L == 3) k_particles<3, 30><<<blocks, threads, 0, s>>>(a);
-    else if (a.time_integration_num == 30 && L == 4) k_particles<4, 30><<<blocks, threads, 0, s>>>(a);
-    else return cudaErrorInvalidValue;
+    const int threads = 256;
+    const unsigned blocks = (unsigned)((a.num + threads - 1) / threads);
+    const bool inert = a.tau != 0;
+    if (inert && !a.vel) return cudaErrorInvalidValue;
+#define CMM_PART(LL, TT)                                                                    \
+    do {                                                                                    \
+        if (inert) k_particles_inertia<LL, TT><<<blocks, threads, 0, s>>>(a);               \
+        else k_particles<LL, TT><<<blocks, threads, 0, s>>>(a);                             \
+    } while (0)
+    // level 1 (t_n) is read by every scheme, level 2 by RK3Mod; the half-step
+    // combination uses all L levels
+    switch (a.time_integration_num * 10 + a.l_order) {
+        case 101: case 102: case 103: case 104: CMM_PART(1, 10); break;
+        case 202: case 203: case 204: CMM_PART(1, 20); break;
+        case 303: CMM_PART(3, 30); break;
+        case 304: CMM_PART(4, 30); break;
+        case 404: CMM_PART(4, 40); break;
+        case 313: case 314: CMM_PART(1, 31); break;
+        case 414: CMM_PART(4, 41); break;
+        default: return cudaErrorInvalidValue;
+    }
+#undef CMM_PART
+    return cudaGetLastError();
+}
+
+__global__ void k_particle_vel_init(const double* __restrict__ pos, int num, const double* __restrict__ psi0, Grid g,
+                                    double* __restrict__ vel)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= num) return;
+    const double* lv[1] = {psi0};
+    double ux[1], uy[1];
+    velocity_levels<1>(lv, g, pos[2 * i], pos[2 * i + 1], ux, uy);
+    vel[2 * i] = ux[0];
+    vel[2 * i + 1] = uy[0];
+}
+
+cudaError_t launch_particle_vel_init(const double* pos, int num, const double* psi0, const Grid& gp, double* vel,
+                                     cudaStream_t s)
+{
+    if (num <= 0) return cudaSuccess;
+    k_particle_vel_init<<<(num + 255) / 256, 256, 0, s>>>(pos, num, psi0, gp, vel);
     return cudaGetLastError();
 }
 

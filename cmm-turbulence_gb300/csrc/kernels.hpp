@@ -24,7 +24,7 @@ struct AdvectArgs {
     double L1[kMaxLagrange], L12[kMaxLagrange];
     double coef[4][kMaxFoot];            // c1, cx, cy, cxy footpoint weights
     double dt, ep;
-    int time_integration_num;            // 10 EulerExp, 21 RK2 (Heun), 30 RK3
+    int time_integration_num;            // 10 EulerExp, 21 RK2 (Heun), 20 AB2, 30 RK3, 40 RK4, 31 RK3Mod, 41 RK4Mod
     int l_order;                         // Lagrange levels used (1..4)
     int nfoot;                           // 4, 8 or 12 footpoints
 };
@@ -63,18 +63,24 @@ cudaError_t launch_sample_vort(const Grid& gm, const Grid& gout, const Grid& gf,
                                const double* Y, const double* Wf, int molly, double* out, long long ld,
                                cudaStream_t s);
 
-// tracer particles (Particle_advect, src/numerical/cmm-particles.cu:119-276)
+// tracer and inertial particles (Particle_advect / Particle_advect_inertia,
+// src/numerical/cmm-particles.cu:119-551); psi[0] is t_{n+1}, psi[1] t_n, psi[2] t_{n-1}
 struct ParticleArgs {
     Grid gp;
     double* pos;
+    double* vel;                // inertial velocity state (tau != 0), else unused
     int num;
     const double* psi[kMaxLagrange];
     double Lp12[kMaxLagrange];
     double dt;
-    int time_integration_num;   // 10, 20, 30
+    double tau;                 // 0: fluid tracers
+    int time_integration_num;   // 10, 20, 30, 40, 31, 41
     int l_order;
 };
 cudaError_t launch_particles(const ParticleArgs& a, cudaStream_t s);
+// v = u(x) of psi level psi0 (Particle_advect_inertia_init, cmm-particles.cu:50-60)
+cudaError_t launch_particle_vel_init(const double* pos, int num, const double* psi0, const Grid& gp, double* vel,
+                                     cudaStream_t s);
 // U(0,1) -> frame and wrap (k_rescale, cmm-particles.cu:30-46)
 cudaError_t launch_particle_rescale(double* pos, int num, const double* p4, const Grid& g, cudaStream_t s);
 // circle / uniform grid / sine-sheet layouts (mode 2, 3, 4)

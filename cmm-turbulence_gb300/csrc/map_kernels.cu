@@ -56,35 +56,87 @@ void map_update_coefficients(int order_num, double ep, double coef[4][kMaxFoot],
 
 // ---------------------------------------------------------------------------
 // backward characteristic integrators on the Hermite stream function
-// (src/numerical/cmm-timestep.cu:35-45 euler_exp_b, :66-81 RK2_heun_b,
-//  :175-207 RK3_classical_b).  u = (psi_y, -psi_x).
+// (src/numerical/cmm-timestep.cu: :35-45 euler_exp_b, :66-81 RK2_heun_b,
+//  :112-135 adam_bashford_2_pc_b, :175-207 RK3_classical_b, :260-307 RK4_classical_b,
+//  :348-374 RK3_optimized_b, :428-466 RK4_optimized_b).  u = (psi_y, -psi_x); psi level 0
+// is t_n, level 1 t_{n-1}; L1 / L12 extrapolate the levels to t_{n+1} / t_{n+1/2}.
 // ---------------------------------------------------------------------------
-template <int L, int TI>
-__device__ __forceinline__ void integrate_back(const AdvectArgs& a, double x, double y, double& xo, double& yo)
+template <int L>
+__device__ __forceinline__ void vel_comb(const AdvectArgs& a, const double* c, double x, double y, double& kx, double& ky)
 {
     double ux[L], uy[L];
     velocity_levels<L>(a.psi, a.gp, x, y, ux, uy);
-    double k1x = a.L1[0] * ux[0], k1y = a.L1[0] * uy[0];
+    kx = c[0] * ux[0];
+    ky = c[0] * uy[0];
 #pragma unroll
-    for (int l = 1; l < L; ++l) { k1x = fma(a.L1[l], ux[l], k1x); k1y = fma(a.L1[l], uy[l], k1y); }
+    for (int l = 1; l < L; ++l) { kx = fma(c[l], ux[l], kx); ky = fma(c[l], uy[l], ky); }
+}
+
+__device__ __forceinline__ void vel_level(const AdvectArgs& a, int l, double x, double y, double& ux, double& uy)
+{
+    const double* lv[1] = {a.psi[l]};
+    double u1[1], v1[1];
+    velocity_levels<1>(lv, a.gp, x, y, u1, v1);
+    ux = u1[0];
+    uy = v1[0];
+}
+
+template <int L, int TI>
+__device__ __forceinline__ void integrate_back(const AdvectArgs& a, double x, double y, double& xo, double& yo)
+{
     const double dt = a.dt;
+    if (TI == 20) {
+        // second-order Adams-Bashforth, ten fixed-point sweeps on levels 0 and 1
+        double px = x, py = y, ox = x, oy = y, u2x, u2y, ux, uy;
+        for (int it = 0; it < 10; ++it) {
+            vel_level(a, 1, px, py, u2x, u2y);
+            px = ox - dt * u2x;
+            py = oy - dt * u2y;
+            vel_level(a, 1, px, py, u2x, u2y);
+            vel_level(a, 0, ox, oy, ux, uy);
+            ox = x - dt * (1.5 * ux - 0.5 * u2x);
+            oy = y - dt * (1.5 * uy - 0.5 * u2y);
+        }
+        xo = ox;
+        yo = oy;
+        return;
+    }
+    double k1x, k1y;
+    vel_comb<L>(a, a.L1, x, y, k1x, k1y);
     if (TI == 10) {
         xo = x - dt * k1x;
         yo = y - dt * k1y;
     } else if (TI == 21) {
-        double u2x[1], u2y[1];
-        velocity_levels<1>(a.psi, a.gp, x - dt * k1x, y - dt * k1y, u2x, u2y);
-        xo = x - dt * (k1x + u2x[0]) / 2;
-        yo = y - dt * (k1y + u2y[0]) / 2;
-    } else {  // 30: RK3
-        velocity_levels<L>(a.psi, a.gp, x - dt * k1x / 2.0, y - dt * k1y / 2.0, ux, uy);
-        double k2x = a.L12[0] * ux[0], k2y = a.L12[0] * uy[0];
-#pragma unroll
-        for (int l = 1; l < L; ++l) { k2x = fma(a.L12[l], ux[l], k2x); k2y = fma(a.L12[l], uy[l], k2y); }
-        double u3x[1], u3y[1];
-        velocity_levels<1>(a.psi, a.gp, x + dt * k1x - 2 * dt * k2x, y + dt * k1y - 2 * dt * k2y, u3x, u3y);
-        xo = x - dt * (k1x + 4 * k2x + u3x[0]) / 6.0;
-        yo = y - dt * (k1y + 4 * k2y + u3y[0]) / 6.0;
+        double k2x, k2y;
+        vel_level(a, 0, x - dt * k1x, y - dt * k1y, k2x, k2y);
+        xo = x - dt * (k1x + k2x) / 2;
+        yo = y - dt * (k1y + k2y) / 2;
+    } else if (TI == 30) {
+        double k2x, k2y, k3x, k3y;
+        vel_comb<L>(a, a.L12, x - dt * k1x / 2.0, y - dt * k1y / 2.0, k2x, k2y);
+        vel_level(a, 0, x + dt * k1x - 2 * dt * k2x, y + dt * k1y - 2 * dt * k2y, k3x, k3y);
+        xo = x - dt * (k1x + 4 * k2x + k3x) / 6.0;
+        yo = y - dt * (k1y + 4 * k2y + k3y) / 6.0;
+    } else if (TI == 40) {
+        double k2x, k2y, k3x, k3y, k4x, k4y;
+        vel_comb<L>(a, a.L12, x - dt * k1x / 2.0, y - dt * k1y / 2.0, k2x, k2y);
+        vel_comb<L>(a, a.L12, x - dt * k2x / 2.0, y - dt * k2y / 2.0, k3x, k3y);
+        vel_level(a, 0, x - dt * k3x, y - dt * k3y, k4x, k4y);
+        xo = x - dt * (k1x + 2 * k2x + 2 * k3x + k4x) / 6.0;
+        yo = y - dt * (k1y + 2 * k2y + 2 * k3y + k4y) / 6.0;
+    } else if (TI == 31) {
+        double k2x, k2y, k3x, k3y;
+        vel_level(a, 0, x - dt * k1x, y - dt * k1y, k2x, k2y);
+        vel_level(a, 1, x + 2 * dt * (-2 * k1x + k2x), y + 2 * dt * (-2 * k1y + k2y), k3x, k3y);
+        xo = x - dt * (5 * k1x + 8 * k2x - k3x) / 12.0;
+        yo = y - dt * (5 * k1y + 8 * k2y - k3y) / 12.0;
+    } else {   // 41
+        double k2x, k2y, k3x, k3y, k4x, k4y;
+        vel_level(a, 0, x - dt * k1x, y - dt * k1y, k2x, k2y);
+        vel_comb<L>(a, a.L12, x - dt * (3 * k1x + k2x) / 8.0, y - dt * (3 * k1y + k2y) / 8.0, k3x, k3y);
+        vel_level(a, 0, x + dt * (k2x - 4 * k3x) / 3.0, y + dt * (k2y - 4 * k3y) / 3.0, k4x, k4y);
+        xo = x - dt * (2 * k1x - k2x + 8 * k3x + 3 * k4x) / 12.0;
+        yo = y - dt * (2 * k1y - k2y + 8 * k3y + 3 * k4y) / 12.0;
     }
 }
 
@@ -152,6 +204,13 @@ cudaError_t launch_advect(const AdvectArgs& a, cudaStream_t s)
         case 302: CMM_ADV(2, 30); break;
         case 303: CMM_ADV(3, 30); break;
         case 304: CMM_ADV(4, 30); break;
+        case 202: CMM_ADV(2, 20); break;
+        case 203: CMM_ADV(3, 20); break;
+        case 204: CMM_ADV(4, 20); break;
+        case 404: CMM_ADV(4, 40); break;
+        case 313: CMM_ADV(3, 31); break;
+        case 314: CMM_ADV(4, 31); break;
+        case 414: CMM_ADV(4, 41); break;
         default: return cudaErrorInvalidValue;
     }
 #undef CMM_ADV

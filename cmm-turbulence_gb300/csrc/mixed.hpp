@@ -17,6 +17,7 @@ struct AdvectMArgs {
     const float4* psiA;     // k1 field: sum_l L1[l] psi_l
     const float4* psiB;     // k2 field of RK3: sum_l L12[l] psi_l
     const float4* psi0;     // newest level
+    const float4* psi1;     // level 1 (Adams-Bashforth 2, RK3Mod)
     // separable stream function (Vlasov-Poisson): FP64 1D tables (f(i+1) - f(i), f'(i)) of
     // the x-part of each combination and of h(v); tv != nullptr selects them (and FP64
     // characteristics, coef64 / dt64 / ep64) over the nodes
@@ -28,7 +29,7 @@ struct AdvectMArgs {
     double dt64, ep64;
     float coef[4][kMaxFoot];
     float dt, ep;
-    int time_integration_num;   // 10, 21, 30
+    int time_integration_num;   // 10, 21, 20, 30, 40, 31, 41
     int nfoot;
     int rp;                     // psi cells per map cell (Npsi / Nmap, integer)
 };
@@ -62,10 +63,17 @@ cudaError_t launch_sample_m(const Grid& gm, const Grid& go, const Grid& gf, cons
                             float* out_f, double* out_d, cudaStream_t s);
 // tracers at 64-bit fixed-point positions P = (x - b0) / W * 2^64 (interleaved x, y)
 // (tA, tB, t0, tv: separable tables as in AdvectMArgs, used when tv != nullptr)
+// psiA = level t_n, psiB = the t_{n+1/2} combination, psi0 = t_{n+1}, psiC = t_{n-1} (RK3Mod);
+// tau != 0: inertial particles with FP32 velocity state vel; tv != nullptr: separable psi tables
 cudaError_t launch_particles_m(const Grid& gp, unsigned long long* pos, int num, const float4* psiA,
                                const float4* psiB, const float4* psi0, double dt, int ti, cudaStream_t s,
                                const double2* tA = nullptr, const double2* tB = nullptr,
-                               const double2* t0 = nullptr, const double2* tv = nullptr);
+                               const double2* t0 = nullptr, const double2* tv = nullptr,
+                               const float4* psiC = nullptr, float2* vel = nullptr, double tau = 0.0);
+cudaError_t launch_particle_vel_init_m(const Grid& gp, const unsigned long long* pos, int num, const float4* psi0,
+                                       float2* vel, cudaStream_t s);
+cudaError_t launch_vel_to_f64(const float2* v, int num, double* out, cudaStream_t s);
+cudaError_t launch_vel_from_f64(const double* v, int num, float2* out, cudaStream_t s);
 cudaError_t launch_pos_to_fix(const double* pos, int num, const Grid& g, unsigned long long* out, cudaStream_t s);
 cudaError_t launch_fix_to_pos(const unsigned long long* in, int num, const Grid& g, double* pos, cudaStream_t s);
 cudaError_t launch_spec_psi_f(const float2* Fv, const Grid& gv, const Grid& gp, double freq, float2* out4,

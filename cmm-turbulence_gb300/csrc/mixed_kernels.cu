@@ -303,13 +303,54 @@ __global__ void __launch_bounds__(256) k_advect_m(const AdvectMArgs a, int lpn_l
             velocity_f(a.psi0, a.gp, locate_rel(a.gp, bx, by, ex - dt * k1x, ey - dt * k1y), k2x, k2y);
             Dx = dt * (k1x + k2x) * 0.5f;
             Dy = dt * (k1y + k2y) * 0.5f;
-        } else {
+        } else if (TI == 30) {
             float k2x, k2y, k3x, k3y;
             velocity_f(a.psiB, a.gp, locate_rel(a.gp, bx, by, ex - 0.5f * dt * k1x, ey - 0.5f * dt * k1y), k2x, k2y);
             velocity_f(a.psi0, a.gp,
                        locate_rel(a.gp, bx, by, ex + dt * k1x - 2.0f * dt * k2x, ey + dt * k1y - 2.0f * dt * k2y), k3x, k3y);
             Dx = dt * (k1x + 4.0f * k2x + k3x) * (1.0f / 6.0f);
             Dy = dt * (k1y + 4.0f * k2y + k3y) * (1.0f / 6.0f);
+        } else if (TI == 20) {
+            // Adams-Bashforth 2, ten fixed-point sweeps on levels 0 and 1 (adam_bashford_2_pc_b)
+            float px = ex, py = ey, ox = ex, oy = ey, u2x, u2y, ux, uy;
+            for (int it = 0; it < 10; ++it) {
+                velocity_f(a.psi1, a.gp, locate_rel(a.gp, bx, by, px, py), u2x, u2y);
+                px = ox - dt * u2x;
+                py = oy - dt * u2y;
+                velocity_f(a.psi1, a.gp, locate_rel(a.gp, bx, by, px, py), u2x, u2y);
+                velocity_f(a.psi0, a.gp, locate_rel(a.gp, bx, by, ox, oy), ux, uy);
+                ox = ex - dt * (1.5f * ux - 0.5f * u2x);
+                oy = ey - dt * (1.5f * uy - 0.5f * u2y);
+            }
+            Dx = ex - ox;
+            Dy = ey - oy;
+        } else if (TI == 40) {
+            float k2x, k2y, k3x, k3y, k4x, k4y;
+            velocity_f(a.psiB, a.gp, locate_rel(a.gp, bx, by, ex - 0.5f * dt * k1x, ey - 0.5f * dt * k1y), k2x, k2y);
+            velocity_f(a.psiB, a.gp, locate_rel(a.gp, bx, by, ex - 0.5f * dt * k2x, ey - 0.5f * dt * k2y), k3x, k3y);
+            velocity_f(a.psi0, a.gp, locate_rel(a.gp, bx, by, ex - dt * k3x, ey - dt * k3y), k4x, k4y);
+            Dx = dt * (k1x + 2.0f * k2x + 2.0f * k3x + k4x) * (1.0f / 6.0f);
+            Dy = dt * (k1y + 2.0f * k2y + 2.0f * k3y + k4y) * (1.0f / 6.0f);
+        } else if (TI == 31) {
+            float k2x, k2y, k3x, k3y;
+            velocity_f(a.psi0, a.gp, locate_rel(a.gp, bx, by, ex - dt * k1x, ey - dt * k1y), k2x, k2y);
+            velocity_f(a.psi1, a.gp,
+                       locate_rel(a.gp, bx, by, ex + 2.0f * dt * fmaf(-2.0f, k1x, k2x), ey + 2.0f * dt * fmaf(-2.0f, k1y, k2y)),
+                       k3x, k3y);
+            Dx = dt * (5.0f * k1x + 8.0f * k2x - k3x) * (1.0f / 12.0f);
+            Dy = dt * (5.0f * k1y + 8.0f * k2y - k3y) * (1.0f / 12.0f);
+        } else {   // 41
+            float k2x, k2y, k3x, k3y, k4x, k4y;
+            velocity_f(a.psi0, a.gp, locate_rel(a.gp, bx, by, ex - dt * k1x, ey - dt * k1y), k2x, k2y);
+            velocity_f(a.psiB, a.gp,
+                       locate_rel(a.gp, bx, by, ex - 0.125f * dt * fmaf(3.0f, k1x, k2x), ey - 0.125f * dt * fmaf(3.0f, k1y, k2y)),
+                       k3x, k3y);
+            velocity_f(a.psi0, a.gp,
+                       locate_rel(a.gp, bx, by, ex + dt * (1.0f / 3.0f) * fmaf(-4.0f, k3x, k2x),
+                                  ey + dt * (1.0f / 3.0f) * fmaf(-4.0f, k3y, k2y)),
+                       k4x, k4y);
+            Dx = dt * (2.0f * k1x - k2x + 8.0f * k3x + 3.0f * k4x) * (1.0f / 12.0f);
+            Dy = dt * (2.0f * k1y - k2y + 8.0f * k3y + 3.0f * k4y) * (1.0f / 12.0f);
         }
         float fx = ex - Dx, fy = ey - Dy;
         float mx, my;
@@ -468,6 +509,10 @@ cudaError_t launch_advect_m(const AdvectMArgs& a, cudaStream_t s)
         case 10: k_advect_m<10><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
         case 21: k_advect_m<21><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
         case 30: k_advect_m<30><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
+        case 20: k_advect_m<20><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
+        case 40: k_advect_m<40><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
+        case 31: k_advect_m<31><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
+        case 41: k_advect_m<41><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -846,49 +891,184 @@ cudaError_t launch_sample_m(const Grid& gm, const Grid& go, const Grid& gf, cons
 }
 
 // ---------------------------------------------------------------------------
-// tracers at 64-bit fixed-point positions (see fix_increment): the stage
-// positions are FP32 offsets from the start cell, velocities are FP32
-// (psiA = level 1 = t_n, psiB = Lagrange t_{n+1/2} combination, psi0 =
-// t_{n+1}); stages as Particle_advect (src/numerical/cmm-particles.cu:159-183).
+// particles at 64-bit fixed-point positions (see fix_increment): the stage
+// positions are FP32 offsets from the start cell, velocities are FP32.  Levels:
+// l1 = t_n, l0 = t_{n+1}, l2 = t_{n-1}, half = the Lagrange t_{n+1/2} combination;
+// stages as Particle_advect / Particle_advect_inertia
+// (src/numerical/cmm-particles.cu:119-276, 280-551).
 // ---------------------------------------------------------------------------
 struct SepTables { const double2* tA; const double2* tB; const double2* t0; const double2* tv; };
 
-template <int TI>
-__global__ void __launch_bounds__(256) k_particles_m(Grid gp, ulonglong2* __restrict__ pos, int num,
-                                                     const float4* __restrict__ psiA, const float4* __restrict__ psiB,
-                                                     const float4* __restrict__ psi0, float dt, float2 scx, float2 scy)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= num) return;
-    ulonglong2 P = pos[i];
+struct PartM {
+    Grid gp;
+    ulonglong2* pos;
+    float2* vel;           // inertial velocity state
+    int num;
+    const float4* l1;
+    const float4* l0;
+    const float4* l2;
+    const float4* half;
+    float dt, tau;
+    float2 scx, scy;
+};
+
+enum { kLvN = 1, kLvN1 = 0, kLvNm1 = 2, kLvHalf = 3 };
+
+struct StageVel {
+    const PartM& a;
     int bx, by;
     float tx, ty;
-    fix_cell(P.x, gp.NX, bx, tx);
-    fix_cell(P.y, gp.NY, by, ty);
-    float k1x, k1y, Dx, Dy;
-    velocity_f(psiA, gp, locate_q(gp, bx, by, tx, ty), k1x, k1y);
+    // velocity of level `which` at the start position displaced by (dx, dy)
+    __device__ __forceinline__ void operator()(int which, float dx, float dy, float& ux, float& uy) const
+    {
+        const float4* f = which == kLvN ? a.l1 : which == kLvN1 ? a.l0 : which == kLvNm1 ? a.l2 : a.half;
+        velocity_f(f, a.gp, locate_q(a.gp, bx, by, fmaf(dx, a.gp.ihxf, tx), fmaf(dy, a.gp.ihyf, ty)), ux, uy);
+    }
+};
+
+template <int TI>
+__device__ __forceinline__ void tracer_step_m(const StageVel& V, float dt, float& Dx, float& Dy)
+{
+    float k1x, k1y, k2x, k2y, k3x, k3y, k4x, k4y;
+    V(kLvN, 0.0f, 0.0f, k1x, k1y);
     if (TI == 10) {
         Dx = dt * k1x;
         Dy = dt * k1y;
     } else if (TI == 20) {
-        float k2x, k2y;
-        velocity_f(psi0, gp, locate_q(gp, bx, by, fmaf(dt * k1x, gp.ihxf, tx), fmaf(dt * k1y, gp.ihyf, ty)), k2x, k2y);
+        V(kLvN1, dt * k1x, dt * k1y, k2x, k2y);
         Dx = dt * (k1x + k2x) * 0.5f;
         Dy = dt * (k1y + k2y) * 0.5f;
-    } else {
-        float k2x, k2y, k3x, k3y;
-        velocity_f(psiB, gp, locate_q(gp, bx, by, fmaf(0.5f * dt * k1x, gp.ihxf, tx), fmaf(0.5f * dt * k1y, gp.ihyf, ty)),
-                   k2x, k2y);
-        velocity_f(psi0, gp,
-                   locate_q(gp, bx, by, fmaf(dt * fmaf(2.0f, k2x, -k1x), gp.ihxf, tx),
-                            fmaf(dt * fmaf(2.0f, k2y, -k1y), gp.ihyf, ty)),
-                   k3x, k3y);
+    } else if (TI == 30) {
+        V(kLvHalf, 0.5f * dt * k1x, 0.5f * dt * k1y, k2x, k2y);
+        V(kLvN1, dt * fmaf(2.0f, k2x, -k1x), dt * fmaf(2.0f, k2y, -k1y), k3x, k3y);
         Dx = dt * (k1x + 4.0f * k2x + k3x) * (1.0f / 6.0f);
         Dy = dt * (k1y + 4.0f * k2y + k3y) * (1.0f / 6.0f);
+    } else if (TI == 40) {
+        V(kLvHalf, 0.5f * dt * k1x, 0.5f * dt * k1y, k2x, k2y);
+        V(kLvHalf, 0.5f * dt * k2x, 0.5f * dt * k2y, k3x, k3y);
+        V(kLvN1, dt * k3x, dt * k3y, k4x, k4y);
+        Dx = dt * (k1x + 2.0f * k2x + 2.0f * k3x + k4x) * (1.0f / 6.0f);
+        Dy = dt * (k1y + 2.0f * k2y + 2.0f * k3y + k4y) * (1.0f / 6.0f);
+    } else if (TI == 31) {
+        V(kLvN1, dt * k1x, dt * k1y, k2x, k2y);
+        V(kLvNm1, dt * fmaf(-2.0f, k2x, k1x), dt * fmaf(-2.0f, k2y, k1y), k3x, k3y);
+        Dx = dt * (8.0f * k1x + 5.0f * k2x - k3x) * (1.0f / 12.0f);
+        Dy = dt * (8.0f * k1y + 5.0f * k2y - k3y) * (1.0f / 12.0f);
+    } else {   // 41
+        V(kLvN1, dt * k1x, dt * k1y, k2x, k2y);
+        V(kLvHalf, dt * 0.125f * fmaf(3.0f, k1x, k2x), dt * 0.125f * fmaf(3.0f, k1y, k2y), k3x, k3y);
+        V(kLvN1, dt * (1.0f / 3.0f) * fmaf(4.0f, k3x, -k2x), dt * (1.0f / 3.0f) * fmaf(4.0f, k3y, -k2y), k4x, k4y);
+        Dx = dt * (2.0f * k1x - k2x + 8.0f * k3x + 3.0f * k4x) * (1.0f / 12.0f);
+        Dy = dt * (2.0f * k1y - k2y + 8.0f * k3y + 3.0f * k4y) * (1.0f / 12.0f);
     }
-    P.x += fix_increment(Dx, scx);
-    P.y += fix_increment(Dy, scy);
-    pos[i] = P;
+}
+
+// inertial: stage s has a position rate xs (a velocity) and an acceleration
+// as = -(xs - u) / tau; D is the position change, dv the velocity change
+template <int TI>
+__device__ __forceinline__ void inertial_step_m(const StageVel& V, float dt, float tau, float vx, float vy, float& Dx,
+                                                float& Dy, float& dvx, float& dvy)
+{
+    const float it = 1.0f / tau;
+    float ux, uy;
+    V(kLvN, 0.0f, 0.0f, ux, uy);
+    const float a1x = (ux - vx) * it, a1y = (uy - vy) * it;
+    if (TI == 10) {
+        Dx = dt * vx; Dy = dt * vy;
+        dvx = dt * a1x; dvy = dt * a1y;
+    } else if (TI == 20) {
+        const float x2x = fmaf(dt, a1x, vx), x2y = fmaf(dt, a1y, vy);
+        V(kLvN1, dt * vx, dt * vy, ux, uy);
+        const float a2x = (ux - x2x) * it, a2y = (uy - x2y) * it;
+        Dx = 0.5f * dt * (vx + x2x); Dy = 0.5f * dt * (vy + x2y);
+        dvx = 0.5f * dt * (a1x + a2x); dvy = 0.5f * dt * (a1y + a2y);
+    } else if (TI == 30) {
+        const float x2x = fmaf(0.5f * dt, a1x, vx), x2y = fmaf(0.5f * dt, a1y, vy);
+        V(kLvHalf, 0.5f * dt * vx, 0.5f * dt * vy, ux, uy);
+        const float a2x = (ux - x2x) * it, a2y = (uy - x2y) * it;
+        const float x3x = fmaf(dt, fmaf(2.0f, a2x, -a1x), vx), x3y = fmaf(dt, fmaf(2.0f, a2y, -a1y), vy);
+        V(kLvN1, dt * fmaf(2.0f, x2x, -vx), dt * fmaf(2.0f, x2y, -vy), ux, uy);
+        const float a3x = (ux - x3x) * it, a3y = (uy - x3y) * it;
+        Dx = dt * (1.0f / 6.0f) * (vx + 4.0f * x2x + x3x); Dy = dt * (1.0f / 6.0f) * (vy + 4.0f * x2y + x3y);
+        dvx = dt * (1.0f / 6.0f) * (a1x + 4.0f * a2x + a3x); dvy = dt * (1.0f / 6.0f) * (a1y + 4.0f * a2y + a3y);
+    } else if (TI == 40) {
+        const float x2x = fmaf(0.5f * dt, a1x, vx), x2y = fmaf(0.5f * dt, a1y, vy);
+        V(kLvHalf, 0.5f * dt * vx, 0.5f * dt * vy, ux, uy);
+        const float a2x = (ux - x2x) * it, a2y = (uy - x2y) * it;
+        const float x3x = fmaf(0.5f * dt, a2x, vx), x3y = fmaf(0.5f * dt, a2y, vy);
+        V(kLvHalf, 0.5f * dt * x2x, 0.5f * dt * x2y, ux, uy);
+        const float a3x = (ux - x3x) * it, a3y = (uy - x3y) * it;
+        const float x4x = fmaf(dt, a3x, vx), x4y = fmaf(dt, a3y, vy);
+        V(kLvN1, dt * x3x, dt * x3y, ux, uy);
+        const float a4x = (ux - x4x) * it, a4y = (uy - x4y) * it;
+        Dx = dt * (1.0f / 6.0f) * (vx + 2.0f * x2x + 2.0f * x3x + x4x);
+        Dy = dt * (1.0f / 6.0f) * (vy + 2.0f * x2y + 2.0f * x3y + x4y);
+        dvx = dt * (1.0f / 6.0f) * (a1x + 2.0f * a2x + 2.0f * a3x + a4x);
+        dvy = dt * (1.0f / 6.0f) * (a1y + 2.0f * a2y + 2.0f * a3y + a4y);
+    } else if (TI == 31) {
+        const float x2x = fmaf(dt, a1x, vx), x2y = fmaf(dt, a1y, vy);
+        V(kLvN1, dt * vx, dt * vy, ux, uy);
+        const float a2x = (ux - x2x) * it, a2y = (uy - x2y) * it;
+        const float x3x = fmaf(dt, fmaf(-2.0f, a2x, a1x), vx), x3y = fmaf(dt, fmaf(-2.0f, a2y, a1y), vy);
+        V(kLvNm1, dt * fmaf(-2.0f, x2x, vx), dt * fmaf(-2.0f, x2y, vy), ux, uy);
+        const float a3x = (ux - x3x) * it, a3y = (uy - x3y) * it;
+        Dx = dt * (1.0f / 12.0f) * (8.0f * vx + 5.0f * x2x - x3x);
+        Dy = dt * (1.0f / 12.0f) * (8.0f * vy + 5.0f * x2y - x3y);
+        dvx = dt * (1.0f / 12.0f) * (8.0f * a1x + 5.0f * a2x - a3x);
+        dvy = dt * (1.0f / 12.0f) * (8.0f * a1y + 5.0f * a2y - a3y);
+    } else {   // 41
+        const float x2x = fmaf(dt, a1x, vx), x2y = fmaf(dt, a1y, vy);
+        V(kLvN1, dt * vx, dt * vy, ux, uy);
+        const float a2x = (ux - x2x) * it, a2y = (uy - x2y) * it;
+        const float x3x = fmaf(0.125f * dt, fmaf(3.0f, a1x, a2x), vx), x3y = fmaf(0.125f * dt, fmaf(3.0f, a1y, a2y), vy);
+        V(kLvHalf, 0.125f * dt * fmaf(3.0f, vx, x2x), 0.125f * dt * fmaf(3.0f, vy, x2y), ux, uy);
+        const float a3x = (ux - x3x) * it, a3y = (uy - x3y) * it;
+        const float x4x = fmaf(dt * (1.0f / 3.0f), fmaf(4.0f, a3x, -a2x), vx);
+        const float x4y = fmaf(dt * (1.0f / 3.0f), fmaf(4.0f, a3y, -a2y), vy);
+        V(kLvN1, dt * (1.0f / 3.0f) * fmaf(4.0f, x3x, -x2x), dt * (1.0f / 3.0f) * fmaf(4.0f, x3y, -x2y), ux, uy);
+        const float a4x = (ux - x4x) * it, a4y = (uy - x4y) * it;
+        Dx = dt * (1.0f / 12.0f) * (2.0f * vx - x2x + 8.0f * x3x + 3.0f * x4x);
+        Dy = dt * (1.0f / 12.0f) * (2.0f * vy - x2y + 8.0f * x3y + 3.0f * x4y);
+        dvx = dt * (1.0f / 12.0f) * (2.0f * a1x - a2x + 8.0f * a3x + 3.0f * a4x);
+        dvy = dt * (1.0f / 12.0f) * (2.0f * a1y - a2y + 8.0f * a3y + 3.0f * a4y);
+    }
+}
+
+template <int TI, bool INERT>
+__global__ void __launch_bounds__(256) k_particles_m(const PartM a)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.num) return;
+    ulonglong2 P = a.pos[i];
+    StageVel V{a, 0, 0, 0.0f, 0.0f};
+    fix_cell(P.x, a.gp.NX, V.bx, V.tx);
+    fix_cell(P.y, a.gp.NY, V.by, V.ty);
+    float Dx, Dy;
+    if (INERT) {
+        float2 v = a.vel[i];
+        float dvx, dvy;
+        inertial_step_m<TI>(V, a.dt, a.tau, v.x, v.y, Dx, Dy, dvx, dvy);
+        a.vel[i] = make_float2(v.x + dvx, v.y + dvy);
+    } else {
+        tracer_step_m<TI>(V, a.dt, Dx, Dy);
+    }
+    P.x += fix_increment(Dx, a.scx);
+    P.y += fix_increment(Dy, a.scy);
+    a.pos[i] = P;
+}
+
+// v = u of a level at the particles (Particle_advect_inertia_init, cmm-particles.cu:50-60)
+__global__ void k_particle_vel_init_m(const PartM a)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.num) return;
+    ulonglong2 P = a.pos[i];
+    StageVel V{a, 0, 0, 0.0f, 0.0f};
+    fix_cell(P.x, a.gp.NX, V.bx, V.tx);
+    fix_cell(P.y, a.gp.NY, V.by, V.ty);
+    float ux, uy;
+    V(kLvN1, 0.0f, 0.0f, ux, uy);
+    a.vel[i] = make_float2(ux, uy);
 }
 
 // tracers in a separable stream function: FP64 stages from the 1D tables
@@ -929,13 +1109,15 @@ __global__ void __launch_bounds__(256) k_particles_sep(Grid gp, ulonglong2* __re
 
 cudaError_t launch_particles_m(const Grid& gp, unsigned long long* pos, int num, const float4* psiA,
                                const float4* psiB, const float4* psi0, double dt, int ti, cudaStream_t s,
-                               const double2* tA, const double2* tB, const double2* t0, const double2* tv)
+                               const double2* tA, const double2* tB, const double2* t0, const double2* tv,
+                               const float4* psiC, float2* vel, double tau)
 {
     if (num <= 0) return cudaSuccess;
     unsigned blocks = (unsigned)((num + 255) / 256);
     ulonglong2* P = reinterpret_cast<ulonglong2*>(pos);
     float2 sx = fix_scale(gp.Wx), sy = fix_scale(gp.Wy);
     if (tv) {
+        if (tau != 0) return cudaErrorInvalidValue;
         SepTables tb{tA, tB, t0, tv};
         if (ti == 10) k_particles_sep<10><<<blocks, 256, 0, s>>>(gp, P, num, tb, dt, sx, sy);
         else if (ti == 20) k_particles_sep<20><<<blocks, 256, 0, s>>>(gp, P, num, tb, dt, sx, sy);
@@ -943,11 +1125,57 @@ cudaError_t launch_particles_m(const Grid& gp, unsigned long long* pos, int num,
         else return cudaErrorInvalidValue;
         return cudaGetLastError();
     }
-    float d = (float)dt;
-    if (ti == 10) k_particles_m<10><<<blocks, 256, 0, s>>>(gp, P, num, psiA, psiB, psi0, d, sx, sy);
-    else if (ti == 20) k_particles_m<20><<<blocks, 256, 0, s>>>(gp, P, num, psiA, psiB, psi0, d, sx, sy);
-    else if (ti == 30) k_particles_m<30><<<blocks, 256, 0, s>>>(gp, P, num, psiA, psiB, psi0, d, sx, sy);
-    else return cudaErrorInvalidValue;
+    const bool inert = tau != 0;
+    if ((inert && !vel) || (ti == 31 && !psiC)) return cudaErrorInvalidValue;
+    PartM a{gp, P, vel, num, psiA, psi0, psiC, psiB, (float)dt, (float)tau, sx, sy};
+#define CMM_PM(TT)                                                         \
+    do {                                                                   \
+        if (inert) k_particles_m<TT, true><<<blocks, 256, 0, s>>>(a);      \
+        else k_particles_m<TT, false><<<blocks, 256, 0, s>>>(a);           \
+    } while (0)
+    switch (ti) {
+        case 10: CMM_PM(10); break;
+        case 20: CMM_PM(20); break;
+        case 30: CMM_PM(30); break;
+        case 40: CMM_PM(40); break;
+        case 31: CMM_PM(31); break;
+        case 41: CMM_PM(41); break;
+        default: return cudaErrorInvalidValue;
+    }
+#undef CMM_PM
+    return cudaGetLastError();
+}
+
+cudaError_t launch_particle_vel_init_m(const Grid& gp, const unsigned long long* pos, int num, const float4* psi0,
+                                       float2* vel, cudaStream_t s)
+{
+    if (num <= 0) return cudaSuccess;
+    PartM a{gp, reinterpret_cast<ulonglong2*>(const_cast<unsigned long long*>(pos)), vel, num, nullptr, psi0,
+            nullptr, nullptr, 0.0f, 0.0f, make_float2(0, 0), make_float2(0, 0)};
+    k_particle_vel_init_m<<<(unsigned)((num + 255) / 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+__global__ void k_vel_convert(const float2* __restrict__ vf, double* __restrict__ vd, const double* __restrict__ vin,
+                              float2* __restrict__ vout, int num)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= num) return;
+    if (vf) { float2 v = vf[i]; vd[2 * i] = v.x; vd[2 * i + 1] = v.y; }
+    else vout[i] = make_float2((float)vin[2 * i], (float)vin[2 * i + 1]);
+}
+
+cudaError_t launch_vel_to_f64(const float2* v, int num, double* out, cudaStream_t s)
+{
+    if (num <= 0) return cudaSuccess;
+    k_vel_convert<<<(num + 255) / 256, 256, 0, s>>>(v, out, nullptr, nullptr, num);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vel_from_f64(const double* v, int num, float2* out, cudaStream_t s)
+{
+    if (num <= 0) return cudaSuccess;
+    k_vel_convert<<<(num + 255) / 256, 256, 0, s>>>(nullptr, nullptr, v, out, num);
     return cudaGetLastError();
 }
 

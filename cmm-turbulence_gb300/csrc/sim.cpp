@@ -143,9 +143,19 @@ int EulerSim::alloc()
         err = "initial condition turbulence_gaussienne is not built (needs device cuRAND sequences)";
         return kErrUnsupported;
     }
-    if (s.time_integration_num != 10 && s.time_integration_num != 21 && s.time_integration_num != 30) {
-        err = "map time integration " + s.time_integration + " is not built (EulerExp, RK2/Heun, RK3 are)";
-        return kErrUnsupported;
+    auto levels_needed = [](int ti) {
+        // Lagrange levels a scheme reads (settings.cu time-integration table)
+        switch (ti) {
+            case 10: return 1;
+            case 20: case 21: return 2;
+            case 30: case 31: return 3;
+            case 40: case 41: return 4;
+            default: return -1;
+        }
+    };
+    if (levels_needed(s.time_integration_num) < 0) {
+        err = "unknown map time integration " + s.time_integration;
+        return kErrParam;
     }
     if (s.map_update_order_num < 0) { err = "unknown map_update_order " + s.map_update_order; return kErrParam; }
     if (s.forward_map) { err = "forward_map is not built"; return kErrUnsupported; }
@@ -154,7 +164,22 @@ int EulerSim::alloc()
     dt = s.dt();
     L = s.effective_lagrange_order();
     if (L < 1 || L > kMaxLagrange) { err = "lagrange order out of range"; return kErrParam; }
-    if (L < 3 && s.time_integration_num == 30) { err = "RK3 needs lagrange order >= 3"; return kErrParam; }
+    if (L < levels_needed(s.time_integration_num)) {
+        err = "map time integration " + s.time_integration + " needs lagrange order >= " +
+              std::to_string(levels_needed(s.time_integration_num));
+        return kErrParam;
+    }
+    for (auto& p : s.particles_advected) {
+        int need = p.time_integration_num == 20 ? 2 : levels_needed(p.time_integration_num);
+        if (need < 0 || p.time_integration_num == 21) {
+            err = "unknown particle time integration " + p.time_integration;
+            return kErrParam;
+        }
+        if (L < need) {
+            err = "particle time integration " + p.time_integration + " needs lagrange order >= " + std::to_string(need);
+            return kErrParam;
+        }
+    }
     s.lagrange_order = L;
     s.file_name = s.derived_file_name();
     max_maps = s.cpu_map_num();
@@ -164,6 +189,17 @@ int EulerSim::alloc()
                       s.grid_fine % s.grid_vort == 0 && s.grid_fine % s.grid_coarse == 0;
         if (!ratios) { err = "precision=mixed needs psi, vort and fine grids that are integer multiples of the map grid"; return kErrUnsupported; }
         if (s.molly_stencil != 0) { err = "precision=mixed does not build mollified sampling"; return kErrUnsupported; }
+        if (vlasov_) {
+            // the separable-psi kernels of the mixed Vlasov form carry EulerExp, Heun and RK3
+            bool ok = s.time_integration_num == 10 || s.time_integration_num == 21 || s.time_integration_num == 30;
+            for (auto& p : s.particles_advected)
+                ok = ok && p.tau == 0 && (p.time_integration_num == 10 || p.time_integration_num == 20 ||
+                                          p.time_integration_num == 30);
+            if (!ok) {
+                err = "precision=mixed for Vlasov-Poisson builds EulerExp, Heun and RK3 maps and fluid tracers only";
+                return kErrUnsupported;
+            }
+        }
         mixed_ = true;
     } else if (s.precision != "fp64") {
         err = "precision must be fp64 or mixed";
@@ -213,6 +249,9 @@ int EulerSim::alloc()
         double* d = nullptr;
         if ((rc = dalloc(&d, 2ll * std::max(p.num, 1)))) return rc;
         parts.push_back(d);
+        double* v = nullptr;
+        if (p.tau != 0 && (rc = dalloc(&v, 2ll * std::max(p.num, 1)))) return rc;
+        vels.push_back(v);
     }
     if (!make_plans(pf_, gf, stream) || !make_plans(pv_, gv, stream) || !make_plans(pp_, gp, stream) ||
         !make_plans(pc_, gc, stream) || (s.initial_discrete && !make_plans(pd_, gd, stream))) {
@@ -248,6 +287,9 @@ int EulerSim::alloc()
             unsigned long long* d = nullptr;
             if ((rc = falloc((void**)&d, sizeof(unsigned long long) * 2 * (size_t)std::max(p.num, 1)))) return rc;
             partfix_.push_back(d);
+            float2* v = nullptr;
+            if (p.tau != 0 && (rc = falloc((void**)&v, sizeof(float2) * (size_t)std::max(p.num, 1)))) return rc;
+            velm_.push_back(v);
         }
         if (stack_cap_ > 0 && (rc = falloc((void**)&stackm_, mapb * stack_cap_))) return rc;
         int nv[2] = {gv.NY, gv.NX}, np[2] = {gp.NY, gp.NX}, nf[2] = {gf.NY, gf.NX};
@@ -282,8 +324,12 @@ void EulerSim::release()
     f(real_buf_); f(spec_); f(spec4_); f(red_); f(d_scal_); f(d_params_); f(d_rand_);
     for (auto p : parts) f(p);
     parts.clear();
+    for (auto p : vels) f(p);
+    vels.clear();
     for (auto p : partfix_) f(p);
     partfix_.clear();
+    for (auto p : velm_) f(p);
+    velm_.clear();
     for (int l = 0; l < kMaxLagrange; ++l) { f(phi_lv_[l]); phi_lv_[l] = nullptr; }
     f(vl_h_); f(vl_rho_); f(vl_part_);
     vl_h_ = vl_rho_ = vl_part_ = nullptr;
@@ -405,8 +451,10 @@ int EulerSim::sync_fp64_views()
     CMM_LAUNCH(1, launch_map_to_planes(mapm_, gc, ChiX, ChiY, stream));
     for (int l = 0; l < L; ++l) CMM_LAUNCH(1, launch_float4_to_planes(psim_[l], gp.N, psi[l], stream));
     CMM_LAUNCH(1, launch_float4_to_planes(wfm_, gf.N, wfine, stream));
-    for (size_t i = 0; i < partfix_.size(); ++i)
+    for (size_t i = 0; i < partfix_.size(); ++i) {
         CMM_LAUNCH(1, launch_fix_to_pos(partfix_[i], s.particles_advected[i].num, gp, parts[i], stream));
+        if (velm_[i]) CMM_LAUNCH(1, launch_vel_to_f64(velm_[i], s.particles_advected[i].num, vels[i], stream));
+    }
     if (vlasov_)   // psi levels are held as phi(x) and h(v): write their Hermite planes
         for (int l = 0; l < L; ++l)
             CMM_LAUNCH(1, launch_vlasov_assemble(phi_lv_[l], phi_lv_[l] + gp.NX, vl_h_, vl_h_ + gp.NY, gp, psi[l], stream));
@@ -505,16 +553,17 @@ int EulerSim::advect_m(const double* t, const double* dtv, int lc, int ti_num, i
         // Lagrange extrapolation is linear in psi: combine the levels once per
         // step, then every RK stage interpolates a single field (already done by
         // the previous psi solve when its predicted coefficients are these)
+        const bool half = ti_num == 30 || ti_num == 40 || ti_num == 41;   // schemes with a t_{n+1/2} stage
         bool have = fused_ && l_order == 3;
         for (int i = 0; i < l_order && have; ++i)
-            have = L1[i] == fusedL1_[i] && (ti_num != 30 || L12[i] == fusedL12_[i]);
-        if (!have)
-            CMM_LAUNCH(1, launch_precombine(psim_, l_order, L1, ti_num == 30 ? L12 : nullptr, gp.N, psiA_,
-                                            ti_num == 30 ? psiB_ : nullptr, stream));
+            have = L1[i] == fusedL1_[i] && (!half || L12[i] == fusedL12_[i]);
+        if (!have && ti_num != 20)
+            CMM_LAUNCH(1, launch_precombine(psim_, l_order, L1, half ? L12 : nullptr, gp.N, psiA_,
+                                            half ? psiB_ : nullptr, stream));
     }
     a.gm = gc; a.gp = gp;
     a.map = mapm_; a.out = mapm_new_;
-    a.psiA = psiA_; a.psiB = psiB_; a.psi0 = psim_[0];
+    a.psiA = psiA_; a.psiB = psiB_; a.psi0 = psim_[0]; a.psi1 = psim_[l_order > 1 ? 1 : 0];
     double coef[4][kMaxFoot];
     map_update_coefficients(s.map_update_order_num, s.map_epsilon, coef, &a.nfoot);
     for (int p = 0; p < 4; ++p)
@@ -648,7 +697,8 @@ int EulerSim::write_map_stack(int map_num)
 
 int EulerSim::write_particles_state()
 {
-    // writeParticlesState (src/ui/cmm-io.cu:638-657): positions of every advected set
+    // writeParticlesState (src/ui/cmm-io.cu:638-657): positions of every advected set and the
+    // velocity state of the inertial ones
     const std::string dir = run_dir(s) + "/MapStack";
     if (!make_dir(dir)) { err = "cannot create " + dir; return kErrIO; }
     for (size_t i = 0; i < s.particles_advected.size(); ++i) {
@@ -658,7 +708,14 @@ int EulerSim::write_particles_state()
         std::vector<double> h((size_t)2 * num);
         CMM_CUDA(cudaMemcpyAsync(h.data(), parts[i], sizeof(double) * 2 * num, cudaMemcpyDeviceToHost, stream));
         CMM_CUDA(cudaStreamSynchronize(stream));
-        if (!write_f64(dir + "/Particles_advected_pos_P" + two_digits((int)i + 1) + ".data", h.data(), h.size())) {
+        bool ok = write_f64(dir + "/Particles_advected_pos_P" + two_digits((int)i + 1) + ".data", h.data(), h.size());
+        if (ok && s.particles_advected[i].tau != 0) {
+            if (mixed_) CMM_LAUNCH(1, launch_vel_to_f64(velm_[i], num, vels[i], stream));
+            CMM_CUDA(cudaMemcpyAsync(h.data(), vels[i], sizeof(double) * 2 * num, cudaMemcpyDeviceToHost, stream));
+            CMM_CUDA(cudaStreamSynchronize(stream));
+            ok = write_f64(dir + "/Particles_advected_vel_U" + two_digits((int)i + 1) + ".data", h.data(), h.size());
+        }
+        if (!ok) {
             err = "cannot write particle state under " + dir;
             return kErrIO;
         }
@@ -740,6 +797,11 @@ int EulerSim::restart_from_map_stack()
         CMM_CUDA(cudaMemcpyAsync(parts[i], pos.data(), sizeof(double) * pos.size(), cudaMemcpyHostToDevice, stream));
         if (mixed_) CMM_LAUNCH(1, launch_pos_to_fix(parts[i], num, gp, partfix_[i], stream));
         CMM_CUDA(cudaStreamSynchronize(stream));
+        if (s.particles_advected[i].tau == 0) continue;
+        if (!read("Particles_advected_vel_U" + two_digits((int)i + 1) + ".data", pos.data(), pos.size())) continue;
+        CMM_CUDA(cudaMemcpyAsync(vels[i], pos.data(), sizeof(double) * pos.size(), cudaMemcpyHostToDevice, stream));
+        if (mixed_) CMM_LAUNCH(1, launch_vel_from_f64(vels[i], num, velm_[i], stream));
+        CMM_CUDA(cudaStreamSynchronize(stream));
     }
     if (!msg.empty()) { log_.push(msg + "Exitting .."); err = msg; return kErrIO; }
     if (!s.particles_advected.empty() && s.verbose >= 2) log_.push("Loaded data for particle sets");
@@ -768,24 +830,40 @@ int EulerSim::init_particles()
             err = "unknown particle init_name " + p.init_name;
             return kErrParam;
         }
-        if (p.tau != 0)
-            log_.push("Particles set P" + two((int)i + 1) + " : inertial particles (tau != 0) are not advected by this build");
+    }
+    return kOk;
+}
+
+int EulerSim::init_inertial_velocity(size_t i)
+{
+    // Particle_advect_inertia_init (cmm-particles.cu:50-60) or a set at rest
+    // (cmm-euler2d.cu:620-632, 883-895)
+    auto& p = s.particles_advected[i];
+    if (p.tau == 0 || p.num <= 0) return kOk;
+    if (mixed_) {
+        if (p.init_vel) CMM_LAUNCH(1, launch_particle_vel_init_m(gp, partfix_[i], p.num, psim_[0], velm_[i], stream));
+        else CMM_CUDA(cudaMemsetAsync(velm_[i], 0, sizeof(float2) * (size_t)p.num, stream));
+    } else {
+        if (p.init_vel) CMM_LAUNCH(1, launch_particle_vel_init(parts[i], p.num, psi[0], gp, vels[i], stream));
+        else CMM_CUDA(cudaMemsetAsync(vels[i], 0, sizeof(double) * 2 * (size_t)p.num, stream));
     }
     return kOk;
 }
 
 int EulerSim::advect_particles(int lcl)
 {
-    // particles_advect (src/numerical/cmm-particles.cu:63-87): L12 for
-    // t_n + dt/2 on the history ending at the new psi
+    // particles_advect (src/numerical/cmm-particles.cu:63-87): Lp12 for t_n + dt/2 on
+    // the history ending at the new psi; fluid tracers (tau == 0) and inertial sets
     double Lp12[kMaxLagrange] = {0, 0, 0, 0};
     for (int i = 0; i < L; ++i)
         Lp12[i] = lagrange_coefficient(t_vec_.data(), t_vec_[lcl] + dt_vec_[lcl + 1] / 2.0, lcl + 1, i, L);
     bool combined = false;
     for (size_t i = 0; i < s.particles_advected.size(); ++i) {
         auto& p = s.particles_advected[i];
-        if (p.num <= 0 || p.tau != 0) continue;
+        if (p.num <= 0) continue;
         if (!(t_vec_[lcl + 1] + 1e-5 * dt_vec_[lcl + 1] >= p.init_time)) continue;
+        const int ti = p.time_integration_num;
+        const bool half = ti == 30 || ti == 40 || ti == 41;   // schemes with a t_{n+1/2} stage
         if (mixed_) {
             if (!combined && vlasov_) {
                 // separable psi: tables of level 1 (t_n), the t_{n+1/2} combination and level 0
@@ -796,33 +874,42 @@ int EulerSim::advect_particles(int lcl)
                 CMM_LAUNCH(1, launch_vlasov_table(lv, Lp12, L, gp.NX, vtab_[1], stream));
                 CMM_LAUNCH(1, launch_vlasov_table(lv, one, 1, gp.NX, vtab_[2], stream));
                 combined = true;
-            } else if (p.time_integration_num == 30 && !combined) {
+            } else if (half && !combined && !vlasov_) {
                 bool have = fused_ && L == 3;
                 for (int k = 0; k < L && have; ++k) have = Lp12[k] == fusedLp_[k];
                 if (!have) CMM_LAUNCH(1, launch_precombine(psim_, L, Lp12, nullptr, gp.N, psiP_, nullptr, stream));
                 combined = true;
             }
             cudaError_t e = vlasov_
-                ? launch_particles_m(gp, partfix_[i], p.num, nullptr, nullptr, nullptr, dt_vec_[lcl + 1],
-                                     p.time_integration_num, stream, vtab_[0], vtab_[1], vtab_[2], vtab_[3])
-                : launch_particles_m(gp, partfix_[i], p.num, psim_[1], psiP_, psim_[0], dt_vec_[lcl + 1],
-                                     p.time_integration_num, stream);
+                ? launch_particles_m(gp, partfix_[i], p.num, nullptr, nullptr, nullptr, dt_vec_[lcl + 1], ti, stream,
+                                     vtab_[0], vtab_[1], vtab_[2], vtab_[3])
+                : launch_particles_m(gp, partfix_[i], p.num, psim_[L > 1 ? 1 : 0], psiP_, psim_[0], dt_vec_[lcl + 1], ti,
+                                     stream, nullptr, nullptr, nullptr, nullptr, L > 2 ? psim_[2] : nullptr, velm_[i],
+                                     p.tau);
             kernel_launches++;
             if (e == cudaErrorInvalidValue) { err = "particle time integration " + p.time_integration + " is not built"; return kErrUnsupported; }
             CMM_CUDA(e);
             continue;
         }
         ParticleArgs a{};
-        a.gp = gp; a.pos = parts[i]; a.num = p.num;
+        a.gp = gp; a.pos = parts[i]; a.vel = vels[i]; a.num = p.num; a.tau = p.tau;
         for (int l = 0; l < kMaxLagrange; ++l) a.psi[l] = psi[l];
         for (int l = 0; l < kMaxLagrange; ++l) a.Lp12[l] = Lp12[l];
         a.dt = dt_vec_[lcl + 1];
-        a.time_integration_num = p.time_integration_num;
+        a.time_integration_num = ti;
         a.l_order = L;
         cudaError_t e = launch_particles(a, stream);
         kernel_launches++;
         if (e == cudaErrorInvalidValue) { err = "particle time integration " + p.time_integration + " is not built"; return kErrUnsupported; }
         CMM_CUDA(e);
+    }
+    // an inertial set whose start time was crossed in this step restarts its velocity
+    // (cmm-euler2d.cu:883-895)
+    int rc;
+    for (size_t i = 0; i < s.particles_advected.size(); ++i) {
+        auto& p = s.particles_advected[i];
+        if (p.tau != 0 && t_vec_[lcl] - p.init_time + dt * 1e-5 < 0 && t_vec_[lcl + 1] - p.init_time + dt * 1e-5 > 0)
+            if ((rc = init_inertial_velocity(i))) return rc;
     }
     return kOk;
 }
@@ -888,7 +975,7 @@ int EulerSim::init()
             if (s.lagrange_init_higher_order) {
                 ti = io == 1 ? 10 : io == 2 ? 21 : 30;
                 lo = io;
-                if (io == 4) { err = "Lagrange order 4 initialisation needs RK4 (not built)"; return kErrUnsupported; }
+                if (io == 4) ti = 40;
             }
             int nsteps = io - (io == L);
             for (int k = 1; k <= nsteps; ++k) {
@@ -911,6 +998,9 @@ int EulerSim::init()
         if ((rc = init_particles())) return rc;
         for (size_t i = 0; i < partfix_.size(); ++i)
             CMM_LAUNCH(1, launch_pos_to_fix(parts[i], s.particles_advected[i].num, gp, partfix_[i], stream));
+        // inertial particles start at the fluid velocity of psi(t_0) or at rest (cmm-euler2d.cu:620-632)
+        for (size_t i = 0; i < s.particles_advected.size(); ++i)
+            if ((rc = init_inertial_velocity(i))) return rc;
     }
 
     t_vec_.assign((size_t)s.iter_max() + L + 8, 0.0);
@@ -1272,13 +1362,17 @@ int EulerSim::write_time_step(double t_now, double dt_now)
     }
     for (size_t i = 0; i < s.particles_advected.size(); ++i) {
         auto& p = s.particles_advected[i];
-        if (p.tau != 0) continue;   // inertial sets are not advected by this build
         std::string id = two((int)i + 1);
         if (has(var, ("PartA_" + id).c_str()) || all)
             if ((rc = arr(psub, "Particles_advected_pos_P" + id, parts[i], 2ll * p.num))) return rc;
         if (has(var, ("PartA_Vel_" + id).c_str()) || all) {
-            CMM_LAUNCH(1, launch_sample_points_dxdy(gp, psi[0], parts[i], real_buf_, p.num, stream));
-            if ((rc = arr(psub, "Particles_advected_vel_U" + id, real_buf_, 2ll * p.num))) return rc;
+            // inertial sets: their velocity state; tracers: (psi_x, psi_y) sampled there (cmm-io.cu:580-600)
+            if (p.tau != 0) {
+                if ((rc = arr(psub, "Particles_advected_vel_U" + id, vels[i], 2ll * p.num))) return rc;
+            } else {
+                CMM_LAUNCH(1, launch_sample_points_dxdy(gp, psi[0], parts[i], real_buf_, p.num, stream));
+                if ((rc = arr(psub, "Particles_advected_vel_U" + id, real_buf_, 2ll * p.num))) return rc;
+            }
         }
     }
     return kOk;
@@ -1394,6 +1488,7 @@ int EulerSim::get_field(const std::string& n, void* dst, size_t bytes)
         for (size_t i = 0; i < s.particles_advected.size(); ++i) {
             std::string id = two((int)i + 1);
             if (n == "Particles_advected_pos_P" + id) rc = cp(parts[i], bytes);
+            else if (n == "Particles_advected_vel_U" + id && s.particles_advected[i].tau != 0) rc = cp(vels[i], bytes);
             else if (n == "Particles_advected_vel_U" + id) {
                 rc = check(launch_sample_points_dxdy(gp, psi[0], parts[i], real_buf_, s.particles_advected[i].num, stream), "dxdy");
                 if (!rc) rc = cp(real_buf_, bytes);

@@ -65,6 +65,7 @@ public:
     double* wdisc = nullptr;       // discrete initial vorticity Hermite (4 planes)
     double* stack = nullptr;       // n maps, 8*Nc doubles each
     std::vector<double*> parts;    // particle positions per set
+    std::vector<double*> vels;     // inertial velocity state per set (tau != 0; null for tracers)
     cudaStream_t stream = nullptr;
 
     // diagnostics (reference Mesure)
@@ -91,6 +92,7 @@ private:
     void swap_levels(int a, int b);
     int incomp(double* out);
     int init_particles();
+    int init_inertial_velocity(size_t i);   // v = u(x) of psi level 0, or 0 (init_vel)
     int advect_particles(int lcl);
     int push_stack();
     int reserve_stack(int n);          // device stack capacity for n sub-maps
@@ -137,6 +139,7 @@ private:
     float4* wdiscm_ = nullptr;       // discrete initial vorticity nodes (FP32 Hermite)
     float4* stackm_ = nullptr;       // n maps, 2*Nc float4 each
     std::vector<unsigned long long*> partfix_;   // tracer positions, 64-bit fixed point (x, y interleaved)
+    std::vector<float2*> velm_;                  // inertial velocity state (FP32), null for tracer sets
 
     // sampled outputs: buffers and plans of the largest sample grid seen so far
     int smp_n_ = 0, smp_plan_n_ = 0;

@@ -99,9 +99,10 @@ void og_fourier_hermite(const og_grid* g, const double* in_c, double* out4);
 /* ---------------- the Euler-2D driver (src/simulation/cmm-euler2d.cu) ---------------- */
 typedef struct {
     int num;                      /* particles in the set */
-    double tau;                   /* only tau == 0 (fluid tracers) is restated */
-    int time_integration_num;     /* 10, 20, 30, 40 */
+    double tau;                   /* 0: fluid tracers; otherwise inertial particles */
+    int time_integration_num;     /* 10, 20, 30, 40, 31, 41 */
     double init_time;
+    int init_vel;                 /* inertial: start at the fluid velocity (1) or at rest (0) */
 } og_particle_set;
 
 typedef struct {
@@ -135,6 +136,10 @@ void og_destroy(og_state* st);
 int og_set_discrete_initial(og_state* st, const double* values);
 /* particle initial positions (interleaved x,y) for set i */
 int og_set_particles(og_state* st, int i_set, const double* pos);
+/* Particle_advect_inertia (src/numerical/cmm-particles.cu:280-551) and its initialisation (:50-60) */
+void og_particle_advect_inertia(int num, double dt, double* pos, double* vel, const double* psi, const og_grid* g,
+                                double tau, int ti, int l_order, const double* Lp12);
+void og_particle_inertia_init(int num, const double* pos, double* vel, const double* psi, const og_grid* g);
 /* initial state + Lagrange history (src/simulation/cmm-euler2d.cu:495-619,
  * src/simulation/cmm-vlasov1d.cu:516-656); -1 if the Vlasov potential rejects the grids */
 int og_init(og_state* st);
@@ -161,6 +166,7 @@ const double* og_psi(const og_state* st);         /* L*4*Npsi, level 0 first */
 const double* og_vort_coarse(const og_state* st); /* Nc */
 const double* og_vort_fine(const og_state* st);   /* 4*Nf */
 const double* og_particles(const og_state* st, int i_set);
+double* og_particle_vel(og_state* st, int i_set);  /* inertial velocity state (2*num) */
 const og_grid* og_grid_of(const og_state* st, int which); /* 0 coarse,1 fine,2 psi,3 vort */
 
 /* diagnostics: src/numerical/cmm-mesure.cu:30-89, cmm-simulation-host.cu:668-680 */

@@ -66,6 +66,82 @@ static void rk3_classical_b(const double* psi, const double* x_in, double* x_out
     x_out[1] = x_in[1] - dt * (k[1] + 4 * k[3] + k[5]) / 6.0;
 }
 
+/* velocity u = (psi_y, -psi_x) of psi level lv at x */
+static void vel_level(const double* psi, int lv, const double* x, double* u, const og_grid* g)
+{
+    og_hermite_interpolate_grad_2D(psi + 4 * g->N * (long)lv, x, u, g, 1);
+}
+
+/* sum_l c[l] u_l(x) over l_order levels, accumulated from level 0 upwards */
+static void vel_comb(const double* psi, const double* c, int l_order, const double* x, double* k, const og_grid* g)
+{
+    double u[8];
+    og_hermite_interpolate_grad_2D(psi, x, u, g, l_order);
+    k[0] = c[0] * u[0]; k[1] = c[0] * u[1];
+    for (int i_l = 1; i_l < l_order; i_l++) { k[0] += c[i_l] * u[i_l * 2]; k[1] += c[i_l] * u[i_l * 2 + 1]; }
+}
+
+/* adam_bashford_2_pc_b: cmm-timestep.cu:112-135 -- ten fixed-point sweeps on levels 0 and 1 */
+static void ab2_pc_b(const double* psi, const double* x_in, double* x_out, const og_grid* g, double dt)
+{
+    double u[2], u2[2], xf_p[2] = {x_in[0], x_in[1]};
+    x_out[0] = x_in[0]; x_out[1] = x_in[1];
+    for (int ctr = 0; ctr < 10; ctr++) {
+        vel_level(psi, 1, xf_p, u2, g);
+        xf_p[0] = x_out[0] - dt * u2[0]; xf_p[1] = x_out[1] - dt * u2[1];
+        vel_level(psi, 1, xf_p, u2, g);
+        vel_level(psi, 0, x_out, u, g);
+        x_out[0] = x_in[0] - dt * (1.5 * u[0] - 0.5 * u2[0]);
+        x_out[1] = x_in[1] - dt * (1.5 * u[1] - 0.5 * u2[1]);
+    }
+}
+
+/* RK4_classical_b: cmm-timestep.cu:260-307 */
+static void rk4_classical_b(const double* psi, const double* x_in, double* x_out, const og_grid* g,
+                            double dt, int l_order, const og_lcoef* lc)
+{
+    double k1[2], k2[2], k3[2], k4[2], y[2];
+    vel_comb(psi, lc->L1, l_order, x_in, k1, g);
+    y[0] = x_in[0] - dt * k1[0] / 2.0; y[1] = x_in[1] - dt * k1[1] / 2.0;
+    vel_comb(psi, lc->L12, l_order, y, k2, g);
+    y[0] = x_in[0] - dt * k2[0] / 2.0; y[1] = x_in[1] - dt * k2[1] / 2.0;
+    vel_comb(psi, lc->L12, l_order, y, k3, g);
+    y[0] = x_in[0] - dt * k3[0]; y[1] = x_in[1] - dt * k3[1];
+    vel_level(psi, 0, y, k4, g);
+    x_out[0] = x_in[0] - dt * (k1[0] + 2 * k2[0] + 2 * k3[0] + k4[0]) / 6.0;
+    x_out[1] = x_in[1] - dt * (k1[1] + 2 * k2[1] + 2 * k3[1] + k4[1]) / 6.0;
+}
+
+/* RK3_optimized_b: cmm-timestep.cu:348-374 */
+static void rk3_optimized_b(const double* psi, const double* x_in, double* x_out, const og_grid* g,
+                            double dt, int l_order, const og_lcoef* lc)
+{
+    double k1[2], k2[2], k3[2], y[2];
+    vel_comb(psi, lc->L1, l_order, x_in, k1, g);
+    y[0] = x_in[0] - dt * k1[0]; y[1] = x_in[1] - dt * k1[1];
+    vel_level(psi, 0, y, k2, g);
+    y[0] = x_in[0] + 2 * dt * (-2 * k1[0] + k2[0]); y[1] = x_in[1] + 2 * dt * (-2 * k1[1] + k2[1]);
+    vel_level(psi, 1, y, k3, g);
+    x_out[0] = x_in[0] - dt * (5 * k1[0] + 8 * k2[0] - k3[0]) / 12.0;
+    x_out[1] = x_in[1] - dt * (5 * k1[1] + 8 * k2[1] - k3[1]) / 12.0;
+}
+
+/* RK4_optimized_b: cmm-timestep.cu:428-466 */
+static void rk4_optimized_b(const double* psi, const double* x_in, double* x_out, const og_grid* g,
+                            double dt, int l_order, const og_lcoef* lc)
+{
+    double k1[2], k2[2], k3[2], k4[2], y[2];
+    vel_comb(psi, lc->L1, l_order, x_in, k1, g);
+    y[0] = x_in[0] - dt * k1[0]; y[1] = x_in[1] - dt * k1[1];
+    vel_level(psi, 0, y, k2, g);
+    y[0] = x_in[0] - dt * (3 * k1[0] + k2[0]) / 8.0; y[1] = x_in[1] - dt * (3 * k1[1] + k2[1]) / 8.0;
+    vel_comb(psi, lc->L12, l_order, y, k3, g);
+    y[0] = x_in[0] + dt * (k2[0] - 4 * k3[0]) / 3.0; y[1] = x_in[1] + dt * (k2[1] - 4 * k3[1]) / 3.0;
+    vel_level(psi, 0, y, k4, g);
+    x_out[0] = x_in[0] - dt * (2 * k1[0] - k2[0] + 8 * k3[0] + 3 * k4[0]) / 12.0;
+    x_out[1] = x_in[1] - dt * (2 * k1[1] - k2[1] + 8 * k3[1] + 3 * k4[1]) / 12.0;
+}
+
 /* ------------------------------------------------------------------ */
 /* kernels restated as loops                                           */
 /* ------------------------------------------------------------------ */
@@ -120,6 +196,10 @@ void og_advect_map(const double* ChiX, const double* ChiY, double* ChiX_new, dou
                     case 10: euler_exp_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
                     case 21: rk2_heun_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
                     case 30: rk3_classical_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
+                    case 20: ab2_pc_b(psi, x_ep, x_f, gp, dt); break;
+                    case 40: rk4_classical_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
+                    case 31: rk3_optimized_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
+                    case 41: rk4_optimized_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
                     default: x_f[0] = x_f[1] = 0;
                 }
                 og_diffeo_interpolate_2D(ChiX, ChiY, x_f[0], x_f[1], &x_f[0], &x_f[1], gm);
@@ -259,11 +339,170 @@ void og_particle_advect(int num, double dt, double* pos, const double* psi, cons
                 p[1] += dt * (k[1] + 4 * k[3] + k[5]) / 6.0;
                 break;
             }
+            case 40: {   /* :206-240 */
+                double k1[2], k2[2], k3[2], k4[2], y[2];
+                vel_level(psi, 1, p, k1, g);
+                y[0] = p[0] + dt * k1[0] / 2.0; y[1] = p[1] + dt * k1[1] / 2.0;
+                vel_comb(psi, Lp12, l_order, y, k2, g);
+                y[0] = p[0] + dt * k2[0] / 2.0; y[1] = p[1] + dt * k2[1] / 2.0;
+                vel_comb(psi, Lp12, l_order, y, k3, g);
+                y[0] = p[0] + dt * k3[0]; y[1] = p[1] + dt * k3[1];
+                vel_level(psi, 0, y, k4, g);
+                p[0] += dt * (k1[0] + 2 * k2[0] + 2 * k3[0] + k4[0]) / 6.0;
+                p[1] += dt * (k1[1] + 2 * k2[1] + 2 * k3[1] + k4[1]) / 6.0;
+                break;
+            }
+            case 31: {   /* :242-262 */
+                double k1[2], k2[2], k3[2], y[2];
+                vel_level(psi, 1, p, k1, g);
+                y[0] = p[0] + dt * k1[0]; y[1] = p[1] + dt * k1[1];
+                vel_level(psi, 0, y, k2, g);
+                y[0] = p[0] + dt * (k1[0] - 2 * k2[0]); y[1] = p[1] + dt * (k1[1] - 2 * k2[1]);
+                vel_level(psi, 2, y, k3, g);
+                p[0] += dt * (8 * k1[0] + 5 * k2[0] - k3[0]) / 12.0;
+                p[1] += dt * (8 * k1[1] + 5 * k2[1] - k3[1]) / 12.0;
+                break;
+            }
+            case 41: {   /* :263-293 */
+                double k1[2], k2[2], k3[2], k4[2], y[2];
+                vel_level(psi, 1, p, k1, g);
+                y[0] = p[0] + dt * k1[0]; y[1] = p[1] + dt * k1[1];
+                vel_level(psi, 0, y, k2, g);
+                y[0] = p[0] + dt / 8.0 * (3 * k1[0] + k2[0]); y[1] = p[1] + dt / 8.0 * (3 * k1[1] + k2[1]);
+                vel_comb(psi, Lp12, l_order, y, k3, g);
+                y[0] = p[0] + dt / 3.0 * (-k2[0] + 4 * k3[0]); y[1] = p[1] + dt / 3.0 * (-k2[1] + 4 * k3[1]);
+                vel_level(psi, 0, y, k4, g);
+                p[0] += dt * (2 * k1[0] - k2[0] + 8 * k3[0] + 3 * k4[0]) / 12.0;
+                p[1] += dt * (2 * k1[1] - k2[1] + 8 * k3[1] + 3 * k4[1]) / 12.0;
+                break;
+            }
             default: p[0] = p[1] = 0; break;
         }
         pos[2 * i] = p[0] - floor((p[0] - g->bounds[0]) / LX) * LX;
         pos[2 * i + 1] = p[1] - floor((p[1] - g->bounds[2]) / LY) * LY;
     }
+}
+
+/* Particle_advect_inertia: src/numerical/cmm-particles.cu:280-551.  State (x, v); the
+ * particle relaxes to the fluid velocity u with time constant tau:
+ *   dx/dt = v,  dv/dt = -(v - u(x, t)) / tau
+ * u(t_n) is psi level 1, u(t_{n+1}) level 0, u(t_{n-1}) level 2 and u(t_{n+1/2}) the Lp12
+ * combination, as for the tracers. */
+void og_particle_advect_inertia(int num, double dt, double* pos, double* vel, const double* psi, const og_grid* g,
+                                double tau, int ti, int l_order, const double* Lp12)
+{
+    double LX = g->bounds[1] - g->bounds[0], LY = g->bounds[3] - g->bounds[2];
+    #pragma omp parallel for schedule(static)
+    for (int i = 0; i < num; ++i) {
+        double p[2] = {pos[2 * i], pos[2 * i + 1]};
+        double v[2] = {vel[2 * i], vel[2 * i + 1]};
+        double u[2], y[2];
+        switch (ti) {
+            case 10: {   /* :300-317 */
+                vel_level(psi, 1, p, u, g);
+                p[0] += dt * v[0]; p[1] += dt * v[1];
+                vel[2 * i] -= dt * (v[0] - u[0]) / tau;
+                vel[2 * i + 1] -= dt * (v[1] - u[1]) / tau;
+                break;
+            }
+            case 20: {   /* :318-348 */
+                vel_level(psi, 1, p, u, g);
+                double a1[2] = {-(v[0] - u[0]) / tau, -(v[1] - u[1]) / tau};
+                double x2[2] = {v[0] + dt * a1[0], v[1] + dt * a1[1]};
+                y[0] = p[0] + dt * v[0]; y[1] = p[1] + dt * v[1];
+                vel_level(psi, 0, y, u, g);
+                double a2[2] = {-(x2[0] - u[0]) / tau, -(x2[1] - u[1]) / tau};
+                p[0] += dt / 2.0 * (v[0] + x2[0]); p[1] += dt / 2.0 * (v[1] + x2[1]);
+                vel[2 * i] += dt / 2.0 * (a1[0] + a2[0]);
+                vel[2 * i + 1] += dt / 2.0 * (a1[1] + a2[1]);
+                break;
+            }
+            case 30: {   /* :349-397 */
+                vel_level(psi, 1, p, u, g);
+                double a1[2] = {-(v[0] - u[0]) / tau, -(v[1] - u[1]) / tau};
+                double x2[2] = {v[0] + dt / 2.0 * a1[0], v[1] + dt / 2.0 * a1[1]};
+                y[0] = p[0] + dt / 2.0 * v[0]; y[1] = p[1] + dt / 2.0 * v[1];
+                vel_comb(psi, Lp12, l_order, y, u, g);
+                double a2[2] = {-(x2[0] - u[0]) / tau, -(x2[1] - u[1]) / tau};
+                double x3[2] = {v[0] + dt * (-a1[0] + 2 * a2[0]), v[1] + dt * (-a1[1] + 2 * a2[1])};
+                y[0] = p[0] + dt * (-v[0] + 2 * x2[0]); y[1] = p[1] + dt * (-v[1] + 2 * x2[1]);
+                vel_level(psi, 0, y, u, g);
+                double a3[2] = {-(x3[0] - u[0]) / tau, -(x3[1] - u[1]) / tau};
+                p[0] += dt / 6.0 * (v[0] + 4 * x2[0] + x3[0]); p[1] += dt / 6.0 * (v[1] + 4 * x2[1] + x3[1]);
+                vel[2 * i] += dt / 6.0 * (a1[0] + 4 * a2[0] + a3[0]);
+                vel[2 * i + 1] += dt / 6.0 * (a1[1] + 4 * a2[1] + a3[1]);
+                break;
+            }
+            case 40: {   /* :398-462 */
+                vel_level(psi, 1, p, u, g);
+                double a1[2] = {-(v[0] - u[0]) / tau, -(v[1] - u[1]) / tau};
+                double x2[2] = {v[0] + dt / 2.0 * a1[0], v[1] + dt / 2.0 * a1[1]};
+                y[0] = p[0] + dt / 2.0 * v[0]; y[1] = p[1] + dt / 2.0 * v[1];
+                vel_comb(psi, Lp12, l_order, y, u, g);
+                double a2[2] = {-(x2[0] - u[0]) / tau, -(x2[1] - u[1]) / tau};
+                double x3[2] = {v[0] + dt / 2.0 * a2[0], v[1] + dt / 2.0 * a2[1]};
+                y[0] = p[0] + dt / 2.0 * x2[0]; y[1] = p[1] + dt / 2.0 * x2[1];
+                vel_comb(psi, Lp12, l_order, y, u, g);
+                double a3[2] = {-(x3[0] - u[0]) / tau, -(x3[1] - u[1]) / tau};
+                double x4[2] = {v[0] + dt * a3[0], v[1] + dt * a3[1]};
+                y[0] = p[0] + dt * x3[0]; y[1] = p[1] + dt * x3[1];
+                vel_level(psi, 0, y, u, g);
+                double a4[2] = {-(x4[0] - u[0]) / tau, -(x4[1] - u[1]) / tau};
+                p[0] += dt / 6.0 * (v[0] + 2 * x2[0] + 2 * x3[0] + x4[0]);
+                p[1] += dt / 6.0 * (v[1] + 2 * x2[1] + 2 * x3[1] + x4[1]);
+                vel[2 * i] += dt / 6.0 * (a1[0] + 2 * a2[0] + 2 * a3[0] + a4[0]);
+                vel[2 * i + 1] += dt / 6.0 * (a1[1] + 2 * a2[1] + 2 * a3[1] + a4[1]);
+                break;
+            }
+            case 31: {   /* :463-497 */
+                vel_level(psi, 1, p, u, g);
+                double a1[2] = {-(v[0] - u[0]) / tau, -(v[1] - u[1]) / tau};
+                double x2[2] = {v[0] + dt * a1[0], v[1] + dt * a1[1]};
+                y[0] = p[0] + dt * v[0]; y[1] = p[1] + dt * v[1];
+                vel_level(psi, 0, y, u, g);
+                double a2[2] = {-(x2[0] - u[0]) / tau, -(x2[1] - u[1]) / tau};
+                double x3[2] = {v[0] + dt * (a1[0] - 2 * a2[0]), v[1] + dt * (a1[1] - 2 * a2[1])};
+                y[0] = p[0] + dt * (v[0] - 2 * x2[0]); y[1] = p[1] + dt * (v[1] - 2 * x2[1]);
+                vel_level(psi, 2, y, u, g);
+                double a3[2] = {-(x3[0] - u[0]) / tau, -(x3[1] - u[1]) / tau};
+                p[0] += dt / 12.0 * (8 * v[0] + 5 * x2[0] - x3[0]); p[1] += dt / 12.0 * (8 * v[1] + 5 * x2[1] - x3[1]);
+                vel[2 * i] += dt / 12.0 * (8 * a1[0] + 5 * a2[0] - a3[0]);
+                vel[2 * i + 1] += dt / 12.0 * (8 * a1[1] + 5 * a2[1] - a3[1]);
+                break;
+            }
+            case 41: {   /* :498-545 */
+                vel_level(psi, 1, p, u, g);
+                double a1[2] = {-(v[0] - u[0]) / tau, -(v[1] - u[1]) / tau};
+                double x2[2] = {v[0] + dt * a1[0], v[1] + dt * a1[1]};
+                y[0] = p[0] + dt * v[0]; y[1] = p[1] + dt * v[1];
+                vel_level(psi, 0, y, u, g);
+                double a2[2] = {-(x2[0] - u[0]) / tau, -(x2[1] - u[1]) / tau};
+                double x3[2] = {v[0] + dt / 8.0 * (3 * a1[0] + a2[0]), v[1] + dt / 8.0 * (3 * a1[1] + a2[1])};
+                y[0] = p[0] + dt / 8.0 * (3 * v[0] + x2[0]); y[1] = p[1] + dt / 8.0 * (3 * v[1] + x2[1]);
+                vel_comb(psi, Lp12, l_order, y, u, g);
+                double a3[2] = {-(x3[0] - u[0]) / tau, -(x3[1] - u[1]) / tau};
+                double x4[2] = {v[0] + dt / 3.0 * (-a2[0] + 4 * a3[0]), v[1] + dt / 3.0 * (-a2[1] + 4 * a3[1])};
+                y[0] = p[0] + dt / 3.0 * (-x2[0] + 4 * x3[0]); y[1] = p[1] + dt / 3.0 * (-x2[1] + 4 * x3[1]);
+                vel_level(psi, 0, y, u, g);
+                double a4[2] = {-(x4[0] - u[0]) / tau, -(x4[1] - u[1]) / tau};
+                p[0] += dt / 12.0 * (2 * v[0] - x2[0] + 8 * x3[0] + 3 * x4[0]);
+                p[1] += dt / 12.0 * (2 * v[1] - x2[1] + 8 * x3[1] + 3 * x4[1]);
+                vel[2 * i] += dt / 12.0 * (2 * a1[0] - a2[0] + 8 * a3[0] + 3 * a4[0]);
+                vel[2 * i + 1] += dt / 12.0 * (2 * a1[1] - a2[1] + 8 * a3[1] + 3 * a4[1]);
+                break;
+            }
+            default: p[0] = p[1] = 0; vel[2 * i] = vel[2 * i + 1] = 0; break;
+        }
+        pos[2 * i] = p[0] - floor((p[0] - g->bounds[0]) / LX) * LX;
+        pos[2 * i + 1] = p[1] - floor((p[1] - g->bounds[2]) / LY) * LY;
+    }
+}
+
+/* Particle_advect_inertia_init: cmm-particles.cu:50-60 -- v = u of psi level 0 at x */
+void og_particle_inertia_init(int num, const double* pos, double* vel, const double* psi, const og_grid* g)
+{
+    #pragma omp parallel for schedule(static)
+    for (int i = 0; i < num; ++i) vel_level(psi, 0, pos + 2 * i, vel + 2 * i, g);
 }
 
 /* ------------------------------------------------------------------ */
@@ -281,6 +520,7 @@ struct og_state {
     double* xy;             /* 2*Nf */
     double* cbuf1; double* cbuf2; double* rbuf;
     double* parts[8];
+    double* vels[8];        /* inertial velocity state per set */
     double* t_vec; double* dt_vec; int t_cap;
     int loop_ctr, old_ctr;
 };
@@ -320,8 +560,10 @@ og_state* og_create(const og_settings* s)
     long rmax = st->gf.N > st->gv.N ? st->gf.N : st->gv.N;
     if (st->gc.N > rmax) rmax = st->gc.N;
     st->rbuf = (double*)xmalloc(sizeof(double) * rmax);
-    for (int i = 0; i < s->n_particle_sets; ++i)
+    for (int i = 0; i < s->n_particle_sets; ++i) {
         st->parts[i] = (double*)xmalloc(sizeof(double) * 2 * (size_t)s->psets[i].num);
+        st->vels[i] = (double*)xmalloc(sizeof(double) * 2 * (size_t)s->psets[i].num);
+    }
     st->t_cap = 1 << 16;
     st->t_vec = (double*)xmalloc(sizeof(double) * st->t_cap);
     st->dt_vec = (double*)xmalloc(sizeof(double) * st->t_cap);
@@ -335,7 +577,7 @@ void og_destroy(og_state* st)
     free(st->psi); free(st->vort); free(st->vort_fine); free(st->vort_disc);
     free(st->stackX); free(st->stackY); free(st->xy);
     free(st->cbuf1); free(st->cbuf2); free(st->rbuf);
-    for (int i = 0; i < st->s.n_particle_sets; ++i) free(st->parts[i]);
+    for (int i = 0; i < st->s.n_particle_sets; ++i) { free(st->parts[i]); free(st->vels[i]); }
     free(st->t_vec); free(st->dt_vec);
     free(st);
 }
@@ -502,6 +744,13 @@ int og_init(og_state* st)
         }
         og_init_diffeo(st->ChiX, st->ChiY, &st->gc);
     }
+    /* inertial particles start at the fluid velocity or at rest (cmm-euler2d.cu:620-632) */
+    for (int i_p = 0; i_p < s->n_particle_sets; ++i_p) {
+        og_particle_set* ps = &s->psets[i_p];
+        if (ps->tau == 0) continue;
+        if (ps->init_vel) og_particle_inertia_init(ps->num, st->parts[i_p], st->vels[i_p], st->psi, &st->gp);
+        else memset(st->vels[i_p], 0, sizeof(double) * 2 * (size_t)ps->num);
+    }
     for (int i = 0; i < Lo; i++) { st->t_vec[i] = 0 - (Lo - 1 - i) * s->dt; st->dt_vec[i] = s->dt; }
     st->loop_ctr = 0; st->old_ctr = 0;
     return 0;
@@ -578,9 +827,23 @@ int og_step(og_state* st, double dt_now, double* e_inc, int* remapped)
         Lp12[i] = og_get_L_coefficient(st->t_vec, st->t_vec[lcl] + st->dt_vec[lcl + 1] / 2.0, lcl + 1, i, Lo);
     for (int i_p = 0; i_p < s->n_particle_sets; ++i_p) {
         og_particle_set* ps = &s->psets[i_p];
-        if (st->t_vec[lcl + 1] + 1e-5 * st->dt_vec[lcl + 1] >= ps->init_time && ps->tau == 0)
+        if (!(st->t_vec[lcl + 1] + 1e-5 * st->dt_vec[lcl + 1] >= ps->init_time)) continue;
+        if (ps->tau == 0)
             og_particle_advect(ps->num, st->dt_vec[lcl + 1], st->parts[i_p], st->psi, &st->gp,
                                ps->time_integration_num, Lo, Lp12);
+        else
+            og_particle_advect_inertia(ps->num, st->dt_vec[lcl + 1], st->parts[i_p], st->vels[i_p], st->psi,
+                                       &st->gp, ps->tau, ps->time_integration_num, Lo, Lp12);
+    }
+    /* a set whose start time was crossed in this step restarts its inertial velocity
+     * (cmm-euler2d.cu:883-895) */
+    for (int i_p = 0; i_p < s->n_particle_sets; ++i_p) {
+        og_particle_set* ps = &s->psets[i_p];
+        if (ps->tau == 0) continue;
+        if (st->t_vec[lcl] - ps->init_time + s->dt * 1e-5 < 0 && st->t_vec[lcl + 1] - ps->init_time + s->dt * 1e-5 > 0) {
+            if (ps->init_vel) og_particle_inertia_init(ps->num, st->parts[i_p], st->vels[i_p], st->psi, &st->gp);
+            else memset(st->vels[i_p], 0, sizeof(double) * 2 * (size_t)ps->num);
+        }
     }
     st->loop_ctr++;
     return saturated;
@@ -596,6 +859,7 @@ const double* og_psi(const og_state* st) { return st->psi; }
 const double* og_vort_coarse(const og_state* st) { return st->vort; }
 const double* og_vort_fine(const og_state* st) { return st->vort_fine; }
 const double* og_particles(const og_state* st, int i) { return st->parts[i]; }
+double* og_particle_vel(og_state* st, int i) { return st->vels[i]; }
 const og_grid* og_grid_of(const og_state* st, int which)
 {
     switch (which) { case 0: return &st->gc; case 1: return &st->gf; case 2: return &st->gp; default: return &st->gv; }

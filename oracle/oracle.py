@@ -38,7 +38,7 @@ class OgGrid(C.Structure):
 
 class OgParticleSet(C.Structure):
     _fields_ = [("num", C.c_int), ("tau", C.c_double), ("time_integration_num", C.c_int),
-                ("init_time", C.c_double)]
+                ("init_time", C.c_double), ("init_vel", C.c_int)]
 
 
 class OgSettings(C.Structure):
@@ -75,6 +75,8 @@ def lib():
             getattr(L, name).argtypes = [C.c_void_p]
         L.og_particles.restype = dp
         L.og_particles.argtypes = [C.c_void_p, C.c_int]
+        L.og_particle_vel.restype = dp
+        L.og_particle_vel.argtypes = [C.c_void_p, C.c_int]
         L.og_grid_of.restype = C.POINTER(OgGrid)
         L.og_grid_of.argtypes = [C.c_void_p, C.c_int]
         for name in ("og_time", "og_energy_H", "og_enstrophy", "og_palinstrophy", "og_max_vorticity"):
@@ -147,6 +149,7 @@ class EulerOracle:
             s.psets[i].tau = p["tau"]
             s.psets[i].time_integration_num = p["time_integration_num"]
             s.psets[i].init_time = p["init_time"]
+            s.psets[i].init_vel = int(p.get("init_vel", 0))
         self._s = s
         self.h = L.og_create(C.byref(s))
         self.L = L
@@ -196,6 +199,8 @@ class EulerOracle:
             prev[(l - 1) * np4:l * np4] = files["Stream_function_Psi_H_psi_%d" % l]
         for i, p in enumerate(self.cfg.get("particles", [])):
             self.set_particles(i, files["Particles_advected_pos_P%02d" % (i + 1)])
+            if p["tau"] != 0:
+                self.set_particle_velocity(i, files["Particles_advected_vel_U%02d" % (i + 1)])
         rc = self.L.og_restart(self.h, restart_time, n, _dp(sx), _dp(sy), _dp(chix), _dp(chiy), _dp(prev))
         if rc:
             raise ValueError("oracle restart rejected the stored map stack (%d maps, capacity %d)"
@@ -240,10 +245,21 @@ class EulerOracle:
         return np.ctypeslib.as_array(self.L.og_particles(self.h, i), shape=(2 * n,)).copy()
 
     def particle_velocity(self, i):
+        """What the reference saves as Particles_advected_vel_U<i>: the velocity state of
+        an inertial set (tau != 0), else (psi_x, psi_y) sampled at the tracers
+        (k_h_sample_points_dxdy, src/ui/cmm-io.cu:580-600)."""
+        p = self.cfg["particles"][i]
+        if p["tau"] != 0:
+            return np.ctypeslib.as_array(self.L.og_particle_vel(self.h, i), shape=(2 * p["num"],)).copy()
         pos = self.particles(i)
         out = np.empty_like(pos)
         self.L.og_sample_points_dxdy(self.h, _dp(pos), _dp(out), len(pos) // 2)
         return out
+
+    def set_particle_velocity(self, i, vel):
+        n = 2 * self.cfg["particles"][i]["num"]
+        v = np.ascontiguousarray(vel, dtype=np.float64)
+        np.ctypeslib.as_array(self.L.og_particle_vel(self.h, i), shape=(n,))[:] = v[:n]
 
     def time(self):
         return self.L.og_time(self.h)
@@ -297,7 +313,8 @@ def map_stack_files(o):
     every stacked sub-map (Map_ChiX_H_<i>, Map_ChiY_H_<i>, 4*Nc planar doubles), the
     active map (..._H_coarse) and Stream_function_Psi_H_psi_<l> for l = 1..L-1 -- each
     of them a copy of psi level 0, as the reference writes Psi.Dev_var for every l
-    (src/ui/cmm-io.cu:631-633) -- and the tracer positions Particles_advected_pos_P<ii>."""
+    (src/ui/cmm-io.cu:631-633) -- the particle positions Particles_advected_pos_P<ii> and,
+    for inertial sets, their velocities Particles_advected_vel_U<ii>."""
     files = {}
     sx, sy = o.map_stack()
     for i in range(sx.shape[0]):
@@ -308,8 +325,10 @@ def map_stack_files(o):
     p0 = o.psi(1)
     for l in range(1, o.cfg["lagrange_order"]):
         files["Stream_function_Psi_H_psi_%d" % l] = p0
-    for i in range(len(o.cfg.get("particles", []))):
+    for i, p in enumerate(o.cfg.get("particles", [])):
         files["Particles_advected_pos_P%02d" % (i + 1)] = o.particles(i)
+        if p["tau"] != 0:
+            files["Particles_advected_vel_U%02d" % (i + 1)] = o.particle_velocity(i)
     return files
 
 

@@ -104,8 +104,8 @@ class DebugRecorder:
                 if ("PartA_%02d" % (i + 1)) in var or all_:
                     self._stat("Particles_advected_pos_P%02d" % (i + 1), stats_raw(st.particles(i)))
                 if ("PartA_Vel_%02d" % (i + 1)) in var or all_:
-                    if p.tau == 0:
-                        self._stat("Particles_advected_vel_U%02d" % (i + 1), stats_raw(st.particle_velocity(i)))
+                    # inertial sets: their velocity state; tracers: (psi_x, psi_y) sampled there
+                    self._stat("Particles_advected_vel_U%02d" % (i + 1), stats_raw(st.particle_velocity(i)))
         # compute_conservation_targets (cmm-simulation-host.cu:615-698)
         if save_instant(s.save_comp, t_now, dt_now, dt, need_conv=True) and s.simulation_type_num == 2:
             m = st.vlasov_mesure()

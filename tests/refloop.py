@@ -286,7 +286,7 @@ class Settings:
                     initial_discrete=self.initial_discrete, initial_discrete_grid=self.initial_discrete_grid,
                     max_maps=self.cpu_map_num, simulation_type_num=self.simulation_type_num,
                     particles=[dict(num=p.num, tau=p.tau, time_integration_num=p.time_integration_num,
-                                    init_time=p.init_time) for p in self.particles_advected])
+                                    init_time=p.init_time, init_vel=p.init_vel) for p in self.particles_advected])
 
 
 def settings_from_param_text(text, cli=()):

@@ -61,6 +61,27 @@ __device__ __forceinline__ double init_vorticity(double x, double y, int ic, con
             double c = exp(-d * (y - PI)) + exp(d * (y - PI));
             return 5.0 * (1 + 0.01 * cos(freq * x)) * 4 / c / c;
         }
+        case 7: {  // turbulence_gaussienne: 8 x 8 positive blobs on the corners, 7 x 7 negative ones
+                   // between them, offset by the cuRAND table after the 1000 uniform values
+            x -= floor(x / kTwoPi) * kTwoPi;
+            y -= floor(y / kTwoPi) * kTwoPi;
+            const int NB = 8;
+            const double sig = 0.2, amp = 1 / (kTwoPi * sig * sig), den = 2 * sig * sig;
+            double r = 0;
+            for (int mx = 0; mx < NB; mx++)
+                for (int my = 0; my < NB; my++) {
+                    const double ex = x - mx * kTwoPi / (NB - 1), ey = y - my * kTwoPi / (NB - 1);
+                    r += amp * exp(-(ex * ex / den + ey * ey / den));
+                }
+            const double* off = rnd + 1000;
+            for (int mx = 0; mx < NB - 1; mx++)
+                for (int my = 0; my < NB - 1; my++) {
+                    const double ex = x - (2 * mx + 1) * kTwoPi / (2 * (NB - 1)) + off[mx * (NB - 1) + my];
+                    const double ey = y - (2 * my + 1) * kTwoPi / (2 * (NB - 1)) + off[49 + mx * (NB - 1) + my];
+                    r -= amp * exp(-(ex * ex / den + ey * ey / den));
+                }
+            return r - 0.008857380480028442;   // the reference's mean correction
+        }
         case 8: {  // gaussian_blobs (random offsets from a host-drawn table)
             x -= floor(x / kTwoPi) * kTwoPi;
             y -= floor(y / kTwoPi) * kTwoPi;

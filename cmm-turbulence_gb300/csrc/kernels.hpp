@@ -40,13 +40,21 @@ cudaError_t launch_incomp(const Grid& gcheck, const Grid& gmap, const double* X,
 
 // Initial-condition selector for sampling omega_0 (k_h_sample_from_init,
 // src/simulation/cmm-simulation-kernel.cu:342-373).
+// random tables of the analytic initial conditions: kRandTable uniform(-1, 1) values of
+// mt19937_64 seed 0 (gaussian_blobs, cmm-euler2d.cu:347-352) followed by the
+// 2 * kGaussBlobs^2 cuRAND offsets of turbulence_gaussienne (init_tables.cu)
+constexpr int kRandTable = 1000;
+constexpr int kGaussBlobs = 7;
+constexpr int kInitTable = kRandTable + 2 * kGaussBlobs * kGaussBlobs;
+cudaError_t launch_gaussienne_offsets(double* out, cudaStream_t s);
+
 struct InitSource {
     int kind;                 // 0 analytic vorticity, 1 analytic passive scalar, 2 Vlasov distribution, 3 discrete Hermite
     int ic_num;               // analytic initial-condition number
     const double* discrete;   // Hermite planes of the discrete initial field
     Grid gd;                  // its grid
     const double* params;     // 10 initial_params (device)
-    const double* rand_table; // 1000 uniform(-1,1) values (device), gaussian_blobs
+    const double* rand_table; // kInitTable values (device): gaussian_blobs, turbulence_gaussienne
 };
 
 // omega_0( X_0( ... X_{n-1}( X_cur(x) ) ) ) on the target grid, fused over a

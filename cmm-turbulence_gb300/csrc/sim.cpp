@@ -139,10 +139,6 @@ int EulerSim::alloc()
     }
     vlasov_ = s.simulation_type == "cmm_vlasov_poisson_1d";
     if (s.initial_condition_num < 0) { err = "unknown initial condition " + s.initial_condition; return kErrParam; }
-    if (!vlasov_ && s.initial_condition_num == 7 && !s.initial_discrete) {
-        err = "initial condition turbulence_gaussienne is not built (needs device cuRAND sequences)";
-        return kErrUnsupported;
-    }
     auto levels_needed = [](int ti) {
         // Lagrange levels a scheme reads (settings.cu time-integration table)
         switch (ti) {
@@ -242,7 +238,7 @@ int EulerSim::alloc()
     CMM_CUDA(cudaMalloc((void**)&spec_, sizeof(double2) * (size_t)cmax));
     CMM_CUDA(cudaMalloc((void**)&spec4_, sizeof(double2) * 4 * (size_t)cmax));
     if ((rc = dalloc(&red_, 3 * kReduceBlocks)) || (rc = dalloc(&d_scal_, 16)) || (rc = dalloc(&d_params_, 10)) ||
-        (rc = dalloc(&d_rand_, 1000)))
+        (rc = dalloc(&d_rand_, kInitTable)))
         return rc;
     CMM_CUDA(cudaMallocHost((void**)&h_scal_, sizeof(double) * 16));
     for (auto& p : s.particles_advected) {
@@ -310,7 +306,8 @@ int EulerSim::alloc()
     std::mt19937_64 gen(0);
     std::uniform_real_distribution<double> dist(-1.0, 1.0);
     for (auto& v : rnd) v = dist(gen);
-    CMM_CUDA(cudaMemcpyAsync(d_rand_, rnd.data(), sizeof(double) * 1000, cudaMemcpyHostToDevice, stream));
+    CMM_CUDA(cudaMemcpyAsync(d_rand_, rnd.data(), sizeof(double) * kRandTable, cudaMemcpyHostToDevice, stream));
+    CMM_LAUNCH(1, launch_gaussienne_offsets(d_rand_ + kRandTable, stream));
     CMM_CUDA(cudaMemcpyAsync(d_params_, s.initial_params, sizeof(double) * 10, cudaMemcpyHostToDevice, stream));
     CMM_CUDA(cudaStreamSynchronize(stream));
     return kOk;
@@ -1446,6 +1443,7 @@ size_t EulerSim::field_bytes(const std::string& n) const
     if (n == "Vorticity_W_coarse" || n == "Distribution_coarse") return sizeof(double) * gc.N;
     if (n == "Vorticity_W_fine_H") return sizeof(double) * 4 * gf.N;
     if (n == "Map_stack") return sizeof(double) * 8 * gc.N * n_maps_;
+    if (n == "Init_random_table") return sizeof(double) * kInitTable;
     for (size_t i = 0; i < s.particles_advected.size(); ++i) {
         std::string id = two((int)i + 1);
         if (n == "Particles_advected_pos_P" + id || n == "Particles_advected_vel_U" + id)
@@ -1474,6 +1472,7 @@ int EulerSim::get_field(const std::string& n, void* dst, size_t bytes)
     }
     else if (n == "Vorticity_W_coarse" || n == "Distribution_coarse") rc = cp(vort, bytes);
     else if (n == "Vorticity_W_fine_H") rc = cp(wfine, bytes);
+    else if (n == "Init_random_table") rc = cp(d_rand_, bytes);
     else if (n == "Map_stack" && !mixed_) rc = bytes ? cp(stack, bytes) : kOk;
     else if (n == "Map_stack") {
         // FP32 displacement maps -> the reference's planar X | Y layout, one map at a time

@@ -86,7 +86,10 @@ int cmm_run(cmm_ctx* ctx);
  * (L*4*Npsi), "Vorticity_W_coarse" (Nc; for Vlasov-Poisson the distribution,
  * also as "Distribution_coarse"), "Vorticity_W_fine_H" (4*Nf), "Map_stack"
  * (n_maps * 8*Nc, oldest first),
- * "Particles_advected_pos_PNN" (2*num), "Particles_advected_vel_UNN" (2*num).
+ * "Particles_advected_pos_PNN" (2*num), "Particles_advected_vel_UNN" (2*num: the
+ * velocity state of an inertial set, (psi_x, psi_y) at the particles of a tracer set),
+ * "Init_random_table" (1098: the 1000 uniform(-1,1) values of gaussian_blobs, then the
+ * 98 cuRAND blob offsets of turbulence_gaussienne).
  * bytes must equal the field size. */
 int cmm_get_field(cmm_ctx* ctx, const char* name, void* host_dst, size_t bytes);
 /* Size in bytes of a field (0 if unknown). */

@@ -78,6 +78,9 @@ void og_compose_sample(const double* ChiX, const double* ChiY, const double* sta
                        const og_grid* gt, int ic_num, const double* discrete, const og_grid* gd, double* out);
 /* d_init_vorticity "4_nodes": src/simulation/cmm-init.cu:45-52 */
 double og_init_vorticity(double x, double y, int ic_num);
+/* initial_params (10) and the random tables (1000 uniform(-1,1) then 98 turbulence_gaussienne
+ * offsets) that the analytic initial conditions read; NULL leaves one unchanged */
+void og_set_init_data(const double* params10, const double* table1098);
 /* k_apply_map_and_sample_from_hermite: src/simulation/cmm-simulation-kernel.cu:402-461 */
 void og_apply_map_and_sample_from_hermite(const double* ChiX, const double* ChiY, double* fs,
                                           const double* H, const og_grid* gmap, const og_grid* gvort,

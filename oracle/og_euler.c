@@ -253,13 +253,112 @@ void og_apply_map_compact(const double* ChiX, const double* ChiY, double* x_y, c
     }
 }
 
+/* inputs of the analytic initial conditions that are not formulas: initial_params, the
+ * 1000 uniform(-1, 1) values of mt19937_64 seed 0 (cmm-euler2d.cu:347-352) and the 98
+ * cuRAND blob offsets of turbulence_gaussienne (cmm-init.cu:148-160), given by the caller */
+static double og_params[10];
+static double og_rand[1000 + 98];
+
+void og_set_init_data(const double* params10, const double* table1098)
+{
+    if (params10) memcpy(og_params, params10, sizeof(og_params));
+    if (table1098) memcpy(og_rand, table1098, sizeof(og_rand));
+}
+
+/* d_init_vorticity: src/simulation/cmm-init.cu:30-241 */
 double og_init_vorticity(double x, double y, int ic)
 {
+    const double PI = OG_TWO_PI / 2, TP = OG_TWO_PI;
     switch (ic) {
-        case 0: /* 4_nodes, src/simulation/cmm-init.cu:45-52 */
-            x -= floor(x / OG_TWO_PI) * OG_TWO_PI;
-            y -= floor(y / OG_TWO_PI) * OG_TWO_PI;
+        case 0: /* 4_nodes :45-52 */
+            x -= floor(x / TP) * TP;
+            y -= floor(y / TP) * TP;
             return cos(x) + cos(y) + 0.6 * cos(2 * x) + 0.2 * cos(3 * x);
+        case 1: { /* quadropole :53-70, 5 x 5 periodic images */
+            double r = 0;
+            for (int iy = -2; iy <= 2; iy++)
+                for (int ix = -2; ix <= 2; ix++) {
+                    double dx = x - PI / 2 + ix * 2 * PI, dy = y - PI / 2 + iy * 2 * PI, s = 0.5;
+                    double B = 0.6258473 / (s * s * s * s) * (dx * dy) * (dx * dx + dy * dy - 6 * s * s);
+                    r += B * exp(-(dx * dx + dy * dy) / (2 * s * s));
+                }
+            return r;
+        }
+        case 2: { /* one_vortex :71-77 */
+            double sg = TP * 0.125;
+            return 1.0 / (TP * sg * sg) * exp(-((x - PI) * (x - PI) + (y - PI) * (y - PI)) / (2 * sg * sg));
+        }
+        case 3: case 4: { /* two_votices :78-89, three_vortices :90-109 (3 x 3 images) */
+            double r = 0, LX = PI / 2, LY = PI / (2.0 * sqrt(2.0));
+            for (int iy = -1; iy <= 1; iy++)
+                for (int ix = -1; ix <= 1; ix++) {
+                    double a = x + TP * ix, b = y + TP * iy, c = b + TP * iy;
+                    double env = sin(0.5 * a) * sin(0.5 * a) * sin(0.5 * c) * sin(0.5 * c), e;
+                    if (ic == 3)
+                        e = exp(-((a - PI) * (a - PI) + (b - 0.33 * TP) * (b - 0.33 * TP)) * 5) +
+                            exp(-((a - PI) * (a - PI) + (b - 0.67 * TP) * (b - 0.67 * TP)) * 5);
+                    else
+                        e = exp(-((a - PI - LX) * (a - PI - LX) + (b - PI) * (b - PI)) * 5) +
+                            exp(-((a - PI + LX) * (a - PI + LX) + (b - PI) * (b - PI)) * 5) -
+                            exp(-((a - PI + LX) * (a - PI + LX) + (b - PI - LY) * (b - PI - LY)) * 5);
+                    r += env * e;
+                }
+            return r;
+        }
+        case 5: /* single_shear_layer :110-117 */
+            return (1 + 0.01 * cos(2 * x)) * exp(-50.0 * (y - PI) * (y - PI));
+        case 6: { /* tanh_shear_layer :118-129 */
+            double d = 14 * 2 / TP, q = exp(-d * (y - PI)) + exp(d * (y - PI));
+            return 5.0 * (1 + 0.01 * cos(2 * x)) * 4 / q / q;
+        }
+        case 7: { /* turbulence_gaussienne :130-171 */
+            x -= floor(x / TP) * TP;
+            y -= floor(y / TP) * TP;
+            const int NB = 8;
+            double sg = 0.2, den = 2 * sg * sg, amp = 1 / (TP * sg * sg), r = 0;
+            for (int mx = 0; mx < NB; mx++)
+                for (int my = 0; my < NB; my++) {
+                    double ex = x - mx * TP / (NB - 1), ey = y - my * TP / (NB - 1);
+                    r += amp * exp(-(ex * ex / den + ey * ey / den));
+                }
+            for (int mx = 0; mx < NB - 1; mx++)
+                for (int my = 0; my < NB - 1; my++) {
+                    double ex = x - (2 * mx + 1) * TP / (2 * (NB - 1)) + og_rand[1000 + mx * (NB - 1) + my];
+                    double ey = y - (2 * my + 1) * TP / (2 * (NB - 1)) + og_rand[1049 + mx * (NB - 1) + my];
+                    r -= amp * exp(-(ex * ex / den + ey * ey / den));
+                }
+            return r - 0.008857380480028442;
+        }
+        case 8: { /* gaussian_blobs :172-203, alternating signs, 2-cell border of images */
+            x -= floor(x / TP) * TP;
+            y -= floor(y / TP) * TP;
+            const int NB = 10, border = 2;
+            double sg = TP * 0.01, off = TP * 0.005, r = 0;
+            int dir = 1;
+            for (int mx = -border; mx < 2 * NB + border; mx++) {
+                for (int my = -border; my < 2 * NB + border; my++) {
+                    int bn = (int)((mx - floor(mx / (double)(NB * 2)) * NB * 2) + (my - floor(my / (double)(NB * 2)) * NB * 2) * NB * 2);
+                    double ex = x - (mx + 0.5) * TP / (2 * NB) + og_rand[bn] * off;
+                    double ey = y - (my + 0.5) * TP / (2 * NB) + og_rand[bn + NB * NB * 4] * off;
+                    r += dir / (TP * sg * sg) * exp(-(ex * ex + ey * ey) / (2 * sg * sg));
+                    dir = -dir;
+                }
+                dir = -dir;
+            }
+            return r;
+        }
+        case 9: { /* shielded_vortex :207-219 */
+            double nu = 2e-1, xr = PI - x, yr = PI - y;
+            return 1 / (2 * nu * nu * nu) * (4 * nu - xr * xr - yr * yr) * exp(-(xr * xr + yr * yr) / (4 * nu));
+        }
+        case 10: /* two_cosine :220-226 */
+            x -= floor(x / TP) * TP;
+            y -= floor(y / TP) * TP;
+            return cos(x) * cos(y);
+        case 11: { /* vortex_sheets :228-234, delta = 1 / sqrt(initial_params[0]) */
+            double d = 1 / sqrt(og_params[0]), q = y - PI - sin(x) / 2.0;
+            return exp(-q * q / (2 * d * d)) / sqrt(2 * PI) / d;
+        }
         default: return 0.0;
     }
 }

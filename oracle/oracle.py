@@ -89,6 +89,7 @@ def lib():
         L.og_init.restype = C.c_int
         L.og_state_sample.argtypes = [C.c_void_p, C.c_int, C.c_int, dp, dp]
         L.og_vlasov_state_mesure.argtypes = [C.c_void_p, dp]
+        L.og_set_init_data.argtypes = [dp, dp]
         L.og_restart.argtypes = [C.c_void_p, C.c_double, C.c_int, dp, dp, dp, dp, dp]
         L.og_restart.restype = C.c_int
         for name in ("og_stack_x", "og_stack_y"):
@@ -153,6 +154,8 @@ class EulerOracle:
         self._s = s
         self.h = L.og_create(C.byref(s))
         self.L = L
+        if "initial_params" in cfg:
+            set_init_data(params=cfg["initial_params"])
 
     def close(self):
         if self.h:
@@ -304,6 +307,17 @@ class EulerOracle:
         self.L.og_vlasov_state_mesure(self.h, _dp(out))
         keys = ("Etot", "Ekin", "Epot", "Mass", "Momentum", "Emode1", "Emode2", "Emode3", "Emode4")
         return dict(zip(keys, out.tolist()))
+
+
+def set_init_data(params=None, table=None):
+    """initial_params (10 values) and the random table of the analytic initial conditions
+    (1000 uniform(-1, 1) values then the 98 turbulence_gaussienne offsets: the product's
+    "Init_random_table" field), shared by every oracle state of the process."""
+    p = None if params is None else np.ascontiguousarray(params, dtype=np.float64)
+    t = None if table is None else np.ascontiguousarray(table, dtype=np.float64)
+    if t is not None and t.size != 1098:
+        raise ValueError("the initial-condition table has 1098 values")
+    lib().og_set_init_data(None if p is None else _dp(p), None if t is None else _dp(t))
 
 
 # ---------------------------------------------------------------- MapStack folder

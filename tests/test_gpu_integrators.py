@@ -21,7 +21,7 @@ import pytest
 import refloop
 from oracle_adapter import OracleRun
 from product import cmm, read_monitoring
-from test_gpu_parity import map_err, rel_linf
+from test_gpu_parity import herm_err, map_err, rel_linf
 from test_gpu_vlasov import einc_tol
 
 pytestmark = pytest.mark.gpu
@@ -128,3 +128,40 @@ def test_mixed_form_follows_plain_fp64_for_every_scheme(tmp_path, map_ti, part_t
                           b.field("Particles_advected_pos_P%02d" % (i + 1))) < 1e-4
     v, w = a.field("Particles_advected_vel_U02"), b.field("Particles_advected_vel_U02")
     assert np.max(np.abs(v - w)) < 1e-4 * max(1.0, np.max(np.abs(v)))
+
+
+IC_EULER = ["4_nodes", "quadropole", "one_vortex", "two_votices", "three_vortices", "single_shear_layer",
+            "tanh_shear_layer", "turbulence_gaussienne", "gaussian_blobs", "shielded_vortex", "two_cosine",
+            "vortex_sheets"]
+
+
+@pytest.mark.parametrize("ic", IC_EULER)
+def test_every_analytic_initial_condition_matches_oracle(tmp_path, ic):
+    """Each analytic Euler initial condition (src/simulation/cmm-init.cu:30-241), composed
+    through the Lagrange start and 8 steps with remaps: fine and coarse vorticity and psi
+    against the oracle.  The oracle receives the product's random table (mt19937_64 values
+    for gaussian_blobs and the cuRAND blob offsets of turbulence_gaussienne, both library
+    draws, the latter checked here for its range and granularity)."""
+    m = cmm()
+    text = _param_text("RK3", [], final_time=0.125).replace(
+        "initial_condition\t=\t4_nodes", "initial_condition\t=\t%s" % ic) + "initial_params\t=\t{500,0,0,0,0,0,0,0,0,0}\n"
+    pf = tmp_path / "params.txt"
+    pf.write_text(text)
+    sim = m.Simulation(["param_file=%s" % pf, "workspace=%s/" % tmp_path])
+    sim.init()
+    table = sim.field("Init_random_table")
+    assert table.size == 1098 and np.all(np.abs(table[:1000]) <= 1)
+    off = table[1000:]
+    assert np.all(np.abs(off) <= 0.005) and np.allclose(off * 1e5, np.round(off * 1e5), atol=1e-6)
+    import oracle as O
+    O.set_init_data(table=table)
+    s = refloop.settings_from_param_text(text)
+    o = O.EulerOracle(s.oracle_config())
+    o.init()
+    assert herm_err(sim.field("Vorticity_W_fine_H"), o.vort_fine(), 128) < 1e-10
+    while sim.step(1) != 1:
+        o.step(1.0 / 64)
+    assert sim.scalar("map_counter") == o.map_count()
+    w, wo = sim.field("Vorticity_W_coarse"), o.vort()
+    assert np.max(np.abs(w - wo)) <= 1e-10 * np.max(np.abs(wo))
+    assert rel_linf(sim.field("Stream_function_Psi_H_psi"), o.psi()) < 1e-10

@@ -123,6 +123,8 @@ cudaError_t launch_spec_grad(const double2* F, const Grid& g, double2* out2, cud
 cudaError_t launch_compose_pos(const Grid& gm, const Grid& gt, const double* X, const double* Y, const double* stack,
                                int n_maps, double* px, double* py, cudaStream_t s);
 // an initial field at n positions (src.kind 0 vorticity, 1 scalar, 2 distribution, 3 discrete)
+// the Hermite field src.discrete (on src.gd) at the nodes of g
+cudaError_t launch_eval_grid(const Grid& g, const InitSource& src, double* out, cudaStream_t s);
 cudaError_t launch_eval_init(const double* px, const double* py, long long n, const InitSource& src, double* out,
                              cudaStream_t s);
 // normalised spectral operator on a D2Z half spectrum: 0 Laplacian, 1 d/dx, 2 d/dy, 3 inverse Laplacian

@@ -790,16 +790,31 @@ cudaError_t launch_spec_hermite_f(const float2* F, const Grid& g, float2* out4, 
     return cudaGetLastError();
 }
 
+// FP64 coordinate -> 64-bit fixed point of the periodic domain [b, b + W)
+__device__ __forceinline__ unsigned long long fix_from(double x, double b, double W)
+{
+    double t = (x - b) / W;
+    t -= floor(t);
+    const double v = t * 18446744073709551616.0;
+    return v >= 18446744073709551616.0 ? 0ull : __double2ull_rn(v);
+}
+
 // positions of the nodes of gt through the current map and the stack, at
-// fixed-point precision, returned as FP64 coordinates in [b0, b0 + W)
+// fixed-point precision, returned as FP64 coordinates in [b0, b0 + W).  gt spans
+// the map's domain (node i at i * stx exactly) or, with window set, any frame (its
+// nodes converted from FP64 coordinates)
 __global__ void __launch_bounds__(256) k_compose_pos_m(Grid gm, Grid gt, unsigned long long stx, unsigned long long sty,
                                                        float2 scx, float2 scy, const float4* __restrict__ map,
                                                        const float4* __restrict__ stack, int n_maps,
-                                                       double* __restrict__ px, double* __restrict__ py)
+                                                       double* __restrict__ px, double* __restrict__ py, bool window)
 {
     const int iX = blockIdx.x * blockDim.x + threadIdx.x, iY = blockIdx.y;
     if (iX >= gt.NX) return;
     unsigned long long Px = (unsigned long long)iX * stx, Py = (unsigned long long)iY * sty;
+    if (window) {
+        Px = fix_from(gt.b0 + iX * gt.hx, gm.b0, gm.Wx);
+        Py = fix_from(gt.b2 + iY * gt.hy, gm.b2, gm.Wy);
+    }
     int cx, cy;
     float tx, ty, dx, dy;
     fix_cell(Px, gm.NX, cx, tx);
@@ -822,10 +837,11 @@ __global__ void __launch_bounds__(256) k_compose_pos_m(Grid gm, Grid gt, unsigne
 cudaError_t launch_compose_pos_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
                                  double* px, double* py, cudaStream_t s)
 {
-    if (gt.b0 != gm.b0 || gt.b2 != gm.b2 || gt.Wx != gm.Wx || gt.Wy != gm.Wy || gt.NY > 65535) return cudaErrorInvalidValue;
+    if (gt.NY > 65535) return cudaErrorInvalidValue;
+    const bool window = gt.b0 != gm.b0 || gt.b2 != gm.b2 || gt.Wx != gm.Wx || gt.Wy != gm.Wy;
     dim3 blocks((unsigned)((gt.NX + 255) / 256), (unsigned)gt.NY);
     k_compose_pos_m<<<blocks, 256, 0, s>>>(gm, gt, fix_step(gt.NX), fix_step(gt.NY), fix_scale(gm.Wx), fix_scale(gm.Wy),
-                                           map, stack, n_maps, px, py);
+                                           map, stack, n_maps, px, py, window);
     return cudaGetLastError();
 }
 

@@ -62,6 +62,23 @@ cudaError_t launch_eval_init(const double* px, const double* py, long long n, co
     return cudaGetLastError();
 }
 
+// a Hermite field (src.discrete on src.gd) at the nodes of grid g (k_h_sample,
+// src/simulation/cmm-simulation-kernel.cu:122-135)
+__global__ void __launch_bounds__(256) k_eval_grid(Grid g, InitSource src, double* __restrict__ out)
+{
+    const int iX = blockIdx.x * blockDim.x + threadIdx.x, iY = blockIdx.y;
+    if (iX >= g.NX) return;
+    out[(long long)iY * g.NX + iX] = interp_value(src.discrete, src.gd, g.b0 + iX * g.hx, g.b2 + iY * g.hy);
+}
+
+cudaError_t launch_eval_grid(const Grid& g, const InitSource& src, double* out, cudaStream_t s)
+{
+    if (g.NY > 65535 || !src.discrete) return cudaErrorInvalidValue;
+    dim3 blocks((unsigned)((g.NX + 255) / 256), (unsigned)g.NY);
+    k_eval_grid<<<blocks, 256, 0, s>>>(g, src, out);
+    return cudaGetLastError();
+}
+
 // normalised spectral operator on a D2Z half spectrum: 0 Laplacian (k_fft_lap_h),
 // 1 d/dx, 2 d/dy (k_fft_dx_h, k_fft_dy_h), 3 inverse Laplacian (k_fft_iLap_h);
 // cmm-fft.cu:27-78,147-187,326-339

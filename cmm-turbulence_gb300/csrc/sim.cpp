@@ -1161,6 +1161,7 @@ int EulerSim::save_functions(double t_now, double dt_now)
     if ((rc = write_time_step(t_now, dt_now))) return rc;
     if ((rc = conservation(t_now, dt_now))) return rc;
     if ((rc = sample_outputs(t_now, dt_now))) return rc;
+    if ((rc = zoom_outputs(t_now, dt_now))) return rc;
     return kOk;
 }
 
@@ -1174,14 +1175,8 @@ int EulerSim::sample_outputs(double t_now, double dt_now)
         if (r.grid <= 0 || !instant_fires(r.is_instant, r.time_start, r.time_end, r.time_step, t_now, dt_now, dt)) continue;
         const int n = r.grid;
         Grid gs = make_grid(n, n, s.domain_bounds);
-        if (n > smp_n_) {
-            auto f = [](void* p) { if (p) cudaFree(p); };
-            for (auto& p : smp_) { f(p); p = nullptr; }
-            for (auto& p : smp_c_) { f(p); p = nullptr; }
-            for (auto& p : smp_) CMM_CUDA(cudaMalloc((void**)&p, sizeof(double) * (size_t)gs.N));
-            for (auto& p : smp_c_) CMM_CUDA(cudaMalloc((void**)&p, sizeof(double2) * (size_t)gs.Nfft));
-            smp_n_ = n;
-        }
+        int rb;
+        if ((rb = reserve_sample_buffers(n))) return rb;
         if (n != smp_plan_n_) {
             destroy_plans(ps_);
             smp_plan_n_ = 0;
@@ -1280,6 +1275,103 @@ int EulerSim::sample_outputs(double t_now, double dt_now)
             log_.push("Processed sample data on grid " + ns + ", Cons : Energ = " + to_str_prec(mes[0], 8) +
                       " \t Enstr = " + to_str_prec(mes[1], 8) + " \t Palinstr = " + to_str_prec(mes[2], 8) +
                       " \t Wmax = " + to_str_prec(mes[3], 8));
+    }
+    return kOk;
+}
+
+int EulerSim::reserve_sample_buffers(int n)
+{
+    if (n <= smp_n_) return kOk;
+    Grid g = make_grid(n, n, s.domain_bounds);
+    auto f = [](void* p) { if (p) cudaFree(p); };
+    for (auto& p : smp_) { f(p); p = nullptr; }
+    for (auto& p : smp_c_) { f(p); p = nullptr; }
+    smp_n_ = 0;
+    for (auto& p : smp_) CMM_CUDA(cudaMalloc((void**)&p, sizeof(double) * (size_t)g.N));
+    for (auto& p : smp_c_) CMM_CUDA(cudaMalloc((void**)&p, sizeof(double2) * (size_t)g.Nfft));
+    smp_n_ = n;
+    return kOk;
+}
+
+int EulerSim::zoom_outputs(double t_now, double dt_now)
+{
+    // compute_zoom, backward-map part (src/simulation/cmm-simulation-host.cu:1039-1201): for
+    // each firing zoom record, rep windows of half-width width/2 * rep_fac^k around
+    // (pos_x, pos_y); on each n x n window grid the full backward map, the passive scalar,
+    // the vorticity, the distribution function and psi sampled at the window points.
+    // Statistics use the spacing of the n x n grid over the whole domain, the reference's
+    // zoom variable's own grid.
+    if (vlasov_) return kOk;
+    bool synced = false;
+    for (size_t iz = 0; iz < s.save_zoom.size(); ++iz) {
+        auto& r = s.save_zoom[iz];
+        if (r.grid <= 0 || r.rep <= 0 || !instant_fires(r.is_instant, r.time_start, r.time_end, r.time_step, t_now, dt_now, dt))
+            continue;
+        const int n = r.grid;
+        int rc;
+        if ((rc = reserve_sample_buffers(n))) return rc;
+        if (!synced && mixed_) {
+            if ((rc = sync_fp64_views())) return rc;   // psi level 0 as FP64 planes
+            synced = true;
+        }
+        const Grid gstat = make_grid(n, n, s.domain_bounds);
+        const std::string ns = std::to_string(n), zs = "_Zoom_" + std::to_string(iz + 1), var = r.var;
+        const bool all = has(var, "All"), dbg = s.verbose >= 4;
+        const std::string tname = std::abs(t_now - kTMax) < 1 ? "final" : to_str3(t_now);
+        if (dbg) append_f64(run_dir(s) + "/Monitoring_data/Debug_globals/Time_s_" + ns + zs + ".data", &t_now, 1);
+        double wx = r.width_x / 2.0, wy = r.width_y / 2.0;
+        double *X = smp_[0], *Y = smp_[1], *V = smp_[2];
+        for (int rep = 0; rep < r.rep; ++rep) {
+            const double b[4] = {r.pos_x - wx, r.pos_x + wx, r.pos_y - wy, r.pos_y + wy};
+            const Grid gz = make_grid(n, n, b);
+            const std::string rs = zs + "_rep_" + std::to_string(rep);
+            const std::string sub = "/Zoom_data/Time_" + tname + "/Zoom_" + std::to_string(iz + 1) + "_rep_" + std::to_string(rep);
+            if (!dbg) {
+                make_dir(run_dir(s) + "/Zoom_data/Time_" + tname);
+                make_dir(run_dir(s) + sub);
+            }
+            auto out = [&](const std::string& name, const double* v) {
+                return dbg ? debug_globals(name + "_" + ns + rs, v, gz.N, true, gstat) : write_field(sub, name + "_" + ns, v, gz.N);
+            };
+            if (mixed_) CMM_LAUNCH(1, launch_compose_pos_m(gc, gz, mapm_, stackm_, n_maps_, X, Y, stream));
+            else CMM_LAUNCH(1, launch_compose_pos(gc, gz, ChiX, ChiY, stack, n_maps_, X, Y, stream));
+            if (has(var, "Map_b") || has(var, "Chi_b") || all)
+                if ((rc = out("Map_ChiX", X)) || (rc = out("Map_ChiY", Y))) return rc;
+            InitSource src{};
+            src.params = d_params_;
+            src.rand_table = d_rand_;
+            src.discrete = wdisc;
+            src.gd = gd;
+            if (has(var, "Scalar") || has(var, "Theta") || all) {
+                src.kind = 1;
+                src.ic_num = s.scalar_num;
+                CMM_LAUNCH(1, launch_eval_init(X, Y, gz.N, src, V, stream));
+                if ((rc = out("Scalar_Theta", V))) return rc;
+            }
+            src.ic_num = s.initial_condition_num;
+            if (has(var, "Vorticity") || has(var, "W") || all) {
+                src.kind = s.initial_discrete ? 3 : 0;
+                CMM_LAUNCH(1, launch_eval_init(X, Y, gz.N, src, V, stream));
+                if ((rc = out("Vorticity_W", V))) return rc;
+            }
+            if (has(var, "Dist") || has(var, "F") || all) {
+                // var 2 of k_h_sample_from_init: the distribution-function formula with this run's IC number
+                src.kind = s.initial_discrete ? 3 : 2;
+                CMM_LAUNCH(1, launch_eval_init(X, Y, gz.N, src, V, stream));
+                if ((rc = out("Distribution", V))) return rc;
+            }
+            if (has(var, "Stream") || has(var, "Psi") || all) {
+                InitSource ps{};
+                ps.kind = 3;
+                ps.discrete = psi[0];
+                ps.gd = gp;
+                CMM_LAUNCH(1, launch_eval_grid(gz, ps, V, stream));
+                if ((rc = out("Stream_function_Psi", V))) return rc;
+            }
+            wx *= r.rep_fac;
+            wy *= r.rep_fac;
+        }
+        if (s.verbose >= 3) log_.push("Processed zoom data " + std::to_string(iz + 1) + " on grid " + ns);
     }
     return kOk;
 }

@@ -102,6 +102,8 @@ private:
     int write_particles_state();
     int restart_from_map_stack();      // the restart branch of init (cmm-euler2d.cu:634-685)
     int sample_outputs(double t_now, double dt_now);   // sampled outputs on user grids
+    int zoom_outputs(double t_now, double dt_now);     // zoom windows (compute_zoom)
+    int reserve_sample_buffers(int n);                 // smp_ / smp_c_ for an n x n grid
     int evaluate_potential();          // Vlasov-Poisson psi from the distribution function
     int vlasov_setup_h();              // the periodification h(v), once per run
     int vlasov_mesure(double* out9);   // Etot, Ekin, Epot, Mass, Momentum, Emode1..4

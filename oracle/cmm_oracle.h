@@ -209,6 +209,8 @@ typedef struct {
     const double* discrete;         /* Hermite discrete initial vorticity or NULL */
     const og_grid* gd;
     int ic_num;
+    const double* psi;              /* psi level 0 (4*Np), for the zoom's psi samples */
+    const og_grid* gp;
 } og_state_view;
 /* sample_compute_and_write, backward part (cmm-simulation-host.cu:706-893) on grid gs:
  * out = 10 planes of gs->N: map X, map Y, scalar, W, Laplacian W, dW/dx, dW/dy, psi,
@@ -216,6 +218,11 @@ typedef struct {
  * Palinstrophy, Max_vorticity, Scalar_integral} with the reference's quirks */
 void og_sample_fields(const og_state_view* st, const og_grid* gs, int scalar_num, double* out, double* mes);
 void og_state_sample(const og_state* st, int n_sample, int scalar_num, double* out, double* mes);
+/* compute_zoom, backward part (cmm-simulation-host.cu:1039-1201) on an n x n window grid with
+ * bounds4 = (x_min, x_max, y_min, y_max): out = 6 planes of n*n: map X, map Y, scalar,
+ * vorticity, distribution function, psi level 0 at the window points */
+void og_zoom_fields(const og_state_view* st, int n, const double* bounds4, int scalar_num, double* out);
+void og_state_zoom(const og_state* st, int n, const double* bounds4, int scalar_num, double* out);
 
 /* ψ_x, ψ_y at particle positions (k_h_sample_points_dxdy, cmm-simulation-kernel.cu:138-155) */
 void og_sample_points_dxdy(const og_state* st, const double* pos, double* out, int num);

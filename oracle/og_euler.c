@@ -1043,10 +1043,8 @@ void og_vlasov_state_mesure(const og_state* st, double* out)
     og_vlasov_mesure(st->vort, &st->gc, st->psi, &st->gp, out);
 }
 
-void og_state_sample(const og_state* st, int n_sample, int scalar_num, double* out, double* mes)
+static og_state_view state_view(const og_state* st)
 {
-    og_grid gs;
-    og_grid_fill(&gs, n_sample, n_sample, st->gc.bounds);
     og_state_view v;
     v.gc = &st->gc;
     v.ChiX = st->ChiX; v.ChiY = st->ChiY;
@@ -1055,5 +1053,21 @@ void og_state_sample(const og_state* st, int n_sample, int scalar_num, double* o
     v.discrete = st->s.initial_discrete ? st->vort_disc : NULL;
     v.gd = &st->gd;
     v.ic_num = st->s.initial_condition_num;
+    v.psi = st->psi;
+    v.gp = &st->gp;
+    return v;
+}
+
+void og_state_sample(const og_state* st, int n_sample, int scalar_num, double* out, double* mes)
+{
+    og_grid gs;
+    og_grid_fill(&gs, n_sample, n_sample, st->gc.bounds);
+    og_state_view v = state_view(st);
     og_sample_fields(&v, &gs, scalar_num, out, mes);
+}
+
+void og_state_zoom(const og_state* st, int n, const double* bounds4, int scalar_num, double* out)
+{
+    og_state_view v = state_view(st);
+    og_zoom_fields(&v, n, bounds4, scalar_num, out);
 }

@@ -119,3 +119,33 @@ void og_sample_fields(const og_state_view* st, const og_grid* gs, int scalar_num
     mes[3] = wmax > -wmax ? wmax : -wmax;                          /* Max_vorticity */
     mes[4] = hh * tmax;                                            /* Scalar_integral */
 }
+
+/* compute_zoom, backward-map part (src/simulation/cmm-simulation-host.cu:1039-1201): on the
+ * n x n window grid with bounds (x_min, x_max, y_min, y_max) -- points x_min + i h, h the
+ * window width over n -- the full backward map through the stack, the passive scalar, the
+ * vorticity and the distribution function (the Vlasov formula with the run's initial-condition
+ * number, as k_h_sample_from_init with var 2 does) there, and psi level 0 interpolated at the
+ * window points themselves (k_h_sample).  out: 6 planes of n*n. */
+void og_zoom_fields(const og_state_view* st, int n, const double* bounds4, int scalar_num, double* out)
+{
+    og_grid gz;
+    og_grid_fill(&gz, n, n, bounds4);
+    const og_grid* gm = st->gc;
+    long N = gz.N;
+    double* xy = (double*)malloc(sizeof(double) * 2 * N);
+    og_sample_map_compact(st->ChiX, st->ChiY, xy, gm, &gz);
+    for (int i = st->n_maps - 1; i >= 0; i--)
+        og_apply_map_compact(st->stackX + 4 * gm->N * (size_t)i, st->stackY + 4 * gm->N * (size_t)i, xy, gm, &gz);
+    double *mapx = out, *mapy = out + N, *theta = out + 2 * N, *w = out + 3 * N, *f = out + 4 * N, *psi = out + 5 * N;
+    for (long i = 0; i < N; ++i) {
+        double x = xy[2 * i], y = xy[2 * i + 1];
+        mapx[i] = x;
+        mapy[i] = y;
+        theta[i] = og_init_scalar(x, y, scalar_num);
+        w[i] = st->discrete ? og_hermite_interpolate_2D(st->discrete, x, y, st->gd) : og_init_vorticity(x, y, st->ic_num);
+        f[i] = st->discrete ? og_hermite_interpolate_2D(st->discrete, x, y, st->gd) : og_init_distribution(x, y, st->ic_num);
+        long iX = i % gz.NX, iY = i / gz.NX;
+        psi[i] = og_hermite_interpolate_2D(st->psi, gz.bounds[0] + iX * gz.hx, gz.bounds[2] + iY * gz.hy, st->gp);
+    }
+    free(xy);
+}

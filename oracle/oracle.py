@@ -90,6 +90,7 @@ def lib():
         L.og_state_sample.argtypes = [C.c_void_p, C.c_int, C.c_int, dp, dp]
         L.og_vlasov_state_mesure.argtypes = [C.c_void_p, dp]
         L.og_set_init_data.argtypes = [dp, dp]
+        L.og_state_zoom.argtypes = [C.c_void_p, C.c_int, dp, C.c_int, dp]
         L.og_restart.argtypes = [C.c_void_p, C.c_double, C.c_int, dp, dp, dp, dp, dp]
         L.og_restart.restype = C.c_int
         for name in ("og_stack_x", "og_stack_y"):
@@ -299,6 +300,15 @@ class EulerOracle:
         planes = {k: out[i * n * n:(i + 1) * n * n].copy() for i, k in enumerate(names)}
         return planes, dict(zip(("Energy", "Enstrophy", "Palinstrophy", "Max_vorticity", "Scalar_integral"),
                                 mes.tolist()))
+
+    def zoom(self, n, bounds, scalar_num):
+        """compute_zoom planes on an n x n window (bounds = x_min, x_max, y_min, y_max):
+        dict Map_ChiX, Map_ChiY, Scalar_Theta, Vorticity_W, Distribution, Stream_function_Psi."""
+        out = np.zeros(6 * n * n)
+        b = np.ascontiguousarray(bounds[:4], dtype=np.float64)
+        self.L.og_state_zoom(self.h, n, _dp(b), scalar_num, _dp(out))
+        names = ("Map_ChiX", "Map_ChiY", "Scalar_Theta", "Vorticity_W", "Distribution", "Stream_function_Psi")
+        return {k: out[i * n * n:(i + 1) * n * n].copy() for i, k in enumerate(names)}
 
     def vlasov_mesure(self):
         """{Etot, Ekin, Epot, Mass, Momentum, Emode1..4} of the current state

@@ -23,6 +23,10 @@ TESTS = {
                   "tests/euler2D_init_fields/params_conv.txt"),
     "init_particles": ("tests/euler2D_init_fields/data/reference-results_particles_4_nodes_C256_F512_t1_T0",
                        "tests/euler2D_init_fields/params_particles.txt"),
+    "init_zoom": ("tests/euler2D_init_fields/data/reference-results_zoom_4_nodes_C256_F512_t1_T0",
+                  "tests/euler2D_init_fields/params_zoom.txt"),
+    "init_forward": ("tests/euler2D_init_fields/data/reference-results_forward_4_nodes_C256_F512_t1_T0",
+                     "tests/euler2D_init_fields/params_forward.txt"),
     "init_sample": ("tests/euler2D_init_fields/data/reference-results_sample_4_nodes_C256_F512_t1_T0",
                     "tests/euler2D_init_fields/params_sample.txt"),
     "one_step": ("tests/euler2D_one_step/data/reference-results_4_nodes_C256_F512_t1_T1",

@@ -155,6 +155,38 @@ class DebugRecorder:
                 for k in ("Energy", "Enstrophy", "Palinstrophy", "Max_vorticity"):
                     self._app("Mesure/%s_%d" % (k, n), [mes[k]])
 
+        # compute_zoom (cmm-simulation-host.cu:1039-1201), backward-map part: statistics with
+        # the spacing of an n x n grid over the whole domain (the zoom variable's own grid)
+        if s.simulation_type_num != 2:
+            for iz, r in enumerate(s.save_zoom):
+                if not save_instant([r], t_now, dt_now, dt):
+                    continue
+                n, var = r.grid, r.var
+                all_ = "All" in var
+                b = s.domain_bounds
+                hx, hy = (b[1] - b[0]) / n, (b[3] - b[2]) / n
+                self._app("Debug_globals/Time_s_%d_Zoom_%d" % (n, iz + 1), [t_now])
+                wx, wy = r.width_x / 2.0, r.width_y / 2.0
+                for rep in range(r.rep):
+                    win = (r.pos_x - wx, r.pos_x + wx, r.pos_y - wy, r.pos_y + wy)
+                    planes = st.zoom(n, win, s.scalar_num)
+
+                    def stat(name):
+                        self._stat("%s_%d_Zoom_%d_rep_%d" % (name, n, iz + 1, rep), stats_grid(planes[name], hx, hy))
+                    if _has(var, "Map_b", "Chi_b") or all_:
+                        stat("Map_ChiX")
+                        stat("Map_ChiY")
+                    if _has(var, "Scalar", "Theta") or all_:
+                        stat("Scalar_Theta")
+                    if _has(var, "Vorticity", "W") or all_:
+                        stat("Vorticity_W")
+                    if _has(var, "Dist", "F") or all_:
+                        stat("Distribution")
+                    if _has(var, "Stream", "Psi") or all_:
+                        stat("Stream_function_Psi")
+                    wx *= r.rep_fac
+                    wy *= r.rep_fac
+
     def on_step(self, loop_ctr, t, e_inc, gap, maps):
         self._app("Time_s", [t])
         self._app("Error_incompressibility", [e_inc])

@@ -69,3 +69,6 @@ class OracleRun:
 
     def sample(self, n, scalar_num):
         return self.o.sample(n, scalar_num)
+
+    def zoom(self, n, bounds, scalar_num):
+        return self.o.zoom(n, bounds, scalar_num)

@@ -62,6 +62,9 @@ class SaveRec:
         self.var = ""
         self.conv = False
         self.grid = 0
+        self.pos_x = self.pos_y = self.width_x = self.width_y = 0.0
+        self.rep = 0
+        self.rep_fac = 0.0
         for k, v in _record(text).items():
             if k == "is_instant": self.is_instant = _bool(v)
             elif k == "time_start": self.time_start = float(v)
@@ -70,6 +73,8 @@ class SaveRec:
             elif k == "var": self.var = v
             elif k == "conv" and kind == "comp": self.conv = _bool(v)
             elif k == "grid" and kind != "comp": self.grid = int(v)
+            elif kind == "zoom" and k in ("pos_x", "pos_y", "width_x", "width_y", "rep_fac"): setattr(self, k, float(v))
+            elif kind == "zoom" and k == "rep": self.rep = int(float(v))
 
 
 class PartRec:

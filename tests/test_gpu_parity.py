@@ -245,7 +245,7 @@ def test_c1_full_run_matches_oracle_field_by_field(tmp_path, threshold):
         assert abs(sim.scalar(name) - ref) <= 1e-11 * abs(ref), name
 
 
-@pytest.mark.parametrize("name", ["init_sample", "init_particles", "one_step", "remap_11b"])
+@pytest.mark.parametrize("name", ["init_sample", "init_particles", "init_zoom", "one_step", "remap_11b"])
 def test_reference_goldens_through_the_cli_interface(tmp_path, name):
     """The product, configured by the reference's own param file, writes the
     reference's monitoring files; they match every golden series, including the
@@ -267,3 +267,43 @@ def test_reference_goldens_through_the_cli_interface(tmp_path, name):
     assert not fails, fails          # a series missing from ours is a failure too
     if "Map_counter" in g["files"]:   # absent for the t = 0 initialisation goldens
         assert ours["Map_counter"] == g["files"]["Map_counter"]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_zoom_windows_through_remaps_match_oracle(tmp_path, precision):
+    """Zoom windows (compute_zoom) off the domain's origin, three repetitions, every
+    1/8 time unit of a run with remaps: every Debug_globals series of the zoomed map,
+    scalar, vorticity, distribution and psi against the oracle's restatement (plain
+    FP64 to 1e-9 of the data's magnitude; the mixed form to 1e-5)."""
+    m = cmm()
+    text = "\n".join([
+        "CMM Parameter file", "param_version\t=\t3", "",
+        "simulation_type\t=\tcmm_euler_2d", "sim_name\t=\tzoom", "initial_condition\t=\t4_nodes",
+        "grid_coarse\t=\t64", "grid_fine\t=\t128", "grid_vort\t=\t128", "grid_psi\t=\t64",
+        "set_dt_by_steps\t=\t1", "steps_per_sec\t=\t64", "final_time\t=\t0.25", "time_integration\t=\tRK3",
+        "map_update_order\t=\t4th", "map_epsilon\t=\t0.001", "incomp_threshold\t=\t%s" % (
+            "1e-05" if precision == "fp64" else "0.001"),
+        "skip_remapping\t=\t0", "molly_stencil\t=\t0", "lagrange_init_higher_order\t=\t1",
+        "freq_cut_psi\t=\t32", "mem_RAM_CPU_remaps\t=\t100", "save_map_stack\t=\t0", "verbose\t=\t4",
+        "precision\t=\t%s" % precision, "save_computational_num\t=\t0", "save_sample_num\t=\t0",
+        "scalar_name\t=\tgaussian", "particles_advected_num\t=\t0", "save_zoom_num\t=\t1",
+        "save_zoom\t=\t{is_instant=0,time_start=0,time_end=10000,time_step=0.125,var=All,grid=96,pos_x=1.3,"
+        "pos_y=5.9,width_x=3.5,width_y=2.5,rep=3,rep_fac=0.5}", ""])
+    pf = tmp_path / "params.txt"
+    pf.write_text(text)
+    sim = m.Simulation(["param_file=%s" % pf, "workspace=%s/" % tmp_path])
+    sim.init()
+    sim.run()
+    ours = read_monitoring(os.path.join(str(tmp_path), "data", sim.file_name()))
+    s = refloop.settings_from_param_text(text.replace("precision\t=\tmixed", "precision\t=\tfp64"))
+    from oracle_adapter import OracleRun
+    run = OracleRun(s)
+    rec = DebugRecorder(s, run)
+    refloop.run_reference_loop(s, run, rec.on_save, rec.on_step)
+    keys = [k for k in rec.series if "Zoom" in k]
+    assert len(keys) == 1 + 3 * 6 * 4
+    if precision == "fp64":
+        assert max(rec.series["Map_counter"]) >= 1
+    worst, fails = compare_series(ours, rec.series, keys, 1e-9 if precision == "fp64" else 1e-5)
+    assert not fails, fails
+

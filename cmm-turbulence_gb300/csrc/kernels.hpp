@@ -27,12 +27,16 @@ struct AdvectArgs {
     int time_integration_num;            // 10 EulerExp, 21 RK2 (Heun), 20 AB2, 30 RK3, 40 RK4, 31 RK3Mod, 41 RK4Mod
     int l_order;                         // Lagrange levels used (1..4)
     int nfoot;                           // 4, 8 or 12 footpoints
+    int direction;                       // -1 backward map (default), 1 forward map
 };
 
 void map_update_coefficients(int order_num, double ep, double coef[4][kMaxFoot], int* nfoot);
 
 cudaError_t launch_init_map(double* X, double* Y, const Grid& g, cudaStream_t s);
 cudaError_t launch_advect(const AdvectArgs& a, cudaStream_t s);
+// max |x - X_b(X_f(x))| over the half-shifted nodes of gc -> *d_result (forward map check)
+cudaError_t launch_invert(const Grid& gc, const Grid& gm, const double* Xb, const double* Yb, const double* Xf,
+                          const double* Yf, double* d_result, cudaStream_t s);
 // max |1 - det grad X| over the half-shifted check grid -> *d_result (double);
 // d_result is reset by the launcher
 cudaError_t launch_incomp(const Grid& gcheck, const Grid& gmap, const double* X, const double* Y,
@@ -122,6 +126,13 @@ cudaError_t launch_spec_grad(const double2* F, const Grid& g, double2* out2, cud
 // positions of the nodes of gt through the current map and n_maps stacked maps (wrapped)
 cudaError_t launch_compose_pos(const Grid& gm, const Grid& gt, const double* X, const double* Y, const double* stack,
                                int n_maps, double* px, double* py, cudaStream_t s);
+// nodes of gt through the forward stack (oldest first) and then the active forward map
+cudaError_t launch_compose_fwd(const Grid& gm, const Grid& gt, const double* X, const double* Y, const double* stack,
+                               int n_maps, double* px, double* py, cudaStream_t s);
+// num points (x, y interleaved) through one map; NaN for points not strictly inside the
+// frame (x_min, x_max, y_min, y_max)
+cudaError_t launch_map_points(const Grid& gm, const double* frame, const double* X, const double* Y, const double* in,
+                              double* out, int num, cudaStream_t s);
 // an initial field at n positions (src.kind 0 vorticity, 1 scalar, 2 distribution, 3 discrete)
 // the Hermite field src.discrete (on src.gd) at the nodes of g
 cudaError_t launch_eval_grid(const Grid& g, const InitSource& src, double* out, cudaStream_t s);

@@ -140,11 +140,69 @@ __device__ __forceinline__ void integrate_back(const AdvectArgs& a, double x, do
     }
 }
 
+// forward integrators for the forward map (src/numerical/cmm-timestep.cu: :26-31
+// euler_exp, :48-64 RK2_heun, :84-110 adam_bashford_2_pc, :144-173 RK3_classical,
+// :216-258 RK4_classical, :314-339 RK3_optimized, :385-420 RK4_optimized): from the
+// footpoint's current position forward over dt.  Kept as the reference has them:
+// RK4_classical's first half-step velocity is the t_{n+1} extrapolation and its last
+// stage the t_{n+1/2} one, and RK4_optimized is the backward scheme.
+template <int L, int TI>
+__device__ __forceinline__ void integrate_fwd(const AdvectArgs& a, double x, double y, double& xo, double& yo)
+{
+    const double dt = a.dt;
+    if (TI == 41) { integrate_back<L, 41>(a, x, y, xo, yo); return; }
+    if (TI == 20) {
+        double px = x, py = y, ox = x, oy = y, u2x, u2y, ux, uy;
+        for (int it = 0; it < 10; ++it) {
+            vel_level(a, 1, px, py, u2x, u2y);
+            px = ox + dt * u2x;
+            py = oy + dt * u2y;
+            vel_level(a, 1, px, py, u2x, u2y);
+            vel_level(a, 0, ox, oy, ux, uy);
+            ox = x + dt * (1.5 * ux - 0.5 * u2x);
+            oy = y + dt * (1.5 * uy - 0.5 * u2y);
+        }
+        xo = ox;
+        yo = oy;
+        return;
+    }
+    double k1x, k1y;
+    vel_level(a, 0, x, y, k1x, k1y);
+    if (TI == 10) {
+        xo = x + dt * k1x;
+        yo = y + dt * k1y;
+    } else if (TI == 21) {
+        double k2x, k2y;
+        vel_comb<L>(a, a.L1, x + dt * k1x, y + dt * k1y, k2x, k2y);
+        xo = x + dt * (k1x + k2x) / 2;
+        yo = y + dt * (k1y + k2y) / 2;
+    } else if (TI == 30) {
+        double k2x, k2y, k3x, k3y;
+        vel_comb<L>(a, a.L12, x + dt * k1x / 2.0, y + dt * k1y / 2.0, k2x, k2y);
+        vel_comb<L>(a, a.L1, x - dt * k1x + 2 * dt * k2x, y - dt * k1y + 2 * dt * k2y, k3x, k3y);
+        xo = x + dt * (k1x + 4 * k2x + k3x) / 6.0;
+        yo = y + dt * (k1y + 4 * k2y + k3y) / 6.0;
+    } else if (TI == 40) {
+        double k2x, k2y, k3x, k3y, k4x, k4y;
+        vel_comb<L>(a, a.L1, x + dt * k1x / 2.0, y + dt * k1y / 2.0, k2x, k2y);
+        vel_comb<L>(a, a.L12, x + dt * k2x / 2.0, y + dt * k2y / 2.0, k3x, k3y);
+        vel_comb<L>(a, a.L12, x + dt * k3x, y + dt * k3y, k4x, k4y);
+        xo = x + dt * (k1x + 2 * k2x + 2 * k3x + k4x) / 6.0;
+        yo = y + dt * (k1y + 2 * k2y + 2 * k3y + k4y) / 6.0;
+    } else {   // 31
+        double k2x, k2y, k3x, k3y;
+        vel_level(a, 1, x - dt * k1x, y - dt * k1y, k2x, k2y);
+        vel_level(a, 2, x - dt * (8 * k1x + 2 * k2x) / 5.0, y - dt * (8 * k1y + 2 * k2y) / 5.0, k3x, k3y);
+        xo = x + dt * (23 * k1x - 16 * k2x + 5 * k3x) / 12.0;
+        yo = y + dt * (23 * k1y - 16 * k2y + 5 * k3y) / 12.0;
+    }
+}
+
 // One lane per (node, footpoint); LPN lanes per node (power of two >= nfoot).
 // Lanes 0..7 of each group combine the footpoints into the 8 output planes
 // [X, X_x, X_y, X_xy, Y, Y_x, Y_y, Y_xy] with the same sequential
 // multiply-add order as the reference's accumulation (:280-289).
-template <int L, int TI>
+template <int L, int TI, bool FWD>
 __global__ void __launch_bounds__(256) k_advect(const AdvectArgs a, int lpn_log2)
 {
     __shared__ double sc[4][kMaxFoot];
@@ -165,9 +223,17 @@ __global__ void __launch_bounds__(256) k_advect(const AdvectArgs a, int lpn_log2
         double r = (double)((k >> 2) + 1) * a.ep;
         double x = a.gm.b0 + iX * a.gm.hx + r * (1 - 2 * ((k >> 1) & 1));
         double y = a.gm.b2 + iY * a.gm.hy + r * (1 - 2 * (((k + 1) >> 1) & 1));
-        double xb, yb;
-        integrate_back<L, TI>(a, x, y, xb, yb);
-        map_value(a.ChiX, a.ChiY, a.gm, xb, yb, xf, yf);
+        if (FWD) {
+            // forward map: the footpoint's image under the map, carried forward over dt
+            double mx, my;
+            map_value(a.ChiX, a.ChiY, a.gm, x, y, mx, my);
+            integrate_fwd<L, TI>(a, mx, my, xf, yf);
+        } else {
+            // backward map: the footpoint carried back over dt, then looked up in the map
+            double xb, yb;
+            integrate_back<L, TI>(a, x, y, xb, yb);
+            map_value(a.ChiX, a.ChiY, a.gm, xb, yb, xf, yf);
+        }
     }
     // gather the footpoints of this node in every lane of the group
     const int comp = (k >> 2) & 1, plane = k & 3;
@@ -190,7 +256,11 @@ cudaError_t launch_advect(const AdvectArgs& a, cudaStream_t s)
     long long total = a.gm.N * lpn;
     int threads = 256;
     unsigned blocks = (unsigned)((total + threads - 1) / threads);
-#define CMM_ADV(LL, TT) k_advect<LL, TT><<<blocks, threads, 0, s>>>(a, lpn_log2)
+#define CMM_ADV(LL, TT)                                                          \
+    do {                                                                          \
+        if (a.direction == 1) k_advect<LL, TT, true><<<blocks, threads, 0, s>>>(a, lpn_log2);   \
+        else k_advect<LL, TT, false><<<blocks, threads, 0, s>>>(a, lpn_log2);     \
+    } while (0)
     switch (a.time_integration_num * 10 + a.l_order) {
         case 101: CMM_ADV(1, 10); break;
         case 102: CMM_ADV(2, 10); break;
@@ -249,6 +319,50 @@ __global__ void __launch_bounds__(256) k_incomp(Grid gc, Grid gm, const double* 
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = wmax[w] > m ? wmax[w] : m;
         atomicMax(result, m);
     }
+}
+
+// max over the half-shifted check grid of |x - X_b(X_f(x))| (k_invertibility_check,
+// src/simulation/cmm-simulation-kernel.cu:177-198), fused with its reduction
+__global__ void __launch_bounds__(256) k_invert(Grid gc, Grid gm, const double* __restrict__ Xb,
+                                                const double* __restrict__ Yb, const double* __restrict__ Xf,
+                                                const double* __restrict__ Yf, unsigned long long* result)
+{
+    __shared__ unsigned long long wmax[8];
+    unsigned long long best = 0ull;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < gc.N;
+         i += (long long)gridDim.x * blockDim.x) {
+        int iX = (int)(i % gc.NX), iY = (int)(i / gc.NX);
+        double x = gc.b0 + iX * gc.hx + 0.5 * gc.hx;
+        double y = gc.b2 + iY * gc.hy + 0.5 * gc.hy;
+        double a, b, c, d;
+        map_value(Xf, Yf, gm, x, y, a, b);
+        map_value(Xb, Yb, gm, a, b, c, d);
+        double e = hypot(x - c, y - d);
+        unsigned long long v = (unsigned long long)__double_as_longlong(e);
+        best = v > best ? v : best;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long v = __shfl_xor_sync(0xffffffffu, best, o);
+        best = v > best ? v : best;
+    }
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = best;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long m = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = wmax[w] > m ? wmax[w] : m;
+        atomicMax(result, m);
+    }
+}
+
+cudaError_t launch_invert(const Grid& gc, const Grid& gm, const double* Xb, const double* Yb, const double* Xf,
+                          const double* Yf, double* d_result, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(d_result, 0, sizeof(double), s);
+    if (e != cudaSuccess) return e;
+    long long need = (gc.N + 255) / 256;
+    unsigned blocks = (unsigned)(need < 152 * 16 ? need : 152 * 16);
+    k_invert<<<blocks, 256, 0, s>>>(gc, gm, Xb, Yb, Xf, Yf, reinterpret_cast<unsigned long long*>(d_result));
+    return cudaGetLastError();
 }
 
 cudaError_t launch_incomp(const Grid& gc, const Grid& gm, const double* X, const double* Y, double* d_result,

@@ -44,6 +44,63 @@ cudaError_t launch_compose_pos(const Grid& gm, const Grid& gt, const double* X, 
     return cudaGetLastError();
 }
 
+// forward composition (apply_map_stack, direction 1, cmm-simulation-host.cu:130-152): the nodes
+// of gt through the forward stack oldest first, then the active forward map, wrapped after each
+__global__ void __launch_bounds__(256) k_compose_fwd(Grid gm, Grid gt, const double* __restrict__ X,
+                                                     const double* __restrict__ Y, const double* __restrict__ stack,
+                                                     int n_maps, double* __restrict__ px, double* __restrict__ py)
+{
+    const int iX = blockIdx.x * blockDim.x + threadIdx.x, iY = blockIdx.y;
+    if (iX >= gt.NX) return;
+    double x = gt.b0 + iX * gt.hx, y = gt.b2 + iY * gt.hy, xo, yo;
+    for (int m = 0; m <= n_maps; ++m) {
+        const double* MX = m < n_maps ? stack + (long long)m * 8 * gm.N : X;
+        const double* MY = m < n_maps ? MX + 4 * gm.N : Y;
+        map_value(MX, MY, gm, x, y, xo, yo);
+        x = wrap(xo, gm.b0, gm.Wx);
+        y = wrap(yo, gm.b2, gm.Wy);
+    }
+    const long long i = (long long)iY * gt.NX + iX;
+    px[i] = x;
+    py[i] = y;
+}
+
+cudaError_t launch_compose_fwd(const Grid& gm, const Grid& gt, const double* X, const double* Y, const double* stack,
+                               int n_maps, double* px, double* py, cudaStream_t s)
+{
+    if (gt.NY > 65535) return cudaErrorInvalidValue;
+    dim3 blocks((unsigned)((gt.NX + 255) / 256), (unsigned)gt.NY);
+    k_compose_fwd<<<blocks, 256, 0, s>>>(gm, gt, X, Y, stack, n_maps, px, py);
+    return cudaGetLastError();
+}
+
+// points through one map (k_h_sample_points_map, cmm-simulation-kernel.cu:97-118): a point
+// strictly inside the frame is mapped and wrapped by the domain width (floor(x / L) L, the
+// reference's wrap), any other point becomes NaN; in and out may alias
+__global__ void k_map_points(Grid gm, double f0, double f1, double f2, double f3, const double* __restrict__ X,
+                             const double* __restrict__ Y, const double* in, double* out, int num)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= num) return;
+    const double x = in[2 * i], y = in[2 * i + 1];
+    if (x > f0 && x < f1 && y > f2 && y < f3) {
+        double a, b;
+        map_value(X, Y, gm, x, y, a, b);
+        out[2 * i] = a - floor(a / gm.Wx) * gm.Wx;
+        out[2 * i + 1] = b - floor(b / gm.Wy) * gm.Wy;
+    } else {
+        out[2 * i] = out[2 * i + 1] = __longlong_as_double(0x7ff8000000000000ll);
+    }
+}
+
+cudaError_t launch_map_points(const Grid& gm, const double* frame, const double* X, const double* Y, const double* in,
+                              double* out, int num, cudaStream_t s)
+{
+    if (num <= 0) return cudaSuccess;
+    k_map_points<<<(num + 255) / 256, 256, 0, s>>>(gm, frame[0], frame[1], frame[2], frame[3], X, Y, in, out, num);
+    return cudaGetLastError();
+}
+
 // an initial field (analytic kind 0/1/2, or the discrete Hermite field, kind 3) at given positions
 __global__ void __launch_bounds__(256) k_eval_init(const double* __restrict__ px, const double* __restrict__ py,
                                                    long long n, InitSource src, double* __restrict__ out)

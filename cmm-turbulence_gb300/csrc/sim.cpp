@@ -154,7 +154,10 @@ int EulerSim::alloc()
         return kErrParam;
     }
     if (s.map_update_order_num < 0) { err = "unknown map_update_order " + s.map_update_order; return kErrParam; }
-    if (s.forward_map) { err = "forward_map is not built"; return kErrUnsupported; }
+    if (s.forward_map && s.precision == "mixed") {
+        err = "forward_map is built for the plain FP64 form (precision=fp64)";
+        return kErrUnsupported;
+    }
     if (s.grid_coarse <= 0 || s.grid_fine <= 0 || s.grid_psi <= 0 || s.grid_vort <= 0) { err = "grid sizes must be positive"; return kErrParam; }
 
     dt = s.dt();
@@ -230,8 +233,21 @@ int EulerSim::alloc()
         return rc;
     for (int l = 0; l < L; ++l) if ((rc = dalloc(&psi[l], 4 * gp.N))) return rc;
     if (s.initial_discrete && (rc = dalloc(&wdisc, 4 * gd.N))) return rc;
+    if (s.forward_map) {
+        if ((rc = dalloc(&ChiX_f, 4 * gc.N)) || (rc = dalloc(&ChiY_f, 4 * gc.N))) return rc;
+        for (auto& p : s.particles_forwarded) {
+            double* d = nullptr;
+            if ((rc = dalloc(&d, 2ll * std::max(p.num, 1)))) return rc;
+            fparts_.push_back(d);
+        }
+        init_map_.assign(s.particles_forwarded.size(), 0);
+        long long tot = 0;
+        for (auto& p : s.particles_forwarded) tot += std::max(p.num, 0);
+        if ((rc = dalloc(&fpos_, 2 * std::max(tot, 1ll)))) return rc;
+    }
     stack_cap_ = std::max(0, std::min(max_maps, 16));
     if (!mixed_ && stack_cap_ > 0 && (rc = dalloc(&stack, 8 * gc.N * stack_cap_))) return rc;
+    if (s.forward_map && stack_cap_ > 0 && (rc = dalloc(&stack_f, 8 * gc.N * stack_cap_))) return rc;
     long long rmax = std::max({gf.N, gv.N, gd.N, gc.N, gp.N});
     long long cmax = std::max({gf.Nfft, gv.Nfft, gd.Nfft, gc.Nfft, gp.Nfft});
     if ((rc = dalloc(&real_buf_, rmax))) return rc;
@@ -317,6 +333,10 @@ void EulerSim::release()
 {
     auto f = [](void* p) { if (p) cudaFree(p); };
     f(ChiX); f(ChiY); f(ChiX_new); f(ChiY_new); f(vort); f(wfine); f(wdisc); f(stack);
+    f(ChiX_f); f(ChiY_f); f(stack_f); f(fpos_);
+    ChiX_f = ChiY_f = stack_f = fpos_ = nullptr;
+    for (auto p : fparts_) f(p);
+    fparts_.clear();
     for (int l = 0; l < kMaxLagrange; ++l) f(psi[l]);
     f(real_buf_); f(spec_); f(spec4_); f(red_); f(d_scal_); f(d_params_); f(d_rand_);
     for (auto p : parts) f(p);
@@ -599,6 +619,78 @@ int EulerSim::advect(const double* t, const double* dtv, int lc, int ti_num, int
     return kOk;
 }
 
+int EulerSim::forward_step(int lcl, bool* forced_remap)
+{
+    // the forward map's part of a step (cmm-euler2d.cu:780-811): advect_using_stream_hermite
+    // with direction 1 on the same psi history, then the invertibility check X_b(X_f(x)) ~ x
+    // and the incompressibility check on the coarse grid, and a forced remap in the step
+    // that reaches a forwarded set's start time (its particles are mapped from the sub-map
+    // after that remap on)
+    *forced_remap = false;
+    if (!s.forward_map) return kOk;
+    AdvectArgs a{};
+    a.gm = gc; a.gp = gp;
+    a.ChiX = ChiX_f; a.ChiY = ChiY_f; a.outX = ChiX_new; a.outY = ChiY_new;
+    for (int l = 0; l < kMaxLagrange; ++l) a.psi[l] = psi[l];
+    for (int i = 0; i < L; ++i) {
+        a.L1[i] = lagrange_coefficient(t_vec_.data(), t_vec_[lcl + 1], lcl, i, L);
+        a.L12[i] = lagrange_coefficient(t_vec_.data(), t_vec_[lcl] + dt_vec_[lcl + 1] / 2.0, lcl, i, L);
+    }
+    map_update_coefficients(s.map_update_order_num, s.map_epsilon, a.coef, &a.nfoot);
+    a.dt = dt_vec_[lcl + 1];
+    a.ep = s.map_epsilon;
+    a.time_integration_num = s.time_integration_num;
+    a.l_order = L;
+    a.direction = 1;
+    CMM_LAUNCH(1, launch_advect(a, stream));
+    std::swap(ChiX_f, ChiX_new);
+    std::swap(ChiY_f, ChiY_new);
+    CMM_LAUNCH(1, launch_invert(gc, gc, ChiX, ChiY, ChiX_f, ChiY_f, d_scal_ + 14, stream));
+    CMM_LAUNCH(1, launch_incomp(gc, gc, ChiX_f, ChiY_f, d_scal_ + 15, stream));
+    CMM_CUDA(cudaMemcpyAsync(h_scal_ + 14, d_scal_ + 14, sizeof(double) * 2, cudaMemcpyDeviceToHost, stream));
+    CMM_CUDA(cudaStreamSynchronize(stream));
+    e_inv_ = h_scal_[14];
+    e_inc_f_ = h_scal_[15];
+    for (size_t i = 0; i < s.particles_forwarded.size(); ++i) {
+        double d = t_vec_[lcl + 1] - s.particles_forwarded[i].init_time + dt * 1e-5;
+        if (d < dt_vec_[lcl + 1] && d >= 0) {
+            *forced_remap = true;
+            init_map_[i] = n_maps_ + 1;
+        }
+    }
+    return kOk;
+}
+
+int EulerSim::forwarded_positions(const double* frame, double* out)
+{
+    // apply_map_stack_points, direction 1 (cmm-simulation-host.cu:204-289): each set's
+    // initial positions through the forward stack from its start map on, then the active
+    // forward map; a set starting at t = 0 goes through every map; points leaving the frame
+    // become NaN (k_h_sample_points_map)
+    double* o = out;
+    const int n = n_maps_f_;
+    for (size_t i = 0; i < s.particles_forwarded.size(); ++i) {
+        const int num = s.particles_forwarded[i].num;
+        const double t0 = s.particles_forwarded[i].init_time;
+        const int im = init_map_[i];
+        if (num <= 0) continue;
+        auto fmap = [&](int m) { return stack_f + (size_t)m * 8 * gc.N; };
+        if (n > 0) {
+            if (t0 == 0) CMM_LAUNCH(1, launch_map_points(gc, frame, fmap(0), fmap(0) + 4 * gc.N, fparts_[i], o, num, stream));
+            else CMM_CUDA(cudaMemcpyAsync(o, fparts_[i], sizeof(double) * 2 * num, cudaMemcpyDeviceToDevice, stream));
+            for (int m = 1; m < n; ++m)
+                if ((m >= im && t0 != 0) || t0 == 0)
+                    CMM_LAUNCH(1, launch_map_points(gc, frame, fmap(m), fmap(m) + 4 * gc.N, o, o, num, stream));
+            if ((im != 0 && t0 != 0) || t0 == 0)
+                CMM_LAUNCH(1, launch_map_points(gc, frame, ChiX_f, ChiY_f, o, o, num, stream));
+        } else {
+            CMM_LAUNCH(1, launch_map_points(gc, frame, ChiX_f, ChiY_f, fparts_[i], o, num, stream));
+        }
+        o += 2 * (size_t)num;
+    }
+    return kOk;
+}
+
 int EulerSim::incomp(double* out)
 {
     if (mixed_) CMM_LAUNCH(1, launch_incomp_m(gc, gf.NX / gc.NX, mapm_, d_scal_, stream));
@@ -634,10 +726,21 @@ int EulerSim::reserve_stack(int n)
     CMM_CUDA(cudaMalloc(&bigger, mapb * cap));
     void* old = mixed_ ? (void*)stackm_ : (void*)stack;
     if (old && n_maps_ > 0) CMM_CUDA(cudaMemcpyAsync(bigger, old, mapb * n_maps_, cudaMemcpyDeviceToDevice, stream));
+    void* bigger_f = nullptr;
+    if (s.forward_map) {
+        // the forward stack grows with the backward one (one forward sub-map per remap)
+        CMM_CUDA(cudaMalloc(&bigger_f, mapb * cap));
+        if (stack_f && n_maps_ > 0)
+            CMM_CUDA(cudaMemcpyAsync(bigger_f, stack_f, mapb * n_maps_, cudaMemcpyDeviceToDevice, stream));
+    }
     CMM_CUDA(cudaStreamSynchronize(stream));
     if (old) cudaFree(old);
     if (mixed_) stackm_ = (float4*)bigger;
     else stack = (double*)bigger;
+    if (s.forward_map) {
+        if (stack_f) cudaFree(stack_f);
+        stack_f = (double*)bigger_f;
+    }
     stack_cap_ = cap;
     return kOk;
 }
@@ -655,6 +758,14 @@ int EulerSim::push_stack()
     double* slot = stack + (size_t)n_maps_ * 8 * gc.N;
     CMM_CUDA(cudaMemcpyAsync(slot, ChiX, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToDevice, stream));
     CMM_CUDA(cudaMemcpyAsync(slot + 4 * gc.N, ChiY, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToDevice, stream));
+    if (s.forward_map) {
+        // the forward map goes onto its own stack and restarts from the identity (cmm-euler2d.cu:847-851)
+        double* fslot = stack_f + (size_t)n_maps_ * 8 * gc.N;
+        CMM_CUDA(cudaMemcpyAsync(fslot, ChiX_f, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToDevice, stream));
+        CMM_CUDA(cudaMemcpyAsync(fslot + 4 * gc.N, ChiY_f, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToDevice, stream));
+        CMM_LAUNCH(1, launch_init_map(ChiX_f, ChiY_f, gc, stream));
+        n_maps_f_++;
+    }
     n_maps_++;
     return kOk;
 }
@@ -662,7 +773,7 @@ int EulerSim::push_stack()
 // ---------------------------------------------------------------- MapStack folder
 static std::string two_digits(int i) { return (i < 10 ? "0" : "") + std::to_string(i); }
 
-int EulerSim::write_map_stack(int map_num)
+int EulerSim::write_map_stack(int map_num, bool forward)
 {
     // writeMapStack (src/ui/cmm-io.cu:611-635): one backward map in the reference's planar
     // FP64 layout under MapStack/Map_Chi{X,Y}_H_<n|coarse>.data, and psi for the restart.
@@ -672,10 +783,16 @@ int EulerSim::write_map_stack(int map_num)
     const std::string dir = run_dir(s) + "/MapStack";
     if (!make_dir(dir)) { err = "cannot create " + dir; return kErrIO; }
     const std::string name = map_num < 0 ? std::string("coarse") : std::to_string(map_num);
+    // forward maps go under Map_Chi{X,Y}_f_H_<n|coarse>, the names the reference's reader
+    // expects (its writer puts a forward sub-map under the next backward name at a remap,
+    // cmm-euler2d.cu:848, which a later restart would read as a backward sub-map)
+    const std::string fw = forward ? "_f" : "";
     if (mixed_) CMM_LAUNCH(1, launch_map_to_planes(mapm_, gc, ChiX, ChiY, stream));
     std::vector<double> h((size_t)8 * gc.N);
-    CMM_CUDA(cudaMemcpyAsync(h.data(), ChiX, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToHost, stream));
-    CMM_CUDA(cudaMemcpyAsync(h.data() + 4 * gc.N, ChiY, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToHost, stream));
+    const double* MX = forward ? ChiX_f : ChiX;
+    const double* MY = forward ? ChiY_f : ChiY;
+    CMM_CUDA(cudaMemcpyAsync(h.data(), MX, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToHost, stream));
+    CMM_CUDA(cudaMemcpyAsync(h.data() + 4 * gc.N, MY, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToHost, stream));
     const double* p0 = psi[0];
     if (mixed_ && vlasov_)
         CMM_LAUNCH(1, launch_vlasov_assemble(phi_lv_[0], phi_lv_[0] + gp.NX, vl_h_, vl_h_ + gp.NY, gp, psi[0], stream));
@@ -684,9 +801,9 @@ int EulerSim::write_map_stack(int map_num)
     std::vector<double> hp(L > 1 ? (size_t)4 * gp.N : 0);
     if (L > 1) CMM_CUDA(cudaMemcpyAsync(hp.data(), p0, sizeof(double) * 4 * gp.N, cudaMemcpyDeviceToHost, stream));
     CMM_CUDA(cudaStreamSynchronize(stream));
-    bool ok = write_f64(dir + "/Map_ChiX_H_" + name + ".data", h.data(), (size_t)4 * gc.N) &&
-              write_f64(dir + "/Map_ChiY_H_" + name + ".data", h.data() + 4 * gc.N, (size_t)4 * gc.N);
-    for (int l = 1; l < L && ok; ++l)
+    bool ok = write_f64(dir + "/Map_ChiX" + fw + "_H_" + name + ".data", h.data(), (size_t)4 * gc.N) &&
+              write_f64(dir + "/Map_ChiY" + fw + "_H_" + name + ".data", h.data() + 4 * gc.N, (size_t)4 * gc.N);
+    for (int l = 1; l < L && ok && !forward; ++l)
         ok = write_f64(dir + "/Stream_function_Psi_H_psi_" + std::to_string(l) + ".data", hp.data(), (size_t)4 * gp.N);
     if (!ok) { err = "cannot write the map stack under " + dir; return kErrIO; }
     return kOk;
@@ -774,6 +891,25 @@ int EulerSim::restart_from_map_stack()
     bool ok = read("Map_ChiX_H_coarse.data", h.data(), nc4);
     ok = read("Map_ChiY_H_coarse.data", h.data() + nc4, nc4) && ok;
     if (ok && (rc = upload_map(ChiX, ChiY, mapm_))) return rc;
+    if (s.forward_map) {
+        // the forward stack and active forward map (readMapStack with isForward, :1256-1302)
+        const int nf = count_files_containing(dir, "Map_ChiX_f_H") - 1;
+        if (nf > n_maps_) {
+            err = "the forward map stack at " + dir + " holds more maps than the backward one";
+            return kErrParam;
+        }
+        for (int i = 0; i < nf; ++i) {
+            bool okf = read("Map_ChiX_f_H_" + std::to_string(i) + ".data", h.data(), nc4);
+            okf = read("Map_ChiY_f_H_" + std::to_string(i) + ".data", h.data() + nc4, nc4) && okf;
+            if (okf && (rc = upload_map(stack_f + (size_t)i * 8 * gc.N, stack_f + (size_t)i * 8 * gc.N + nc4, nullptr)))
+                return rc;
+        }
+        n_maps_f_ = std::max(nf, 0);
+        bool okf = read("Map_ChiX_f_H_coarse.data", h.data(), nc4);
+        okf = read("Map_ChiY_f_H_coarse.data", h.data() + nc4, nc4) && okf;
+        if (okf && (rc = upload_map(ChiX_f, ChiY_f, nullptr))) return rc;
+        if (s.verbose >= 2) log_.push("Loaded " + std::to_string(n_maps_f_) + " maps to forward map stack");
+    }
     std::vector<double> hp(np4);
     for (int l = 1; l < L; ++l) {
         if (!read("Stream_function_Psi_H_psi_" + std::to_string(l) + ".data", hp.data(), np4)) continue;
@@ -805,28 +941,40 @@ int EulerSim::restart_from_map_stack()
     return kOk;
 }
 
-int EulerSim::init_particles()
+int EulerSim::init_positions(double* dst, int num, unsigned long long seed, int init_num, const double* param,
+                             const std::string& init_name)
 {
     // init_particles (src/simulation/cmm-init.cu:311-389); bounds of the psi grid
+    if (num <= 0) return kOk;
+    if (init_num == 0 || init_num == 1) {
+        curandGenerator_t g;
+        if (curandCreateGenerator(&g, CURAND_RNG_PSEUDO_DEFAULT) != CURAND_STATUS_SUCCESS) { err = "cuRAND create"; return kErrCuda; }
+        curandSetStream(g, stream);
+        curandSetPseudoRandomGeneratorSeed(g, seed);
+        curandStatus_t st = init_num == 0 ? curandGenerateUniformDouble(g, dst, 2 * (size_t)num)
+                                          : curandGenerateNormalDouble(g, dst, 2 * (size_t)num, 0.5, 1.0);
+        curandDestroyGenerator(g);
+        if (st != CURAND_STATUS_SUCCESS) { err = "cuRAND generate"; return kErrCuda; }
+        CMM_LAUNCH(1, launch_particle_rescale(dst, num, param, gp, stream));
+    } else if (init_num >= 2 && init_num <= 4) {
+        CMM_LAUNCH(1, launch_particle_layout(dst, num, init_num, param, gp, stream));
+    } else {
+        err = "unknown particle init_name " + init_name;
+        return kErrParam;
+    }
+    return kOk;
+}
+
+int EulerSim::init_particles()
+{
+    int rc;
     for (size_t i = 0; i < s.particles_advected.size(); ++i) {
         auto& p = s.particles_advected[i];
-        if (p.num <= 0) continue;
-        if (p.init_num == 0 || p.init_num == 1) {
-            curandGenerator_t g;
-            if (curandCreateGenerator(&g, CURAND_RNG_PSEUDO_DEFAULT) != CURAND_STATUS_SUCCESS) { err = "cuRAND create"; return kErrCuda; }
-            curandSetStream(g, stream);
-            curandSetPseudoRandomGeneratorSeed(g, p.seed);
-            curandStatus_t st = p.init_num == 0 ? curandGenerateUniformDouble(g, parts[i], 2 * (size_t)p.num)
-                                                : curandGenerateNormalDouble(g, parts[i], 2 * (size_t)p.num, 0.5, 1.0);
-            curandDestroyGenerator(g);
-            if (st != CURAND_STATUS_SUCCESS) { err = "cuRAND generate"; return kErrCuda; }
-            CMM_LAUNCH(1, launch_particle_rescale(parts[i], p.num, p.init_param, gp, stream));
-        } else if (p.init_num >= 2 && p.init_num <= 4) {
-            CMM_LAUNCH(1, launch_particle_layout(parts[i], p.num, p.init_num, p.init_param, gp, stream));
-        } else {
-            err = "unknown particle init_name " + p.init_name;
-            return kErrParam;
-        }
+        if ((rc = init_positions(parts[i], p.num, p.seed, p.init_num, p.init_param, p.init_name))) return rc;
+    }
+    for (size_t i = 0; i < fparts_.size(); ++i) {
+        auto& p = s.particles_forwarded[i];
+        if ((rc = init_positions(fparts_[i], p.num, p.seed, p.init_num, p.init_param, p.init_name))) return rc;
     }
     return kOk;
 }
@@ -950,6 +1098,8 @@ int EulerSim::init()
 
     if ((rc = reset_map())) return rc;
     if (vlasov_ && (rc = vlasov_setup_h())) return rc;
+    if (s.forward_map) CMM_LAUNCH(1, launch_init_map(ChiX_f, ChiY_f, gc, stream));
+    n_maps_f_ = 0;
     const bool restart = s.restart_time != 0;
     if (restart) {
         if ((rc = restart_from_map_stack())) return rc;
@@ -1056,6 +1206,8 @@ int EulerSim::step_once()
 
     ph_begin(kPhAdvect);
     if ((rc = advect(t_vec_.data(), dt_vec_.data(), loop_ctr_, s.time_integration_num, L))) return rc;
+    bool forced_remap = false;
+    if ((rc = forward_step(lcl, &forced_remap))) return rc;
     ph_end(kPhAdvect);
     ph_begin(kPhIncomp);
     if ((rc = incomp(&e_inc_))) return rc;
@@ -1068,7 +1220,7 @@ int EulerSim::step_once()
         return kErrState;
     }
     bool saturated = false;
-    if (e_inc_ > s.incomp_threshold && !s.skip_remapping) {
+    if ((e_inc_ > s.incomp_threshold && !s.skip_remapping) || forced_remap) {
         if (n_maps_ >= max_maps) {
             if (s.verbose >= 0) log_.push("Stack Saturated : Exitting");
             saturated = true;
@@ -1081,6 +1233,7 @@ int EulerSim::step_once()
             ph_begin(kPhRemap);
             if ((rc = translate_ic())) return rc;
             if (s.save_map_stack && (rc = write_map_stack(n_maps_))) return rc;
+            if (s.save_map_stack && s.forward_map && (rc = write_map_stack(n_maps_f_, true))) return rc;
             if ((rc = push_stack())) return rc;
             if ((rc = reset_map())) return rc;
             kernel_launches++;
@@ -1111,12 +1264,18 @@ int EulerSim::step_once()
     std::string dir = run_dir(s) + "/Monitoring_data/";
     append_f64(dir + "Time_s.data", &t_vec_[lcl + 1], 1);
     append_f64(dir + "Error_incompressibility.data", &e_inc_, 1);
+    if (s.forward_map) {
+        append_f64(dir + "Error_incompressibility_forward.data", &e_inc_f_, 1);
+        append_f64(dir + "Error_invertibility.data", &e_inv_, 1);
+    }
     append_f64(dir + "Map_gaps.data", &gap, 1);
     append_f64(dir + "Map_counter.data", &counter, 1);
     double tc = wall();
     if (s.verbose >= 2)
         log_.push("Step = " + std::to_string(loop_ctr_) + " \t S-Time = " + to_str3(t_vec_[lcl + 1]) + "/" +
-                  to_str3(s.final_time) + " \t E-inc = " + to_str3(e_inc_) + " \t C-Time = " + format_duration(tc));
+                  to_str3(s.final_time) + " \t E-inc = " + to_str3(e_inc_) +
+                  (s.forward_map ? " \t E-inc_f = " + to_str3(e_inc_f_) + " \t E-inv = " + to_str3(e_inv_) : std::string()) +
+                  " \t C-Time = " + format_duration(tc));
     append_f64(dir + "Time_c.data", &tc, 1);
     return saturated ? kErrSaturated : kOk;
 }
@@ -1137,6 +1296,7 @@ int EulerSim::finish()
             log_.push(os.str());
         }
         if ((rc = write_map_stack(-1)) || (rc = write_particles_state())) return rc;
+        if (s.forward_map && (rc = write_map_stack(-1, true))) return rc;
     }
     CMM_CUDA(cudaStreamSynchronize(stream));
     double tc = wall();
@@ -1214,6 +1374,14 @@ int EulerSim::sample_outputs(double t_now, double dt_now)
             return rc2;
         };
         int rc;
+        if (s.forward_map && (has(var, "Map_f") || has(var, "Chi_f") || all || !s.particles_forwarded.empty())) {
+            // forward part (cmm-simulation-host.cu:736-782): the forward map on the sample grid and
+            // the forwarded particles, written raw to Particle_data at every verbosity
+            CMM_LAUNCH(1, launch_compose_fwd(gc, gs, ChiX_f, ChiY_f, stack_f, n_maps_f_, X, Y, stream));
+            if (has(var, "Map_f") || has(var, "Chi_f") || all)
+                if ((rc = out("Map_ChiX_f", X)) || (rc = out("Map_ChiY_f", Y))) return rc;
+            if ((rc = write_forwarded(s.domain_bounds, "/Particle_data/Time_" + tname, false, var))) return rc;
+        }
         if (mixed_) CMM_LAUNCH(1, launch_compose_pos_m(gc, gs, mapm_, stackm_, n_maps_, X, Y, stream));
         else CMM_LAUNCH(1, launch_compose_pos(gc, gs, ChiX, ChiY, stack, n_maps_, X, Y, stream));
         if (has(var, "Map_b") || has(var, "Chi_b") || all) {
@@ -1279,6 +1447,26 @@ int EulerSim::sample_outputs(double t_now, double dt_now)
     return kOk;
 }
 
+int EulerSim::write_forwarded(const double* frame, const std::string& sub, bool zoom, const std::string& var)
+{
+    if (s.particles_forwarded.empty()) return kOk;
+    int rc;
+    if ((rc = forwarded_positions(frame, fpos_))) return rc;
+    size_t off = 0;
+    for (size_t i = 0; i < s.particles_forwarded.size(); ++i) {
+        const int num = std::max(s.particles_forwarded[i].num, 0);
+        const bool want = has(var, ("PartF_" + two((int)i + 1)).c_str()) || (!zoom && has(var, "All"));
+        if (want && num > 0) {
+            make_dir(run_dir(s) + sub.substr(0, sub.rfind('/')));
+            make_dir(run_dir(s) + sub);
+            if ((rc = write_field(sub, "Particles_forwarded_pos_P" + two(zoom ? (int)i : (int)i + 1), fpos_ + off, 2ll * num)))
+                return rc;
+        }
+        off += 2 * (size_t)num;
+    }
+    return kOk;
+}
+
 int EulerSim::reserve_sample_buffers(int n)
 {
     if (n <= smp_n_) return kOk;
@@ -1333,6 +1521,14 @@ int EulerSim::zoom_outputs(double t_now, double dt_now)
             auto out = [&](const std::string& name, const double* v) {
                 return dbg ? debug_globals(name + "_" + ns + rs, v, gz.N, true, gstat) : write_field(sub, name + "_" + ns, v, gz.N);
             };
+            if (s.forward_map && (has(var, "Map_f") || has(var, "Chi_f") || all || !s.particles_forwarded.empty())) {
+                // forward part (cmm-simulation-host.cu:1087-1136): the forwarded particles are
+                // written only for sets named with PartF_<ii>, as P<ii - 1>
+                CMM_LAUNCH(1, launch_compose_fwd(gc, gz, ChiX_f, ChiY_f, stack_f, n_maps_f_, X, Y, stream));
+                if (has(var, "Map_f") || has(var, "Chi_f") || all)
+                    if ((rc = out("Map_ChiX_f", X)) || (rc = out("Map_ChiY_f", Y))) return rc;
+                if ((rc = write_forwarded(b, sub, true, var))) return rc;
+            }
             if (mixed_) CMM_LAUNCH(1, launch_compose_pos_m(gc, gz, mapm_, stackm_, n_maps_, X, Y, stream));
             else CMM_LAUNCH(1, launch_compose_pos(gc, gz, ChiX, ChiY, stack, n_maps_, X, Y, stream));
             if (has(var, "Map_b") || has(var, "Chi_b") || all)
@@ -1444,6 +1640,14 @@ int EulerSim::write_time_step(double t_now, double dt_now)
         if ((rc = arr(sub, "Map_ChiX_H_coarse", ChiX, 4 * gc.N))) return rc;
         if ((rc = arr(sub, "Map_ChiY_H_coarse", ChiY, 4 * gc.N))) return rc;
     }
+    if (s.forward_map && (has(var, "Map_f") || has(var, "Chi_f") || all)) {
+        if ((rc = var2d("Map_ChiX_f_coarse", ChiX_f, gc))) return rc;
+        if ((rc = var2d("Map_ChiY_f_coarse", ChiY_f, gc))) return rc;
+    }
+    if (s.forward_map && (has(var, "Map_f_H") || has(var, "Chi_f_H") || all)) {
+        if ((rc = arr(sub, "Map_ChiX_f_H_coarse", ChiX_f, 4 * gc.N))) return rc;
+        if ((rc = arr(sub, "Map_ChiY_f_H_coarse", ChiY_f, 4 * gc.N))) return rc;
+    }
     std::string psub = "/Particle_data/Time_" + tname;
     if (has(var, "PartA_") || all) {
         make_dir(run_dir(s) + psub);
@@ -1536,6 +1740,9 @@ size_t EulerSim::field_bytes(const std::string& n) const
     if (n == "Vorticity_W_fine_H") return sizeof(double) * 4 * gf.N;
     if (n == "Map_stack") return sizeof(double) * 8 * gc.N * n_maps_;
     if (n == "Init_random_table") return sizeof(double) * kInitTable;
+    if (s.forward_map && (n == "Map_ChiX_f_H_coarse" || n == "Map_ChiY_f_H_coarse")) return sizeof(double) * 4 * gc.N;
+    for (size_t i = 0; i < s.particles_forwarded.size() && s.forward_map; ++i)
+        if (n == "Particles_forwarded_pos_P" + two((int)i + 1)) return sizeof(double) * 2 * s.particles_forwarded[i].num;
     for (size_t i = 0; i < s.particles_advected.size(); ++i) {
         std::string id = two((int)i + 1);
         if (n == "Particles_advected_pos_P" + id || n == "Particles_advected_vel_U" + id)
@@ -1565,6 +1772,17 @@ int EulerSim::get_field(const std::string& n, void* dst, size_t bytes)
     else if (n == "Vorticity_W_coarse" || n == "Distribution_coarse") rc = cp(vort, bytes);
     else if (n == "Vorticity_W_fine_H") rc = cp(wfine, bytes);
     else if (n == "Init_random_table") rc = cp(d_rand_, bytes);
+    else if (n == "Map_ChiX_f_H_coarse") rc = cp(ChiX_f, bytes);
+    else if (n == "Map_ChiY_f_H_coarse") rc = cp(ChiY_f, bytes);
+    else if (n.rfind("Particles_forwarded_pos_P", 0) == 0) {
+        // positions now, mapped on the whole domain
+        rc = forwarded_positions(s.domain_bounds, fpos_);
+        size_t off = 0;
+        for (size_t i = 0; i < s.particles_forwarded.size() && !rc; ++i) {
+            if (n == "Particles_forwarded_pos_P" + two((int)i + 1)) rc = cp(fpos_ + off, bytes);
+            off += 2 * (size_t)std::max(s.particles_forwarded[i].num, 0);
+        }
+    }
     else if (n == "Map_stack" && !mixed_) rc = bytes ? cp(stack, bytes) : kOk;
     else if (n == "Map_stack") {
         // FP32 displacement maps -> the reference's planar X | Y layout, one map at a time
@@ -1600,6 +1818,8 @@ int EulerSim::get_scalar(const std::string& n, double* out)
     if (n == "time") { *out = time(); return kOk; }
     if (n == "e_inc") { *out = e_inc_; return kOk; }
     if (n == "map_counter") { *out = n_maps_; return kOk; }
+    if (n == "e_inc_forward") { *out = e_inc_f_; return kOk; }
+    if (n == "e_invertibility") { *out = e_inv_; return kOk; }
     if (n == "map_gap") { *out = (loop_ctr_ - 1) - old_ctr_; return kOk; }
     if (n == "loop_ctr") { *out = loop_ctr_; return kOk; }
     if (n == "kernel_launches") { *out = (double)kernel_launches; return kOk; }

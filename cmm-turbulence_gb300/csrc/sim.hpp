@@ -66,6 +66,15 @@ public:
     double* stack = nullptr;       // n maps, 8*Nc doubles each
     std::vector<double*> parts;    // particle positions per set
     std::vector<double*> vels;     // inertial velocity state per set (tau != 0; null for tracers)
+    // forward map (forward_map = 1): active map, its stack (n maps like stack), forwarded
+    // particles' initial positions and the stack index each forwarded set starts from
+    double* ChiX_f = nullptr; double* ChiY_f = nullptr;
+    double* stack_f = nullptr;
+    std::vector<double*> fparts_;
+    std::vector<int> init_map_;
+    double e_inc_f_ = 0, e_inv_ = 0;
+    int n_maps_f_ = 0;             // forward sub-maps (one per remap; a restart may load fewer)
+    double* fpos_ = nullptr;       // forwarded particle positions of a save (all sets)
     cudaStream_t stream = nullptr;
 
     // diagnostics (reference Mesure)
@@ -92,18 +101,26 @@ private:
     void swap_levels(int a, int b);
     int incomp(double* out);
     int init_particles();
+    int init_positions(double* dst, int num, unsigned long long seed, int init_num, const double* param,
+                       const std::string& init_name);
+    // forward map (forward_map = 1, plain FP64 form): advection, checks and forced remaps of one
+    // step, and the forwarded particles' positions on a frame (apply_map_stack_points, direction 1)
+    int forward_step(int lcl, bool* forced_remap);
+    int forwarded_positions(const double* frame, double* out);
     int init_inertial_velocity(size_t i);   // v = u(x) of psi level 0, or 0 (init_vel)
     int advect_particles(int lcl);
     int push_stack();
     int reserve_stack(int n);          // device stack capacity for n sub-maps
     // MapStack folder (writeMapStack / writeParticlesState / readMapStack, cmm-io.cu:611-688,
     // cmm-simulation-host.cu:1256-1302): map_num >= 0 a stacked sub-map, -1 the active map
-    int write_map_stack(int map_num);
+    int write_map_stack(int map_num, bool forward = false);
     int write_particles_state();
     int restart_from_map_stack();      // the restart branch of init (cmm-euler2d.cu:634-685)
     int sample_outputs(double t_now, double dt_now);   // sampled outputs on user grids
     int zoom_outputs(double t_now, double dt_now);     // zoom windows (compute_zoom)
     int reserve_sample_buffers(int n);                 // smp_ / smp_c_ for an n x n grid
+    // forwarded particles mapped on a frame, raw files under sub for the sets var names
+    int write_forwarded(const double* frame, const std::string& sub, bool zoom, const std::string& var);
     int evaluate_potential();          // Vlasov-Poisson psi from the distribution function
     int vlasov_setup_h();              // the periodification h(v), once per run
     int vlasov_mesure(double* out9);   // Etot, Ekin, Epot, Mass, Momentum, Emode1..4

@@ -109,6 +109,11 @@ typedef struct {
 } og_particle_set;
 
 typedef struct {
+    int num;                      /* forwarded particles in the set */
+    double init_time;             /* the set is mapped forward from this time on */
+} og_fwd_set;
+
+typedef struct {
     int grid_coarse, grid_fine, grid_psi, grid_vort;
     double bounds[4];
     double dt;
@@ -128,6 +133,9 @@ typedef struct {
     int n_particle_sets;
     og_particle_set psets[8];
     int simulation_type_num;      /* 0 = cmm_euler_2d, 2 = cmm_vlasov_poisson_1d */
+    int forward_map;              /* advect a forward map beside the backward one */
+    int n_fwd_sets;               /* forwarded particle sets */
+    og_fwd_set fsets[8];
 } og_settings;
 
 typedef struct og_state og_state;
@@ -156,6 +164,21 @@ int og_step(og_state* st, double dt_now, double* e_inc, int* remapped);
 int og_restart(og_state* st, double restart_time, int n_maps, const double* stackX, const double* stackY,
                const double* chix, const double* chiy, const double* psi_prev);
 const double* og_stack_x(const og_state* st);     /* n_maps x 4*Nc */
+/* forward map (forward_map = 1): the active forward map, the last step's forward
+ * incompressibility and invertibility errors, the forwarded particles' initial positions,
+ * and the forward composition on an n x n frame (bounds4; the map through the forward
+ * stack oldest first, then the active map) with the forwarded particles mapped from their
+ * start map on (NaN outside the frame): apply_map_stack / apply_map_stack_points with
+ * direction 1, src/simulation/cmm-simulation-host.cu:130-152, 160-292 */
+const double* og_chix_f(const og_state* st);
+const double* og_chiy_f(const og_state* st);
+void og_forward_monitors(const og_state* st, double* einc_f, double* einv);
+int og_set_forwarded_particles(og_state* st, int i_set, const double* pos);
+void og_forward_sample(const og_state* st, int n, const double* bounds4, double* map_xy, double* parts);
+/* k_invertibility_check (src/simulation/cmm-simulation-kernel.cu:177-198): max over the
+ * half-shifted check grid of |x - X_b(X_f(x))| */
+double og_invertibility_check(const og_grid* gcheck, const og_grid* gb, const double* Xb, const double* Yb,
+                              const og_grid* gf, const double* Xf, const double* Yf);
 const double* og_stack_y(const og_state* st);
 
 /* state access (reference layouts) */

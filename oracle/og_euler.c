@@ -142,6 +142,84 @@ static void rk4_optimized_b(const double* psi, const double* x_in, double* x_out
     x_out[1] = x_in[1] - dt * (2 * k1[1] - k2[1] + 8 * k3[1] + 3 * k4[1]) / 12.0;
 }
 
+/* forward integrators (forward map), src/numerical/cmm-timestep.cu: psi level 0 is t_n,
+ * level 1 t_{n-1}, level 2 t_{n-2}; L1 / L12 extrapolate to t_{n+1} / t_{n+1/2}.  Two of
+ * them are kept exactly as the reference has them: RK4_classical takes its first
+ * half-step velocity from L1 and its last stage from L12, and RK4_optimized is the
+ * backward scheme (it integrates with -dt). */
+static void euler_exp_f(const double* psi, const double* x_in, double* x_out, const og_grid* g, double dt)
+{   /* :26-31 */
+    double u[2];
+    vel_level(psi, 0, x_in, u, g);
+    x_out[0] = x_in[0] + dt * u[0];
+    x_out[1] = x_in[1] + dt * u[1];
+}
+
+static void rk2_heun_f(const double* psi, const double* x_in, double* x_out, const og_grid* g, double dt, int l_order,
+                       const og_lcoef* lc)
+{   /* :48-64 */
+    double k1[2], k2[2], y[2];
+    vel_level(psi, 0, x_in, k1, g);
+    y[0] = x_in[0] + dt * k1[0]; y[1] = x_in[1] + dt * k1[1];
+    vel_comb(psi, lc->L1, l_order, y, k2, g);
+    x_out[0] = x_in[0] + dt * (k1[0] + k2[0]) / 2;
+    x_out[1] = x_in[1] + dt * (k1[1] + k2[1]) / 2;
+}
+
+static void ab2_pc_f(const double* psi, const double* x_in, double* x_out, const og_grid* g, double dt)
+{   /* :84-110 */
+    double u[2], u2[2], xf_p[2] = {x_in[0], x_in[1]}, o[2] = {x_in[0], x_in[1]};
+    for (int ctr = 0; ctr < 10; ctr++) {
+        vel_level(psi, 1, xf_p, u2, g);
+        xf_p[0] = o[0] + dt * u2[0]; xf_p[1] = o[1] + dt * u2[1];
+        vel_level(psi, 1, xf_p, u2, g);
+        vel_level(psi, 0, o, u, g);
+        o[0] = x_in[0] + dt * (1.5 * u[0] - 0.5 * u2[0]);
+        o[1] = x_in[1] + dt * (1.5 * u[1] - 0.5 * u2[1]);
+    }
+    x_out[0] = o[0]; x_out[1] = o[1];
+}
+
+static void rk3_classical_f(const double* psi, const double* x_in, double* x_out, const og_grid* g, double dt,
+                            int l_order, const og_lcoef* lc)
+{   /* :144-173 */
+    double k1[2], k2[2], k3[2], y[2];
+    vel_level(psi, 0, x_in, k1, g);
+    y[0] = x_in[0] + dt * k1[0] / 2.0; y[1] = x_in[1] + dt * k1[1] / 2.0;
+    vel_comb(psi, lc->L12, l_order, y, k2, g);
+    y[0] = x_in[0] - dt * k1[0] + 2 * dt * k2[0]; y[1] = x_in[1] - dt * k1[1] + 2 * dt * k2[1];
+    vel_comb(psi, lc->L1, l_order, y, k3, g);
+    x_out[0] = x_in[0] + dt * (k1[0] + 4 * k2[0] + k3[0]) / 6.0;
+    x_out[1] = x_in[1] + dt * (k1[1] + 4 * k2[1] + k3[1]) / 6.0;
+}
+
+static void rk4_classical_f(const double* psi, const double* x_in, double* x_out, const og_grid* g, double dt,
+                            int l_order, const og_lcoef* lc)
+{   /* :216-258 */
+    double k1[2], k2[2], k3[2], k4[2], y[2];
+    vel_level(psi, 0, x_in, k1, g);
+    y[0] = x_in[0] + dt * k1[0] / 2.0; y[1] = x_in[1] + dt * k1[1] / 2.0;
+    vel_comb(psi, lc->L1, l_order, y, k2, g);
+    y[0] = x_in[0] + dt * k2[0] / 2.0; y[1] = x_in[1] + dt * k2[1] / 2.0;
+    vel_comb(psi, lc->L12, l_order, y, k3, g);
+    y[0] = x_in[0] + dt * k3[0]; y[1] = x_in[1] + dt * k3[1];
+    vel_comb(psi, lc->L12, l_order, y, k4, g);
+    x_out[0] = x_in[0] + dt * (k1[0] + 2 * k2[0] + 2 * k3[0] + k4[0]) / 6.0;
+    x_out[1] = x_in[1] + dt * (k1[1] + 2 * k2[1] + 2 * k3[1] + k4[1]) / 6.0;
+}
+
+static void rk3_optimized_f(const double* psi, const double* x_in, double* x_out, const og_grid* g, double dt)
+{   /* :314-339 */
+    double k1[2], k2[2], k3[2], y[2];
+    vel_level(psi, 0, x_in, k1, g);
+    y[0] = x_in[0] - dt * k1[0]; y[1] = x_in[1] - dt * k1[1];
+    vel_level(psi, 1, y, k2, g);
+    y[0] = x_in[0] - dt * (8 * k1[0] + 2 * k2[0]) / 5.0; y[1] = x_in[1] - dt * (8 * k1[1] + 2 * k2[1]) / 5.0;
+    vel_level(psi, 2, y, k3, g);
+    x_out[0] = x_in[0] + dt * (23 * k1[0] - 16 * k2[0] + 5 * k3[0]) / 12.0;
+    x_out[1] = x_in[1] + dt * (23 * k1[1] - 16 * k2[1] + 5 * k3[1]) / 12.0;
+}
+
 /* ------------------------------------------------------------------ */
 /* kernels restated as loops                                           */
 /* ------------------------------------------------------------------ */
@@ -174,11 +252,30 @@ void og_map_update_coefficients(int order_num, double ep, double* c1, double* cx
     }
 }
 
+static void advect_map_dir(const double* ChiX, const double* ChiY, double* ChiX_new, double* ChiY_new,
+                           const double* psi, const og_grid* gm, const og_grid* gp,
+                           double dt, double ep, int ti_num, int order_num, int l_order,
+                           const double* L1, const double* L12,
+                           const double* c1, const double* cx, const double* cy, const double* cxy, int direction);
+
 void og_advect_map(const double* ChiX, const double* ChiY, double* ChiX_new, double* ChiY_new,
                    const double* psi, const og_grid* gm, const og_grid* gp,
                    double dt, double ep, int ti_num, int order_num, int l_order,
                    const double* L1, const double* L12,
                    const double* c1, const double* cx, const double* cy, const double* cxy)
+{
+    advect_map_dir(ChiX, ChiY, ChiX_new, ChiY_new, psi, gm, gp, dt, ep, ti_num, order_num, l_order, L1, L12,
+                   c1, cx, cy, cxy, -1);
+}
+
+/* k_advect_using_stream_hermite (src/simulation/cmm-simulation-kernel.cu:207-298): direction -1
+ * integrates each footpoint back in time and looks it up in the map; direction 1 (forward
+ * map) looks the footpoint up in the map first and integrates it forward */
+static void advect_map_dir(const double* ChiX, const double* ChiY, double* ChiX_new, double* ChiY_new,
+                           const double* psi, const og_grid* gm, const og_grid* gp,
+                           double dt, double ep, int ti_num, int order_num, int l_order,
+                           const double* L1, const double* L12,
+                           const double* c1, const double* cx, const double* cy, const double* cxy, int direction)
 {
     og_lcoef lc = {L1, L12};
     long N = gm->N;
@@ -192,17 +289,32 @@ void og_advect_map(const double* ChiX, const double* ChiY, double* ChiX_new, dou
             for (int k = 0; k < nfoot; k++) {
                 x_ep[0] = gm->bounds[0] + iX * gm->hx + ((k >> 2) + 1) * ep * (1 - 2 * ((k >> 1) & 1));
                 x_ep[1] = gm->bounds[2] + iY * gm->hy + ((k >> 2) + 1) * ep * (1 - 2 * (((k + 1) >> 1) & 1));
-                switch (ti_num) {
-                    case 10: euler_exp_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
-                    case 21: rk2_heun_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
-                    case 30: rk3_classical_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
-                    case 20: ab2_pc_b(psi, x_ep, x_f, gp, dt); break;
-                    case 40: rk4_classical_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
-                    case 31: rk3_optimized_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
-                    case 41: rk4_optimized_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
-                    default: x_f[0] = x_f[1] = 0;
+                if (direction == -1) {
+                    switch (ti_num) {
+                        case 10: euler_exp_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
+                        case 21: rk2_heun_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
+                        case 30: rk3_classical_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
+                        case 20: ab2_pc_b(psi, x_ep, x_f, gp, dt); break;
+                        case 40: rk4_classical_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
+                        case 31: rk3_optimized_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
+                        case 41: rk4_optimized_b(psi, x_ep, x_f, gp, dt, l_order, &lc); break;
+                        default: x_f[0] = x_f[1] = 0;
+                    }
+                    og_diffeo_interpolate_2D(ChiX, ChiY, x_f[0], x_f[1], &x_f[0], &x_f[1], gm);
+                } else {
+                    double y[2];
+                    og_diffeo_interpolate_2D(ChiX, ChiY, x_ep[0], x_ep[1], &y[0], &y[1], gm);
+                    switch (ti_num) {
+                        case 10: euler_exp_f(psi, y, x_f, gp, dt); break;
+                        case 20: ab2_pc_f(psi, y, x_f, gp, dt); break;
+                        case 21: rk2_heun_f(psi, y, x_f, gp, dt, l_order, &lc); break;
+                        case 30: rk3_classical_f(psi, y, x_f, gp, dt, l_order, &lc); break;
+                        case 40: rk4_classical_f(psi, y, x_f, gp, dt, l_order, &lc); break;
+                        case 31: rk3_optimized_f(psi, y, x_f, gp, dt); break;
+                        case 41: rk4_optimized_b(psi, y, x_f, gp, dt, l_order, &lc); break;
+                        default: x_f[0] = x_f[1] = 0;
+                    }
                 }
-                og_diffeo_interpolate_2D(ChiX, ChiY, x_f[0], x_f[1], &x_f[0], &x_f[1], gm);
                 fx[0] += x_f[0] * c1[k];  fy[0] += x_f[1] * c1[k];
                 fx[1] += x_f[0] * cx[k];  fy[1] += x_f[1] * cx[k];
                 fx[2] += x_f[0] * cy[k];  fy[2] += x_f[1] * cy[k];
@@ -620,6 +732,12 @@ struct og_state {
     double* cbuf1; double* cbuf2; double* rbuf;
     double* parts[8];
     double* vels[8];        /* inertial velocity state per set */
+    /* forward map: active map, its stack, the forwarded particles' initial positions and
+     * the stack index each forwarded set starts from (init_map), last step's monitors */
+    double *ChiX_f, *ChiY_f, *stackX_f, *stackY_f;
+    double* fparts[8];
+    int init_map[8];
+    double einc_f, einv;
     double* t_vec; double* dt_vec; int t_cap;
     int loop_ctr, old_ctr;
 };
@@ -663,6 +781,14 @@ og_state* og_create(const og_settings* s)
         st->parts[i] = (double*)xmalloc(sizeof(double) * 2 * (size_t)s->psets[i].num);
         st->vels[i] = (double*)xmalloc(sizeof(double) * 2 * (size_t)s->psets[i].num);
     }
+    if (s->forward_map) {
+        st->ChiX_f = (double*)xmalloc(sizeof(double) * 4 * Nc);
+        st->ChiY_f = (double*)xmalloc(sizeof(double) * 4 * Nc);
+        st->stackX_f = (double*)xmalloc(sizeof(double) * 4 * Nc * (size_t)(s->max_maps > 0 ? s->max_maps : 1));
+        st->stackY_f = (double*)xmalloc(sizeof(double) * 4 * Nc * (size_t)(s->max_maps > 0 ? s->max_maps : 1));
+        for (int i = 0; i < s->n_fwd_sets; ++i)
+            st->fparts[i] = (double*)xmalloc(sizeof(double) * 2 * (size_t)(s->fsets[i].num > 0 ? s->fsets[i].num : 1));
+    }
     st->t_cap = 1 << 16;
     st->t_vec = (double*)xmalloc(sizeof(double) * st->t_cap);
     st->dt_vec = (double*)xmalloc(sizeof(double) * st->t_cap);
@@ -677,6 +803,8 @@ void og_destroy(og_state* st)
     free(st->stackX); free(st->stackY); free(st->xy);
     free(st->cbuf1); free(st->cbuf2); free(st->rbuf);
     for (int i = 0; i < st->s.n_particle_sets; ++i) { free(st->parts[i]); free(st->vels[i]); }
+    free(st->ChiX_f); free(st->ChiY_f); free(st->stackX_f); free(st->stackY_f);
+    for (int i = 0; i < st->s.n_fwd_sets; ++i) free(st->fparts[i]);
     free(st->t_vec); free(st->dt_vec);
     free(st);
 }
@@ -790,6 +918,23 @@ static void advect(og_state* st, const double* t, const double* dt, int loop_ctr
     double* ty = st->ChiY; st->ChiY = st->ChiY_new; st->ChiY_new = ty;
 }
 
+/* the forward map's step: advect_using_stream_hermite with direction 1 (cmm-euler2d.cu:780-786) */
+static void advect_forward(og_state* st, const double* t, const double* dt, int loop_ctr, int ti_num, int l_order)
+{
+    double L1[4] = {0, 0, 0, 0}, L12[4] = {0, 0, 0, 0};
+    int lcl = loop_ctr + l_order - 1;
+    for (int i = 0; i < l_order; ++i) {
+        L1[i] = og_get_L_coefficient(t, t[lcl + 1], lcl, i, l_order);
+        L12[i] = og_get_L_coefficient(t, t[lcl] + dt[lcl + 1] / 2.0, lcl, i, l_order);
+    }
+    double c1[12], cx[12], cy[12], cxy[12];
+    og_map_update_coefficients(st->s.map_update_order_num, st->s.map_epsilon, c1, cx, cy, cxy);
+    advect_map_dir(st->ChiX_f, st->ChiY_f, st->ChiX_new, st->ChiY_new, st->psi, &st->gc, &st->gp, dt[lcl + 1],
+                   st->s.map_epsilon, ti_num, st->s.map_update_order_num, l_order, L1, L12, c1, cx, cy, cxy, 1);
+    double* tx = st->ChiX_f; st->ChiX_f = st->ChiX_new; st->ChiX_new = tx;
+    double* ty = st->ChiY_f; st->ChiY_f = st->ChiY_new; st->ChiY_new = ty;
+}
+
 /* k_swap_h over whole Hermite levels: cmm-simulation-kernel.cu:62-74 */
 static void swap_levels(og_state* st, int a, int b)
 {
@@ -803,6 +948,8 @@ int og_init(og_state* st)
     og_settings* s = &st->s;
     long Np4 = 4 * st->gp.N;
     og_init_diffeo(st->ChiX, st->ChiY, &st->gc);
+    if (s->forward_map) og_init_diffeo(st->ChiX_f, st->ChiY_f, &st->gc);
+    for (int i = 0; i < 8; ++i) st->init_map[i] = 0;
     st->n_maps = 0;
     translate_ic(st);
     if (evaluate_stream(st)) return -1;
@@ -898,11 +1045,26 @@ int og_step(og_state* st, double dt_now, double* e_inc, int* remapped)
     st->t_vec[lcl + 1] = st->t_vec[lcl] + dt_now;
     st->dt_vec[lcl + 1] = dt_now;
     advect(st, st->t_vec, st->dt_vec, st->loop_ctr, s->time_integration_num, Lo);
+    if (s->forward_map) advect_forward(st, st->t_vec, st->dt_vec, st->loop_ctr, s->time_integration_num, Lo);
     double einc = og_incompressibility_check(&st->gf, &st->gc, st->ChiX, st->ChiY);
     *e_inc = einc; *remapped = 0;
     if (s->simulation_type_num == 2 && (einc <= 0 || einc > 1e15)) return 2;
+    /* forward map: invertibility and incompressibility on the coarse grid, and a forced remap
+     * in the step that reaches a forwarded set's start time (cmm-euler2d.cu:795-811) */
+    int forwarded_init = 0;
+    if (s->forward_map) {
+        st->einv = og_invertibility_check(&st->gc, &st->gc, st->ChiX, st->ChiY, &st->gc, st->ChiX_f, st->ChiY_f);
+        st->einc_f = og_incompressibility_check(&st->gc, &st->gc, st->ChiX_f, st->ChiY_f);
+        for (int i_p = 0; i_p < s->n_fwd_sets; ++i_p) {
+            double d = st->t_vec[lcl + 1] - s->fsets[i_p].init_time + s->dt * 1e-5;
+            if (d < st->dt_vec[lcl + 1] && d >= 0) {
+                forwarded_init = 1;
+                st->init_map[i_p] = st->n_maps + 1;
+            }
+        }
+    }
     int saturated = 0;
-    if (einc > s->incomp_threshold && !s->skip_remapping) {
+    if ((einc > s->incomp_threshold && !s->skip_remapping) || forwarded_init) {
         if (st->n_maps >= s->max_maps) saturated = 1;
         else {
             st->old_ctr = st->loop_ctr;
@@ -910,6 +1072,11 @@ int og_step(og_state* st, double dt_now, double* e_inc, int* remapped)
             long Nc4 = 4 * st->gc.N;
             memcpy(st->stackX + Nc4 * (size_t)st->n_maps, st->ChiX, sizeof(double) * Nc4);
             memcpy(st->stackY + Nc4 * (size_t)st->n_maps, st->ChiY, sizeof(double) * Nc4);
+            if (s->forward_map) {
+                memcpy(st->stackX_f + Nc4 * (size_t)st->n_maps, st->ChiX_f, sizeof(double) * Nc4);
+                memcpy(st->stackY_f + Nc4 * (size_t)st->n_maps, st->ChiY_f, sizeof(double) * Nc4);
+                og_init_diffeo(st->ChiX_f, st->ChiY_f, &st->gc);
+            }
             st->n_maps++;
             og_init_diffeo(st->ChiX, st->ChiY, &st->gc);
             *remapped = 1;
@@ -1070,4 +1237,91 @@ void og_state_zoom(const og_state* st, int n, const double* bounds4, int scalar_
 {
     og_state_view v = state_view(st);
     og_zoom_fields(&v, n, bounds4, scalar_num, out);
+}
+
+/* ------------------------------------------------------------------ */
+/* forward map outputs                                                 */
+
+double og_invertibility_check(const og_grid* gc, const og_grid* gb, const double* Xb, const double* Yb,
+                              const og_grid* gfw, const double* Xf, const double* Yf)
+{
+    double m = 0.0;
+    #pragma omp parallel for reduction(max : m) schedule(static)
+    for (long In = 0; In < gc->N; ++In) {
+        long iX = In % gc->NX, iY = In / gc->NX;
+        double x = gc->bounds[0] + iX * gc->hx + 0.5 * gc->hx, y = gc->bounds[2] + iY * gc->hy + 0.5 * gc->hy;
+        double a, b;
+        og_diffeo_interpolate_2D(Xf, Yf, x, y, &a, &b, gfw);
+        og_diffeo_interpolate_2D(Xb, Yb, a, b, &a, &b, gb);
+        double d = hypot(x - a, y - b);
+        if (d > m) m = d;
+    }
+    return m;
+}
+
+const double* og_chix_f(const og_state* st) { return st->ChiX_f; }
+const double* og_chiy_f(const og_state* st) { return st->ChiY_f; }
+void og_forward_monitors(const og_state* st, double* einc_f, double* einv) { *einc_f = st->einc_f; *einv = st->einv; }
+
+int og_set_forwarded_particles(og_state* st, int i, const double* pos)
+{
+    if (!st->s.forward_map || i < 0 || i >= st->s.n_fwd_sets) return -1;
+    memcpy(st->fparts[i], pos, sizeof(double) * 2 * (size_t)st->s.fsets[i].num);
+    return 0;
+}
+
+/* k_h_sample_points_map (cmm-simulation-kernel.cu:97-118): a point strictly inside the frame
+ * goes through the map and is wrapped to the domain; any other point becomes NaN */
+static void map_points(const double* X, const double* Y, const og_grid* gm, const og_grid* frame, const double* in,
+                       double* out, int num)
+{
+    double LX = gm->bounds[1] - gm->bounds[0], LY = gm->bounds[3] - gm->bounds[2];
+    for (int i = 0; i < num; ++i) {
+        double x = in[2 * i], y = in[2 * i + 1];
+        if (x > frame->bounds[0] && x < frame->bounds[1] && y > frame->bounds[2] && y < frame->bounds[3]) {
+            double a, b;
+            og_diffeo_interpolate_2D(X, Y, x, y, &a, &b, gm);
+            out[2 * i] = a - floor(a / LX) * LX;
+            out[2 * i + 1] = b - floor(b / LY) * LY;
+        } else {
+            out[2 * i] = out[2 * i + 1] = NAN;
+        }
+    }
+}
+
+void og_forward_sample(const og_state* st, int n, const double* bounds4, double* map_xy, double* parts)
+{
+    og_grid gz;
+    og_grid_fill(&gz, n, n, bounds4);
+    const og_grid* gm = &st->gc;
+    const og_settings* s = &st->s;
+    long Nc4 = 4 * gm->N;
+    int nm = st->n_maps;
+    /* the frame's nodes: forward stack oldest first, then the active forward map */
+    if (nm > 0) {
+        og_sample_map_compact(st->stackX_f, st->stackY_f, map_xy, gm, &gz);
+        for (int i = 1; i < nm; ++i) og_apply_map_compact(st->stackX_f + Nc4 * i, st->stackY_f + Nc4 * i, map_xy, gm, &gz);
+        og_apply_map_compact(st->ChiX_f, st->ChiY_f, map_xy, gm, &gz);
+    } else {
+        og_sample_map_compact(st->ChiX_f, st->ChiY_f, map_xy, gm, &gz);
+    }
+    if (!parts) return;
+    /* forwarded particles, each set from its start map on (apply_map_stack_points, direction 1) */
+    double* p = parts;
+    for (int i_p = 0; i_p < s->n_fwd_sets; ++i_p) {
+        int num = s->fsets[i_p].num, im = st->init_map[i_p];
+        double t0 = s->fsets[i_p].init_time;
+        const double* in = st->fparts[i_p];
+        if (nm > 0) {
+            if (t0 == 0) map_points(st->stackX_f, st->stackY_f, gm, &gz, in, p, num);
+            else memcpy(p, in, sizeof(double) * 2 * (size_t)num);
+            for (int i = 1; i < nm; ++i)
+                if ((i >= im && t0 != 0) || t0 == 0)
+                    map_points(st->stackX_f + Nc4 * i, st->stackY_f + Nc4 * i, gm, &gz, p, p, num);
+            if ((im != 0 && t0 != 0) || t0 == 0) map_points(st->ChiX_f, st->ChiY_f, gm, &gz, p, p, num);
+        } else {
+            map_points(st->ChiX_f, st->ChiY_f, gm, &gz, in, p, num);
+        }
+        p += 2 * (size_t)num;
+    }
 }

@@ -41,6 +41,10 @@ class OgParticleSet(C.Structure):
                 ("init_time", C.c_double), ("init_vel", C.c_int)]
 
 
+class OgFwdSet(C.Structure):
+    _fields_ = [("num", C.c_int), ("init_time", C.c_double)]
+
+
 class OgSettings(C.Structure):
     _fields_ = [("grid_coarse", C.c_int), ("grid_fine", C.c_int), ("grid_psi", C.c_int),
                 ("grid_vort", C.c_int), ("bounds", C.c_double * 4), ("dt", C.c_double),
@@ -51,7 +55,8 @@ class OgSettings(C.Structure):
                 ("freq_cut_psi", C.c_double), ("initial_condition_num", C.c_int),
                 ("initial_discrete", C.c_int), ("initial_discrete_grid", C.c_int),
                 ("max_maps", C.c_int), ("n_particle_sets", C.c_int),
-                ("psets", OgParticleSet * 8), ("simulation_type_num", C.c_int)]
+                ("psets", OgParticleSet * 8), ("simulation_type_num", C.c_int),
+                ("forward_map", C.c_int), ("n_fwd_sets", C.c_int), ("fsets", OgFwdSet * 8)]
 
 
 _lib = None
@@ -91,6 +96,12 @@ def lib():
         L.og_vlasov_state_mesure.argtypes = [C.c_void_p, dp]
         L.og_set_init_data.argtypes = [dp, dp]
         L.og_state_zoom.argtypes = [C.c_void_p, C.c_int, dp, C.c_int, dp]
+        for name in ("og_chix_f", "og_chiy_f"):
+            getattr(L, name).restype = dp
+            getattr(L, name).argtypes = [C.c_void_p]
+        L.og_forward_monitors.argtypes = [C.c_void_p, dp, dp]
+        L.og_set_forwarded_particles.argtypes = [C.c_void_p, C.c_int, dp]
+        L.og_forward_sample.argtypes = [C.c_void_p, C.c_int, dp, dp, dp]
         L.og_restart.argtypes = [C.c_void_p, C.c_double, C.c_int, dp, dp, dp, dp, dp]
         L.og_restart.restype = C.c_int
         for name in ("og_stack_x", "og_stack_y"):
@@ -144,6 +155,12 @@ class EulerOracle:
         s.initial_discrete_grid = cfg.get("initial_discrete_grid", 1)
         s.max_maps = cfg["max_maps"]
         s.simulation_type_num = int(cfg.get("simulation_type_num", 0))
+        s.forward_map = int(cfg.get("forward_map", 0))
+        fsets = cfg.get("forwarded", [])
+        s.n_fwd_sets = len(fsets)
+        for i, p in enumerate(fsets):
+            s.fsets[i].num = p["num"]
+            s.fsets[i].init_time = p["init_time"]
         psets = cfg.get("particles", [])
         s.n_particle_sets = len(psets)
         for i, p in enumerate(psets):
@@ -300,6 +317,38 @@ class EulerOracle:
         planes = {k: out[i * n * n:(i + 1) * n * n].copy() for i, k in enumerate(names)}
         return planes, dict(zip(("Energy", "Enstrophy", "Palinstrophy", "Max_vorticity", "Scalar_integral"),
                                 mes.tolist()))
+
+    # forward map
+    def chix_f(self):
+        return self._arr(self.L.og_chix_f, 4 * self.grid(0).N)
+
+    def chiy_f(self):
+        return self._arr(self.L.og_chiy_f, 4 * self.grid(0).N)
+
+    def forward_monitors(self):
+        """(forward incompressibility error, invertibility error) of the last step"""
+        a, b = C.c_double(), C.c_double()
+        self.L.og_forward_monitors(self.h, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def set_forwarded_particles(self, i, pos):
+        p = np.ascontiguousarray(pos, dtype=np.float64)
+        if self.L.og_set_forwarded_particles(self.h, i, _dp(p)):
+            raise ValueError("no forwarded particle set %d" % i)
+
+    def forward_sample(self, n, bounds):
+        """Forward map on an n x n frame (x planes, y planes) and the forwarded particle
+        positions of every set (list of 2*num arrays, NaN outside the frame)."""
+        xy = np.zeros(2 * n * n)
+        nums = [p["num"] for p in self.cfg.get("forwarded", [])]
+        parts = np.zeros(max(1, 2 * sum(nums)))
+        b = np.ascontiguousarray(bounds[:4], dtype=np.float64)
+        self.L.og_forward_sample(self.h, n, _dp(b), _dp(xy), _dp(parts))
+        out, k = [], 0
+        for m in nums:
+            out.append(parts[k:k + 2 * m].copy())
+            k += 2 * m
+        return xy[0::2].copy(), xy[1::2].copy(), out
 
     def zoom(self, n, bounds, scalar_num):
         """compute_zoom planes on an n x n window (bounds = x_min, x_max, y_min, y_max):

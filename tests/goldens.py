@@ -51,6 +51,7 @@ class DebugRecorder:
         self.s = settings
         self.st = state
         self.series = {}
+        self.forwarded = {}     # (t_now, set index) -> forwarded positions at a sample instant
 
     def _app(self, key, vals):
         self.series.setdefault(key, []).extend(vals)
@@ -97,6 +98,12 @@ class DebugRecorder:
             if _has(var, "Map_H", "Chi_H") or all_:
                 self._stat("Map_ChiX_H_coarse", stats_raw(st.chix()))
                 self._stat("Map_ChiY_H_coarse", stats_raw(st.chiy()))
+            if s.forward_map and (_has(var, "Map_f", "Chi_f") or all_):
+                self._stat("Map_ChiX_f_coarse", stats_grid(st.chix_f()[:gc[0]], gc[1], gc[2]))
+                self._stat("Map_ChiY_f_coarse", stats_grid(st.chiy_f()[:gc[0]], gc[1], gc[2]))
+            if s.forward_map and (_has(var, "Map_f_H", "Chi_f_H") or all_):
+                self._stat("Map_ChiX_f_H_coarse", stats_raw(st.chix_f()))
+                self._stat("Map_ChiY_f_H_coarse", stats_raw(st.chiy_f()))
             if "PartA_" in var or all_:
                 if not saved_any:
                     self._app("Debug_globals/Time_s", [t_now])
@@ -129,6 +136,13 @@ class DebugRecorder:
                 b = s.domain_bounds
                 hx, hy = (b[1] - b[0]) / n, (b[3] - b[2]) / n
                 self._app("Debug_globals/Time_s_%d" % n, [t_now])
+                if s.forward_map and (_has(var, "Map_f", "Chi_f") or all_ or s.particles_forwarded):
+                    fx, fy, parts = st.forward_sample(n, b[:4])
+                    if _has(var, "Map_f", "Chi_f") or all_:
+                        self._stat("Map_ChiX_f_%d" % n, stats_grid(fx, hx, hy))
+                        self._stat("Map_ChiY_f_%d" % n, stats_grid(fy, hx, hy))
+                    for i, p in enumerate(parts):
+                        self.forwarded[(t_now, i)] = p
                 planes, mes = st.sample(n, s.scalar_num)
 
                 def stat(name):
@@ -170,9 +184,14 @@ class DebugRecorder:
                 for rep in range(r.rep):
                     win = (r.pos_x - wx, r.pos_x + wx, r.pos_y - wy, r.pos_y + wy)
                     planes = st.zoom(n, win, s.scalar_num)
+                    if s.forward_map and (_has(var, "Map_f", "Chi_f") or all_):
+                        planes["Map_ChiX_f"], planes["Map_ChiY_f"], _ = st.forward_sample(n, win)
 
                     def stat(name):
                         self._stat("%s_%d_Zoom_%d_rep_%d" % (name, n, iz + 1, rep), stats_grid(planes[name], hx, hy))
+                    if s.forward_map and (_has(var, "Map_f", "Chi_f") or all_):
+                        stat("Map_ChiX_f")
+                        stat("Map_ChiY_f")
                     if _has(var, "Map_b", "Chi_b") or all_:
                         stat("Map_ChiX")
                         stat("Map_ChiY")
@@ -190,6 +209,10 @@ class DebugRecorder:
     def on_step(self, loop_ctr, t, e_inc, gap, maps):
         self._app("Time_s", [t])
         self._app("Error_incompressibility", [e_inc])
+        if self.s.forward_map:
+            ef, ev = self.st.forward_monitors()
+            self._app("Error_incompressibility_forward", [ef])
+            self._app("Error_invertibility", [ev])
         self._app("Map_gaps", [float(gap)])
         self._app("Map_counter", [float(maps)])
 
@@ -220,27 +243,32 @@ def compare_series(ours, gold, keys, rtol):
                 scale = np.maximum(area_scale, 1e-300)
             else:
                 scale = np.maximum(mag, 1e-300)
-        elif k == "Error_incompressibility":
-            # |1 - det grad X| with det ~ 1: the error is absolute on the scale of det
+        elif k in ("Error_incompressibility", "Error_incompressibility_forward", "Error_invertibility"):
+            # |1 - det grad X| with det ~ 1, |x - X_b(X_f(x))| with x ~ 1: deviations of O(1)
+            # quantities, absolute on their scale
             scale = np.ones_like(g)
         else:
             scale = np.maximum(np.abs(g), 1e-300)
         err = np.abs(o - g) / scale
-        m = re.match(r"Debug_globals/Map_Chi[XY]_(\d+)_(Min|Max|L2)$", k)
+        m = re.match(r"Debug_globals/Map_Chi[XY](?:_f)?_(\d+)(?:_Zoom_\d+_rep_\d+)?_(Min|Max|L2|Avg)$", k)
         if m:
-            # positions of a sampled backward map are wrapped into [0, W): a point whose
-            # composed position lies within rounding of the boundary lands at ~0 in one
-            # implementation and at ~W in another.  Accept whole periods of such points.
+            # positions of a sampled (backward or forward) map are wrapped into [0, W): a point
+            # whose composed position lies within rounding of the boundary lands at ~0 in one
+            # implementation and at ~W in another (for 4_nodes the line y = 0 is invariant, so
+            # such points always exist).  Accept whole periods of such points.
             n, stat = int(m.group(1)), m.group(2)
             W, near = 2 * np.pi, 1e-10
+            hh = (W / n) ** 2     # statistics use the spacing of the n x n grid over the domain
             if stat == "L2":
-                per = W * (W / n) ** 2
+                per = W * hh
                 kk = np.round((o - g) / per)
                 err = np.where(np.abs(kk) <= 4, np.abs(o - g - kk * per) / scale, err)
             elif stat == "Min":
                 err = np.where(np.minimum(o, g) < near * W, 0.0, err)
-            else:
+            elif stat == "Max":
                 err = np.where(np.maximum(o, g) > W * (1 - near), 0.0, err)
+            else:   # Avg = hx hy max(0, max)
+                err = np.where(np.maximum(o, g) > hh * W * (1 - near), 0.0, err)
         e = float(err.max()) if err.size else 0.0
         worst.append((k, e))
         if not np.all(err <= rtol):

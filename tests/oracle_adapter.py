@@ -6,10 +6,11 @@ import oracle as O
 
 
 class OracleRun:
-    def __init__(self, settings, particle_init=None, restart_files=None):
+    def __init__(self, settings, particle_init=None, restart_files=None, forwarded_init=None):
         self.s = settings
         self.o = O.EulerOracle(settings.oracle_config())
         self.particle_init = particle_init or {}
+        self.forwarded_init = forwarded_init or {}
         self.restart_files = restart_files
         self.loaded_maps = None
 
@@ -17,6 +18,8 @@ class OracleRun:
     def init(self):
         for i, pos in self.particle_init.items():
             self.o.set_particles(i, pos)
+        for i, pos in self.forwarded_init.items():
+            self.o.set_forwarded_particles(i, pos)
         if self.s.restart_time != 0:
             # the restart branch of the driver reads the stored state instead of
             # building the Lagrange history (cmm-euler2d.cu:520-685)
@@ -72,3 +75,16 @@ class OracleRun:
 
     def zoom(self, n, bounds, scalar_num):
         return self.o.zoom(n, bounds, scalar_num)
+
+    def chix_f(self):
+        return self.o.chix_f()
+
+    def chiy_f(self):
+        return self.o.chiy_f()
+
+    def forward_monitors(self):
+        return self.o.forward_monitors()
+
+    def forward_sample(self, n, bounds):
+        return self.o.forward_sample(n, bounds)
+

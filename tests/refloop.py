@@ -290,7 +290,8 @@ class Settings:
                     initial_condition_num=self.initial_condition_num,
                     initial_discrete=self.initial_discrete, initial_discrete_grid=self.initial_discrete_grid,
                     max_maps=self.cpu_map_num, simulation_type_num=self.simulation_type_num,
-                    initial_params=list(self.initial_params),
+                    initial_params=list(self.initial_params), forward_map=int(self.forward_map),
+                    forwarded=[dict(num=p.num, init_time=p.init_time) for p in self.particles_forwarded],
                     particles=[dict(num=p.num, tau=p.tau, time_integration_num=p.time_integration_num,
                                     init_time=p.init_time, init_vel=p.init_vel) for p in self.particles_advected])
 

@@ -1,0 +1,100 @@
+"""The forward map (forward_map = 1) on the GPU against the oracle.
+
+A run with remaps: the forward map is advected beside the backward one
+(k_advect_using_stream_hermite, direction 1), checked for invertibility and
+incompressibility each step, pushed onto its own stack at every remap, and composed
+oldest-first on the sample grid and on zoom windows (apply_map_stack, direction 1).
+Two forwarded particle sets: one from t = 0, one whose start time forces a remap and
+which is mapped only from the sub-map after it (apply_map_stack_points); particles
+leaving a zoom frame are NaN.  Every Debug_globals series, the two forward monitors per
+step and the raw forwarded-particle files are compared with the oracle, for each forward
+integrator (the reference's RK4 and RK4Mod quirks included).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import refloop
+from goldens import DebugRecorder, compare_series
+from oracle_adapter import OracleRun
+from product import cmm, read_monitoring
+from test_gpu_parity import map_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _text(ti):
+    rec = ("{num=%d,seed=%d,time_integration=RK3,init_name=uniform,init_time=%r,"
+           "init_param_1=3.141592653589793,init_param_2=3.141592653589793,init_param_3=6.283185307179586,"
+           "init_param_4=6.283185307179586}")
+    return "\n".join([
+        "CMM Parameter file", "param_version\t=\t3", "",
+        "simulation_type\t=\tcmm_euler_2d", "sim_name\t=\tfw", "initial_condition\t=\t4_nodes",
+        "grid_coarse\t=\t64", "grid_fine\t=\t128", "grid_vort\t=\t128", "grid_psi\t=\t64", "set_dt_by_steps\t=\t1",
+        "steps_per_sec\t=\t64", "final_time\t=\t0.25", "time_integration\t=\t%s" % ti, "map_update_order\t=\t4th",
+        "map_epsilon\t=\t0.001", "incomp_threshold\t=\t1e-05", "skip_remapping\t=\t0", "molly_stencil\t=\t0",
+        "lagrange_init_higher_order\t=\t1", "freq_cut_psi\t=\t32", "mem_RAM_CPU_remaps\t=\t200",
+        "save_map_stack\t=\t0", "verbose\t=\t4", "scalar_name\t=\tgaussian",
+        "save_computational_num\t=\t1",
+        "save_computational\t=\t{is_instant=0,time_start=0,time_end=10000,time_step=0.0625,var=All,conv=1}",
+        "save_sample_num\t=\t1",
+        "save_sample\t=\t{is_instant=0,time_start=0,time_end=10000,time_step=0.0625,var=All,grid=64}",
+        "save_zoom_num\t=\t1",
+        "save_zoom\t=\t{is_instant=0,time_start=0,time_end=10000,time_step=0.125,var=AllPartF_01,grid=48,"
+        "pos_x=2.5,pos_y=4.0,width_x=3.0,width_y=3.0,rep=2,rep_fac=0.5}",
+        "forward_map\t=\t1", "particles_advected_num\t=\t0", "particles_forwarded_num\t=\t2",
+        "particles_forwarded\t=\t" + rec % (400, 5, 0.0), "particles_forwarded\t=\t" + rec % (300, 6, 0.109375), ""])
+
+
+@pytest.mark.parametrize("ti", ["EulerExp", "Heun", "AB2", "RK3", "RK4", "RK3Mod", "RK4Mod"])
+def test_forward_map_run_matches_oracle(tmp_path, ti):
+    m = cmm()
+    text = _text(ti)
+    pf = tmp_path / "params.txt"
+    pf.write_text(text)
+    sim = m.Simulation(["param_file=%s" % pf, "workspace=%s/" % tmp_path])
+    sim.init()
+    f0 = [sim.field("Particles_forwarded_pos_P%02d" % (i + 1)).copy() for i in range(2)]
+    assert all(np.isfinite(f).all() for f in f0)
+    sim.run()
+    run_dir = os.path.join(str(tmp_path), "data", sim.file_name())
+    ours = read_monitoring(run_dir)
+    s = refloop.settings_from_param_text(text)
+    run = OracleRun(s, forwarded_init={0: f0[0], 1: f0[1]})
+    rec = DebugRecorder(s, run)
+    refloop.run_reference_loop(s, run, rec.on_save, rec.on_step)
+    assert max(rec.series["Map_counter"]) >= 2
+    assert len(ours["Error_invertibility"]) == 16
+    keys = list(rec.series)
+    assert len([k for k in keys if "_f_" in k]) >= 4 * 6
+    worst, fails = compare_series(ours, rec.series, keys, 1e-9)
+    assert not fails, fails
+    assert map_err(sim.field("Map_ChiX_f_H_coarse"), run.o.chix_f()) < 1e-10
+    # raw forwarded-particle files at every sample instant (the whole domain as frame)
+    n_files = 0
+    for (t, i), pos in rec.forwarded.items():
+        # folders are named with 3 significant digits (the reference's to_str), "final" at the end
+        folder = "Time_final" if t > 1e3 else "Time_%.3g" % t
+        got = np.fromfile(os.path.join(run_dir, "Particle_data", folder, "Particles_forwarded_pos_P%02d.data" % (i + 1)))
+        assert got.shape == pos.shape
+        assert np.array_equal(np.isnan(got), np.isnan(pos))
+        ok = ~np.isnan(pos)
+        dd = np.abs(got[ok] - pos[ok])
+        assert np.all(np.minimum(dd, 2 * np.pi - dd) < 1e-10), (t, i)
+        n_files += 1
+    assert n_files >= 8
+    # zoom frames: the first set's file (named P00 as in the reference), NaN outside the frame
+    zf = os.path.join(run_dir, "Zoom_data", "Time_final", "Zoom_1_rep_1", "Particles_forwarded_pos_P00.data")
+    z = np.fromfile(zf)
+    assert z.size == 800 and np.isnan(z).any() and np.isfinite(z).any()
+
+
+def test_forward_map_is_plain_fp64_only(tmp_path):
+    m = cmm()
+    pf = tmp_path / "params.txt"
+    pf.write_text(_text("RK3"))
+    sim = m.Simulation(["param_file=%s" % pf, "workspace=%s/" % tmp_path, "precision=mixed"])
+    with pytest.raises(m.CmmError) as e:
+        sim.init()
+    assert e.value.code == m.CMM_ERR_UNSUPPORTED

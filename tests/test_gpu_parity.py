@@ -245,7 +245,7 @@ def test_c1_full_run_matches_oracle_field_by_field(tmp_path, threshold):
         assert abs(sim.scalar(name) - ref) <= 1e-11 * abs(ref), name
 
 
-@pytest.mark.parametrize("name", ["init_sample", "init_particles", "init_zoom", "one_step", "remap_11b"])
+@pytest.mark.parametrize("name", ["init_sample", "init_particles", "init_zoom", "init_forward", "one_step", "remap_11b"])
 def test_reference_goldens_through_the_cli_interface(tmp_path, name):
     """The product, configured by the reference's own param file, writes the
     reference's monitoring files; they match every golden series, including the

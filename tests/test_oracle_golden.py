@@ -33,7 +33,7 @@ def _run(name):
     return rec, g, keys
 
 
-@pytest.mark.parametrize("name", ["init_comp", "init_conv", "init_sample", "init_zoom", "one_step"])
+@pytest.mark.parametrize("name", ["init_comp", "init_conv", "init_sample", "init_zoom", "init_forward", "one_step"])
 def test_oracle_matches_reference_goldens(name):
     rec, g, keys = _run(name)
     worst, fails = compare_series(rec.series, g["files"], keys, RTOL)

@@ -412,6 +412,144 @@ def run_t10(args):
     shutil.rmtree(work, ignore_errors=True)
 
 
+class MT19937_64:
+    """The 64-bit Mersenne Twister (Matsumoto and Nishimura, 2000) with the standard
+    seeding (the engine std::mt19937_64 names), for drawing the ensemble's members."""
+    def __init__(self, seed):
+        m = (1 << 64) - 1
+        self.mt = [seed & m]
+        for i in range(1, 312):
+            self.mt.append((6364136223846793005 * (self.mt[-1] ^ (self.mt[-1] >> 62)) + i) & m)
+        self.i = 312
+
+    def __call__(self):
+        m = (1 << 64) - 1
+        if self.i >= 312:
+            mt = self.mt
+            for k in range(312):
+                y = (mt[k] & 0xFFFFFFFF80000000) | (mt[(k + 1) % 312] & 0x7FFFFFFF)
+                mt[k] = mt[(k + 156) % 312] ^ (y >> 1) ^ (0xB5026F5AA96619E9 if y & 1 else 0)
+            self.i = 0
+        y = self.mt[self.i]
+        self.i += 1
+        y ^= (y >> 29) & 0x5555555555555555
+        y ^= (y << 17) & 0x71D67FFFEDA60000
+        y ^= (y << 37) & 0xFFF7EEE000000000
+        y ^= y >> 43
+        return y & m
+
+
+ENSEMBLE = dict(members=64, sizes=(64, 96, 128, 192, 256), seed=0, final_time=5.0, incomp_threshold=1e-3)
+
+
+def ensemble_members(n=ENSEMBLE["members"], seed=ENSEMBLE["seed"]):
+    """Member i: N = sizes[g() % 5], k0 = 4 + 12 u with u = (g() >> 11) 2^-53, g = mt19937_64(seed)."""
+    g = MT19937_64(seed)
+    out = []
+    for _ in range(n):
+        size = ENSEMBLE["sizes"][g() % len(ENSEMBLE["sizes"])]
+        k0 = 4.0 + 12.0 * ((g() >> 11) * 2.0 ** -53)
+        out.append((size, k0))
+    return out
+
+
+def ensemble_args(work, i, n, precision="mixed"):
+    """N / 4N / 2N grids (map / fine = vort / psi), dt = 1/(N/2) (the metric workload's
+    CFL ratio), remaps at 1e-3 (FP32 rounding of E_inc is ~0.75/N^2, 1.8e-4 at N = 64)."""
+    e = ENSEMBLE
+    return ["workspace=%s/" % work, "sim_name=e%02d_%s" % (i, precision), "simulation_type=cmm_euler_2d",
+            "grid_coarse=%d" % n, "grid_fine=%d" % (4 * n), "grid_vort=%d" % (4 * n), "grid_psi=%d" % (2 * n),
+            "set_dt_by_steps=1", "steps_per_sec=%d" % (n // 2), "final_time=%r" % e["final_time"],
+            "initial_condition=4_nodes", "initial_discrete=1", "initial_discrete_grid=%d" % (4 * n),
+            "time_integration=RK3", "map_update_order=4th", "map_epsilon=0.001",
+            "incomp_threshold=%r" % e["incomp_threshold"], "skip_remapping=0", "molly_stencil=0",
+            "freq_cut_psi=%d" % n, "lagrange_init_higher_order=1", "mem_RAM_CPU_remaps=100000",
+            "save_computational_num=0", "save_sample_num=0", "save_zoom_num=0", "forward_map=0",
+            "particles_advected_num=0", "save_map_stack=0", "verbose=0", "precision=%s" % precision]
+
+
+def run_ensemble(args):
+    """The 64-member ensemble of uneven sizes to T = 5: member-steps/s batched
+    (cmm_ensemble_*, autotuned persistent grids, CUDA graphs) against the same members
+    run one after another as single simulations, and every member's energy and
+    enstrophy against the member run alone in plain FP64."""
+    import __graft_entry__ as ge
+    ge.build()
+    m = ge.package()
+    import torch
+    members = ensemble_members()
+    ics = [initial_vorticity(4 * n, seed=i, k0=k0) for i, (n, k0) in enumerate(members)]
+    work = tempfile.mkdtemp(prefix="cmm_ens_")
+    stream = torch.cuda.Stream()
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, a.elapsed_time(b) / 1e3
+
+    res = {}
+    for graphs in ((True,) if args.ensemble_batched_only else (True, False)):
+        ens = m.Ensemble([ensemble_args(work, i, n) for i, (n, _) in enumerate(members)],
+                         stream=stream.cuda_stream, graphs=graphs)
+        for i, w in enumerate(ics):
+            ens.set_initial_discrete(i, w)
+        init_wall, _ = timed(ens.init)
+        wall, dev = timed(ens.run)
+        st = ens.stats()
+        res[graphs] = dict(st, init_s=init_wall, wall_s=wall, device_s=dev,
+                           member_steps_per_s=st["member_steps"] / wall,
+                           diag=[(ens.scalar(i, "energy"), ens.scalar(i, "enstrophy"),
+                                  int(ens.scalar(i, "map_counter"))) for i in range(len(members))])
+        ens.close()
+    if args.ensemble_batched_only:
+        b = res[True]
+        print(json.dumps({"batched_graphs": {k: v for k, v in b.items() if k != "diag"}}))
+        return
+    seq = {"mixed": dict(member_steps=0, wall_s=0.0, diag=[]), "fp64": dict(member_steps=0, wall_s=0.0, diag=[])}
+    for prec in ("mixed", "fp64"):
+        for i, (n, _) in enumerate(members):
+            sim = m.Simulation(ensemble_args(work, i, n, prec), stream=stream.cuda_stream)
+            sim.set_initial_discrete(ics[i])
+            sim.init()
+
+            def go():
+                while sim.step(1) != 1:
+                    seq[prec]["member_steps"] += 1
+
+            wall, _ = timed(go)
+            seq[prec]["wall_s"] += wall
+            seq[prec]["diag"].append((sim.scalar("energy"), sim.scalar("enstrophy"), int(sim.scalar("map_counter"))))
+            sim.close()
+    b, plain = res[True], seq["fp64"]
+    rel = [(abs(x[0] - y[0]) / abs(y[0]), abs(x[1] - y[1]) / abs(y[1])) for x, y in zip(b["diag"], plain["diag"])]
+    counts = {str(s): sum(1 for n, _ in members if n == s) for s in ENSEMBLE["sizes"]}
+    out = {"validation": "64-member ensemble of uneven sizes, batched vs one after another, vs plain FP64",
+           "workload": "euler2d-ensemble 64 members N in {64,96,128,192,256} (mt19937_64 seed 0), fine 4N, psi 2N, "
+                       "dt 1/(N/2), T=5, k0~U[4,16], remap 1e-3",
+           "sizes": counts, "unit": "member-steps/s",
+           "batched_graphs": {k: b[k] for k in ("member_steps", "iterations", "launches", "advect_blocks",
+                                                "sample_blocks", "init_s", "wall_s", "device_s",
+                                                "member_steps_per_s")},
+           "batched_no_graphs": {k: res[False][k] for k in ("wall_s", "member_steps_per_s")},
+           "sequential_mixed": {"member_steps": seq["mixed"]["member_steps"], "wall_s": seq["mixed"]["wall_s"],
+                                "member_steps_per_s": seq["mixed"]["member_steps"] / seq["mixed"]["wall_s"]},
+           "sequential_fp64": {"member_steps": plain["member_steps"], "wall_s": plain["wall_s"],
+                               "member_steps_per_s": plain["member_steps"] / plain["wall_s"]},
+           "speedup_vs_sequential_mixed": b["member_steps_per_s"] * seq["mixed"]["wall_s"] / seq["mixed"]["member_steps"],
+           "speedup_vs_sequential_fp64": b["member_steps_per_s"] * plain["wall_s"] / plain["member_steps"],
+           "max_energy_rel_err_vs_fp64": max(r[0] for r in rel),
+           "max_enstrophy_rel_err_vs_fp64": max(r[1] for r in rel),
+           "batched_equals_sequential_mixed_maps": sum(1 for x, y in zip(b["diag"], seq["mixed"]["diag"]) if x[2] == y[2]),
+           "remaps_batched": sum(x[2] for x in b["diag"]), "remaps_fp64": sum(y[2] for y in plain["diag"])}
+    print(json.dumps(out))
+    shutil.rmtree(work, ignore_errors=True)
+
+
 def run_ours(args):
     import __graft_entry__ as ge
     ge.build()
@@ -558,9 +696,13 @@ def main():
     ap.add_argument("--fp64-peak", action="store_true", help="measure the FP64 rate (cuBLAS DGEMM) and exit")
     ap.add_argument("--vlasov", action="store_true", help="run the Vlasov-Poisson configuration in both forms")
     ap.add_argument("--vlasov-final", type=float, default=VLASOV["final_time"])
+    ap.add_argument("--ensemble", action="store_true", help="run the 64-member ensemble batched and one by one")
+    ap.add_argument("--ensemble-batched-only", action="store_true", help="with --ensemble: only the batched run")
     args = ap.parse_args()
     if args.fp64_peak:
         measure_fp64_peak()
+    elif args.ensemble:
+        run_ensemble(args)
     elif args.vlasov:
         run_vlasov(args)
     elif args.impl == "reference":

@@ -30,7 +30,10 @@ EXPORTS = [
     "cmm_file_name", "cmm_destroy", "cmm_advect_map", "cmm_incomp_max", "cmm_compose_stack", "cmm_sample_vort",
     "cmm_poisson_create", "cmm_poisson_hermite", "cmm_poisson_destroy", "cmm_particles_advect", "cmm_diagnostics",
     "cmm_diagnostics_noalloc", "cmm_compose_stack_var", "cmm_vlasov_create", "cmm_vlasov_potential",
-    "cmm_vlasov_diagnostics", "cmm_vlasov_destroy",
+    "cmm_vlasov_diagnostics", "cmm_vlasov_destroy", "cmm_ensemble_create", "cmm_ensemble_set_initial_discrete",
+    "cmm_ensemble_set_graphs", "cmm_ensemble_init", "cmm_ensemble_step", "cmm_ensemble_run",
+    "cmm_ensemble_get_scalar", "cmm_ensemble_get_field", "cmm_ensemble_field_bytes", "cmm_ensemble_stats",
+    "cmm_ensemble_destroy",
 ]
 
 
@@ -96,6 +99,18 @@ def lib():
     L.cmm_vlasov_potential.argtypes = [vp, gp, gp, vp, vp, vp, ip, vp]
     L.cmm_vlasov_diagnostics.argtypes = [vp, gp, vp, vp, dp]
     L.cmm_vlasov_destroy.argtypes = [vp]
+    L.cmm_ensemble_create.argtypes = [ip, C.POINTER(ip), C.POINTER(C.c_char_p), vp, C.POINTER(vp)]
+    L.cmm_ensemble_set_initial_discrete.argtypes = [vp, ip, dp, C.c_size_t]
+    L.cmm_ensemble_set_graphs.argtypes = [vp, ip]
+    L.cmm_ensemble_init.argtypes = [vp]
+    L.cmm_ensemble_step.argtypes = [vp, ip]
+    L.cmm_ensemble_run.argtypes = [vp]
+    L.cmm_ensemble_get_scalar.argtypes = [vp, ip, C.c_char_p, dp]
+    L.cmm_ensemble_get_field.argtypes = [vp, ip, C.c_char_p, vp, C.c_size_t]
+    L.cmm_ensemble_field_bytes.argtypes = [vp, ip, C.c_char_p]
+    L.cmm_ensemble_field_bytes.restype = C.c_size_t
+    L.cmm_ensemble_stats.argtypes = [vp, C.POINTER(C.c_longlong)]
+    L.cmm_ensemble_destroy.argtypes = [vp]
     _lib = L
     return L
 
@@ -283,3 +298,67 @@ class VlasovPotential:
 
     def __del__(self):
         self.close()
+
+
+class Ensemble:
+    """Many mixed-form runs of uneven sizes advanced together (cmm_ensemble_*): members[i] is
+    the argument list member i would get as a Simulation."""
+
+    def __init__(self, members, stream=None, graphs=True):
+        L = lib()
+        flat, counts = [], []
+        for argv in members:
+            args = ["cmm"] + [str(a) for a in argv]
+            flat += args
+            counts.append(len(args))
+        self._keep = [a.encode() for a in flat]
+        arr = (C.c_char_p * len(flat))(*self._keep)
+        cnt = (C.c_int * len(counts))(*counts)
+        h = C.c_void_p()
+        check(L.cmm_ensemble_create(len(counts), cnt, arr, stream, C.byref(h)))
+        self.h, self.L, self.n = h, L, len(counts)
+        check(L.cmm_ensemble_set_graphs(self.h, 1 if graphs else 0))
+
+    def close(self):
+        if self.h:
+            self.L.cmm_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_initial_discrete(self, i, values):
+        import numpy as np
+        v = np.ascontiguousarray(values, dtype=np.float64).ravel()
+        check(self.L.cmm_ensemble_set_initial_discrete(self.h, i, v.ctypes.data_as(C.POINTER(C.c_double)), v.size))
+
+    def init(self):
+        check(self.L.cmm_ensemble_init(self.h))
+
+    def step(self, n=1):
+        return check(self.L.cmm_ensemble_step(self.h, int(n)), allow=(CMM_ERR_SATURATED,))
+
+    def run(self):
+        return check(self.L.cmm_ensemble_run(self.h), allow=(CMM_ERR_SATURATED,))
+
+    def scalar(self, i, name):
+        out = C.c_double()
+        check(self.L.cmm_ensemble_get_scalar(self.h, i, name.encode(), C.byref(out)))
+        return out.value
+
+    def field(self, i, name):
+        import numpy as np
+        nb = self.L.cmm_ensemble_field_bytes(self.h, i, name.encode())
+        if nb == 0:
+            raise CmmError(CMM_ERR_NOT_FOUND, "unknown field " + name)
+        out = np.empty(nb // 8, dtype=np.float64)
+        check(self.L.cmm_ensemble_get_field(self.h, i, name.encode(), out.ctypes.data_as(C.c_void_p), nb))
+        return out
+
+    def stats(self):
+        """{member_steps, iterations, launches, members, advect_blocks, sample_blocks}"""
+        out = (C.c_longlong * 6)()
+        check(self.L.cmm_ensemble_stats(self.h, out))
+        return dict(zip(("member_steps", "iterations", "launches", "members", "advect_blocks", "sample_blocks"),
+                        list(out)))
+

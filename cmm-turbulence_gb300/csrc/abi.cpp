@@ -8,6 +8,7 @@
 #include <new>
 #include <string>
 
+#include "ensemble.hpp"
 #include "kernels.hpp"
 #include "settings.hpp"
 #include "sim.hpp"
@@ -22,6 +23,14 @@ struct cmm_ctx {
     cmm::EulerSim* sim = nullptr;
     cudaStream_t stream = nullptr;
     std::vector<double> discrete;
+};
+
+struct cmm_ensemble {
+    std::vector<cmm::Settings> settings;
+    std::vector<std::vector<double>> discrete;
+    cmm::EnsembleSim* ens = nullptr;
+    cudaStream_t stream = nullptr;
+    bool graphs = true;
 };
 
 struct cmm_poisson {
@@ -495,6 +504,141 @@ int cmm_diagnostics(const cmm_grid* grid_psi, const double* psi, const cmm_grid*
     out3[1] = 0.5 * gc.hx * gc.hy * h[1];
     double w_max = h[5] > 0 ? h[5] : 0.0, w_min = h[4] < 0 ? h[4] : 0.0;
     out3[2] = w_max > -w_min ? w_max : -w_min;
+    return CMM_OK;
+}
+
+// ---------------------------------------------------------------- ensembles
+int cmm_ensemble_create(int n_members, const int* argc, const char* const* argv, void* stream, cmm_ensemble** out)
+{
+    if (!out) return fail(CMM_ERR_PARAM, "out is NULL");
+    *out = nullptr;
+    if (n_members <= 0 || !argc || !argv) return fail(CMM_ERR_PARAM, "an ensemble needs members and their arguments");
+    cmm_ensemble* e = new (std::nothrow) cmm_ensemble();
+    if (!e) return fail(CMM_ERR_PARAM, "out of host memory");
+    e->stream = static_cast<cudaStream_t>(stream);
+    const char* const* a = argv;
+    for (int i = 0; i < n_members; ++i) {
+        cmm::Settings st;
+        if (argc[i] < 0 || !st.apply_cli(argc[i], a)) {
+            std::string msg = "member " + std::to_string(i) + ": " + st.error;
+            delete e;
+            return fail(msg.find("parameter file") != std::string::npos ? CMM_ERR_IO : CMM_ERR_PARAM, msg);
+        }
+        st.file_name = st.derived_file_name();
+        e->settings.push_back(st);
+        a += argc[i];
+    }
+    e->discrete.resize((size_t)n_members);
+    *out = e;
+    g_err.clear();
+    return CMM_OK;
+}
+
+int cmm_ensemble_set_initial_discrete(cmm_ensemble* e, int member, const double* v, size_t n)
+{
+    if (!e || !v) return fail(CMM_ERR_PARAM, "NULL argument");
+    if (e->ens) return fail(CMM_ERR_STATE, "cmm_ensemble_set_initial_discrete after cmm_ensemble_init");
+    if (member < 0 || member >= (int)e->settings.size()) return fail(CMM_ERR_PARAM, "no such member");
+    size_t need = (size_t)e->settings[(size_t)member].initial_discrete_grid * e->settings[(size_t)member].initial_discrete_grid;
+    if (n != need) return fail(CMM_ERR_PARAM, "discrete initial condition needs initial_discrete_grid^2 values");
+    e->discrete[(size_t)member].assign(v, v + n);
+    return CMM_OK;
+}
+
+int cmm_ensemble_set_graphs(cmm_ensemble* e, int on)
+{
+    if (!e) return fail(CMM_ERR_PARAM, "ensemble is NULL");
+    e->graphs = on != 0;
+    if (e->ens) e->ens->use_graphs = e->graphs;
+    return CMM_OK;
+}
+
+int cmm_ensemble_init(cmm_ensemble* e)
+{
+    if (!e) return fail(CMM_ERR_PARAM, "ensemble is NULL");
+    if (e->ens) return fail(CMM_ERR_STATE, "cmm_ensemble_init called twice");
+    cmm::EnsembleSim* ens = new (std::nothrow) cmm::EnsembleSim(e->settings);
+    if (!ens) return fail(CMM_ERR_PARAM, "out of host memory");
+    ens->stream = e->stream;
+    ens->use_graphs = e->graphs;
+    for (int i = 0; i < ens->size(); ++i) {
+        const auto& d = e->discrete[(size_t)i];
+        if (!d.empty() && ens->set_initial_discrete(i, d.data(), d.size())) {
+            std::string msg = ens->err;
+            delete ens;
+            return fail(CMM_ERR_PARAM, msg);
+        }
+    }
+    int rc = ens->init();
+    if (rc) {
+        std::string msg = ens->err;
+        delete ens;
+        return fail(rc, msg);
+    }
+    e->ens = ens;
+    return CMM_OK;
+}
+
+int cmm_ensemble_step(cmm_ensemble* e, int n)
+{
+    if (!e || !e->ens) return fail(CMM_ERR_STATE, "cmm_ensemble_step before cmm_ensemble_init");
+    for (int k = 0; k < n; ++k) {
+        int rc = e->ens->step();
+        if (rc == 1) return 1;
+        if (rc) return fail(rc, e->ens->err);
+    }
+    return CMM_OK;
+}
+
+int cmm_ensemble_run(cmm_ensemble* e)
+{
+    if (!e || !e->ens) return fail(CMM_ERR_STATE, "cmm_ensemble_run before cmm_ensemble_init");
+    int rc = e->ens->run();
+    return rc ? fail(rc, e->ens->err) : CMM_OK;
+}
+
+int cmm_ensemble_get_scalar(cmm_ensemble* e, int member, const char* name, double* out)
+{
+    if (!e || !e->ens || !name || !out) return fail(CMM_ERR_STATE, "ensemble not initialised or NULL argument");
+    if (member < 0 || member >= e->ens->size()) return fail(CMM_ERR_PARAM, "no such member");
+    cmm::EulerSim& s = e->ens->member(member);
+    int rc = s.get_scalar(name, out);
+    return rc ? fail(rc, s.err) : CMM_OK;
+}
+
+int cmm_ensemble_get_field(cmm_ensemble* e, int member, const char* name, void* dst, size_t bytes)
+{
+    if (!e || !e->ens || !name || (!dst && bytes)) return fail(CMM_ERR_STATE, "ensemble not initialised or NULL argument");
+    if (member < 0 || member >= e->ens->size()) return fail(CMM_ERR_PARAM, "no such member");
+    cmm::EulerSim& s = e->ens->member(member);
+    int rc = s.get_field(name, dst, bytes);
+    return rc ? fail(rc, s.err) : CMM_OK;
+}
+
+size_t cmm_ensemble_field_bytes(cmm_ensemble* e, int member, const char* name)
+{
+    if (!e || !e->ens || !name || member < 0 || member >= e->ens->size()) return 0;
+    return e->ens->member(member).field_bytes(name);
+}
+
+int cmm_ensemble_stats(cmm_ensemble* e, long long* out6)
+{
+    if (!e || !e->ens || !out6) return fail(CMM_ERR_STATE, "ensemble not initialised or NULL argument");
+    cmm::EnsembleSim& x = *e->ens;
+    out6[0] = x.member_steps;
+    out6[1] = x.iterations;
+    out6[2] = x.launches;
+    out6[3] = x.size();
+    out6[4] = x.blocks[cmm::kEnsAdvect];
+    out6[5] = x.blocks[cmm::kEnsSampleVort];
+    return CMM_OK;
+}
+
+int cmm_ensemble_destroy(cmm_ensemble* e)
+{
+    if (!e) return CMM_OK;
+    delete e->ens;
+    delete e;
     return CMM_OK;
 }
 

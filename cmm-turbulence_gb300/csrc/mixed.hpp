@@ -87,4 +87,48 @@ cudaError_t launch_planes_to_map(const double* X, const double* Y, const Grid& g
 // sum psi_x^2 + psi_y^2 (FP64 accumulation) -> out[0]
 cudaError_t launch_energy_m(const float4* psi, long long n, double* scratch, double* out, cudaStream_t s);
 
+// ---------------------------------------------------------------- ensembles
+// Lagrange coefficients of three psi levels for three combinations
+struct Combo3 { float c[3][3]; };
+
+// one member of an ensemble step, as the batched kernels see it (csrc/ensemble.cpp fills it)
+struct EnsMember {
+    AdvectMArgs adv;                 // advection of the member's map (gm, gp, map, out, combinations, ...)
+    int active;                      // 0: the member's tiles do nothing
+    int r_check;                     // check points per map cell and axis (fine / map)
+    float ir_check;
+    int fused;                       // the nodes pass also writes the three Lagrange combinations
+    unsigned long long* einc;        // the member's incompressibility result (FP64 bits)
+    Grid gv, gf;                     // vort and fine grids
+    const float4* wfm;               // fine vorticity nodes
+    float* sample_out;               // omega on the vort grid (R2C input, class buffer slot)
+    const float2* spec_v;            // its half spectrum (class buffer slot)
+    float2* spec4;                   // the four psi spectra (C2R input, class buffer slot)
+    const float* planes;             // the four psi planes (C2R output, class buffer slot)
+    float freq, inv_nv;              // psi cut-off frequency, 1 / N of the vort grid
+    float4* psi_new;                 // the new psi level's nodes
+    const float4* lv1n;              // levels 1 and 2 after the rotation (fused combinations)
+    const float4* lv2n;
+    float4* o1;
+    float4* o2;
+    float4* o3;
+    Combo3 cm;
+    double* vort;                    // coarse vorticity
+    int precombine;                  // combine lv0..lv2 into pa (ca) and pb (cb) before the advection
+    const float4* lv0;
+    const float4* lv1;
+    const float4* lv2;
+    float4* pa;
+    float4* pb;
+    float ca[3], cb[3];
+    int pad_;
+};
+
+enum { kEnsAdvect = 0, kEnsIncomp, kEnsSampleVort, kEnsSampleCoarse, kEnsSpec, kEnsNodes, kEnsPrecombine, kEnsKinds };
+// one batched launch of kernel kind over the work list cum (M members, cum[M] tiles) with
+// blocks persistent blocks; TI / lpn_log2 for the advection
+cudaError_t launch_ens(int kind, int TI, const EnsMember* mem, const int* cum, int M, int blocks, int lpn_log2,
+                       cudaStream_t s);
+
 }  // namespace cmm
+

@@ -214,7 +214,6 @@ __global__ void k_precombine(const float4* __restrict__ p0, const float4* __rest
 // the psi solve's last pass for three Lagrange levels: the new level's four FP32
 // planes -> its nodes, and in the same pass three combinations of the levels
 // (new, 1, 2), accumulated in the order of k_precombine so the results are identical
-struct Combo3 { float c[3][3]; };
 
 __device__ __forceinline__ float4 combo(const float* c, const float4& v0, const float4& v1, const float4& v2)
 {
@@ -271,15 +270,13 @@ cudaError_t launch_precombine(float4* const* levels, int L, const double* cA, co
 // new map:  d = d(node) + sum c1 g,  d_x = sum cx g,  d_y = sum cy g,  d_xy = sum cxy g
 // (the identity parts sum c1 e = 0, sum cx e_x = 1, ... are applied exactly).
 // ---------------------------------------------------------------------------
+// one 256-lane tile of the advection: global lane t of the map a (the footpoint weights
+// already in shared memory, sc); shared by the single-map and the ensemble launches
 template <int TI>
-__global__ void __launch_bounds__(256) k_advect_m(const AdvectMArgs a, int lpn_log2)
+__device__ __forceinline__ void advect_m_tile(const AdvectMArgs& a, int lpn_log2, long long t,
+                                              const float (&sc)[4][kMaxFoot])
 {
-    __shared__ float sc[4][kMaxFoot];
-    if (threadIdx.x < 4 * kMaxFoot) sc[threadIdx.x / kMaxFoot][threadIdx.x % kMaxFoot] =
-        a.coef[threadIdx.x / kMaxFoot][threadIdx.x % kMaxFoot];
-    __syncthreads();
     const int lpn = 1 << lpn_log2;
-    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     long long node = t >> lpn_log2;
     int k = (int)(t & (lpn - 1));
     bool live = node < a.gm.N;
@@ -369,6 +366,16 @@ __global__ void __launch_bounds__(256) k_advect_m(const AdvectMArgs a, int lpn_l
         if (plane == 0) acc += comp ? n0.y : n0.x;
         reinterpret_cast<float*>(a.out)[8 * node + k] = acc;
     }
+}
+
+template <int TI>
+__global__ void __launch_bounds__(256) k_advect_m(const AdvectMArgs a, int lpn_log2)
+{
+    __shared__ float sc[4][kMaxFoot];
+    if (threadIdx.x < 4 * kMaxFoot) sc[threadIdx.x / kMaxFoot][threadIdx.x % kMaxFoot] =
+        a.coef[threadIdx.x / kMaxFoot][threadIdx.x % kMaxFoot];
+    __syncthreads();
+    advect_m_tile<TI>(a, lpn_log2, blockIdx.x * (long long)blockDim.x + threadIdx.x, sc);
 }
 
 // ---------------------------------------------------------------------------
@@ -590,20 +597,20 @@ __device__ __forceinline__ void ycol_grad(const YCol& c, const W4f& wx, const W4
 
 constexpr int kMaxCheckRatio = 32;   // check points per map cell and axis
 
-__global__ void __launch_bounds__(256) k_incomp_m(Grid gm, int r, float ir, const float4* __restrict__ M,
-                                                  unsigned long long* result)
+// x-weights of the r check columns of a map cell (shared by the threads of a block)
+__device__ __forceinline__ void incomp_tables(const Grid& gm, int r, float ir, W4f* sw, W4f* sd)
 {
-    __shared__ W4f sw[kMaxCheckRatio], sd[kMaxCheckRatio];   // x-weights of the r check columns
-    __shared__ F2 wmax[8];
     if ((int)threadIdx.x < r) {
         float tx = ((float)threadIdx.x + 0.5f) * ir;
         sw[threadIdx.x] = value_weights_f(tx, gm.hxf);
         sd[threadIdx.x] = slope_weights_f(tx, gm.ihxf);
     }
-    __syncthreads();
-    F2 best = {0.0f, 0.0f};
-    const int total = (int)gm.N * r;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+}
+
+// check item i (map cell, row of check points in it): the largest deviation over its r points
+__device__ __forceinline__ void incomp_item(const Grid& gm, int r, float ir, const float4* __restrict__ M, int i,
+                                            const W4f* sw, const W4f* sd, F2& best)
+{
         int cell = i / r, sub_y = i - cell * r;
         int cy = cell / gm.NX, cx = cell - cy * gm.NX;
         int cx1 = cx + 1 == gm.NX ? 0 : cx + 1, cy1 = cy + 1 == gm.NY ? 0 : cy + 1;
@@ -627,7 +634,11 @@ __global__ void __launch_bounds__(256) k_incomp_m(Grid gm, int r, float ir, cons
             F2 dev = abs_det_deviation(Xx, Yy, Xy, Yx);
             if (f2_greater(dev, best)) best = dev;
         }
-    }
+}
+
+// block maximum of best (an exact FP32 pair), one atomicMax of its FP64 value into result
+__device__ __forceinline__ void incomp_block_max(F2 best, F2* wmax, unsigned long long* result)
+{
     for (int o = 16; o > 0; o >>= 1) {
         F2 v;
         v.hi = __shfl_xor_sync(0xffffffffu, best.hi, o);
@@ -642,6 +653,20 @@ __global__ void __launch_bounds__(256) k_incomp_m(Grid gm, int r, float ir, cons
         double dev = (double)best.hi + (double)best.lo;   // non-negative: its bits order like its value
         atomicMax(result, (unsigned long long)__double_as_longlong(dev));
     }
+}
+
+__global__ void __launch_bounds__(256) k_incomp_m(Grid gm, int r, float ir, const float4* __restrict__ M,
+                                                  unsigned long long* result)
+{
+    __shared__ W4f sw[kMaxCheckRatio], sd[kMaxCheckRatio];
+    __shared__ F2 wmax[8];
+    incomp_tables(gm, r, ir, sw, sd);
+    __syncthreads();
+    F2 best = {0.0f, 0.0f};
+    const int total = (int)gm.N * r;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x)
+        incomp_item(gm, r, ir, M, i, sw, sd, best);
+    incomp_block_max(best, wmax, result);
 }
 
 cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_result, cudaStream_t s)
@@ -852,15 +877,12 @@ cudaError_t launch_compose_pos_m(const Grid& gm, const Grid& gt, const float4* m
 // y once, then the ro output points of the cell in that row are evaluated
 // (x-weights from a table); positions are integer node + FP32 offset.
 // ---------------------------------------------------------------------------
+// map column mx, output row iY of the sample (x-weights of the ro output columns in swx)
 template <typename T>
-__global__ void __launch_bounds__(256) k_sample_m(Grid gm, Grid go, Grid gf, int ro, int rf, float iro,
-                                                  const float4* __restrict__ map, const float4* __restrict__ W,
-                                                  T* __restrict__ out)
+__device__ __forceinline__ void sample_m_item(const Grid& gm, const Grid& go, const Grid& gf, int ro, int rf, float iro,
+                                              const float4* __restrict__ map, const float4* __restrict__ W,
+                                              T* __restrict__ out, int mx, int iY, const W4f* swx)
 {
-    __shared__ W4f swx[kMaxCheckRatio];
-    if ((int)threadIdx.x < ro) swx[threadIdx.x] = value_weights_f((float)threadIdx.x * iro, gm.hxf);
-    __syncthreads();
-    const int mx = blockIdx.x * blockDim.x + threadIdx.x, iY = blockIdx.y;
     if (mx >= gm.NX) return;
     const int my = iY / ro, sy = iY - my * ro;
     const int mx1 = mx + 1 == gm.NX ? 0 : mx + 1, my1 = my + 1 == gm.NY ? 0 : my + 1;
@@ -891,6 +913,17 @@ __global__ void __launch_bounds__(256) k_sample_m(Grid gm, Grid go, Grid gf, int
         q.c00 = __ldg(W + c.i00); q.c10 = __ldg(W + c.i10); q.c01 = __ldg(W + c.i01); q.c11 = __ldg(W + c.i11);
         row[iX] = (T)herm_value_f(q, value_weights_f(c.tx, gf.hxf), value_weights_f(c.ty, gf.hyf));
     }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_sample_m(Grid gm, Grid go, Grid gf, int ro, int rf, float iro,
+                                                  const float4* __restrict__ map, const float4* __restrict__ W,
+                                                  T* __restrict__ out)
+{
+    __shared__ W4f swx[kMaxCheckRatio];
+    if ((int)threadIdx.x < ro) swx[threadIdx.x] = value_weights_f((float)threadIdx.x * iro, gm.hxf);
+    __syncthreads();
+    sample_m_item<T>(gm, go, gf, ro, rf, iro, map, W, out, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y, swx);
 }
 
 cudaError_t launch_sample_m(const Grid& gm, const Grid& go, const Grid& gf, const float4* map, const float4* W,
@@ -1235,10 +1268,9 @@ cudaError_t launch_fix_to_pos(const unsigned long long* in, int num, const Grid&
 // FP32 spectral step of the psi solve and layout conversions
 // ---------------------------------------------------------------------------
 // (integer forms of the reference's "index > N/2.0" tests: 2*index > N)
-__global__ void k_spec_psi_f(const float2* __restrict__ Fv, Grid gv, Grid gp, float freq, float inv_nv,
-                             float2* __restrict__ out4)
+__device__ __forceinline__ void spec_psi_item(const float2* __restrict__ Fv, const Grid& gv, const Grid& gp, float freq,
+                                              float inv_nv, float2* __restrict__ out4, int iXc, int iYc)
 {
-    const int iXc = blockIdx.x * blockDim.x + threadIdx.x, iYc = blockIdx.y;
     if (iXc >= gp.NX_fft) return;
     const long long i = (long long)iYc * gp.NX_fft + iXc;
     const bool hx = 2 * iXc > gp.NX, hy = 2 * iYc > gp.NY;
@@ -1263,6 +1295,12 @@ __global__ void k_spec_psi_f(const float2* __restrict__ Fv, Grid gv, Grid gp, fl
     out4[gp.Nfft + i] = make_float2(-P.y * kx, P.x * kx);
     out4[2 * gp.Nfft + i] = Py;
     out4[3 * gp.Nfft + i] = make_float2(-Py.y * kx, Py.x * kx);
+}
+
+__global__ void k_spec_psi_f(const float2* __restrict__ Fv, Grid gv, Grid gp, float freq, float inv_nv,
+                             float2* __restrict__ out4)
+{
+    spec_psi_item(Fv, gv, gp, freq, inv_nv, out4, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
 }
 
 cudaError_t launch_spec_psi_f(const float2* Fv, const Grid& gv, const Grid& gp, double freq, float2* out4, cudaStream_t s)
@@ -1381,6 +1419,177 @@ cudaError_t launch_energy_m(const float4* psi, long long n, double* scratch, dou
     int nb = (int)(need < kReduceBlocks ? (need > 0 ? need : 1) : kReduceBlocks);
     k_energy_partial<<<nb, 256, 0, s>>>(psi, n, scratch);
     k_energy_final<<<1, 256, 0, s>>>(scratch, nb, out);
+    return cudaGetLastError();
+}
+
+// ===========================================================================
+// Ensembles: every member's step kernels in one launch.  A launch covers a work
+// list of 256-thread tiles, member m owning tiles [cum[m], cum[m+1]); blocks walk
+// the list with a grid stride, so the grid size is a tuning choice, not a
+// function of the work.  Each tile runs the same device body as the single-member
+// kernel on that member's descriptor (copied to shared memory), so a member of an
+// ensemble computes exactly what it computes alone.
+// ===========================================================================
+namespace {
+
+__device__ __forceinline__ int ens_member_of(const int* __restrict__ cum, int M, int tile)
+{
+    int lo = 0, hi = M - 1;
+    while (lo < hi) {   // last m with cum[m] <= tile
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(cum + mid) <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// copy a descriptor into shared memory, 4 bytes per thread
+template <typename T>
+__device__ __forceinline__ void ens_load(T& dst, const T* src)
+{
+    static_assert(sizeof(T) % 4 == 0, "descriptor size");
+    const int* s = reinterpret_cast<const int*>(src);
+    int* d = reinterpret_cast<int*>(&dst);
+    for (int k = threadIdx.x; k < (int)(sizeof(T) / 4); k += blockDim.x) d[k] = __ldg(s + k);
+}
+
+}  // namespace
+
+template <int TI>
+__global__ void __launch_bounds__(256) k_ens_advect(const EnsMember* __restrict__ mem, const int* __restrict__ cum, int M,
+                                                    int lpn_log2)
+{
+    __shared__ float sc[4][kMaxFoot];
+    __shared__ AdvectMArgs sa;
+    const int total = __ldg(cum + M);
+    for (int tile = blockIdx.x; tile < total; tile += gridDim.x) {
+        const int m = ens_member_of(cum, M, tile);
+        if (!mem[m].active) continue;   // the same member for every thread of the block
+        ens_load(sa, &mem[m].adv);
+        __syncthreads();
+        if (threadIdx.x < 4 * kMaxFoot) sc[threadIdx.x / kMaxFoot][threadIdx.x % kMaxFoot] =
+            sa.coef[threadIdx.x / kMaxFoot][threadIdx.x % kMaxFoot];
+        __syncthreads();
+        advect_m_tile<TI>(sa, lpn_log2, (long long)(tile - __ldg(cum + m)) * 256 + threadIdx.x, sc);
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) k_ens_incomp(const EnsMember* __restrict__ mem, const int* __restrict__ cum, int M)
+{
+    __shared__ W4f sw[kMaxCheckRatio], sd[kMaxCheckRatio];
+    __shared__ F2 wmax[8];
+    const int total = __ldg(cum + M);
+    for (int tile = blockIdx.x; tile < total; tile += gridDim.x) {
+        const int m = ens_member_of(cum, M, tile);
+        const EnsMember& e = mem[m];
+        if (!e.active) continue;   // block-uniform
+        const Grid gm = e.adv.gm;
+        const int r = e.r_check;
+        const float ir = e.ir_check;
+        incomp_tables(gm, r, ir, sw, sd);
+        __syncthreads();
+        F2 best = {0.0f, 0.0f};
+        const int i = (tile - __ldg(cum + m)) * 256 + threadIdx.x;
+        if (i < (int)gm.N * r) incomp_item(gm, r, ir, e.adv.out, i, sw, sd, best);   // the advected map
+        incomp_block_max(best, wmax, e.einc);
+        __syncthreads();
+    }
+}
+
+// omega through the map on the vort grid (which = 0, into the class buffer) or on the
+// coarse grid (which = 1, FP64 into the member's coarse vorticity); items are (row, column)
+// pairs of map columns, flattened
+__global__ void __launch_bounds__(256) k_ens_sample(const EnsMember* __restrict__ mem, const int* __restrict__ cum, int M,
+                                                    int which)
+{
+    __shared__ W4f swx[kMaxCheckRatio];
+    const int total = __ldg(cum + M);
+    for (int tile = blockIdx.x; tile < total; tile += gridDim.x) {
+        const int m = ens_member_of(cum, M, tile);
+        const EnsMember& e = mem[m];
+        if (!e.active) continue;   // block-uniform
+        const Grid gm = e.adv.gm, gf = e.gf;
+        const Grid go = which == 0 ? e.gv : gm;
+        const int ro = go.NX / gm.NX, rf = gf.NX / go.NX;
+        const float iro = 1.0f / (float)ro;
+        if ((int)threadIdx.x < ro) swx[threadIdx.x] = value_weights_f((float)threadIdx.x * iro, gm.hxf);
+        __syncthreads();
+        const int i = (tile - __ldg(cum + m)) * 256 + threadIdx.x;
+        if (i < gm.NX * go.NY) {
+            const int iY = i / gm.NX, mx = i - iY * gm.NX;
+            if (which == 0) sample_m_item<float>(gm, go, gf, ro, rf, iro, e.adv.map, e.wfm, e.sample_out, mx, iY, swx);
+            else sample_m_item<double>(gm, go, gf, ro, rf, iro, e.adv.map, e.wfm, e.vort, mx, iY, swx);
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) k_ens_spec(const EnsMember* __restrict__ mem, const int* __restrict__ cum, int M)
+{
+    const int total = __ldg(cum + M);
+    for (int tile = blockIdx.x; tile < total; tile += gridDim.x) {
+        const int m = ens_member_of(cum, M, tile);
+        const EnsMember& e = mem[m];
+        if (!e.active) continue;
+        const Grid gp = e.adv.gp;
+        const int i = (tile - __ldg(cum + m)) * 256 + threadIdx.x;
+        if (i < gp.NX_fft * gp.NY)
+            spec_psi_item(e.spec_v, e.gv, gp, e.freq, e.inv_nv, e.spec4, i % gp.NX_fft, i / gp.NX_fft);
+    }
+}
+
+// the new psi level's nodes (and, fused, the three Lagrange combinations), or a
+// precombination of the levels (which = 1) before an advection that found no fused fields
+__global__ void __launch_bounds__(256) k_ens_nodes(const EnsMember* __restrict__ mem, const int* __restrict__ cum, int M,
+                                                   int which)
+{
+    const int total = __ldg(cum + M);
+    for (int tile = blockIdx.x; tile < total; tile += gridDim.x) {
+        const int m = ens_member_of(cum, M, tile);
+        const EnsMember& e = mem[m];
+        const long long n = e.adv.gp.N;
+        const long long i = (long long)(tile - __ldg(cum + m)) * 256 + threadIdx.x;
+        if (!e.active || i >= n) continue;
+        if (which == 1) {
+            if (!e.precombine) continue;
+            const float4 v0 = __ldg(e.lv0 + i), v1 = __ldg(e.lv1 + i), v2 = __ldg(e.lv2 + i);
+            e.pa[i] = combo(e.ca, v0, v1, v2);
+            if (e.pb) e.pb[i] = combo(e.cb, v0, v1, v2);
+            continue;
+        }
+        const float* pl = e.planes;
+        const float4 v0 = make_float4(pl[i], pl[n + i], pl[2 * n + i], pl[3 * n + i]);
+        e.psi_new[i] = v0;
+        if (!e.fused) continue;
+        const float4 v1 = __ldg(e.lv1n + i), v2 = __ldg(e.lv2n + i);
+        e.o1[i] = combo(e.cm.c[0], v0, v1, v2);
+        e.o2[i] = combo(e.cm.c[1], v0, v1, v2);
+        e.o3[i] = combo(e.cm.c[2], v0, v1, v2);
+    }
+}
+
+cudaError_t launch_ens(int kind, int TI, const EnsMember* mem, const int* cum, int M, int blocks, int lpn_log2,
+                       cudaStream_t s)
+{
+    if (blocks <= 0) return cudaSuccess;
+    switch (kind) {
+        case kEnsAdvect:
+            switch (TI) {
+                case 10: k_ens_advect<10><<<blocks, 256, 0, s>>>(mem, cum, M, lpn_log2); break;
+                case 21: k_ens_advect<21><<<blocks, 256, 0, s>>>(mem, cum, M, lpn_log2); break;
+                case 30: k_ens_advect<30><<<blocks, 256, 0, s>>>(mem, cum, M, lpn_log2); break;
+                default: return cudaErrorInvalidValue;
+            }
+            break;
+        case kEnsIncomp: k_ens_incomp<<<blocks, 256, 0, s>>>(mem, cum, M); break;
+        case kEnsSampleVort: k_ens_sample<<<blocks, 256, 0, s>>>(mem, cum, M, 0); break;
+        case kEnsSampleCoarse: k_ens_sample<<<blocks, 256, 0, s>>>(mem, cum, M, 1); break;
+        case kEnsSpec: k_ens_spec<<<blocks, 256, 0, s>>>(mem, cum, M); break;
+        case kEnsNodes: k_ens_nodes<<<blocks, 256, 0, s>>>(mem, cum, M, 0); break;
+        case kEnsPrecombine: k_ens_nodes<<<blocks, 256, 0, s>>>(mem, cum, M, 1); break;
+        default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 

@@ -42,6 +42,7 @@ EulerSim::EulerSim(const Settings& st) : s(st) {}
 
 EulerSim::~EulerSim()
 {
+    flush_monitor();
     set_profiling(false);
     release();
 }
@@ -1280,10 +1281,179 @@ int EulerSim::step_once()
     return saturated ? kErrSaturated : kOk;
 }
 
+// ---------------------------------------------------------------- ensemble step pieces
+int EulerSim::ens_check(std::string* why) const
+{
+    auto no = [&](const char* w) { if (why) *why = w; return 0; };
+    if (!mixed_) return no("ensemble members run in the mixed form (precision=mixed)");
+    if (vlasov_) return no("ensemble members are 2D Euler runs");
+    if (L != 3) return no("ensemble members use three Lagrange levels");
+    if (s.time_integration_num != 10 && s.time_integration_num != 21 && s.time_integration_num != 30)
+        return no("ensemble members advect their maps with EulerExp, RK2 or RK3");
+    if (s.forward_map) return no("ensemble members have no forward map");
+    if (s.map_update_order_num > 1) return no("ensemble members use 2nd or 4th order map updates");
+    // the batched kernels keep per-member weight tables of the vort/map and fine/map ratios
+    if (gv.NX / gc.NX > 32 || gf.NX / gc.NX > 32) return no("ensemble members need vort and fine grids at most 32x the map grid");
+    return 1;
+}
+
+void EulerSim::ens_bind(float* sample_out, const float2* spec_v, float2* spec4, const float* planes,
+                        unsigned long long* einc)
+{
+    ens_sample_ = sample_out;
+    ens_spec_v_ = spec_v;
+    ens_spec4_ = spec4;
+    ens_planes_ = planes;
+    ens_einc_ = einc;
+}
+
+void EulerSim::flush_monitor()
+{
+    static const char* names[4] = {"Time_s", "Error_incompressibility", "Map_gaps", "Map_counter"};
+    if (mon_buf_[0].empty()) return;
+    std::string dir = run_dir(s) + "/Monitoring_data/";
+    for (int k = 0; k < 4; ++k) {
+        append_f64(dir + names[k] + ".data", mon_buf_[k].data(), mon_buf_[k].size());
+        mon_buf_[k].clear();
+    }
+}
+
+int EulerSim::ens_begin(EnsMember& e)
+{
+    // step_once up to the advection: the time step (compute_next_timestep, clipped to the
+    // final time), the Lagrange coefficients and the advection's descriptor (advect_m)
+    e.active = 0;
+    if (done()) return 1;
+    const int lcl = loop_ctr_ + L - 1;
+    const double t = t_vec_[lcl];
+    double dt_now = compute_next_timestep(t);
+    if (t + dt_now > s.final_time) dt_now = s.final_time - t;
+    t_vec_[lcl + 1] = t + dt_now;
+    dt_vec_[lcl + 1] = dt_now;
+    ens_lcl_ = lcl;
+    ens_dt_ = dt_now;
+    const double* tv = t_vec_.data();
+    double L1[kMaxLagrange] = {0, 0, 0, 0}, L12[kMaxLagrange] = {0, 0, 0, 0};
+    for (int i = 0; i < L; ++i) {
+        L1[i] = lagrange_coefficient(tv, tv[lcl + 1], lcl, i, L);
+        L12[i] = lagrange_coefficient(tv, tv[lcl] + dt_now / 2.0, lcl, i, L);
+    }
+    const int ti = s.time_integration_num;
+    AdvectMArgs a{};
+    a.gm = gc; a.gp = gp;
+    a.map = mapm_; a.out = mapm_new_;
+    a.psiA = psiA_; a.psiB = psiB_; a.psi0 = psim_[0]; a.psi1 = psim_[1];
+    double coef[4][kMaxFoot];
+    map_update_coefficients(s.map_update_order_num, s.map_epsilon, coef, &a.nfoot);
+    for (int p = 0; p < 4; ++p)
+        for (int k = 0; k < kMaxFoot; ++k) { a.coef[p][k] = (float)coef[p][k]; a.coef64[p][k] = coef[p][k]; }
+    a.dt = (float)dt_now;
+    a.ep = (float)s.map_epsilon;
+    a.dt64 = dt_now;
+    a.ep64 = s.map_epsilon;
+    a.time_integration_num = ti;
+    a.rp = gp.NX / gc.NX;
+    e.adv = a;
+    e.active = 1;
+    // the previous psi solve's fused combinations, if its predicted coefficients are these
+    const bool half = ti == 30;
+    bool have = fused_;
+    for (int i = 0; i < L && have; ++i) have = L1[i] == fusedL1_[i] && (!half || L12[i] == fusedL12_[i]);
+    e.precombine = !have;
+    e.lv0 = psim_[0]; e.lv1 = psim_[1]; e.lv2 = psim_[2];
+    e.pa = psiA_;
+    e.pb = half ? psiB_ : nullptr;
+    for (int i = 0; i < 3; ++i) { e.ca[i] = (float)L1[i]; e.cb[i] = (float)L12[i]; }
+    e.r_check = gf.NX / gc.NX;
+    e.ir_check = 1.0f / (float)e.r_check;
+    e.einc = ens_einc_;
+    e.fused = 0;
+    return 0;
+}
+
+int EulerSim::ens_middle(double e_inc, EnsMember& e)
+{
+    // step_once after the incompressibility check: the remap decision and remap, the
+    // psi rotation, and the descriptor of the psi solve with its fused combinations
+    std::swap(mapm_, mapm_new_);
+    e_inc_ = e_inc;
+    ens_saturated_ = false;
+    int rc;
+    if (e_inc_ > s.incomp_threshold && !s.skip_remapping) {
+        if (n_maps_ >= max_maps) {
+            if (s.verbose >= 0) log_.push("Stack Saturated : Exitting");
+            ens_saturated_ = true;
+            continue_ = false;
+        } else {
+            old_ctr_ = loop_ctr_;
+            if ((rc = translate_ic())) return rc;
+            if (s.save_map_stack && (rc = write_map_stack(n_maps_))) return rc;
+            if ((rc = push_stack())) return rc;
+            if ((rc = reset_map())) return rc;
+            kernel_launches++;
+        }
+    }
+    ens_gap_ = loop_ctr_ - old_ctr_;
+    ens_counter_ = n_maps_;
+    rotate_psi(L - 1);
+    // the next advection's and this step's tracers' combinations, for the predicted next dt
+    const int lcl = ens_lcl_;
+    const double* t = t_vec_.data();
+    const double tn = t[lcl + 1];
+    double dtn = compute_next_timestep(tn);
+    if (tn + dtn > s.final_time) dtn = s.final_time - tn;
+    for (int i = 0; i < L; ++i) {
+        fusedLp_[i] = lagrange_coefficient(t, t[lcl] + dt_vec_[lcl + 1] / 2.0, lcl + 1, i, L);
+        fusedL1_[i] = lagrange_coefficient(t, tn + dtn, lcl + 1, i, L);
+        fusedL12_[i] = lagrange_coefficient(t, tn + dtn / 2.0, lcl + 1, i, L);
+    }
+    fused_ = true;
+    e.adv.map = mapm_;
+    e.gv = gv;
+    e.gf = gf;
+    e.wfm = wfm_;
+    e.sample_out = ens_sample_;
+    e.spec_v = ens_spec_v_;
+    e.spec4 = ens_spec4_;
+    e.planes = ens_planes_;
+    e.freq = (float)s.freq_cut_psi;
+    e.inv_nv = (float)(1.0 / (double)gv.N);
+    e.psi_new = psim_[0];
+    e.lv1n = psim_[1];
+    e.lv2n = psim_[2];
+    e.o1 = psiP_; e.o2 = psiA_; e.o3 = psiB_;
+    for (int l = 0; l < 3; ++l) {
+        e.cm.c[0][l] = (float)fusedLp_[l];
+        e.cm.c[1][l] = (float)fusedL1_[l];
+        e.cm.c[2][l] = (float)fusedL12_[l];
+    }
+    e.fused = 1;
+    e.vort = vort;
+    e.precombine = 0;
+    return kOk;
+}
+
+int EulerSim::ens_end()
+{
+    // step_once after the psi solve and the coarse vorticity
+    int rc;
+    const int lcl = ens_lcl_;
+    if ((rc = advect_particles(lcl))) return rc;
+    if ((rc = save_functions(t_vec_[lcl + 1], ens_dt_))) return rc;
+    loop_ctr_++;
+    mon_buf_[0].push_back(t_vec_[lcl + 1]);
+    mon_buf_[1].push_back(e_inc_);
+    mon_buf_[2].push_back(ens_gap_);
+    mon_buf_[3].push_back(ens_counter_);
+    if (mon_buf_[0].size() >= 1024) flush_monitor();
+    return ens_saturated_ ? kErrSaturated : kOk;
+}
+
 int EulerSim::finish()
 {
     if (!initialised_) { err = "finish before init"; return kErrState; }
     if (finished_) return kOk;
+    flush_monitor();
     int rc = save_functions(kTMax, dt);
     if (rc) return rc;
     if (s.save_map_stack) {

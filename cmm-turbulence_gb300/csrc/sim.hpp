@@ -23,6 +23,8 @@ namespace cmm {
 enum Status { kOk = 0, kErrParam = -1, kErrIO = -2, kErrCuda = -3, kErrSaturated = -4, kErrState = -5,
               kErrUnsupported = -6, kErrNotFound = -7 };
 
+struct EnsMember;
+
 class EulerSim {
 public:
     explicit EulerSim(const Settings& s);
@@ -36,6 +38,19 @@ public:
     int step_once();
     int finish();       // final save + log line
     bool done() const;
+
+    // ensemble step pieces (csrc/ensemble.cpp): the work of step_once for a mixed-form Euler
+    // member whose advection, incompressibility check, psi solve and coarse sample run in
+    // batched launches over the whole ensemble.  ens_begin: time step, Lagrange
+    // coefficients, the advection descriptor and any precombination (returns 1 when the
+    // member is done); ens_middle: the map swap, a remap when the checked E_inc asks for
+    // one, the psi rotation and the psi-solve descriptor; ens_end: particles, saves and
+    // counters.  ens_bind gives the member its slots in the ensemble's class buffers.
+    int ens_check(std::string* why) const;
+    void ens_bind(float* sample_out, const float2* spec_v, float2* spec4, const float* planes, unsigned long long* einc);
+    int ens_begin(EnsMember& e);
+    int ens_middle(double e_inc, EnsMember& e);
+    int ens_end();
 
     int get_field(const std::string& name, void* dst, size_t bytes);
     size_t field_bytes(const std::string& name) const;
@@ -142,6 +157,19 @@ private:
 
     // mixed form (precision=mixed): FP32 displacement maps and FP32 Hermite nodes
     bool mixed_ = false;
+    // ensemble members keep their per-step Monitoring_data records (Time_s,
+    // Error_incompressibility, Map_gaps, Map_counter) here and append them in blocks
+    std::vector<double> mon_buf_[4];
+    void flush_monitor();
+    // ensemble binding
+    float* ens_sample_ = nullptr;
+    const float2* ens_spec_v_ = nullptr;
+    float2* ens_spec4_ = nullptr;
+    const float* ens_planes_ = nullptr;
+    unsigned long long* ens_einc_ = nullptr;
+    int ens_lcl_ = 0;
+    double ens_dt_ = 0, ens_gap_ = 0, ens_counter_ = 0;
+    bool ens_saturated_ = false;
     float4* mapm_ = nullptr;         // 2*Nc float4 (current map)
     float4* mapm_new_ = nullptr;
     float4* psim_[kMaxLagrange] = {nullptr, nullptr, nullptr, nullptr};

@@ -231,6 +231,30 @@ int cmm_diagnostics(const cmm_grid* grid_psi, const double* psi, const cmm_grid*
 int cmm_diagnostics_noalloc(const cmm_grid* grid_psi, const double* psi, const cmm_grid* grid_coarse,
                             const double* vort, double* out3, void* stream);
 
+/* ---------------------------------------------------------------- ensembles
+ * Many mixed-form 2D Euler runs of uneven sizes advanced together: one iteration
+ * advances every member by one of its own time steps, with the advection,
+ * incompressibility check, psi solve and coarse sample of all members in batched
+ * launches (one cuFFT call per size class), captured as CUDA graphs.  Each member is
+ * configured like cmm_create (argc[i] strings of argv, members one after another) and
+ * must be precision=mixed, 2D Euler, three Lagrange levels, EulerExp / RK2 / RK3 maps.
+ * The reference has no ensemble driver; this is new API. */
+typedef struct cmm_ensemble cmm_ensemble;
+int cmm_ensemble_create(int n_members, const int* argc, const char* const* argv, void* stream, cmm_ensemble** out);
+int cmm_ensemble_set_initial_discrete(cmm_ensemble* e, int member, const double* values, size_t n);
+/* 0: plain launches every iteration; 1 (default): CUDA graphs after the first iteration */
+int cmm_ensemble_set_graphs(cmm_ensemble* e, int on);
+int cmm_ensemble_init(cmm_ensemble* e);
+/* n iterations; 1 when every member has reached its final time */
+int cmm_ensemble_step(cmm_ensemble* e, int n);
+int cmm_ensemble_run(cmm_ensemble* e);
+int cmm_ensemble_get_scalar(cmm_ensemble* e, int member, const char* name, double* out);
+int cmm_ensemble_get_field(cmm_ensemble* e, int member, const char* name, void* host_dst, size_t bytes);
+size_t cmm_ensemble_field_bytes(cmm_ensemble* e, int member, const char* name);
+/* out6 = {member time steps, iterations, batched launches, members, advection grid, sample grid} */
+int cmm_ensemble_stats(cmm_ensemble* e, long long* out6);
+int cmm_ensemble_destroy(cmm_ensemble* e);
+
 #ifdef __cplusplus
 }
 #endif

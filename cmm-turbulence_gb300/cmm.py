@@ -33,7 +33,11 @@ EXPORTS = [
     "cmm_vlasov_diagnostics", "cmm_vlasov_destroy", "cmm_ensemble_create", "cmm_ensemble_set_initial_discrete",
     "cmm_ensemble_set_graphs", "cmm_ensemble_init", "cmm_ensemble_step", "cmm_ensemble_run",
     "cmm_ensemble_get_scalar", "cmm_ensemble_get_field", "cmm_ensemble_field_bytes", "cmm_ensemble_stats",
-    "cmm_ensemble_destroy",
+    "cmm_ensemble_destroy", "cmm_upsampler_create", "cmm_upsampler_destroy", "cmm_upsampler_num_params",
+    "cmm_upsampler_get_params", "cmm_upsampler_set_params", "cmm_upsampler_get_grads", "cmm_upsampler_set_scales",
+    "cmm_upsampler_get_scales", "cmm_upsampler_collect", "cmm_upsampler_dataset_size", "cmm_upsampler_train",
+    "cmm_upsampler_loss_grad", "cmm_upsampler_infer", "cmm_upsampler_evaluate", "cmm_upsampler_save",
+    "cmm_upsampler_load", "cmm_attach_upsampler", "cmm_conv3x3", "cmm_conv3x3_weight_grad",
 ]
 
 
@@ -111,6 +115,26 @@ def lib():
     L.cmm_ensemble_field_bytes.restype = C.c_size_t
     L.cmm_ensemble_stats.argtypes = [vp, C.POINTER(C.c_longlong)]
     L.cmm_ensemble_destroy.argtypes = [vp]
+    fp, u16p, llp = C.POINTER(C.c_float), C.POINTER(C.c_ushort), C.POINTER(C.c_longlong)
+    L.cmm_upsampler_create.argtypes = [ip, ip, C.c_ulonglong, vp, C.POINTER(vp)]
+    L.cmm_upsampler_destroy.argtypes = [vp]
+    L.cmm_upsampler_num_params.argtypes = [vp]
+    L.cmm_upsampler_num_params.restype = C.c_longlong
+    for name in ("cmm_upsampler_get_params", "cmm_upsampler_set_params", "cmm_upsampler_get_grads"):
+        getattr(L, name).argtypes = [vp, fp, C.c_longlong]
+    L.cmm_upsampler_set_scales.argtypes = [vp, dp, C.c_double]
+    L.cmm_upsampler_get_scales.argtypes = [vp, dp, dp]
+    L.cmm_upsampler_collect.argtypes = [vp, vp]
+    L.cmm_upsampler_dataset_size.argtypes = [vp]
+    L.cmm_upsampler_train.argtypes = [vp, ip, ip, C.c_double, C.c_ulonglong, dp, dp]
+    L.cmm_upsampler_loss_grad.argtypes = [vp, fp, fp, ip, ip, ip, dp]
+    L.cmm_upsampler_infer.argtypes = [vp, fp, ip, ip, fp]
+    L.cmm_upsampler_evaluate.argtypes = [vp, vp, dp]
+    L.cmm_upsampler_save.argtypes = [vp, C.c_char_p]
+    L.cmm_upsampler_load.argtypes = [vp, C.c_char_p]
+    L.cmm_attach_upsampler.argtypes = [vp, vp, ip, C.c_double]
+    L.cmm_conv3x3.argtypes = [u16p, u16p, fp, u16p, u16p, ip, ip, ip, ip, ip, ip, fp, u16p]
+    L.cmm_conv3x3_weight_grad.argtypes = [u16p, u16p, ip, ip, ip, ip, ip, fp, fp]
     _lib = L
     return L
 
@@ -199,6 +223,10 @@ class Simulation:
         buf = C.create_string_buffer(n + 1)
         self.L.cmm_settings_text(self.h, buf, n + 1)
         return buf.value.decode()
+
+    def attach_upsampler(self, ups, every=8, tol=1e-4):
+        """Learned psi between exact evaluations every `every` steps (None detaches)."""
+        check(self.L.cmm_attach_upsampler(self.h, ups.h if ups is not None else None, int(every), float(tol)))
 
     def file_name(self):
         buf = C.create_string_buffer(4096)
@@ -362,3 +390,143 @@ class Ensemble:
         return dict(zip(("member_steps", "iterations", "launches", "members", "advect_blocks", "sample_blocks"),
                         list(out)))
 
+
+
+class Upsampler:
+    """The learned psi network (cmm_upsampler_*): BF16 tensor-core training and inference."""
+
+    def __init__(self, blocks=6, channels=32, seed=0, stream=None):
+        L = lib()
+        h = C.c_void_p()
+        check(L.cmm_upsampler_create(int(blocks), int(channels), int(seed), stream, C.byref(h)))
+        self.h, self.L, self.blocks, self.channels = h, L, blocks, channels
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cmm_upsampler_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def num_params(self):
+        return int(self.L.cmm_upsampler_num_params(self.h))
+
+    def _vec(self, fn):
+        import numpy as np
+        out = np.empty(self.num_params(), dtype=np.float32)
+        check(fn(self.h, out.ctypes.data_as(C.POINTER(C.c_float)), out.size))
+        return out
+
+    def params(self):
+        return self._vec(self.L.cmm_upsampler_get_params)
+
+    def grads(self):
+        return self._vec(self.L.cmm_upsampler_get_grads)
+
+    def set_params(self, p):
+        import numpy as np
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        check(self.L.cmm_upsampler_set_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float)), p.size))
+
+    def set_scales(self, s_in, s_out):
+        arr = (C.c_double * 7)(*[float(v) for v in s_in])
+        check(self.L.cmm_upsampler_set_scales(self.h, arr, float(s_out)))
+
+    def scales(self):
+        arr = (C.c_double * 7)()
+        out = C.c_double()
+        check(self.L.cmm_upsampler_get_scales(self.h, arr, C.byref(out)))
+        return list(arr), out.value
+
+    def collect(self, sim):
+        check(self.L.cmm_upsampler_collect(self.h, sim.h))
+
+    def dataset_size(self):
+        return int(self.L.cmm_upsampler_dataset_size(self.h))
+
+    def train(self, iters, batch=8, lr=1e-3, seed=0):
+        """-> (mean loss of the last steps, device seconds)"""
+        loss, sec = C.c_double(), C.c_double()
+        check(self.L.cmm_upsampler_train(self.h, int(iters), int(batch), float(lr), int(seed), C.byref(loss),
+                                         C.byref(sec)))
+        return loss.value, sec.value
+
+    def loss_grad(self, inputs, targets):
+        """inputs[B, 7, h, w], targets[B, 2h, 2w] -> loss (gradient via grads())"""
+        import numpy as np
+        x = np.ascontiguousarray(inputs, dtype=np.float32)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        B, _, h, w = x.shape
+        loss = C.c_double()
+        fp = C.POINTER(C.c_float)
+        check(self.L.cmm_upsampler_loss_grad(self.h, x.ctypes.data_as(fp), t.ctypes.data_as(fp), B, h, w,
+                                             C.byref(loss)))
+        return loss.value
+
+    def infer(self, inputs):
+        """inputs[7, h, w] -> correction[2h, 2w]"""
+        import numpy as np
+        x = np.ascontiguousarray(inputs, dtype=np.float32)
+        _, h, w = x.shape
+        out = np.empty((2 * h, 2 * w), dtype=np.float32)
+        fp = C.POINTER(C.c_float)
+        check(self.L.cmm_upsampler_infer(self.h, x.ctypes.data_as(fp), h, w, out.ctypes.data_as(fp)))
+        return out
+
+    def evaluate(self, sim):
+        """relative differences from sim's exact psi: {cheap_linf, cheap_l2, learned_linf, learned_l2}"""
+        arr = (C.c_double * 4)()
+        check(self.L.cmm_upsampler_evaluate(self.h, sim.h, arr))
+        return dict(zip(("cheap_linf", "cheap_l2", "learned_linf", "learned_l2"), list(arr)))
+
+    def save(self, path):
+        check(self.L.cmm_upsampler_save(self.h, str(path).encode()))
+
+    def load(self, path):
+        check(self.L.cmm_upsampler_load(self.h, str(path).encode()))
+
+
+def conv3x3(x_bits, w_bits, bias=None, mask_bits=None, res_bits=None, relu=False):
+    """One periodic 3x3 convolution of the network on BF16 bit arrays: x[B, H, W, cin],
+    w[9, cin, cout] (uint16) -> (out float32, out BF16 bits), both [B, H, W, cout]."""
+    import numpy as np
+    L = lib()
+    x = np.ascontiguousarray(x_bits, dtype=np.uint16)
+    w = np.ascontiguousarray(w_bits, dtype=np.uint16)
+    B, H, W, cin = x.shape
+    cout = w.shape[2]
+    u16 = C.POINTER(C.c_ushort)
+    fp = C.POINTER(C.c_float)
+    keep = []
+
+    def opt(a, dt, ptr):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=dt)
+        keep.append(a)
+        return a.ctypes.data_as(ptr)
+
+    out = np.empty((B, H, W, cout), dtype=np.float32)
+    outb = np.empty((B, H, W, cout), dtype=np.uint16)
+    check(L.cmm_conv3x3(x.ctypes.data_as(u16), w.ctypes.data_as(u16), opt(bias, np.float32, fp),
+                        opt(mask_bits, np.uint16, u16), opt(res_bits, np.uint16, u16), 1 if relu else 0, B, H, W,
+                        cin, cout, out.ctypes.data_as(fp), outb.ctypes.data_as(u16)))
+    return out, outb
+
+
+def conv3x3_weight_grad(x_bits, dy_bits):
+    """Weight and bias gradients of conv3x3 for x[B, H, W, cin], dy[B, H, W, cout] (BF16 bits)."""
+    import numpy as np
+    L = lib()
+    x = np.ascontiguousarray(x_bits, dtype=np.uint16)
+    dy = np.ascontiguousarray(dy_bits, dtype=np.uint16)
+    B, H, W, cin = x.shape
+    cout = dy.shape[3]
+    dw = np.empty((9, cin, cout), dtype=np.float32)
+    db = np.empty(cout, dtype=np.float32)
+    u16 = C.POINTER(C.c_ushort)
+    fp = C.POINTER(C.c_float)
+    check(L.cmm_conv3x3_weight_grad(x.ctypes.data_as(u16), dy.ctypes.data_as(u16), B, H, W, cin, cout,
+                                    dw.ctypes.data_as(fp), db.ctypes.data_as(fp)))
+    return dw, db

@@ -8,22 +8,12 @@
 #include <new>
 #include <string>
 
+#include "abi_internal.hpp"
 #include "ensemble.hpp"
 #include "kernels.hpp"
 #include "settings.hpp"
 #include "sim.hpp"
 #include "vlasov.hpp"
-
-namespace cmm {
-void set_last_error(const std::string& msg);
-}
-
-struct cmm_ctx {
-    cmm::Settings settings;
-    cmm::EulerSim* sim = nullptr;
-    cudaStream_t stream = nullptr;
-    std::vector<double> discrete;
-};
 
 struct cmm_ensemble {
     std::vector<cmm::Settings> settings;

@@ -1264,6 +1264,38 @@ cudaError_t launch_fix_to_pos(const unsigned long long* in, int num, const Grid&
     return cudaGetLastError();
 }
 
+// omega and its gradient at the map-grid nodes: omega = W(X(x)) and, with J the map's
+// Jacobian at the node (identity plus the displacement's stored derivatives),
+// grad omega = J^T grad W(X(x)); three planes of gm.N values
+__global__ void __launch_bounds__(256) k_sample_grad_m(Grid gm, Grid gf, int rf, const float4* __restrict__ map,
+                                                      const float4* __restrict__ W, float* __restrict__ out3)
+{
+    const int mx = blockIdx.x * blockDim.x + threadIdx.x, my = blockIdx.y;
+    if (mx >= gm.NX) return;
+    const long long i = (long long)my * gm.NX + mx;
+    const float4 a = __ldg(map + 2 * i), b = __ldg(map + 2 * i + 1);   // (X, Y, X_x, Y_x), (X_y, Y_y, X_xy, Y_xy)
+    const CellF c = locate_rel(gf, mx * rf, my * rf, a.x, a.y);
+    Q4 q;
+    q.c00 = __ldg(W + c.i00); q.c10 = __ldg(W + c.i10); q.c01 = __ldg(W + c.i01); q.c11 = __ldg(W + c.i11);
+    const W4f wx = value_weights_f(c.tx, gf.hxf), wy = value_weights_f(c.ty, gf.hyf);
+    const W4f dx = slope_weights_f(c.tx, gf.ihxf), dy = slope_weights_f(c.ty, gf.ihyf);
+    float gx, gy;
+    herm_grad_f(q, wx, wy, dx, dy, gx, gy);
+    out3[i] = herm_value_f(q, wx, wy);
+    out3[gm.N + i] = gx * (1.0f + a.z) + gy * a.w;
+    out3[2 * gm.N + i] = gx * b.x + gy * (1.0f + b.y);
+}
+
+cudaError_t launch_sample_grad_m(const Grid& gm, const Grid& gf, const float4* map, const float4* W, float* out3,
+                                 cudaStream_t s)
+{
+    const int rf = gf.NX / gm.NX;
+    if (rf < 1 || rf * gm.NX != gf.NX || rf * gm.NY != gf.NY || gm.NY > 65535) return cudaErrorInvalidValue;
+    dim3 blocks((unsigned)((gm.NX + 255) / 256), (unsigned)gm.NY);
+    k_sample_grad_m<<<blocks, 256, 0, s>>>(gm, gf, rf, map, W, out3);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // FP32 spectral step of the psi solve and layout conversions
 // ---------------------------------------------------------------------------
@@ -1308,6 +1340,46 @@ cudaError_t launch_spec_psi_f(const float2* Fv, const Grid& gv, const Grid& gp, 
     if (gp.NY > 65535) return cudaErrorInvalidValue;
     dim3 blocks((unsigned)((gp.NX_fft + 255) / 256), (unsigned)gp.NY);
     k_spec_psi_f<<<blocks, 256, 0, s>>>(Fv, gv, gp, (float)freq, (float)(1.0 / (double)gv.N), out4);
+    return cudaGetLastError();
+}
+
+__global__ void k_spec_psi_learned(const float2* __restrict__ Fc, Grid gc, const float2* __restrict__ D, Grid gp,
+                                   float freq, float inv_nc, float inv_np, float2* __restrict__ out4)
+{
+    const int iXc = blockIdx.x * blockDim.x + threadIdx.x, iYc = blockIdx.y;
+    if (iXc >= gp.NX_fft) return;
+    const long long i = (long long)iYc * gp.NX_fft + iXc;
+    const bool hx = 2 * iXc > gp.NX, hy = 2 * iYc > gp.NY;
+    const int fX = hx ? gp.NX - iXc : iXc, fY = hy ? gp.NY - iYc : iYc;
+    float2 W = make_float2(0.f, 0.f);
+    if (!(2 * fX > gc.NX || 2 * fY > gc.NY)) {
+        const int iXs = iXc + (hx ? gc.NX - gp.NX : 0);
+        const int iYs = iYc + (hy ? gc.NY - gp.NY : 0);
+        const float2 f = Fc[(long long)iYs * gc.NX_fft + iXs];
+        W = make_float2(f.x * inv_nc, f.y * inv_nc);
+    }
+    const float kx = gp.kfxf * (float)(hx ? iXc - gp.NX : iXc);
+    const float ky = gp.kfyf * (float)(hy ? iYc - gp.NY : iYc);
+    float2 P = make_float2(0.f, 0.f);
+    if (!(iXc == 0 && iYc == 0) && !((float)(fX * fX + fY * fY) > freq * freq)) {
+        const float ik2 = 1.0f / (kx * kx + ky * ky);
+        const float2 d = D[i];
+        P = make_float2(-W.x * ik2 + d.x * inv_np, -W.y * ik2 + d.y * inv_np);
+    }
+    const float2 Py = make_float2(-P.y * ky, P.x * ky);
+    out4[i] = P;
+    out4[gp.Nfft + i] = make_float2(-P.y * kx, P.x * kx);
+    out4[2 * gp.Nfft + i] = Py;
+    out4[3 * gp.Nfft + i] = make_float2(-Py.y * kx, Py.x * kx);
+}
+
+cudaError_t launch_spec_psi_learned(const float2* Fc, const Grid& gc, const float2* D, const Grid& gp, double freq,
+                                    float2* out4, cudaStream_t s)
+{
+    if (gp.NY > 65535) return cudaErrorInvalidValue;
+    dim3 blocks((unsigned)((gp.NX_fft + 255) / 256), (unsigned)gp.NY);
+    k_spec_psi_learned<<<blocks, 256, 0, s>>>(Fc, gc, D, gp, (float)freq, (float)(1.0 / (double)gc.N),
+                                              (float)(1.0 / (double)gp.N), out4);
     return cudaGetLastError();
 }
 

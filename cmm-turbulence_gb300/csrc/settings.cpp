@@ -423,6 +423,9 @@ int Settings::set_variable(const std::string& line, const std::string& delim)
     }
     else if (k == "particles_steps") particles_steps = to_int(v, particles_steps, &ok);
     else if (k == "precision") precision = v;
+    else if (k == "psi_upsampler") psi_upsampler = v;
+    else if (k == "psi_exact_every") psi_exact_every = to_int(v, psi_exact_every, &ok);
+    else if (k == "psi_learned_tol") psi_learned_tol = to_dbl(v, psi_learned_tol, &ok);
     if (!ok) error = "bad value for " + k + ": " + v;
     return kNoList;
 }

@@ -125,6 +125,12 @@ public:
     // precision of the map / stream-function arithmetic: "fp64" (reference
     // method) or "mixed" (FP32 displacement maps); not a reference key
     std::string precision = "fp64";
+    // learned psi (precision=mixed): upsampler file, exact evaluation every n steps, and the
+    // relative L-infinity psi difference above which the exact evaluation takes over; not
+    // reference keys
+    std::string psi_upsampler;
+    int psi_exact_every = 8;
+    double psi_learned_tol = 1e-4;
 
     // status of the last failed parse / validation (empty when fine)
     std::string error;

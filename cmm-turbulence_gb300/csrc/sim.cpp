@@ -43,6 +43,7 @@ EulerSim::EulerSim(const Settings& st) : s(st) {}
 EulerSim::~EulerSim()
 {
     flush_monitor();
+    learned_release();
     set_profiling(false);
     release();
 }
@@ -417,10 +418,15 @@ int EulerSim::evaluate_stream()
 {
     if (vlasov_) return evaluate_potential();
     if (mixed_) {
-        CMM_LAUNCH(1, launch_sample_m(gc, gv, gf, mapm_, wfm_, realf_, nullptr, stream));
-        CMM_FFT(cufftExecR2C(r2c_v_, realf_, reinterpret_cast<cufftComplex*>(specf_)));
-        CMM_LAUNCH(1, launch_spec_psi_f(specf_, gv, gp, s.freq_cut_psi, spec4f_, stream));
-        CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), realf_));
+        if (ups_ && in_step_) {
+            int rc = learned_stream();
+            if (rc) return rc;
+        } else {
+            CMM_LAUNCH(1, launch_sample_m(gc, gv, gf, mapm_, wfm_, realf_, nullptr, stream));
+            CMM_FFT(cufftExecR2C(r2c_v_, realf_, reinterpret_cast<cufftComplex*>(specf_)));
+            CMM_LAUNCH(1, launch_spec_psi_f(specf_, gv, gp, s.freq_cut_psi, spec4f_, stream));
+            CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), realf_));
+        }
         fused_ = false;
         if (psi_lcl_ >= 0 && L == 3) {
             // one pass writes the new level and the Lagrange combinations this step's
@@ -1067,6 +1073,7 @@ int EulerSim::init()
     begin_ = std::chrono::steady_clock::now();
     int rc = alloc();
     if (rc) return rc;
+    if (!s.psi_upsampler.empty() && (rc = load_upsampler())) return rc;
     if (!create_directory_structure(s)) { err = "cannot create output folders under " + s.workspace; return kErrIO; }
     log_.start(run_dir(s) + "/log.txt", s.restart_time != 0, s.file_name);
     log_.quiet = s.verbose < 1;
@@ -1245,7 +1252,9 @@ int EulerSim::step_once()
     rotate_psi(L - 1);
     ph_begin(kPhPsi);
     psi_lcl_ = lcl;
+    in_step_ = true;
     rc = evaluate_stream();
+    in_step_ = false;
     psi_lcl_ = -1;
     if (rc) return rc;
     ph_end(kPhPsi);
@@ -1287,6 +1296,7 @@ int EulerSim::ens_check(std::string* why) const
     auto no = [&](const char* w) { if (why) *why = w; return 0; };
     if (!mixed_) return no("ensemble members run in the mixed form (precision=mixed)");
     if (vlasov_) return no("ensemble members are 2D Euler runs");
+    if (ups_) return no("ensemble members evaluate psi exactly (no upsampler)");
     if (L != 3) return no("ensemble members use three Lagrange levels");
     if (s.time_integration_num != 10 && s.time_integration_num != 21 && s.time_integration_num != 30)
         return no("ensemble members advect their maps with EulerExp, RK2 or RK3");
@@ -1992,6 +2002,12 @@ int EulerSim::get_scalar(const std::string& n, double* out)
     if (n == "e_invertibility") { *out = e_inv_; return kOk; }
     if (n == "map_gap") { *out = (loop_ctr_ - 1) - old_ctr_; return kOk; }
     if (n == "loop_ctr") { *out = loop_ctr_; return kOk; }
+    if (n == "learned_steps") { *out = (double)learned_steps_; return kOk; }
+    if (n == "exact_steps") { *out = (double)exact_steps_; return kOk; }
+    if (n == "learned_checks") { *out = (double)learned_checks_; return kOk; }
+    if (n == "learned_failures") { *out = (double)learned_fails_; return kOk; }
+    if (n == "learned_last_err") { *out = learned_last_err_; return kOk; }
+    if (n == "learned_max_err") { *out = learned_max_err_; return kOk; }
     if (n == "kernel_launches") { *out = (double)kernel_launches; return kOk; }
     if (n == "fft_calls") { *out = (double)fft_calls; return kOk; }
     for (int p = 0; p < kNumPhases; ++p) {

@@ -24,6 +24,7 @@ enum Status { kOk = 0, kErrParam = -1, kErrIO = -2, kErrCuda = -3, kErrSaturated
               kErrUnsupported = -6, kErrNotFound = -7 };
 
 struct EnsMember;
+namespace lrn { class Upsampler; }
 
 class EulerSim {
 public:
@@ -51,6 +52,18 @@ public:
     int ens_begin(EnsMember& e);
     int ens_middle(double e_inc, EnsMember& e);
     int ens_end();
+
+    // learned psi (precision=mixed, Euler; csrc/sim_learned.cpp).  With an upsampler attached,
+    // a step evaluates psi from omega sampled on the map grid plus the network's correction,
+    // except every `every`-th step, which runs the vorticity-grid evaluation and compares the
+    // learned psi with it: a relative L-infinity difference above `tol` makes the next
+    // every - 1 steps exact as well.  null detaches.  learned_collect appends the current
+    // state's training pair (cheap fields, exact psi - cheap psi); learned_evaluate gives the
+    // relative L-infinity and L2 differences of the cheap and of the learned psi from the
+    // current exact psi level (out = {cheap Linf, cheap L2, learned Linf, learned L2}).
+    int attach_upsampler(lrn::Upsampler* u, int every, double tol);
+    int learned_collect(lrn::Upsampler& u);
+    int learned_evaluate(lrn::Upsampler& u, double* out4);
 
     int get_field(const std::string& name, void* dst, size_t bytes);
     size_t field_bytes(const std::string& name) const;
@@ -157,6 +170,28 @@ private:
 
     // mixed form (precision=mixed): FP32 displacement maps and FP32 Hermite nodes
     bool mixed_ = false;
+    // learned psi state
+    int learned_check() const;
+    int load_upsampler();     // psi_upsampler=<file>: an owned network read from the file
+    int learned_setup();
+    void learned_release();
+    int cheap_fields();
+    int learned_planes(lrn::Upsampler& u, float* out);
+    int learned_stream();
+    int diff_stats(const float* a, long long sa, const float* e, long long se, long long n, double* host4);
+    lrn::Upsampler* ups_ = nullptr;
+    lrn::Upsampler* ups_owned_ = nullptr;
+    int learned_every_ = 8;
+    double learned_tol_ = 1e-4;
+    int learned_fallback_ = 0;
+    long long learned_steps_ = 0, exact_steps_ = 0, learned_checks_ = 0, learned_fails_ = 0;
+    double learned_last_err_ = 0, learned_max_err_ = 0;
+    float *lc_omega_ = nullptr, *lc_planes_ = nullptr, *l_delta_ = nullptr, *l_planes_ = nullptr;
+    float2 *lc_spec_ = nullptr, *lc_spec4_ = nullptr, *l_dspec_ = nullptr;
+    int lc_r2c_ = 0, lc_c2r4_ = 0, l_r2c_ = 0;    // cuFFT handles
+    double* d_stats_ = nullptr;
+    bool in_step_ = false;
+
     // ensemble members keep their per-step Monitoring_data records (Time_s,
     // Error_incompressibility, Map_gaps, Map_counter) here and append them in blocks
     std::vector<double> mon_buf_[4];

@@ -1,0 +1,227 @@
+// sim_learned.cpp -- the learned psi of the mixed Euler form.
+//
+// Exact psi (the method): omega sampled through the map on the vorticity grid, FFT,
+// Poisson solve with the psi cut-off, Hermite planes on the psi grid.
+// Cheap psi: the same solve from omega sampled on the map grid (16x fewer samples at the
+// metric's 512^2 map / 2048^2 vorticity grids), which aliases the vorticity scales the map
+// grid cannot hold into the retained modes.
+// Learned psi: the cheap psi plus the upsampler's correction (its network sees the cheap
+// psi planes, omega and omega's gradient on the map grid -- the gradient, through the map's
+// Jacobian, tells the vorticity scales the map grid cannot hold apart from the ones it
+// can -- and outputs the correction on the psi grid, twice as fine), projected through the
+// same cut-off and differentiated spectrally.
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "learned.hpp"
+#include "mixed.hpp"
+#include "sim.hpp"
+
+namespace cmm {
+
+#define CMM_CUDA(call) do { int rc_ = check((call), #call); if (rc_) return rc_; } while (0)
+#define CMM_LAUNCH(k, call) do { kernel_launches += (k); int rc_ = check((call), #call); if (rc_) return rc_; } while (0)
+#define CMM_FFT(call) do { fft_calls++; if ((call) != CUFFT_SUCCESS) { err = std::string("cuFFT: ") + #call; return kErrCuda; } } while (0)
+
+int EulerSim::learned_check() const
+{
+    if (!mixed_ || vlasov_) return 0;
+    if (gp.NX != 2 * gc.NX || gp.NY != 2 * gc.NY) return 0;
+    if (gc.NX % lrn::kTile != 0) return 0;
+    return 1;
+}
+
+int EulerSim::learned_setup()
+{
+    if (lc_omega_) return kOk;
+    if (!learned_check()) {
+        err = "the learned psi needs precision=mixed, a 2D Euler run, a psi grid twice the map grid and a map grid "
+              "width that is a multiple of 128";
+        return kErrUnsupported;
+    }
+    auto falloc = [&](void** p, size_t bytes) { return check(cudaMalloc(p, bytes), "cudaMalloc"); };
+    int rc;
+    if ((rc = falloc((void**)&lc_omega_, sizeof(float) * 3 * (size_t)gc.N)) ||
+        (rc = falloc((void**)&lc_planes_, sizeof(float) * 4 * (size_t)gc.N)) ||
+        (rc = falloc((void**)&l_delta_, sizeof(float) * (size_t)gp.N)) ||
+        (rc = falloc((void**)&l_planes_, sizeof(float) * 4 * (size_t)gp.N)) ||
+        (rc = falloc((void**)&lc_spec_, sizeof(float2) * (size_t)gc.Nfft)) ||
+        (rc = falloc((void**)&lc_spec4_, sizeof(float2) * 4 * (size_t)gc.Nfft)) ||
+        (rc = falloc((void**)&l_dspec_, sizeof(float2) * (size_t)gp.Nfft)) ||
+        (rc = falloc((void**)&d_stats_, sizeof(double) * 4)))
+        return rc;
+    int nc[2] = {gc.NY, gc.NX}, np[2] = {gp.NY, gp.NX};
+    cufftHandle a = 0, b = 0, c = 0;
+    if (cufftPlanMany(&a, 2, nc, nullptr, 1, 0, nullptr, 1, 0, CUFFT_R2C, 1) != CUFFT_SUCCESS ||
+        cufftPlanMany(&b, 2, nc, nullptr, 1, 0, nullptr, 1, 0, CUFFT_C2R, 4) != CUFFT_SUCCESS ||
+        cufftPlanMany(&c, 2, np, nullptr, 1, 0, nullptr, 1, 0, CUFFT_R2C, 1) != CUFFT_SUCCESS) {
+        err = "cuFFT plan creation for the learned psi failed";
+        return kErrCuda;
+    }
+    cufftSetStream(a, stream);
+    cufftSetStream(b, stream);
+    cufftSetStream(c, stream);
+    lc_r2c_ = (int)a;
+    lc_c2r4_ = (int)b;
+    l_r2c_ = (int)c;
+    return kOk;
+}
+
+void EulerSim::learned_release()
+{
+    auto f = [](void* p) { if (p) cudaFree(p); };
+    f(lc_omega_); f(lc_planes_); f(l_delta_); f(l_planes_); f(lc_spec_); f(lc_spec4_); f(l_dspec_); f(d_stats_);
+    lc_omega_ = lc_planes_ = l_delta_ = l_planes_ = nullptr;
+    lc_spec_ = lc_spec4_ = l_dspec_ = nullptr;
+    d_stats_ = nullptr;
+    if (lc_r2c_) cufftDestroy((cufftHandle)lc_r2c_);
+    if (lc_c2r4_) cufftDestroy((cufftHandle)lc_c2r4_);
+    if (l_r2c_) cufftDestroy((cufftHandle)l_r2c_);
+    lc_r2c_ = lc_c2r4_ = l_r2c_ = 0;
+    delete ups_owned_;
+    ups_owned_ = nullptr;
+    ups_ = nullptr;
+}
+
+int EulerSim::load_upsampler()
+{
+    auto* u = new lrn::Upsampler();
+    if (!u->err.empty() || u->load(s.psi_upsampler)) {
+        err = u->err.empty() ? "cannot read " + s.psi_upsampler : u->err;
+        delete u;
+        return kErrIO;
+    }
+    int rc = attach_upsampler(u, s.psi_exact_every, s.psi_learned_tol);
+    if (rc) {
+        delete u;
+        return rc;
+    }
+    ups_owned_ = u;
+    return kOk;
+}
+
+int EulerSim::attach_upsampler(lrn::Upsampler* u, int every, double tol)
+{
+    if (!u) {
+        ups_ = nullptr;
+        return kOk;
+    }
+    if (every < 1 || !(tol > 0)) {
+        err = "psi_exact_every must be >= 1 and psi_learned_tol > 0";
+        return kErrParam;
+    }
+    int rc = learned_setup();
+    if (rc) return rc;
+    ups_ = u;
+    learned_every_ = every;
+    learned_tol_ = tol;
+    learned_fallback_ = 0;
+    return kOk;
+}
+
+int EulerSim::cheap_fields()
+{
+    // omega and its gradient on the map grid, omega's spectrum, and the cheap psi's
+    // Hermite planes there
+    CMM_LAUNCH(1, launch_sample_grad_m(gc, gf, mapm_, wfm_, lc_omega_, stream));
+    CMM_FFT(cufftExecR2C((cufftHandle)lc_r2c_, lc_omega_, reinterpret_cast<cufftComplex*>(lc_spec_)));
+    CMM_LAUNCH(1, launch_spec_psi_f(lc_spec_, gc, gc, s.freq_cut_psi, lc_spec4_, stream));
+    CMM_FFT(cufftExecC2R((cufftHandle)lc_c2r4_, reinterpret_cast<cufftComplex*>(lc_spec4_), lc_planes_));
+    return kOk;
+}
+
+int EulerSim::learned_planes(lrn::Upsampler& u, float* out)
+{
+    int rc;
+    if ((rc = cheap_fields())) return rc;
+    if (u.infer(lc_planes_, lc_omega_, gc.NY, gc.NX, l_delta_, stream)) {
+        err = u.err;
+        return kErrCuda;
+    }
+    kernel_launches += u.launches;
+    CMM_FFT(cufftExecR2C((cufftHandle)l_r2c_, l_delta_, reinterpret_cast<cufftComplex*>(l_dspec_)));
+    CMM_LAUNCH(1, launch_spec_psi_learned(lc_spec_, gc, l_dspec_, gp, s.freq_cut_psi, spec4f_, stream));
+    CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), out));
+    return kOk;
+}
+
+int EulerSim::diff_stats(const float* a, long long sa, const float* e, long long se, long long n, double* host4)
+{
+    CMM_CUDA(cudaMemsetAsync(d_stats_, 0, sizeof(double) * 4, stream));
+    CMM_LAUNCH(1, lrn::launch_diff_stats(a, sa, e, se, n, d_stats_, stream));
+    CMM_CUDA(cudaMemcpyAsync(host4, d_stats_, sizeof(double) * 4, cudaMemcpyDeviceToHost, stream));
+    CMM_CUDA(cudaStreamSynchronize(stream));
+    return kOk;
+}
+
+int EulerSim::learned_stream()
+{
+    const bool exact = learned_fallback_ > 0 || loop_ctr_ % learned_every_ == 0;
+    if (!exact) {
+        ++learned_steps_;
+        return learned_planes(*ups_, realf_);
+    }
+    ++exact_steps_;
+    CMM_LAUNCH(1, launch_sample_m(gc, gv, gf, mapm_, wfm_, realf_, nullptr, stream));
+    CMM_FFT(cufftExecR2C(r2c_v_, realf_, reinterpret_cast<cufftComplex*>(specf_)));
+    CMM_LAUNCH(1, launch_spec_psi_f(specf_, gv, gp, s.freq_cut_psi, spec4f_, stream));
+    CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), realf_));
+    if (learned_fallback_ > 0) {
+        --learned_fallback_;
+        return kOk;
+    }
+    // the exact evaluation judges the learned one on the same state
+    int rc;
+    if ((rc = learned_planes(*ups_, l_planes_))) return rc;
+    double st[4];
+    if ((rc = diff_stats(l_planes_, 1, realf_, 1, gp.N, st))) return rc;
+    const double e = st[1] > 0 ? st[0] / st[1] : 0.0;
+    ++learned_checks_;
+    learned_last_err_ = e;
+    learned_max_err_ = std::max(learned_max_err_, e);
+    if (!(e <= learned_tol_)) {
+        ++learned_fails_;
+        learned_fallback_ = learned_every_ - 1;
+    }
+    return kOk;
+}
+
+int EulerSim::learned_collect(lrn::Upsampler& u)
+{
+    if (!initialised_) { err = "learned_collect before init"; return kErrState; }
+    int rc;
+    if ((rc = learned_setup()) || (rc = cheap_fields())) return rc;
+    // the cheap psi on the psi grid; target = exact psi level 0 (node values) - cheap psi
+    CMM_LAUNCH(1, launch_spec_psi_f(lc_spec_, gc, gp, s.freq_cut_psi, spec4f_, stream));
+    CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), l_planes_));
+    CMM_LAUNCH(1, lrn::launch_sub_strided(reinterpret_cast<const float*>(psim_[0]), 4, l_planes_, gp.N, l_delta_, stream));
+    if (u.append(lc_planes_, lc_omega_, l_delta_, gc.NY, gc.NX, stream)) {
+        err = u.err;
+        return kErrCuda;
+    }
+    CMM_CUDA(cudaStreamSynchronize(stream));
+    return kOk;
+}
+
+int EulerSim::learned_evaluate(lrn::Upsampler& u, double* out4)
+{
+    if (!initialised_) { err = "learned_evaluate before init"; return kErrState; }
+    int rc;
+    if ((rc = learned_setup()) || (rc = cheap_fields())) return rc;
+    const float* exact = reinterpret_cast<const float*>(psim_[0]);
+    double st[4];
+    CMM_LAUNCH(1, launch_spec_psi_f(lc_spec_, gc, gp, s.freq_cut_psi, spec4f_, stream));
+    CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), l_planes_));
+    if ((rc = diff_stats(l_planes_, 1, exact, 4, gp.N, st))) return rc;
+    out4[0] = st[1] > 0 ? st[0] / st[1] : 0.0;
+    out4[1] = st[3] > 0 ? std::sqrt(st[2] / st[3]) : 0.0;
+    if ((rc = learned_planes(u, l_planes_))) return rc;
+    if ((rc = diff_stats(l_planes_, 1, exact, 4, gp.N, st))) return rc;
+    out4[2] = st[1] > 0 ? st[0] / st[1] : 0.0;
+    out4[3] = st[3] > 0 ? std::sqrt(st[2] / st[3]) : 0.0;
+    return kOk;
+}
+
+}  // namespace cmm

@@ -255,6 +255,69 @@ size_t cmm_ensemble_field_bytes(cmm_ensemble* e, int member, const char* name);
 int cmm_ensemble_stats(cmm_ensemble* e, long long* out6);
 int cmm_ensemble_destroy(cmm_ensemble* e);
 
+/* ---------------------------------------------------------------- learned psi
+ * A residual network of 3x3 periodic convolutions (BF16 tensor-core kernels, FP32
+ * accumulation) that corrects the psi of omega sampled on the map grid towards the psi of
+ * the full vorticity-grid evaluation.  Inputs on the map grid (h x w, w a multiple of 128):
+ * the cheap psi and its derivatives psi_x, psi_y, psi_xy, and omega with omega_x, omega_y
+ * (through the map's Jacobian); output on the psi grid (2h x 2w).  Trained on the GPU on pairs collected from running simulations
+ * (precision=mixed, psi grid = 2 x map grid).  The reference has no learned part; this is
+ * new API.  With cmm_attach_upsampler (or psi_upsampler=<file> in the settings) a
+ * simulation evaluates psi through the network except every exact_every-th step, where
+ * the exact evaluation runs and judges the learned one: a relative L-infinity psi
+ * difference above tol makes the following exact_every - 1 steps exact too.  Scalars of
+ * the context: learned_steps, exact_steps, learned_checks, learned_failures,
+ * learned_last_err, learned_max_err. */
+typedef struct cmm_upsampler cmm_upsampler;
+/* blocks residual blocks of two convolutions of `channels` (= 32) channels; weights drawn
+ * from mt19937_64(seed) */
+int cmm_upsampler_create(int blocks, int channels, unsigned long long seed, void* stream, cmm_upsampler** out);
+int cmm_upsampler_destroy(cmm_upsampler* u);
+long long cmm_upsampler_num_params(const cmm_upsampler* u);
+/* FP32 parameters, layer by layer: W[9][cin][cout] (tap = 3 (dy + 1) + dx + 1), b[cout];
+ * layers: head (16 -> C, input channels 7..15 unused), per block two (C -> C), tail
+ * (C -> 16, output channels 4..15 unused) */
+int cmm_upsampler_get_params(const cmm_upsampler* u, float* out, long long n);
+int cmm_upsampler_set_params(cmm_upsampler* u, const float* in, long long n);
+/* gradient of the last cmm_upsampler_loss_grad, same layout */
+int cmm_upsampler_get_grads(const cmm_upsampler* u, float* out, long long n);
+/* input channel scales (7) and target scale: the network sees inputs / s_in and predicts
+ * target / s_out; set from the training pairs' RMS by the first cmm_upsampler_train */
+int cmm_upsampler_set_scales(cmm_upsampler* u, const double* s_in7, double s_out);
+int cmm_upsampler_get_scales(const cmm_upsampler* u, double* s_in7, double* s_out);
+/* one training pair from the context's current state (its last psi must be exact) */
+int cmm_upsampler_collect(cmm_upsampler* u, cmm_ctx* c);
+int cmm_upsampler_dataset_size(const cmm_upsampler* u);
+/* iters Adam steps (lr) on batches of `batch` pairs drawn with mt19937_64(seed); mean loss
+ * of the last min(iters, 16) steps and the device seconds of the call */
+int cmm_upsampler_train(cmm_upsampler* u, int iters, int batch, double lr, unsigned long long seed, double* loss,
+                        double* seconds);
+/* mean squared error (scaled units) and its gradient for B host samples:
+ * inputs[B][7][h][w] (psi, psi_x, psi_y, psi_xy, omega, omega_x, omega_y), targets[B][2h][2w] */
+int cmm_upsampler_loss_grad(cmm_upsampler* u, const float* inputs, const float* targets, int B, int h, int w,
+                            double* loss);
+/* the correction on the psi grid (fine[2h][2w], physical units) for host inputs[7][h][w] */
+int cmm_upsampler_infer(cmm_upsampler* u, const float* inputs, int h, int w, float* fine);
+/* relative differences from the context's exact psi level:
+ * out4 = {cheap Linf, cheap L2, learned Linf, learned L2} */
+int cmm_upsampler_evaluate(cmm_upsampler* u, cmm_ctx* c, double* out4);
+int cmm_upsampler_save(const cmm_upsampler* u, const char* path);
+int cmm_upsampler_load(cmm_upsampler* u, const char* path);
+/* attach (NULL detaches) after cmm_init; the upsampler must outlive the attachment */
+int cmm_attach_upsampler(cmm_ctx* c, cmm_upsampler* u, int exact_every, double tol);
+
+/* one periodic 3x3 convolution on host buffers (the network's kernel):
+ * out = [relu](conv(x, w) + bias) [* (mask > 0)] [+ res]; x[B*H][W][cin] BF16 bits,
+ * w[9][cin][cout] BF16 bits, bias[cout] or NULL, mask / res [B*H][W][cout] BF16 bits or
+ * NULL; out_f32 and/or out_bf16 [B*H][W][cout]; cin, cout in {16, 32}; W a multiple of 128 */
+int cmm_conv3x3(const unsigned short* x, const unsigned short* w, const float* bias, const unsigned short* mask,
+                const unsigned short* res, int relu, int B, int H, int W, int cin, int cout, float* out_f32,
+                unsigned short* out_bf16);
+/* its weight and bias gradients for the output gradient dy[B*H][W][cout]:
+ * dw[9][cin][cout] = sum_p x[p + tap offset][ci] dy[p][co], db[cout] = sum_p dy[p][co] */
+int cmm_conv3x3_weight_grad(const unsigned short* x, const unsigned short* dy, int B, int H, int W, int cin, int cout,
+                            float* dw, float* db);
+
 #ifdef __cplusplus
 }
 #endif

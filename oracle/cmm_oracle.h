@@ -254,6 +254,17 @@ void og_sample_points_dxdy(const og_state* st, const double* pos, double* out, i
 void og_particle_advect(int num, double dt, double* pos, const double* psi, const og_grid* g,
                         int time_integration_num, int l_order, const double* Lp12);
 
+/* ---- learned psi upsampler (og_learned.c): FP64 network, optional BF16 rounding emulation */
+double og_bf16_round(double v);
+void og_conv3x3(const double* x, int B, int H, int W, int cin, const double* w, const double* bias, int cout,
+                const double* mask, const double* res, int relu, double* out);
+void og_conv3x3_t(const double* dy, int B, int H, int W, int cin, const double* w, int cout, const double* mask,
+                  const double* res, double* dx);
+void og_conv3x3_dw(const double* x, const double* dy, int B, int H, int W, int cin, int cout, double* dw, double* db);
+double og_upsampler_loss_grad(const double* params, int nb, int C, const double* s_in, double s_out,
+                              const float* inputs, const float* targets, int B, int h, int w, int emulate_bf16,
+                              double* grad);
+
 #ifdef __cplusplus
 }
 #endif

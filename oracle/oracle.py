@@ -22,7 +22,8 @@ LIB_PATH = os.path.join(HERE, "liboracle.so")
 
 def build(force=False):
     """Compile liboracle.so with the committed Makefile (gcc + OpenMP)."""
-    srcs = [os.path.join(HERE, f) for f in ("og_hermite.c", "og_fft.c", "og_euler.c", "og_vlasov.c", "og_sample.c", "cmm_oracle.h")]
+    srcs = [os.path.join(HERE, f) for f in ("og_hermite.c", "og_fft.c", "og_euler.c", "og_vlasov.c", "og_sample.c", "og_learned.c",
+                                          "cmm_oracle.h")]
     if not force and os.path.exists(LIB_PATH):
         if os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(s) for s in srcs):
             return LIB_PATH
@@ -551,3 +552,100 @@ def poisson_hermite(vort, gv, gp, freq):
 def lagrange(t, t_next, loop_ctr, i_point, l_order):
     tt = np.ascontiguousarray(t, dtype=np.float64)
     return _kernel_lib().og_get_L_coefficient(_dp(tt), t_next, loop_ctr, i_point, l_order)
+
+
+# ---------------------------------------------------------------- learned psi upsampler
+def _learned_lib():
+    L = lib()
+    if not getattr(L, "_learned", False):
+        dp = C.POINTER(C.c_double)
+        fp = C.POINTER(C.c_float)
+        L.og_bf16_round.argtypes = [C.c_double]
+        L.og_bf16_round.restype = C.c_double
+        L.og_conv3x3.argtypes = [dp, C.c_int, C.c_int, C.c_int, C.c_int, dp, dp, C.c_int, dp, dp, C.c_int, dp]
+        L.og_conv3x3_t.argtypes = [dp, C.c_int, C.c_int, C.c_int, C.c_int, dp, C.c_int, dp, dp, dp]
+        L.og_conv3x3_dw.argtypes = [dp, dp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, dp, dp]
+        L.og_upsampler_loss_grad.argtypes = [dp, C.c_int, C.c_int, dp, C.c_double, fp, fp, C.c_int, C.c_int, C.c_int,
+                                             C.c_int, dp]
+        L.og_upsampler_loss_grad.restype = C.c_double
+        L._learned = True
+    return L
+
+
+def bf16_round(a):
+    """Round to the nearest BF16 value (ties to even), as float64."""
+    f = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    f = (f + 0x7FFF + ((f >> 16) & 1)) & 0xFFFF0000
+    return f.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def bf16_bits(a):
+    """BF16 bit patterns (uint16) of values already representable in BF16."""
+    return (np.ascontiguousarray(a, dtype=np.float32).view(np.uint32) >> 16).astype(np.uint16)
+
+
+def _opt(a):
+    """A float64 array already kept alive by the caller, or None (NULL)."""
+    return None if a is None else _dp(a)
+
+
+def conv3x3(x, w, bias=None, mask=None, res=None, relu=False):
+    """x[B, H, W, cin], w[9, cin, cout] -> out[B, H, W, cout] (periodic 3x3, FP64)."""
+    L = _learned_lib()
+    B, H, W, cin = x.shape
+    cout = w.shape[2]
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    bias, mask, res = (None if v is None else np.ascontiguousarray(v, dtype=np.float64) for v in (bias, mask, res))
+    out = np.empty((B, H, W, cout))
+    L.og_conv3x3(_dp(x), B, H, W, cin, _dp(w), _opt(bias), cout, _opt(mask), _opt(res), 1 if relu else 0, _dp(out))
+    return out
+
+
+def conv3x3_input_grad(dy, w, mask=None, res=None):
+    """dy[B, H, W, cout], w[9, cin, cout] -> dx[B, H, W, cin]."""
+    L = _learned_lib()
+    B, H, W, cout = dy.shape
+    cin = w.shape[1]
+    dy = np.ascontiguousarray(dy, dtype=np.float64)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    mask, res = (None if v is None else np.ascontiguousarray(v, dtype=np.float64) for v in (mask, res))
+    dx = np.empty((B, H, W, cin))
+    L.og_conv3x3_t(_dp(dy), B, H, W, cin, _dp(w), cout, _opt(mask), _opt(res), _dp(dx))
+    return dx
+
+
+def conv3x3_weight_grad(x, dy):
+    """x[B, H, W, cin], dy[B, H, W, cout] -> (dw[9, cin, cout], db[cout])."""
+    L = _learned_lib()
+    B, H, W, cin = x.shape
+    cout = dy.shape[3]
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    dy = np.ascontiguousarray(dy, dtype=np.float64)
+    dw = np.empty((9, cin, cout))
+    db = np.empty(cout)
+    L.og_conv3x3_dw(_dp(x), _dp(dy), B, H, W, cin, cout, _dp(dw), _dp(db))
+    return dw, db
+
+
+def upsampler_loss_grad(params, blocks, channels, s_in, s_out, inputs, targets, emulate_bf16=True):
+    """Loss and gradient of the upsampler: inputs[B, 7, h, w], targets[B, 2h, 2w] (float32)."""
+    L = _learned_lib()
+    params = np.ascontiguousarray(params, dtype=np.float64)
+    s_in = np.ascontiguousarray(s_in, dtype=np.float64)
+    inputs = np.ascontiguousarray(inputs, dtype=np.float32)
+    targets = np.ascontiguousarray(targets, dtype=np.float32)
+    B, _, h, w = inputs.shape
+    grad = np.zeros_like(params)
+    fp = C.POINTER(C.c_float)
+    loss = L.og_upsampler_loss_grad(_dp(params), blocks, channels, _dp(s_in), float(s_out),
+                                    inputs.ctypes.data_as(fp), targets.ctypes.data_as(fp), B, h, w,
+                                    1 if emulate_bf16 else 0, _dp(grad))
+    return loss, grad
+
+
+def upsampler_param_count(blocks, channels):
+    n = 9 * 16 * channels + channels
+    n += blocks * 2 * (9 * channels * channels + channels)
+    n += 9 * channels * 16 + 16
+    return n

@@ -127,7 +127,7 @@ def lib():
     L.cmm_upsampler_collect.argtypes = [vp, vp]
     L.cmm_upsampler_dataset_size.argtypes = [vp]
     L.cmm_upsampler_train.argtypes = [vp, ip, ip, C.c_double, C.c_ulonglong, dp, dp]
-    L.cmm_upsampler_loss_grad.argtypes = [vp, fp, fp, ip, ip, ip, dp]
+    L.cmm_upsampler_loss_grad.argtypes = [vp, fp, fp, ip, ip, ip, ip, dp]
     L.cmm_upsampler_infer.argtypes = [vp, fp, ip, ip, fp]
     L.cmm_upsampler_evaluate.argtypes = [vp, vp, dp]
     L.cmm_upsampler_save.argtypes = [vp, C.c_char_p]
@@ -452,20 +452,21 @@ class Upsampler:
                                          C.byref(sec)))
         return loss.value, sec.value
 
-    def loss_grad(self, inputs, targets):
-        """inputs[B, 7, h, w], targets[B, 2h, 2w] -> loss (gradient via grads())"""
+    def loss_grad(self, inputs, targets, cut=0):
+        """inputs[B, 7, h, w], targets[B, 2h, 2w] -> loss (gradient via grads()); cut > 0: the
+        psi-space spectral loss of training"""
         import numpy as np
         x = np.ascontiguousarray(inputs, dtype=np.float32)
         t = np.ascontiguousarray(targets, dtype=np.float32)
         B, _, h, w = x.shape
         loss = C.c_double()
         fp = C.POINTER(C.c_float)
-        check(self.L.cmm_upsampler_loss_grad(self.h, x.ctypes.data_as(fp), t.ctypes.data_as(fp), B, h, w,
+        check(self.L.cmm_upsampler_loss_grad(self.h, x.ctypes.data_as(fp), t.ctypes.data_as(fp), B, h, w, int(cut),
                                              C.byref(loss)))
         return loss.value
 
     def infer(self, inputs):
-        """inputs[7, h, w] -> correction[2h, 2w]"""
+        """inputs[7, h, w] -> predicted sub-grid vorticity on the 2x grid [2h, 2w]"""
         import numpy as np
         x = np.ascontiguousarray(inputs, dtype=np.float32)
         _, h, w = x.shape
@@ -475,10 +476,10 @@ class Upsampler:
         return out
 
     def evaluate(self, sim):
-        """relative differences from sim's exact psi: {cheap_linf, cheap_l2, learned_linf, learned_l2}"""
-        arr = (C.c_double * 4)()
+        """relative differences from sim's exact psi of the cheap, learned and psi-grid psi"""
+        arr = (C.c_double * 6)()
         check(self.L.cmm_upsampler_evaluate(self.h, sim.h, arr))
-        return dict(zip(("cheap_linf", "cheap_l2", "learned_linf", "learned_l2"), list(arr)))
+        return dict(zip(("cheap_linf", "cheap_l2", "learned_linf", "learned_l2", "grid_linf", "grid_l2"), list(arr)))
 
     def save(self, path):
         check(self.L.cmm_upsampler_save(self.h, str(path).encode()))

@@ -164,7 +164,7 @@ int cmm_upsampler_train(cmm_upsampler* u, int iters, int batch, double lr, unsig
 }
 
 int cmm_upsampler_loss_grad(cmm_upsampler* u, const float* inputs, const float* targets, int B, int h, int w,
-                            double* loss)
+                            int cut, double* loss)
 {
     if (!u || !inputs || !targets || !loss) return fail(CMM_ERR_PARAM, "NULL argument");
     if (B < 1 || h < 1 || w < 1 || w % cmm::lrn::kTile != 0) return fail(CMM_ERR_PARAM, "bad shape (w % 128 != 0?)");
@@ -180,7 +180,11 @@ int cmm_upsampler_loss_grad(cmm_upsampler* u, const float* inputs, const float* 
         om[(size_t)b] = din + (size_t)b * kIn * hw + 4 * hw;
         tg[(size_t)b] = dt + (size_t)b * 4 * hw;
     }
-    return up_rc(u, u->u->loss_grad(pl.data(), om.data(), tg.data(), B, h, w, loss, u->stream));
+    const int keep = u->u->spectral_cut();
+    u->u->set_spectral_cut(cut);
+    const int rc = u->u->loss_grad(pl.data(), om.data(), tg.data(), B, h, w, loss, u->stream);
+    u->u->set_spectral_cut(keep);
+    return up_rc(u, rc);
 }
 
 int cmm_upsampler_infer(cmm_upsampler* u, const float* inputs, int h, int w, float* fine)
@@ -200,10 +204,10 @@ int cmm_upsampler_infer(cmm_upsampler* u, const float* inputs, int h, int w, flo
     return e == cudaSuccess ? CMM_OK : fail(CMM_ERR_CUDA, cudaGetErrorString(e));
 }
 
-int cmm_upsampler_evaluate(cmm_upsampler* u, cmm_ctx* c, double* out4)
+int cmm_upsampler_evaluate(cmm_upsampler* u, cmm_ctx* c, double* out6)
 {
-    if (!u || !c || !c->sim || !out4) return fail(CMM_ERR_STATE, "cmm_upsampler_evaluate needs an initialised context");
-    int rc = c->sim->learned_evaluate(*u->u, out4);
+    if (!u || !c || !c->sim || !out6) return fail(CMM_ERR_STATE, "cmm_upsampler_evaluate needs an initialised context");
+    int rc = c->sim->learned_evaluate(*u->u, out6);
     if (rc) return fail(rc, c->sim->err);
     return CMM_OK;
 }

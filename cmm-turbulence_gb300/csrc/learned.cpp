@@ -3,6 +3,8 @@
 // learned_kernels.cu.
 #include "learned.hpp"
 
+#include <cufft.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -13,7 +15,7 @@ namespace cmm {
 namespace lrn {
 
 namespace {
-constexpr char kMagic[8] = {'C', 'M', 'M', 'U', 'P', 'S', '0', '2'};
+constexpr char kMagic[8] = {'C', 'M', 'M', 'U', 'P', 'S', '0', '3'};
 constexpr float kB1 = 0.9f, kB2 = 0.999f, kEps = 1e-8f;
 
 template <typename T>
@@ -80,7 +82,7 @@ Upsampler::Upsampler(int blocks, int channels) : nb_(blocks), ch_(channels)
     if (e == cudaSuccess) e = alloc(&wb_, n_wf_);
     if (e == cudaSuccess) e = alloc(&d_layers_, (long long)layers_.size());
     if (e == cudaSuccess) e = alloc(&d_sin_, kInCh);
-    if (e == cudaSuccess) e = alloc(&d_loss_, 1);
+    if (e == cudaSuccess) e = alloc(&d_loss_, 2 * kMaxBatch);
     if (e == cudaSuccess) e = alloc(&d_status_, 1);
     if (e == cudaSuccess)
         e = cudaMemcpy(d_layers_, layers_.data(), sizeof(LayerDesc) * layers_.size(), cudaMemcpyHostToDevice);
@@ -120,6 +122,11 @@ Upsampler::~Upsampler()
     release(part_);
     release(dbpart_);
     release(d_ptrs_);
+    release(rbuf_);
+    release(rspec_);
+    release(tspec_);
+    if (fft_r2c_) cufftDestroy((cufftHandle)fft_r2c_);
+    if (fft_c2r_) cufftDestroy((cufftHandle)fft_c2r_);
 }
 
 int Upsampler::init_weights(uint64_t seed)
@@ -284,6 +291,41 @@ int Upsampler::ensure(int B, int h, int w)
         cap_h_ = h;
         cap_w_ = w;
     }
+    return ensure_ptrs(B);
+}
+
+int Upsampler::ensure_fft(int B, int h, int w)
+{
+    const long long n = (long long)B * h * w;
+    if (B != fft_B_ || h != fft_h_ || w != fft_w_) {
+        if (fft_r2c_) cufftDestroy((cufftHandle)fft_r2c_);
+        if (fft_c2r_) cufftDestroy((cufftHandle)fft_c2r_);
+        fft_r2c_ = fft_c2r_ = 0;
+        release(rbuf_);
+        release(rspec_);
+        release(tspec_);
+        const long long nspec = (long long)B * 2 * h * (w + 1);
+        LRN_CHECK(alloc(&rbuf_, 4 * n), "buffers");
+        LRN_CHECK(alloc(&rspec_, nspec), "buffers");
+        LRN_CHECK(alloc(&tspec_, nspec), "buffers");
+        int dims[2] = {2 * h, 2 * w};
+        cufftHandle a = 0, b = 0;
+        if (cufftPlanMany(&a, 2, dims, nullptr, 1, 4 * h * w, nullptr, 1, 2 * h * (w + 1), CUFFT_R2C, B) != CUFFT_SUCCESS ||
+            cufftPlanMany(&b, 2, dims, nullptr, 1, 2 * h * (w + 1), nullptr, 1, 4 * h * w, CUFFT_C2R, B) != CUFFT_SUCCESS) {
+            err = "upsampler: cuFFT plan creation failed";
+            return 1;
+        }
+        fft_r2c_ = (int)a;
+        fft_c2r_ = (int)b;
+        fft_B_ = B;
+        fft_h_ = h;
+        fft_w_ = w;
+    }
+    return 0;
+}
+
+int Upsampler::ensure_ptrs(int B)
+{
     if (3 * B > ptr_cap_) {
         release(d_ptrs_);
         LRN_CHECK(alloc(&d_ptrs_, 3 * B), "buffers");
@@ -376,10 +418,47 @@ int Upsampler::backward(int B, int h, int w, cudaStream_t s)
     return dw(0, x0_, da_[cur], B, h, w, s);
 }
 
+double Upsampler::mean_ratio(const double* acc, int B)
+{
+    double m = 0;
+    for (int b = 0; b < B; ++b) m += acc[2 * b + 1] > 0 ? acc[2 * b] / acc[2 * b + 1] : 0.0;
+    return m / B;
+}
+
+int Upsampler::loss(int B, int h, int w, double* acc, cudaStream_t s)
+{
+    if (cut_ <= 0) {
+        LRN_CHECK(launch_loss(out32_, tgt_, B, h, w, dout_, acc, s), "loss");
+        ++launches;
+        return 0;
+    }
+    if (ensure_fft(B, h, w)) return 1;
+    LRN_CHECK(launch_shuffle_resid(out32_, tgt_, B, h, w, rbuf_, s), "loss");
+    cufftSetStream((cufftHandle)fft_r2c_, s);
+    cufftSetStream((cufftHandle)fft_c2r_, s);
+    if (cufftExecR2C((cufftHandle)fft_r2c_, rbuf_, reinterpret_cast<cufftComplex*>(rspec_)) != CUFFT_SUCCESS ||
+        cufftExecR2C((cufftHandle)fft_r2c_, tgt_, reinterpret_cast<cufftComplex*>(tspec_)) != CUFFT_SUCCESS) {
+        err = "upsampler: cuFFT R2C failed";
+        return 1;
+    }
+    LRN_CHECK(launch_spec_loss(rspec_, tspec_, B, 2 * h, 2 * w, cut_, acc, s), "loss");
+    if (cufftExecC2R((cufftHandle)fft_c2r_, reinterpret_cast<cufftComplex*>(rspec_), rbuf_) != CUFFT_SUCCESS) {
+        err = "upsampler: cuFFT C2R failed";
+        return 1;
+    }
+    LRN_CHECK(launch_grad_pack(rbuf_, acc, B, h, w, dout_, s), "loss");
+    launches += 3;
+    return 0;
+}
+
 int Upsampler::loss_grad(const float* const* planes, const float* const* omega, const float* const* target, int B,
                          int h, int w, double* loss, cudaStream_t s)
 {
     if (!params_) return 1;
+    if (B > kMaxBatch) {
+        err = "upsampler: at most 256 samples";
+        return 1;
+    }
     if (ensure(B, h, w) || prepare(s)) return 1;
     std::vector<const float*> ptr(3 * (size_t)B);
     for (int b = 0; b < B; ++b) {
@@ -392,17 +471,19 @@ int Upsampler::loss_grad(const float* const* planes, const float* const* omega, 
                               s),
               "assemble");
     if (forward(B, h, w, true, s)) return 1;
-    LRN_CHECK(cudaMemsetAsync(d_loss_, 0, sizeof(double), s), "loss_grad");
-    LRN_CHECK(launch_loss(out32_, tgt_, B, h, w, dout_, d_loss_, s), "loss");
+    LRN_CHECK(cudaMemsetAsync(d_loss_, 0, 2 * sizeof(double) * B, s), "loss_grad");
+    if (this->loss(B, h, w, d_loss_, s)) return 1;
     if (backward(B, h, w, s)) return 1;
     int st = 0;
-    LRN_CHECK(cudaMemcpyAsync(loss, d_loss_, sizeof(double), cudaMemcpyDeviceToHost, s), "loss_grad");
+    std::vector<double> acc(2 * (size_t)B);
+    LRN_CHECK(cudaMemcpyAsync(acc.data(), d_loss_, 2 * sizeof(double) * B, cudaMemcpyDeviceToHost, s), "loss_grad");
     LRN_CHECK(cudaMemcpyAsync(&st, d_status_, sizeof(int), cudaMemcpyDeviceToHost, s), "loss_grad");
     LRN_CHECK(cudaStreamSynchronize(s), "loss_grad");
     if (st) {
         err = "upsampler: a tensor-core wait ran out";
         return 1;
     }
+    *loss = cut_ > 0 ? mean_ratio(acc.data(), B) : acc[0];
     return 0;
 }
 
@@ -412,8 +493,8 @@ int Upsampler::train(int iters, int batch, double lr, uint64_t seed, double* los
         err = "upsampler: no training pairs";
         return 1;
     }
-    if (iters < 1 || batch < 1) {
-        err = "upsampler: iterations and batch must be positive";
+    if (iters < 1 || batch < 1 || batch > kMaxBatch) {
+        err = "upsampler: iterations >= 1 and 1 <= batch <= 256";
         return 1;
     }
     if (!scaled_ && fit_scales(s)) return 1;
@@ -435,9 +516,9 @@ int Upsampler::train(int iters, int batch, double lr, uint64_t seed, double* los
     const float** dptr = nullptr;
     double* dloss = nullptr;
     LRN_CHECK(alloc(&dptr, (long long)ptr.size()), "train");
-    LRN_CHECK(alloc(&dloss, iters), "train");
+    LRN_CHECK(alloc(&dloss, 2ll * batch * iters), "train");
     LRN_CHECK(cudaMemcpyAsync(dptr, ptr.data(), sizeof(float*) * ptr.size(), cudaMemcpyHostToDevice, s), "train");
-    LRN_CHECK(cudaMemsetAsync(dloss, 0, sizeof(double) * iters, s), "train");
+    LRN_CHECK(cudaMemsetAsync(dloss, 0, sizeof(double) * 2 * batch * iters, s), "train");
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -447,7 +528,7 @@ int Upsampler::train(int iters, int batch, double lr, uint64_t seed, double* los
         LRN_CHECK(launch_assemble(p, p + batch, p + 2 * batch, batch, h, w, d_sin_, (float)(1.0 / s_out_), x0_, tgt_, s),
                   "assemble");
         if (forward(batch, h, w, true, s)) return 1;
-        LRN_CHECK(launch_loss(out32_, tgt_, batch, h, w, dout_, dloss + it, s), "loss");
+        if (this->loss(batch, h, w, dloss + 2ll * batch * it, s)) return 1;
         if (backward(batch, h, w, s)) return 1;
         ++adam_t_;
         const float c1 = (float)(1.0 - std::pow((double)kB1, (double)adam_t_));
@@ -459,9 +540,9 @@ int Upsampler::train(int iters, int batch, double lr, uint64_t seed, double* los
         if (prepare(s)) return 1;
     }
     cudaEventRecord(e1, s);
-    std::vector<double> hl((size_t)iters);
+    std::vector<double> hl(2 * (size_t)batch * iters);
     int st = 0;
-    LRN_CHECK(cudaMemcpyAsync(hl.data(), dloss, sizeof(double) * iters, cudaMemcpyDeviceToHost, s), "train");
+    LRN_CHECK(cudaMemcpyAsync(hl.data(), dloss, sizeof(double) * hl.size(), cudaMemcpyDeviceToHost, s), "train");
     LRN_CHECK(cudaMemcpyAsync(&st, d_status_, sizeof(int), cudaMemcpyDeviceToHost, s), "train");
     LRN_CHECK(cudaStreamSynchronize(s), "train");
     float ms = 0;
@@ -478,7 +559,8 @@ int Upsampler::train(int iters, int batch, double lr, uint64_t seed, double* los
     }
     const int k = std::min(iters, 16);
     double m = 0;
-    for (int i = iters - k; i < iters; ++i) m += hl[(size_t)i];
+    for (int i = iters - k; i < iters; ++i)
+        m += cut_ > 0 ? mean_ratio(hl.data() + 2 * (size_t)batch * i, batch) : hl[2 * (size_t)batch * i];
     if (loss) *loss = m / k;
     return 0;
 }
@@ -492,7 +574,7 @@ int Upsampler::infer(const float* planes4, const float* omega, int h, int w, flo
     LRN_CHECK(cudaMemcpyAsync(d_ptrs_, ptr, sizeof(ptr), cudaMemcpyHostToDevice, s), "infer");
     LRN_CHECK(launch_assemble(d_ptrs_, d_ptrs_ + 1, nullptr, 1, h, w, d_sin_, 1.f, x0_, nullptr, s), "assemble");
     if (forward(1, h, w, false, s)) return 1;
-    LRN_CHECK(launch_shuffle_out(out32_, h, w, (float)s_out_, fine, s), "shuffle");
+    LRN_CHECK(launch_shuffle_out(out32_, nullptr, h, w, (float)s_out_, fine, s), "shuffle");
     launches += 2;
     return 0;
 }
@@ -503,7 +585,7 @@ int Upsampler::save(const std::string& path) const
     if (get_params(p.data(), n_params_)) return 1;
     std::ofstream f(path, std::ios::binary);
     if (!f) return 1;
-    const int32_t hdr[2] = {nb_, ch_};
+    const int32_t hdr[3] = {nb_, ch_, cut_};
     const int64_t n = n_params_;
     f.write(kMagic, 8);
     f.write(reinterpret_cast<const char*>(hdr), sizeof(hdr));
@@ -518,7 +600,7 @@ int Upsampler::load(const std::string& path)
 {
     std::ifstream f(path, std::ios::binary);
     char magic[8];
-    int32_t hdr[2];
+    int32_t hdr[3];
     int64_t n = 0;
     double sin[kInCh], sout = 1;
     if (!f.read(magic, 8) || std::memcmp(magic, kMagic, 8) != 0 || !f.read(reinterpret_cast<char*>(hdr), sizeof(hdr)) ||
@@ -537,6 +619,7 @@ int Upsampler::load(const std::string& path)
         return 1;
     }
     set_scales(sin, sout);
+    cut_ = hdr[2];
     return set_params(p.data(), n);
 }
 

@@ -1,9 +1,12 @@
 // learned.hpp -- the learned psi upsampler.
 //
-// A residual network of 3x3 periodic convolutions maps the cheap coarse-grid fields
-// (psi and its Hermite derivatives from omega sampled on the map grid, that omega and its
-// gradient) to the correction that turns the cheap psi into the psi the full vorticity-grid
-// evaluation gives, on the psi grid (twice the map grid).  Layout: activations BF16,
+// A residual network of 3x3 periodic convolutions maps the cheap coarse-grid fields (psi
+// and its Hermite derivatives from omega sampled on the map grid, that omega and its
+// gradient) to the vorticity the map-grid samples miss, on the psi grid (twice the map
+// grid: the 2 x 2 sub-pixels of each map cell): omega sampled through the map on the psi
+// grid minus the spectral interpolation of the map-grid samples.  That sub-grid content is
+// local, and small where the flow is resolved, so BF16 relative errors on it become small
+// psi errors: the learned psi is the cheap psi plus the psi solve of the prediction.  Layout: activations BF16,
 // pixel-major [rows][W][C] with rows = images x H; the image is periodic in both
 // directions.  Layers: head conv 7(16) -> C, B residual blocks (conv, ReLU, conv, + skip),
 // tail conv C -> 4(16) whose four channels are the 2 x 2 sub-pixels of the psi grid.
@@ -31,6 +34,7 @@ constexpr int kPitch = 130;    // staged pixels per row (the tile and one halo p
 constexpr int kInCh = 7;       // psi, psi_x, psi_y, psi_xy (cheap), omega, omega_x, omega_y (map grid)
 constexpr int kHeadIn = 16;    // input channels padded to the K = 16 MMA slice
 constexpr int kTailOut = 16;   // output channels padded to N = 16 (4 used: the 2 x 2 sub-pixels)
+constexpr int kMaxBatch = 256;
 
 // out = [relu](conv3x3(in, w) + bias) [* (mask > 0)] [+ res]
 struct ConvArgs {
@@ -83,8 +87,19 @@ cudaError_t launch_assemble(const float* const* planes, const float* const* omeg
 // channels) and the loss (added to *loss)
 cudaError_t launch_loss(const float* out16, const float* tgt, int B, int h, int w, bf16* dout, double* loss,
                         cudaStream_t s);
-// tail output (channels 0..3) -> 2h x 2w field times scale
-cudaError_t launch_shuffle_out(const float* out16, int h, int w, float scale, float* fine, cudaStream_t s);
+// tail output (channels 0..3) -> 2h x 2w field: fine[2y + i][2x + j] = base[y][x] + scale out[y][x][2i + j]
+// (base may be null)
+cudaError_t launch_shuffle_out(const float* out16, const float* base, int h, int w, float scale, float* fine,
+                               cudaStream_t s);
+// out = a - b
+cudaError_t launch_sub(const float* a, const float* b, long long n, float* out, cudaStream_t s);
+// spectral (psi-space) loss: r = shuffled tail output - target (B x 2h x 2w); on the half
+// spectra of r and the target, per sample acc[2b..2b+1] += {sum w |R|^2, sum w |T|^2} with
+// w = 1/|k|^4 on 0 < |k| <= cut and R *= w; the loss is the mean over samples of
+// num / den, the tail's output gradient 2 C2R(w R_b) / (B den_b)
+cudaError_t launch_shuffle_resid(const float* out16, const float* tgt, int B, int h, int w, float* r, cudaStream_t s);
+cudaError_t launch_spec_loss(float2* R, const float2* T, int B, int H2, int W2, int cut, double* acc, cudaStream_t s);
+cudaError_t launch_grad_pack(const float* g, const double* acc, int B, int h, int w, bf16* dout, cudaStream_t s);
 // sum of squares per channel over n fields of `count` values each: out[k] += sum x^2
 cudaError_t launch_sumsq_ptrs(const float* const* ptrs, int n, long long offset, long long count, double* out,
                               cudaStream_t s);
@@ -93,8 +108,6 @@ cudaError_t launch_sumsq_ptrs(const float* const* ptrs, int n, long long offset,
 // (out4 zeroed by the caller; maxima of non-negative values through their bit patterns)
 cudaError_t launch_diff_stats(const float* a, long long sa, const float* e, long long se, long long n, double* out4,
                               cudaStream_t s);
-// out[i] = e[i se] - c[i]
-cudaError_t launch_sub_strided(const float* e, long long se, const float* c, long long n, float* out, cudaStream_t s);
 
 // The network, its optimiser, its training pairs and its work buffers.
 class Upsampler {
@@ -114,19 +127,26 @@ public:
     void get_scales(double* s_in, double* s_out) const;
 
     // one training pair from device fields of the map grid (h x w) and the psi grid
-    // (2h x 2w): the 4 cheap psi planes, omega and its gradient (3 planes), and
-    // target = exact psi - cheap psi
+    // (2h x 2w): the 4 cheap psi planes, omega and its gradient (3 planes), and the target
+    // (omega on the psi grid minus the spectral interpolation of the map-grid samples)
     int append(const float* planes4, const float* omega, const float* target, int h, int w, cudaStream_t s);
     int dataset_size() const { return (int)snaps_.size(); }
     void clear_dataset();
     int fit_scales(cudaStream_t s);                 // RMS of each input channel and of the target
+    // Loss: with a spectral cut-off set (the psi solve's, in integer wavenumbers of the 2 pi
+    // periodic domain) the mean over the batch of each sample's relative psi-space error
+    // sum w |FFT(pred - target)|^2 / sum w |FFT(target)|^2, w = 1/|k|^4 on 0 < |k| <= cut,
+    // i.e. the part of the prediction the psi solve keeps, weighted as psi; with cut 0 the
+    // mean squared error.
+    void set_spectral_cut(int cut) { cut_ = cut; }
+    int spectral_cut() const { return cut_; }
     // iters Adam steps on batches drawn from the pairs (mt19937_64(seed)); the mean loss of
     // the last min(iters, 16) steps in *loss
     int train(int iters, int batch, double lr, uint64_t seed, double* loss, cudaStream_t s);
     // loss and gradient (kept for get_grads) of B samples given as device fields
     int loss_grad(const float* const* planes, const float* const* omega, const float* const* target, int B, int h,
                   int w, double* loss, cudaStream_t s);
-    // correction on the psi grid (2h x 2w, physical units) from the cheap fields
+    // the predicted sub-grid vorticity on the psi grid (2h x 2w)
     int infer(const float* planes4, const float* omega, int h, int w, float* fine, cudaStream_t s);
 
     int save(const std::string& path) const;
@@ -139,8 +159,12 @@ public:
 
 private:
     int ensure(int B, int h, int w);
+    int ensure_fft(int B, int h, int w);
+    int ensure_ptrs(int B);
     int prepare(cudaStream_t s);
     int forward(int B, int h, int w, bool keep, cudaStream_t s);
+    int loss(int B, int h, int w, double* acc, cudaStream_t s);   // acc: {loss} or B x {num, den}
+    static double mean_ratio(const double* acc, int B);
     int backward(int B, int h, int w, cudaStream_t s);
     int fail(const char* what, cudaError_t e);
     int conv(int layer, bool flipped, const bf16* in, const bf16* mask, const bf16* res, bf16* out, float* out32,
@@ -177,6 +201,10 @@ private:
     float *part_ = nullptr, *dbpart_ = nullptr;
     int part_cap_ = 0;
     double* d_loss_ = nullptr;
+    int cut_ = 0;
+    float* rbuf_ = nullptr;              // B x 2h x 2w residual / gradient
+    float2 *rspec_ = nullptr, *tspec_ = nullptr;
+    int fft_r2c_ = 0, fft_c2r_ = 0, fft_B_ = 0, fft_h_ = 0, fft_w_ = 0;   // cuFFT: B transforms of 2h x 2w
     int* d_status_ = nullptr;
     const float** d_ptrs_ = nullptr;     // 3 x B device pointers for assemble
     int ptr_cap_ = 0;

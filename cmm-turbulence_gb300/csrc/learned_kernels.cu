@@ -517,16 +517,108 @@ __global__ void k_loss(const float* __restrict__ out16, const float* __restrict_
     if (threadIdx.x == 0) atomicAdd(loss, (double)red[0] * (double)inv_n);
 }
 
-__global__ void k_shuffle_out(const float* __restrict__ out16, int h, int w, float scale, float* __restrict__ fine)
+__global__ void k_shuffle_out(const float* __restrict__ out16, const float* __restrict__ base, int h, int w,
+                              float scale, float* __restrict__ fine)
 {
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= (long long)h * w) return;
     const int y = (int)(i / w), x = (int)(i % w);
     const float4 v = *reinterpret_cast<const float4*>(out16 + i * 16);
+    const float b = base ? base[i] : 0.f;
     float2* r0 = reinterpret_cast<float2*>(fine + (2ll * y) * 2 * w + 2 * x);
     float2* r1 = reinterpret_cast<float2*>(fine + (2ll * y + 1) * 2 * w + 2 * x);
-    *r0 = make_float2(v.x * scale, v.y * scale);
-    *r1 = make_float2(v.z * scale, v.w * scale);
+    *r0 = make_float2(fmaf(v.x, scale, b), fmaf(v.y, scale, b));
+    *r1 = make_float2(fmaf(v.z, scale, b), fmaf(v.w, scale, b));
+}
+
+// spectral loss: r = shuffled prediction - target on the 2h x 2w grid of each sample
+__global__ void k_shuffle_resid(const float* __restrict__ out16, const float* __restrict__ tgt, int B, int h, int w,
+                                float* __restrict__ r)
+{
+    const long long hw = (long long)h * w;
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= (long long)B * hw) return;
+    const int b = (int)(i / hw);
+    const long long p = i - b * hw;
+    const int y = (int)(p / w), x = (int)(p % w);
+    const float4 v = *reinterpret_cast<const float4*>(out16 + i * 16);
+    const long long q0 = (long long)b * 4 * hw + (2ll * y) * 2 * w + 2 * x, q1 = q0 + 2ll * w;
+    r[q0] = v.x - tgt[q0];
+    r[q0 + 1] = v.y - tgt[q0 + 1];
+    r[q1] = v.z - tgt[q1];
+    r[q1 + 1] = v.w - tgt[q1 + 1];
+}
+
+// half spectra (R2C layout, B x H2 x (W2/2 + 1)) of the residual and the target: per sample b,
+// acc[2b], acc[2b + 1] += {sum w |R|^2, sum w |T|^2} over the full spectrum with w = 1/|k|^4
+// on 0 < |k| <= cut, and R *= w in place (the gradient's spectrum).  blockIdx.y = sample.
+__global__ void k_spec_loss(float2* __restrict__ R, const float2* __restrict__ T, int H2, int W2, float cut2,
+                            double* __restrict__ acc)
+{
+    __shared__ double red[2][256];
+    const int nxf = W2 / 2 + 1;
+    const long long n = (long long)H2 * nxf;
+    const long long b0 = (long long)blockIdx.y * n;
+    double num = 0, den = 0;
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
+        const long long i = b0 + j;
+        const int kx = (int)(i % nxf);
+        const int ky0 = (int)((i / nxf) % H2);
+        const int ky = 2 * ky0 > H2 ? ky0 - H2 : ky0;
+        const float k2 = (float)(kx * kx + ky * ky);
+        const float wk = (k2 > 0.f && k2 <= cut2) ? 1.0f / (k2 * k2) : 0.f;
+        const double mult = (kx == 0 || 2 * kx == W2) ? 1.0 : 2.0;
+        const float2 r = R[i], t = T[i];
+        num += mult * wk * ((double)r.x * r.x + (double)r.y * r.y);
+        den += mult * wk * ((double)t.x * t.x + (double)t.y * t.y);
+        R[i] = make_float2(r.x * wk, r.y * wk);
+    }
+    red[0][threadIdx.x] = num;
+    red[1][threadIdx.x] = den;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + s];
+            red[1][threadIdx.x] += red[1][threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        atomicAdd(acc + 2 * blockIdx.y, red[0][0]);
+        atomicAdd(acc + 2 * blockIdx.y + 1, red[1][0]);
+    }
+}
+
+// gradient of L = (1/B) sum_b num_b / den_b: dL/dpred_b = 2 C2R(w R_b) / (B den_b), packed
+// into the tail's 16 channels
+__global__ void k_grad_pack(const float* __restrict__ g, const double* __restrict__ acc, int B, int h, int w,
+                            bf16* __restrict__ dout)
+{
+    const long long hw = (long long)h * w;
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= (long long)B * hw) return;
+    const int b = (int)(i / hw);
+    const double den = acc[2 * b + 1];
+    const float sc = den > 0 ? (float)(2.0 / ((double)B * den)) : 0.f;
+    const long long p = i - b * hw;
+    const int y = (int)(p / w), x = (int)(p % w);
+    const long long q0 = (long long)b * 4 * hw + (2ll * y) * 2 * w + 2 * x, q1 = q0 + 2ll * w;
+    float f[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) f[c] = 0.f;
+    f[0] = g[q0] * sc;
+    f[1] = g[q0 + 1] * sc;
+    f[2] = g[q1] * sc;
+    f[3] = g[q1 + 1] * sc;
+    uint4* o = reinterpret_cast<uint4*>(dout + i * 16);
+    o[0] = pack8(f);
+    o[1] = pack8(f + 8);
+}
+
+__global__ void k_sub(const float* __restrict__ a, const float* __restrict__ b, long long n, float* __restrict__ out)
+{
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = a[i] - b[i];
 }
 
 __global__ void k_sumsq_ptrs(const float* const* __restrict__ ptrs, int n, long long offset, long long count,
@@ -583,13 +675,6 @@ __global__ void k_diff_stats(const float* __restrict__ a, long long sa, const fl
         atomicAdd(out4 + 2, r[2][0]);
         atomicAdd(out4 + 3, r[3][0]);
     }
-}
-
-__global__ void k_sub_strided(const float* __restrict__ e, long long se, const float* __restrict__ c, long long n,
-                              float* __restrict__ out)
-{
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i < n) out[i] = e[i * se] - c[i];
 }
 
 template <int CIN, int COUT>
@@ -707,10 +792,40 @@ cudaError_t launch_loss(const float* out16, const float* tgt, int B, int h, int 
     return cudaGetLastError();
 }
 
-cudaError_t launch_shuffle_out(const float* out16, int h, int w, float scale, float* fine, cudaStream_t s)
+cudaError_t launch_shuffle_out(const float* out16, const float* base, int h, int w, float scale, float* fine,
+                               cudaStream_t s)
 {
     const long long n = (long long)h * w;
-    k_shuffle_out<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out16, h, w, scale, fine);
+    k_shuffle_out<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out16, base, h, w, scale, fine);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shuffle_resid(const float* out16, const float* tgt, int B, int h, int w, float* r, cudaStream_t s)
+{
+    const long long n = (long long)B * h * w;
+    k_shuffle_resid<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out16, tgt, B, h, w, r);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spec_loss(float2* R, const float2* T, int B, int H2, int W2, int cut, double* acc, cudaStream_t s)
+{
+    const long long n = (long long)H2 * (W2 / 2 + 1);
+    if (B > 65535) return cudaErrorInvalidValue;
+    dim3 blocks((unsigned)std::max(1ll, std::min(256ll, (n + 255) / 256)), (unsigned)B);
+    k_spec_loss<<<blocks, 256, 0, s>>>(R, T, H2, W2, (float)cut * (float)cut, acc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grad_pack(const float* g, const double* acc, int B, int h, int w, bf16* dout, cudaStream_t s)
+{
+    const long long n = (long long)B * h * w;
+    k_grad_pack<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, acc, B, h, w, dout);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sub(const float* a, const float* b, long long n, float* out, cudaStream_t s)
+{
+    k_sub<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, b, n, out);
     return cudaGetLastError();
 }
 
@@ -727,12 +842,6 @@ cudaError_t launch_diff_stats(const float* a, long long sa, const float* e, long
 {
     const int blocks = (int)std::max(1ll, std::min(1024ll, (n + 255) / 256));
     k_diff_stats<<<blocks, 256, 0, s>>>(a, sa, e, se, n, out4);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_sub_strided(const float* e, long long se, const float* c, long long n, float* out, cudaStream_t s)
-{
-    k_sub_strided<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(e, se, c, n, out);
     return cudaGetLastError();
 }
 

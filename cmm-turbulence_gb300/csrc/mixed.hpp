@@ -76,13 +76,17 @@ cudaError_t launch_vel_to_f64(const float2* v, int num, double* out, cudaStream_
 cudaError_t launch_vel_from_f64(const double* v, int num, float2* out, cudaStream_t s);
 cudaError_t launch_pos_to_fix(const double* pos, int num, const Grid& g, unsigned long long* out, cudaStream_t s);
 cudaError_t launch_fix_to_pos(const unsigned long long* in, int num, const Grid& g, double* pos, cudaStream_t s);
+// learned psi: the psi solve of (omega sampled on the map grid gc, spectrum Fc, interpolated
+// spectrally) + (vorticity correction on the psi grid, spectrum D); cut off and
+// differentiated like launch_spec_psi_f
+cudaError_t launch_spec_psi_learned(const float2* Fc, const Grid& gc, const float2* D, const Grid& gp, double freq,
+                                    float2* out4, cudaStream_t s);
+// the map-grid spectrum Fc placed in the psi grid's spectrum (normalised by 1/gc.N): its
+// inverse transform on the psi grid is the spectral interpolation of the map-grid samples
+cudaError_t launch_spec_pad(const float2* Fc, const Grid& gc, const Grid& gp, float2* out, cudaStream_t s);
 // omega, omega_x, omega_y at the map-grid nodes (3 planes of gm.N floats)
 cudaError_t launch_sample_grad_m(const Grid& gm, const Grid& gf, const float4* map, const float4* W, float* out3,
                                  cudaStream_t s);
-// learned psi: the psi of omega sampled on the map grid gc (spectrum Fc) plus the correction
-// with spectrum D on the psi grid, cut off and differentiated like launch_spec_psi_f
-cudaError_t launch_spec_psi_learned(const float2* Fc, const Grid& gc, const float2* D, const Grid& gp, double freq,
-                                    float2* out4, cudaStream_t s);
 cudaError_t launch_spec_psi_f(const float2* Fv, const Grid& gv, const Grid& gp, double freq, float2* out4,
                               cudaStream_t s);
 // 4 planes (float or double) -> float4 nodes

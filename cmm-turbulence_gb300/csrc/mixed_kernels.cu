@@ -1343,6 +1343,18 @@ cudaError_t launch_spec_psi_f(const float2* Fv, const Grid& gv, const Grid& gp, 
     return cudaGetLastError();
 }
 
+__device__ __forceinline__ float2 padded_mode(const float2* __restrict__ Fc, const Grid& gc, const Grid& gp, int iXc,
+                                              int iYc, float inv_nc)
+{
+    const bool hx = 2 * iXc > gp.NX, hy = 2 * iYc > gp.NY;
+    const int fX = hx ? gp.NX - iXc : iXc, fY = hy ? gp.NY - iYc : iYc;
+    if (2 * fX > gc.NX || 2 * fY > gc.NY) return make_float2(0.f, 0.f);
+    const int iXs = iXc + (hx ? gc.NX - gp.NX : 0);
+    const int iYs = iYc + (hy ? gc.NY - gp.NY : 0);
+    const float2 f = Fc[(long long)iYs * gc.NX_fft + iXs];
+    return make_float2(f.x * inv_nc, f.y * inv_nc);
+}
+
 __global__ void k_spec_psi_learned(const float2* __restrict__ Fc, Grid gc, const float2* __restrict__ D, Grid gp,
                                    float freq, float inv_nc, float inv_np, float2* __restrict__ out4)
 {
@@ -1351,20 +1363,14 @@ __global__ void k_spec_psi_learned(const float2* __restrict__ Fc, Grid gc, const
     const long long i = (long long)iYc * gp.NX_fft + iXc;
     const bool hx = 2 * iXc > gp.NX, hy = 2 * iYc > gp.NY;
     const int fX = hx ? gp.NX - iXc : iXc, fY = hy ? gp.NY - iYc : iYc;
-    float2 W = make_float2(0.f, 0.f);
-    if (!(2 * fX > gc.NX || 2 * fY > gc.NY)) {
-        const int iXs = iXc + (hx ? gc.NX - gp.NX : 0);
-        const int iYs = iYc + (hy ? gc.NY - gp.NY : 0);
-        const float2 f = Fc[(long long)iYs * gc.NX_fft + iXs];
-        W = make_float2(f.x * inv_nc, f.y * inv_nc);
-    }
     const float kx = gp.kfxf * (float)(hx ? iXc - gp.NX : iXc);
     const float ky = gp.kfyf * (float)(hy ? iYc - gp.NY : iYc);
     float2 P = make_float2(0.f, 0.f);
     if (!(iXc == 0 && iYc == 0) && !((float)(fX * fX + fY * fY) > freq * freq)) {
-        const float ik2 = 1.0f / (kx * kx + ky * ky);
+        const float2 w = padded_mode(Fc, gc, gp, iXc, iYc, inv_nc);
         const float2 d = D[i];
-        P = make_float2(-W.x * ik2 + d.x * inv_np, -W.y * ik2 + d.y * inv_np);
+        const float ik2 = 1.0f / (kx * kx + ky * ky);
+        P = make_float2(-(w.x + d.x * inv_np) * ik2, -(w.y + d.y * inv_np) * ik2);
     }
     const float2 Py = make_float2(-P.y * ky, P.x * ky);
     out4[i] = P;
@@ -1380,6 +1386,21 @@ cudaError_t launch_spec_psi_learned(const float2* Fc, const Grid& gc, const floa
     dim3 blocks((unsigned)((gp.NX_fft + 255) / 256), (unsigned)gp.NY);
     k_spec_psi_learned<<<blocks, 256, 0, s>>>(Fc, gc, D, gp, (float)freq, (float)(1.0 / (double)gc.N),
                                               (float)(1.0 / (double)gp.N), out4);
+    return cudaGetLastError();
+}
+
+__global__ void k_spec_pad(const float2* __restrict__ Fc, Grid gc, Grid gp, float inv_nc, float2* __restrict__ out)
+{
+    const int iXc = blockIdx.x * blockDim.x + threadIdx.x, iYc = blockIdx.y;
+    if (iXc >= gp.NX_fft) return;
+    out[(long long)iYc * gp.NX_fft + iXc] = padded_mode(Fc, gc, gp, iXc, iYc, inv_nc);
+}
+
+cudaError_t launch_spec_pad(const float2* Fc, const Grid& gc, const Grid& gp, float2* out, cudaStream_t s)
+{
+    if (gp.NY > 65535) return cudaErrorInvalidValue;
+    dim3 blocks((unsigned)((gp.NX_fft + 255) / 256), (unsigned)gp.NY);
+    k_spec_pad<<<blocks, 256, 0, s>>>(Fc, gc, gp, (float)(1.0 / (double)gc.N), out);
     return cudaGetLastError();
 }
 

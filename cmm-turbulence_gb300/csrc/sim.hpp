@@ -54,16 +54,17 @@ public:
     int ens_end();
 
     // learned psi (precision=mixed, Euler; csrc/sim_learned.cpp).  With an upsampler attached,
-    // a step evaluates psi from omega sampled on the map grid plus the network's correction,
-    // except every `every`-th step, which runs the vorticity-grid evaluation and compares the
+    // a step evaluates psi from the cheap vorticity plus the network's sub-grid vorticity on the psi grid (predicted from omega and
+    // its gradient on the map grid), except every `every`-th step, which runs the vorticity-grid evaluation and compares the
     // learned psi with it: a relative L-infinity difference above `tol` makes the next
     // every - 1 steps exact as well.  null detaches.  learned_collect appends the current
-    // state's training pair (cheap fields, exact psi - cheap psi); learned_evaluate gives the
-    // relative L-infinity and L2 differences of the cheap and of the learned psi from the
-    // current exact psi level (out = {cheap Linf, cheap L2, learned Linf, learned L2}).
+    // state's training pair (map-grid fields, the sub-grid vorticity on the psi grid); learned_evaluate gives the
+    // relative L-infinity and L2 differences of the cheap psi, the learned psi and the psi of
+    // omega sampled exactly on the psi grid from the current exact psi level
+    // (out = {cheap Linf, cheap L2, learned Linf, learned L2, psi-grid Linf, psi-grid L2}).
     int attach_upsampler(lrn::Upsampler* u, int every, double tol);
     int learned_collect(lrn::Upsampler& u);
-    int learned_evaluate(lrn::Upsampler& u, double* out4);
+    int learned_evaluate(lrn::Upsampler& u, double* out6);
 
     int get_field(const std::string& name, void* dst, size_t bytes);
     size_t field_bytes(const std::string& name) const;
@@ -188,7 +189,7 @@ private:
     double learned_last_err_ = 0, learned_max_err_ = 0;
     float *lc_omega_ = nullptr, *lc_planes_ = nullptr, *l_delta_ = nullptr, *l_planes_ = nullptr;
     float2 *lc_spec_ = nullptr, *lc_spec4_ = nullptr, *l_dspec_ = nullptr;
-    int lc_r2c_ = 0, lc_c2r4_ = 0, l_r2c_ = 0;    // cuFFT handles
+    int lc_r2c_ = 0, lc_c2r4_ = 0, l_r2c_ = 0, l_c2r_ = 0;    // cuFFT handles
     double* d_stats_ = nullptr;
     bool in_step_ = false;
 

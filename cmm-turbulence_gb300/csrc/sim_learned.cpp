@@ -5,11 +5,12 @@
 // Cheap psi: the same solve from omega sampled on the map grid (16x fewer samples at the
 // metric's 512^2 map / 2048^2 vorticity grids), which aliases the vorticity scales the map
 // grid cannot hold into the retained modes.
-// Learned psi: the cheap psi plus the upsampler's correction (its network sees the cheap
-// psi planes, omega and omega's gradient on the map grid -- the gradient, through the map's
-// Jacobian, tells the vorticity scales the map grid cannot hold apart from the ones it
-// can -- and outputs the correction on the psi grid, twice as fine), projected through the
-// same cut-off and differentiated spectrally.
+// Learned psi: the upsampler's network sees the cheap psi planes, omega and omega's
+// gradient on the map grid (the gradient, through the map's Jacobian, tells the vorticity
+// scales the map grid cannot hold apart from the ones it can) and predicts, on the psi grid,
+// the vorticity the map-grid samples miss (omega on the psi grid minus the spectral
+// interpolation of the samples); the learned psi solves the cheap vorticity plus that
+// prediction with the method's cut-off, Poisson step and Hermite derivatives.
 #include <cufft.h>
 
 #include <algorithm>
@@ -53,19 +54,22 @@ int EulerSim::learned_setup()
         (rc = falloc((void**)&d_stats_, sizeof(double) * 4)))
         return rc;
     int nc[2] = {gc.NY, gc.NX}, np[2] = {gp.NY, gp.NX};
-    cufftHandle a = 0, b = 0, c = 0;
+    cufftHandle a = 0, b = 0, c = 0, d = 0;
     if (cufftPlanMany(&a, 2, nc, nullptr, 1, 0, nullptr, 1, 0, CUFFT_R2C, 1) != CUFFT_SUCCESS ||
         cufftPlanMany(&b, 2, nc, nullptr, 1, 0, nullptr, 1, 0, CUFFT_C2R, 4) != CUFFT_SUCCESS ||
-        cufftPlanMany(&c, 2, np, nullptr, 1, 0, nullptr, 1, 0, CUFFT_R2C, 1) != CUFFT_SUCCESS) {
+        cufftPlanMany(&c, 2, np, nullptr, 1, 0, nullptr, 1, 0, CUFFT_R2C, 1) != CUFFT_SUCCESS ||
+        cufftPlanMany(&d, 2, np, nullptr, 1, 0, nullptr, 1, 0, CUFFT_C2R, 1) != CUFFT_SUCCESS) {
         err = "cuFFT plan creation for the learned psi failed";
         return kErrCuda;
     }
     cufftSetStream(a, stream);
     cufftSetStream(b, stream);
     cufftSetStream(c, stream);
+    cufftSetStream(d, stream);
     lc_r2c_ = (int)a;
     lc_c2r4_ = (int)b;
     l_r2c_ = (int)c;
+    l_c2r_ = (int)d;
     return kOk;
 }
 
@@ -79,7 +83,8 @@ void EulerSim::learned_release()
     if (lc_r2c_) cufftDestroy((cufftHandle)lc_r2c_);
     if (lc_c2r4_) cufftDestroy((cufftHandle)lc_c2r4_);
     if (l_r2c_) cufftDestroy((cufftHandle)l_r2c_);
-    lc_r2c_ = lc_c2r4_ = l_r2c_ = 0;
+    if (l_c2r_) cufftDestroy((cufftHandle)l_c2r_);
+    lc_r2c_ = lc_c2r4_ = l_r2c_ = l_c2r_ = 0;
     delete ups_owned_;
     ups_owned_ = nullptr;
     ups_ = nullptr;
@@ -193,10 +198,13 @@ int EulerSim::learned_collect(lrn::Upsampler& u)
     if (!initialised_) { err = "learned_collect before init"; return kErrState; }
     int rc;
     if ((rc = learned_setup()) || (rc = cheap_fields())) return rc;
-    // the cheap psi on the psi grid; target = exact psi level 0 (node values) - cheap psi
-    CMM_LAUNCH(1, launch_spec_psi_f(lc_spec_, gc, gp, s.freq_cut_psi, spec4f_, stream));
-    CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), l_planes_));
-    CMM_LAUNCH(1, lrn::launch_sub_strided(reinterpret_cast<const float*>(psim_[0]), 4, l_planes_, gp.N, l_delta_, stream));
+    // target: omega sampled through the map on the psi grid minus the spectral
+    // interpolation of the map-grid samples there
+    CMM_LAUNCH(1, launch_spec_pad(lc_spec_, gc, gp, l_dspec_, stream));
+    CMM_FFT(cufftExecC2R((cufftHandle)l_c2r_, reinterpret_cast<cufftComplex*>(l_dspec_), l_planes_ + gp.N));
+    CMM_LAUNCH(1, launch_sample_m(gc, gp, gf, mapm_, wfm_, l_planes_, nullptr, stream));
+    CMM_LAUNCH(1, lrn::launch_sub(l_planes_, l_planes_ + gp.N, gp.N, l_delta_, stream));
+    u.set_spectral_cut((int)std::floor(s.freq_cut_psi));
     if (u.append(lc_planes_, lc_omega_, l_delta_, gc.NY, gc.NX, stream)) {
         err = u.err;
         return kErrCuda;
@@ -205,7 +213,7 @@ int EulerSim::learned_collect(lrn::Upsampler& u)
     return kOk;
 }
 
-int EulerSim::learned_evaluate(lrn::Upsampler& u, double* out4)
+int EulerSim::learned_evaluate(lrn::Upsampler& u, double* out6)
 {
     if (!initialised_) { err = "learned_evaluate before init"; return kErrState; }
     int rc;
@@ -214,13 +222,22 @@ int EulerSim::learned_evaluate(lrn::Upsampler& u, double* out4)
     double st[4];
     CMM_LAUNCH(1, launch_spec_psi_f(lc_spec_, gc, gp, s.freq_cut_psi, spec4f_, stream));
     CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), l_planes_));
+    auto rel = [&](double* o) {
+        o[0] = st[1] > 0 ? st[0] / st[1] : 0.0;
+        o[1] = st[3] > 0 ? std::sqrt(st[2] / st[3]) : 0.0;
+    };
     if ((rc = diff_stats(l_planes_, 1, exact, 4, gp.N, st))) return rc;
-    out4[0] = st[1] > 0 ? st[0] / st[1] : 0.0;
-    out4[1] = st[3] > 0 ? std::sqrt(st[2] / st[3]) : 0.0;
+    rel(out6);
     if ((rc = learned_planes(u, l_planes_))) return rc;
     if ((rc = diff_stats(l_planes_, 1, exact, 4, gp.N, st))) return rc;
-    out4[2] = st[1] > 0 ? st[0] / st[1] : 0.0;
-    out4[3] = st[3] > 0 ? std::sqrt(st[2] / st[3]) : 0.0;
+    rel(out6 + 2);
+    // the ceiling: psi of omega sampled exactly on the psi grid (what a perfect network gives)
+    CMM_LAUNCH(1, launch_sample_m(gc, gp, gf, mapm_, wfm_, l_delta_, nullptr, stream));
+    CMM_FFT(cufftExecR2C((cufftHandle)l_r2c_, l_delta_, reinterpret_cast<cufftComplex*>(l_dspec_)));
+    CMM_LAUNCH(1, launch_spec_psi_f(l_dspec_, gp, gp, s.freq_cut_psi, spec4f_, stream));
+    CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), l_planes_));
+    if ((rc = diff_stats(l_planes_, 1, exact, 4, gp.N, st))) return rc;
+    rel(out6 + 4);
     return kOk;
 }
 

@@ -257,10 +257,12 @@ int cmm_ensemble_destroy(cmm_ensemble* e);
 
 /* ---------------------------------------------------------------- learned psi
  * A residual network of 3x3 periodic convolutions (BF16 tensor-core kernels, FP32
- * accumulation) that corrects the psi of omega sampled on the map grid towards the psi of
- * the full vorticity-grid evaluation.  Inputs on the map grid (h x w, w a multiple of 128):
- * the cheap psi and its derivatives psi_x, psi_y, psi_xy, and omega with omega_x, omega_y
- * (through the map's Jacobian); output on the psi grid (2h x 2w).  Trained on the GPU on pairs collected from running simulations
+ * accumulation) that predicts, on the psi grid (2h x 2w, the 2 x 2 sub-pixels of each map
+ * cell), the vorticity the map-grid samples miss (omega sampled through the map on the psi
+ * grid minus the spectral interpolation of the map-grid samples) from fields of the map
+ * grid (h x w, w a multiple of 128): the cheap psi (from omega sampled on the map grid) with
+ * psi_x, psi_y, psi_xy, and omega with omega_x, omega_y (through the map's Jacobian).  The
+ * learned psi is the method's spectral solve of the cheap vorticity plus the prediction.  Trained on the GPU on pairs collected from running simulations
  * (precision=mixed, psi grid = 2 x map grid).  The reference has no learned part; this is
  * new API.  With cmm_attach_upsampler (or psi_upsampler=<file> in the settings) a
  * simulation evaluates psi through the network except every exact_every-th step, where
@@ -292,15 +294,19 @@ int cmm_upsampler_dataset_size(const cmm_upsampler* u);
  * of the last min(iters, 16) steps and the device seconds of the call */
 int cmm_upsampler_train(cmm_upsampler* u, int iters, int batch, double lr, unsigned long long seed, double* loss,
                         double* seconds);
-/* mean squared error (scaled units) and its gradient for B host samples:
- * inputs[B][7][h][w] (psi, psi_x, psi_y, psi_xy, omega, omega_x, omega_y), targets[B][2h][2w] */
-int cmm_upsampler_loss_grad(cmm_upsampler* u, const float* inputs, const float* targets, int B, int h, int w,
+/* loss and its gradient for B host samples: inputs[B][7][h][w] (psi, psi_x, psi_y, psi_xy,
+ * omega, omega_x, omega_y), targets[B][2h][2w] (the sub-grid vorticity).  cut = 0: mean
+ * squared error of the scaled prediction; cut > 0: the training loss, the relative
+ * psi-space error sum w |FFT(pred - target)|^2 / sum w |FFT(target)|^2 with w = 1/|k|^4 on
+ * 0 < |k| <= cut (integer wavenumbers of the 2h x 2w grid) */
+int cmm_upsampler_loss_grad(cmm_upsampler* u, const float* inputs, const float* targets, int B, int h, int w, int cut,
                             double* loss);
-/* the correction on the psi grid (fine[2h][2w], physical units) for host inputs[7][h][w] */
+/* the predicted sub-grid vorticity on the psi grid (fine[2h][2w]) for host inputs[7][h][w] */
 int cmm_upsampler_infer(cmm_upsampler* u, const float* inputs, int h, int w, float* fine);
-/* relative differences from the context's exact psi level:
- * out4 = {cheap Linf, cheap L2, learned Linf, learned L2} */
-int cmm_upsampler_evaluate(cmm_upsampler* u, cmm_ctx* c, double* out4);
+/* relative differences from the context's exact psi level of the cheap psi, the learned psi
+ * and the psi of omega sampled exactly on the psi grid (the best a network can reach):
+ * out6 = {cheap Linf, cheap L2, learned Linf, learned L2, psi-grid Linf, psi-grid L2} */
+int cmm_upsampler_evaluate(cmm_upsampler* u, cmm_ctx* c, double* out6);
 int cmm_upsampler_save(const cmm_upsampler* u, const char* path);
 int cmm_upsampler_load(cmm_upsampler* u, const char* path);
 /* attach (NULL detaches) after cmm_init; the upsampler must outlive the attachment */

@@ -262,7 +262,7 @@ void og_conv3x3_t(const double* dy, int B, int H, int W, int cin, const double* 
                   const double* res, double* dx);
 void og_conv3x3_dw(const double* x, const double* dy, int B, int H, int W, int cin, int cout, double* dw, double* db);
 double og_upsampler_loss_grad(const double* params, int nb, int C, const double* s_in, double s_out,
-                              const float* inputs, const float* targets, int B, int h, int w, int emulate_bf16,
+                              const float* inputs, const float* targets, int B, int h, int w, int emulate_bf16, int cut,
                               double* grad);
 
 #ifdef __cplusplus

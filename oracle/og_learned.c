@@ -133,6 +133,77 @@ void og_conv3x3_dw(const double* x, const double* dy, int B, int H, int W, int c
     }
 }
 
+/* full 2D DFT of a real H x W field (unnormalised, exp(-i k x)) */
+static void dft2(const double* in, int H, int W, double* re, double* im)
+{
+    double* tr = (double*)malloc(sizeof(double) * H * W);
+    double* ti = (double*)malloc(sizeof(double) * H * W);
+    const double tp = 6.283185307179586;
+    for (int y = 0; y < H; ++y)
+        for (int kx = 0; kx < W; ++kx) {
+            double a = 0, b = 0;
+            for (int x = 0; x < W; ++x) {
+                const double ph = -tp * (double)((long)kx * x % W) / W;
+                a += in[(long)y * W + x] * cos(ph);
+                b += in[(long)y * W + x] * sin(ph);
+            }
+            tr[(long)y * W + kx] = a;
+            ti[(long)y * W + kx] = b;
+        }
+    for (int ky = 0; ky < H; ++ky)
+        for (int kx = 0; kx < W; ++kx) {
+            double a = 0, b = 0;
+            for (int y = 0; y < H; ++y) {
+                const double ph = -tp * (double)((long)ky * y % H) / H;
+                const double c = cos(ph), s = sin(ph);
+                a += tr[(long)y * W + kx] * c - ti[(long)y * W + kx] * s;
+                b += tr[(long)y * W + kx] * s + ti[(long)y * W + kx] * c;
+            }
+            re[(long)ky * W + kx] = a;
+            im[(long)ky * W + kx] = b;
+        }
+    free(tr);
+    free(ti);
+}
+
+/* real part of the unnormalised inverse DFT (exp(+i k x)) */
+static void idft2_real(const double* re, const double* im, int H, int W, double* out)
+{
+    double* tr = (double*)malloc(sizeof(double) * H * W);
+    double* ti = (double*)malloc(sizeof(double) * H * W);
+    const double tp = 6.283185307179586;
+    for (int y = 0; y < H; ++y)
+        for (int kx = 0; kx < W; ++kx) {
+            double a = 0, b = 0;
+            for (int ky = 0; ky < H; ++ky) {
+                const double ph = tp * (double)((long)ky * y % H) / H;
+                const double c = cos(ph), s = sin(ph);
+                a += re[(long)ky * W + kx] * c - im[(long)ky * W + kx] * s;
+                b += re[(long)ky * W + kx] * s + im[(long)ky * W + kx] * c;
+            }
+            tr[(long)y * W + kx] = a;
+            ti[(long)y * W + kx] = b;
+        }
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            double a = 0;
+            for (int kx = 0; kx < W; ++kx) {
+                const double ph = tp * (double)((long)kx * x % W) / W;
+                a += tr[(long)y * W + kx] * cos(ph) - ti[(long)y * W + kx] * sin(ph);
+            }
+            out[(long)y * W + x] = a;
+        }
+    free(tr);
+    free(ti);
+}
+
+static double spec_weight(int ky, int kx, int H, int W, int cut)
+{
+    const int a = 2 * kx >= W ? kx - W : kx, b = 2 * ky >= H ? ky - H : ky;
+    const double k2 = (double)a * a + (double)b * b;
+    return (k2 > 0 && k2 <= (double)cut * cut) ? 1.0 / (k2 * k2) : 0.0;
+}
+
 static void round_all(double* v, long n, int emu)
 {
     if (!emu) return;
@@ -140,7 +211,8 @@ static void round_all(double* v, long n, int emu)
 }
 
 double og_upsampler_loss_grad(const double* params, int nb, int C, const double* s_in, double s_out,
-                              const float* inputs, const float* targets, int B, int h, int w, int emu, double* grad)
+                              const float* inputs, const float* targets, int B, int h, int w, int emu, int cut,
+                              double* grad)
 {
     const int n_layers = 2 * nb + 2;
     long woff[130], boff[130];
@@ -208,6 +280,65 @@ double og_upsampler_loss_grad(const double* params, int nb, int C, const double*
             }
         }
     loss *= inv_n;
+    if (cut > 0) {
+        /* psi-space loss: the mean over samples of num_b / den_b over the full spectra of
+         * r = pred - target and of the target on the 2h x 2w grid, w = 1/|k|^4 on
+         * 0 < |k| <= cut; gradient 2 IDFT(w R_b) / (B den_b) */
+        const int H2 = 2 * h, W2 = 2 * w;
+        const long m2 = (long)H2 * W2;
+        double *r = (double*)malloc(sizeof(double) * m2), *t = (double*)malloc(sizeof(double) * m2);
+        double *rr = (double*)malloc(sizeof(double) * m2), *ri = (double*)malloc(sizeof(double) * m2);
+        double *tr = (double*)malloc(sizeof(double) * m2), *ti = (double*)malloc(sizeof(double) * m2);
+        double *g = (double*)malloc(sizeof(double) * m2);
+        double* num = (double*)calloc((size_t)B, sizeof(double));
+        double* den = (double*)calloc((size_t)B, sizeof(double));
+        double** spec = (double**)malloc(sizeof(double*) * 2 * B);
+        for (int b = 0; b < B; ++b) {
+            for (long p = 0; p < hw; ++p) {
+                const long y = p / w, x = p % w;
+                for (int k = 0; k < 4; ++k) {
+                    const long q = (2 * y + k / 2) * W2 + 2 * x + k % 2;
+                    const float tv = targets[(long)b * 4 * hw + q];
+                    const double tt = emu ? (double)(tv * inv_out_f) : (double)tv / s_out;
+                    const double pv = out[((long)b * hw + p) * 16 + k];
+                    r[q] = emu ? (double)((float)pv - (float)tt) : pv - tt;
+                    t[q] = tt;
+                }
+            }
+            dft2(r, H2, W2, rr, ri);
+            dft2(t, H2, W2, tr, ti);
+            spec[2 * b] = (double*)malloc(sizeof(double) * m2);
+            spec[2 * b + 1] = (double*)malloc(sizeof(double) * m2);
+            for (int ky = 0; ky < H2; ++ky)
+                for (int kx = 0; kx < W2; ++kx) {
+                    const long q = (long)ky * W2 + kx;
+                    const double wk = spec_weight(ky, kx, H2, W2, cut);
+                    num[b] += wk * (rr[q] * rr[q] + ri[q] * ri[q]);
+                    den[b] += wk * (tr[q] * tr[q] + ti[q] * ti[q]);
+                    spec[2 * b][q] = wk * rr[q];
+                    spec[2 * b + 1][q] = wk * ri[q];
+                }
+        }
+        for (int b = 0; b < B; ++b) {
+            idft2_real(spec[2 * b], spec[2 * b + 1], H2, W2, g);
+            for (long p = 0; p < hw; ++p) {
+                const long y = p / w, x = p % w;
+                for (int k = 0; k < 4; ++k) {
+                    const double v = den[b] > 0 ? g[(2 * y + k / 2) * W2 + 2 * x + k % 2] * 2.0 / (B * den[b]) : 0.0;
+                    dout[((long)b * hw + p) * 16 + k] = emu ? og_bf16_round(v) : v;
+                }
+            }
+            free(spec[2 * b]);
+            free(spec[2 * b + 1]);
+        }
+        free(spec);
+        free(r); free(t); free(rr); free(ri); free(tr); free(ti); free(g);
+        loss = 0;
+        for (int b = 0; b < B; ++b) loss += den[b] > 0 ? num[b] / den[b] : 0.0;
+        loss /= B;
+        free(num);
+        free(den);
+    }
     /* backward */
     double* da = (double*)malloc(sizeof(double) * n * C);
     double* da2 = (double*)malloc(sizeof(double) * n * C);

@@ -566,7 +566,7 @@ def _learned_lib():
         L.og_conv3x3_t.argtypes = [dp, C.c_int, C.c_int, C.c_int, C.c_int, dp, C.c_int, dp, dp, dp]
         L.og_conv3x3_dw.argtypes = [dp, dp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, dp, dp]
         L.og_upsampler_loss_grad.argtypes = [dp, C.c_int, C.c_int, dp, C.c_double, fp, fp, C.c_int, C.c_int, C.c_int,
-                                             C.c_int, dp]
+                                             C.c_int, C.c_int, dp]
         L.og_upsampler_loss_grad.restype = C.c_double
         L._learned = True
     return L
@@ -628,8 +628,9 @@ def conv3x3_weight_grad(x, dy):
     return dw, db
 
 
-def upsampler_loss_grad(params, blocks, channels, s_in, s_out, inputs, targets, emulate_bf16=True):
-    """Loss and gradient of the upsampler: inputs[B, 7, h, w], targets[B, 2h, 2w] (float32)."""
+def upsampler_loss_grad(params, blocks, channels, s_in, s_out, inputs, targets, emulate_bf16=True, cut=0):
+    """Loss and gradient of the upsampler: inputs[B, 7, h, w], targets[B, 2h, 2w] (float32);
+    cut > 0: the psi-space spectral loss (w = 1/|k|^4 on 0 < |k| <= cut)."""
     L = _learned_lib()
     params = np.ascontiguousarray(params, dtype=np.float64)
     s_in = np.ascontiguousarray(s_in, dtype=np.float64)
@@ -640,7 +641,7 @@ def upsampler_loss_grad(params, blocks, channels, s_in, s_out, inputs, targets, 
     fp = C.POINTER(C.c_float)
     loss = L.og_upsampler_loss_grad(_dp(params), blocks, channels, _dp(s_in), float(s_out),
                                     inputs.ctypes.data_as(fp), targets.ctypes.data_as(fp), B, h, w,
-                                    1 if emulate_bf16 else 0, _dp(grad))
+                                    1 if emulate_bf16 else 0, int(cut), _dp(grad))
     return loss, grad
 
 

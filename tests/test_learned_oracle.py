@@ -1,6 +1,7 @@
-"""The CPU oracle of the learned psi upsampler (no GPU): its FP64 gradients against
-central finite differences, its BF16 rounding, and its convolution against a direct
-numpy restatement of the periodic 3x3 stencil."""
+"""The CPU oracle of the learned psi upsampler (no GPU): its FP64 gradients (mean squared
+error and psi-space spectral loss) against central finite differences, its BF16 rounding,
+its convolution against a direct numpy restatement of the periodic 3x3 stencil, and its
+spectral loss against numpy's FFT."""
 import os
 import sys
 
@@ -44,21 +45,56 @@ def test_conv_matches_numpy_stencil():
     assert np.allclose(db, g.sum(axis=(0, 1, 2)))
 
 
-def test_network_gradient_matches_finite_differences():
-    rng = np.random.default_rng(1)
+import pytest  # noqa: E402
+
+
+@pytest.mark.parametrize("cut", [0, 3])
+def test_network_gradient_matches_finite_differences(cut):
+    rng = np.random.default_rng(1 + cut)
     nb, C = 1, 32
     n = O.upsampler_param_count(nb, C)
     p = rng.normal(0, 0.1, n)
     inputs = rng.normal(0, 1, (1, 7, 4, 8)).astype(np.float32)
     targets = rng.normal(0, 1, (1, 8, 16)).astype(np.float32)
     s_in = np.array([1.0, 2.0, 0.5, 1.0, 3.0, 5.0, 4.0])
-    loss, g = O.upsampler_loss_grad(p, nb, C, s_in, 0.5, inputs, targets, emulate_bf16=False)
+    loss, g = O.upsampler_loss_grad(p, nb, C, s_in, 0.5, inputs, targets, emulate_bf16=False, cut=cut)
     for i in rng.choice(n, 16, replace=False):
         e = 1e-6
         pp, pm = p.copy(), p.copy()
         pp[i] += e
         pm[i] -= e
-        lp, _ = O.upsampler_loss_grad(pp, nb, C, s_in, 0.5, inputs, targets, emulate_bf16=False)
-        lm, _ = O.upsampler_loss_grad(pm, nb, C, s_in, 0.5, inputs, targets, emulate_bf16=False)
+        lp, _ = O.upsampler_loss_grad(pp, nb, C, s_in, 0.5, inputs, targets, emulate_bf16=False, cut=cut)
+        lm, _ = O.upsampler_loss_grad(pm, nb, C, s_in, 0.5, inputs, targets, emulate_bf16=False, cut=cut)
         fd = (lp - lm) / (2 * e)
-        assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(fd)), (i, fd, g[i])
+        assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(fd)) + 1e-9 * np.max(np.abs(g)), (i, fd, g[i])
+
+
+def test_spectral_loss_matches_numpy_fft():
+    """The oracle's psi-space loss restated with numpy.fft on the network's shuffled output."""
+    rng = np.random.default_rng(4)
+    nb, C, cut = 0, 32, 4
+    n = O.upsampler_param_count(nb, C)
+    p = rng.normal(0, 0.1, n)
+    inputs = rng.normal(0, 1, (2, 7, 4, 8)).astype(np.float32)
+    targets = rng.normal(0, 1, (2, 8, 16)).astype(np.float32)
+    s_in = np.ones(7)
+    loss, _ = O.upsampler_loss_grad(p, nb, C, s_in, 1.0, inputs, targets, emulate_bf16=False, cut=cut)
+    # forward by the oracle's convolutions: head then tail (no blocks)
+    off = 9 * 16 * C
+    wh, bh = p[:off].reshape(9, 16, C), p[off:off + C]
+    off2 = off + C + 9 * C * 16
+    wt, bt = p[off + C:off2].reshape(9, C, 16), p[off2:off2 + 16]
+    x0 = np.zeros((2, 4, 8, 16))
+    x0[..., :7] = inputs.transpose(0, 2, 3, 1)
+    out = O.conv3x3(O.conv3x3(x0, wh, bh), wt, bt)
+    pred = np.zeros((2, 8, 16))
+    for k in range(4):
+        pred[:, k // 2::2, k % 2::2] = out[..., k]
+    ky = np.fft.fftfreq(8, 1.0 / 8)[:, None]
+    kx = np.fft.fftfreq(16, 1.0 / 16)[None, :]
+    k2 = kx ** 2 + ky ** 2
+    wk = np.where((k2 > 0) & (k2 <= cut * cut), 1.0 / np.where(k2 > 0, k2, 1) ** 2, 0.0)
+    num = np.sum(wk * np.abs(np.fft.fft2(pred - targets)) ** 2, axis=(1, 2))
+    den = np.sum(wk * np.abs(np.fft.fft2(targets.astype(np.float64))) ** 2, axis=(1, 2))
+    ref = np.mean(num / den)
+    assert abs(loss - ref) <= 1e-10 * ref

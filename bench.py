@@ -270,14 +270,17 @@ def measure_form(m, torch, pf, ic, precision, args, world, clocks=None, profile=
     return out
 
 
-def full_run(m, torch, pf, ic, precision, every=64, final_time=10.0):
+def full_run(m, torch, pf, ic, precision, every=64, final_time=10.0, ups=None, exact_every=8, tol=1e-4):
     """Run the workload to its final time (T = 10, 2560 steps with every remap)
-    and record (t, enstrophy, energy, maps) every `every` steps (0.25 time units)."""
+    and record (t, enstrophy, energy, maps) every `every` steps (0.25 time units);
+    with `ups` the learned psi form (exact evaluation every exact_every steps)."""
     stream = torch.cuda.Stream()
     sim = m.Simulation(["param_file=" + pf, "precision=" + precision, "final_time=%g" % final_time],
                        stream=stream.cuda_stream)
     sim.set_initial_discrete(ic)
     sim.init()
+    if ups is not None:
+        sim.attach_upsampler(ups, every=exact_every, tol=tol)
     rec = [(sim.scalar("time"), sim.scalar("enstrophy"), sim.scalar("energy"), 0)]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -300,8 +303,12 @@ def full_run(m, torch, pf, ic, precision, every=64, final_time=10.0):
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     maps = int(sim.scalar("map_counter"))
+    out = {"steps": n, "wall_s": wall, "steps_per_s": n / wall, "maps": maps, "series": rec}
+    if ups is not None:
+        out.update({k: sim.scalar(k) for k in ("learned_steps", "cheap_steps", "exact_steps", "learned_checks",
+                                               "learned_cheaper", "learned_failures", "learned_max_err")})
     sim.close()
-    return {"steps": n, "wall_s": wall, "steps_per_s": n / wall, "maps": maps, "series": rec}
+    return out
 
 
 VLASOV = dict(grid_coarse=256, grid_fine=1024, grid_vort=1024, grid_psi=1024, steps_per_sec=32, final_time=40.0,
@@ -550,6 +557,154 @@ def run_ensemble(args):
     shutil.rmtree(work, ignore_errors=True)
 
 
+LEARNED = dict(blocks=6, channels=32, train_seeds=8, collect_every=32, iters=1200, batch=8, lr=1e-3,
+               exact_every=8, tol=1e-4)
+
+
+def conv_flops_per_pixel(blocks, C=32):
+    """Tensor-core FLOPs per map-grid pixel of one training step (padded channel counts as
+    executed): forward of every layer, input gradient of every layer but the head, weight
+    gradient of every layer (M padded to 128 rows: 3 dx x cin)."""
+    layers = [(16, C)] + [(C, C)] * (2 * blocks) + [(C, 16)]
+    fwd = sum(2 * 9 * ci * co for ci, co in layers)
+    dx = sum(2 * 9 * ci * co for ci, co in layers[1:])
+    dw = sum(2 * 3 * 128 * co for ci, co in layers)
+    return fwd, fwd + dx + dw
+
+
+def run_learned(args):
+    """The learned psi on the metric workload: training pairs from seeded runs (seeds 1..S,
+    every 32 steps to T = 10), on-GPU training of the 6-block network, then the held-out
+    seed 0 to T = 10 three ways (exact mixed form, learned form with exact evaluation every
+    8 steps at psi tolerance 1e-4, plain FP64) plus the psi errors of the cheap, learned and
+    psi-grid evaluations along an exact run."""
+    import __graft_entry__ as ge
+    ge.build()
+    m = ge.package()
+    import torch
+    L = LEARNED
+    work = tempfile.mkdtemp(prefix="cmm_learned_")
+    cli, _ = sim_args(work, "mixed", particles=1000)
+    cli = [c for c in cli if not c.startswith("particles_advected_num")] + ["particles_advected_num=0"]
+    pf = os.path.join(work, "params.txt")
+    write_param_file(pf, cli, [])
+    stream = torch.cuda.Stream()
+    u = m.Upsampler(blocks=L["blocks"], channels=L["channels"], seed=1, stream=stream.cuda_stream)
+    t0 = time.perf_counter()
+    for seed in range(1, 1 + args.learned_seeds):
+        sim = m.Simulation(["param_file=" + pf, "final_time=%g" % args.t10_final], stream=stream.cuda_stream)
+        sim.set_initial_discrete(initial_vorticity(WORKLOAD["grid_fine"], seed, WORKLOAD["k0"]))
+        sim.init()
+        k = 0
+        while sim.step(1) != 1:
+            k += 1
+            if k % L["collect_every"] == 0:
+                u.collect(sim)
+        sim.close()
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    rounds = max(1, args.learned_iters // 100)
+    losses, train_s = [], 0.0
+    for r in range(rounds):
+        loss, sec = u.train(100, batch=L["batch"], lr=L["lr"] if r < 0.8 * rounds else L["lr"] / 5, seed=r)
+        losses.append(loss)
+        train_s += sec
+    fwd_pp, train_pp = conv_flops_per_pixel(L["blocks"], L["channels"])
+    px = WORKLOAD["grid_coarse"] ** 2
+    ic = initial_vorticity(WORKLOAD["grid_fine"], WORKLOAD["seed"], WORKLOAD["k0"])
+    exact = full_run(m, torch, pf, ic, "mixed", final_time=args.t10_final)
+    learned = full_run(m, torch, pf, ic, "mixed", final_time=args.t10_final, ups=u, exact_every=L["exact_every"],
+                       tol=L["tol"])
+    plain = full_run(m, torch, pf, ic, "fp64", final_time=args.t10_final)
+    # psi errors along an exact run of the held-out seed
+    sim = m.Simulation(["param_file=" + pf, "final_time=%g" % args.t10_final], stream=stream.cuda_stream)
+    sim.set_initial_discrete(ic)
+    sim.init()
+    errs, k = [], 0
+    while sim.step(1) != 1:
+        k += 1
+        if k % 256 == 0:
+            e = u.evaluate(sim)
+            errs.append({"t": round(sim.scalar("time"), 3), **{q: float("%.3e" % v) for q, v in e.items()}})
+    sim.close()
+
+    def zerr(a, b):
+        return max(abs(x[1] - y[1]) / abs(y[1]) for x, y in zip(a["series"], b["series"]))
+
+    keep = ("steps", "wall_s", "steps_per_s", "maps")
+    out = {"validation": "learned psi on the metric workload (held-out seed 0), against the exact mixed form and plain FP64",
+           "workload": "euler2d-turbulence coarse512 fine2048 psi1024 dt1/256 T=%g, no tracers" % args.t10_final,
+           "network": {"blocks": L["blocks"], "channels": L["channels"], "params": u.num_params(),
+                       "inputs": "psi, psi_x, psi_y, psi_xy (cheap), omega, omega_x, omega_y on 512^2",
+                       "output": "sub-grid vorticity on the 1024^2 psi grid"},
+           "training": {"pairs": u.dataset_size(), "seeds": args.learned_seeds, "collect_every_steps": L["collect_every"],
+                        "pair_generation_s": gen_s, "iterations": rounds * 100, "batch": L["batch"],
+                        "device_s": train_s, "samples_per_s": rounds * 100 * L["batch"] / train_s,
+                        "conv_tflops": rounds * 100 * L["batch"] * px * train_pp / train_s / 1e12,
+                        "loss_first_last": [losses[0], losses[-1]], "loss": "mean relative psi-space error"},
+           "exact_mixed": {k: exact[k] for k in keep},
+           "learned": {k: learned[k] for k in keep + ("learned_steps", "cheap_steps", "exact_steps", "learned_checks",
+                                                      "learned_cheaper", "learned_failures", "learned_max_err")},
+           "plain_fp64": {k: plain[k] for k in keep},
+           "learned_vs_plain_fp64": {"speedup": learned["steps_per_s"] / plain["steps_per_s"],
+                                     "max_enstrophy_rel_err": zerr(learned, plain)},
+           "exact_mixed_vs_plain_fp64": {"speedup": exact["steps_per_s"] / plain["steps_per_s"],
+                                         "max_enstrophy_rel_err": zerr(exact, plain)},
+           "learned_vs_exact_mixed_max_enstrophy_rel_err": zerr(learned, exact),
+           "inference_conv_gflop_per_step": px * fwd_pp / 1e9,
+           "psi_errors_along_exact_run": errs}
+    print(json.dumps(out))
+    shutil.rmtree(work, ignore_errors=True)
+
+
+def run_learned_profile(args):
+    """Small runs of the learned psi's kernels for ncu captures.  infer: the metric workload
+    (no tracers) with a 6-block network attached and only the first step exact, 3 + 4 steps;
+    train: pairs every 8 steps of a 128^2 map / 512^2 vorticity run to T = 2, then 4 Adam
+    steps of batch 32 (weights of either are untrained: the cost does not depend on them)."""
+    import __graft_entry__ as ge
+    ge.build()
+    m = ge.package()
+    import torch
+    work = tempfile.mkdtemp(prefix="cmm_lprof_")
+    if args.learned_profile == "infer":
+        cli, _ = sim_args(work, "mixed", particles=1000)
+        cli = [c for c in cli if not c.startswith("particles_advected_num")] + ["particles_advected_num=0",
+                                                                                 "final_time=1"]
+        sim = m.Simulation(cli)
+        sim.set_initial_discrete(initial_vorticity(WORKLOAD["grid_fine"], 0, WORKLOAD["k0"]))
+        sim.init()
+        u = m.Upsampler(blocks=LEARNED["blocks"], seed=2)
+        sim.attach_upsampler(u, every=1000000, tol=1e9)
+        sim.step(3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.step(4)
+        torch.cuda.synchronize()
+        print(json.dumps({"learned_steps_per_s": 4 / (time.perf_counter() - t0)}))
+    else:
+        n = 128
+        cli = ["workspace=%s/" % work, "sim_name=prof", "grid_coarse=%d" % n, "grid_fine=%d" % (4 * n),
+               "grid_vort=%d" % (4 * n), "grid_psi=%d" % (2 * n), "set_dt_by_steps=1", "steps_per_sec=%d" % (n // 2),
+               "final_time=2", "initial_condition=4_nodes", "initial_discrete=1", "initial_discrete_grid=%d" % (4 * n),
+               "time_integration=RK3", "map_update_order=4th", "map_epsilon=0.001", "incomp_threshold=1e-4",
+               "molly_stencil=0", "freq_cut_psi=%d" % (n // 4), "mem_RAM_CPU_remaps=100000",
+               "save_computational_num=0", "save_sample_num=0", "save_zoom_num=0", "particles_advected_num=0",
+               "save_map_stack=0", "verbose=0", "precision=mixed"]
+        sim = m.Simulation(cli)
+        sim.set_initial_discrete(initial_vorticity(4 * n, 1, 8.0))
+        sim.init()
+        u = m.Upsampler(blocks=LEARNED["blocks"], seed=1)
+        k = 0
+        while sim.step(1) != 1:
+            k += 1
+            if k % 8 == 0:
+                u.collect(sim)
+        loss, sec = u.train(4, batch=32, lr=1e-3, seed=0)
+        print(json.dumps({"pairs": u.dataset_size(), "loss": loss, "train_s": sec}))
+    shutil.rmtree(work, ignore_errors=True)
+
+
 def run_ours(args):
     import __graft_entry__ as ge
     ge.build()
@@ -698,11 +853,19 @@ def main():
     ap.add_argument("--vlasov-final", type=float, default=VLASOV["final_time"])
     ap.add_argument("--ensemble", action="store_true", help="run the 64-member ensemble batched and one by one")
     ap.add_argument("--ensemble-batched-only", action="store_true", help="with --ensemble: only the batched run")
+    ap.add_argument("--learned", action="store_true", help="train the psi upsampler and run the learned form")
+    ap.add_argument("--learned-seeds", type=int, default=LEARNED["train_seeds"])
+    ap.add_argument("--learned-iters", type=int, default=LEARNED["iters"])
+    ap.add_argument("--learned-profile", choices=["infer", "train"], help="small learned-psi runs for ncu captures")
     args = ap.parse_args()
     if args.fp64_peak:
         measure_fp64_peak()
     elif args.ensemble:
         run_ensemble(args)
+    elif args.learned:
+        run_learned(args)
+    elif args.learned_profile:
+        run_learned_profile(args)
     elif args.vlasov:
         run_vlasov(args)
     elif args.impl == "reference":

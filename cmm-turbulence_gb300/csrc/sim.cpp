@@ -2003,6 +2003,8 @@ int EulerSim::get_scalar(const std::string& n, double* out)
     if (n == "map_gap") { *out = (loop_ctr_ - 1) - old_ctr_; return kOk; }
     if (n == "loop_ctr") { *out = loop_ctr_; return kOk; }
     if (n == "learned_steps") { *out = (double)learned_steps_; return kOk; }
+    if (n == "cheap_steps") { *out = (double)cheap_steps_; return kOk; }
+    if (n == "learned_cheaper") { *out = (double)learned_cheaper_; return kOk; }
     if (n == "exact_steps") { *out = (double)exact_steps_; return kOk; }
     if (n == "learned_checks") { *out = (double)learned_checks_; return kOk; }
     if (n == "learned_failures") { *out = (double)learned_fails_; return kOk; }

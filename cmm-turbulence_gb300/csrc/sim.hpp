@@ -54,10 +54,12 @@ public:
     int ens_end();
 
     // learned psi (precision=mixed, Euler; csrc/sim_learned.cpp).  With an upsampler attached,
-    // a step evaluates psi from the cheap vorticity plus the network's sub-grid vorticity on the psi grid (predicted from omega and
-    // its gradient on the map grid), except every `every`-th step, which runs the vorticity-grid evaluation and compares the
-    // learned psi with it: a relative L-infinity difference above `tol` makes the next
-    // every - 1 steps exact as well.  null detaches.  learned_collect appends the current
+    // every `every`-th step runs the exact vorticity-grid evaluation and judges the learned
+    // psi (cheap vorticity plus the network's sub-grid vorticity on the psi grid, predicted
+    // from omega and its gradient on the map grid) and the cheap psi (omega sampled on the
+    // map grid) against it; the next every - 1 steps use the network if its relative
+    // L-infinity difference is within `tol` and below the cheap one's, else the cheap psi if
+    // that is within `tol`, else the exact evaluation.  null detaches.  learned_collect appends the current
     // state's training pair (map-grid fields, the sub-grid vorticity on the psi grid); learned_evaluate gives the
     // relative L-infinity and L2 differences of the cheap psi, the learned psi and the psi of
     // omega sampled exactly on the psi grid from the current exact psi level
@@ -179,13 +181,15 @@ private:
     int cheap_fields();
     int learned_planes(lrn::Upsampler& u, float* out);
     int learned_stream();
+    int cheap_planes(float* out);
     int diff_stats(const float* a, long long sa, const float* e, long long se, long long n, double* host4);
     lrn::Upsampler* ups_ = nullptr;
     lrn::Upsampler* ups_owned_ = nullptr;
     int learned_every_ = 8;
     double learned_tol_ = 1e-4;
-    int learned_fallback_ = 0;
-    long long learned_steps_ = 0, exact_steps_ = 0, learned_checks_ = 0, learned_fails_ = 0;
+    int learned_level_ = 2;            // 0 network, 1 cheap psi, 2 exact until the next judged step
+    long long learned_steps_ = 0, cheap_steps_ = 0, exact_steps_ = 0, learned_checks_ = 0, learned_fails_ = 0,
+              learned_cheaper_ = 0;
     double learned_last_err_ = 0, learned_max_err_ = 0;
     float *lc_omega_ = nullptr, *lc_planes_ = nullptr, *l_delta_ = nullptr, *l_planes_ = nullptr;
     float2 *lc_spec_ = nullptr, *lc_spec4_ = nullptr, *l_dspec_ = nullptr;

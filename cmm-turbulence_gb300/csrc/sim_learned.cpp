@@ -122,7 +122,7 @@ int EulerSim::attach_upsampler(lrn::Upsampler* u, int every, double tol)
     ups_ = u;
     learned_every_ = every;
     learned_tol_ = tol;
-    learned_fallback_ = 0;
+    learned_level_ = 2;
     return kOk;
 }
 
@@ -161,34 +161,54 @@ int EulerSim::diff_stats(const float* a, long long sa, const float* e, long long
     return kOk;
 }
 
+int EulerSim::cheap_planes(float* out)
+{
+    int rc;
+    if ((rc = cheap_fields())) return rc;
+    CMM_LAUNCH(1, launch_spec_psi_f(lc_spec_, gc, gp, s.freq_cut_psi, spec4f_, stream));
+    CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), out));
+    return kOk;
+}
+
 int EulerSim::learned_stream()
 {
-    const bool exact = learned_fallback_ > 0 || loop_ctr_ % learned_every_ == 0;
-    if (!exact) {
-        ++learned_steps_;
-        return learned_planes(*ups_, realf_);
+    // between judged steps: the level the last judgement chose
+    if (loop_ctr_ % learned_every_ != 0) {
+        if (learned_level_ == 0) {
+            ++learned_steps_;
+            return learned_planes(*ups_, realf_);
+        }
+        if (learned_level_ == 1) {
+            ++cheap_steps_;
+            return cheap_planes(realf_);
+        }
     }
     ++exact_steps_;
     CMM_LAUNCH(1, launch_sample_m(gc, gv, gf, mapm_, wfm_, realf_, nullptr, stream));
     CMM_FFT(cufftExecR2C(r2c_v_, realf_, reinterpret_cast<cufftComplex*>(specf_)));
     CMM_LAUNCH(1, launch_spec_psi_f(specf_, gv, gp, s.freq_cut_psi, spec4f_, stream));
     CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), realf_));
-    if (learned_fallback_ > 0) {
-        --learned_fallback_;
-        return kOk;
-    }
-    // the exact evaluation judges the learned one on the same state
+    if (loop_ctr_ % learned_every_ != 0) return kOk;
+    // the exact evaluation judges the learned and the cheap psi on the same state and picks
+    // the level of the next every - 1 steps: the network where it meets the tolerance and
+    // beats the cheap psi, else the cheap psi where that meets it, else the exact one
     int rc;
-    if ((rc = learned_planes(*ups_, l_planes_))) return rc;
     double st[4];
-    if ((rc = diff_stats(l_planes_, 1, realf_, 1, gp.N, st))) return rc;
-    const double e = st[1] > 0 ? st[0] / st[1] : 0.0;
+    if ((rc = learned_planes(*ups_, l_planes_)) || (rc = diff_stats(l_planes_, 1, realf_, 1, gp.N, st))) return rc;
+    const double el = st[1] > 0 ? st[0] / st[1] : 0.0;
+    if ((rc = cheap_planes(l_planes_)) || (rc = diff_stats(l_planes_, 1, realf_, 1, gp.N, st))) return rc;
+    const double ec = st[1] > 0 ? st[0] / st[1] : 0.0;
     ++learned_checks_;
-    learned_last_err_ = e;
-    learned_max_err_ = std::max(learned_max_err_, e);
-    if (!(e <= learned_tol_)) {
+    learned_last_err_ = el;
+    learned_max_err_ = std::max(learned_max_err_, el);
+    if (el <= learned_tol_ && el <= ec) {
+        learned_level_ = 0;
+    } else if (ec <= learned_tol_) {
+        learned_level_ = 1;
+        ++learned_cheaper_;
+    } else {
+        learned_level_ = 2;
         ++learned_fails_;
-        learned_fallback_ = learned_every_ - 1;
     }
     return kOk;
 }

@@ -264,12 +264,14 @@ int cmm_ensemble_destroy(cmm_ensemble* e);
  * psi_x, psi_y, psi_xy, and omega with omega_x, omega_y (through the map's Jacobian).  The
  * learned psi is the method's spectral solve of the cheap vorticity plus the prediction.  Trained on the GPU on pairs collected from running simulations
  * (precision=mixed, psi grid = 2 x map grid).  The reference has no learned part; this is
- * new API.  With cmm_attach_upsampler (or psi_upsampler=<file> in the settings) a
- * simulation evaluates psi through the network except every exact_every-th step, where
- * the exact evaluation runs and judges the learned one: a relative L-infinity psi
- * difference above tol makes the following exact_every - 1 steps exact too.  Scalars of
- * the context: learned_steps, exact_steps, learned_checks, learned_failures,
- * learned_last_err, learned_max_err. */
+ * new API.  With cmm_attach_upsampler (or psi_upsampler=<file> in the settings) every
+ * exact_every-th step of a simulation runs the exact evaluation and judges the learned psi
+ * and the cheap psi against it (relative L-infinity difference); the following
+ * exact_every - 1 steps use the network if it is within tol and closer than the cheap psi,
+ * else the cheap psi if that is within tol, else the exact evaluation.  Scalars of the
+ * context: learned_steps, cheap_steps, exact_steps, learned_checks, learned_cheaper (checks
+ * where the cheap psi was chosen), learned_failures (checks where neither met tol),
+ * learned_last_err, learned_max_err (of the learned psi at the checks). */
 typedef struct cmm_upsampler cmm_upsampler;
 /* blocks residual blocks of two convolutions of `channels` (= 32) channels; weights drawn
  * from mt19937_64(seed) */

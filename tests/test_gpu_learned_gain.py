@@ -9,9 +9,10 @@ L2 difference from the exact psi of the cheap psi (omega sampled on the map grid
 without the network) and of the learned psi (the same plus the network's sub-grid
 vorticity).  The learned psi must be closer on average (ratio < 0.95) and at most instants.
 
-The learned form inside a run: every 8th step is exact and judges the learned psi; with a
-tolerance nothing meets, every check fails and the run falls back to exact steps; with a
-tolerance everything meets, only the judged steps are exact.
+The learned form inside a run: every 8th step is exact and judges the learned and the cheap
+psi; with a tolerance nothing meets, every check fails and the run falls back to exact
+steps; with a tolerance everything meets, only the judged steps are exact and the others
+use whichever of the network and the cheap psi was closer at the last check.
 """
 import numpy as np
 import pytest
@@ -91,17 +92,21 @@ def test_learned_form_judge_and_fallback(trained):
         sim.init()
         sim.attach_upsampler(u, every=8, tol=tol)
         sim.run()
-        runs[name] = {k: sim.scalar(k) for k in ("learned_steps", "exact_steps", "learned_checks",
-                                                "learned_failures", "learned_max_err", "enstrophy", "energy")}
+        runs[name] = {k: sim.scalar(k) for k in ("learned_steps", "cheap_steps", "exact_steps", "learned_checks",
+                                                "learned_cheaper", "learned_failures", "learned_max_err",
+                                                "enstrophy", "energy")}
         sim.close()
     s, l_ = runs["strict"], runs["loose"]
     steps = int(1.0 * N / 2)
     # strict: every judged step fails, so everything after a check is exact
-    assert s["learned_steps"] == 0 and s["exact_steps"] == steps
+    assert s["learned_steps"] == s["cheap_steps"] == 0 and s["exact_steps"] == steps
     assert s["learned_checks"] == s["learned_failures"] == steps // 8
-    # loose: exactly every 8th step is exact (and judged), the others learned
+    # loose: exactly every 8th step is exact (and judged), the others learned or cheap as judged,
+    # and the trained network is chosen at some checks
     assert l_["exact_steps"] == l_["learned_checks"] == steps // 8 and l_["learned_failures"] == 0
-    assert l_["learned_steps"] == steps - steps // 8
+    assert l_["learned_steps"] + l_["cheap_steps"] == steps - steps // 8
+    assert l_["cheap_steps"] == 7 * l_["learned_cheaper"]
+    assert l_["learned_steps"] > 0
     assert 0 < l_["learned_max_err"] < 1e-2
     # a run of learned steps conserves like the exact one
     for q in ("enstrophy", "energy"):

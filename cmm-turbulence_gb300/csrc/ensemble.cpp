@@ -138,7 +138,7 @@ int EnsembleSim::init()
             switch (kind) {
                 case kEnsAdvect: items = s.gc.N << lpn_log2_; break;
                 case kEnsIncomp: items = s.gc.N * (s.gf.NX / s.gc.NX); break;
-                case kEnsSampleVort: items = (long long)s.gc.NX * s.gv.NY; break;
+                case kEnsSampleVort: items = s.gv.N; break;
                 case kEnsSampleCoarse: items = s.gc.N; break;
                 case kEnsSpec: items = (long long)s.gp.NX_fft * s.gp.NY; break;
                 default: items = s.gp.N; break;

@@ -32,6 +32,7 @@ struct AdvectMArgs {
     int time_integration_num;   // 10, 21, 20, 30, 40, 31, 41
     int nfoot;
     int rp;                     // psi cells per map cell (Npsi / Nmap, integer)
+    int nx_log2;                // log2 of the map grid's NX when a power of two, else -1
 };
 
 cudaError_t launch_init_map_m(float4* map, const Grid& g, cudaStream_t s);
@@ -72,10 +73,23 @@ cudaError_t launch_particles_m(const Grid& gp, unsigned long long* pos, int num,
                                const float4* psiC = nullptr, float2* vel = nullptr, double tau = 0.0);
 cudaError_t launch_particle_vel_init_m(const Grid& gp, const unsigned long long* pos, int num, const float4* psi0,
                                        float2* vel, cudaStream_t s);
-cudaError_t launch_vel_to_f64(const float2* v, int num, double* out, cudaStream_t s);
+cudaError_t launch_vel_to_f64(const float2* v, int num, double* out, cudaStream_t s, const int* perm = nullptr);
 cudaError_t launch_vel_from_f64(const double* v, int num, float2* out, cudaStream_t s);
 cudaError_t launch_pos_to_fix(const double* pos, int num, const Grid& g, unsigned long long* out, cudaStream_t s);
-cudaError_t launch_fix_to_pos(const unsigned long long* in, int num, const Grid& g, double* pos, cudaStream_t s);
+cudaError_t launch_fix_to_pos(const unsigned long long* in, int num, const Grid& g, double* pos, cudaStream_t s,
+                              const int* perm = nullptr);
+// tracer storage order (counting sort by bucket of 4 x 4 psi cells; perm = original index of
+// each stored tracer; the FP64 views above write through perm)
+struct TracerScratch {
+    unsigned long long* pos = nullptr;   // 2 x cap
+    float2* vel = nullptr;               // cap
+    int *perm = nullptr, *key = nullptr, *rank = nullptr;   // cap each
+    int* count = nullptr;                // nb_cap
+    int cap = 0, nb_cap = 0;
+};
+cudaError_t launch_tracer_reorder(const Grid& gp, unsigned long long* pos, float2* vel, int* perm, int num,
+                                  TracerScratch& t, cudaStream_t s);
+cudaError_t launch_iota(int* p, int num, cudaStream_t s);
 // learned psi: the psi solve of (omega sampled on the map grid gc, spectrum Fc, interpolated
 // spectrally) + (vorticity correction on the psi grid, spectrum D); cut off and
 // differentiated like launch_spec_psi_f

@@ -281,7 +281,7 @@ __device__ __forceinline__ void advect_m_tile(const AdvectMArgs& a, int lpn_log2
     int k = (int)(t & (lpn - 1));
     bool live = node < a.gm.N;
     const int nd = live ? (int)node : 0;
-    const int iY = nd / a.gm.NX, iX = nd - iY * a.gm.NX;
+    const int iY = a.nx_log2 >= 0 ? nd >> a.nx_log2 : nd / a.gm.NX, iX = nd - iY * a.gm.NX;
     float4 n0 = __ldg(a.map + 2 * nd);     // (dX, dY, dX_x, dY_x) at the node
     float gX = 0.0f, gY = 0.0f;
     if (live && k < a.nfoot) {
@@ -607,12 +607,15 @@ __device__ __forceinline__ void incomp_tables(const Grid& gm, int r, float ir, W
     }
 }
 
-// check item i (map cell, row of check points in it): the largest deviation over its r points
-__device__ __forceinline__ void incomp_item(const Grid& gm, int r, float ir, const float4* __restrict__ M, int i,
-                                            const W4f* sw, const W4f* sd, F2& best)
+// check item i (map cell, row of check points in it): the largest deviation over its r points;
+// R > 0 a compile-time r, nx_log2 >= 0 a power-of-two map width (shifts for the index split)
+template <int R = 0>
+__device__ __forceinline__ void incomp_item(const Grid& gm, int r_rt, float ir, const float4* __restrict__ M, int i,
+                                            const W4f* sw, const W4f* sd, F2& best, int nx_log2 = -1)
 {
+        const int r = R > 0 ? R : r_rt;
         int cell = i / r, sub_y = i - cell * r;
-        int cy = cell / gm.NX, cx = cell - cy * gm.NX;
+        int cy = nx_log2 >= 0 ? cell >> nx_log2 : cell / gm.NX, cx = cell - cy * gm.NX;
         int cx1 = cx + 1 == gm.NX ? 0 : cx + 1, cy1 = cy + 1 == gm.NY ? 0 : cy + 1;
         int i00 = cy * gm.NX + cx, i10 = cy * gm.NX + cx1;
         int i01 = cy1 * gm.NX + cx, i11 = cy1 * gm.NX + cx1;
@@ -655,8 +658,9 @@ __device__ __forceinline__ void incomp_block_max(F2 best, F2* wmax, unsigned lon
     }
 }
 
+template <int R>
 __global__ void __launch_bounds__(256) k_incomp_m(Grid gm, int r, float ir, const float4* __restrict__ M,
-                                                  unsigned long long* result)
+                                                  unsigned long long* result, int nx_log2)
 {
     __shared__ W4f sw[kMaxCheckRatio], sd[kMaxCheckRatio];
     __shared__ F2 wmax[8];
@@ -665,7 +669,7 @@ __global__ void __launch_bounds__(256) k_incomp_m(Grid gm, int r, float ir, cons
     F2 best = {0.0f, 0.0f};
     const int total = (int)gm.N * r;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x)
-        incomp_item(gm, r, ir, M, i, sw, sd, best);
+        incomp_item<R>(gm, r, ir, M, i, sw, sd, best, nx_log2);
     incomp_block_max(best, wmax, result);
 }
 
@@ -677,7 +681,15 @@ cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_
     long long total = gm.N * r;
     long long need = (total + 255) / 256;
     unsigned blocks = (unsigned)(need < 152 * 8 ? need : 152 * 8);
-    k_incomp_m<<<blocks, 256, 0, s>>>(gm, r, 1.0f / (float)r, map, reinterpret_cast<unsigned long long*>(d_result));
+    const int nx_log2 = (gm.NX & (gm.NX - 1)) == 0 ? __builtin_ctz((unsigned)gm.NX) : -1;
+    unsigned long long* res = reinterpret_cast<unsigned long long*>(d_result);
+    const float ir = 1.0f / (float)r;
+    switch (r) {
+        case 2: k_incomp_m<2><<<blocks, 256, 0, s>>>(gm, r, ir, map, res, nx_log2); break;
+        case 4: k_incomp_m<4><<<blocks, 256, 0, s>>>(gm, r, ir, map, res, nx_log2); break;
+        case 8: k_incomp_m<8><<<blocks, 256, 0, s>>>(gm, r, ir, map, res, nx_log2); break;
+        default: k_incomp_m<0><<<blocks, 256, 0, s>>>(gm, r, ir, map, res, nx_log2); break;
+    }
     return cudaGetLastError();
 }
 
@@ -878,12 +890,18 @@ cudaError_t launch_compose_pos_m(const Grid& gm, const Grid& gt, const float4* m
 // (x-weights from a table); positions are integer node + FP32 offset.
 // ---------------------------------------------------------------------------
 // map column mx, output row iY of the sample (x-weights of the ro output columns in swx)
-template <typename T>
-__device__ __forceinline__ void sample_m_item(const Grid& gm, const Grid& go, const Grid& gf, int ro, int rf, float iro,
-                                              const float4* __restrict__ map, const float4* __restrict__ W,
-                                              T* __restrict__ out, int mx, int iY, const W4f* swx)
+// omega = W(X(x)) at output point (iX, iY) of grid go (ro output points per map cell in x and
+// y).  One thread per output point: the lanes of a warp sample consecutive points, so their
+// fine-grid gathers land on consecutive nodes (one 128-byte line per 8 lanes) instead of
+// nodes ro apart; the map cell's y-contraction is recomputed by each of its ro points.
+template <typename T, int RO = 0>
+__device__ __forceinline__ void sample_m_point(const Grid& gm, const Grid& go, const Grid& gf, int ro_rt, int rf,
+                                               float iro, const float4* __restrict__ map, const float4* __restrict__ W,
+                                               T* __restrict__ out, int iX, int iY, const W4f* swx)
 {
-    if (mx >= gm.NX) return;
+    if (iX >= go.NX) return;
+    const int ro = RO > 0 ? RO : ro_rt;   // RO > 0: a compile-time ratio, the divisions become shifts
+    const int mx = iX / ro, k = iX - mx * ro;
     const int my = iY / ro, sy = iY - my * ro;
     const int mx1 = mx + 1 == gm.NX ? 0 : mx + 1, my1 = my + 1 == gm.NY ? 0 : my + 1;
     const int i00 = my * gm.NX + mx, i10 = my * gm.NX + mx1, i01 = my1 * gm.NX + mx, i11 = my1 * gm.NX + mx1;
@@ -901,21 +919,17 @@ __device__ __forceinline__ void sample_m_item(const Grid& gm, const Grid& go, co
     const float VY1 = fmaf(wy.w3, b11.y, fmaf(wy.w2, b10.y, fmaf(wy.w1, a11.y, wy.w0 * a10.y)));
     const float SY0 = fmaf(wy.w3, b01.w, fmaf(wy.w2, b00.w, fmaf(wy.w1, a01.w, wy.w0 * a00.w)));
     const float SY1 = fmaf(wy.w3, b11.w, fmaf(wy.w2, b10.w, fmaf(wy.w1, a11.w, wy.w0 * a10.w)));
-    T* row = out + (long long)iY * go.NX;
-    for (int k = 0; k < ro; ++k) {
-        const W4f w = swx[k];
-        float dx = fmaf(w.w3, SX1, fmaf(w.w2, SX0, fmaf(w.w1, VX1, w.w0 * VX0)));
-        float dy = fmaf(w.w3, SY1, fmaf(w.w2, SY0, fmaf(w.w1, VY1, w.w0 * VY0)));
-        const int iX = mx * ro + k;
-        // on the fine grid the output point is node iX * rf
-        CellF c = locate_rel(gf, iX * rf, iY * rf, dx, dy);
-        Q4 q;
-        q.c00 = __ldg(W + c.i00); q.c10 = __ldg(W + c.i10); q.c01 = __ldg(W + c.i01); q.c11 = __ldg(W + c.i11);
-        row[iX] = (T)herm_value_f(q, value_weights_f(c.tx, gf.hxf), value_weights_f(c.ty, gf.hyf));
-    }
+    const W4f w = swx[k];
+    const float dx = fmaf(w.w3, SX1, fmaf(w.w2, SX0, fmaf(w.w1, VX1, w.w0 * VX0)));
+    const float dy = fmaf(w.w3, SY1, fmaf(w.w2, SY0, fmaf(w.w1, VY1, w.w0 * VY0)));
+    // on the fine grid the output point is node iX * rf
+    const CellF c = locate_rel(gf, iX * rf, iY * rf, dx, dy);
+    Q4 q;
+    q.c00 = __ldg(W + c.i00); q.c10 = __ldg(W + c.i10); q.c01 = __ldg(W + c.i01); q.c11 = __ldg(W + c.i11);
+    out[(long long)iY * go.NX + iX] = (T)herm_value_f(q, value_weights_f(c.tx, gf.hxf), value_weights_f(c.ty, gf.hyf));
 }
 
-template <typename T>
+template <typename T, int RO>
 __global__ void __launch_bounds__(256) k_sample_m(Grid gm, Grid go, Grid gf, int ro, int rf, float iro,
                                                   const float4* __restrict__ map, const float4* __restrict__ W,
                                                   T* __restrict__ out)
@@ -923,7 +937,21 @@ __global__ void __launch_bounds__(256) k_sample_m(Grid gm, Grid go, Grid gf, int
     __shared__ W4f swx[kMaxCheckRatio];
     if ((int)threadIdx.x < ro) swx[threadIdx.x] = value_weights_f((float)threadIdx.x * iro, gm.hxf);
     __syncthreads();
-    sample_m_item<T>(gm, go, gf, ro, rf, iro, map, W, out, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y, swx);
+    sample_m_point<T, RO>(gm, go, gf, ro, rf, iro, map, W, out, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y,
+                          swx);
+}
+
+template <typename T>
+void sample_m_dispatch(dim3 blocks, cudaStream_t s, const Grid& gm, const Grid& go, const Grid& gf, int ro, int rf,
+                       float iro, const float4* map, const float4* W, T* out)
+{
+    switch (ro) {
+        case 1: k_sample_m<T, 1><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out); break;
+        case 2: k_sample_m<T, 2><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out); break;
+        case 4: k_sample_m<T, 4><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out); break;
+        case 8: k_sample_m<T, 8><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out); break;
+        default: k_sample_m<T, 0><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out); break;
+    }
 }
 
 cudaError_t launch_sample_m(const Grid& gm, const Grid& go, const Grid& gf, const float4* map, const float4* W,
@@ -932,10 +960,10 @@ cudaError_t launch_sample_m(const Grid& gm, const Grid& go, const Grid& gf, cons
     int ro = go.NX / gm.NX, rf = gf.NX / go.NX;
     if (ro < 1 || ro > kMaxCheckRatio || ro * gm.NX != go.NX || ro * gm.NY != go.NY || go.NY > 65535)
         return cudaErrorInvalidValue;
-    dim3 blocks((unsigned)((gm.NX + 255) / 256), (unsigned)go.NY);
+    dim3 blocks((unsigned)((go.NX + 255) / 256), (unsigned)go.NY);
     float iro = 1.0f / (float)ro;
-    if (out_f) k_sample_m<float><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out_f);
-    else k_sample_m<double><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out_d);
+    if (out_f) sample_m_dispatch<float>(blocks, s, gm, go, gf, ro, rf, iro, map, W, out_f);
+    else sample_m_dispatch<double>(blocks, s, gm, go, gf, ro, rf, iro, map, W, out_d);
     return cudaGetLastError();
 }
 
@@ -1206,25 +1234,29 @@ cudaError_t launch_particle_vel_init_m(const Grid& gp, const unsigned long long*
 }
 
 __global__ void k_vel_convert(const float2* __restrict__ vf, double* __restrict__ vd, const double* __restrict__ vin,
-                              float2* __restrict__ vout, int num)
+                              float2* __restrict__ vout, int num, const int* __restrict__ perm)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= num) return;
-    if (vf) { float2 v = vf[i]; vd[2 * i] = v.x; vd[2 * i + 1] = v.y; }
-    else vout[i] = make_float2((float)vin[2 * i], (float)vin[2 * i + 1]);
+    if (vf) {
+        const float2 v = vf[i];
+        const long long o = perm ? perm[i] : i;
+        vd[2 * o] = v.x;
+        vd[2 * o + 1] = v.y;
+    } else vout[i] = make_float2((float)vin[2 * i], (float)vin[2 * i + 1]);
 }
 
-cudaError_t launch_vel_to_f64(const float2* v, int num, double* out, cudaStream_t s)
+cudaError_t launch_vel_to_f64(const float2* v, int num, double* out, cudaStream_t s, const int* perm)
 {
     if (num <= 0) return cudaSuccess;
-    k_vel_convert<<<(num + 255) / 256, 256, 0, s>>>(v, out, nullptr, nullptr, num);
+    k_vel_convert<<<(num + 255) / 256, 256, 0, s>>>(v, out, nullptr, nullptr, num, perm);
     return cudaGetLastError();
 }
 
 cudaError_t launch_vel_from_f64(const double* v, int num, float2* out, cudaStream_t s)
 {
     if (num <= 0) return cudaSuccess;
-    k_vel_convert<<<(num + 255) / 256, 256, 0, s>>>(nullptr, nullptr, v, out, num);
+    k_vel_convert<<<(num + 255) / 256, 256, 0, s>>>(nullptr, nullptr, v, out, num, nullptr);
     return cudaGetLastError();
 }
 
@@ -1240,12 +1272,14 @@ __global__ void k_pos_to_fix(const double* __restrict__ pos, long long n2, Grid 
     out[j] = v >= 18446744073709551616.0 ? 0ull : __double2ull_rn(v);
 }
 
-__global__ void k_fix_to_pos(const unsigned long long* __restrict__ in, long long n2, Grid g, double* __restrict__ pos)
+__global__ void k_fix_to_pos(const unsigned long long* __restrict__ in, long long n2, Grid g, double* __restrict__ pos,
+                             const int* __restrict__ perm)
 {
     long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (j >= n2) return;
     const bool y = j & 1;
-    pos[j] = (y ? g.b2 : g.b0) + __ull2double_rn(in[j]) * ((y ? g.Wy : g.Wx) * 5.42101086242752217e-20);
+    const long long o = perm ? 2ll * perm[j >> 1] + (j & 1) : j;
+    pos[o] = (y ? g.b2 : g.b0) + __ull2double_rn(in[j]) * ((y ? g.Wy : g.Wx) * 5.42101086242752217e-20);
 }
 
 cudaError_t launch_pos_to_fix(const double* pos, int num, const Grid& g, unsigned long long* out, cudaStream_t s)
@@ -1256,11 +1290,100 @@ cudaError_t launch_pos_to_fix(const double* pos, int num, const Grid& g, unsigne
     return cudaGetLastError();
 }
 
-cudaError_t launch_fix_to_pos(const unsigned long long* in, int num, const Grid& g, double* pos, cudaStream_t s)
+cudaError_t launch_fix_to_pos(const unsigned long long* in, int num, const Grid& g, double* pos, cudaStream_t s,
+                              const int* perm)
 {
     long long n2 = 2LL * num;
     if (n2 <= 0) return cudaSuccess;
-    k_fix_to_pos<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(in, n2, g, pos);
+    k_fix_to_pos<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(in, n2, g, pos, perm);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// tracer storage order: a counting sort by bucket of 4 x 4 psi cells, so a warp's tracers
+// gather psi nodes from one neighbourhood.  Each tracer's arithmetic does not depend on the
+// order; perm[i] is the original index of stored tracer i (the FP64 views write through it).
+// ---------------------------------------------------------------------------
+__global__ void k_bucket_count(const unsigned long long* __restrict__ pos, int num, int nx, int ny, int nbx,
+                               int* __restrict__ key, int* __restrict__ rank, int* __restrict__ count)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= num) return;
+    const int cx = (int)__umul64hi(pos[2 * i], (unsigned long long)nx);
+    const int cy = (int)__umul64hi(pos[2 * i + 1], (unsigned long long)ny);
+    const int b = (cy >> 2) * nbx + (cx >> 2);
+    key[i] = b;
+    rank[i] = atomicAdd(count + b, 1);
+}
+
+// exclusive scan of count[0..nb) in place, one block of 1024 threads
+__global__ void __launch_bounds__(1024) k_bucket_scan(int* __restrict__ count, int nb)
+{
+    __shared__ int part[1024];
+    const int per = (nb + 1023) / 1024;
+    const int b0 = threadIdx.x * per, b1 = min(nb, b0 + per);
+    int s = 0;
+    for (int b = b0; b < b1; ++b) s += count[b];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int run = part[threadIdx.x] - s;   // exclusive prefix of this thread's range
+    for (int b = b0; b < b1; ++b) {
+        const int c = count[b];
+        count[b] = run;
+        run += c;
+    }
+}
+
+__global__ void k_bucket_scatter(const unsigned long long* __restrict__ pos, const float2* __restrict__ vel,
+                                 const int* __restrict__ perm, const int* __restrict__ key, const int* __restrict__ rank,
+                                 const int* __restrict__ start, int num, unsigned long long* __restrict__ pos2,
+                                 float2* __restrict__ vel2, int* __restrict__ perm2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= num) return;
+    const int j = start[key[i]] + rank[i];
+    pos2[2 * j] = pos[2 * i];
+    pos2[2 * j + 1] = pos[2 * i + 1];
+    perm2[j] = perm[i];
+    if (vel) vel2[j] = vel[i];
+}
+
+cudaError_t launch_tracer_reorder(const Grid& gp, unsigned long long* pos, float2* vel, int* perm, int num,
+                                  TracerScratch& t, cudaStream_t s)
+{
+    if (num <= 0) return cudaSuccess;
+    const int nbx = (gp.NX + 3) / 4, nby = (gp.NY + 3) / 4, nb = nbx * nby;
+    if (num > t.cap || nb > t.nb_cap) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(t.count, 0, sizeof(int) * (size_t)nb, s);
+    if (e != cudaSuccess) return e;
+    const unsigned blocks = (unsigned)((num + 255) / 256);
+    k_bucket_count<<<blocks, 256, 0, s>>>(pos, num, gp.NX, gp.NY, nbx, t.key, t.rank, t.count);
+    k_bucket_scan<<<1, 1024, 0, s>>>(t.count, nb);
+    k_bucket_scatter<<<blocks, 256, 0, s>>>(pos, vel, perm, t.key, t.rank, t.count, num, t.pos, t.vel, t.perm);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(pos, t.pos, sizeof(unsigned long long) * 2 * (size_t)num, cudaMemcpyDeviceToDevice, s)))
+        return e;
+    if ((e = cudaMemcpyAsync(perm, t.perm, sizeof(int) * (size_t)num, cudaMemcpyDeviceToDevice, s))) return e;
+    if (vel && (e = cudaMemcpyAsync(vel, t.vel, sizeof(float2) * (size_t)num, cudaMemcpyDeviceToDevice, s))) return e;
+    return cudaSuccess;
+}
+
+__global__ void k_iota(int* __restrict__ p, int num)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < num) p[i] = i;
+}
+
+cudaError_t launch_iota(int* p, int num, cudaStream_t s)
+{
+    if (num <= 0) return cudaSuccess;
+    k_iota<<<(unsigned)((num + 255) / 256), 256, 0, s>>>(p, num);
     return cudaGetLastError();
 }
 
@@ -1609,10 +1732,10 @@ __global__ void __launch_bounds__(256) k_ens_sample(const EnsMember* __restrict_
         if ((int)threadIdx.x < ro) swx[threadIdx.x] = value_weights_f((float)threadIdx.x * iro, gm.hxf);
         __syncthreads();
         const int i = (tile - __ldg(cum + m)) * 256 + threadIdx.x;
-        if (i < gm.NX * go.NY) {
-            const int iY = i / gm.NX, mx = i - iY * gm.NX;
-            if (which == 0) sample_m_item<float>(gm, go, gf, ro, rf, iro, e.adv.map, e.wfm, e.sample_out, mx, iY, swx);
-            else sample_m_item<double>(gm, go, gf, ro, rf, iro, e.adv.map, e.wfm, e.vort, mx, iY, swx);
+        if (i < go.NX * go.NY) {
+            const int iY = i / go.NX, iX = i - iY * go.NX;
+            if (which == 0) sample_m_point<float>(gm, go, gf, ro, rf, iro, e.adv.map, e.wfm, e.sample_out, iX, iY, swx);
+            else sample_m_point<double>(gm, go, gf, ro, rf, iro, e.adv.map, e.wfm, e.vort, iX, iY, swx);
         }
         __syncthreads();
     }

@@ -297,13 +297,33 @@ int EulerSim::alloc()
             return rc;
         for (int l = 0; l < L; ++l) if ((rc = falloc((void**)&psim_[l], psib))) return rc;
         if (s.initial_discrete && (rc = falloc((void**)&wdiscm_, sizeof(float4) * (size_t)gd.N))) return rc;
+        int tmax = 0;
         for (auto& p : s.particles_advected) {
             unsigned long long* d = nullptr;
             if ((rc = falloc((void**)&d, sizeof(unsigned long long) * 2 * (size_t)std::max(p.num, 1)))) return rc;
             partfix_.push_back(d);
+            // large tracer sets of the Euler form are kept in spatial storage order
+            int* perm = nullptr;
+            if (!vlasov_ && p.num >= kReorderMin) {
+                if ((rc = falloc((void**)&perm, sizeof(int) * (size_t)p.num))) return rc;
+                tmax = std::max(tmax, p.num);
+            }
+            tperm_.push_back(perm);
             float2* v = nullptr;
             if (p.tau != 0 && (rc = falloc((void**)&v, sizeof(float2) * (size_t)std::max(p.num, 1)))) return rc;
             velm_.push_back(v);
+        }
+        if (tmax > 0) {
+            TracerScratch& t = tscratch_;
+            t.cap = tmax;
+            t.nb_cap = ((gp.NX + 3) / 4) * ((gp.NY + 3) / 4);
+            if ((rc = falloc((void**)&t.pos, sizeof(unsigned long long) * 2 * (size_t)tmax)) ||
+                (rc = falloc((void**)&t.vel, sizeof(float2) * (size_t)tmax)) ||
+                (rc = falloc((void**)&t.perm, sizeof(int) * (size_t)tmax)) ||
+                (rc = falloc((void**)&t.key, sizeof(int) * (size_t)tmax)) ||
+                (rc = falloc((void**)&t.rank, sizeof(int) * (size_t)tmax)) ||
+                (rc = falloc((void**)&t.count, sizeof(int) * (size_t)t.nb_cap)))
+                return rc;
         }
         if (stack_cap_ > 0 && (rc = falloc((void**)&stackm_, mapb * stack_cap_))) return rc;
         int nv[2] = {gv.NY, gv.NX}, np[2] = {gp.NY, gp.NX}, nf[2] = {gf.NY, gf.NX};
@@ -318,6 +338,23 @@ int EulerSim::alloc()
         cufftSetStream(c2r4_p_, stream);
         cufftSetStream(r2c_f_, stream);
         cufftSetStream(c2r4_f_, stream);
+        if (!vlasov_) {
+            // the psi solve keeps the columns kx <= freq_cut_psi of omega's spectrum only: a
+            // row R2C of every row, then a column C2C of just those columns (same modes,
+            // about half the work of the full 2D transform)
+            vcols_ = std::min(gv.NX_fft, (int)std::floor(s.freq_cut_psi) + 1);
+            int nrow[1] = {gv.NX}, nrowf[1] = {gv.NX_fft}, ncol[1] = {gv.NY};
+            if (cufftPlanMany(&r2c_vrows_, 1, nrow, nrow, 1, gv.NX, nrowf, 1, gv.NX_fft, CUFFT_R2C, gv.NY) != CUFFT_SUCCESS ||
+                cufftPlanMany(&c2c_vcols_, 1, ncol, ncol, gv.NX_fft, 1, ncol, gv.NX_fft, 1, CUFFT_C2C, vcols_) !=
+                    CUFFT_SUCCESS) {
+                err = "cuFFT FP32 plan creation failed";
+                return kErrCuda;
+            }
+            cufftSetStream(r2c_vrows_, stream);
+            cufftSetStream(c2c_vcols_, stream);
+            // (the inverse transform of the four psi spectra stays one batched 2D C2R: pruned
+            // the same way -- strided column C2C per plane, then row C2R -- it measured slower)
+        }
     }
     // random table for gaussian_blobs (cmm-euler2d.cu:348-354)
     std::vector<double> rnd(1000);
@@ -347,6 +384,10 @@ void EulerSim::release()
     vels.clear();
     for (auto p : partfix_) f(p);
     partfix_.clear();
+    for (auto p : tperm_) f(p);
+    tperm_.clear();
+    f(tscratch_.pos); f(tscratch_.vel); f(tscratch_.perm); f(tscratch_.key); f(tscratch_.rank); f(tscratch_.count);
+    tscratch_ = TracerScratch{};
     for (auto p : velm_) f(p);
     velm_.clear();
     for (int l = 0; l < kMaxLagrange; ++l) { f(phi_lv_[l]); phi_lv_[l] = nullptr; }
@@ -370,7 +411,9 @@ void EulerSim::release()
     if (c2r4_p_) cufftDestroy(c2r4_p_);
     if (r2c_f_) cufftDestroy(r2c_f_);
     if (c2r4_f_) cufftDestroy(c2r4_f_);
-    r2c_v_ = c2r4_p_ = r2c_f_ = c2r4_f_ = 0;
+    if (r2c_vrows_) cufftDestroy(r2c_vrows_);
+    if (c2c_vcols_) cufftDestroy(c2c_vcols_);
+    r2c_v_ = c2r4_p_ = r2c_f_ = c2r4_f_ = r2c_vrows_ = c2c_vcols_ = 0;
     r2c_v_ = c2r4_p_ = 0;
     if (h_scal_) cudaFreeHost(h_scal_);
     h_scal_ = nullptr;
@@ -423,9 +466,9 @@ int EulerSim::evaluate_stream()
             if (rc) return rc;
         } else {
             CMM_LAUNCH(1, launch_sample_m(gc, gv, gf, mapm_, wfm_, realf_, nullptr, stream));
-            CMM_FFT(cufftExecR2C(r2c_v_, realf_, reinterpret_cast<cufftComplex*>(specf_)));
+            if (int rc = vort_spectrum()) return rc;
             CMM_LAUNCH(1, launch_spec_psi_f(specf_, gv, gp, s.freq_cut_psi, spec4f_, stream));
-            CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), realf_));
+            if (int rc = psi_planes(spec4f_, realf_)) return rc;
         }
         fused_ = false;
         if (psi_lcl_ >= 0 && L == 3) {
@@ -457,6 +500,26 @@ int EulerSim::evaluate_stream()
     return kOk;
 }
 
+int EulerSim::vort_spectrum()
+{
+    // omega on the vorticity grid (realf_) -> the modes the psi solve keeps (specf_)
+    if (!r2c_vrows_) {
+        CMM_FFT(cufftExecR2C(r2c_v_, realf_, reinterpret_cast<cufftComplex*>(specf_)));
+        return kOk;
+    }
+    CMM_FFT(cufftExecR2C(r2c_vrows_, realf_, reinterpret_cast<cufftComplex*>(specf_)));
+    CMM_FFT(cufftExecC2C(c2c_vcols_, reinterpret_cast<cufftComplex*>(specf_), reinterpret_cast<cufftComplex*>(specf_),
+                         CUFFT_FORWARD));
+    return kOk;
+}
+
+int EulerSim::psi_planes(float2* spec4, float* out)
+{
+    // the four Hermite spectra (gp layout) -> the planes on the psi grid
+    CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4), out));
+    return kOk;
+}
+
 int EulerSim::coarse_vort()
 {
     if (mixed_) {
@@ -476,8 +539,9 @@ int EulerSim::sync_fp64_views()
     for (int l = 0; l < L; ++l) CMM_LAUNCH(1, launch_float4_to_planes(psim_[l], gp.N, psi[l], stream));
     CMM_LAUNCH(1, launch_float4_to_planes(wfm_, gf.N, wfine, stream));
     for (size_t i = 0; i < partfix_.size(); ++i) {
-        CMM_LAUNCH(1, launch_fix_to_pos(partfix_[i], s.particles_advected[i].num, gp, parts[i], stream));
-        if (velm_[i]) CMM_LAUNCH(1, launch_vel_to_f64(velm_[i], s.particles_advected[i].num, vels[i], stream));
+        CMM_LAUNCH(1, launch_fix_to_pos(partfix_[i], s.particles_advected[i].num, gp, parts[i], stream, tperm_[i]));
+        if (velm_[i])
+            CMM_LAUNCH(1, launch_vel_to_f64(velm_[i], s.particles_advected[i].num, vels[i], stream, tperm_[i]));
     }
     if (vlasov_)   // psi levels are held as phi(x) and h(v): write their Hermite planes
         for (int l = 0; l < L; ++l)
@@ -598,6 +662,7 @@ int EulerSim::advect_m(const double* t, const double* dtv, int lc, int ti_num, i
     a.ep64 = s.map_epsilon;
     a.time_integration_num = ti_num;
     a.rp = gp.NX / gc.NX;
+    a.nx_log2 = (gc.NX & (gc.NX - 1)) == 0 ? __builtin_ctz((unsigned)gc.NX) : -1;
     CMM_LAUNCH(1, launch_advect_m(a, stream));
     std::swap(mapm_, mapm_new_);
     return kOk;
@@ -825,13 +890,13 @@ int EulerSim::write_particles_state()
     for (size_t i = 0; i < s.particles_advected.size(); ++i) {
         const int num = s.particles_advected[i].num;
         if (num <= 0) continue;
-        if (mixed_) CMM_LAUNCH(1, launch_fix_to_pos(partfix_[i], num, gp, parts[i], stream));
+        if (mixed_) CMM_LAUNCH(1, launch_fix_to_pos(partfix_[i], num, gp, parts[i], stream, tperm_[i]));
         std::vector<double> h((size_t)2 * num);
         CMM_CUDA(cudaMemcpyAsync(h.data(), parts[i], sizeof(double) * 2 * num, cudaMemcpyDeviceToHost, stream));
         CMM_CUDA(cudaStreamSynchronize(stream));
         bool ok = write_f64(dir + "/Particles_advected_pos_P" + two_digits((int)i + 1) + ".data", h.data(), h.size());
         if (ok && s.particles_advected[i].tau != 0) {
-            if (mixed_) CMM_LAUNCH(1, launch_vel_to_f64(velm_[i], num, vels[i], stream));
+            if (mixed_) CMM_LAUNCH(1, launch_vel_to_f64(velm_[i], num, vels[i], stream, tperm_[i]));
             CMM_CUDA(cudaMemcpyAsync(h.data(), vels[i], sizeof(double) * 2 * num, cudaMemcpyDeviceToHost, stream));
             CMM_CUDA(cudaStreamSynchronize(stream));
             ok = write_f64(dir + "/Particles_advected_vel_U" + two_digits((int)i + 1) + ".data", h.data(), h.size());
@@ -936,6 +1001,7 @@ int EulerSim::restart_from_map_stack()
         if (!read("Particles_advected_pos_P" + two_digits((int)i + 1) + ".data", pos.data(), pos.size())) continue;
         CMM_CUDA(cudaMemcpyAsync(parts[i], pos.data(), sizeof(double) * pos.size(), cudaMemcpyHostToDevice, stream));
         if (mixed_) CMM_LAUNCH(1, launch_pos_to_fix(parts[i], num, gp, partfix_[i], stream));
+        if (mixed_ && tperm_[i]) CMM_LAUNCH(1, launch_iota(tperm_[i], num, stream));
         CMM_CUDA(cudaStreamSynchronize(stream));
         if (s.particles_advected[i].tau == 0) continue;
         if (!read("Particles_advected_vel_U" + two_digits((int)i + 1) + ".data", pos.data(), pos.size())) continue;
@@ -1031,6 +1097,9 @@ int EulerSim::advect_particles(int lcl)
                 for (int k = 0; k < L && have; ++k) have = Lp12[k] == fusedLp_[k];
                 if (!have) CMM_LAUNCH(1, launch_precombine(psim_, L, Lp12, nullptr, gp.N, psiP_, nullptr, stream));
                 combined = true;
+            }
+            if (tperm_[i] && loop_ctr_ % kReorderEvery == 0) {
+                CMM_LAUNCH(3, launch_tracer_reorder(gp, partfix_[i], velm_[i], tperm_[i], p.num, tscratch_, stream));
             }
             cudaError_t e = vlasov_
                 ? launch_particles_m(gp, partfix_[i], p.num, nullptr, nullptr, nullptr, dt_vec_[lcl + 1], ti, stream,
@@ -1151,8 +1220,10 @@ int EulerSim::init()
     }
     if (!restart) {
         if ((rc = init_particles())) return rc;
-        for (size_t i = 0; i < partfix_.size(); ++i)
+        for (size_t i = 0; i < partfix_.size(); ++i) {
             CMM_LAUNCH(1, launch_pos_to_fix(parts[i], s.particles_advected[i].num, gp, partfix_[i], stream));
+            if (tperm_[i]) CMM_LAUNCH(1, launch_iota(tperm_[i], s.particles_advected[i].num, stream));
+        }
         // inertial particles start at the fluid velocity of psi(t_0) or at rest (cmm-euler2d.cu:620-632)
         for (size_t i = 0; i < s.particles_advected.size(); ++i)
             if ((rc = init_inertial_velocity(i))) return rc;
@@ -1363,6 +1434,7 @@ int EulerSim::ens_begin(EnsMember& e)
     a.ep64 = s.map_epsilon;
     a.time_integration_num = ti;
     a.rp = gp.NX / gc.NX;
+    a.nx_log2 = (gc.NX & (gc.NX - 1)) == 0 ? __builtin_ctz((unsigned)gc.NX) : -1;
     e.adv = a;
     e.active = 1;
     // the previous psi solve's fused combinations, if its predicted coefficients are these

@@ -14,6 +14,7 @@
 
 #include "io.hpp"
 #include "kernels.hpp"
+#include "mixed.hpp"
 #include "settings.hpp"
 #include "vlasov.hpp"
 
@@ -125,6 +126,8 @@ private:
     void release();
     int translate_ic();
     int evaluate_stream();
+    int vort_spectrum();
+    int psi_planes(float2* spec4, float* out);
     int coarse_vort();
     int advect(const double* t, const double* dtv, int loop_ctr, int ti_num, int l_order);
     int advect_m(const double* t, const double* dtv, int loop_ctr, int ti_num, int l_order);
@@ -210,6 +213,11 @@ private:
     int ens_lcl_ = 0;
     double ens_dt_ = 0, ens_gap_ = 0, ens_counter_ = 0;
     bool ens_saturated_ = false;
+    // tracer storage order: sets of at least kReorderMin tracers are sorted by 4 x 4 psi-cell
+    // bucket every kReorderEvery steps; tperm_[i][j] = original index of stored tracer j
+    static constexpr int kReorderMin = 4096, kReorderEvery = 32;
+    std::vector<int*> tperm_;
+    TracerScratch tscratch_;
     float4* mapm_ = nullptr;         // 2*Nc float4 (current map)
     float4* mapm_new_ = nullptr;
     float4* psim_[kMaxLagrange] = {nullptr, nullptr, nullptr, nullptr};
@@ -247,6 +255,8 @@ private:
     float2* specf_ = nullptr;        // FP32 complex scratch
     float2* spec4f_ = nullptr;       // 4 FP32 spectra
     cufftHandle r2c_v_ = 0, c2r4_p_ = 0, r2c_f_ = 0, c2r4_f_ = 0;
+    cufftHandle r2c_vrows_ = 0, c2c_vcols_ = 0;   // pruned forward transform of omega (mixed Euler)
+    int vcols_ = 0;
     bool prof_ = false;
     cudaEvent_t ev_[kNumPhases][2] = {};
     bool ev_live_[kNumPhases] = {};

@@ -148,7 +148,7 @@ int EulerSim::learned_planes(lrn::Upsampler& u, float* out)
     kernel_launches += u.launches;
     CMM_FFT(cufftExecR2C((cufftHandle)l_r2c_, l_delta_, reinterpret_cast<cufftComplex*>(l_dspec_)));
     CMM_LAUNCH(1, launch_spec_psi_learned(lc_spec_, gc, l_dspec_, gp, s.freq_cut_psi, spec4f_, stream));
-    CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), out));
+    if ((rc = psi_planes(spec4f_, out))) return rc;
     return kOk;
 }
 
@@ -166,7 +166,7 @@ int EulerSim::cheap_planes(float* out)
     int rc;
     if ((rc = cheap_fields())) return rc;
     CMM_LAUNCH(1, launch_spec_psi_f(lc_spec_, gc, gp, s.freq_cut_psi, spec4f_, stream));
-    CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), out));
+    if ((rc = psi_planes(spec4f_, out))) return rc;
     return kOk;
 }
 
@@ -184,15 +184,15 @@ int EulerSim::learned_stream()
         }
     }
     ++exact_steps_;
+    int rc;
     CMM_LAUNCH(1, launch_sample_m(gc, gv, gf, mapm_, wfm_, realf_, nullptr, stream));
-    CMM_FFT(cufftExecR2C(r2c_v_, realf_, reinterpret_cast<cufftComplex*>(specf_)));
+    if ((rc = vort_spectrum())) return rc;
     CMM_LAUNCH(1, launch_spec_psi_f(specf_, gv, gp, s.freq_cut_psi, spec4f_, stream));
-    CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), realf_));
+    if ((rc = psi_planes(spec4f_, realf_))) return rc;
     if (loop_ctr_ % learned_every_ != 0) return kOk;
     // the exact evaluation judges the learned and the cheap psi on the same state and picks
     // the level of the next every - 1 steps: the network where it meets the tolerance and
     // beats the cheap psi, else the cheap psi where that meets it, else the exact one
-    int rc;
     double st[4];
     if ((rc = learned_planes(*ups_, l_planes_)) || (rc = diff_stats(l_planes_, 1, realf_, 1, gp.N, st))) return rc;
     const double el = st[1] > 0 ? st[0] / st[1] : 0.0;
@@ -241,7 +241,7 @@ int EulerSim::learned_evaluate(lrn::Upsampler& u, double* out6)
     const float* exact = reinterpret_cast<const float*>(psim_[0]);
     double st[4];
     CMM_LAUNCH(1, launch_spec_psi_f(lc_spec_, gc, gp, s.freq_cut_psi, spec4f_, stream));
-    CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), l_planes_));
+    if ((rc = psi_planes(spec4f_, l_planes_))) return rc;
     auto rel = [&](double* o) {
         o[0] = st[1] > 0 ? st[0] / st[1] : 0.0;
         o[1] = st[3] > 0 ? std::sqrt(st[2] / st[3]) : 0.0;
@@ -255,7 +255,7 @@ int EulerSim::learned_evaluate(lrn::Upsampler& u, double* out6)
     CMM_LAUNCH(1, launch_sample_m(gc, gp, gf, mapm_, wfm_, l_delta_, nullptr, stream));
     CMM_FFT(cufftExecR2C((cufftHandle)l_r2c_, l_delta_, reinterpret_cast<cufftComplex*>(l_dspec_)));
     CMM_LAUNCH(1, launch_spec_psi_f(l_dspec_, gp, gp, s.freq_cut_psi, spec4f_, stream));
-    CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4f_), l_planes_));
+    if ((rc = psi_planes(spec4f_, l_planes_))) return rc;
     if ((rc = diff_stats(l_planes_, 1, exact, 4, gp.N, st))) return rc;
     rel(out6 + 4);
     return kOk;

@@ -259,6 +259,7 @@ int EulerSim::alloc()
         (rc = dalloc(&d_rand_, kInitTable)))
         return rc;
     CMM_CUDA(cudaMallocHost((void**)&h_scal_, sizeof(double) * 16));
+    CMM_CUDA(cudaEventCreateWithFlags(&einc_ev_, cudaEventDisableTiming));
     for (auto& p : s.particles_advected) {
         double* d = nullptr;
         if ((rc = dalloc(&d, 2ll * std::max(p.num, 1)))) return rc;
@@ -417,6 +418,10 @@ void EulerSim::release()
     r2c_v_ = c2r4_p_ = 0;
     if (h_scal_) cudaFreeHost(h_scal_);
     h_scal_ = nullptr;
+    if (einc_ev_) cudaEventDestroy(einc_ev_);
+    einc_ev_ = nullptr;
+    if (step_graph_) cudaGraphExecDestroy(step_graph_);
+    step_graph_ = nullptr;
     destroy_plans(pf_); destroy_plans(pv_); destroy_plans(pp_); destroy_plans(pc_); destroy_plans(pd_);
     ChiX = ChiY = ChiX_new = ChiY_new = vort = wfine = wdisc = stack = nullptr;
     for (int l = 0; l < kMaxLagrange; ++l) psi[l] = nullptr;
@@ -518,6 +523,13 @@ int EulerSim::psi_planes(float2* spec4, float* out)
     // the four Hermite spectra (gp layout) -> the planes on the psi grid
     CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4), out));
     return kOk;
+}
+
+int EulerSim::ensure_vort()
+{
+    if (!vort_stale_) return kOk;
+    vort_stale_ = false;
+    return coarse_vort();
 }
 
 int EulerSim::coarse_vort()
@@ -771,6 +783,20 @@ int EulerSim::incomp(double* out)
     CMM_CUDA(cudaStreamSynchronize(stream));
     *out = h_scal_[0];
     return kOk;
+}
+
+void EulerSim::unrotate_psi(int n)
+{
+    // the inverse of rotate_psi(n)
+    double* tmp = psi[0];
+    for (int j = 0; j < n; ++j) psi[j] = psi[j + 1];
+    psi[n] = tmp;
+    float4* tmf = psim_[0];
+    for (int j = 0; j < n; ++j) psim_[j] = psim_[j + 1];
+    psim_[n] = tmf;
+    double* tph = phi_lv_[0];
+    for (int j = 0; j < n; ++j) phi_lv_[j] = phi_lv_[j + 1];
+    phi_lv_[n] = tph;
 }
 
 void EulerSim::rotate_psi(int n)
@@ -1283,14 +1309,73 @@ int EulerSim::step_once()
     t_vec_[lcl + 1] = t + dt_now;
     dt_vec_[lcl + 1] = dt_now;
 
+    // mixed Euler: the psi of the advected map is enqueued before the host reads E_inc, so
+    // the GPU computes while the host waits; a remap (a few steps in a hundred) undoes the
+    // psi rotation and redoes the evaluation on the remapped state.  That front of the step
+    // (advection, incompressibility check and its readback, psi solve) is captured as a CUDA
+    // graph and replayed through one executable updated in place (no gaps between its
+    // kernels); profiled steps launch plainly
+    const bool spec = mixed_ && !vlasov_ && !ups_ && !s.forward_map;
+    bool capturing = spec && use_graphs_ && !prof_ &&
+                     cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    auto end_capture = [&](int rc_in) -> int {
+        if (!capturing) return rc_in;
+        capturing = false;
+        cudaGraph_t g = nullptr;
+        cudaError_t ec = cudaStreamEndCapture(stream, &g);
+        if (rc_in) {
+            if (g) cudaGraphDestroy(g);
+            return rc_in;
+        }
+        if (ec != cudaSuccess || !g) return check(ec != cudaSuccess ? ec : cudaErrorUnknown, "cudaStreamEndCapture");
+        if (step_graph_) {
+            cudaGraphExecUpdateResultInfo info;
+            if (cudaGraphExecUpdate(step_graph_, g, &info) != cudaSuccess) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(step_graph_);
+                step_graph_ = nullptr;
+            }
+        }
+        cudaError_t ei = step_graph_ ? cudaSuccess : cudaGraphInstantiate(&step_graph_, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) return check(ei, "cudaGraphInstantiate");
+        ++graph_launches_;
+        return check(cudaGraphLaunch(step_graph_, stream), "cudaGraphLaunch");
+    };
     ph_begin(kPhAdvect);
-    if ((rc = advect(t_vec_.data(), dt_vec_.data(), loop_ctr_, s.time_integration_num, L))) return rc;
+    if ((rc = advect(t_vec_.data(), dt_vec_.data(), loop_ctr_, s.time_integration_num, L))) return end_capture(rc);
     bool forced_remap = false;
-    if ((rc = forward_step(lcl, &forced_remap))) return rc;
+    if ((rc = forward_step(lcl, &forced_remap))) return end_capture(rc);
     ph_end(kPhAdvect);
     ph_begin(kPhIncomp);
-    if ((rc = incomp(&e_inc_))) return rc;
+    if (spec) {
+        kernel_launches++;
+        if ((rc = check(launch_incomp_m(gc, gf.NX / gc.NX, mapm_, d_scal_, stream), "launch_incomp_m")) ||
+            (rc = check(cudaMemcpyAsync(h_scal_, d_scal_, sizeof(double), cudaMemcpyDeviceToHost, stream), "cudaMemcpyAsync")) ||
+            (rc = check(capturing ? cudaEventRecordWithFlags(einc_ev_, stream, cudaEventRecordExternal)
+                                  : cudaEventRecord(einc_ev_, stream),
+                        "cudaEventRecord")))
+            return end_capture(rc);
+    } else if ((rc = incomp(&e_inc_))) {
+        return rc;
+    }
     ph_end(kPhIncomp);
+    bool psi_done = false;
+    if (spec) {
+        rotate_psi(L - 1);
+        ph_begin(kPhPsi);
+        psi_lcl_ = lcl;
+        in_step_ = true;
+        rc = evaluate_stream();
+        in_step_ = false;
+        psi_lcl_ = -1;
+        if ((rc = end_capture(rc))) return rc;
+        ph_end(kPhPsi);
+        CMM_CUDA(cudaEventSynchronize(einc_ev_));
+        e_inc_ = h_scal_[0];
+        psi_done = !((e_inc_ > s.incomp_threshold && !s.skip_remapping) || forced_remap);
+        if (!psi_done) unrotate_psi(L - 1);
+    }
     if (vlasov_ && (e_inc_ <= 0 || e_inc_ > 1e15)) {
         // the Vlasov driver aborts on a vanishing or exploding incompressibility error (cmm-vlasov1d.cu:838-840)
         err = "incompressibility error out of range in the coarse grid (" + to_str3(e_inc_) + "): run aborted";
@@ -1320,17 +1405,25 @@ int EulerSim::step_once()
         }
     }
     double gap = loop_ctr_ - old_ctr_, counter = n_maps_;
-    rotate_psi(L - 1);
-    ph_begin(kPhPsi);
-    psi_lcl_ = lcl;
-    in_step_ = true;
-    rc = evaluate_stream();
-    in_step_ = false;
-    psi_lcl_ = -1;
-    if (rc) return rc;
-    ph_end(kPhPsi);
+    if (!psi_done) {
+        rotate_psi(L - 1);
+        ph_begin(kPhPsi);
+        psi_lcl_ = lcl;
+        in_step_ = true;
+        rc = evaluate_stream();
+        in_step_ = false;
+        psi_lcl_ = -1;
+        if (rc) return rc;
+        ph_end(kPhPsi);
+    }
+    // the coarse vorticity is read only by the diagnostics, the saves and get_field: the 2D Euler
+    // form samples it when first read after a step (same map, same fine vorticity, same values)
     ph_begin(kPhCoarse);
-    if ((rc = coarse_vort())) return rc;
+    if (vlasov_) {
+        if ((rc = coarse_vort())) return rc;
+    } else {
+        vort_stale_ = true;
+    }
     ph_end(kPhCoarse);
     ph_begin(kPhParticles);
     if ((rc = advect_particles(lcl))) return rc;
@@ -1342,22 +1435,24 @@ int EulerSim::step_once()
     loop_ctr_++;
     CMM_CUDA(cudaGetLastError());
 
-    std::string dir = run_dir(s) + "/Monitoring_data/";
-    append_f64(dir + "Time_s.data", &t_vec_[lcl + 1], 1);
-    append_f64(dir + "Error_incompressibility.data", &e_inc_, 1);
+    // the per-step Monitoring_data records are kept in host buffers and appended in blocks
+    // (every 256 steps, at the final step, in finish and before any state is read)
+    mon_buf_[kMonTimeS].push_back(t_vec_[lcl + 1]);
+    mon_buf_[kMonEinc].push_back(e_inc_);
     if (s.forward_map) {
-        append_f64(dir + "Error_incompressibility_forward.data", &e_inc_f_, 1);
-        append_f64(dir + "Error_invertibility.data", &e_inv_, 1);
+        mon_buf_[kMonEincF].push_back(e_inc_f_);
+        mon_buf_[kMonEinv].push_back(e_inv_);
     }
-    append_f64(dir + "Map_gaps.data", &gap, 1);
-    append_f64(dir + "Map_counter.data", &counter, 1);
+    mon_buf_[kMonGap].push_back(gap);
+    mon_buf_[kMonCounter].push_back(counter);
     double tc = wall();
     if (s.verbose >= 2)
         log_.push("Step = " + std::to_string(loop_ctr_) + " \t S-Time = " + to_str3(t_vec_[lcl + 1]) + "/" +
                   to_str3(s.final_time) + " \t E-inc = " + to_str3(e_inc_) +
                   (s.forward_map ? " \t E-inc_f = " + to_str3(e_inc_f_) + " \t E-inv = " + to_str3(e_inv_) : std::string()) +
                   " \t C-Time = " + format_duration(tc));
-    append_f64(dir + "Time_c.data", &tc, 1);
+    mon_buf_[kMonTimeC].push_back(tc);
+    if (mon_buf_[kMonTimeS].size() >= 256 || saturated || done()) flush_monitor();
     return saturated ? kErrSaturated : kOk;
 }
 
@@ -1390,10 +1485,14 @@ void EulerSim::ens_bind(float* sample_out, const float2* spec_v, float2* spec4, 
 
 void EulerSim::flush_monitor()
 {
-    static const char* names[4] = {"Time_s", "Error_incompressibility", "Map_gaps", "Map_counter"};
-    if (mon_buf_[0].empty()) return;
+    static const char* names[kMonSeries] = {"Time_s", "Error_incompressibility", "Error_incompressibility_forward",
+                                            "Error_invertibility", "Map_gaps", "Map_counter", "Time_c"};
+    bool any = false;
+    for (auto& b : mon_buf_) any = any || !b.empty();
+    if (!any) return;
     std::string dir = run_dir(s) + "/Monitoring_data/";
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < kMonSeries; ++k) {
+        if (mon_buf_[k].empty()) continue;
         append_f64(dir + names[k] + ".data", mon_buf_[k].data(), mon_buf_[k].size());
         mon_buf_[k].clear();
     }
@@ -1523,11 +1622,11 @@ int EulerSim::ens_end()
     if ((rc = advect_particles(lcl))) return rc;
     if ((rc = save_functions(t_vec_[lcl + 1], ens_dt_))) return rc;
     loop_ctr_++;
-    mon_buf_[0].push_back(t_vec_[lcl + 1]);
-    mon_buf_[1].push_back(e_inc_);
-    mon_buf_[2].push_back(ens_gap_);
-    mon_buf_[3].push_back(ens_counter_);
-    if (mon_buf_[0].size() >= 1024) flush_monitor();
+    mon_buf_[kMonTimeS].push_back(t_vec_[lcl + 1]);
+    mon_buf_[kMonEinc].push_back(e_inc_);
+    mon_buf_[kMonGap].push_back(ens_gap_);
+    mon_buf_[kMonCounter].push_back(ens_counter_);
+    if (mon_buf_[kMonTimeS].size() >= 1024) flush_monitor();
     return ens_saturated_ ? kErrSaturated : kOk;
 }
 
@@ -1855,6 +1954,7 @@ int EulerSim::write_time_step(double t_now, double dt_now)
     for (auto& r : s.save_computational)
         if (instant_fires(r.is_instant, r.time_start, r.time_end, r.time_step, t_now, dt_now, dt)) { fire = true; var += r.var; }
     if (!fire) return kOk;
+    if (int rc0 = ensure_vort()) return rc0;
     int rs = sync_fp64_views();
     if (rs) return rs;
     std::string tname = std::abs(t_now - kTMax) < 1 ? "final" : to_str3(t_now);
@@ -1927,6 +2027,7 @@ int EulerSim::diagnostics(double* energy, double* enstrophy, double* palinstroph
 {
     // Compute_Energy_H, Compute_Enstrophy, Compute_Palinstrophy, w max
     // (src/numerical/cmm-mesure.cu:30-89, cmm-simulation-host.cu:668-673)
+    if (int rc0 = ensure_vort()) return rc0;
     if (mixed_) CMM_LAUNCH(2, launch_energy_m(psim_[0], gp.N, red_, d_scal_ + 1, stream));
     else CMM_LAUNCH(2, launch_sumsq(psi[0] + gp.N, 2 * gp.N, red_, d_scal_ + 1, stream));
     CMM_LAUNCH(2, launch_sumsq(vort, gc.N, red_, d_scal_ + 2, stream));
@@ -2006,6 +2107,7 @@ size_t EulerSim::field_bytes(const std::string& n) const
 int EulerSim::get_field(const std::string& n, void* dst, size_t bytes)
 {
     if (!initialised_) { err = "get_field before init"; return kErrState; }
+    flush_monitor();
     int rs = sync_fp64_views();
     if (rs) return rs;
     size_t need = field_bytes(n);
@@ -2021,7 +2123,7 @@ int EulerSim::get_field(const std::string& n, void* dst, size_t bytes)
         size_t lb = sizeof(double) * 4 * gp.N;
         for (int l = 0; l < L && !rc; ++l) { rc = check(cudaMemcpyAsync(d + l * lb, psi[l], lb, cudaMemcpyDeviceToHost, stream), "get_field"); }
     }
-    else if (n == "Vorticity_W_coarse" || n == "Distribution_coarse") rc = cp(vort, bytes);
+    else if (n == "Vorticity_W_coarse" || n == "Distribution_coarse") rc = ensure_vort() ? kErrCuda : cp(vort, bytes);
     else if (n == "Vorticity_W_fine_H") rc = cp(wfine, bytes);
     else if (n == "Init_random_table") rc = cp(d_rand_, bytes);
     else if (n == "Map_ChiX_f_H_coarse") rc = cp(ChiX_f, bytes);
@@ -2063,6 +2165,7 @@ int EulerSim::get_field(const std::string& n, void* dst, size_t bytes)
 
 int EulerSim::get_scalar(const std::string& n, double* out)
 {
+    flush_monitor();
     if (n == "dt") { *out = dt; return kOk; }
     if (n == "lagrange_order") { *out = L; return kOk; }
     if (n == "stack_capacity") { *out = max_maps; return kOk; }
@@ -2074,6 +2177,7 @@ int EulerSim::get_scalar(const std::string& n, double* out)
     if (n == "e_invertibility") { *out = e_inv_; return kOk; }
     if (n == "map_gap") { *out = (loop_ctr_ - 1) - old_ctr_; return kOk; }
     if (n == "loop_ctr") { *out = loop_ctr_; return kOk; }
+    if (n == "graph_launches") { *out = (double)graph_launches_; return kOk; }
     if (n == "learned_steps") { *out = (double)learned_steps_; return kOk; }
     if (n == "cheap_steps") { *out = (double)cheap_steps_; return kOk; }
     if (n == "learned_cheaper") { *out = (double)learned_cheaper_; return kOk; }

@@ -129,6 +129,8 @@ private:
     int vort_spectrum();
     int psi_planes(float2* spec4, float* out);
     int coarse_vort();
+    int ensure_vort();           // sample the coarse vorticity if a step left it stale
+    bool vort_stale_ = false;
     int advect(const double* t, const double* dtv, int loop_ctr, int ti_num, int l_order);
     int advect_m(const double* t, const double* dtv, int loop_ctr, int ti_num, int l_order);
     int reset_map();
@@ -167,6 +169,11 @@ private:
     int check(cudaError_t e, const char* what);
     double compute_next_timestep(double t) const;
     void rotate_psi(int n);
+    void unrotate_psi(int n);
+    cudaEvent_t einc_ev_ = nullptr;    // E_inc's readback (speculative psi evaluation)
+    cudaGraphExec_t step_graph_ = nullptr;   // the captured front of a mixed Euler step
+    bool use_graphs_ = true;
+    long long graph_launches_ = 0;
     double wall() const;
 
     void ph_begin(int p);
@@ -202,8 +209,11 @@ private:
 
     // ensemble members keep their per-step Monitoring_data records (Time_s,
     // Error_incompressibility, Map_gaps, Map_counter) here and append them in blocks
-    std::vector<double> mon_buf_[4];
+    enum { kMonTimeS, kMonEinc, kMonEincF, kMonEinv, kMonGap, kMonCounter, kMonTimeC, kMonSeries };
+    std::vector<double> mon_buf_[kMonSeries];
+public:
     void flush_monitor();
+private:
     // ensemble binding
     float* ens_sample_ = nullptr;
     const float2* ens_spec_v_ = nullptr;

@@ -1436,7 +1436,7 @@ int EulerSim::step_once()
     CMM_CUDA(cudaGetLastError());
 
     // the per-step Monitoring_data records are kept in host buffers and appended in blocks
-    // (every 256 steps, at the final step, in finish and before any state is read)
+    // (every 256 steps, at the final step, when the stack saturates, in finish and on destruction)
     mon_buf_[kMonTimeS].push_back(t_vec_[lcl + 1]);
     mon_buf_[kMonEinc].push_back(e_inc_);
     if (s.forward_map) {
@@ -2107,7 +2107,6 @@ size_t EulerSim::field_bytes(const std::string& n) const
 int EulerSim::get_field(const std::string& n, void* dst, size_t bytes)
 {
     if (!initialised_) { err = "get_field before init"; return kErrState; }
-    flush_monitor();
     int rs = sync_fp64_views();
     if (rs) return rs;
     size_t need = field_bytes(n);
@@ -2165,7 +2164,6 @@ int EulerSim::get_field(const std::string& n, void* dst, size_t bytes)
 
 int EulerSim::get_scalar(const std::string& n, double* out)
 {
-    flush_monitor();
     if (n == "dt") { *out = dt; return kOk; }
     if (n == "lagrange_order") { *out = L; return kOk; }
     if (n == "stack_capacity") { *out = max_maps; return kOk; }

@@ -653,6 +653,8 @@ def run_learned(args):
                                          "max_enstrophy_rel_err": zerr(exact, plain)},
            "learned_vs_exact_mixed_max_enstrophy_rel_err": zerr(learned, exact),
            "inference_conv_gflop_per_step": px * fwd_pp / 1e9,
+           "inference": {"ms": u.time_infer(WORKLOAD["grid_coarse"], WORKLOAD["grid_coarse"]),
+                         "note": "one forward pass at 512^2 (input assembly, 14 convs, sub-pixel output)"},
            "psi_errors_along_exact_run": errs}
     print(json.dumps(out))
     shutil.rmtree(work, ignore_errors=True)
@@ -678,11 +680,9 @@ def run_learned_profile(args):
         u = m.Upsampler(blocks=LEARNED["blocks"], seed=2)
         sim.attach_upsampler(u, every=1000000, tol=1e9)
         sim.step(3)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        sim.step(4)
-        torch.cuda.synchronize()
-        print(json.dumps({"learned_steps_per_s": 4 / (time.perf_counter() - t0)}))
+        ms = u.time_infer(WORKLOAD["grid_coarse"], WORKLOAD["grid_coarse"], 20)
+        fwd_pp, _ = conv_flops_per_pixel(LEARNED["blocks"], LEARNED["channels"])
+        print(json.dumps({"inference_ms": ms, "conv_tflops": WORKLOAD["grid_coarse"] ** 2 * fwd_pp / (ms * 1e-3) / 1e12}))
     else:
         n = 128
         cli = ["workspace=%s/" % work, "sim_name=prof", "grid_coarse=%d" % n, "grid_fine=%d" % (4 * n),

@@ -37,7 +37,7 @@ EXPORTS = [
     "cmm_upsampler_get_params", "cmm_upsampler_set_params", "cmm_upsampler_get_grads", "cmm_upsampler_set_scales",
     "cmm_upsampler_get_scales", "cmm_upsampler_collect", "cmm_upsampler_dataset_size", "cmm_upsampler_train",
     "cmm_upsampler_loss_grad", "cmm_upsampler_infer", "cmm_upsampler_evaluate", "cmm_upsampler_save",
-    "cmm_upsampler_load", "cmm_attach_upsampler", "cmm_conv3x3", "cmm_conv3x3_weight_grad",
+    "cmm_upsampler_load", "cmm_attach_upsampler", "cmm_conv3x3", "cmm_conv3x3_weight_grad", "cmm_upsampler_time_infer",
 ]
 
 
@@ -131,6 +131,7 @@ def lib():
     L.cmm_upsampler_infer.argtypes = [vp, fp, ip, ip, fp]
     L.cmm_upsampler_evaluate.argtypes = [vp, vp, dp]
     L.cmm_upsampler_save.argtypes = [vp, C.c_char_p]
+    L.cmm_upsampler_time_infer.argtypes = [vp, ip, ip, ip, dp]
     L.cmm_upsampler_load.argtypes = [vp, C.c_char_p]
     L.cmm_attach_upsampler.argtypes = [vp, vp, ip, C.c_double]
     L.cmm_conv3x3.argtypes = [u16p, u16p, fp, u16p, u16p, ip, ip, ip, ip, ip, ip, fp, u16p]
@@ -480,6 +481,12 @@ class Upsampler:
         arr = (C.c_double * 6)()
         check(self.L.cmm_upsampler_evaluate(self.h, sim.h, arr))
         return dict(zip(("cheap_linf", "cheap_l2", "learned_linf", "learned_l2", "grid_linf", "grid_l2"), list(arr)))
+
+    def time_infer(self, h, w, iters=20):
+        """device milliseconds of one inference on an h x w map grid"""
+        ms = C.c_double()
+        check(self.L.cmm_upsampler_time_infer(self.h, int(h), int(w), int(iters), C.byref(ms)))
+        return ms.value
 
     def save(self, path):
         check(self.L.cmm_upsampler_save(self.h, str(path).encode()))

@@ -212,6 +212,13 @@ int cmm_upsampler_evaluate(cmm_upsampler* u, cmm_ctx* c, double* out6)
     return CMM_OK;
 }
 
+int cmm_upsampler_time_infer(cmm_upsampler* u, int h, int w, int iters, double* ms)
+{
+    if (!u || !ms) return fail(CMM_ERR_PARAM, "NULL argument");
+    if (h < 1 || w < 1 || w % cmm::lrn::kTile != 0 || iters < 1) return fail(CMM_ERR_PARAM, "bad shape or iters");
+    return up_rc(u, u->u->time_infer(h, w, iters, ms, u->stream));
+}
+
 int cmm_upsampler_save(const cmm_upsampler* u, const char* path)
 {
     if (!u || !path) return fail(CMM_ERR_PARAM, "NULL argument");

@@ -579,6 +579,35 @@ int Upsampler::infer(const float* planes4, const float* omega, int h, int w, flo
     return 0;
 }
 
+int Upsampler::time_infer(int h, int w, int iters, double* ms, cudaStream_t s)
+{
+    const long long hw = (long long)h * w;
+    float* in = nullptr;
+    float* fine = nullptr;
+    LRN_CHECK(alloc(&in, kInCh * hw), "time_infer");
+    LRN_CHECK(alloc(&fine, 4 * hw), "time_infer");
+    LRN_CHECK(cudaMemsetAsync(in, 0, sizeof(float) * kInCh * hw, s), "time_infer");
+    int rc = 0;
+    for (int i = 0; i < 2 && !rc; ++i) rc = infer(in, in + 4 * hw, h, w, fine, s);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    for (int i = 0; i < iters && !rc; ++i) rc = infer(in, in + 4 * hw, h, w, fine, s);
+    cudaEventRecord(e1, s);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float t = 0;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    release(in);
+    release(fine);
+    if (rc) return rc;
+    LRN_CHECK(e, "time_infer");
+    *ms = iters > 0 ? t / iters : 0.0;
+    return 0;
+}
+
 int Upsampler::save(const std::string& path) const
 {
     std::vector<float> p((size_t)n_params_);

@@ -149,6 +149,10 @@ public:
     // the predicted sub-grid vorticity on the psi grid (2h x 2w)
     int infer(const float* planes4, const float* omega, int h, int w, float* fine, cudaStream_t s);
 
+    // device time of one inference on an h x w map grid (iters repeats after 2 warm-ups,
+    // zero inputs: the cost does not depend on the values)
+    int time_infer(int h, int w, int iters, double* ms, cudaStream_t s);
+
     int save(const std::string& path) const;
     int load(const std::string& path);
 

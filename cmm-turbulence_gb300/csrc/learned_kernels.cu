@@ -87,18 +87,147 @@ __device__ __forceinline__ uint4 pack8(const float* f)
 // ---------------------------------------------------------------------------
 // forward / input-gradient convolution
 // ---------------------------------------------------------------------------
+// Software pipeline over the CTA's strip of rows: while one thread issues row r's MMAs into
+// accumulator r % 2, the CTA stages (cp.async) the source rows row r + 1 still lacks and then
+// drains row r - 1's accumulator (the epilogue).  Two mbarriers track the two accumulators;
+// a source row's slot is reused only after the MMAs reading it completed.
+template <int CIN, int COUT>
+__device__ __forceinline__ void conv_issue(uint32_t d_tmem, uint32_t rbase, uint32_t wbase, const int (&slot)[3])
+{
+    constexpr int C8 = CIN / 8;
+    constexpr int SLOT = C8 * kPitch * 16;
+    constexpr uint32_t idesc = tc::idesc_bf16(128, COUT);
+    uint32_t acc = 0;
+#pragma unroll
+    for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+        for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+            for (int kk = 0; kk < CIN / 16; ++kk) {
+                const uint32_t aaddr = rbase + slot[dy] * SLOT + ((2 * kk) * kPitch + dx) * 16;
+                const uint32_t baddr = wbase + ((dy * 3 + dx) * C8 + 2 * kk) * COUT * 16;
+                tc::mma_bf16(d_tmem, tc::desc_kmajor(aaddr, kPitch * 16, 128), tc::desc_kmajor(baddr, COUT * 16, 128),
+                             idesc, acc);
+                acc = 1;
+            }
+}
+
+template <int CIN>
+__device__ __forceinline__ void conv_stage(unsigned char* dst, const bf16* __restrict__ in, int src, int W, int x0)
+{
+    constexpr int C8 = CIN / 8;
+    const bf16* row = in + (long long)src * W * CIN;
+    for (int i = threadIdx.x; i < C8 * kPitch; i += 128) {
+        const int c = i % C8, p = i / C8;
+        int x = x0 - 1 + p;
+        x = x < 0 ? x + W : (x >= W ? x - W : x);
+        cp_async16(dst + (c * kPitch + p) * 16, row + (long long)x * CIN + c * 8);
+    }
+}
+
+template <int COUT>
+__device__ __forceinline__ void conv_epilogue(const ConvArgs& a, uint32_t d_tmem, int r, int x0, const float (&bias)[COUT],
+                                              bool store)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float v[COUT];
+#pragma unroll
+    for (int c = 0; c < COUT; c += 16) {
+        float t[16];
+        tc::tmem_ld16(d_tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, t);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[c + j] = t[j] + bias[c + j];
+    }
+    if (!store) return;
+    const long long pix = (long long)r * a.W + x0 + warp * 32 + lane;
+    if (a.relu) {
+#pragma unroll
+        for (int j = 0; j < COUT; ++j) v[j] = fmaxf(v[j], 0.f);
+    }
+    if (a.mask) {
+        const uint4* mp = reinterpret_cast<const uint4*>(a.mask + pix * COUT);
+#pragma unroll
+        for (int q = 0; q < COUT / 8; ++q) {
+            float m[8];
+            unpack8(mp[q], m);
+#pragma unroll
+            for (int e = 0; e < 8; ++e) v[8 * q + e] = m[e] > 0.f ? v[8 * q + e] : 0.f;
+        }
+    }
+    if (a.res) {
+        const uint4* rp = reinterpret_cast<const uint4*>(a.res + pix * COUT);
+#pragma unroll
+        for (int q = 0; q < COUT / 8; ++q) {
+            float m[8];
+            unpack8(rp[q], m);
+#pragma unroll
+            for (int e = 0; e < 8; ++e) v[8 * q + e] += m[e];
+        }
+    }
+    if (a.out) {
+        uint4* op = reinterpret_cast<uint4*>(a.out + pix * COUT);
+#pragma unroll
+        for (int q = 0; q < COUT / 8; ++q) op[q] = pack8(v + 8 * q);
+    }
+    if (a.out_f32) {
+        float4* op = reinterpret_cast<float4*>(a.out_f32 + pix * COUT);
+#pragma unroll
+        for (int q = 0; q < COUT / 4; ++q) op[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    }
+}
+
+// slots for the source rows of output row r: rows already staged keep their slot; missing
+// rows go to slots outside `busy` (the slots MMAs in flight read) and not holding a row r
+// needs.  Returns the number of rows it could not place (0 on success).  Uniform over the CTA.
+template <int CIN>
+__device__ __forceinline__ int conv_place(const ConvArgs& a, int r, int x0, unsigned char* sr, int (&tag)[4],
+                                          const int (&busy)[3], int nbusy, int (&slot)[3])
+{
+    constexpr int SLOT = (CIN / 8) * kPitch * 16;
+    int src[3];
+#pragma unroll
+    for (int dy = 0; dy < 3; ++dy) {
+        src[dy] = src_row(r, dy - 1, a.H);
+        slot[dy] = -1;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (tag[k] == src[dy]) slot[dy] = k;
+    }
+    int unplaced = 0;
+#pragma unroll
+    for (int dy = 0; dy < 3; ++dy) {
+        if (slot[dy] >= 0) continue;
+        int s = -1;
+        for (int k = 3; k >= 0; --k) {
+            bool used = false;
+            for (int e = 0; e < nbusy; ++e) used = used || busy[e] == k;
+            for (int e = 0; e < 3; ++e) used = used || slot[e] == k || (tag[k] >= 0 && tag[k] == src[e]);
+            if (!used) s = k;
+        }
+        if (s < 0) {
+            ++unplaced;
+            continue;
+        }
+        conv_stage<CIN>(sr + s * SLOT, a.in, src[dy], a.W, x0);
+        tag[s] = src[dy];
+#pragma unroll
+        for (int e = 0; e < 3; ++e)
+            if (src[e] == src[dy]) slot[e] = s;
+    }
+    return unplaced;
+}
+
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a)
 {
     constexpr int C8 = CIN / 8;
-    constexpr int SLOT = C8 * kPitch * 16;
     constexpr int WB = 9 * C8 * COUT * 16;
     extern __shared__ __align__(128) unsigned char sm[];
-    __shared__ uint64_t bar;
+    __shared__ uint64_t bar[2];
     __shared__ uint32_t tslot;
     unsigned char* sw = sm;
     unsigned char* sr = sm + WB;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tid = threadIdx.x, warp = tid >> 5;
     const int segs = a.W / kTile;
     const int seg = blockIdx.x % segs;
     const int r0 = (blockIdx.x / segs) * a.rows_per_cta;
@@ -109,134 +238,69 @@ __global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a)
     for (int i = tid; i < WB / 16; i += 128)
         cp_async16(sw + 16 * i, reinterpret_cast<const unsigned char*>(a.wt) + 16 * (long long)i);
     if (warp == 0) {
-        tc::tmem_alloc(&tslot, 32);
+        tc::tmem_alloc(&tslot, 64);   // two accumulators of 32 columns
         tc::tmem_relinquish();
     }
     if (tid == 0) {
-        tc::mbar_init(&bar, 1);
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
         tc::mbar_fence_init();
     }
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    const uint32_t tmem = tslot;
-
     float bias[COUT];
 #pragma unroll
     for (int j = 0; j < COUT; ++j) bias[j] = a.bias ? a.bias[j] : 0.f;
 
     int tag[4] = {-1, -1, -1, -1};
-    uint32_t phase = 0;
-    for (int r = r0; r < r1; ++r) {
-        int slot_of[3];
-#pragma unroll
-        for (int dy = 0; dy < 3; ++dy) {
-            const int src = src_row(r, dy - 1, a.H);
-            slot_of[dy] = -1;
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (tag[k] == src) slot_of[dy] = k;
-        }
-#pragma unroll
-        for (int dy = 0; dy < 3; ++dy) {
-            if (slot_of[dy] >= 0) continue;
-            const int src = src_row(r, dy - 1, a.H);
-            int s = 0;
-            for (int k = 3; k >= 0; --k)
-                if (k != slot_of[0] && k != slot_of[1] && k != slot_of[2]) s = k;
-            unsigned char* dst = sr + s * SLOT;
-            const bf16* row = a.in + (long long)src * a.W * CIN;
-            for (int i = tid; i < C8 * kPitch; i += 128) {
-                const int c = i % C8, p = i / C8;
-                int x = x0 - 1 + p;
-                x = x < 0 ? x + a.W : (x >= a.W ? x - a.W : x);
-                cp_async16(dst + (c * kPitch + p) * 16, row + (long long)x * CIN + c * 8);
-            }
-            tag[s] = src;
-            slot_of[dy] = s;
-        }
+    int cur[3], nxt[3];
+    const int none[3] = {-1, -1, -1};
+    conv_place<CIN>(a, r0, x0, sr, tag, none, 0, cur);   // four free slots: always places all
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tslot;
+    const uint32_t wbase = tc::smem_u32(sw), rbase = tc::smem_u32(sr);
+
+    bool ok = true;
+    int it = 0;
+    for (int r = r0; r < r1; ++r, ++it) {
+        // this row's source rows (staged in the previous iteration or above) visible to the MMAs
         cp_async_wait_all();
         tc::fence_smem_to_async();
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
         if (tid == 0) {
-            const uint32_t wbase = tc::smem_u32(sw), rbase = tc::smem_u32(sr);
-            constexpr uint32_t idesc = tc::idesc_bf16(128, COUT);
-            uint32_t acc = 0;
-#pragma unroll
-            for (int dy = 0; dy < 3; ++dy)
-#pragma unroll
-                for (int dx = 0; dx < 3; ++dx)
-#pragma unroll
-                    for (int kk = 0; kk < CIN / 16; ++kk) {
-                        const uint32_t aaddr = rbase + slot_of[dy] * SLOT + ((2 * kk) * kPitch + dx) * 16;
-                        const uint32_t baddr = wbase + ((dy * 3 + dx) * C8 + 2 * kk) * COUT * 16;
-                        tc::mma_bf16(tmem, tc::desc_kmajor(aaddr, kPitch * 16, 128),
-                                     tc::desc_kmajor(baddr, COUT * 16, 128), idesc, acc);
-                        acc = 1;
-                    }
-            tc::mma_commit(&bar);
+            conv_issue<CIN, COUT>(tmem + (uint32_t)((it & 1) * 32), rbase, wbase, cur);
+            tc::mma_commit(&bar[it & 1]);
         }
         __syncwarp();
-        const bool ok = __all_sync(0xffffffffu, tc::mbar_wait(&bar, phase, kMaxPolls));
-        phase ^= 1u;
+        // the previous row's MMAs: their accumulator is drained below, their slots free up
+        if (it > 0) ok = ok && tc::mbar_wait(&bar[(it - 1) & 1], ((it - 1) >> 1) & 1, kMaxPolls);
+        if (r + 1 < r1) {
+            if (conv_place<CIN>(a, r + 1, x0, sr, tag, cur, 3, nxt) > 0) {
+                // a new image starts: the rows it needs outnumber the free slots; wait for this
+                // row's MMAs, after which only the rows row r + 1 needs are kept
+                ok = ok && tc::mbar_wait(&bar[it & 1], (it >> 1) & 1, kMaxPolls);
+                conv_place<CIN>(a, r + 1, x0, sr, tag, none, 0, nxt);
+            }
+        }
+        ok = __all_sync(0xffffffffu, ok);
         tc::fence_after_sync();
-
-        // epilogue: this thread's pixel, COUT accumulators
-        float v[COUT];
-#pragma unroll
-        for (int c = 0; c < COUT; c += 16) {
-            float t[16];
-            tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, t);
-#pragma unroll
-            for (int j = 0; j < 16; ++j) v[c + j] = t[j] + bias[c + j];
-        }
-        const long long pix = (long long)r * a.W + x0 + warp * 32 + lane;
-        if (ok) {
-            if (a.relu) {
-#pragma unroll
-                for (int j = 0; j < COUT; ++j) v[j] = fmaxf(v[j], 0.f);
-            }
-            if (a.mask) {
-                const uint4* mp = reinterpret_cast<const uint4*>(a.mask + pix * COUT);
-#pragma unroll
-                for (int q = 0; q < COUT / 8; ++q) {
-                    float m[8];
-                    unpack8(mp[q], m);
-#pragma unroll
-                    for (int e = 0; e < 8; ++e) v[8 * q + e] = m[e] > 0.f ? v[8 * q + e] : 0.f;
-                }
-            }
-            if (a.res) {
-                const uint4* rp = reinterpret_cast<const uint4*>(a.res + pix * COUT);
-#pragma unroll
-                for (int q = 0; q < COUT / 8; ++q) {
-                    float m[8];
-                    unpack8(rp[q], m);
-#pragma unroll
-                    for (int e = 0; e < 8; ++e) v[8 * q + e] += m[e];
-                }
-            }
-            if (a.out) {
-                uint4* op = reinterpret_cast<uint4*>(a.out + pix * COUT);
-#pragma unroll
-                for (int q = 0; q < COUT / 8; ++q) op[q] = pack8(v + 8 * q);
-            }
-            if (a.out_f32) {
-                float4* op = reinterpret_cast<float4*>(a.out_f32 + pix * COUT);
-#pragma unroll
-                for (int q = 0; q < COUT / 4; ++q) op[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-            }
-        }
+        if (it > 0) conv_epilogue<COUT>(a, tmem + (uint32_t)(((it - 1) & 1) * 32), r - 1, x0, bias, ok);
         tc::fence_before_sync();
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0 && a.status) atomicExch(a.status, 1);
-            break;
-        }
+        if (__syncthreads_or(!ok)) break;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) cur[d] = nxt[d];
     }
-    __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, 32);
+    if (ok && it > 0) {
+        ok = __all_sync(0xffffffffu, tc::mbar_wait(&bar[(it - 1) & 1], ((it - 1) >> 1) & 1, kMaxPolls));
+        tc::fence_after_sync();
+        conv_epilogue<COUT>(a, tmem + (uint32_t)(((it - 1) & 1) * 32), r1 - 1, x0, bias, ok);
+    }
+    cp_async_wait_all();
+    tc::fence_before_sync();
+    if (__syncthreads_or(!ok) && tid == 0 && a.status) atomicExch(a.status, 1);
+    if (warp == 0) tc::tmem_dealloc(tmem, 64);
 }
 
 // ---------------------------------------------------------------------------
@@ -710,9 +774,10 @@ cudaError_t dw_launch(const DwArgs& a, int grid, cudaStream_t s)
 
 int conv_rows_per_cta(int rows, int W)
 {
+    // about two pipelined CTAs per SM, at least four rows each
     const long long tiles = (long long)rows * (W / kTile);
-    const long long target = 152 * 4;
-    return (int)std::max(2ll, (tiles + target - 1) / target);
+    const long long target = 152 * 2;
+    return (int)std::max(4ll, (tiles + target - 1) / target);
 }
 
 int conv_grid(int rows, int W, int rows_per_cta)

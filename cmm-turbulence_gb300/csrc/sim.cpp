@@ -156,6 +156,10 @@ int EulerSim::alloc()
         return kErrParam;
     }
     if (s.map_update_order_num < 0) { err = "unknown map_update_order " + s.map_update_order; return kErrParam; }
+    if (s.scalar_discrete && !s.initial_discrete) {
+        err = "scalar_discrete samples the discrete initial vorticity (as the reference does): it needs initial_discrete=1";
+        return kErrUnsupported;
+    }
     if (s.forward_map && s.precision == "mixed") {
         err = "forward_map is built for the plain FP64 form (precision=fp64)";
         return kErrUnsupported;
@@ -523,6 +527,21 @@ int EulerSim::psi_planes(float2* spec4, float* out)
     // the four Hermite spectra (gp layout) -> the planes on the psi grid
     CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4), out));
     return kOk;
+}
+
+void EulerSim::scalar_source(InitSource& src) const
+{
+    // the passive scalar's initial field: the analytic scalar_name, or with scalar_discrete
+    // the discrete initial *vorticity* (k_h_sample_from_init on Vort_discrete_init,
+    // cmm-simulation-host.cu:803-805, 1160-1162: the reference has no discrete scalar input)
+    if (s.scalar_discrete) {
+        src.kind = 3;
+        src.discrete = wdisc;
+        src.gd = gd;
+    } else {
+        src.kind = 1;
+        src.ic_num = s.scalar_num;
+    }
 }
 
 int EulerSim::ensure_vort()
@@ -1742,8 +1761,7 @@ int EulerSim::sample_outputs(double t_now, double dt_now)
         src.params = d_params_;
         src.rand_table = d_rand_;
         if (has(var, "Scalar") || has(var, "Theta") || all) {
-            src.kind = 1;
-            src.ic_num = s.scalar_num;
+            scalar_source(src);
             CMM_LAUNCH(1, launch_eval_init(X, Y, gs.N, src, S, stream));
             if ((rc = out("Scalar_Theta", S))) return rc;
             // Compute_avg reduces with thrust::maximum: hx hy max(0, max theta) (cmm-mesure.cu:226-229)
@@ -1890,8 +1908,7 @@ int EulerSim::zoom_outputs(double t_now, double dt_now)
             src.discrete = wdisc;
             src.gd = gd;
             if (has(var, "Scalar") || has(var, "Theta") || all) {
-                src.kind = 1;
-                src.ic_num = s.scalar_num;
+                scalar_source(src);
                 CMM_LAUNCH(1, launch_eval_init(X, Y, gz.N, src, V, stream));
                 if ((rc = out("Scalar_Theta", V))) return rc;
             }

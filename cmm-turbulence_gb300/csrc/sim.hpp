@@ -130,6 +130,7 @@ private:
     int psi_planes(float2* spec4, float* out);
     int coarse_vort();
     int ensure_vort();           // sample the coarse vorticity if a step left it stale
+    void scalar_source(InitSource& src) const;
     bool vort_stale_ = false;
     int advect(const double* t, const double* dtv, int loop_ctr, int ti_num, int l_order);
     int advect_m(const double* t, const double* dtv, int loop_ctr, int ti_num, int l_order);

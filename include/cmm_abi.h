@@ -309,6 +309,8 @@ int cmm_upsampler_infer(cmm_upsampler* u, const float* inputs, int h, int w, flo
  * and the psi of omega sampled exactly on the psi grid (the best a network can reach):
  * out6 = {cheap Linf, cheap L2, learned Linf, learned L2, psi-grid Linf, psi-grid L2} */
 int cmm_upsampler_evaluate(cmm_upsampler* u, cmm_ctx* c, double* out6);
+/* device milliseconds of one inference on an h x w map grid (mean of iters after 2 warm-ups) */
+int cmm_upsampler_time_infer(cmm_upsampler* u, int h, int w, int iters, double* ms);
 int cmm_upsampler_save(const cmm_upsampler* u, const char* path);
 int cmm_upsampler_load(cmm_upsampler* u, const char* path);
 /* attach (NULL detaches) after cmm_init; the upsampler must outlive the attachment */

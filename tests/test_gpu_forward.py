@@ -98,3 +98,47 @@ def test_forward_map_is_plain_fp64_only(tmp_path):
     with pytest.raises(m.CmmError) as e:
         sim.init()
     assert e.value.code == m.CMM_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_discrete_scalar_samples_the_discrete_initial_vorticity(tmp_path, precision):
+    """scalar_discrete=1: the reference's k_h_sample_from_init reads Vort_discrete_init for
+    the passive scalar (cmm-simulation-host.cu:803-805), so on a sample grid the scalar equals
+    the composed discrete initial vorticity, i.e. the sampled vorticity, value for value;
+    without a discrete initial field the option is refused."""
+    m = cmm()
+    n = 64
+    rng = np.random.default_rng(5)
+    k = np.fft.rfftfreq(4 * n, 1.0 / (4 * n))
+    w = np.fft.irfft2(np.exp(-((k[None, :] ** 2 + np.fft.fftfreq(4 * n, 1.0 / (4 * n))[:, None] ** 2) / 40.0))
+                      * np.exp(2j * np.pi * rng.uniform(size=(4 * n, 2 * n + 1))), s=(4 * n, 4 * n)) * 1e3
+    lines = ["CMM Parameter file", "param_version\t=\t3", ""]
+    kv = [("sim_name", "dscal"), ("grid_coarse", n), ("grid_fine", 4 * n), ("grid_vort", 4 * n), ("grid_psi", 2 * n),
+          ("set_dt_by_steps", 1), ("steps_per_sec", 32), ("final_time", 0.5), ("initial_discrete", 1),
+          ("initial_discrete_grid", 4 * n), ("incomp_threshold", 1e-4), ("freq_cut_psi", n // 2),
+          ("scalar_discrete", 1), ("save_computational_num", 0), ("save_zoom_num", 0), ("particles_advected_num", 0),
+          ("save_map_stack", 0), ("verbose", 0), ("precision", precision), ("save_sample_num", 1)]
+    lines += ["%s\t=\t%s" % (a, b) for a, b in kv]
+    lines.append("save_sample\t=\t{is_instant=0,time_start=0,time_end=0.5,time_step=0.25,var=Vorticity Scalar,grid=64}")
+    pf = tmp_path / "p.txt"
+    pf.write_text("\n".join(lines) + "\n")
+    sim = m.Simulation(["param_file=%s" % pf, "workspace=%s/" % tmp_path])
+    sim.set_initial_discrete(np.ascontiguousarray(w))
+    sim.init()
+    sim.run()
+    run = os.path.join(str(tmp_path), "data", sim.file_name(), "Time_data")
+    found = 0
+    for d in sorted(os.listdir(run)):
+        sc = os.path.join(run, d, "Scalar_Theta_64.data")
+        vo = os.path.join(run, d, "Vorticity_W_64.data")
+        if os.path.exists(sc) and os.path.exists(vo):
+            a, b = np.fromfile(sc, dtype="<f8"), np.fromfile(vo, dtype="<f8")
+            assert a.size == 64 * 64 and np.array_equal(a, b), d
+            found += 1
+    assert found >= 2
+    sim.close()
+    bad = m.Simulation(["workspace=%s/" % tmp_path, "sim_name=dscal_bad", "scalar_discrete=1", "initial_discrete=0",
+                        "grid_coarse=32", "grid_fine=64", "grid_vort=64", "grid_psi=32", "verbose=0"])
+    with pytest.raises(m.CmmError) as e:
+        bad.init()
+    assert e.value.code == m.CMM_ERR_UNSUPPORTED

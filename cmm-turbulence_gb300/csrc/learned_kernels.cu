@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "learned.hpp"
 #include "tc_sm100.cuh"
@@ -777,6 +778,7 @@ int conv_rows_per_cta(int rows, int W)
     // about two pipelined CTAs per SM, at least four rows each
     const long long tiles = (long long)rows * (W / kTile);
     const long long target = 152 * 2;
+    if (const char* e = getenv("CMM_CONV_ROWS")) return atoi(e);
     return (int)std::max(4ll, (tiles + target - 1) / target);
 }
 

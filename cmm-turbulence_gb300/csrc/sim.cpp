@@ -405,7 +405,8 @@ void EulerSim::release()
     for (auto& p : smp_) { f(p); p = nullptr; }
     for (auto& p : smp_c_) { f(p); p = nullptr; }
     destroy_plans(ps_);
-    smp_n_ = smp_plan_n_ = 0;
+    destroy_vlasov_plans(vps_);
+    smp_n_ = smp_plan_n_ = vsmp_plan_n_ = 0;
     f(mapm_); f(mapm_new_); f(psiA_); f(psiB_); f(psiP_); f(wfm_); f(stackm_); f(realf_); f(specf_); f(spec4f_);
     psiP_ = nullptr;
     fused_ = false;
@@ -1700,7 +1701,7 @@ int EulerSim::sample_outputs(double t_now, double dt_now)
     // sample_compute_and_write, backward-map part (src/simulation/cmm-simulation-host.cu:706-893):
     // the full map on the sample grid, scalar and vorticity there, their spectral
     // derivatives, psi and velocity, the sample-grid conservation values
-    if (vlasov_) return kOk;
+    if (vlasov_) return vlasov_sample_outputs(t_now, dt_now);
     for (auto& r : s.save_sample) {
         if (r.grid <= 0 || !instant_fires(r.is_instant, r.time_start, r.time_end, r.time_step, t_now, dt_now, dt)) continue;
         const int n = r.grid;
@@ -1812,6 +1813,102 @@ int EulerSim::sample_outputs(double t_now, double dt_now)
             log_.push("Processed sample data on grid " + ns + ", Cons : Energ = " + to_str_prec(mes[0], 8) +
                       " \t Enstr = " + to_str_prec(mes[1], 8) + " \t Palinstr = " + to_str_prec(mes[2], 8) +
                       " \t Wmax = " + to_str_prec(mes[3], 8));
+    }
+    return kOk;
+}
+
+int EulerSim::vlasov_sample_outputs(double t_now, double dt_now)
+{
+    // sample_compute_and_write_vlasov, backward-map part (cmm-simulation-host.cu:898-1030): the
+    // full map and the distribution function on the sample grid, its kinetic energy, momentum
+    // and mass there (Compute_Kinetic_Energy / _Momentum / _Mass, cmm-mesure.cu:97-183), the
+    // field e = d phi / dx of calc_phi on the sample grid itself (v-integral, 1D inverse
+    // Laplacian, 1D derivative: cmm-simulation-host.cu:436-471, 1006-1009) and its potential
+    // energy, and the four mode amplitudes of the run's own field (Compute_kth_Mode on psi_x
+    // row 0).  The reference writes its sample buffer as Stream_function_Psi after those in-place
+    // steps: e in the first n entries, the distribution from entry N / 8 on, left-over scratch
+    // between (written here as 0).
+    for (size_t i_save = 0; i_save < s.save_sample.size(); ++i_save) {
+        auto& r = s.save_sample[i_save];
+        if (r.grid <= 0 || !instant_fires(r.is_instant, r.time_start, r.time_end, r.time_step, t_now, dt_now, dt)) continue;
+        const int n = r.grid;
+        Grid gs = make_grid(n, n, s.domain_bounds);
+        int rc;
+        if ((rc = reserve_sample_buffers(n))) return rc;
+        if (n != vsmp_plan_n_) {
+            destroy_vlasov_plans(vps_);
+            vsmp_plan_n_ = 0;
+            if (!make_vlasov_plans(vps_, gs, gs, stream)) { err = "cuFFT 1D plan creation failed (sample grid)"; return kErrCuda; }
+            vsmp_plan_n_ = n;
+        }
+        double *X = smp_[0], *Y = smp_[1], *E = smp_[2], *F = smp_[3], *P = smp_[4], *T = smp_[5];
+        double2 *F0 = smp_c_[0], *F1 = smp_c_[1];
+        const std::string ns = std::to_string(n), var = r.var;
+        const bool all = has(var, "All"), dbg = s.verbose >= 4;
+        const std::string tname = std::abs(t_now - kTMax) < 1 ? "final" : to_str3(t_now);
+        const std::string sub = "/Time_data/Time_" + tname, mdir = run_dir(s) + "/Monitoring_data/";
+        if (dbg) append_f64(mdir + "Debug_globals/Time_s_" + ns + ".data", &t_now, 1);
+        else make_dir(run_dir(s) + sub);
+        auto out = [&](const std::string& name, const double* v) {
+            return dbg ? debug_globals(name + "_" + ns, v, gs.N, true, gs) : write_field(sub, name + "_" + ns, v, gs.N);
+        };
+        if (s.forward_map && (has(var, "Map_f") || has(var, "Chi_f") || all)) {
+            CMM_LAUNCH(1, launch_compose_fwd(gc, gs, ChiX_f, ChiY_f, stack_f, n_maps_f_, X, Y, stream));
+            if ((rc = out("Map_ChiX_f", X)) || (rc = out("Map_ChiY_f", Y))) return rc;
+        }
+        if (mixed_) CMM_LAUNCH(1, launch_compose_pos_m(gc, gs, mapm_, stackm_, n_maps_, X, Y, stream));
+        else CMM_LAUNCH(1, launch_compose_pos(gc, gs, ChiX, ChiY, stack, n_maps_, X, Y, stream));
+        if (has(var, "Map_b") || has(var, "Chi_b") || all)
+            if ((rc = out("Map_ChiX", X)) || (rc = out("Map_ChiY", Y))) return rc;
+        InitSource src{};
+        src.kind = s.initial_discrete ? 3 : 2;
+        src.ic_num = s.initial_condition_num;
+        src.discrete = wdisc;
+        src.gd = gd;
+        src.params = d_params_;
+        src.rand_table = d_rand_;
+        CMM_LAUNCH(1, launch_eval_init(X, Y, gs.N, src, F, stream));
+        if (has(var, "Dist") || has(var, "F") || all)
+            if ((rc = out("Distribution_F", F))) return rc;
+        // moments of f on the sample grid -> d_scal_[0..2]
+        CMM_LAUNCH(2, launch_vlasov_moments(F, gs, red_, d_scal_, stream));
+        // e = d phi / dx from f on the sample grid: rho (partials in T) -> 1D spectra -> E
+        CMM_LAUNCH(2, launch_vlasov_rho(F, nullptr, gs, T, P, stream));
+        CMM_FFT(cufftExecD2Z(vps_.d2z_v, P, reinterpret_cast<cufftDoubleComplex*>(F0)));
+        CMM_LAUNCH(1, launch_vlasov_phi_spec(F0, gs, gs, F1, reinterpret_cast<double2*>(T), stream));
+        CMM_FFT(cufftExecZ2D(vps_.z2d_p, reinterpret_cast<cufftDoubleComplex*>(T), E));
+        CMM_LAUNCH(2, launch_sumsq(E, n, red_, d_scal_ + 3, stream));
+        // mode amplitudes of the run's field phi' (psi_x row 0)
+        CMM_CUDA(cudaMemcpyAsync(real_buf_, phi_lv_[0] + gp.NX, sizeof(double) * gp.NX, cudaMemcpyDeviceToDevice, stream));
+        CMM_FFT(cufftExecD2Z(vp_.d2z_p, real_buf_, vl_c_[0]));
+        CMM_LAUNCH(1, launch_vlasov_modes(vl_c_[0], gp.NX, gp.NX_fft, d_scal_ + 4, stream));
+        if (has(var, "Stream") || has(var, "Psi") || all) {
+            const long long tail = std::max<long long>(gs.N / 8, (long long)n + 2);
+            CMM_CUDA(cudaMemsetAsync(P, 0, sizeof(double) * gs.N, stream));
+            CMM_CUDA(cudaMemcpyAsync(P, E, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
+            if (tail < gs.N)
+                CMM_CUDA(cudaMemcpyAsync(P + tail, F + tail, sizeof(double) * (gs.N - tail), cudaMemcpyDeviceToDevice,
+                                         stream));
+            if ((rc = out("Stream_function_Psi", P))) return rc;
+        }
+        CMM_CUDA(cudaMemcpyAsync(h_scal_, d_scal_, sizeof(double) * 8, cudaMemcpyDeviceToHost, stream));
+        CMM_CUDA(cudaStreamSynchronize(stream));
+        const double hh = gs.hx * gs.hy;
+        double mes[9];
+        mes[1] = 0.5 * hh * h_scal_[2];
+        mes[2] = 0.5 * gs.hx * h_scal_[3];
+        mes[0] = mes[1] + mes[2];
+        mes[3] = hh * h_scal_[0];
+        mes[4] = hh * h_scal_[1];
+        for (int k = 0; k < 4; ++k) mes[5 + k] = h_scal_[4 + k];
+        static const char* names[9] = {"Etot", "Ekin", "Epot", "Mass", "Momentum", "Emode1", "Emode2", "Emode3", "Emode4"};
+        append_f64(mdir + "Mesure/Time_s_" + ns + ".data", &t_now, 1);
+        for (int k = 0; k < 9; ++k) append_f64(mdir + "Mesure/" + names[k] + "_" + ns + ".data", &mes[k], 1);
+        if (s.verbose >= 3)
+            log_.push("Saved sample data " + std::to_string(i_save + 1) + " on grid " + ns + ", Cons : Etot = " +
+                      to_str_prec(mes[0], 8) + " \t Momenta = " + to_str_prec(mes[4], 8) + " \t Ekin = " +
+                      to_str_prec(mes[1], 8) + " \t Epot = " + to_str_prec(mes[2], 8) + " \t Mass = " +
+                      to_str_prec(mes[3], 8));
     }
     return kOk;
 }

@@ -154,6 +154,7 @@ private:
     int write_particles_state();
     int restart_from_map_stack();      // the restart branch of init (cmm-euler2d.cu:634-685)
     int sample_outputs(double t_now, double dt_now);   // sampled outputs on user grids
+    int vlasov_sample_outputs(double t_now, double dt_now);   // their Vlasov-Poisson form
     int zoom_outputs(double t_now, double dt_now);     // zoom windows (compute_zoom)
     int reserve_sample_buffers(int n);                 // smp_ / smp_c_ for an n x n grid
     // forwarded particles mapped on a frame, raw files under sub for the sets var names
@@ -256,6 +257,8 @@ private:
     // Vlasov-Poisson (simulation_type cmm_vlasov_poisson_1d)
     bool vlasov_ = false;
     VlasovPlans vp_;
+    VlasovPlans vps_;          // 1D plans of the Vlasov sample grid's length
+    int vsmp_plan_n_ = 0;
     double* phi_lv_[kMaxLagrange] = {nullptr, nullptr, nullptr, nullptr};   // per psi level: phi (NX), phi' (NX)
     double* vl_h_ = nullptr;         // h(v) (NY), h'(v) (NY) on the psi grid
     double* vl_rho_ = nullptr;       // rho - 1 on the vort grid's x-nodes

@@ -245,6 +245,10 @@ void og_state_sample(const og_state* st, int n_sample, int scalar_num, double* o
  * bounds4 = (x_min, x_max, y_min, y_max): out = 6 planes of n*n: map X, map Y, scalar,
  * vorticity, distribution function, psi level 0 at the window points */
 void og_zoom_fields(const og_state_view* st, int n, const double* bounds4, int scalar_num, double* out);
+/* Vlasov sampled outputs on gs: 4 planes (map x, map y, distribution, stream) and
+ * {Etot, Ekin, Epot, Mass, Momentum, Emode1..4} */
+void og_vlasov_sample_fields(const og_state_view* st, const og_grid* gs, double* out, double* mes);
+void og_state_vlasov_sample(const og_state* st, int n_sample, double* out, double* mes);
 void og_state_zoom(const og_state* st, int n, const double* bounds4, int scalar_num, double* out);
 
 /* ψ_x, ψ_y at particle positions (k_h_sample_points_dxdy, cmm-simulation-kernel.cu:138-155) */

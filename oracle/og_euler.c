@@ -1233,6 +1233,14 @@ void og_state_sample(const og_state* st, int n_sample, int scalar_num, double* o
     og_sample_fields(&v, &gs, scalar_num, out, mes);
 }
 
+void og_state_vlasov_sample(const og_state* st, int n_sample, double* out, double* mes)
+{
+    og_grid gs;
+    og_grid_fill(&gs, n_sample, n_sample, st->gc.bounds);
+    og_state_view v = state_view(st);
+    og_vlasov_sample_fields(&v, &gs, out, mes);
+}
+
 void og_state_zoom(const og_state* st, int n, const double* bounds4, int scalar_num, double* out)
 {
     og_state_view v = state_view(st);

@@ -149,3 +149,77 @@ void og_zoom_fields(const og_state_view* st, int n, const double* bounds4, int s
     }
     free(xy);
 }
+
+/* sample_compute_and_write_vlasov, backward-map part (src/simulation/cmm-simulation-host.cu:898-1030)
+ * on the n x n sample grid gs: the full backward map through the stack, the distribution
+ * function there (k_h_sample_from_init with var 2: the Vlasov formula of the run's
+ * initial-condition number, or the discrete initial field), and from it
+ *   Ekin = hx hy / 2 sum f v^2, Momentum = hx hy sum f v, Mass = hx hy sum f
+ * (cmm-mesure.cu:97-183, v = bounds[2] + iY hy), the field e = d phi / dx of calc_phi on
+ * the sample grid itself (integral_v, solve_1D_laplace, k_fft_dx_h_1D with the Nyquist
+ * mode kept, a 1D Z2D of length n: cmm-simulation-host.cu:436-471) and
+ * Epot = hx / 2 sum e^2; the four mode amplitudes come from the run's psi (Compute_kth_Mode
+ * on psi_x row 0).  The reference writes its sample buffer as Stream_function_Psi after
+ * those in-place steps: e in its first n entries, the distribution from entry N / 8 on
+ * (a copy of N bytes of the spectrum sits before it, left-over scratch past the
+ * spectrum); here the entries between are 0.
+ * out: 4 planes of N (map x, map y, distribution, stream); mes = {Etot, Ekin, Epot, Mass,
+ * Momentum, Emode1..4}. */
+void og_vlasov_sample_fields(const og_state_view* st, const og_grid* gs, double* out, double* mes)
+{
+    const og_grid* gm = st->gc;
+    long N = gs->N;
+    int n = gs->NX;
+    double* xy = (double*)malloc(sizeof(double) * 2 * N);
+    og_sample_map_compact(st->ChiX, st->ChiY, xy, gm, gs);
+    for (int i = st->n_maps - 1; i >= 0; i--)
+        og_apply_map_compact(st->stackX + 4 * gm->N * (size_t)i, st->stackY + 4 * gm->N * (size_t)i, xy, gm, gs);
+    double *mapx = out, *mapy = out + N, *f = out + 2 * N, *stream = out + 3 * N;
+    for (long i = 0; i < N; ++i) {
+        double x = xy[2 * i], y = xy[2 * i + 1];
+        mapx[i] = x;
+        mapy[i] = y;
+        f[i] = st->discrete ? og_hermite_interpolate_2D(st->discrete, x, y, st->gd) : og_init_distribution(x, y, st->ic_num);
+    }
+    free(xy);
+    double ekin = 0, mom = 0, mass = 0;
+    for (int iY = 0; iY < gs->NY; ++iY) {
+        double v = gs->bounds[2] + iY * gs->hy;
+        for (int iX = 0; iX < n; ++iX) {
+            double fv = f[(long)iY * n + iX];
+            ekin += v * v * fv;
+            mom += v * fv;
+            mass += fv;
+        }
+    }
+    double hh = gs->hx * gs->hy;
+    double* rho = (double*)malloc(sizeof(double) * n);
+    og_integral_v(f, rho, n, gs->NY, gs->hy);
+    og_grid g1;
+    og_grid_fill(&g1, n, 1, gs->bounds);
+    double* c = (double*)malloc(sizeof(double) * 2 * g1.NX_fft);
+    double* d = (double*)malloc(sizeof(double) * 2 * g1.NX_fft);
+    og_fft_d2z(&g1, rho, c);
+    d[0] = d[1] = 0.0;
+    for (int i = 1; i < g1.NX_fft; ++i) {
+        double kx = OG_TWO_PI_S / (gs->hx * n) * (i - (i > n / 2) * n);
+        double re = c[2 * i] / (double)n / (kx * kx), im = c[2 * i + 1] / (double)n / (kx * kx);
+        d[2 * i] = -im * kx;     /* k_fft_dx_h_1D: i kx */
+        d[2 * i + 1] = re * kx;
+    }
+    memset(stream, 0, sizeof(double) * N);
+    og_fft_z2d(&g1, d, stream);
+    double epot = 0;
+    for (int i = 0; i < n; ++i) epot += stream[i] * stream[i];
+    long tail = N / 8 > n + 2 ? N / 8 : n + 2;
+    for (long i = tail; i < N; ++i) stream[i] = f[i];
+    free(rho); free(c); free(d);
+    double vm[9];
+    og_vlasov_mesure(f, gs, st->psi, st->gp, vm);
+    mes[1] = 0.5 * hh * ekin;
+    mes[2] = 0.5 * gs->hx * epot;
+    mes[0] = mes[1] + mes[2];
+    mes[3] = hh * mass;
+    mes[4] = hh * mom;
+    for (int k = 0; k < 4; ++k) mes[5 + k] = vm[5 + k];
+}

@@ -94,6 +94,7 @@ def lib():
         L.og_sample_points_dxdy.argtypes = [C.c_void_p, dp, dp, C.c_int]
         L.og_init.restype = C.c_int
         L.og_state_sample.argtypes = [C.c_void_p, C.c_int, C.c_int, dp, dp]
+        L.og_state_vlasov_sample.argtypes = [C.c_void_p, C.c_int, dp, dp]
         L.og_vlasov_state_mesure.argtypes = [C.c_void_p, dp]
         L.og_set_init_data.argtypes = [dp, dp]
         L.og_state_zoom.argtypes = [C.c_void_p, C.c_int, dp, C.c_int, dp]
@@ -318,6 +319,18 @@ class EulerOracle:
         planes = {k: out[i * n * n:(i + 1) * n * n].copy() for i, k in enumerate(names)}
         return planes, dict(zip(("Energy", "Enstrophy", "Palinstrophy", "Max_vorticity", "Scalar_integral"),
                                 mes.tolist()))
+
+    def vlasov_sample(self, n):
+        """Vlasov sampled outputs on an n x n grid: dict of the four planes (Map_ChiX,
+        Map_ChiY, Distribution_F, Stream_function_Psi) and the nine conservation values
+        (sample_compute_and_write_vlasov, backward part)."""
+        out = np.zeros(4 * n * n)
+        mes = np.zeros(9)
+        self.L.og_state_vlasov_sample(self.h, n, _dp(out), _dp(mes))
+        names = ("Map_ChiX", "Map_ChiY", "Distribution_F", "Stream_function_Psi")
+        planes = {k: out[i * n * n:(i + 1) * n * n].copy() for i, k in enumerate(names)}
+        keys = ("Etot", "Ekin", "Epot", "Mass", "Momentum", "Emode1", "Emode2", "Emode3", "Emode4")
+        return planes, dict(zip(keys, mes.tolist()))
 
     # forward map
     def chix_f(self):

@@ -138,6 +138,130 @@ def test_vlasov_mixed_matches_plain_fp64(tmp_path, case):
     assert abs(mm - mp) <= 1
 
 
+def _sample_files(run, n):
+    """{time directory: {plane name: array}} of the sampled outputs on the n grid"""
+    import os
+    base = os.path.join(run, "Time_data")
+    out = {}
+    for d in os.listdir(base):
+        planes = {}
+        for k in ("Map_ChiX", "Map_ChiY", "Distribution_F", "Stream_function_Psi"):
+            f = os.path.join(base, d, "%s_%d.data" % (k, n))
+            if os.path.exists(f):
+                planes[k] = np.fromfile(f, dtype="<f8")
+        if planes:
+            out[d] = planes
+    return out
+
+
+def _periods(bounds):
+    b = [float(v) * PI for v in bounds.strip("{}").split(",")[:4]]
+    return b[1] - b[0], b[3] - b[2]
+
+
+def _with_sample(work, args, rec):
+    """the run's settings as a parameter file with one save_sample record (record lists are
+    read from parameter files only, as in the reference) -> command-line arguments"""
+    kv = [a.split("=", 1) for a in args if not a.startswith(("workspace=", "save_sample_num"))]
+    lines = ["CMM Parameter file", "param_version\t=\t3", ""]
+    lines += ["%s\t=\t%s" % (k, v) for k, v in kv]
+    lines += ["save_sample_num\t=\t1", "save_sample\t=\t" + rec]
+    pf = work / "params_sample.txt"
+    pf.write_text("\n".join(lines) + "\n")
+    return ["param_file=%s" % pf, "workspace=%s/" % work]
+
+
+def wrap_err(a, b, period):
+    """relative L-infinity of composed positions modulo whole periods (a point within rounding
+    of the periodic boundary may land on either side)"""
+    d = np.asarray(a) - np.asarray(b)
+    d -= period * np.round(d / period)
+    return float(np.max(np.abs(d)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_vlasov_sampled_outputs_match_oracle(tmp_path, case):
+    """sample_compute_and_write_vlasov on a 96 x 96 sample grid (non-power-of-two 1D
+    transforms) at t = 0, 1 and 2 of a run with remaps: the composed map, the distribution
+    function, the written stream buffer (d phi / dx of the sample grid's own potential in
+    its first 96 entries, the distribution from entry N / 8 on) and the nine Mesure series,
+    against the oracle at the same instants; at t = 0 Landau damping's known answers."""
+    import os
+    ic, bounds = CASES[case]
+    lx, ly = _periods(bounds)
+    n = 96
+    args = _args(tmp_path, ic, bounds)
+    m = cmm()
+    sim = m.Simulation(_with_sample(tmp_path, args, "{is_instant=0,time_start=0,time_end=2,time_step=1,var=All,grid=%d}" % n))
+    sim.init()
+    o, s = _oracle(args)
+    o.init()
+    expect = [o.vlasov_sample(n)]
+    k = 0
+    while sim.step(1) != 1:
+        o.step(s.dt)
+        k += 1
+        if k % 32 == 0:
+            expect.append(o.vlasov_sample(n))
+    run = os.path.join(str(tmp_path), "data", sim.file_name())
+    maps = int(sim.scalar("map_counter"))
+    sim.close()
+    assert maps >= 2
+    mon = read_monitoring(run)
+    assert np.allclose(mon["Mesure/Time_s_%d" % n], [0.0, 1.0, 2.0], atol=1e-12)
+    files = _sample_files(run, n)
+    assert len(files) == 3
+    N = n * n
+    for i, d in enumerate(sorted(files, key=lambda t: float(t.split("_")[-1]) if t[-1].isdigit() else 1e9)):
+        planes, mes = expect[i]
+        got = files[d]
+        assert wrap_err(got["Map_ChiX"], planes["Map_ChiX"], lx) < 1e-10, (d, "x")
+        assert wrap_err(got["Map_ChiY"], planes["Map_ChiY"], ly) < 1e-10, (d, "y")
+        assert rel_linf(got["Distribution_F"], planes["Distribution_F"]) < 1e-10, d
+        e, er = got["Stream_function_Psi"][:n], planes["Stream_function_Psi"][:n]
+        assert np.max(np.abs(e - er)) <= 1e-9 * np.max(np.abs(er)), d
+        assert np.array_equal(got["Stream_function_Psi"][N // 8:], got["Distribution_F"][N // 8:])
+        assert not np.any(got["Stream_function_Psi"][n:N // 8])
+        for key in ("Etot", "Ekin", "Epot", "Mass", "Emode1"):
+            assert abs(mon["Mesure/%s_%d" % (key, n)][i] - mes[key]) <= 1e-9 * abs(mes[key]), (d, key)
+        assert abs(mon["Mesure/Momentum_%d" % n][i] - mes["Momentum"]) <= 1e-10 * mes["Mass"], d
+    if case == "landau":
+        assert abs(mon["Mesure/Epot_%d" % n][0] - PI / 100) < 1e-12
+        assert abs(mon["Mesure/Mass_%d" % n][0] - 4 * PI) < 1e-11
+        assert abs(mon["Mesure/Ekin_%d" % n][0] - 2 * PI) < 1e-11
+        assert abs(mon["Mesure/Emode1_%d" % n][0] - 0.05) < 1e-12
+
+
+def test_vlasov_sampled_outputs_mixed_form(tmp_path):
+    """The mixed form's sampled outputs (fixed-point composition through the FP32 stack) against
+    the plain FP64 form's after a run with remaps."""
+    import os
+    ic, bounds = CASES["two_stream"]
+    n = 64
+    res = {}
+    for prec in ("fp64", "mixed"):
+        work = tmp_path / prec
+        work.mkdir()
+        args = _args(work, ic, bounds, precision=prec)
+        m = cmm()
+        sim = m.Simulation(_with_sample(work, args, "{is_instant=1,time_start=2,var=Dist Map_b,grid=%d}" % n))
+        sim.init()
+        sim.run()
+        run = os.path.join(str(work), "data", sim.file_name())
+        sim.close()
+        res[prec] = (_sample_files(run, n), read_monitoring(run))
+    (fp, mp), (fm, mm) = res["fp64"], res["mixed"]
+    assert len(fp) == len(fm) == 1
+    a, b = list(fp.values())[0], list(fm.values())[0]
+    assert set(a) == set(b) == {"Map_ChiX", "Map_ChiY", "Distribution_F"}
+    lx, ly = _periods(bounds)
+    assert wrap_err(b["Map_ChiX"], a["Map_ChiX"], lx) < 1e-5 and wrap_err(b["Map_ChiY"], a["Map_ChiY"], ly) < 1e-5
+    assert np.max(np.abs(b["Distribution_F"] - a["Distribution_F"])) <= 1e-5 * np.max(np.abs(a["Distribution_F"]))
+    for key in ("Mass", "Ekin"):
+        x, y = mp["Mesure/%s_%d" % (key, n)][0], mm["Mesure/%s_%d" % (key, n)][0]
+        assert abs(y - x) <= 1e-6 * abs(x), key
+
+
 def test_vlasov_golden_initial_state_through_param_file(tmp_path):
     """The reference's Vlasov parameter file with grid_psi raised to the vort
     grid (the current reference rejects its own 256 < 512): the t = 0

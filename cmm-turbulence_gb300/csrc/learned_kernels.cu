@@ -1,15 +1,15 @@
 // learned_kernels.cu -- BF16 tcgen05 convolution kernels of the learned psi upsampler and
 // the elementwise steps around them (see learned.hpp for the layouts).
 //
-// Forward / input-gradient convolution (k_conv3x3<CIN, COUT>): a CTA of 128 threads walks
-// a strip of consecutive rows of one 128-pixel column segment.  Each source row it needs
-// (the tile's row and its two periodic neighbours) is staged once into one of four row
-// slots with cp.async, laid out as [channel chunk of 8][pixel 0..129][8 channels]: a
-// K-major operand whose 8-pixel core matrices are 128 contiguous bytes, so the tap with
-// column offset dx is the same slot addressed dx * 16 bytes further.  The 9 taps x CIN/16
-// MMAs (M = 128 pixels, N = COUT, K = 16) accumulate in TMEM; the epilogue reads one
-// pixel's COUT accumulators per thread and fuses bias, ReLU, the ReLU mask of the
-// backward pass and the residual add.
+// Forward / input-gradient convolution (k_conv3x3<CIN, COUT>): a persistent warp-specialised
+// kernel, one CTA per SM, over strips of rows of 128-pixel column segments.  Each source row
+// is staged once with cp.async as [channel chunk of 8][pixel 0..129][8 channels]: a K-major
+// operand whose 8-pixel core matrices are 128 contiguous bytes, so the tap with column offset
+// dx is the same slot addressed dx * 16 bytes further.  One source row meets all three kernel
+// rows in the same MMAs (M = 128 pixels, N = 3 COUT (dy, co), K = 16): its accumulator in TMEM
+// holds its contribution to three output rows, and the epilogue sums the matching column
+// blocks of three consecutive accumulators and fuses bias, ReLU, the ReLU mask of the
+// backward pass and the residual add (details at the kernel).
 //
 // Weight gradient (k_conv3x3_dw<CIN, COUT>): dW[(dy, dx, ci)][co] = sum over pixels of
 // x[p + (dy - 1, dx - 1)][ci] dy[p][co], a GEMM with K = pixels.  Each staged input row
@@ -21,7 +21,6 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <cstdlib>
 
 #include "learned.hpp"
 #include "tc_sm100.cuh"
@@ -32,6 +31,7 @@ namespace lrn {
 namespace {
 
 constexpr long long kMaxPolls = 1ll << 22;   // ~0.2 s of polling before a wait gives up
+constexpr long long kMaxTries = 1ll << 20;   // try_wait rounds (each suspends for at most a few us)
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
 {
@@ -88,79 +88,179 @@ __device__ __forceinline__ uint4 pack8(const float* f)
 // ---------------------------------------------------------------------------
 // forward / input-gradient convolution
 // ---------------------------------------------------------------------------
-// Software pipeline over the CTA's strip of rows: while one thread issues row r's MMAs into
-// accumulator r % 2, the CTA stages (cp.async) the source rows row r + 1 still lacks and then
-// drains row r - 1's accumulator (the epilogue).  Two mbarriers track the two accumulators;
-// a source row's slot is reused only after the MMAs reading it completed.
-template <int CIN, int COUT>
-__device__ __forceinline__ void conv_issue(uint32_t d_tmem, uint32_t rbase, uint32_t wbase, const int (&slot)[3])
+// Warp-specialised persistent kernel, one CTA per SM (it holds the whole tensor memory).
+// Work items ("tasks") are strips of at most rows_per_cta rows of one 128-pixel column
+// segment inside one image; a strip of n rows reads the n + 2 source rows r0 - 1 .. r0 + n
+// (wrapped periodically inside the image).  Each source row k is multiplied once by all
+// three kernel rows dy at a time: N = 3 COUT columns (dy, co), so an MMA reads its 4 KB
+// pixel tile for 96 output columns rather than 32,
+//   D_k[p][dy COUT + co] = sum_{dx, ci} x_k[p + dx - 1][ci] w[dy][dx][ci][co],
+// and output row j of the strip is D_j[., 0 : COUT] + D_{j+1}[., COUT : 2 COUT] +
+// D_{j+2}[., 2 COUT : 3 COUT].  CTA b takes tasks b, b + grid, ...
+//   warp 0      producer: stages each source row into a ring of kConvSlots row slots with
+//               cp.async; each lane's copies arrive on the slot's "full" barrier when they
+//               land (cp.async.mbarrier.arrive);
+//   warp 1      one lane issues a source row's 3 x CIN/16 MMAs into one of kConvAcc TMEM
+//               accumulators (after a proxy fence for the staged row), then commits to the
+//               row slot's "empty" barrier and the accumulator's "full" barrier;
+//   warps 2-9   epilogue, two groups of four warps taking alternate output rows: load the
+//               row's ReLU mask and residual, wait for its three accumulators, read their
+//               column blocks (warp w owns TMEM lanes 32 (w % 4) ..), arrive on each one's
+//               "empty" barrier, and apply bias, ReLU, mask, residual and the stores.  An
+//               accumulator is free once all its reader rows arrived: 3 x 128 arrivals, the
+//               last reader of a strip-edge source row (fewer than three readers) arriving
+//               for the missing ones.
+// Every wait is bounded: a wait that runs out ends the kernel's loops and sets *status.
+constexpr int kConvSlots = 8;       // staged source rows
+constexpr int kConvAcc = 5;         // source-row accumulators in TMEM (3 live + 2 ahead)
+constexpr int kConvAccCols = 96;    // 3 COUT columns each (COUT <= 32)
+constexpr int kConvTmemCols = 512;
+constexpr int kConvGroups = 2;      // epilogue groups
+constexpr int kConvThreads = 64 + 128 * kConvGroups;
+constexpr int kConvMinSmem = 120 * 1024;   // keeps a second CTA (and its TMEM request) off the SM
+static_assert(kConvAcc * kConvAccCols <= kConvTmemCols, "accumulators exceed the TMEM allocation");
+static_assert(kConvAcc >= 4, "three live accumulators and one being written");
+
+struct ConvTask {
+    int x0, r0, nr;
+};
+
+__device__ __forceinline__ int conv_tasks(const ConvArgs& a)
 {
-    constexpr int C8 = CIN / 8;
-    constexpr int SLOT = C8 * kPitch * 16;
-    constexpr uint32_t idesc = tc::idesc_bf16(128, COUT);
-    uint32_t acc = 0;
-#pragma unroll
-    for (int dy = 0; dy < 3; ++dy)
-#pragma unroll
-        for (int dx = 0; dx < 3; ++dx)
-#pragma unroll
-            for (int kk = 0; kk < CIN / 16; ++kk) {
-                const uint32_t aaddr = rbase + slot[dy] * SLOT + ((2 * kk) * kPitch + dx) * 16;
-                const uint32_t baddr = wbase + ((dy * 3 + dx) * C8 + 2 * kk) * COUT * 16;
-                tc::mma_bf16(d_tmem, tc::desc_kmajor(aaddr, kPitch * 16, 128), tc::desc_kmajor(baddr, COUT * 16, 128),
-                             idesc, acc);
-                acc = 1;
-            }
+    const int per_img = (a.H + a.rows_per_cta - 1) / a.rows_per_cta;
+    return (a.W / kTile) * (a.rows / a.H) * per_img;
 }
 
-template <int CIN>
-__device__ __forceinline__ void conv_stage(unsigned char* dst, const bf16* __restrict__ in, int src, int W, int x0)
+__device__ __forceinline__ ConvTask conv_task(const ConvArgs& a, int t)
+{
+    const int segs = a.W / kTile;
+    const int per_img = (a.H + a.rows_per_cta - 1) / a.rows_per_cta;
+    const int strip = t / segs;
+    const int img = strip / per_img, k = strip - img * per_img;
+    ConvTask c;
+    c.x0 = (t - strip * segs) * kTile;
+    c.r0 = img * a.H + k * a.rows_per_cta;
+    c.nr = min(a.rows_per_cta, a.H - k * a.rows_per_cta);
+    return c;
+}
+
+// the barrier receives this thread's arrival when all its earlier cp.async copies have landed
+// (the arrival counts against the barrier's expected count: no increment)
+__device__ __forceinline__ void cp_async_arrive(uint64_t* bar)
+{
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar, uint32_t count)
+{
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(tc::smem_u32(bar)),
+                 "r"(count)
+                 : "memory");
+}
+
+// arrivals output row j of an n-row strip makes on the accumulator of its source row k
+// (k = j .. j + 2): 1, plus, from k's last reader, one for each reader k lacks
+__device__ __forceinline__ uint32_t conv_arrivals(int j, int k, int n)
+{
+    const int lo = k - 2 > 0 ? k - 2 : 0, hi = k < n - 1 ? k : n - 1;
+    return j == hi ? 1u + (uint32_t)(3 - (hi - lo + 1)) : 1u;
+}
+
+// D (TMEM, 3 COUT columns) = the staged source row times all 9 taps; weights in shared
+// memory as [dx][ci / 8][dy][co][8]
+template <int CIN, int COUT>
+__device__ __forceinline__ void conv_issue(uint32_t d_tmem, uint32_t row, uint32_t wbase)
 {
     constexpr int C8 = CIN / 8;
-    const bf16* row = in + (long long)src * W * CIN;
-    for (int i = threadIdx.x; i < C8 * kPitch; i += 128) {
+    constexpr uint32_t idesc = tc::idesc_bf16(128, 3 * COUT);
+    uint32_t acc = 0;
+#pragma unroll
+    for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+        for (int kk = 0; kk < CIN / 16; ++kk) {
+            const uint32_t aaddr = row + ((2 * kk) * kPitch + dx) * 16;
+            const uint32_t baddr = wbase + ((dx * C8 + 2 * kk) * 3 * COUT) * 16;
+            tc::mma_bf16(d_tmem, tc::desc_kmajor(aaddr, kPitch * 16, 128), tc::desc_kmajor(baddr, 3 * COUT * 16, 128),
+                         idesc, acc);
+            acc = 1;
+        }
+}
+
+// a staged row is C8 x kPitch 16-byte chunks ([ci / 8][pixel][8]); lane l copies chunks
+// l, l + 32, ...: their byte offsets inside the source row (periodic in x) depend on the
+// segment only
+template <int CIN>
+struct StageMap {
+    static constexpr int C8 = CIN / 8;
+    static constexpr int kChunks = C8 * kPitch;
+    static constexpr int kPer = (kChunks + 31) / 32;
+    uint32_t src[kPer];
+};
+
+template <int CIN>
+__device__ __forceinline__ void stage_map(StageMap<CIN>& m, int W, int x0, int lane)
+{
+    constexpr int C8 = CIN / 8;
+#pragma unroll
+    for (int k = 0; k < StageMap<CIN>::kPer; ++k) {
+        const int i = lane + 32 * k;
         const int c = i % C8, p = i / C8;
         int x = x0 - 1 + p;
         x = x < 0 ? x + W : (x >= W ? x - W : x);
-        cp_async16(dst + (c * kPitch + p) * 16, row + (long long)x * CIN + c * 8);
+        m.src[k] = (uint32_t)(x * CIN + c * 8) * 2u;
     }
 }
 
-template <int COUT>
-__device__ __forceinline__ void conv_epilogue(const ConvArgs& a, uint32_t d_tmem, int r, int x0, const float (&bias)[COUT],
-                                              bool store)
+template <int CIN>
+__device__ __forceinline__ void conv_stage_warp(unsigned char* dst, const bf16* __restrict__ in, int src, int W,
+                                                const StageMap<CIN>& m, int lane)
 {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float v[COUT];
+    constexpr int C8 = CIN / 8;
+    const unsigned char* row = reinterpret_cast<const unsigned char*>(in + (long long)src * W * CIN);
 #pragma unroll
-    for (int c = 0; c < COUT; c += 16) {
-        float t[16];
-        tc::tmem_ld16(d_tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, t);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) v[c + j] = t[j] + bias[c + j];
+    for (int k = 0; k < StageMap<CIN>::kPer; ++k) {
+        const int i = lane + 32 * k;
+        if (k + 1 < StageMap<CIN>::kPer || i < StageMap<CIN>::kChunks)
+            cp_async16(dst + ((i % C8) * kPitch + i / C8) * 16, row + m.src[k]);
     }
-    if (!store) return;
-    const long long pix = (long long)r * a.W + x0 + warp * 32 + lane;
+}
+
+// the ReLU mask and residual of one output row at this thread's pixel (zero when absent)
+template <int COUT>
+__device__ __forceinline__ void conv_extra(const ConvArgs& a, int r, int x0, int q4, int lane, uint4 (&mk)[COUT / 8],
+                                           uint4 (&rs)[COUT / 8])
+{
+    const long long pix = (long long)r * a.W + x0 + q4 * 32 + lane;
+#pragma unroll
+    for (int q = 0; q < COUT / 8; ++q) {
+        mk[q] = a.mask ? reinterpret_cast<const uint4*>(a.mask + pix * COUT)[q] : make_uint4(0, 0, 0, 0);
+        rs[q] = a.res ? reinterpret_cast<const uint4*>(a.res + pix * COUT)[q] : make_uint4(0, 0, 0, 0);
+    }
+}
+
+// epilogue of one output row for the 32 pixels of TMEM lane quarter q4 (v: bias included)
+template <int COUT>
+__device__ __forceinline__ void conv_store(const ConvArgs& a, float (&v)[COUT], const uint4 (&mk)[COUT / 8],
+                                           const uint4 (&rs)[COUT / 8], int r, int x0, int q4, int lane)
+{
+    const long long pix = (long long)r * a.W + x0 + q4 * 32 + lane;
     if (a.relu) {
 #pragma unroll
         for (int j = 0; j < COUT; ++j) v[j] = fmaxf(v[j], 0.f);
     }
     if (a.mask) {
-        const uint4* mp = reinterpret_cast<const uint4*>(a.mask + pix * COUT);
 #pragma unroll
         for (int q = 0; q < COUT / 8; ++q) {
             float m[8];
-            unpack8(mp[q], m);
+            unpack8(mk[q], m);
 #pragma unroll
             for (int e = 0; e < 8; ++e) v[8 * q + e] = m[e] > 0.f ? v[8 * q + e] : 0.f;
         }
     }
     if (a.res) {
-        const uint4* rp = reinterpret_cast<const uint4*>(a.res + pix * COUT);
 #pragma unroll
         for (int q = 0; q < COUT / 8; ++q) {
             float m[8];
-            unpack8(rp[q], m);
+            unpack8(rs[q], m);
 #pragma unroll
             for (int e = 0; e < 8; ++e) v[8 * q + e] += m[e];
         }
@@ -177,131 +277,138 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, uint32_t d_tmem
     }
 }
 
-// slots for the source rows of output row r: rows already staged keep their slot; missing
-// rows go to slots outside `busy` (the slots MMAs in flight read) and not holding a row r
-// needs.  Returns the number of rows it could not place (0 on success).  Uniform over the CTA.
-template <int CIN>
-__device__ __forceinline__ int conv_place(const ConvArgs& a, int r, int x0, unsigned char* sr, int (&tag)[4],
-                                          const int (&busy)[3], int nbusy, int (&slot)[3])
-{
-    constexpr int SLOT = (CIN / 8) * kPitch * 16;
-    int src[3];
-#pragma unroll
-    for (int dy = 0; dy < 3; ++dy) {
-        src[dy] = src_row(r, dy - 1, a.H);
-        slot[dy] = -1;
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (tag[k] == src[dy]) slot[dy] = k;
-    }
-    int unplaced = 0;
-#pragma unroll
-    for (int dy = 0; dy < 3; ++dy) {
-        if (slot[dy] >= 0) continue;
-        int s = -1;
-        for (int k = 3; k >= 0; --k) {
-            bool used = false;
-            for (int e = 0; e < nbusy; ++e) used = used || busy[e] == k;
-            for (int e = 0; e < 3; ++e) used = used || slot[e] == k || (tag[k] >= 0 && tag[k] == src[e]);
-            if (!used) s = k;
-        }
-        if (s < 0) {
-            ++unplaced;
-            continue;
-        }
-        conv_stage<CIN>(sr + s * SLOT, a.in, src[dy], a.W, x0);
-        tag[s] = src[dy];
-#pragma unroll
-        for (int e = 0; e < 3; ++e)
-            if (src[e] == src[dy]) slot[e] = s;
-    }
-    return unplaced;
-}
-
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a)
+__global__ void __launch_bounds__(kConvThreads, 1) k_conv3x3(ConvArgs a)
 {
     constexpr int C8 = CIN / 8;
     constexpr int WB = 9 * C8 * COUT * 16;
+    constexpr int SLOT = C8 * kPitch * 16;
     extern __shared__ __align__(128) unsigned char sm[];
-    __shared__ uint64_t bar[2];
+    __shared__ uint64_t full[kConvSlots], empty[kConvSlots], dfull[kConvAcc], dempty[kConvAcc], done;
     __shared__ uint32_t tslot;
+    __shared__ float sbias[COUT];
     unsigned char* sw = sm;
     unsigned char* sr = sm + WB;
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const int segs = a.W / kTile;
-    const int seg = blockIdx.x % segs;
-    const int r0 = (blockIdx.x / segs) * a.rows_per_cta;
-    if (r0 >= a.rows) return;
-    const int r1 = min(r0 + a.rows_per_cta, a.rows);
-    const int x0 = seg * kTile;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ntasks = conv_tasks(a);
 
-    for (int i = tid; i < WB / 16; i += 128)
-        cp_async16(sw + 16 * i, reinterpret_cast<const unsigned char*>(a.wt) + 16 * (long long)i);
-    if (warp == 0) {
-        tc::tmem_alloc(&tslot, 64);   // two accumulators of 32 columns
+    // weights: prepared [dy dx][ci / 8][co][8] -> shared [dx][ci / 8][dy][co][8]
+    for (int i = tid; i < WB / 16; i += kConvThreads) {
+        const int co = i % COUT, t = i / COUT, dy = t % 3, t2 = t / 3, c8 = t2 % C8, dx = t2 / C8;
+        const int gi = ((dy * 3 + dx) * C8 + c8) * COUT + co;
+        cp_async16(sw + 16 * i, reinterpret_cast<const unsigned char*>(a.wt) + 16 * (long long)gi);
+    }
+    if (tid < COUT) sbias[tid] = a.bias ? a.bias[tid] : 0.f;
+    if (warp == 1) {
+        tc::tmem_alloc(&tslot, kConvTmemCols);
         tc::tmem_relinquish();
     }
     if (tid == 0) {
-        tc::mbar_init(&bar[0], 1);
-        tc::mbar_init(&bar[1], 1);
+        for (int k = 0; k < kConvSlots; ++k) {
+            tc::mbar_init(&full[k], 32);
+            tc::mbar_init(&empty[k], 1);
+        }
+        for (int k = 0; k < kConvAcc; ++k) {
+            tc::mbar_init(&dfull[k], 1);
+            tc::mbar_init(&dempty[k], 3 * 128);
+        }
+        tc::mbar_init(&done, 1);
         tc::mbar_fence_init();
     }
-    float bias[COUT];
-#pragma unroll
-    for (int j = 0; j < COUT; ++j) bias[j] = a.bias ? a.bias[j] : 0.f;
-
-    int tag[4] = {-1, -1, -1, -1};
-    int cur[3], nxt[3];
-    const int none[3] = {-1, -1, -1};
-    conv_place<CIN>(a, r0, x0, sr, tag, none, 0, cur);   // four free slots: always places all
+    cp_async_wait_all();
+    tc::fence_smem_to_async();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = tslot;
-    const uint32_t wbase = tc::smem_u32(sw), rbase = tc::smem_u32(sr);
-
     bool ok = true;
-    int it = 0;
-    for (int r = r0; r < r1; ++r, ++it) {
-        // this row's source rows (staged in the previous iteration or above) visible to the MMAs
-        cp_async_wait_all();
-        tc::fence_smem_to_async();
-        tc::fence_before_sync();
-        __syncthreads();
-        tc::fence_after_sync();
-        if (tid == 0) {
-            conv_issue<CIN, COUT>(tmem + (uint32_t)((it & 1) * 32), rbase, wbase, cur);
-            tc::mma_commit(&bar[it & 1]);
-        }
-        __syncwarp();
-        // the previous row's MMAs: their accumulator is drained below, their slots free up
-        if (it > 0) ok = ok && tc::mbar_wait(&bar[(it - 1) & 1], ((it - 1) >> 1) & 1, kMaxPolls);
-        if (r + 1 < r1) {
-            if (conv_place<CIN>(a, r + 1, x0, sr, tag, cur, 3, nxt) > 0) {
-                // a new image starts: the rows it needs outnumber the free slots; wait for this
-                // row's MMAs, after which only the rows row r + 1 needs are kept
-                ok = ok && tc::mbar_wait(&bar[it & 1], (it >> 1) & 1, kMaxPolls);
-                conv_place<CIN>(a, r + 1, x0, sr, tag, none, 0, nxt);
+
+    if (warp == 0) {
+        // producer
+        uint32_t g = 0;
+        StageMap<CIN> map;
+        int map_x0 = -1;
+        for (int t = blockIdx.x; t < ntasks && ok; t += gridDim.x) {
+            const ConvTask c = conv_task(a, t);
+            if (c.x0 != map_x0) {
+                stage_map<CIN>(map, a.W, c.x0, lane);
+                map_x0 = c.x0;
+            }
+            for (int j = 0; j < c.nr + 2; ++j, ++g) {
+                const uint32_t slot = g % kConvSlots, use = g / kConvSlots;
+                if (use > 0) ok = tc::mbar_try_wait(&empty[slot], (use - 1) & 1, kMaxTries);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok) break;
+                conv_stage_warp<CIN>(sr + slot * SLOT, a.in, src_row(c.r0, j - 1, a.H), a.W, map, lane);
+                cp_async_arrive(&full[slot]);
             }
         }
-        ok = __all_sync(0xffffffffu, ok);
-        tc::fence_after_sync();
-        if (it > 0) conv_epilogue<COUT>(a, tmem + (uint32_t)(((it - 1) & 1) * 32), r - 1, x0, bias, ok);
-        tc::fence_before_sync();
-        if (__syncthreads_or(!ok)) break;
+        cp_async_wait_all();
+    } else if (warp == 1) {
+        // MMA issue (one lane): one accumulator per source row
+        if (lane == 0) {
+            const uint32_t wbase = tc::smem_u32(sw), rbase = tc::smem_u32(sr);
+            uint32_t g = 0;
+            for (int t = blockIdx.x; t < ntasks && ok; t += gridDim.x) {
+                const ConvTask c = conv_task(a, t);
+                for (int j = 0; j < c.nr + 2; ++j, ++g) {
+                    const uint32_t slot = g % kConvSlots, d = g % kConvAcc, use = g / kConvAcc;
+                    ok = tc::mbar_try_wait(&full[slot], (g / kConvSlots) & 1, kMaxTries);
+                    if (ok && use > 0) ok = tc::mbar_try_wait(&dempty[d], (use - 1) & 1, kMaxTries);
+                    if (!ok) break;
+                    tc::fence_smem_to_async();   // the staged row (generic proxy) -> the MMAs' operand reads
+                    tc::fence_after_sync();
+                    conv_issue<CIN, COUT>(tmem + d * kConvAccCols, rbase + slot * SLOT, wbase);
+                    tc::mma_commit(&empty[slot]);
+                    tc::mma_commit(&dfull[d]);
+                }
+            }
+            // every MMA retired before the tensor memory is released
+            tc::mma_commit(&done);
+            ok = tc::mbar_try_wait(&done, 0, kMaxTries) && ok;
+        }
+    } else {
+        // epilogue: group e takes the output rows q with q % kConvGroups == e; warps 2.. own TMEM
+        // lane quarters (warp % 4)
+        const int e = (warp - 2) >> 2, q4 = warp & 3;
+        const uint32_t lanes = (uint32_t)(q4 * 32) << 16;
+        uint32_t g = 0, q = 0;
+        for (int t = blockIdx.x; t < ntasks && ok; t += gridDim.x) {
+            const ConvTask c = conv_task(a, t);
+            for (int j = 0; j < c.nr; ++j, ++q) {
+                if ((int)(q % kConvGroups) != e) continue;
+                uint4 mk[COUT / 8], rs[COUT / 8];
+                conv_extra<COUT>(a, c.r0 + j, c.x0, q4, lane, mk, rs);
+                float v[COUT];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) cur[d] = nxt[d];
+                for (int i = 0; i < COUT; ++i) v[i] = sbias[i];
+#pragma unroll
+                for (int dy = 0; dy < 3; ++dy) {
+                    const uint32_t m = g + j + dy, d = m % kConvAcc;
+                    ok = __all_sync(0xffffffffu, tc::mbar_try_wait(&dfull[d], (m / kConvAcc) & 1, kMaxTries));
+                    if (!ok) break;
+                    tc::fence_after_sync();
+                    float part[COUT];
+                    tc::tmem_ld_cols<COUT>(tmem + lanes + d * kConvAccCols + dy * COUT, part);
+#pragma unroll
+                    for (int i = 0; i < COUT; ++i) v[i] += part[i];
+                }
+                if (!ok) break;
+                tc::fence_before_sync();
+#pragma unroll
+                for (int dy = 0; dy < 3; ++dy)
+                    mbar_arrive(&dempty[(g + j + dy) % kConvAcc], conv_arrivals(j, j + dy, c.nr));
+                conv_store<COUT>(a, v, mk, rs, c.r0 + j, c.x0, q4, lane);
+            }
+            g += c.nr + 2;
+        }
     }
-    if (ok && it > 0) {
-        ok = __all_sync(0xffffffffu, tc::mbar_wait(&bar[(it - 1) & 1], ((it - 1) >> 1) & 1, kMaxPolls));
-        tc::fence_after_sync();
-        conv_epilogue<COUT>(a, tmem + (uint32_t)(((it - 1) & 1) * 32), r1 - 1, x0, bias, ok);
-    }
-    cp_async_wait_all();
     tc::fence_before_sync();
     if (__syncthreads_or(!ok) && tid == 0 && a.status) atomicExch(a.status, 1);
-    if (warp == 0) tc::tmem_dealloc(tmem, 64);
+    if (warp == 1) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, kConvTmemCols);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -745,15 +852,21 @@ __global__ void k_diff_stats(const float* __restrict__ a, long long sa, const fl
 template <int CIN, int COUT>
 cudaError_t conv_launch(const ConvArgs& a, cudaStream_t s)
 {
-    constexpr int smem = 9 * (CIN / 8) * COUT * 16 + 4 * (CIN / 8) * kPitch * 16;
-    static bool attr = false;
-    if (!attr) {
+    constexpr int need = 9 * (CIN / 8) * COUT * 16 + kConvSlots * (CIN / 8) * kPitch * 16;
+    constexpr int smem = need > kConvMinSmem ? need : kConvMinSmem;
+    static int sms = 0;
+    if (!sms) {
         cudaError_t e = cudaFuncSetAttribute(k_conv3x3<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        attr = true;
+        int dev = 0, n = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+        sms = std::max(1, n);
     }
-    const int grid = conv_grid(a.rows, a.W, a.rows_per_cta);
-    k_conv3x3<CIN, COUT><<<grid, 128, smem, s>>>(a);
+    const long long per_img = (a.H + a.rows_per_cta - 1) / a.rows_per_cta;
+    const long long tasks = (long long)(a.W / kTile) * (a.rows / a.H) * per_img;
+    const int grid = (int)std::min<long long>(tasks, sms);
+    k_conv3x3<CIN, COUT><<<grid, kConvThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -775,11 +888,11 @@ cudaError_t dw_launch(const DwArgs& a, int grid, cudaStream_t s)
 
 int conv_rows_per_cta(int rows, int W)
 {
-    // about two pipelined CTAs per SM, at least four rows each
-    const long long tiles = (long long)rows * (W / kTile);
-    const long long target = 152 * 2;
-    if (const char* e = getenv("CMM_CONV_ROWS")) return atoi(e);
-    return (int)std::max(4ll, (tiles + target - 1) / target);
+    // strip height of the forward kernel's tasks: two halo rows per strip, so taller strips
+    // stage fewer rows; 16 was the fastest of 4, 8, 16 on the 512 x 512 inference
+    (void)rows;
+    (void)W;
+    return 16;
 }
 
 int conv_grid(int rows, int W, int rows_per_cta)

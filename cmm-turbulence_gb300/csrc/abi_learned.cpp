@@ -271,7 +271,7 @@ int cmm_conv3x3(const unsigned short* x, const unsigned short* w, const float* b
     a.W = W;
     a.rows = B * H;
     a.relu = relu ? 1 : 0;
-    a.rows_per_cta = conv_rows_per_cta(a.rows, W);
+    a.rows_per_cta = conv_rows_per_cta(a.rows, H, W);
     e = launch_conv3x3(cin, cout, a, nullptr);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     int st = 0;

@@ -359,7 +359,7 @@ int Upsampler::conv(int layer, bool flipped, const bf16* in, const bf16* mask, c
     a.W = w;
     a.rows = B * h;
     a.relu = relu ? 1 : 0;
-    a.rows_per_cta = conv_rows_per_cta(a.rows, w);
+    a.rows_per_cta = conv_rows_per_cta(a.rows, h, w);
     a.status = d_status_;
     LRN_CHECK(launch_conv3x3(flipped ? L.cout : L.cin, flipped ? L.cin : L.cout, a, s), "conv3x3");
     ++launches;

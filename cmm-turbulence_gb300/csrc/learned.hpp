@@ -48,7 +48,8 @@ struct ConvArgs {
     int H = 0, W = 0, rows = 0, relu = 0, rows_per_cta = 1;
     int* status = nullptr;       // set to 1 when a tensor-core wait ran out
 };
-int conv_rows_per_cta(int rows, int W);
+// strip height of the forward kernel for rows / H images of H x W
+int conv_rows_per_cta(int rows, int H, int W);
 int conv_grid(int rows, int W, int rows_per_cta);
 cudaError_t launch_conv3x3(int cin, int cout, const ConvArgs& a, cudaStream_t s);
 

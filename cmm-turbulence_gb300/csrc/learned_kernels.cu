@@ -886,13 +886,33 @@ cudaError_t dw_launch(const DwArgs& a, int grid, cudaStream_t s)
 
 }  // namespace
 
-int conv_rows_per_cta(int rows, int W)
+int conv_rows_per_cta(int rows, int H, int W)
 {
-    // strip height of the forward kernel's tasks: two halo rows per strip, so taller strips
-    // stage fewer rows; 16 was the fastest of 4, 8, 16 on the 512 x 512 inference
-    (void)rows;
-    (void)W;
-    return 16;
+    // the persistent grid has one CTA per SM and CTA b takes tasks b, b + SMs, ...: pick the
+    // strip height R that minimises the busiest CTA's rows, R ceil(tasks / SMs), counting each
+    // strip's two halo rows at a third of a row (staged, but no epilogue); ties go to taller
+    // strips (fewer halos)
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                      cudaSuccess || sms < 1)
+            sms = 152;
+    }
+    if (H < 1 || W < kTile || rows < H) return 1;
+    const long long groups = (long long)(W / kTile) * (rows / H);
+    int best = 1;
+    double best_cost = 1e300;
+    for (int R = 1; R <= H && R <= 64; ++R) {
+        const long long tasks = groups * ((H + R - 1) / R);
+        const long long per = (tasks + sms - 1) / sms;
+        const double cost = (double)per * (R + 2.0 / 3.0);
+        if (cost <= best_cost) {
+            best_cost = cost;
+            best = R;
+        }
+    }
+    return best;
 }
 
 int conv_grid(int rows, int W, int rows_per_cta)

@@ -51,6 +51,24 @@ def test_conv3x3_matches_oracle(cin, cout, flags):
     assert np.array_equal(O.bf16_bits(O.bf16_round(out)), outb)   # the epilogue's BF16 store
 
 
+@pytest.mark.parametrize("B,H,W", [(2, 70, 1024), (1, 512, 512)])
+def test_conv3x3_tall_strips_match_oracle(B, H, W):
+    """Images wide enough that the persistent grid takes strips of several rows (4 rows for
+    70 x 1024 with a 2-row last strip, 14 rows for 512 x 512 with an 8-row last strip): the
+    source-row accumulators of a strip, their release counts and the periodic wrap at
+    both image edges."""
+    m = cmm()
+    rng = np.random.default_rng(H + W)
+    x, xb = _bf16(rng, (B, H, W, 32))
+    w, wb = _bf16(rng, (9, 32, 32), 0.2)
+    bias = rng.normal(0, 1, 32).astype(np.float32)
+    res, resb = _bf16(rng, (B, H, W, 32))
+    out, outb = m.conv3x3(xb, wb, bias, None, resb, relu=True)
+    ref = O.conv3x3(x, w, bias, None, res, relu=True)
+    assert np.max(np.abs(out - ref)) <= 1e-5 * np.max(np.abs(ref))
+    assert np.array_equal(O.bf16_bits(O.bf16_round(out)), outb)
+
+
 @pytest.mark.parametrize("cin,cout", [(16, 32), (32, 32), (32, 16), (16, 16)])
 def test_conv3x3_weight_grad_matches_oracle(cin, cout):
     m = cmm()

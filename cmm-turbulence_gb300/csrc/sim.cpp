@@ -160,8 +160,8 @@ int EulerSim::alloc()
         err = "scalar_discrete samples the discrete initial vorticity (as the reference does): it needs initial_discrete=1";
         return kErrUnsupported;
     }
-    if (s.forward_map && s.precision == "mixed") {
-        err = "forward_map is built for the plain FP64 form (precision=fp64)";
+    if (s.forward_map && s.precision == "mixed" && s.simulation_type == "cmm_vlasov_poisson_1d") {
+        err = "forward_map with precision=mixed is built for 2D Euler (Vlasov-Poisson: precision=fp64)";
         return kErrUnsupported;
     }
     if (s.grid_coarse <= 0 || s.grid_fine <= 0 || s.grid_psi <= 0 || s.grid_vort <= 0) { err = "grid sizes must be positive"; return kErrParam; }
@@ -732,6 +732,12 @@ int EulerSim::forward_step(int lcl, bool* forced_remap)
     // after that remap on)
     *forced_remap = false;
     if (!s.forward_map) return kOk;
+    if (mixed_) {
+        // mixed form: the forward map stays FP64; it is advected on FP64 copies of the FP32 psi
+        // levels and checked against the FP64 planes of the FP32 backward map
+        for (int l = 0; l < L; ++l) CMM_LAUNCH(1, launch_float4_to_planes(psim_[l], gp.N, psi[l], stream));
+        CMM_LAUNCH(1, launch_map_to_planes(mapm_, gc, ChiX, ChiY, stream));
+    }
     AdvectArgs a{};
     a.gm = gc; a.gp = gp;
     a.ChiX = ChiX_f; a.ChiY = ChiY_f; a.outX = ChiX_new; a.outY = ChiY_new;
@@ -840,6 +846,7 @@ int EulerSim::reserve_stack(int n)
     if (n <= stack_cap_) return kOk;
     int cap = std::min(max_maps, std::max({2 * stack_cap_, 16, n}));
     const size_t mapb = mixed_ ? sizeof(float4) * 2 * (size_t)gc.N : sizeof(double) * 8 * (size_t)gc.N;
+    const size_t mapb_f = sizeof(double) * 8 * (size_t)gc.N;   // the forward stack is FP64 in both forms
     void* bigger = nullptr;
     CMM_CUDA(cudaMalloc(&bigger, mapb * cap));
     void* old = mixed_ ? (void*)stackm_ : (void*)stack;
@@ -847,9 +854,9 @@ int EulerSim::reserve_stack(int n)
     void* bigger_f = nullptr;
     if (s.forward_map) {
         // the forward stack grows with the backward one (one forward sub-map per remap)
-        CMM_CUDA(cudaMalloc(&bigger_f, mapb * cap));
+        CMM_CUDA(cudaMalloc(&bigger_f, mapb_f * cap));
         if (stack_f && n_maps_ > 0)
-            CMM_CUDA(cudaMemcpyAsync(bigger_f, stack_f, mapb * n_maps_, cudaMemcpyDeviceToDevice, stream));
+            CMM_CUDA(cudaMemcpyAsync(bigger_f, stack_f, mapb_f * n_maps_, cudaMemcpyDeviceToDevice, stream));
     }
     CMM_CUDA(cudaStreamSynchronize(stream));
     if (old) cudaFree(old);
@@ -870,12 +877,11 @@ int EulerSim::push_stack()
     if (mixed_) {
         size_t mapb = sizeof(float4) * 2 * (size_t)gc.N;
         CMM_CUDA(cudaMemcpyAsync(stackm_ + 2 * (size_t)n_maps_ * gc.N, mapm_, mapb, cudaMemcpyDeviceToDevice, stream));
-        n_maps_++;
-        return kOk;
+    } else {
+        double* slot = stack + (size_t)n_maps_ * 8 * gc.N;
+        CMM_CUDA(cudaMemcpyAsync(slot, ChiX, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToDevice, stream));
+        CMM_CUDA(cudaMemcpyAsync(slot + 4 * gc.N, ChiY, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToDevice, stream));
     }
-    double* slot = stack + (size_t)n_maps_ * 8 * gc.N;
-    CMM_CUDA(cudaMemcpyAsync(slot, ChiX, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToDevice, stream));
-    CMM_CUDA(cudaMemcpyAsync(slot + 4 * gc.N, ChiY, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToDevice, stream));
     if (s.forward_map) {
         // the forward map goes onto its own stack and restarts from the identity (cmm-euler2d.cu:847-851)
         double* fslot = stack_f + (size_t)n_maps_ * 8 * gc.N;

@@ -90,13 +90,76 @@ def test_forward_map_run_matches_oracle(tmp_path, ti):
     assert z.size == 800 and np.isnan(z).any() and np.isfinite(z).any()
 
 
-def test_forward_map_is_plain_fp64_only(tmp_path):
+def test_forward_map_in_the_mixed_form(tmp_path):
+    """precision=mixed with forward_map=1: the forward map stays FP64, advected on FP64 copies
+    of the FP32 psi levels and checked against the FP32 backward map.  Against the plain FP64
+    run of the same parameter file (RK3, remaps, both forwarded sets) up to the first step
+    where the two remap histories part (E_inc meets the threshold within FP32 noise): the same
+    remap steps, both forward monitors per step and the forwarded particles (modulo the
+    period) at every sample instant before it.  Threshold 1e-4 (the FP32 maps sit near 2e-5
+    of incompressibility error right after a remap on a 64^2 map, above this file's 1e-5),
+    T = 1.  The mixed Vlasov-Poisson form keeps refusing the option."""
     m = cmm()
-    pf = tmp_path / "params.txt"
-    pf.write_text(_text("RK3"))
-    sim = m.Simulation(["param_file=%s" % pf, "workspace=%s/" % tmp_path, "precision=mixed"])
-    with pytest.raises(m.CmmError) as e:
+    text = _text("RK3").replace("incomp_threshold\t=\t1e-05", "incomp_threshold\t=\t0.0001").replace(
+        "final_time\t=\t0.25", "final_time\t=\t1")
+    res = {}
+    for prec in ("fp64", "mixed"):
+        work = tmp_path / prec
+        work.mkdir()
+        pf = work / "params.txt"
+        pf.write_text(text)
+        sim = m.Simulation(["param_file=%s" % pf, "workspace=%s/" % work, "precision=%s" % prec])
         sim.init()
+        sim.run()
+        run_dir = os.path.join(str(work), "data", sim.file_name())
+        parts = {}
+        pdir = os.path.join(run_dir, "Particle_data")
+        for folder in os.listdir(pdir):
+            for i in range(2):
+                f = os.path.join(pdir, folder, "Particles_forwarded_pos_P%02d.data" % (i + 1))
+                if os.path.exists(f):
+                    parts[(folder, i)] = np.fromfile(f)
+        res[prec] = (read_monitoring(run_dir), sim.field("Map_ChiX_f_H_coarse").copy(),
+                     sim.field("Map_ChiY_f_H_coarse").copy(), parts)
+        sim.close()
+    (mp, xp, yp, pp), (mm, xm, ym, pm) = res["fp64"], res["mixed"]
+    # the two runs remap at the same steps until E_inc meets the threshold within FP32 noise
+    # (a remap one step apart); everything before that step is compared
+    cp, cm = mp["Map_counter"], mm["Map_counter"]
+    assert len(cp) == len(cm) == 64
+    div = next((i for i in range(64) if cp[i] != cm[i]), 64)
+    assert div >= 30 and cp[div - 1] >= 3, (div, cp, cm)
+    assert abs(cp[-1] - cm[-1]) <= 1
+    for k in ("Error_incompressibility_forward", "Error_invertibility"):
+        a, b = np.array(mm[k][:div]), np.array(mp[k][:div])
+        # the forward map is advected on FP32-accurate psi: its determinant deviation carries
+        # the rounding of the psi_xy plane (a floor of ~2e-6 on a 64^2 map), and E_inv the
+        # FP32 backward map's (~1e-7 of the domain)
+        assert np.all(np.abs(a - b) <= 2e-2 * np.abs(b) + 5e-6), (k, a, b)
+    if div == 64:
+        assert np.max(np.abs(xm[: xm.size // 4] - xp[: xp.size // 4])) < 1e-5
+        assert np.max(np.abs(ym[: ym.size // 4] - yp[: yp.size // 4])) < 1e-5
+    # (the Debug_globals statistics of the sampled forward map are not compared: points within
+    # rounding of the periodic boundary flip between 0 and 2 pi in either run)
+    assert set(pm) == set(pp) and len(pp) >= 8
+    n_cmp = 0
+    for (folder, i), a in pp.items():
+        t = 1e9 if folder == "Time_final" else float(folder.split("_")[1])
+        if t * 64 >= div - 0.5:
+            continue
+        b = pm[(folder, i)]
+        assert np.array_equal(np.isnan(a), np.isnan(b))
+        ok = ~np.isnan(a)
+        d = np.abs(b[ok] - a[ok])
+        assert np.all(np.minimum(d, 2 * np.pi - d) < 1e-4), (folder, i)
+        n_cmp += 1
+    assert n_cmp >= 8
+    bad = m.Simulation(["workspace=%s/" % tmp_path, "sim_name=vfw", "simulation_type=cmm_vlasov_poisson_1d",
+                        "initial_condition=landau_damping", "domain_bounds={0,4,-2.5,2.5}", "grid_coarse=32",
+                        "grid_fine=64", "grid_vort=64", "grid_psi=64", "forward_map=1", "precision=mixed",
+                        "verbose=0"])
+    with pytest.raises(m.CmmError) as e:
+        bad.init()
     assert e.value.code == m.CMM_ERR_UNSUPPORTED
 
 

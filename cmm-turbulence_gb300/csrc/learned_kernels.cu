@@ -14,9 +14,9 @@
 // Weight gradient (k_conv3x3_dw<CIN, COUT>): dW[(dy, dx, ci)][co] = sum over pixels of
 // x[p + (dy - 1, dx - 1)][ci] dy[p][co], a GEMM with K = pixels.  Each staged input row
 // is transposed into three K-major copies shifted by dx (M = (dx, ci), padded to 128),
-// the output-gradient row into one K-major tile, and three accumulators (one per dy)
-// stay in TMEM across the CTA's whole strip; the per-CTA partials are summed in a fixed
-// order by k_dw_reduce.
+// the output-gradient row into one of two K-major tiles, and three accumulators (one per dy)
+// stay in TMEM across the CTA's whole strip; a row's MMAs run while the next row is staged;
+// the per-CTA partials are summed in a fixed order by k_dw_reduce.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -416,6 +416,8 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv3x3(ConvArgs a)
 // ---------------------------------------------------------------------------
 constexpr int kARows = 129;                  // 128 M rows + 1 pad row per 8-pixel group
 constexpr int kASlot = 16 * kARows * 16;     // [pixel group 16][m 129][8 pixels]
+template <int COUT>
+constexpr int kBTile = 16 * (COUT + 1) * 16;   // [pixel group 16][co + 1][8 pixels]
 
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(128) k_conv3x3_dw(DwArgs a)
@@ -424,11 +426,11 @@ __global__ void __launch_bounds__(128) k_conv3x3_dw(DwArgs a)
     constexpr int BROWS = COUT + 1;
     constexpr uint32_t TCOLS = 3 * COUT <= 64 ? 64 : 128;
     extern __shared__ __align__(128) unsigned char sm[];
-    __shared__ uint64_t bar;
+    __shared__ uint64_t bar[2];
     __shared__ uint32_t tslot;
     __shared__ float red[16 * CO8][8];
     unsigned char* sa = sm;                       // 4 slots
-    unsigned char* sb = sm + 4 * kASlot;          // dy tile [pixel group 16][co + 1][8 pixels]
+    unsigned char* sb = sm + 4 * kASlot;          // 2 dy tiles [pixel group 16][co + 1][8 pixels]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int segs = a.W / kTile;
     const int seg = blockIdx.x % segs;
@@ -448,7 +450,8 @@ __global__ void __launch_bounds__(128) k_conv3x3_dw(DwArgs a)
         tc::tmem_relinquish();
     }
     if (tid == 0) {
-        tc::mbar_init(&bar, 1);
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
         tc::mbar_fence_init();
     }
     tc::fence_before_sync();
@@ -456,31 +459,57 @@ __global__ void __launch_bounds__(128) k_conv3x3_dw(DwArgs a)
     tc::fence_after_sync();
     const uint32_t tmem = tslot;
 
+    // rows are pipelined: row r's MMAs run while the CTA stages row r + 1 (its new source row
+    // goes to the slot those MMAs do not read, its output-gradient tile to the other buffer);
+    // MMAs of row k commit to bar[k & 1]
     float dbacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int tag[4] = {-1, -1, -1, -1};
-    uint32_t phase = 0;
+    int busy[3] = {-1, -1, -1};   // slots the MMAs in flight (previous row) read
     bool ok = true;
-    for (int r = r0; r < r1; ++r) {
-        int slot_of[3];
+    int it = 0;
+    auto wait_row = [&](int k) {
+        return __all_sync(0xffffffffu, tc::mbar_wait(&bar[k & 1], (uint32_t)(k >> 1) & 1u, kMaxPolls));
+    };
+    for (int r = r0; r < r1; ++r, ++it) {
+        // the output-gradient buffer of this row was last read by row it - 2
+        if (it >= 2) ok = ok && wait_row(it - 2);
+        int src[3], slot_of[3];
 #pragma unroll
         for (int dy = 0; dy < 3; ++dy) {
-            const int src = src_row(r, dy - 1, a.H);
+            src[dy] = src_row(r, dy - 1, a.H);
             slot_of[dy] = -1;
 #pragma unroll
             for (int k = 0; k < 4; ++k)
-                if (tag[k] == src) slot_of[dy] = k;
+                if (tag[k] == src[dy]) slot_of[dy] = k;
+        }
+        // free slots: not read by the MMAs in flight and not holding a row this row needs; when
+        // they are too few (a new image starts), wait for those MMAs first
+        int missing = 0, nfree = 0;
+#pragma unroll
+        for (int dy = 0; dy < 3; ++dy) missing += (slot_of[dy] < 0 && (dy == 0 || src[dy] != src[dy - 1])) ? 1 : 0;
+        for (int k = 0; k < 4; ++k) {
+            bool used = k == busy[0] || k == busy[1] || k == busy[2];
+            for (int e = 0; e < 3; ++e) used = used || k == slot_of[e];
+            nfree += used ? 0 : 1;
+        }
+        if (missing > nfree && it >= 1) {
+            ok = ok && wait_row(it - 1);
+            busy[0] = busy[1] = busy[2] = -1;
         }
 #pragma unroll
         for (int dy = 0; dy < 3; ++dy) {
             if (slot_of[dy] >= 0) continue;
-            const int src = src_row(r, dy - 1, a.H);
-            int s = 0;
-            for (int k = 3; k >= 0; --k)
-                if (k != slot_of[0] && k != slot_of[1] && k != slot_of[2]) s = k;
+            int s = -1;
+            for (int k = 3; k >= 0; --k) {
+                bool used = k == busy[0] || k == busy[1] || k == busy[2];
+                for (int e = 0; e < 3; ++e) used = used || k == slot_of[e] || (tag[k] >= 0 && tag[k] == src[e]);
+                if (!used) s = k;
+            }
+            if (s < 0) s = 0;   // unreachable: four slots, at most three rows needed, busy cleared above
             unsigned char* dst = sa + s * kASlot;
-            const bf16* row = a.x + (long long)src * a.W * CIN;
-            for (int it = tid; it < 48 * C8; it += 128) {
-                const int pg = it % 16, c = (it / 16) % C8, dx = it / (16 * C8);
+            const bf16* row = a.x + (long long)src[dy] * a.W * CIN;
+            for (int i2 = tid; i2 < 48 * C8; i2 += 128) {
+                const int pg = i2 % 16, c = (i2 / 16) % C8, dx = i2 / (16 * C8);
                 uint4 in[8], out[8];
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
@@ -493,9 +522,12 @@ __global__ void __launch_bounds__(128) k_conv3x3_dw(DwArgs a)
                 for (int e = 0; e < 8; ++e)
                     *reinterpret_cast<uint4*>(dst + (pg * kARows + dx * CIN + c * 8 + e) * 16) = out[e];
             }
-            tag[s] = src;
-            slot_of[dy] = s;
+            tag[s] = src[dy];
+#pragma unroll
+            for (int e = 0; e < 3; ++e)
+                if (src[e] == src[dy]) slot_of[e] = s;
         }
+        unsigned char* sbr = sb + (it & 1) * kBTile<COUT>;
         if (tid < 16 * CO8) {
             const int pg = tid % 16, c = tid / 16;
             const bf16* row = a.dy + (long long)r * a.W * COUT;
@@ -510,14 +542,17 @@ __global__ void __launch_bounds__(128) k_conv3x3_dw(DwArgs a)
             }
             transpose8(in, out);
 #pragma unroll
-            for (int e = 0; e < 8; ++e) *reinterpret_cast<uint4*>(sb + (pg * BROWS + c * 8 + e) * 16) = out[e];
+            for (int e = 0; e < 8; ++e) *reinterpret_cast<uint4*>(sbr + (pg * BROWS + c * 8 + e) * 16) = out[e];
         }
         tc::fence_smem_to_async();
         tc::fence_before_sync();
-        __syncthreads();
+        if (__syncthreads_or(!ok)) {
+            ok = false;
+            break;
+        }
         tc::fence_after_sync();
         if (tid == 0) {
-            const uint32_t abase = tc::smem_u32(sa), bbase = tc::smem_u32(sb);
+            const uint32_t abase = tc::smem_u32(sa), bbase = tc::smem_u32(sbr);
             constexpr uint32_t idesc = tc::idesc_bf16(128, COUT);
 #pragma unroll
             for (int dy = 0; dy < 3; ++dy)
@@ -528,18 +563,22 @@ __global__ void __launch_bounds__(128) k_conv3x3_dw(DwArgs a)
                     tc::mma_bf16(tmem + (uint32_t)(dy * COUT), tc::desc_kmajor(aaddr, kARows * 16, 128),
                                  tc::desc_kmajor(baddr, BROWS * 16, 128), idesc, (r > r0 || ks > 0) ? 1u : 0u);
                 }
-            tc::mma_commit(&bar);
+            tc::mma_commit(&bar[it & 1]);
         }
         __syncwarp();
-        ok = __all_sync(0xffffffffu, tc::mbar_wait(&bar, phase, kMaxPolls));
-        phase ^= 1u;
-        tc::fence_after_sync();
-        tc::fence_before_sync();
-        if (__syncthreads_or(!ok)) {
-            ok = false;
-            if (tid == 0 && a.status) atomicExch(a.status, 1);
-            break;
-        }
+#pragma unroll
+        for (int e = 0; e < 3; ++e) busy[e] = slot_of[e];
+    }
+    // the last committed row's MMAs (and, in order, all before them) before the accumulators are
+    // read or released, also after a failed wait
+    if (it > 0) {
+        const bool w = wait_row(it - 1);
+        ok = ok && w;
+    }
+    tc::fence_after_sync();
+    if (__syncthreads_or(!ok)) {
+        ok = false;
+        if (tid == 0 && a.status) atomicExch(a.status, 1);
     }
     // partial gradients of this CTA
     const int m = warp * 32 + lane;
@@ -873,7 +912,7 @@ cudaError_t conv_launch(const ConvArgs& a, cudaStream_t s)
 template <int CIN, int COUT>
 cudaError_t dw_launch(const DwArgs& a, int grid, cudaStream_t s)
 {
-    constexpr int smem = 4 * kASlot + 16 * (COUT + 1) * 16;
+    constexpr int smem = 4 * kASlot + 2 * kBTile<COUT>;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(k_conv3x3_dw<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);

@@ -414,13 +414,14 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv3x3(ConvArgs a)
 // ---------------------------------------------------------------------------
 // weight gradient
 // ---------------------------------------------------------------------------
+constexpr int kDwThreads = 256;              // staging by all; TMEM read-out by warps 0-3
 constexpr int kARows = 129;                  // 128 M rows + 1 pad row per 8-pixel group
 constexpr int kASlot = 16 * kARows * 16;     // [pixel group 16][m 129][8 pixels]
 template <int COUT>
 constexpr int kBTile = 16 * (COUT + 1) * 16;   // [pixel group 16][co + 1][8 pixels]
 
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(128) k_conv3x3_dw(DwArgs a)
+__global__ void __launch_bounds__(kDwThreads, 1) k_conv3x3_dw(DwArgs a)
 {
     constexpr int C8 = CIN / 8, CO8 = COUT / 8;
     constexpr int BROWS = COUT + 1;
@@ -440,7 +441,7 @@ __global__ void __launch_bounds__(128) k_conv3x3_dw(DwArgs a)
     const int x0 = seg * kTile;
 
     // zero the rows no input channel fills (m >= 3 CIN, and the pad row) in every slot
-    for (int i = tid; i < 4 * 16 * (kARows - 3 * CIN); i += 128) {
+    for (int i = tid; i < 4 * 16 * (kARows - 3 * CIN); i += kDwThreads) {
         const int s = i / (16 * (kARows - 3 * CIN)), rem = i % (16 * (kARows - 3 * CIN));
         const int pg = rem / (kARows - 3 * CIN), m = 3 * CIN + rem % (kARows - 3 * CIN);
         *reinterpret_cast<uint4*>(sa + s * kASlot + (pg * kARows + m) * 16) = make_uint4(0, 0, 0, 0);
@@ -508,7 +509,7 @@ __global__ void __launch_bounds__(128) k_conv3x3_dw(DwArgs a)
             if (s < 0) s = 0;   // unreachable: four slots, at most three rows needed, busy cleared above
             unsigned char* dst = sa + s * kASlot;
             const bf16* row = a.x + (long long)src[dy] * a.W * CIN;
-            for (int i2 = tid; i2 < 48 * C8; i2 += 128) {
+            for (int i2 = tid; i2 < 48 * C8; i2 += kDwThreads) {
                 const int pg = i2 % 16, c = (i2 / 16) % C8, dx = i2 / (16 * C8);
                 uint4 in[8], out[8];
 #pragma unroll
@@ -583,18 +584,20 @@ __global__ void __launch_bounds__(128) k_conv3x3_dw(DwArgs a)
     // partial gradients of this CTA
     const int m = warp * 32 + lane;
     float* part = a.part + (long long)blockIdx.x * 3 * 128 * COUT;
+    if (warp < 4) {
 #pragma unroll
-    for (int dy = 0; dy < 3; ++dy)
+        for (int dy = 0; dy < 3; ++dy)
 #pragma unroll
-        for (int c = 0; c < COUT; c += 16) {
-            float t[16];
-            tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(dy * COUT + c), t);
-            if (ok && m < 3 * CIN) {
-                float4* p = reinterpret_cast<float4*>(part + ((long long)dy * 128 + m) * COUT + c);
+            for (int c = 0; c < COUT; c += 16) {
+                float t[16];
+                tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(dy * COUT + c), t);
+                if (ok && m < 3 * CIN) {
+                    float4* p = reinterpret_cast<float4*>(part + ((long long)dy * 128 + m) * COUT + c);
 #pragma unroll
-                for (int q = 0; q < 4; ++q) p[q] = make_float4(t[4 * q], t[4 * q + 1], t[4 * q + 2], t[4 * q + 3]);
+                    for (int q = 0; q < 4; ++q) p[q] = make_float4(t[4 * q], t[4 * q + 1], t[4 * q + 2], t[4 * q + 3]);
+                }
             }
-        }
+    }
     if (tid < 16 * CO8) {
 #pragma unroll
         for (int e = 0; e < 8; ++e) red[tid][e] = dbacc[e];
@@ -919,7 +922,7 @@ cudaError_t dw_launch(const DwArgs& a, int grid, cudaStream_t s)
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    k_conv3x3_dw<CIN, COUT><<<grid, 128, smem, s>>>(a);
+    k_conv3x3_dw<CIN, COUT><<<grid, kDwThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 

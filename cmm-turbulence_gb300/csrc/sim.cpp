@@ -990,12 +990,14 @@ int EulerSim::restart_from_map_stack()
     const size_t nc4 = (size_t)4 * gc.N, np4 = (size_t)4 * gp.N;
     std::vector<double> h(2 * nc4);
     auto upload_map = [&](double* X, double* Y, float4* M) -> int {
-        // host planes -> the device map (FP64 planes, or a displacement map in the mixed form)
-        double* dX = mixed_ ? ChiX_new : X;
-        double* dY = mixed_ ? ChiY_new : Y;
+        // host planes -> the device map: a displacement map M of the mixed form (through the
+        // FP64 scratch planes), or the FP64 planes X, Y (the plain form's maps, and the
+        // forward maps of both forms: M null)
+        double* dX = M ? ChiX_new : X;
+        double* dY = M ? ChiY_new : Y;
         CMM_CUDA(cudaMemcpyAsync(dX, h.data(), sizeof(double) * nc4, cudaMemcpyHostToDevice, stream));
         CMM_CUDA(cudaMemcpyAsync(dY, h.data() + nc4, sizeof(double) * nc4, cudaMemcpyHostToDevice, stream));
-        if (mixed_) CMM_LAUNCH(1, launch_planes_to_map(dX, dY, gc, M, stream));
+        if (M) CMM_LAUNCH(1, launch_planes_to_map(dX, dY, gc, M, stream));
         CMM_CUDA(cudaStreamSynchronize(stream));
         return kOk;
     };

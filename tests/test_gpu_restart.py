@@ -226,6 +226,42 @@ def test_mixed_form_restarts_from_fp64_files_and_writes_restartable_files(tmp_pa
     assert abs(a - b) <= 1e-5 * abs(a)
 
 
+def test_mixed_form_forward_map_writes_and_restarts(tmp_path):
+    """precision=mixed with forward_map=1: the MapStack folder holds the FP64 forward map and
+    one forward sub-map per remap beside the backward ones, equal to the run's state; both
+    forms restart from it at t = 1 with that forward map and continue to t = 1.5 (remaps at
+    5e-4, above the FP32 maps' ~1e-4 of E_inc on this 64^2 map)."""
+    text = _param_text(1.0, precision="mixed", threshold=5e-4).replace("forward_map\t=\t0", "forward_map\t=\t1")
+    (tmp_path / "a").mkdir()
+    sim = _sim(tmp_path / "a", text)
+    sim.init()
+    sim.run()
+    n = int(sim.scalar("map_counter"))
+    assert n >= 1
+    stack_dir = os.path.join(str(tmp_path / "a"), "data", sim.file_name(), "MapStack")
+    files = O.read_map_stack_dir(stack_dir)
+    assert sum(1 for k in files if k.startswith("Map_ChiX_f_H_") and k != "Map_ChiX_f_H_coarse") == n
+    fx, fy = sim.field("Map_ChiX_f_H_coarse").copy(), sim.field("Map_ChiY_f_H_coarse").copy()
+    np.testing.assert_array_equal(files["Map_ChiX_f_H_coarse"], fx)
+    np.testing.assert_array_equal(files["Map_ChiY_f_H_coarse"], fy)
+    sim.close()
+    ends = {}
+    for prec in ("fp64", "mixed"):
+        rtext = _param_text(1.5, restart_time=1.0, save=0, precision=prec, threshold=5e-4).replace(
+            "forward_map\t=\t0", "forward_map\t=\t1")
+        r = _sim(tmp_path, rtext, ["restart_location=%s" % stack_dir, "sim_name=rf_%s" % prec])
+        r.init()
+        assert int(r.scalar("map_counter")) == n
+        np.testing.assert_array_equal(r.field("Map_ChiX_f_H_coarse"), fx)
+        r.run()
+        ends[prec] = (int(r.scalar("map_counter")), r.field("Map_ChiX_f_H_coarse").copy(), r.scalar("enstrophy"))
+        r.close()
+    (cp, xp, zp), (cm, xm, zm) = ends["fp64"], ends["mixed"]
+    assert abs(zm - zp) <= 1e-5 * abs(zp)
+    if cp == cm:
+        assert np.max(np.abs(xm[: xm.size // 4] - xp[: xp.size // 4])) < 1e-4
+
+
 def test_restart_reports_missing_files_and_oversized_stacks(tmp_path):
     m = cmm()
     empty = tmp_path / "nothing"

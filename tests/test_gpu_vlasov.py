@@ -95,6 +95,32 @@ def test_vlasov_plain_fp64_matches_oracle(tmp_path, case):
     sim.close()
 
 
+def test_vlasov_forward_map_matches_oracle(tmp_path):
+    """forward_map=1 in the Vlasov driver (cmm-vlasov1d.cu:815, 845): the forward map advected
+    on the same separable psi history, its incompressibility and the invertibility check each
+    step, and the forward map after a run with remaps, against the oracle."""
+    ic, bounds = CASES["landau"]
+    args = [a for a in _args(tmp_path, ic, bounds) if not a.startswith("forward_map")] + ["forward_map=1"]
+    m = cmm()
+    sim = m.Simulation(args)
+    sim.init()
+    o, s = _oracle(args)
+    o.init()
+    b = s.domain_bounds
+    tol = einc_tol(max(abs(x) for x in b[:4]), (b[1] - b[0]) / s.grid_coarse)
+    steps = 0
+    while sim.step(1) != 1:
+        o.step(s.dt)
+        ef, ev = o.forward_monitors()
+        assert abs(sim.scalar("e_inc_forward") - ef) < tol, steps
+        assert abs(sim.scalar("e_invertibility") - ev) < 1e-9, steps
+        steps += 1
+    assert steps == 64 and int(sim.scalar("map_counter")) == o.map_count() >= 2
+    assert map_err(sim.field("Map_ChiX_f_H_coarse"), o.chix_f()) < 1e-10
+    assert map_err(sim.field("Map_ChiY_f_H_coarse"), o.chiy_f()) < 1e-10
+    sim.close()
+
+
 def test_vlasov_known_answers_at_t0(tmp_path):
     """Landau damping at t = 0: Epot = pi/100, |E_1| = 0.05, Ekin = 2 pi,
     Mass = 4 pi (derivation in test_oracle_golden.py)."""

@@ -22,7 +22,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"] + GENCODE
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + os.path.join(CUDA_HOME, "include")]
-LIBS = ["-L" + os.path.join(CUDA_HOME, "lib64"), "-lcufft", "-lcurand", "-lcudart"]
+LIBS = ["-L" + os.path.join(CUDA_HOME, "lib64"), "-lcurand", "-lcudart"]
 
 
 def sources():

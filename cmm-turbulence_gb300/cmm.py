@@ -38,6 +38,7 @@ EXPORTS = [
     "cmm_upsampler_get_scales", "cmm_upsampler_collect", "cmm_upsampler_dataset_size", "cmm_upsampler_train",
     "cmm_upsampler_loss_grad", "cmm_upsampler_infer", "cmm_upsampler_evaluate", "cmm_upsampler_save",
     "cmm_upsampler_load", "cmm_attach_upsampler", "cmm_conv3x3", "cmm_conv3x3_weight_grad", "cmm_upsampler_time_infer",
+    "cmm_fft_create", "cmm_fft_r2c", "cmm_fft_c2r", "cmm_fft_destroy",
 ]
 
 
@@ -95,6 +96,10 @@ def lib():
     L.cmm_poisson_create.argtypes = [gp, gp, C.c_double, vp, C.POINTER(vp)]
     L.cmm_poisson_hermite.argtypes = [vp, vp, vp]
     L.cmm_poisson_destroy.argtypes = [vp]
+    L.cmm_fft_create.argtypes = [ip, ip, ip, vp, C.POINTER(vp)]
+    L.cmm_fft_r2c.argtypes = [vp, vp, vp, ip]
+    L.cmm_fft_c2r.argtypes = [vp, vp, vp, ip]
+    L.cmm_fft_destroy.argtypes = [vp]
     L.cmm_particles_advect.argtypes = [gp, vp, ip, C.POINTER(vp), ip, dp, C.c_double, ip, vp]
     L.cmm_diagnostics.argtypes = [gp, vp, gp, vp, dp, vp]
     L.cmm_diagnostics_noalloc.argtypes = [gp, vp, gp, vp, dp, vp]
@@ -269,6 +274,29 @@ class Poisson:
     def close(self):
         if self.h:
             lib().cmm_poisson_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+class FFT:
+    """The library's 2D real FFT: ny x nx reals <-> ny x (nx/2+1) complex (unnormalised),
+    precision 0 = FP64, 1 = FP32 (device buffers: torch tensors or raw pointers)."""
+
+    def __init__(self, nx, ny, precision=0, stream=None):
+        self.h = C.c_void_p()
+        check(lib().cmm_fft_create(int(nx), int(ny), int(precision), stream, C.byref(self.h)))
+
+    def r2c(self, x, out, batch=1):
+        return check(lib().cmm_fft_r2c(self.h, _dptr(x), _dptr(out), int(batch)))
+
+    def c2r(self, x, out, batch=1):
+        return check(lib().cmm_fft_c2r(self.h, _dptr(x), _dptr(out), int(batch)))
+
+    def close(self):
+        if self.h:
+            lib().cmm_fft_destroy(self.h)
             self.h = None
 
     def __del__(self):

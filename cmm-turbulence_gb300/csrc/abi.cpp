@@ -2,7 +2,6 @@
 #include "../../include/cmm_abi.h"
 
 #include <cuda_runtime.h>
-#include <cufft.h>
 
 #include <cstring>
 #include <new>
@@ -30,6 +29,11 @@ struct cmm_poisson {
     cmm::FftPlans pv, pp;
     double2* spec = nullptr;
     double2* spec4 = nullptr;
+};
+
+struct cmm_fft {
+    cmm::fft::Plan2D plan;
+    cudaStream_t stream = nullptr;
 };
 
 struct cmm_vlasov {
@@ -325,15 +329,13 @@ int cmm_vlasov_create(const cmm_grid* grid_vort, const cmm_grid* grid_psi, void*
               cudaMalloc((void**)&p->scal, sizeof(double) * 16) == cudaSuccess &&
               cudaMalloc((void**)&p->row, sizeof(double) * (p->gp.NX > p->gp.NY ? p->gp.NX : p->gp.NY)) == cudaSuccess;
     for (int k = 0; k < 3 && ok; ++k) ok = cudaMalloc((void**)&p->c[k], sizeof(double2) * cn) == cudaSuccess;
-    if (!ok) { cmm_vlasov_destroy(p); return fail(CMM_ERR_CUDA, "cuFFT plan or cudaMalloc failed"); }
+    if (!ok) { cmm_vlasov_destroy(p); return fail(CMM_ERR_CUDA, "FFT plan or cudaMalloc failed"); }
     // the periodification h(v) and h'(v) once
     cudaError_t e = cmm::launch_vlasov_bump(p->gp, p->row, p->stream);
-    if (e == cudaSuccess && cufftExecD2Z(p->plans.d2z_p, p->row, reinterpret_cast<cufftDoubleComplex*>(p->c[0])) != CUFFT_SUCCESS)
-        e = cudaErrorUnknown;
+    if (e == cudaSuccess) e = cmm::fft_d2z_1d(p->plans.p, p->row, p->c[0], p->stream);
     if (e == cudaSuccess) e = cmm::launch_vlasov_h_spec(p->c[0], p->gp, p->c[1], p->c[2], p->stream);
-    if (e == cudaSuccess && (cufftExecZ2D(p->plans.z2d_p, reinterpret_cast<cufftDoubleComplex*>(p->c[1]), p->h) != CUFFT_SUCCESS ||
-                             cufftExecZ2D(p->plans.z2d_p, reinterpret_cast<cufftDoubleComplex*>(p->c[2]), p->h + p->gp.NY) != CUFFT_SUCCESS))
-        e = cudaErrorUnknown;
+    if (e == cudaSuccess) e = cmm::fft_z2d_1d(p->plans.p, p->c[1], p->h, p->stream);
+    if (e == cudaSuccess) e = cmm::fft_z2d_1d(p->plans.p, p->c[2], p->h + p->gp.NY, p->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
     if (e != cudaSuccess) { cmm_vlasov_destroy(p); return cuda_rc(e, "cmm_vlasov_create"); }
     *out = p;
@@ -350,12 +352,10 @@ int cmm_vlasov_potential(cmm_vlasov* p, const cmm_grid* grid_map, const cmm_grid
     cudaStream_t s = p->stream;
     cudaError_t e = cmm::launch_sample_vort(gm, p->gv, gf, chix, chiy, f_fine_H, molly_stencil, p->fs, p->gv.NX, s);
     if (e == cudaSuccess) e = cmm::launch_vlasov_rho(p->fs, nullptr, p->gv, p->part, p->rho, s);
-    if (e == cudaSuccess && cufftExecD2Z(p->plans.d2z_v, p->rho, reinterpret_cast<cufftDoubleComplex*>(p->c[0])) != CUFFT_SUCCESS)
-        return fail(CMM_ERR_CUDA, "cuFFT D2Z failed");
+    if (e == cudaSuccess) e = cmm::fft_d2z_1d(p->plans.v, p->rho, p->c[0], s);
     if (e == cudaSuccess) e = cmm::launch_vlasov_phi_spec(p->c[0], p->gv, p->gp, p->c[1], p->c[2], s);
-    if (e == cudaSuccess && (cufftExecZ2D(p->plans.z2d_p, reinterpret_cast<cufftDoubleComplex*>(p->c[1]), p->phi) != CUFFT_SUCCESS ||
-                             cufftExecZ2D(p->plans.z2d_p, reinterpret_cast<cufftDoubleComplex*>(p->c[2]), p->phi + p->gp.NX) != CUFFT_SUCCESS))
-        return fail(CMM_ERR_CUDA, "cuFFT Z2D failed");
+    if (e == cudaSuccess) e = cmm::fft_z2d_1d(p->plans.p, p->c[1], p->phi, s);
+    if (e == cudaSuccess) e = cmm::fft_z2d_1d(p->plans.p, p->c[2], p->phi + p->gp.NX, s);
     if (e == cudaSuccess) e = cmm::launch_vlasov_assemble(p->phi, p->phi + p->gp.NX, p->h, p->h + p->gp.NY, p->gp, psi_out, s);
     return cuda_rc(e, "cmm_vlasov_potential");
 }
@@ -371,8 +371,7 @@ int cmm_vlasov_diagnostics(cmm_vlasov* p, const cmm_grid* grid_coarse, const dou
     cudaError_t e = cmm::launch_vlasov_moments(f_coarse, gc, p->red, p->scal, s);
     if (e == cudaSuccess) e = cmm::launch_sumsq(psi + gp.N, gp.NX, p->red, p->scal + 3, s);   // first row of psi_x
     if (e == cudaSuccess) e = cudaMemcpyAsync(p->row, psi + gp.N, sizeof(double) * gp.NX, cudaMemcpyDeviceToDevice, s);
-    if (e == cudaSuccess && cufftExecD2Z(p->plans.d2z_p, p->row, reinterpret_cast<cufftDoubleComplex*>(p->c[0])) != CUFFT_SUCCESS)
-        return fail(CMM_ERR_CUDA, "cuFFT D2Z failed");
+    if (e == cudaSuccess) e = cmm::fft_d2z_1d(p->plans.p, p->row, p->c[0], s);
     if (e == cudaSuccess) e = cmm::launch_vlasov_modes(p->c[0], gp.NX, gp.NX_fft, p->scal + 4, s);
     double h[8] = {0};
     if (e == cudaSuccess) e = cudaMemcpyAsync(h, p->scal, sizeof(double) * 8, cudaMemcpyDeviceToHost, s);
@@ -407,6 +406,44 @@ int cmm_sample_vort(const cmm_grid* grid_map, const cmm_grid* grid_out, const cm
                                            static_cast<cudaStream_t>(stream)), "cmm_sample_vort");
 }
 
+int cmm_fft_create(int nx, int ny, int precision, void* stream, cmm_fft** out)
+{
+    if (!out) return fail(CMM_ERR_PARAM, "out is NULL");
+    *out = nullptr;
+    if (precision != 0 && precision != 1) return fail(CMM_ERR_PARAM, "precision must be 0 (FP64) or 1 (FP32)");
+    cmm_fft* f = new (std::nothrow) cmm_fft();
+    if (!f) return fail(CMM_ERR_PARAM, "out of host memory");
+    f->stream = static_cast<cudaStream_t>(stream);
+    const int rc = cmm::fft::plan_create(f->plan, nx, ny, precision == 0, f->stream);
+    if (rc) {
+        delete f;
+        return rc == -1 ? fail(CMM_ERR_PARAM, "unsupported FFT shape (nx even, nx/2 and ny <= 8192, prime factors <= 13)")
+                        : fail(CMM_ERR_CUDA, "FFT twiddle tables: CUDA error");
+    }
+    *out = f;
+    return CMM_OK;
+}
+
+int cmm_fft_r2c(cmm_fft* f, const void* in, void* out, int batch)
+{
+    if (!f || !in || !out || batch < 1) return fail(CMM_ERR_PARAM, "bad argument");
+    return cuda_rc(cmm::fft::r2c(f->plan, in, out, batch, f->stream), "cmm_fft_r2c");
+}
+
+int cmm_fft_c2r(cmm_fft* f, void* in, void* out, int batch)
+{
+    if (!f || !in || !out || batch < 1) return fail(CMM_ERR_PARAM, "bad argument");
+    return cuda_rc(cmm::fft::c2r(f->plan, in, out, batch, f->stream), "cmm_fft_c2r");
+}
+
+int cmm_fft_destroy(cmm_fft* f)
+{
+    if (!f) return CMM_OK;
+    cmm::fft::plan_destroy(f->plan);
+    delete f;
+    return CMM_OK;
+}
+
 int cmm_poisson_create(const cmm_grid* grid_vort, const cmm_grid* grid_psi, double freq_cut_psi, void* stream,
                        cmm_poisson** out)
 {
@@ -419,7 +456,7 @@ int cmm_poisson_create(const cmm_grid* grid_vort, const cmm_grid* grid_psi, doub
     p->stream = static_cast<cudaStream_t>(stream);
     if (!cmm::make_plans(p->pv, p->gv, p->stream) || !cmm::make_plans(p->pp, p->gp, p->stream)) {
         cmm_poisson_destroy(p);
-        return fail(CMM_ERR_CUDA, "cuFFT plan creation failed");
+        return fail(CMM_ERR_PARAM, "FFT plan creation failed (grid sizes need NX even, sides <= 8192, prime factors <= 13)");
     }
     long long cmax = p->gv.Nfft > p->gp.Nfft ? p->gv.Nfft : p->gp.Nfft;
     if (cudaMalloc((void**)&p->spec, sizeof(double2) * (size_t)cmax) != cudaSuccess ||
@@ -434,13 +471,10 @@ int cmm_poisson_create(const cmm_grid* grid_vort, const cmm_grid* grid_psi, doub
 int cmm_poisson_hermite(cmm_poisson* p, const double* vort, double* psi_out)
 {
     if (!p || !vort || !psi_out) return fail(CMM_ERR_PARAM, "NULL argument");
-    if (cufftExecD2Z(p->pv.d2z, const_cast<double*>(vort), reinterpret_cast<cufftDoubleComplex*>(p->spec)) != CUFFT_SUCCESS)
-        return fail(CMM_ERR_CUDA, "cuFFT D2Z failed");
-    int rc = cuda_rc(cmm::launch_spec_psi(p->spec, p->gv, p->gp, p->freq, p->spec4, p->stream), "spec_psi");
-    if (rc) return rc;
-    if (cufftExecZ2D(p->pp.z2d4, reinterpret_cast<cufftDoubleComplex*>(p->spec4), psi_out) != CUFFT_SUCCESS)
-        return fail(CMM_ERR_CUDA, "cuFFT Z2D failed");
-    return CMM_OK;
+    int rc = cuda_rc(cmm::fft_d2z(p->pv, vort, p->spec, p->stream), "FFT D2Z");
+    if (!rc) rc = cuda_rc(cmm::launch_spec_psi(p->spec, p->gv, p->gp, p->freq, p->spec4, p->stream), "spec_psi");
+    if (!rc) rc = cuda_rc(cmm::fft_z2d(p->pp, p->spec4, psi_out, 4, p->stream), "FFT Z2D");
+    return rc;
 }
 
 int cmm_poisson_destroy(cmm_poisson* p)

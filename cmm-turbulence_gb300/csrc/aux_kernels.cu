@@ -1,7 +1,6 @@
 // aux_kernels.cu -- tracer particles, spectral operators of the Poisson /
 // Hermite solve, and deterministic reductions (FP64, sm_103a).
 #include <cuda_runtime.h>
-#include <cufft.h>
 
 #include "kernels.hpp"
 
@@ -379,25 +378,25 @@ cudaError_t launch_spec_grad(const double2* F, const Grid& g, double2* out2, cud
 
 bool make_plans(FftPlans& p, const Grid& g, cudaStream_t s)
 {
-    int n[2] = {g.NY, g.NX};
     p.g = g;
-    if (cufftPlanMany(&p.d2z, 2, n, nullptr, 1, 0, nullptr, 1, 0, CUFFT_D2Z, 1) != CUFFT_SUCCESS) return false;
-    if (cufftPlanMany(&p.z2d4, 2, n, nullptr, 1, 0, nullptr, 1, 0, CUFFT_Z2D, 4) != CUFFT_SUCCESS) return false;
-    if (cufftPlanMany(&p.z2d1, 2, n, nullptr, 1, 0, nullptr, 1, 0, CUFFT_Z2D, 1) != CUFFT_SUCCESS) return false;
-    cufftSetStream(p.d2z, s);
-    cufftSetStream(p.z2d4, s);
-    cufftSetStream(p.z2d1, s);
-    p.ok = true;
-    return true;
+    p.ok = fft::plan_create(p.p, g.NX, g.NY, true, s) == 0;
+    return p.ok;
 }
 
 void destroy_plans(FftPlans& p)
 {
-    if (p.d2z) cufftDestroy(p.d2z);
-    if (p.z2d4) cufftDestroy(p.z2d4);
-    if (p.z2d1) cufftDestroy(p.z2d1);
-    p.d2z = p.z2d4 = p.z2d1 = 0;
+    fft::plan_destroy(p.p);
     p.ok = false;
+}
+
+cudaError_t fft_d2z(const FftPlans& p, const double* in, double2* out, cudaStream_t s)
+{
+    return fft::r2c(p.p, in, out, 1, s);
+}
+
+cudaError_t fft_z2d(const FftPlans& p, double2* in, double* out, int batch, cudaStream_t s)
+{
+    return fft::c2r(p.p, in, out, batch, s);
 }
 
 // ---------------------------------------------------------------------------

@@ -15,8 +15,8 @@ EnsembleSim::~EnsembleSim()
 {
     drop_graphs();
     for (auto& c : cls_) {
-        if (c.r2c) cufftDestroy(c.r2c);
-        if (c.c2r4) cufftDestroy(c.c2r4);
+        fft::plan_destroy(c.pv);
+        fft::plan_destroy(c.pp);
         if (c.real) cudaFree(c.real);
         if (c.spec) cudaFree(c.spec);
         if (c.spec4) cudaFree(c.spec4);
@@ -106,18 +106,11 @@ int EnsembleSim::init()
         ENS_CUDA(cudaMalloc((void**)&c.spec4, sizeof(float2) * c.spec4_stride * nb));
         // R2C: one transform per member (input stride real_stride, output stride Nv_fft);
         // C2R: four per member (input stride Np_fft, output stride Np, members contiguous)
-        int nv[2] = {s0.gv.NY, s0.gv.NX}, np[2] = {s0.gp.NY, s0.gp.NX};
-        int inv[2] = {s0.gv.NY, s0.gv.NX}, onv[2] = {s0.gv.NY, s0.gv.NX_fft};
-        int inp[2] = {s0.gp.NY, s0.gp.NX_fft}, onp[2] = {s0.gp.NY, s0.gp.NX};
-        if (cufftPlanMany(&c.r2c, 2, nv, inv, 1, (int)c.real_stride, onv, 1, (int)c.spec_stride, CUFFT_R2C, (int)nb) !=
-                CUFFT_SUCCESS ||
-            cufftPlanMany(&c.c2r4, 2, np, inp, 1, (int)s0.gp.Nfft, onp, 1, (int)s0.gp.N, CUFFT_C2R, (int)(4 * nb)) !=
-                CUFFT_SUCCESS) {
-            err = "cuFFT ensemble plan creation failed";
+        if (fft::plan_create(c.pv, s0.gv.NX, s0.gv.NY, false, stream) ||
+            fft::plan_create(c.pp, s0.gp.NX, s0.gp.NY, false, stream)) {
+            err = "FFT plan creation failed (ensemble size class)";
             return kErrCuda;
         }
-        cufftSetStream(c.r2c, stream);
-        cufftSetStream(c.c2r4, stream);
         for (size_t k = 0; k < c.members.size(); ++k) {
             const int i = c.members[k];
             // one buffer, two views: member k's vort-grid sample at real + k real_stride (R2C
@@ -191,20 +184,17 @@ int EnsembleSim::phase_b()
     if ((rc = launch(kEnsSampleVort, blocks[kEnsSampleVort]))) return rc;
     for (auto& c : cls_) {
         if (!c.active) continue;
-        launches++;
-        if (cufftExecR2C(c.r2c, c.real, reinterpret_cast<cufftComplex*>(c.spec)) != CUFFT_SUCCESS) {
-            err = "cuFFT R2C (ensemble)";
-            return kErrCuda;
-        }
+        launches += 2;   // row pass + column pass
+        const int nb = (int)c.members.size();
+        if ((rc = check(fft::r2c(c.pv, c.real, c.spec, nb, stream, c.real_stride, c.spec_stride), "FFT R2C (ensemble)")))
+            return rc;
     }
     if ((rc = launch(kEnsSpec, blocks[kEnsSpec]))) return rc;
     for (auto& c : cls_) {
         if (!c.active) continue;
-        launches++;
-        if (cufftExecC2R(c.c2r4, reinterpret_cast<cufftComplex*>(c.spec4), c.real) != CUFFT_SUCCESS) {
-            err = "cuFFT C2R (ensemble)";
-            return kErrCuda;
-        }
+        launches += 2;
+        const int nb = (int)c.members.size();
+        if ((rc = check(fft::c2r(c.pp, c.spec4, c.real, 4 * nb, stream), "FFT C2R (ensemble)"))) return rc;
     }
     if ((rc = launch(kEnsNodes, blocks[kEnsNodes])) || (rc = launch(kEnsSampleCoarse, blocks[kEnsSampleCoarse])))
         return rc;

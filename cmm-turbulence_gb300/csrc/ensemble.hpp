@@ -7,18 +7,17 @@
 //   phase A: descriptors up, precombinations, map advection, incompressibility check,
 //            the members' E_inc down (one 8-byte value each, one copy);
 //   host:    remaps of the members whose E_inc asks for one, psi rotation;
-//   phase B: descriptors up, omega on the vort grids, cuFFT R2C per size class, the
-//            spectral psi, cuFFT C2R (4 planes) per size class, psi nodes and Lagrange
+//   phase B: descriptors up, omega on the vort grids, one batched R2C per size class, the
+//            spectral psi, one batched C2R (4 planes) per size class, psi nodes and Lagrange
 //            combinations, coarse vorticity.
 // Members of one size class share contiguous FFT buffers, so each class transforms in one
-// batched cuFFT call.  The batched kernels walk a work list of 256-thread tiles with a
+// batched transform (csrc/fft.hpp).  The batched kernels walk a work list of 256-thread tiles with a
 // persistent grid whose size per kernel is picked by timing the candidates on the first
 // iteration (every batched kernel is idempotent within a step, so the trials cost time but
 // change nothing).  From the second iteration on each phase is a CUDA graph, re-captured
 // when a size class finishes.
 #pragma once
 #include <cuda_runtime.h>
-#include <cufft.h>
 
 #include <memory>
 #include <string>
@@ -48,7 +47,7 @@ public:
     bool use_graphs = true;
     long long member_steps = 0;      // member time steps taken
     long long iterations = 0;
-    long long launches = 0;          // batched launches + cuFFT calls + per-member remap work
+    long long launches = 0;          // batched launches + transform kernels + per-member remap work
     int blocks[kEnsKinds] = {0};     // tuned persistent grid per kernel kind
     int tiles[kEnsKinds] = {0};      // work-list length per kernel kind
 
@@ -60,7 +59,7 @@ private:
         float2* spec = nullptr;          // per member Nv_fft
         float2* spec4 = nullptr;         // per member 4 Np_fft
         long long real_stride = 0, spec_stride = 0, spec4_stride = 0;
-        cufftHandle r2c = 0, c2r4 = 0;
+        fft::Plan2D pv, pp;             // FP32 transforms of the vort and psi grids
         bool active = true;
     };
     int phase_a();

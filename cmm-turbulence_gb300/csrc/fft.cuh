@@ -1,0 +1,262 @@
+// fft.cuh -- the library's own FFT engine (sm_103a): mixed-radix Stockham
+// transforms in shared memory, executed by one thread block over a batch of
+// transforms, and the device pieces of the real <-> half-spectrum transforms.
+//
+// The reference computes every transform of the psi solve and of the remap with
+// cuFFT (D2Z / Z2D plans, Cuda-CMM/src/grid/cmm-grid2d.cu:123-131; called from
+// src/simulation/cmm-simulation-host.cu:299-375 and src/numerical/cmm-fft.cu:398-429).
+// Here they are hand-written so that the passes around them (sampling, spectral
+// operators, Hermite node writes) can be fused into the same kernels.
+//
+// Conventions (those of cuFFT and of the CPU oracle):
+//   forward   X[k] = sum_j x[j] exp(-2 pi i jk/n)      (unnormalised)
+//   inverse   x[j] = sum_k X[k] exp(+2 pi i jk/n)      (unnormalised)
+//   R2C of N reals keeps k = 0..N/2; C2R reads k = 0..N/2 and ignores the
+//   imaginary parts of k = 0 and k = N/2 (the Hermitian extension of the half
+//   spectrum with those two bins taken as real).
+//
+// Algorithm.  A length-n complex transform, n = R_1 R_2 ... R_m with radices
+// 2, 3, 4, 5, 7, 8, 11, 13, runs m Stockham (self-sorting) passes.  Pass with
+// radix R after a span p (product of the previous radices): butterfly
+// i in [0, n/R), k = i mod p, inputs a_r = x[i + r n/R] twiddled by
+// w^(r k n/(pR)) (w = exp(-2 pi i/n)), an R-point DFT, outputs
+// y[(i - k) R + k + r p].  Every pass reads its inputs into registers, the
+// block synchronises, and the outputs are written back in place (one buffer
+// of n values per transform in shared memory).  Twiddles come from a table
+// exp(-2 pi i t/T) (t < T) in global memory, computed on the host in extended
+// precision; a transform of length n = T/ts reads it at stride ts.
+//
+// Real transforms of even length N pack x into the complex length-N/2
+// sequence z[m] = x[2m] + i x[2m+1]:
+//   R2C  X[k] = 1/2 [(Z_k + conj Z_{n-k}) - i W^k (Z_k - conj Z_{n-k})],  W = exp(-2 pi i/N)
+//   C2R  Z_k = (X_k + conj X_{n-k}) + i W^-k (X_k - conj X_{n-k}),  z = inverse(Z),
+//        x[2m] = Re z_m, x[2m+1] = Im z_m.
+// (the standard even/odd split of a real DFT).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace cmm {
+namespace fft {
+
+constexpr int kMaxPasses = 24;
+
+// radices of one transform length, in pass order
+struct RadixPlan {
+    int n;                      // complex length
+    int np;                     // number of passes
+    unsigned char r[kMaxPasses];
+};
+
+#ifdef __CUDACC__
+template <typename T> struct Cx;
+template <> struct Cx<float> { using V = float2; };
+template <> struct Cx<double> { using V = double2; };
+
+__device__ __forceinline__ float2 mk(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ double2 mk(double a, double b) { return make_double2(a, b); }
+
+template <typename V> __device__ __forceinline__ V cadd(const V& a, const V& b) { return mk(a.x + b.x, a.y + b.y); }
+template <typename V> __device__ __forceinline__ V csub(const V& a, const V& b) { return mk(a.x - b.x, a.y - b.y); }
+template <typename V> __device__ __forceinline__ V cmul(const V& a, const V& b)
+{
+    return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename V> __device__ __forceinline__ V cconj(const V& a) { return mk(a.x, -a.y); }
+// multiply by -i (forward) or +i (inverse)
+template <typename V> __device__ __forceinline__ V rot(const V& a, bool inv) { return inv ? mk(-a.y, a.x) : mk(a.y, -a.x); }
+
+// shared-memory padding: one spare slot every 32 (8-byte) or 8 (16-byte) values
+// keeps the strided butterfly writes of the first passes off a single bank
+template <typename V> __device__ __forceinline__ int pad(int i);
+template <> __device__ __forceinline__ int pad<float2>(int i) { return i + (i >> 5); }
+template <> __device__ __forceinline__ int pad<double2>(int i) { return i + (i >> 3); }
+template <typename V> __host__ __device__ constexpr int padded_len(int n) { return sizeof(V) == 8 ? n + (n >> 5) + 1 : n + (n >> 3) + 1; }
+
+// ---------------------------------------------------------------- R-point DFTs (in registers)
+template <typename V> __device__ __forceinline__ void dft2(V* a)
+{
+    V t = a[1];
+    a[1] = csub(a[0], t);
+    a[0] = cadd(a[0], t);
+}
+
+template <typename V> __device__ __forceinline__ void dft4(V* a, bool inv)
+{
+    V s0 = cadd(a[0], a[2]), d0 = csub(a[0], a[2]);
+    V s1 = cadd(a[1], a[3]), d1 = rot(csub(a[1], a[3]), inv);
+    a[0] = cadd(s0, s1);
+    a[2] = csub(s0, s1);
+    a[1] = cadd(d0, d1);
+    a[3] = csub(d0, d1);
+}
+
+template <typename V> __device__ __forceinline__ void dft8(V* a, bool inv)
+{
+    using T = decltype(a[0].x);
+    const T h = (T)0.70710678118654752440084436210484903928;
+    V e[4] = {a[0], a[2], a[4], a[6]}, o[4] = {a[1], a[3], a[5], a[7]};
+    dft4(e, inv);
+    dft4(o, inv);
+    // o[k] *= exp(-+ 2 pi i k / 8)
+    V o1 = o[1], o3 = o[3];
+    if (!inv) {
+        o[1] = mk(h * (o1.x + o1.y), h * (o1.y - o1.x));
+        o[3] = mk(h * (o3.y - o3.x), -h * (o3.x + o3.y));
+    } else {
+        o[1] = mk(h * (o1.x - o1.y), h * (o1.x + o1.y));
+        o[3] = mk(-h * (o3.x + o3.y), h * (o3.x - o3.y));
+    }
+    o[2] = rot(o[2], inv);
+    for (int k = 0; k < 4; ++k) {
+        a[k] = cadd(e[k], o[k]);
+        a[k + 4] = csub(e[k], o[k]);
+    }
+}
+
+template <typename V> __device__ __forceinline__ void dft3(V* a, bool inv)
+{
+    using T = decltype(a[0].x);
+    const T c = (T)-0.5, s = inv ? (T)0.86602540378443864676372317075293618347 : (T)-0.86602540378443864676372317075293618347;
+    V t1 = cadd(a[1], a[2]), t2 = csub(a[1], a[2]);
+    V m1 = mk(a[0].x + c * t1.x, a[0].y + c * t1.y);
+    V m2 = mk(-s * t2.y, s * t2.x);   // i s t2
+    a[0] = cadd(a[0], t1);
+    a[1] = cadd(m1, m2);
+    a[2] = csub(m1, m2);
+}
+
+// any small R: direct DFT, roots of unity from the twiddle table (entry m ts n/R ... )
+template <int R, typename V>
+__device__ __forceinline__ void dft_generic(V* a, bool inv, const V* __restrict__ tw, long long rstep)
+{
+    V out[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        V s = a[0];
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+            V w = __ldg(tw + (long long)((q * r) % R) * rstep);
+            if (inv) w = cconj(w);
+            s = cadd(s, cmul(a[r], w));
+        }
+        out[q] = s;
+    }
+#pragma unroll
+    for (int q = 0; q < R; ++q) a[q] = out[q];
+}
+
+// ---------------------------------------------------------------- one Stockham pass
+// nb transforms of length n at s[pad(b n + i)]; VPT = values per thread the block was
+// sized for (nb n <= VPT blockDim.x)
+template <int R, int VPT, typename V>
+__device__ __forceinline__ void pass(V* s, int nb, int n, int p, const V* __restrict__ tw, int ts, bool inv)
+{
+    constexpr int B = (VPT + R - 1) / R;
+    const int nR = n / R;
+    const int total = nb * nR;
+    const long long tstep = (long long)(n / (p * R)) * ts;   // table step of w^(r k n/(pR))
+    V v[B][R];
+    int dst[B];
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+        const int t = threadIdx.x + j * blockDim.x;
+        dst[j] = -1;
+        if (t < total) {
+            const int b = t / nR, i = t - b * nR;
+            const int k = i % p;
+            const int base = b * n;
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[j][r] = s[pad<V>(base + i + r * nR)];
+            if (k != 0) {
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    V w = __ldg(tw + (long long)(r * k) * tstep);
+                    if (inv) w = cconj(w);
+                    v[j][r] = cmul(v[j][r], w);
+                }
+            }
+            if (R == 2) dft2(v[j]);
+            else if (R == 4) dft4(v[j], inv);
+            else if (R == 8) dft8(v[j], inv);
+            else if (R == 3) dft3(v[j], inv);
+            else dft_generic<R>(v[j], inv, tw, (long long)(n / R) * ts);
+            dst[j] = base + (i - k) * R + k;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+        if (dst[j] >= 0) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) s[pad<V>(dst[j] + r * p)] = v[j][r];
+        }
+    }
+    __syncthreads();
+}
+
+// radix families: a kernel instantiated for a family carries only those radices' passes,
+// so the common power-of-two (and 3 * 2^k) lengths run without the register pressure of
+// the large generic radices
+enum Family { kPow2 = 0, kPow2x3 = 1, kAny = 2 };
+
+inline int family_of(const RadixPlan& P)
+{
+    int f = kPow2;
+    for (int q = 0; q < P.np; ++q) {
+        if (P.r[q] == 3 && f < kPow2x3) f = kPow2x3;
+        if (P.r[q] > 4 && P.r[q] != 8) f = kAny;
+    }
+    return f;
+}
+
+// all passes of nb length-n transforms held in shared memory (in place); every thread
+// of the block takes part.  tw: table exp(-2 pi i t / (n ts)), t < n ts.
+template <int VPT, int FAM, typename V>
+__device__ __forceinline__ void block_fft(V* s, int nb, const RadixPlan& P, const V* __restrict__ tw, int ts, bool inv)
+{
+    int p = 1;
+    for (int q = 0; q < P.np; ++q) {
+        const int R = P.r[q];
+        if (R == 8) pass<8, VPT>(s, nb, P.n, p, tw, ts, inv);
+        else if (R == 4) pass<4, VPT>(s, nb, P.n, p, tw, ts, inv);
+        else if (R == 2) pass<2, VPT>(s, nb, P.n, p, tw, ts, inv);
+        else if (FAM >= kPow2x3 && R == 3) pass<3, VPT>(s, nb, P.n, p, tw, ts, inv);
+        else if (FAM == kAny) {
+            if (R == 5) pass<5, VPT>(s, nb, P.n, p, tw, ts, inv);
+            else if (R == 7) pass<7, VPT>(s, nb, P.n, p, tw, ts, inv);
+            else if (R == 11) pass<11, VPT>(s, nb, P.n, p, tw, ts, inv);
+            else pass<13, VPT>(s, nb, P.n, p, tw, ts, inv);
+        }
+        p *= R;
+    }
+}
+
+// ---------------------------------------------------------------- real packing
+// R2C output bin k (0 <= k <= n) of the real length-2n sequence whose packed transform
+// Z (length n, padded at s + off) sits in shared memory; W^k = tw[k] (table of 2n entries)
+template <typename V>
+__device__ __forceinline__ V r2c_bin(const V* s, int off, int n, int k, const V* __restrict__ tw)
+{
+    using T = decltype(s[0].x);
+    const V zk = s[pad<V>(off + (k == n ? 0 : k))];
+    const V zc = cconj(s[pad<V>(off + (k == 0 ? 0 : n - k))]);
+    const V sum = cadd(zk, zc), dif = csub(zk, zc);
+    const V w = __ldg(tw + k);
+    const V t = cmul(w, dif);            // W^k (Z_k - conj Z_{n-k})
+    return mk((T)0.5 * (sum.x + t.y), (T)0.5 * (sum.y - t.x));   // 1/2 (sum - i t)
+}
+
+// C2R packed input Z_k (0 <= k < n) from the half-spectrum bins X_k and X_{n-k} (with
+// the imaginary parts of X_0 and X_n already dropped); W^-k = conj(tw[k])
+template <typename V>
+__device__ __forceinline__ V c2r_pack(const V& xk, const V& xnk, int k, const V* __restrict__ tw)
+{
+    const V b = cconj(xnk);
+    const V sum = cadd(xk, b), dif = csub(xk, b);
+    const V t = cmul(cconj(__ldg(tw + k)), dif);   // W^-k (X_k - conj X_{n-k})
+    return mk(sum.x - t.y, sum.y + t.x);          // sum + i t
+}
+#endif  // __CUDACC__
+
+}  // namespace fft
+}  // namespace cmm

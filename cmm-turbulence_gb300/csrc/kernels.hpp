@@ -2,9 +2,9 @@
 // Every launcher is stream-ordered and returns the launch status.
 #pragma once
 #include <cuda_runtime.h>
-#include <cufft.h>
 
 #include "cmm_common.cuh"
+#include "fft.hpp"
 
 namespace cmm {
 
@@ -75,6 +75,17 @@ cudaError_t launch_sample_vort(const Grid& gm, const Grid& gout, const Grid& gf,
                                const double* Y, const double* Wf, int molly, double* out, long long ld,
                                cudaStream_t s);
 
+// the fused psi solve (evaluate_stream_hermite, cmm-simulation-host.cu:333-375): omega
+// through the map on gv, its kept modes, the four psi Hermite planes on gp, in three
+// launches on the library's FFT; runs when psi_solve_fits, which also gives the complex
+// values the work arrays w1, w2 need
+bool psi_solve_fits(const Grid& gv, const Grid& gp, double freq, const fft::Plan2D& pv, const fft::Plan2D& pp,
+                    long long* w1_values, long long* w2_values);
+void psi_solve_prepare();
+cudaError_t launch_psi_solve(const Grid& gm, const Grid& gv, const Grid& gf, const double* X, const double* Y,
+                             const double* Wf, int molly, const Grid& gp, double freq, const fft::Plan2D& pv,
+                             const fft::Plan2D& pp, double2* w1, double2* w2, double* psi_out, cudaStream_t s);
+
 // tracer and inertial particles (Particle_advect / Particle_advect_inertia,
 // src/numerical/cmm-particles.cu:119-551); psi[0] is t_{n+1}, psi[1] t_n, psi[2] t_{n-1}
 struct ParticleArgs {
@@ -102,16 +113,19 @@ cudaError_t launch_sample_points_dxdy(const Grid& gp, const double* psi, const d
                                       cudaStream_t s);
 
 // ---------------------------------------------------------------- spectral
-// cuFFT-based transforms plus fused spectral operators (src/numerical/cmm-fft.cu)
+// FP64 2D transforms of one grid (the reference's D2Z / Z2D plans, cmm-grid2d.cu:123-131)
+// on the library's own FFT (csrc/fft.hpp) plus fused spectral operators (src/numerical/cmm-fft.cu)
 struct FftPlans {
-    cufftHandle d2z = 0;        // real -> half spectrum
-    cufftHandle z2d4 = 0;       // batch of 4 half spectra -> 4 real planes
-    cufftHandle z2d1 = 0;       // single inverse
+    fft::Plan2D p;
     Grid g;
     bool ok = false;
 };
 bool make_plans(FftPlans& p, const Grid& g, cudaStream_t s);
 void destroy_plans(FftPlans& p);
+// real -> half spectrum (unnormalised); batch half spectra -> real planes (unnormalised;
+// the input is overwritten)
+cudaError_t fft_d2z(const FftPlans& p, const double* in, double2* out, cudaStream_t s);
+cudaError_t fft_z2d(const FftPlans& p, double2* in, double* out, int batch, cudaStream_t s);
 
 // normalised spectrum -> 4 spectra [F, dx F, dy F, dxdy F] (fourier_hermite prep)
 cudaError_t launch_spec_hermite(const double2* F, const Grid& g, double2* out4, cudaStream_t s);

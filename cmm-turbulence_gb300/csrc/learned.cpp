@@ -3,7 +3,6 @@
 // learned_kernels.cu.
 #include "learned.hpp"
 
-#include <cufft.h>
 
 #include <algorithm>
 #include <cmath>
@@ -125,8 +124,7 @@ Upsampler::~Upsampler()
     release(rbuf_);
     release(rspec_);
     release(tspec_);
-    if (fft_r2c_) cufftDestroy((cufftHandle)fft_r2c_);
-    if (fft_c2r_) cufftDestroy((cufftHandle)fft_c2r_);
+    fft::plan_destroy(fft_);
 }
 
 int Upsampler::init_weights(uint64_t seed)
@@ -298,9 +296,8 @@ int Upsampler::ensure_fft(int B, int h, int w)
 {
     const long long n = (long long)B * h * w;
     if (B != fft_B_ || h != fft_h_ || w != fft_w_) {
-        if (fft_r2c_) cufftDestroy((cufftHandle)fft_r2c_);
-        if (fft_c2r_) cufftDestroy((cufftHandle)fft_c2r_);
-        fft_r2c_ = fft_c2r_ = 0;
+        fft::plan_destroy(fft_);
+        fft_B_ = 0;
         release(rbuf_);
         release(rspec_);
         release(tspec_);
@@ -308,15 +305,10 @@ int Upsampler::ensure_fft(int B, int h, int w)
         LRN_CHECK(alloc(&rbuf_, 4 * n), "buffers");
         LRN_CHECK(alloc(&rspec_, nspec), "buffers");
         LRN_CHECK(alloc(&tspec_, nspec), "buffers");
-        int dims[2] = {2 * h, 2 * w};
-        cufftHandle a = 0, b = 0;
-        if (cufftPlanMany(&a, 2, dims, nullptr, 1, 4 * h * w, nullptr, 1, 2 * h * (w + 1), CUFFT_R2C, B) != CUFFT_SUCCESS ||
-            cufftPlanMany(&b, 2, dims, nullptr, 1, 2 * h * (w + 1), nullptr, 1, 4 * h * w, CUFFT_C2R, B) != CUFFT_SUCCESS) {
-            err = "upsampler: cuFFT plan creation failed";
+        if (fft::plan_create(fft_, 2 * w, 2 * h, false, nullptr)) {
+            err = "upsampler: FFT plan creation failed";
             return 1;
         }
-        fft_r2c_ = (int)a;
-        fft_c2r_ = (int)b;
         fft_B_ = B;
         fft_h_ = h;
         fft_w_ = w;
@@ -434,18 +426,11 @@ int Upsampler::loss(int B, int h, int w, double* acc, cudaStream_t s)
     }
     if (ensure_fft(B, h, w)) return 1;
     LRN_CHECK(launch_shuffle_resid(out32_, tgt_, B, h, w, rbuf_, s), "loss");
-    cufftSetStream((cufftHandle)fft_r2c_, s);
-    cufftSetStream((cufftHandle)fft_c2r_, s);
-    if (cufftExecR2C((cufftHandle)fft_r2c_, rbuf_, reinterpret_cast<cufftComplex*>(rspec_)) != CUFFT_SUCCESS ||
-        cufftExecR2C((cufftHandle)fft_r2c_, tgt_, reinterpret_cast<cufftComplex*>(tspec_)) != CUFFT_SUCCESS) {
-        err = "upsampler: cuFFT R2C failed";
-        return 1;
-    }
+    const long long rd = 4ll * h * w, sd = 2ll * h * (w + 1);
+    LRN_CHECK(fft::r2c(fft_, rbuf_, rspec_, B, s, rd, sd), "loss FFT");
+    LRN_CHECK(fft::r2c(fft_, tgt_, tspec_, B, s, rd, sd), "loss FFT");
     LRN_CHECK(launch_spec_loss(rspec_, tspec_, B, 2 * h, 2 * w, cut_, acc, s), "loss");
-    if (cufftExecC2R((cufftHandle)fft_c2r_, reinterpret_cast<cufftComplex*>(rspec_), rbuf_) != CUFFT_SUCCESS) {
-        err = "upsampler: cuFFT C2R failed";
-        return 1;
-    }
+    LRN_CHECK(fft::c2r(fft_, rspec_, rbuf_, B, s, sd, rd), "loss FFT");
     LRN_CHECK(launch_grad_pack(rbuf_, acc, B, h, w, dout_, s), "loss");
     launches += 3;
     return 0;

@@ -19,6 +19,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include "fft.hpp"
+
 #include <cstdint>
 #include <random>
 #include <string>
@@ -209,7 +211,8 @@ private:
     int cut_ = 0;
     float* rbuf_ = nullptr;              // B x 2h x 2w residual / gradient
     float2 *rspec_ = nullptr, *tspec_ = nullptr;
-    int fft_r2c_ = 0, fft_c2r_ = 0, fft_B_ = 0, fft_h_ = 0, fft_w_ = 0;   // cuFFT: B transforms of 2h x 2w
+    fft::Plan2D fft_;                    // transforms of 2h x 2w (loss)
+    int fft_B_ = 0, fft_h_ = 0, fft_w_ = 0;
     int* d_status_ = nullptr;
     const float** d_ptrs_ = nullptr;     // 3 x B device pointers for assemble
     int ptr_cap_ = 0;

@@ -5,6 +5,7 @@
 
 #include "init_conditions.cuh"
 #include "kernels.hpp"
+#include "psi_solve.cuh"
 
 namespace cmm {
 
@@ -420,13 +421,10 @@ cudaError_t launch_compose_sample(const Grid& gm, const Grid& gt, const double* 
 // ---------------------------------------------------------------------------
 // vorticity through the current map (k_apply_map_and_sample_from_hermite)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_sample_vort(Grid gm, Grid go, Grid gf, const double* __restrict__ X,
-                                                     const double* __restrict__ Y, const double* __restrict__ Wf,
-                                                     int molly, double* __restrict__ out, long long ld)
+__device__ __forceinline__ double sample_vort_point(const Grid& gm, const Grid& go, const Grid& gf,
+                                                   const double* __restrict__ X, const double* __restrict__ Y,
+                                                   const double* __restrict__ Wf, int molly, int iX, int iY)
 {
-    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= go.N) return;
-    int iX = (int)(i % go.NX), iY = (int)(i / go.NX);
     double x = gm.b0 + iX * go.hx, y = gm.b2 + iY * go.hy;
     double x2, y2, v;
     if (molly == 4) {
@@ -453,7 +451,17 @@ __global__ void __launch_bounds__(256) k_sample_vort(Grid gm, Grid go, Grid gf, 
         map_value(X, Y, gm, x, y, x2, y2);
         v = interp_value(Wf, gf, x2, y2);
     }
-    out[(long long)iY * ld + iX] = v;
+    return v;
+}
+
+__global__ void __launch_bounds__(256) k_sample_vort(Grid gm, Grid go, Grid gf, const double* __restrict__ X,
+                                                     const double* __restrict__ Y, const double* __restrict__ Wf,
+                                                     int molly, double* __restrict__ out, long long ld)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= go.N) return;
+    int iX = (int)(i % go.NX), iY = (int)(i / go.NX);
+    out[(long long)iY * ld + iX] = sample_vort_point(gm, go, gf, X, Y, Wf, molly, iX, iY);
 }
 
 cudaError_t launch_sample_vort(const Grid& gm, const Grid& go, const Grid& gf, const double* X, const double* Y,
@@ -463,6 +471,63 @@ cudaError_t launch_sample_vort(const Grid& gm, const Grid& go, const Grid& gf, c
     unsigned blocks = (unsigned)((go.N + threads - 1) / threads);
     k_sample_vort<<<blocks, threads, 0, s>>>(gm, go, gf, X, Y, Wf, molly, out, ld);
     return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// the fused psi solve of the plain form (psi_solve.cuh): omega through the map on
+// the vorticity grid (sample_vort_point), the kept modes, the four psi planes
+// ---------------------------------------------------------------------------
+struct SampleVortSrc {
+    Grid gm, go, gf;
+    const double* X;
+    const double* Y;
+    const double* Wf;
+    int molly;
+    __device__ __forceinline__ double value(int iX, int iY, bool live) const
+    {
+        return live ? sample_vort_point(gm, go, gf, X, Y, Wf, molly, iX, iY) : 0.0;
+    }
+};
+
+struct PlanesEpi {
+    int nx;
+    long long n;
+    double* out;
+    __device__ __forceinline__ void store(int iX, int iY, double f, double fx, double fy, double fxy) const
+    {
+        const long long i = (long long)iY * nx + iX;
+        out[i] = f;
+        out[n + i] = fx;
+        out[2 * n + i] = fy;
+        out[3 * n + i] = fxy;
+    }
+};
+
+bool psi_solve_fits(const Grid& gv, const Grid& gp, double freq, const fft::Plan2D& pv, const fft::Plan2D& pp,
+                    long long* w1_values, long long* w2_values)
+{
+    if (gv.NY > 65535) return false;
+    const psi::Layout L = psi::make_layout<double>(gv, gp, freq, pv, pp);
+    if (!L.ok) return false;
+    if (w1_values) *w1_values = L.w1_values;
+    if (w2_values) *w2_values = L.w2_values;
+    return true;
+}
+
+void psi_solve_prepare()
+{
+    psi::prepare<double, SampleVortSrc, PlanesEpi>();
+}
+
+cudaError_t launch_psi_solve(const Grid& gm, const Grid& gv, const Grid& gf, const double* X, const double* Y,
+                             const double* Wf, int molly, const Grid& gp, double freq, const fft::Plan2D& pv,
+                             const fft::Plan2D& pp, double2* w1, double2* w2, double* psi_out, cudaStream_t s)
+{
+    const psi::Layout L = psi::make_layout<double>(gv, gp, freq, pv, pp);
+    if (!L.ok) return cudaErrorInvalidValue;
+    SampleVortSrc src{gm, gv, gf, X, Y, Wf, molly};
+    PlanesEpi epi{gp.NX, gp.N, psi_out};
+    return psi::launch<double>(L, gv, gp, freq, pv, pp, w1, w2, src, epi, s);
 }
 
 }  // namespace cmm

@@ -45,6 +45,17 @@ cudaError_t launch_psi_nodes3(const float* planes, long long n, const float4* l1
                               const double* c2, const double* c3, float4* out0, float4* o1, float4* o2, float4* o3,
                               cudaStream_t s);
 cudaError_t launch_advect_m(const AdvectMArgs& a, cudaStream_t s);
+// the fused psi solve (omega through the map on gv, the kept modes, psi nodes on gp and, with
+// c1 != nullptr, the three Lagrange combinations of launch_psi_nodes3): three launches on the
+// library's FFT; runs when psi_solve_m_fits (vort grid = 4 x map grid, shapes the fused
+// kernels hold), which also gives the complex values the work arrays w1, w2 need
+bool psi_solve_m_fits(const Grid& gm, const Grid& gv, const Grid& gp, double freq, const fft::Plan2D& pv,
+                      const fft::Plan2D& pp, long long* w1_values, long long* w2_values);
+void psi_solve_m_prepare();
+cudaError_t launch_psi_solve_m(const Grid& gm, const Grid& gv, const Grid& gf, const float4* map, const float4* W,
+                               const Grid& gp, double freq, const fft::Plan2D& pv, const fft::Plan2D& pp, float2* w1,
+                               float2* w2, float4* out0, const float4* l1, const float4* l2, const double* c1,
+                               const double* c2, const double* c3, float4* o1, float4* o2, float4* o3, cudaStream_t s);
 // max |det grad X - 1| on the half-shifted check grid with r = Ncheck / Nmap points per cell and axis
 // (r * Nmap^2 < 2^31)
 cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_result, cudaStream_t s);

@@ -6,7 +6,6 @@
 #include "mixed.hpp"
 
 #include <cuda_runtime.h>
-#include <cufft.h>
 #include <curand.h>
 
 #include <algorithm>
@@ -109,7 +108,7 @@ int EulerSim::check(cudaError_t e, const char* what)
 
 #define CMM_CUDA(call) do { int rc_ = check((call), #call); if (rc_) return rc_; } while (0)
 #define CMM_LAUNCH(k, call) do { kernel_launches += (k); int rc_ = check((call), #call); if (rc_) return rc_; } while (0)
-#define CMM_FFT(call) do { fft_calls++; if ((call) != CUFFT_SUCCESS) { err = std::string("cuFFT: ") + #call; return kErrCuda; } } while (0)
+#define CMM_FFT(call) do { fft_calls++; cudaError_t e_ = (call); if (e_ != cudaSuccess) { err = std::string("FFT: ") + #call + ": " + cudaGetErrorString(e_); return kErrCuda; } } while (0)
 
 double EulerSim::wall() const
 {
@@ -274,7 +273,7 @@ int EulerSim::alloc()
     }
     if (!make_plans(pf_, gf, stream) || !make_plans(pv_, gv, stream) || !make_plans(pp_, gp, stream) ||
         !make_plans(pc_, gc, stream) || (s.initial_discrete && !make_plans(pd_, gd, stream))) {
-        err = "cuFFT plan creation failed";
+        err = "FFT plan creation failed (grid sizes need NX even, sides <= 8192, prime factors <= 13)";
         return kErrCuda;
     }
     if (vlasov_) {
@@ -287,7 +286,7 @@ int EulerSim::alloc()
         for (int k = 0; k < 3; ++k) CMM_CUDA(cudaMalloc((void**)&vl_c_[k], sizeof(double2) * cn));
         if (mixed_)
             for (int k = 0; k < 4; ++k) CMM_CUDA(cudaMalloc((void**)&vtab_[k], sizeof(double2) * std::max(gp.NX, gp.NY)));
-        if (!make_vlasov_plans(vp_, gv, gp, stream)) { err = "cuFFT 1D plan creation failed"; return kErrCuda; }
+        if (!make_vlasov_plans(vp_, gv, gp, stream)) { err = "FFT plan creation failed (1D, Vlasov)"; return kErrParam; }
     }
     if (mixed_) {
         auto falloc = [&](void** p, size_t bytes) { return check(cudaMalloc(p, std::max(bytes, (size_t)16)), "cudaMalloc"); };
@@ -331,34 +330,27 @@ int EulerSim::alloc()
                 return rc;
         }
         if (stack_cap_ > 0 && (rc = falloc((void**)&stackm_, mapb * stack_cap_))) return rc;
-        int nv[2] = {gv.NY, gv.NX}, np[2] = {gp.NY, gp.NX}, nf[2] = {gf.NY, gf.NX};
-        if (cufftPlanMany(&r2c_v_, 2, nv, nullptr, 1, 0, nullptr, 1, 0, CUFFT_R2C, 1) != CUFFT_SUCCESS ||
-            cufftPlanMany(&c2r4_p_, 2, np, nullptr, 1, 0, nullptr, 1, 0, CUFFT_C2R, 4) != CUFFT_SUCCESS ||
-            cufftPlanMany(&r2c_f_, 2, nf, nullptr, 1, 0, nullptr, 1, 0, CUFFT_R2C, 1) != CUFFT_SUCCESS ||
-            cufftPlanMany(&c2r4_f_, 2, nf, nullptr, 1, 0, nullptr, 1, 0, CUFFT_C2R, 4) != CUFFT_SUCCESS) {
-            err = "cuFFT FP32 plan creation failed";
-            return kErrCuda;
+        if (fft::plan_create(fv_, gv.NX, gv.NY, false, stream) || fft::plan_create(fp_, gp.NX, gp.NY, false, stream) ||
+            fft::plan_create(ff_, gf.NX, gf.NY, false, stream)) {
+            err = "FFT plan creation failed (grid sizes need NX even, sides <= 8192, prime factors <= 13)";
+            return kErrParam;
         }
-        cufftSetStream(r2c_v_, stream);
-        cufftSetStream(c2r4_p_, stream);
-        cufftSetStream(r2c_f_, stream);
-        cufftSetStream(c2r4_f_, stream);
-        if (!vlasov_) {
-            // the psi solve keeps the columns kx <= freq_cut_psi of omega's spectrum only: a
-            // row R2C of every row, then a column C2C of just those columns (same modes,
-            // about half the work of the full 2D transform)
-            vcols_ = std::min(gv.NX_fft, (int)std::floor(s.freq_cut_psi) + 1);
-            int nrow[1] = {gv.NX}, nrowf[1] = {gv.NX_fft}, ncol[1] = {gv.NY};
-            if (cufftPlanMany(&r2c_vrows_, 1, nrow, nrow, 1, gv.NX, nrowf, 1, gv.NX_fft, CUFFT_R2C, gv.NY) != CUFFT_SUCCESS ||
-                cufftPlanMany(&c2c_vcols_, 1, ncol, ncol, gv.NX_fft, 1, ncol, gv.NX_fft, 1, CUFFT_C2C, vcols_) !=
-                    CUFFT_SUCCESS) {
-                err = "cuFFT FP32 plan creation failed";
-                return kErrCuda;
-            }
-            cufftSetStream(r2c_vrows_, stream);
-            cufftSetStream(c2c_vcols_, stream);
-            // (the inverse transform of the four psi spectra stays one batched 2D C2R: pruned
-            // the same way -- strided column C2C per plane, then row C2R -- it measured slower)
+        // the psi solve keeps the columns kx <= freq_cut_psi of omega's spectrum only: a
+        // row R2C of every row writing those columns, then a column transform of just them
+        if (!vlasov_) vcols_ = std::min(gv.NX_fft, (int)std::floor(s.freq_cut_psi) + 1);
+    }
+    if (!vlasov_) {
+        // the psi solve as three fused kernels where the sizes allow it (else sample, transform,
+        // spectral step, inverse transforms and node pass one after another)
+        long long n1 = 0, n2 = 0;
+        psi_fused_ = mixed_ ? psi_solve_m_fits(gc, gv, gp, s.freq_cut_psi, fv_, fp_, &n1, &n2)
+                            : psi_solve_fits(gv, gp, s.freq_cut_psi, pv_.p, pp_.p, &n1, &n2);
+        if (psi_fused_) {
+            const size_t vb = mixed_ ? sizeof(float2) : sizeof(double2);
+            CMM_CUDA(cudaMalloc(&psw1_, vb * (size_t)n1));
+            CMM_CUDA(cudaMalloc(&psw2_, vb * (size_t)n2));
+            if (mixed_) psi_solve_m_prepare();
+            else psi_solve_prepare();
         }
     }
     // random table for gaussian_blobs (cmm-euler2d.cu:348-354)
@@ -413,14 +405,12 @@ void EulerSim::release()
     for (int l = 0; l < kMaxLagrange; ++l) { f(psim_[l]); psim_[l] = nullptr; }
     mapm_ = mapm_new_ = psiA_ = psiB_ = wfm_ = stackm_ = nullptr;
     realf_ = nullptr; specf_ = nullptr; spec4f_ = nullptr;
-    if (r2c_v_) cufftDestroy(r2c_v_);
-    if (c2r4_p_) cufftDestroy(c2r4_p_);
-    if (r2c_f_) cufftDestroy(r2c_f_);
-    if (c2r4_f_) cufftDestroy(c2r4_f_);
-    if (r2c_vrows_) cufftDestroy(r2c_vrows_);
-    if (c2c_vcols_) cufftDestroy(c2c_vcols_);
-    r2c_v_ = c2r4_p_ = r2c_f_ = c2r4_f_ = r2c_vrows_ = c2c_vcols_ = 0;
-    r2c_v_ = c2r4_p_ = 0;
+    fft::plan_destroy(fv_);
+    fft::plan_destroy(fp_);
+    fft::plan_destroy(ff_);
+    f(psw1_); f(psw2_);
+    psw1_ = psw2_ = nullptr;
+    psi_fused_ = false;
     if (h_scal_) cudaFreeHost(h_scal_);
     h_scal_ = nullptr;
     if (einc_ev_) cudaEventDestroy(einc_ev_);
@@ -450,9 +440,9 @@ int EulerSim::translate_ic()
         // fixed-point positions through the FP32 displacement stack, then the
         // spectral Hermite planes in FP32, the precision of the nodes they are stored in
         CMM_LAUNCH(1, launch_compose_m(gc, gf, mapm_, stackm_, n_maps_, src, wdiscm_, nullptr, stream, realf_));
-        CMM_FFT(cufftExecR2C(r2c_f_, realf_, reinterpret_cast<cufftComplex*>(specf_)));
+        CMM_FFT(fft::r2c(ff_, realf_, specf_, 1, stream));
         CMM_LAUNCH(1, launch_spec_hermite_f(specf_, gf, spec4f_, stream));
-        CMM_FFT(cufftExecC2R(c2r4_f_, reinterpret_cast<cufftComplex*>(spec4f_), realf_));
+        CMM_FFT(fft::c2r(ff_, spec4f_, realf_, 4, stream));
         CMM_LAUNCH(1, launch_planes_to_float4(realf_, nullptr, gf.N, wfm_, stream));
         return kOk;
     }
@@ -460,9 +450,9 @@ int EulerSim::translate_ic()
     // whole velocity range, where an FP32 transform's noise floor (~1e-7 of max f) would show
     if (mixed_) CMM_LAUNCH(1, launch_compose_m(gc, gf, mapm_, stackm_, n_maps_, src, wdiscm_, real_buf_, stream));
     else CMM_LAUNCH(1, launch_compose_sample(gc, gf, ChiX, ChiY, stack, n_maps_, src, real_buf_, stream));
-    CMM_FFT(cufftExecD2Z(pf_.d2z, real_buf_, reinterpret_cast<cufftDoubleComplex*>(spec_)));
+    CMM_FFT(fft_d2z(pf_, real_buf_, spec_, stream));
     CMM_LAUNCH(1, launch_spec_hermite(spec_, gf, spec4_, stream));
-    CMM_FFT(cufftExecZ2D(pf_.z2d4, reinterpret_cast<cufftDoubleComplex*>(spec4_), wfine));
+    CMM_FFT(fft_z2d(pf_, spec4_, wfine, 4, stream));
     if (mixed_) CMM_LAUNCH(1, launch_planes_to_float4(nullptr, wfine, gf.N, wfm_, stream));
     return kOk;
 }
@@ -474,6 +464,18 @@ int EulerSim::evaluate_stream()
         if (ups_ && in_step_) {
             int rc = learned_stream();
             if (rc) return rc;
+        } else if (psi_fused_) {
+            // sample, transforms, spectral step and node pass in three kernels; with three
+            // Lagrange levels the node pass also writes the combinations below
+            const bool combos = psi_lcl_ >= 0 && L == 3;
+            fused_ = false;
+            if (combos) predict_combinations();
+            CMM_LAUNCH(3, launch_psi_solve_m(gc, gv, gf, mapm_, wfm_, gp, s.freq_cut_psi, fv_, fp_,
+                                             static_cast<float2*>(psw1_), static_cast<float2*>(psw2_), psim_[0],
+                                             psim_[1], psim_[2], combos ? fusedLp_ : nullptr, fusedL1_, fusedL12_,
+                                             psiP_, psiA_, psiB_, stream));
+            fused_ = combos;
+            return kOk;
         } else {
             CMM_LAUNCH(1, launch_sample_m(gc, gv, gf, mapm_, wfm_, realf_, nullptr, stream));
             if (int rc = vort_spectrum()) return rc;
@@ -485,16 +487,7 @@ int EulerSim::evaluate_stream()
             // one pass writes the new level and the Lagrange combinations this step's
             // tracers and the next step's advection will ask for (next dt predicted by
             // compute_next_timestep; the users check the coefficients bitwise)
-            const int lcl = psi_lcl_;
-            const double* t = t_vec_.data();
-            const double tn = t[lcl + 1];
-            double dtn = compute_next_timestep(tn);
-            if (tn + dtn > s.final_time) dtn = s.final_time - tn;
-            for (int i = 0; i < L; ++i) {
-                fusedLp_[i] = lagrange_coefficient(t, t[lcl] + dt_vec_[lcl + 1] / 2.0, lcl + 1, i, L);
-                fusedL1_[i] = lagrange_coefficient(t, tn + dtn, lcl + 1, i, L);
-                fusedL12_[i] = lagrange_coefficient(t, tn + dtn / 2.0, lcl + 1, i, L);
-            }
+            predict_combinations();
             CMM_LAUNCH(1, launch_psi_nodes3(realf_, gp.N, psim_[1], psim_[2], fusedLp_, fusedL1_, fusedL12_, psim_[0],
                                             psiP_, psiA_, psiB_, stream));
             fused_ = true;
@@ -503,30 +496,51 @@ int EulerSim::evaluate_stream()
         }
         return kOk;
     }
+    if (psi_fused_) {
+        CMM_LAUNCH(3, launch_psi_solve(gc, gv, gf, ChiX, ChiY, wfine, s.molly_stencil, gp, s.freq_cut_psi, pv_.p, pp_.p,
+                                       static_cast<double2*>(psw1_), static_cast<double2*>(psw2_), psi[0], stream));
+        return kOk;
+    }
     CMM_LAUNCH(1, launch_sample_vort(gc, gv, gf, ChiX, ChiY, wfine, s.molly_stencil, real_buf_, gv.NX, stream));
-    CMM_FFT(cufftExecD2Z(pv_.d2z, real_buf_, reinterpret_cast<cufftDoubleComplex*>(spec_)));
+    CMM_FFT(fft_d2z(pv_, real_buf_, spec_, stream));
     CMM_LAUNCH(1, launch_spec_psi(spec_, gv, gp, s.freq_cut_psi, spec4_, stream));
-    CMM_FFT(cufftExecZ2D(pp_.z2d4, reinterpret_cast<cufftDoubleComplex*>(spec4_), psi[0]));
+    CMM_FFT(fft_z2d(pp_, spec4_, psi[0], 4, stream));
     return kOk;
+}
+
+void EulerSim::predict_combinations()
+{
+    // the Lagrange combinations this step's tracers (t_{n+1/2}) and the next step's advection
+    // (t_{n+1}, t_{n+1/2} for the dt compute_next_timestep predicts) ask for; their users
+    // check the coefficients bitwise and recombine on a mismatch
+    const int lcl = psi_lcl_;
+    const double* t = t_vec_.data();
+    const double tn = t[lcl + 1];
+    double dtn = compute_next_timestep(tn);
+    if (tn + dtn > s.final_time) dtn = s.final_time - tn;
+    for (int i = 0; i < L; ++i) {
+        fusedLp_[i] = lagrange_coefficient(t, t[lcl] + dt_vec_[lcl + 1] / 2.0, lcl + 1, i, L);
+        fusedL1_[i] = lagrange_coefficient(t, tn + dtn, lcl + 1, i, L);
+        fusedL12_[i] = lagrange_coefficient(t, tn + dtn / 2.0, lcl + 1, i, L);
+    }
 }
 
 int EulerSim::vort_spectrum()
 {
     // omega on the vorticity grid (realf_) -> the modes the psi solve keeps (specf_)
-    if (!r2c_vrows_) {
-        CMM_FFT(cufftExecR2C(r2c_v_, realf_, reinterpret_cast<cufftComplex*>(specf_)));
+    if (vcols_ <= 0) {
+        CMM_FFT(fft::r2c(fv_, realf_, specf_, 1, stream));
         return kOk;
     }
-    CMM_FFT(cufftExecR2C(r2c_vrows_, realf_, reinterpret_cast<cufftComplex*>(specf_)));
-    CMM_FFT(cufftExecC2C(c2c_vcols_, reinterpret_cast<cufftComplex*>(specf_), reinterpret_cast<cufftComplex*>(specf_),
-                         CUFFT_FORWARD));
+    CMM_FFT(fft::rows_r2c(fv_, realf_, gv.NX, gv.N, specf_, gv.NX_fft, gv.Nfft, gv.NY, 1, vcols_, stream));
+    CMM_FFT(fft::cols_c2c(fv_, specf_, gv.NX_fft, gv.Nfft, vcols_, 1, false, stream));
     return kOk;
 }
 
 int EulerSim::psi_planes(float2* spec4, float* out)
 {
     // the four Hermite spectra (gp layout) -> the planes on the psi grid
-    CMM_FFT(cufftExecC2R(c2r4_p_, reinterpret_cast<cufftComplex*>(spec4), out));
+    CMM_FFT(fft::c2r(fp_, spec4, out, 4, stream));
     return kOk;
 }
 
@@ -587,10 +601,10 @@ int EulerSim::vlasov_setup_h()
     // compute_periodification_function (cmm-simulation-host.cu:534-571): the
     // normalised bump, integrated twice in v by 1D spectra; h and h' on the psi grid
     CMM_LAUNCH(1, launch_vlasov_bump(gp, real_buf_, stream));
-    CMM_FFT(cufftExecD2Z(vp_.d2z_p, real_buf_, vl_c_[0]));
+    CMM_FFT(fft_d2z_1d(vp_.p, real_buf_, vl_c_[0], stream));
     CMM_LAUNCH(1, launch_vlasov_h_spec(vl_c_[0], gp, vl_c_[1], vl_c_[2], stream));
-    CMM_FFT(cufftExecZ2D(vp_.z2d_p, vl_c_[1], vl_h_));
-    CMM_FFT(cufftExecZ2D(vp_.z2d_p, vl_c_[2], vl_h_ + gp.NY));
+    CMM_FFT(fft_z2d_1d(vp_.p, vl_c_[1], vl_h_, stream));
+    CMM_FFT(fft_z2d_1d(vp_.p, vl_c_[2], vl_h_ + gp.NY, stream));
     if (mixed_) {
         const double* lv[1] = {vl_h_};
         double one[1] = {1.0};
@@ -607,11 +621,11 @@ int EulerSim::evaluate_potential()
     if (mixed_) CMM_LAUNCH(1, launch_sample_m(gc, gv, gf, mapm_, wfm_, realf_, nullptr, stream));
     else CMM_LAUNCH(1, launch_sample_vort(gc, gv, gf, ChiX, ChiY, wfine, s.molly_stencil, real_buf_, gv.NX, stream));
     CMM_LAUNCH(2, launch_vlasov_rho(mixed_ ? nullptr : real_buf_, mixed_ ? realf_ : nullptr, gv, vl_part_, vl_rho_, stream));
-    CMM_FFT(cufftExecD2Z(vp_.d2z_v, vl_rho_, vl_c_[0]));
+    CMM_FFT(fft_d2z_1d(vp_.v, vl_rho_, vl_c_[0], stream));
     CMM_LAUNCH(1, launch_vlasov_phi_spec(vl_c_[0], gv, gp, vl_c_[1], vl_c_[2], stream));
     double* phi = phi_lv_[0];
-    CMM_FFT(cufftExecZ2D(vp_.z2d_p, vl_c_[1], phi));
-    CMM_FFT(cufftExecZ2D(vp_.z2d_p, vl_c_[2], phi + gp.NX));
+    CMM_FFT(fft_z2d_1d(vp_.p, vl_c_[1], phi, stream));
+    CMM_FFT(fft_z2d_1d(vp_.p, vl_c_[2], phi + gp.NX, stream));
     if (!mixed_) CMM_LAUNCH(1, launch_vlasov_assemble(phi, phi + gp.NX, vl_h_, vl_h_ + gp.NY, gp, psi[0], stream));
     return kOk;
 }
@@ -623,7 +637,7 @@ int EulerSim::vlasov_mesure(double* out)
     CMM_LAUNCH(2, launch_vlasov_moments(vort, gc, red_, d_scal_, stream));
     CMM_LAUNCH(2, launch_sumsq(phi_lv_[0] + gp.NX, gp.NX, red_, d_scal_ + 3, stream));
     CMM_CUDA(cudaMemcpyAsync(real_buf_, phi_lv_[0] + gp.NX, sizeof(double) * gp.NX, cudaMemcpyDeviceToDevice, stream));
-    CMM_FFT(cufftExecD2Z(vp_.d2z_p, real_buf_, vl_c_[0]));
+    CMM_FFT(fft_d2z_1d(vp_.p, real_buf_, vl_c_[0], stream));
     CMM_LAUNCH(1, launch_vlasov_modes(vl_c_[0], gp.NX, gp.NX_fft, d_scal_ + 4, stream));
     CMM_CUDA(cudaMemcpyAsync(h_scal_, d_scal_, sizeof(double) * 8, cudaMemcpyDeviceToHost, stream));
     CMM_CUDA(cudaStreamSynchronize(stream));
@@ -1220,9 +1234,9 @@ int EulerSim::init()
             if (f.gcount() != (std::streamsize)(sizeof(double) * gd.N)) { err = "discrete initial condition too short"; return kErrIO; }
         }
         CMM_CUDA(cudaMemcpyAsync(real_buf_, host_discrete_.data(), sizeof(double) * gd.N, cudaMemcpyHostToDevice, stream));
-        CMM_FFT(cufftExecD2Z(pd_.d2z, real_buf_, reinterpret_cast<cufftDoubleComplex*>(spec_)));
+        CMM_FFT(fft_d2z(pd_, real_buf_, spec_, stream));
         CMM_LAUNCH(1, launch_spec_hermite(spec_, gd, spec4_, stream));
-        CMM_FFT(cufftExecZ2D(pd_.z2d4, reinterpret_cast<cufftDoubleComplex*>(spec4_), wdisc));
+        CMM_FFT(fft_z2d(pd_, spec4_, wdisc, 4, stream));
         if (mixed_) CMM_LAUNCH(1, launch_planes_to_float4(nullptr, wdisc, gd.N, wdiscm_, stream));
         CMM_CUDA(cudaStreamSynchronize(stream));   // host_discrete_ may be released by the caller
     }
@@ -1719,7 +1733,7 @@ int EulerSim::sample_outputs(double t_now, double dt_now)
         if (n != smp_plan_n_) {
             destroy_plans(ps_);
             smp_plan_n_ = 0;
-            if (!make_plans(ps_, gs, stream)) { err = "cuFFT plan creation failed (sample grid)"; return kErrCuda; }
+            if (!make_plans(ps_, gs, stream)) { err = "FFT plan creation failed (sample grid)"; return kErrParam; }
             smp_plan_n_ = n;
         }
         double *X = smp_[0], *Y = smp_[1], *S = smp_[2], *W = smp_[3], *P = smp_[4], *T = smp_[5];
@@ -1745,10 +1759,7 @@ int EulerSim::sample_outputs(double t_now, double dt_now)
         auto spec = [&](int op, double* dst) {
             int rc2 = check(launch_spec_op(F0, gs, op, F1, stream), "spec_op");
             kernel_launches++;
-            if (!rc2 && cufftExecZ2D(ps_.z2d1, reinterpret_cast<cufftDoubleComplex*>(F1), dst) != CUFFT_SUCCESS) {
-                err = "cuFFT Z2D (sample grid)";
-                rc2 = kErrCuda;
-            }
+            if (!rc2) rc2 = check(fft_z2d(ps_, F1, dst, 1, stream), "FFT Z2D (sample grid)");
             fft_calls++;
             return rc2;
         };
@@ -1790,7 +1801,7 @@ int EulerSim::sample_outputs(double t_now, double dt_now)
         double mes[4], a, b2;
         if ((rc = sumsq(W, &a))) return rc;
         mes[1] = 0.5 * gs.hx * gs.hy * a;
-        CMM_FFT(cufftExecD2Z(ps_.d2z, W, reinterpret_cast<cufftDoubleComplex*>(F0)));
+        CMM_FFT(fft_d2z(ps_, W, F0, stream));
         if ((rc = spec(1, T)) || (rc = sumsq(T, &a))) return rc;
         if (has(var, "Grad_W") || all) if ((rc = out("GradX_W", T))) return rc;
         if ((rc = spec(2, T)) || (rc = sumsq(T, &b2))) return rc;
@@ -1806,7 +1817,7 @@ int EulerSim::sample_outputs(double t_now, double dt_now)
         }
         if ((rc = spec(3, P))) return rc;
         if (has(var, "Stream") || has(var, "Psi") || all) if ((rc = out("Stream_function_Psi", P))) return rc;
-        CMM_FFT(cufftExecD2Z(ps_.d2z, P, reinterpret_cast<cufftDoubleComplex*>(F0)));
+        CMM_FFT(fft_d2z(ps_, P, F0, stream));
         if ((rc = spec(1, T)) || (rc = sumsq(T, &a))) return rc;
         if (has(var, "Velocity") || has(var, "U") || all) if ((rc = out("Velocity_UX", T))) return rc;
         if ((rc = spec(2, T)) || (rc = sumsq(T, &b2))) return rc;
@@ -1846,7 +1857,7 @@ int EulerSim::vlasov_sample_outputs(double t_now, double dt_now)
         if (n != vsmp_plan_n_) {
             destroy_vlasov_plans(vps_);
             vsmp_plan_n_ = 0;
-            if (!make_vlasov_plans(vps_, gs, gs, stream)) { err = "cuFFT 1D plan creation failed (sample grid)"; return kErrCuda; }
+            if (!make_vlasov_plans(vps_, gs, gs, stream)) { err = "FFT plan creation failed (1D, sample grid)"; return kErrParam; }
             vsmp_plan_n_ = n;
         }
         double *X = smp_[0], *Y = smp_[1], *E = smp_[2], *F = smp_[3], *P = smp_[4], *T = smp_[5];
@@ -1882,13 +1893,13 @@ int EulerSim::vlasov_sample_outputs(double t_now, double dt_now)
         CMM_LAUNCH(2, launch_vlasov_moments(F, gs, red_, d_scal_, stream));
         // e = d phi / dx from f on the sample grid: rho (partials in T) -> 1D spectra -> E
         CMM_LAUNCH(2, launch_vlasov_rho(F, nullptr, gs, T, P, stream));
-        CMM_FFT(cufftExecD2Z(vps_.d2z_v, P, reinterpret_cast<cufftDoubleComplex*>(F0)));
+        CMM_FFT(fft_d2z_1d(vps_.v, P, F0, stream));
         CMM_LAUNCH(1, launch_vlasov_phi_spec(F0, gs, gs, F1, reinterpret_cast<double2*>(T), stream));
-        CMM_FFT(cufftExecZ2D(vps_.z2d_p, reinterpret_cast<cufftDoubleComplex*>(T), E));
+        CMM_FFT(fft_z2d_1d(vps_.p, reinterpret_cast<const double2*>(T), E, stream));
         CMM_LAUNCH(2, launch_sumsq(E, n, red_, d_scal_ + 3, stream));
         // mode amplitudes of the run's field phi' (psi_x row 0)
         CMM_CUDA(cudaMemcpyAsync(real_buf_, phi_lv_[0] + gp.NX, sizeof(double) * gp.NX, cudaMemcpyDeviceToDevice, stream));
-        CMM_FFT(cufftExecD2Z(vp_.d2z_p, real_buf_, vl_c_[0]));
+        CMM_FFT(fft_d2z_1d(vp_.p, real_buf_, vl_c_[0], stream));
         CMM_LAUNCH(1, launch_vlasov_modes(vl_c_[0], gp.NX, gp.NX_fft, d_scal_ + 4, stream));
         if (has(var, "Stream") || has(var, "Psi") || all) {
             const long long tail = std::max<long long>(gs.N / 8, (long long)n + 2);
@@ -2153,11 +2164,11 @@ int EulerSim::diagnostics(double* energy, double* enstrophy, double* palinstroph
     if (mixed_) CMM_LAUNCH(2, launch_energy_m(psim_[0], gp.N, red_, d_scal_ + 1, stream));
     else CMM_LAUNCH(2, launch_sumsq(psi[0] + gp.N, 2 * gp.N, red_, d_scal_ + 1, stream));
     CMM_LAUNCH(2, launch_sumsq(vort, gc.N, red_, d_scal_ + 2, stream));
-    CMM_FFT(cufftExecD2Z(pc_.d2z, vort, reinterpret_cast<cufftDoubleComplex*>(spec_)));
+    CMM_FFT(fft_d2z(pc_, vort, spec_, stream));
     CMM_LAUNCH(1, launch_spec_grad(spec_, gc, spec4_, stream));
-    CMM_FFT(cufftExecZ2D(pc_.z2d1, reinterpret_cast<cufftDoubleComplex*>(spec4_), real_buf_));
+    CMM_FFT(fft_z2d(pc_, spec4_, real_buf_, 1, stream));
     CMM_LAUNCH(2, launch_sumsq(real_buf_, gc.N, red_, d_scal_ + 3, stream));
-    CMM_FFT(cufftExecZ2D(pc_.z2d1, reinterpret_cast<cufftDoubleComplex*>(spec4_ + gc.Nfft), real_buf_));
+    CMM_FFT(fft_z2d(pc_, spec4_ + gc.Nfft, real_buf_, 1, stream));
     CMM_LAUNCH(2, launch_sumsq(real_buf_, gc.N, red_, d_scal_ + 4, stream));
     CMM_LAUNCH(2, launch_stats(vort, gc.N, 1, red_, d_scal_ + 8, stream));
     CMM_CUDA(cudaMemcpyAsync(h_scal_, d_scal_, sizeof(double) * 12, cudaMemcpyDeviceToHost, stream));

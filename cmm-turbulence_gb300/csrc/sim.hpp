@@ -119,7 +119,7 @@ public:
     double prof_ms[kNumPhases] = {0};
     long long prof_count[kNumPhases] = {0};
     long long kernel_launches = 0;    // launches of this library's kernels
-    long long fft_calls = 0;          // cuFFT executions
+    long long fft_calls = 0;          // 2D / 1D transform calls (csrc/fft.hpp)
 
 private:
     int alloc();
@@ -127,6 +127,7 @@ private:
     int translate_ic();
     int evaluate_stream();
     int vort_spectrum();
+    void predict_combinations();
     int psi_planes(float2* spec4, float* out);
     int coarse_vort();
     int ensure_vort();           // sample the coarse vorticity if a step left it stale
@@ -205,7 +206,7 @@ private:
     double learned_last_err_ = 0, learned_max_err_ = 0;
     float *lc_omega_ = nullptr, *lc_planes_ = nullptr, *l_delta_ = nullptr, *l_planes_ = nullptr;
     float2 *lc_spec_ = nullptr, *lc_spec4_ = nullptr, *l_dspec_ = nullptr;
-    int lc_r2c_ = 0, lc_c2r4_ = 0, l_r2c_ = 0, l_c2r_ = 0;    // cuFFT handles
+    fft::Plan2D fc_;           // FP32 transforms of the map grid (learned psi)
     double* d_stats_ = nullptr;
     bool in_step_ = false;
 
@@ -268,9 +269,11 @@ private:
     float* realf_ = nullptr;         // FP32 real scratch (4 planes of the largest grid)
     float2* specf_ = nullptr;        // FP32 complex scratch
     float2* spec4f_ = nullptr;       // 4 FP32 spectra
-    cufftHandle r2c_v_ = 0, c2r4_p_ = 0, r2c_f_ = 0, c2r4_f_ = 0;
-    cufftHandle r2c_vrows_ = 0, c2c_vcols_ = 0;   // pruned forward transform of omega (mixed Euler)
-    int vcols_ = 0;
+    fft::Plan2D fv_, fp_, ff_;   // FP32 transforms of the vort, psi and fine grids (mixed form)
+    int vcols_ = 0;              // columns kx <= freq_cut_psi the psi solve keeps
+    bool psi_fused_ = false;     // the psi solve runs as the three fused kernels (psi_solve.cuh)
+    void* psw1_ = nullptr;       // their work arrays (kept columns of omega's and psi's spectra)
+    void* psw2_ = nullptr;
     bool prof_ = false;
     cudaEvent_t ev_[kNumPhases][2] = {};
     bool ev_live_[kNumPhases] = {};

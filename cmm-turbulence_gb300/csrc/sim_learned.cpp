@@ -11,7 +11,6 @@
 // the vorticity the map-grid samples miss (omega on the psi grid minus the spectral
 // interpolation of the samples); the learned psi solves the cheap vorticity plus that
 // prediction with the method's cut-off, Poisson step and Hermite derivatives.
-#include <cufft.h>
 
 #include <algorithm>
 #include <cmath>
@@ -24,7 +23,7 @@ namespace cmm {
 
 #define CMM_CUDA(call) do { int rc_ = check((call), #call); if (rc_) return rc_; } while (0)
 #define CMM_LAUNCH(k, call) do { kernel_launches += (k); int rc_ = check((call), #call); if (rc_) return rc_; } while (0)
-#define CMM_FFT(call) do { fft_calls++; if ((call) != CUFFT_SUCCESS) { err = std::string("cuFFT: ") + #call; return kErrCuda; } } while (0)
+#define CMM_FFT(call) do { fft_calls++; cudaError_t e_ = (call); if (e_ != cudaSuccess) { err = std::string("FFT: ") + #call + ": " + cudaGetErrorString(e_); return kErrCuda; } } while (0)
 
 int EulerSim::learned_check() const
 {
@@ -53,23 +52,10 @@ int EulerSim::learned_setup()
         (rc = falloc((void**)&l_dspec_, sizeof(float2) * (size_t)gp.Nfft)) ||
         (rc = falloc((void**)&d_stats_, sizeof(double) * 4)))
         return rc;
-    int nc[2] = {gc.NY, gc.NX}, np[2] = {gp.NY, gp.NX};
-    cufftHandle a = 0, b = 0, c = 0, d = 0;
-    if (cufftPlanMany(&a, 2, nc, nullptr, 1, 0, nullptr, 1, 0, CUFFT_R2C, 1) != CUFFT_SUCCESS ||
-        cufftPlanMany(&b, 2, nc, nullptr, 1, 0, nullptr, 1, 0, CUFFT_C2R, 4) != CUFFT_SUCCESS ||
-        cufftPlanMany(&c, 2, np, nullptr, 1, 0, nullptr, 1, 0, CUFFT_R2C, 1) != CUFFT_SUCCESS ||
-        cufftPlanMany(&d, 2, np, nullptr, 1, 0, nullptr, 1, 0, CUFFT_C2R, 1) != CUFFT_SUCCESS) {
-        err = "cuFFT plan creation for the learned psi failed";
+    if (fft::plan_create(fc_, gc.NX, gc.NY, false, stream)) {
+        err = "FFT plan creation for the learned psi failed";
         return kErrCuda;
     }
-    cufftSetStream(a, stream);
-    cufftSetStream(b, stream);
-    cufftSetStream(c, stream);
-    cufftSetStream(d, stream);
-    lc_r2c_ = (int)a;
-    lc_c2r4_ = (int)b;
-    l_r2c_ = (int)c;
-    l_c2r_ = (int)d;
     return kOk;
 }
 
@@ -80,11 +66,7 @@ void EulerSim::learned_release()
     lc_omega_ = lc_planes_ = l_delta_ = l_planes_ = nullptr;
     lc_spec_ = lc_spec4_ = l_dspec_ = nullptr;
     d_stats_ = nullptr;
-    if (lc_r2c_) cufftDestroy((cufftHandle)lc_r2c_);
-    if (lc_c2r4_) cufftDestroy((cufftHandle)lc_c2r4_);
-    if (l_r2c_) cufftDestroy((cufftHandle)l_r2c_);
-    if (l_c2r_) cufftDestroy((cufftHandle)l_c2r_);
-    lc_r2c_ = lc_c2r4_ = l_r2c_ = l_c2r_ = 0;
+    fft::plan_destroy(fc_);
     delete ups_owned_;
     ups_owned_ = nullptr;
     ups_ = nullptr;
@@ -131,9 +113,9 @@ int EulerSim::cheap_fields()
     // omega and its gradient on the map grid, omega's spectrum, and the cheap psi's
     // Hermite planes there
     CMM_LAUNCH(1, launch_sample_grad_m(gc, gf, mapm_, wfm_, lc_omega_, stream));
-    CMM_FFT(cufftExecR2C((cufftHandle)lc_r2c_, lc_omega_, reinterpret_cast<cufftComplex*>(lc_spec_)));
+    CMM_FFT(fft::r2c(fc_, lc_omega_, lc_spec_, 1, stream));
     CMM_LAUNCH(1, launch_spec_psi_f(lc_spec_, gc, gc, s.freq_cut_psi, lc_spec4_, stream));
-    CMM_FFT(cufftExecC2R((cufftHandle)lc_c2r4_, reinterpret_cast<cufftComplex*>(lc_spec4_), lc_planes_));
+    CMM_FFT(fft::c2r(fc_, lc_spec4_, lc_planes_, 4, stream));
     return kOk;
 }
 
@@ -146,7 +128,7 @@ int EulerSim::learned_planes(lrn::Upsampler& u, float* out)
         return kErrCuda;
     }
     kernel_launches += u.launches;
-    CMM_FFT(cufftExecR2C((cufftHandle)l_r2c_, l_delta_, reinterpret_cast<cufftComplex*>(l_dspec_)));
+    CMM_FFT(fft::r2c(fp_, l_delta_, l_dspec_, 1, stream));
     CMM_LAUNCH(1, launch_spec_psi_learned(lc_spec_, gc, l_dspec_, gp, s.freq_cut_psi, spec4f_, stream));
     if ((rc = psi_planes(spec4f_, out))) return rc;
     return kOk;
@@ -221,7 +203,7 @@ int EulerSim::learned_collect(lrn::Upsampler& u)
     // target: omega sampled through the map on the psi grid minus the spectral
     // interpolation of the map-grid samples there
     CMM_LAUNCH(1, launch_spec_pad(lc_spec_, gc, gp, l_dspec_, stream));
-    CMM_FFT(cufftExecC2R((cufftHandle)l_c2r_, reinterpret_cast<cufftComplex*>(l_dspec_), l_planes_ + gp.N));
+    CMM_FFT(fft::c2r(fp_, l_dspec_, l_planes_ + gp.N, 1, stream));
     CMM_LAUNCH(1, launch_sample_m(gc, gp, gf, mapm_, wfm_, l_planes_, nullptr, stream));
     CMM_LAUNCH(1, lrn::launch_sub(l_planes_, l_planes_ + gp.N, gp.N, l_delta_, stream));
     u.set_spectral_cut((int)std::floor(s.freq_cut_psi));
@@ -253,7 +235,7 @@ int EulerSim::learned_evaluate(lrn::Upsampler& u, double* out6)
     rel(out6 + 2);
     // the ceiling: psi of omega sampled exactly on the psi grid (what a perfect network gives)
     CMM_LAUNCH(1, launch_sample_m(gc, gp, gf, mapm_, wfm_, l_delta_, nullptr, stream));
-    CMM_FFT(cufftExecR2C((cufftHandle)l_r2c_, l_delta_, reinterpret_cast<cufftComplex*>(l_dspec_)));
+    CMM_FFT(fft::r2c(fp_, l_delta_, l_dspec_, 1, stream));
     CMM_LAUNCH(1, launch_spec_psi_f(l_dspec_, gp, gp, s.freq_cut_psi, spec4f_, stream));
     if ((rc = psi_planes(spec4f_, l_planes_))) return rc;
     if ((rc = diff_stats(l_planes_, 1, exact, 4, gp.N, st))) return rc;

@@ -7,11 +7,10 @@
 // 2D transform is exactly
 //   psi = phi(x) - h(v),  psi_x = phi'(x),  psi_y = -h'(v),  psi_xy = 0
 // with phi' and h' the 1D spectral derivatives of the same samples; this
-// library computes those 1D spectra only (cuFFT 1D plans).  h depends on the
+// library computes those 1D spectra only (1D transforms, csrc/fft.hpp).  h depends on the
 // grid alone and is built once.
 #pragma once
 #include <cuda_runtime.h>
-#include <cufft.h>
 
 #include "kernels.hpp"
 
@@ -20,12 +19,14 @@ namespace cmm {
 constexpr int kVlasovRowChunk = 64;   // rows per partial sum of the v-integral
 
 struct VlasovPlans {
-    cufftHandle d2z_v = 0;   // 1D D2Z over x of the vort grid
-    cufftHandle d2z_p = 0;   // 1D D2Z of length NX of the psi grid (x, and v since NX == NY)
-    cufftHandle z2d_p = 0;   // 1D Z2D of length NX of the psi grid
+    fft::Plan2D v;           // 1D transforms of length NX of the vort grid
+    fft::Plan2D p;           // 1D transforms of length NX of the psi grid (x, and v since NX == NY)
 };
 bool make_vlasov_plans(VlasovPlans& p, const Grid& gv, const Grid& gp, cudaStream_t s);
 void destroy_vlasov_plans(VlasovPlans& p);
+// one 1D D2Z / Z2D of a plan's length (unnormalised; the Z2D input is not modified)
+cudaError_t fft_d2z_1d(const fft::Plan2D& p, const double* in, double2* out, cudaStream_t s);
+cudaError_t fft_z2d_1d(const fft::Plan2D& p, const double2* in, double* out, cudaStream_t s);
 
 // rho[ix] = hy * (f[0][ix] + sum_iy f[iy][ix]) - 1 on the vort grid (row 0
 // enters twice, as in the reference, whose integral_v output aliases it);

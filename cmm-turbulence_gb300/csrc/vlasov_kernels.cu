@@ -5,7 +5,6 @@
 // and the periodification h(v) are 1D spectra; the Hermite planes of the
 // separable psi are written directly (see vlasov.hpp).
 #include <cuda_runtime.h>
-#include <cufft.h>
 
 #include "vlasov.hpp"
 
@@ -13,21 +12,23 @@ namespace cmm {
 
 bool make_vlasov_plans(VlasovPlans& p, const Grid& gv, const Grid& gp, cudaStream_t s)
 {
-    if (cufftPlan1d(&p.d2z_v, gv.NX, CUFFT_D2Z, 1) != CUFFT_SUCCESS) return false;
-    if (cufftPlan1d(&p.d2z_p, gp.NX, CUFFT_D2Z, 1) != CUFFT_SUCCESS) return false;
-    if (cufftPlan1d(&p.z2d_p, gp.NX, CUFFT_Z2D, 1) != CUFFT_SUCCESS) return false;
-    cufftSetStream(p.d2z_v, s);
-    cufftSetStream(p.d2z_p, s);
-    cufftSetStream(p.z2d_p, s);
-    return true;
+    return fft::plan_create_rows(p.v, gv.NX, true, s) == 0 && fft::plan_create_rows(p.p, gp.NX, true, s) == 0;
 }
 
 void destroy_vlasov_plans(VlasovPlans& p)
 {
-    if (p.d2z_v) cufftDestroy(p.d2z_v);
-    if (p.d2z_p) cufftDestroy(p.d2z_p);
-    if (p.z2d_p) cufftDestroy(p.z2d_p);
-    p = VlasovPlans();
+    fft::plan_destroy(p.v);
+    fft::plan_destroy(p.p);
+}
+
+cudaError_t fft_d2z_1d(const fft::Plan2D& p, const double* in, double2* out, cudaStream_t s)
+{
+    return fft::rows_r2c(p, in, p.nx, p.nx, out, p.nx / 2 + 1, p.nx / 2 + 1, 1, 1, p.nx / 2 + 1, s);
+}
+
+cudaError_t fft_z2d_1d(const fft::Plan2D& p, const double2* in, double* out, cudaStream_t s)
+{
+    return fft::rows_c2r(p, in, p.nx / 2 + 1, p.nx / 2 + 1, p.nx / 2 + 1, out, p.nx, p.nx, 1, 1, s);
 }
 
 // ---------------------------------------------------------------- v-integral

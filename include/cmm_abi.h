@@ -34,7 +34,7 @@ extern "C" {
 #define CMM_OK 0
 #define CMM_ERR_PARAM (-1)      /* bad setting / argument (reference: error() -> exit) */
 #define CMM_ERR_IO (-2)         /* unreadable input file, unwritable output */
-#define CMM_ERR_CUDA (-3)       /* CUDA / cuFFT / cuRAND failure (reference: exit(0)) */
+#define CMM_ERR_CUDA (-3)       /* CUDA / cuRAND failure (reference: exit(0)) */
 #define CMM_ERR_SATURATED (-4)  /* map stack full; loop stopped (reference: "Stack Saturated") */
 #define CMM_ERR_STATE (-5)      /* call out of order (e.g. step before init) */
 #define CMM_ERR_UNSUPPORTED (-6)/* option of the reference not built in this library */
@@ -106,7 +106,7 @@ int cmm_get_scalar(cmm_ctx* ctx, const char* name, double* out);
  * stream synchronisation per iteration while on).  Totals are read back as
  * scalars "prof_<phase>_ms" / "prof_<phase>_count" for the phases advect,
  * incomp, remap, psi, coarse, particles, save; "kernel_launches" and
- * "fft_calls" count this library's kernel launches and cuFFT executions.
+ * "fft_calls" count this library's kernel launches and 2D / 1D transform calls.
  * The reference has no counterpart (it only logs wall-clock C-Time,
  * src/simulation/cmm-euler2d.cu:940-959). */
 int cmm_set_profiling(cmm_ctx* ctx, int on);
@@ -184,6 +184,23 @@ int cmm_poisson_create(const cmm_grid* grid_vort, const cmm_grid* grid_psi, doub
 int cmm_poisson_hermite(cmm_poisson* p, const double* vort, double* psi_out);
 int cmm_poisson_destroy(cmm_poisson* p);
 
+/* ---------------------------------------------------------------- transforms
+ * The library's own 2D real FFT on sm_103a (no cuFFT): replaces the cuFFT D2Z / Z2D plans
+ * the reference builds per grid (src/grid/cmm-grid2d.cu:123-131) and their cufftExecD2Z /
+ * cufftExecZ2D calls (src/numerical/cmm-fft.cu:398-429, src/simulation/cmm-simulation-host.cu:
+ * 299-375).  ny rows of nx real values <-> ny rows of nx/2+1 complex values (interleaved re,
+ * im), unnormalised, cuFFT's sign conventions; `batch` items back to back; precision 0 =
+ * FP64, 1 = FP32.  C2R ignores the imaginary parts of the kx = 0 and kx = nx/2 columns after
+ * the column transform and may overwrite its input, as cuFFT's C2R does.  Shapes: nx even,
+ * nx/2 and ny at most 8192 (FP64 columns longer than 4096 and lengths with prime factors
+ * 5..13 run slower), every prime factor at most 13 (else CMM_ERR_PARAM).  Stream-ordered;
+ * the transforms allocate nothing. */
+typedef struct cmm_fft cmm_fft;
+int cmm_fft_create(int nx, int ny, int precision, void* stream, cmm_fft** out);
+int cmm_fft_r2c(cmm_fft* f, const void* in, void* out, int batch);
+int cmm_fft_c2r(cmm_fft* f, void* in, void* out, int batch);
+int cmm_fft_destroy(cmm_fft* f);
+
 /* Vlasov-Poisson potential.  Replaces evaluate_potential_from_density_hermite
  * (src/simulation/cmm-simulation-host.cu:385-471,534-571): f = f_fine_H o X on
  * grid_vort, rho = h_v sum_v f - 1, phi from the 1D Poisson solve on the x
@@ -225,9 +242,11 @@ int cmm_diagnostics(const cmm_grid* grid_psi, const double* psi, const cmm_grid*
  * loaded), so 2*NX*NY of grid_psi and NX*NY of grid_coarse may each be at
  * most 4194304 (2048^2 coarse, 1448^2 psi); larger grids -> CMM_ERR_PARAM.
  * The first call on each device looks up the array's address (set-up, with
- * that device current); later calls only launch.  Nothing in the scratch has
- * to start at zero.  Calls that overlap -- other streams or host threads --
- * race on the one array: serialise them.  Synchronises the stream. */
+ * that device current) and keeps it for the life of the process; later calls
+ * only launch.  A cudaDeviceReset ends that address's validity: a process that
+ * resets the device must not call this entry point afterwards.  Nothing in the
+ * scratch has to start at zero.  Calls that overlap -- other streams or host
+ * threads -- race on the one array: serialise them.  Synchronises the stream. */
 int cmm_diagnostics_noalloc(const cmm_grid* grid_psi, const double* psi, const cmm_grid* grid_coarse,
                             const double* vort, double* out3, void* stream);
 
@@ -235,7 +254,7 @@ int cmm_diagnostics_noalloc(const cmm_grid* grid_psi, const double* psi, const c
  * Many mixed-form 2D Euler runs of uneven sizes advanced together: one iteration
  * advances every member by one of its own time steps, with the advection,
  * incompressibility check, psi solve and coarse sample of all members in batched
- * launches (one cuFFT call per size class), captured as CUDA graphs.  Each member is
+ * launches (one batched transform per size class), captured as CUDA graphs.  Each member is
  * configured like cmm_create (argc[i] strings of argv, members one after another) and
  * must be precision=mixed, 2D Euler, three Lagrange levels, EulerExp / RK2 / RK3 maps.
  * The reference has no ensemble driver; this is new API. */

@@ -98,3 +98,15 @@ def test_init_without_gpu_returns_cuda_error(tmp_path):
     with pytest.raises(m.CmmError) as e:
         sim.init()
     assert e.value.code == m.CMM_ERR_CUDA
+
+
+def test_fft_rejects_unsupported_shapes_before_any_gpu_work():
+    """Shapes the library's FFT does not run are a status code at creation (checked
+    before any CUDA call): odd row length, a prime factor above 13, too long a side."""
+    m = cmm()
+    for nx, ny in ((63, 64), (64, 17 * 4), (2 * 17, 64), (2 * 16384, 64), (64, 16384)):
+        with pytest.raises(m.CmmError) as e:
+            m.FFT(nx, ny, 0)
+        assert e.value.code == m.CMM_ERR_PARAM, (nx, ny)
+    with pytest.raises(m.CmmError):
+        m.FFT(64, 64, 2)

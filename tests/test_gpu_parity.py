@@ -236,11 +236,31 @@ def test_c1_full_run_matches_oracle_field_by_field(tmp_path, threshold):
     assert maps_gpu == maps_cpu
     if threshold < 1e-4:
         assert maps_gpu[-1] >= 2
-    assert map_err(sim.field("Map_ChiX_H_coarse"), o.chix()) < 1e-10
-    assert map_err(sim.field("Map_ChiY_H_coarse"), o.chiy()) < 1e-10
-    assert herm_err(sim.field("Vorticity_W_fine_H"), o.vort_fine(), 512) < 1e-10
+    from test_gpu_parity_configs import plane_errs, report
+    for name, ref in (("Map_ChiX_H_coarse", o.chix()), ("Map_ChiY_H_coarse", o.chiy())):
+        report("c1-%g %s" % (threshold, name), planes=plane_errs(sim.field(name), ref),
+               cond=map_err(sim.field(name), ref))
+    for name, ref, n in (("Vorticity_W_fine_H", o.vort_fine(), 512), ("Stream_function_Psi_H_psi", o.psi(), 256)):
+        report("c1-%g %s" % (threshold, name), planes=plane_errs(sim.field(name), ref),
+               herm=herm_err(sim.field(name), ref, n))
+    report("c1-%g Vorticity_W_coarse" % threshold, rel=rel_linf(sim.field("Vorticity_W_coarse"), o.vort()))
+    # conditioning-scaled and plain per-plane bounds (measured on a GB300: map value planes
+    # <= 1.6e-13, slope planes <= 1.3e-10, cross planes <= 3.1e-8 of their own maxima; psi
+    # planes <= 1.3e-12; coarse omega <= 5.3e-13; the fine omega's cross plane is identically
+    # zero for this initial condition, so it is bounded against the value plane instead)
+    for name, ref in (("Map_ChiX_H_coarse", o.chix()), ("Map_ChiY_H_coarse", o.chiy())):
+        got = sim.field(name)
+        pe = plane_errs(got, ref)
+        assert map_err(got, ref) < 1e-12, name
+        assert pe[0] < 1e-12 and max(pe[1:3]) < 1e-9 and pe[3] < 1e-6, (name, pe)
+    wf = sim.field("Vorticity_W_fine_H")
+    pe = plane_errs(wf, o.vort_fine())
+    assert herm_err(wf, o.vort_fine(), 512) < 1e-12
+    assert pe[0] < 1e-11 and max(pe[1:3]) < 1e-9, pe
+    psi = sim.field("Stream_function_Psi_H_psi")
+    assert max(plane_errs(psi, o.psi())) < 1e-11
     for name, ref in (("Stream_function_Psi_H_psi", o.psi()), ("Vorticity_W_coarse", o.vort())):
-        assert rel_linf(sim.field(name), ref) < 1e-10, name
+        assert rel_linf(sim.field(name), ref) < 1e-12, name
     for name, ref in (("energy", o.energy()), ("enstrophy", o.enstrophy()), ("palinstrophy", o.palinstrophy())):
         assert abs(sim.scalar(name) - ref) <= 1e-11 * abs(ref), name
 

@@ -53,6 +53,23 @@ def test_noalloc_matches_diagnostics_on_consecutive_calls():
         assert first == second, "the second call over the reused scratch must repeat the first"
 
 
+def test_noalloc_leaves_device_memory_untouched():
+    """After the first call on the device (which looks up the scratch array's address), calls
+    at the largest sizes change the device's free memory by nothing: no allocation, cached
+    or leaked, happens inside the entry point."""
+    m = cmm()
+    stream = torch.cuda.current_stream().cuda_stream
+    gp, gc = m.grid(1448), m.grid(2048)
+    psi, vort = _fields(1448, 2048, 5)
+    m.diagnostics_noalloc(gp, psi, gc, vort, stream)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(5):
+        m.diagnostics_noalloc(gp, psi, gc, vort, stream)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
 def test_noalloc_rejects_grids_beyond_its_scratch():
     m = cmm()
     psi, vort = _fields(8, 8, 4)

@@ -22,9 +22,11 @@
 // w^(r k n/(pR)) (w = exp(-2 pi i/n)), an R-point DFT, outputs
 // y[(i - k) R + k + r p].  Every pass reads its inputs into registers, the
 // block synchronises, and the outputs are written back in place (one buffer
-// of n values per transform in shared memory).  Twiddles come from a table
-// exp(-2 pi i t/T) (t < T) in global memory, computed on the host in extended
-// precision; a transform of length n = T/ts reads it at stride ts.
+// of n values per transform in shared memory).  Twiddles come from per-pass
+// tables (RadixPlan::toff) laid out so that the butterflies of a warp read
+// consecutive entries, computed on the host in extended precision and copied
+// into shared memory once per block (the kernels are persistent: a block
+// transforms group after group).
 //
 // Real transforms of even length N pack x into the complex length-N/2
 // sequence z[m] = x[2m] + i x[2m+1]:
@@ -40,11 +42,18 @@ namespace fft {
 
 constexpr int kMaxPasses = 24;
 
-// radices of one transform length, in pass order
+// radices of one transform length, in pass order; for power-of-two lengths the log2 of
+// n / R and of the span p before each pass (index arithmetic by shifts).  The twiddles of
+// pass q sit at toff[q] of the plan's table: entry k (R - 1) + r - 1 holds w^(r k n/(pR))
+// (w = exp(-2 pi i / n), k < p, 1 <= r < R), so a warp's butterflies read consecutive
+// entries; a generic radix appends its R roots of unity.  tlen: the table's length.
 struct RadixPlan {
     int n;                      // complex length
     int np;                     // number of passes
     unsigned char r[kMaxPasses];
+    unsigned char lnr[kMaxPasses], lp[kMaxPasses];
+    int toff[kMaxPasses];
+    int tlen;
 };
 
 #ifdef __CUDACC__
@@ -125,9 +134,9 @@ template <typename V> __device__ __forceinline__ void dft3(V* a, bool inv)
     a[2] = csub(m1, m2);
 }
 
-// any small R: direct DFT, roots of unity from the twiddle table (entry m ts n/R ... )
+// any small R: direct DFT with the R roots of unity of the pass table
 template <int R, typename V>
-__device__ __forceinline__ void dft_generic(V* a, bool inv, const V* __restrict__ tw, long long rstep)
+__device__ __forceinline__ void dft_generic(V* a, bool inv, const V* roots)
 {
     V out[R];
 #pragma unroll
@@ -135,7 +144,7 @@ __device__ __forceinline__ void dft_generic(V* a, bool inv, const V* __restrict_
         V s = a[0];
 #pragma unroll
         for (int r = 1; r < R; ++r) {
-            V w = __ldg(tw + (long long)((q * r) % R) * rstep);
+            V w = roots[(q * r) % R];
             if (inv) w = cconj(w);
             s = cadd(s, cmul(a[r], w));
         }
@@ -147,14 +156,14 @@ __device__ __forceinline__ void dft_generic(V* a, bool inv, const V* __restrict_
 
 // ---------------------------------------------------------------- one Stockham pass
 // nb transforms of length n at s[pad(b n + i)]; VPT = values per thread the block was
-// sized for (nb n <= VPT blockDim.x)
-template <int R, int VPT, typename V>
-__device__ __forceinline__ void pass(V* s, int nb, int n, int p, const V* __restrict__ tw, int ts, bool inv)
+// sized for (nb n <= VPT blockDim.x); POW2: n, R and p are powers of two (lnr = log2(n/R),
+// lp = log2(p)); ptw: this pass's twiddles (shared memory, or global for the longest lengths)
+template <int R, int VPT, bool POW2, typename V>
+__device__ __forceinline__ void pass(V* s, int nb, int n, int p, int lnr, int lp, const V* ptw, bool inv)
 {
     constexpr int B = (VPT + R - 1) / R;
     const int nR = n / R;
     const int total = nb * nR;
-    const long long tstep = (long long)(n / (p * R)) * ts;   // table step of w^(r k n/(pR))
     V v[B][R];
     int dst[B];
 #pragma unroll
@@ -162,15 +171,17 @@ __device__ __forceinline__ void pass(V* s, int nb, int n, int p, const V* __rest
         const int t = threadIdx.x + j * blockDim.x;
         dst[j] = -1;
         if (t < total) {
-            const int b = t / nR, i = t - b * nR;
-            const int k = i % p;
+            const int b = POW2 ? t >> lnr : t / nR;
+            const int i = t - b * nR;
+            const int k = POW2 ? i & ((1 << lp) - 1) : i % p;
             const int base = b * n;
 #pragma unroll
             for (int r = 0; r < R; ++r) v[j][r] = s[pad<V>(base + i + r * nR)];
             if (k != 0) {
+                const V* tk = ptw + k * (R - 1);
 #pragma unroll
                 for (int r = 1; r < R; ++r) {
-                    V w = __ldg(tw + (long long)(r * k) * tstep);
+                    V w = tk[r - 1];
                     if (inv) w = cconj(w);
                     v[j][r] = cmul(v[j][r], w);
                 }
@@ -179,7 +190,7 @@ __device__ __forceinline__ void pass(V* s, int nb, int n, int p, const V* __rest
             else if (R == 4) dft4(v[j], inv);
             else if (R == 8) dft8(v[j], inv);
             else if (R == 3) dft3(v[j], inv);
-            else dft_generic<R>(v[j], inv, tw, (long long)(n / R) * ts);
+            else dft_generic<R>(v[j], inv, ptw + p * (R - 1));
             dst[j] = base + (i - k) * R + k;
         }
     }
@@ -210,38 +221,48 @@ inline int family_of(const RadixPlan& P)
 }
 
 // all passes of nb length-n transforms held in shared memory (in place); every thread
-// of the block takes part.  tw: table exp(-2 pi i t / (n ts)), t < n ts.
+// of the block takes part.  tw: the plan's table (RadixPlan::toff).
 template <int VPT, int FAM, typename V>
-__device__ __forceinline__ void block_fft(V* s, int nb, const RadixPlan& P, const V* __restrict__ tw, int ts, bool inv)
+__device__ __forceinline__ void block_fft(V* s, int nb, const RadixPlan& P, const V* tw, bool inv)
 {
+    constexpr bool P2 = FAM == kPow2;
     int p = 1;
     for (int q = 0; q < P.np; ++q) {
-        const int R = P.r[q];
-        if (R == 8) pass<8, VPT>(s, nb, P.n, p, tw, ts, inv);
-        else if (R == 4) pass<4, VPT>(s, nb, P.n, p, tw, ts, inv);
-        else if (R == 2) pass<2, VPT>(s, nb, P.n, p, tw, ts, inv);
-        else if (FAM >= kPow2x3 && R == 3) pass<3, VPT>(s, nb, P.n, p, tw, ts, inv);
+        const int R = P.r[q], lnr = P.lnr[q], lp = P.lp[q];
+        const V* ptw = tw + P.toff[q];
+        if (R == 8) pass<8, VPT, P2>(s, nb, P.n, p, lnr, lp, ptw, inv);
+        else if (R == 4) pass<4, VPT, P2>(s, nb, P.n, p, lnr, lp, ptw, inv);
+        else if (R == 2) pass<2, VPT, P2>(s, nb, P.n, p, lnr, lp, ptw, inv);
+        else if (FAM >= kPow2x3 && R == 3) pass<3, VPT, false>(s, nb, P.n, p, lnr, lp, ptw, inv);
         else if (FAM == kAny) {
-            if (R == 5) pass<5, VPT>(s, nb, P.n, p, tw, ts, inv);
-            else if (R == 7) pass<7, VPT>(s, nb, P.n, p, tw, ts, inv);
-            else if (R == 11) pass<11, VPT>(s, nb, P.n, p, tw, ts, inv);
-            else pass<13, VPT>(s, nb, P.n, p, tw, ts, inv);
+            if (R == 5) pass<5, VPT, false>(s, nb, P.n, p, lnr, lp, ptw, inv);
+            else if (R == 7) pass<7, VPT, false>(s, nb, P.n, p, lnr, lp, ptw, inv);
+            else if (R == 11) pass<11, VPT, false>(s, nb, P.n, p, lnr, lp, ptw, inv);
+            else pass<13, VPT, false>(s, nb, P.n, p, lnr, lp, ptw, inv);
         }
         p *= R;
     }
 }
 
+// the twiddle table (len entries) into shared memory
+template <typename V>
+__device__ __forceinline__ void load_table(V* dst, const V* __restrict__ src, int len)
+{
+    for (int t = threadIdx.x; t < len; t += blockDim.x) dst[t] = __ldg(src + t);
+}
+
 // ---------------------------------------------------------------- real packing
 // R2C output bin k (0 <= k <= n) of the real length-2n sequence whose packed transform
-// Z (length n, padded at s + off) sits in shared memory; W^k = tw[k] (table of 2n entries)
+// Z (length n, padded at s + off) sits in shared memory; W^k = tw[k] (the row plan's
+// table of W^k, k <= n, after its pass twiddles)
 template <typename V>
-__device__ __forceinline__ V r2c_bin(const V* s, int off, int n, int k, const V* __restrict__ tw)
+__device__ __forceinline__ V r2c_bin(const V* s, int off, int n, int k, const V* tw)
 {
     using T = decltype(s[0].x);
     const V zk = s[pad<V>(off + (k == n ? 0 : k))];
     const V zc = cconj(s[pad<V>(off + (k == 0 ? 0 : n - k))]);
     const V sum = cadd(zk, zc), dif = csub(zk, zc);
-    const V w = __ldg(tw + k);
+    const V w = tw[k];
     const V t = cmul(w, dif);            // W^k (Z_k - conj Z_{n-k})
     return mk((T)0.5 * (sum.x + t.y), (T)0.5 * (sum.y - t.x));   // 1/2 (sum - i t)
 }
@@ -249,11 +270,11 @@ __device__ __forceinline__ V r2c_bin(const V* s, int off, int n, int k, const V*
 // C2R packed input Z_k (0 <= k < n) from the half-spectrum bins X_k and X_{n-k} (with
 // the imaginary parts of X_0 and X_n already dropped); W^-k = conj(tw[k])
 template <typename V>
-__device__ __forceinline__ V c2r_pack(const V& xk, const V& xnk, int k, const V* __restrict__ tw)
+__device__ __forceinline__ V c2r_pack(const V& xk, const V& xnk, int k, const V* tw)
 {
     const V b = cconj(xnk);
     const V sum = cadd(xk, b), dif = csub(xk, b);
-    const V t = cmul(cconj(__ldg(tw + k)), dif);   // W^-k (X_k - conj X_{n-k})
+    const V t = cmul(cconj(tw[k]), dif);   // W^-k (X_k - conj X_{n-k})
     return mk(sum.x - t.y, sum.y + t.x);          // sum + i t
 }
 #endif  // __CUDACC__

@@ -22,13 +22,15 @@ constexpr int kMaxLen = 8192;   // longest complex transform (values per transfo
 // true when a complex transform of length n runs here (n <= kMaxLen, primes <= 13)
 bool supported_length(int n);
 bool make_radix_plan(int n, RadixPlan& p);
+// blocks of a persistent launch of func: as many as stay resident on the GPU, at most groups
+int resident_grid(const void* func, int threads, size_t smem, long long groups);
 
 struct Plan2D {
     int nx = 0, ny = 0;
     bool dbl = false;
     RadixPlan rx{}, ry{};      // rx: complex length nx/2 (packed rows), ry: ny (columns)
-    void* twx = nullptr;       // nx entries exp(-2 pi i t / nx) (float2 / double2)
-    void* twy = nullptr;       // ny entries exp(-2 pi i t / ny)
+    void* twx = nullptr;       // rx's pass twiddles, then exp(-2 pi i k / nx) for k <= nx/2 (float2 / double2)
+    void* twy = nullptr;       // ry's pass twiddles
     bool ok() const { return twx != nullptr; }
 };
 

@@ -75,16 +75,17 @@ cudaError_t launch_sample_vort(const Grid& gm, const Grid& gout, const Grid& gf,
                                const double* Y, const double* Wf, int molly, double* out, long long ld,
                                cudaStream_t s);
 
-// the fused psi solve (evaluate_stream_hermite, cmm-simulation-host.cu:333-375): omega
-// through the map on gv, its kept modes, the four psi Hermite planes on gp, in three
-// launches on the library's FFT; runs when psi_solve_fits, which also gives the complex
-// values the work arrays w1, w2 need
+// the psi solve (evaluate_stream_hermite, cmm-simulation-host.cu:333-375) on the library's
+// FFT: omega through the map on gv (into the scratch omega, gv.N doubles), its kept modes,
+// the four psi Hermite planes on gp, in four launches (psi_solve.cuh); runs when
+// psi_solve_fits, which also gives the complex values the work arrays w1, w2 need
 bool psi_solve_fits(const Grid& gv, const Grid& gp, double freq, const fft::Plan2D& pv, const fft::Plan2D& pp,
                     long long* w1_values, long long* w2_values);
 void psi_solve_prepare();
 cudaError_t launch_psi_solve(const Grid& gm, const Grid& gv, const Grid& gf, const double* X, const double* Y,
                              const double* Wf, int molly, const Grid& gp, double freq, const fft::Plan2D& pv,
-                             const fft::Plan2D& pp, double2* w1, double2* w2, double* psi_out, cudaStream_t s);
+                             const fft::Plan2D& pp, double* omega, double2* w1, double2* w2, double* psi_out,
+                             cudaStream_t s);
 
 // tracer and inertial particles (Particle_advect / Particle_advect_inertia,
 // src/numerical/cmm-particles.cu:119-551); psi[0] is t_{n+1}, psi[1] t_n, psi[2] t_{n-1}

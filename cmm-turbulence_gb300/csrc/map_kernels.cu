@@ -474,21 +474,9 @@ cudaError_t launch_sample_vort(const Grid& gm, const Grid& go, const Grid& gf, c
 }
 
 // ---------------------------------------------------------------------------
-// the fused psi solve of the plain form (psi_solve.cuh): omega through the map on
-// the vorticity grid (sample_vort_point), the kept modes, the four psi planes
+// the psi solve of the plain form on the library's FFT (psi_solve.cuh): omega through
+// the map on the vorticity grid (k_sample_vort), the kept modes, the four psi planes
 // ---------------------------------------------------------------------------
-struct SampleVortSrc {
-    Grid gm, go, gf;
-    const double* X;
-    const double* Y;
-    const double* Wf;
-    int molly;
-    __device__ __forceinline__ double value(int iX, int iY, bool live) const
-    {
-        return live ? sample_vort_point(gm, go, gf, X, Y, Wf, molly, iX, iY) : 0.0;
-    }
-};
-
 struct PlanesEpi {
     int nx;
     long long n;
@@ -506,7 +494,6 @@ struct PlanesEpi {
 bool psi_solve_fits(const Grid& gv, const Grid& gp, double freq, const fft::Plan2D& pv, const fft::Plan2D& pp,
                     long long* w1_values, long long* w2_values)
 {
-    if (gv.NY > 65535) return false;
     const psi::Layout L = psi::make_layout<double>(gv, gp, freq, pv, pp);
     if (!L.ok) return false;
     if (w1_values) *w1_values = L.w1_values;
@@ -516,18 +503,20 @@ bool psi_solve_fits(const Grid& gv, const Grid& gp, double freq, const fft::Plan
 
 void psi_solve_prepare()
 {
-    psi::prepare<double, SampleVortSrc, PlanesEpi>();
+    psi::prepare<double, PlanesEpi>();
 }
 
 cudaError_t launch_psi_solve(const Grid& gm, const Grid& gv, const Grid& gf, const double* X, const double* Y,
                              const double* Wf, int molly, const Grid& gp, double freq, const fft::Plan2D& pv,
-                             const fft::Plan2D& pp, double2* w1, double2* w2, double* psi_out, cudaStream_t s)
+                             const fft::Plan2D& pp, double* omega, double2* w1, double2* w2, double* psi_out,
+                             cudaStream_t s)
 {
     const psi::Layout L = psi::make_layout<double>(gv, gp, freq, pv, pp);
     if (!L.ok) return cudaErrorInvalidValue;
-    SampleVortSrc src{gm, gv, gf, X, Y, Wf, molly};
+    cudaError_t e = launch_sample_vort(gm, gv, gf, X, Y, Wf, molly, omega, gv.NX, s);
+    if (e != cudaSuccess) return e;
     PlanesEpi epi{gp.NX, gp.N, psi_out};
-    return psi::launch<double>(L, gv, gp, freq, pv, pp, w1, w2, src, epi, s);
+    return psi::launch<double>(L, gv, gp, freq, pv, pp, omega, w1, w2, epi, s);
 }
 
 }  // namespace cmm

@@ -45,6 +45,20 @@ cudaError_t launch_psi_nodes3(const float* planes, long long n, const float4* l1
                               const double* c2, const double* c3, float4* out0, float4* o1, float4* o2, float4* o3,
                               cudaStream_t s);
 cudaError_t launch_advect_m(const AdvectMArgs& a, cudaStream_t s);
+// the psi solve on the library's FFT (psi_solve.cuh): omega through the map on gv (into the
+// scratch omega, gv.N floats), its kept modes, the psi nodes on gp and, with c1 != nullptr,
+// the three Lagrange combinations of launch_psi_nodes3, in four launches; runs when
+// psi_solve_m_fits (vort grid an integer multiple of the map grid, shapes the kernels
+// hold), which also gives the complex values the work arrays w1, w2 need
+bool psi_solve_m_fits(const Grid& gm, const Grid& gv, const Grid& gp, double freq, const fft::Plan2D& pv,
+                      const fft::Plan2D& pp, long long* w1_values, long long* w2_values);
+void psi_solve_m_prepare();
+cudaError_t launch_psi_solve_m(const Grid& gm, const Grid& gv, const Grid& gf, const float4* map, const float4* W,
+                               const Grid& gp, double freq, const fft::Plan2D& pv, const fft::Plan2D& pp, float* omega,
+                               float2* w1, float2* w2, float4* out0, const float4* l1, const float4* l2,
+                               const double* c1, const double* c2, const double* c3, float4* o1, float4* o2,
+                               float4* o3, cudaStream_t s);
+cudaError_t launch_advect_m(const AdvectMArgs& a, cudaStream_t s);
 // the fused psi solve (omega through the map on gv, the kept modes, psi nodes on gp and, with
 // c1 != nullptr, the three Lagrange combinations of launch_psi_nodes3): three launches on the
 // library's FFT; runs when psi_solve_m_fits (vort grid = 4 x map grid, shapes the fused

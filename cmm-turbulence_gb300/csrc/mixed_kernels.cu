@@ -394,141 +394,6 @@ __global__ void __launch_bounds__(256) k_advect_m(const AdvectMArgs a, int lpn_l
 }
 
 // ---------------------------------------------------------------------------
-// The advection with its gathers staged in shared memory (EulerExp, RK2, RK3; up to 8
-// footpoints per node).  A block takes a tile of 8 x 4 map nodes and first copies, with
-// row-contiguous loads, the psi nodes its footpoints can reach -- the tile's psi cells and
-// a halo of kPsiHalo cells -- of every psi field the scheme reads, and the map nodes
-// around the tile (halo kMapHalo).  A footpoint whose cell lies outside the staged region
-// (a displacement beyond the halo) reads global memory instead.  The arithmetic is that
-// of advect_m_tile on the same values, so the results are identical.
-// ---------------------------------------------------------------------------
-constexpr int kTileNX = 8, kTileNY = 4, kPsiHalo = 2, kMapHalo = 1;
-
-struct Staged {
-    const float4* s;   // tile in shared memory (map: two float4 per node)
-    int x0, y0;        // unwrapped grid coordinates of its first node
-    int wx, wy;        // nodes per row, rows
-};
-
-__device__ __forceinline__ bool staged_cell(const Staged& st, int bx, int by, float qx, float qy, float fx, float fy,
-                                            int& off)
-{
-    const int lx = bx + (int)fx - st.x0, ly = by + (int)fy - st.y0;
-    off = ly * st.wx + lx;
-    return (unsigned)lx < (unsigned)(st.wx - 1) && (unsigned)ly < (unsigned)(st.wy - 1);
-}
-
-// velocity of the psi field P (staged copy st) at (bx h + ox, by h + oy)
-__device__ __forceinline__ void velocity_st(const float4* __restrict__ P, const Staged& st, const Grid& g, int bx,
-                                            int by, float ox, float oy, float& ux, float& uy)
-{
-    const float qx = ox * g.ihxf, qy = oy * g.ihyf;
-    const float fx = floorf(qx), fy = floorf(qy);
-    int off;
-    if (staged_cell(st, bx, by, qx, qy, fx, fy, off)) {
-        const float4* r = st.s + off;
-        Q4 q;
-        q.c00 = r[0]; q.c10 = r[1]; q.c01 = r[st.wx]; q.c11 = r[st.wx + 1];
-        velocity_q(q, g, qx - fx, qy - fy, ux, uy);
-    } else {
-        velocity_f(P, g, locate_q(g, bx, by, qx, qy), ux, uy);
-    }
-}
-
-// map displacement (staged copy st of the map M) at (bx h + ox, by h + oy), minus (rx, ry)
-__device__ __forceinline__ void map_disp_st(const float4* __restrict__ M, const Staged& st, const Grid& g, int bx,
-                                            int by, float ox, float oy, float rx, float ry, float& dxo, float& dyo)
-{
-    const float qx = ox * g.ihxf, qy = oy * g.ihyf;
-    const float fx = floorf(qx), fy = floorf(qy);
-    int off;
-    if (staged_cell(st, bx, by, qx, qy, fx, fy, off)) {
-        const float4* r = st.s + 2 * off;
-        const float4* r1 = r + 2 * st.wx;
-        map_disp_q(r[0], r[1], r[2], r[3], r1[0], r1[1], r1[2], r1[3], g, qx - fx, qy - fy, rx, ry, dxo, dyo);
-    } else {
-        map_disp_f(M, g, locate_q(g, bx, by, qx, qy), rx, ry, dxo, dyo);
-    }
-}
-
-template <int TI>
-__global__ void __launch_bounds__(256) k_advect_ms(const AdvectMArgs a)
-{
-    __shared__ float sc[4][kMaxFoot];
-    extern __shared__ __align__(16) float4 st_mem[];
-    constexpr int nf = TI == 10 ? 1 : (TI == 21 ? 2 : 3);   // psi fields the scheme reads
-    if (threadIdx.x < 4 * kMaxFoot) sc[threadIdx.x / kMaxFoot][threadIdx.x % kMaxFoot] =
-        a.coef[threadIdx.x / kMaxFoot][threadIdx.x % kMaxFoot];
-    const int tiles_x = a.gm.NX / kTileNX;
-    const int tx0 = (int)(blockIdx.x % tiles_x) * kTileNX, ty0 = (int)(blockIdx.x / tiles_x) * kTileNY;
-    const int pwx = (kTileNX - 1) * a.rp + 2 * kPsiHalo + 2, pwy = (kTileNY - 1) * a.rp + 2 * kPsiHalo + 2;
-    const int mwx = kTileNX + 2 * kMapHalo + 1, mwy = kTileNY + 2 * kMapHalo + 1;
-    Staged sA{st_mem, tx0 * a.rp - kPsiHalo, ty0 * a.rp - kPsiHalo, pwx, pwy};
-    Staged sB = sA, s0 = sA;
-    sB.s = st_mem + pwx * pwy;
-    s0.s = st_mem + (nf - 1) * pwx * pwy;
-    Staged sM{st_mem + nf * pwx * pwy, tx0 - kMapHalo, ty0 - kMapHalo, mwx, mwy};
-    const float4* fields[3] = {a.psiA, TI == 21 ? a.psi0 : a.psiB, a.psi0};
-    const int np = pwx * pwy;
-    for (int e = threadIdx.x; e < nf * np; e += blockDim.x) {
-        const int f = e / np, r = e - f * np, ly = r / pwx, lx = r - ly * pwx;
-        const int gx = wrap_index(sA.x0 + lx, a.gp.NX), gy = wrap_index(sA.y0 + ly, a.gp.NY);
-        st_mem[e] = __ldg(fields[f] + (long long)gy * a.gp.NX + gx);
-    }
-    float4* sm = st_mem + nf * np;
-    for (int e = threadIdx.x; e < 2 * mwx * mwy; e += blockDim.x) {
-        const int node = e >> 1, ly = node / mwx, lx = node - ly * mwx;
-        const int gx = wrap_index(sM.x0 + lx, a.gm.NX), gy = wrap_index(sM.y0 + ly, a.gm.NY);
-        sm[e] = __ldg(a.map + 2 * ((long long)gy * a.gm.NX + gx) + (e & 1));
-    }
-    __syncthreads();
-    const int ln = threadIdx.x >> 3, k = threadIdx.x & 7;
-    const int iX = tx0 + (ln % kTileNX), iY = ty0 + ln / kTileNX;
-    const int nd = iY * a.gm.NX + iX;
-    const float4 n0 = sm[2 * ((iY - sM.y0) * mwx + (iX - sM.x0))];   // (dX, dY, dX_x, dY_x) at the node
-    float gX = 0.0f, gY = 0.0f;
-    if (k < a.nfoot) {
-        float r = (float)((k >> 2) + 1) * a.ep;
-        float ex = r * (float)(1 - 2 * ((k >> 1) & 1));
-        float ey = r * (float)(1 - 2 * (((k + 1) >> 1) & 1));
-        const int bx = iX * a.rp, by = iY * a.rp;
-        const float dt = a.dt;
-        float k1x, k1y, Dx, Dy;
-        velocity_st(a.psiA, sA, a.gp, bx, by, ex, ey, k1x, k1y);
-        if (TI == 10) {
-            Dx = dt * k1x;
-            Dy = dt * k1y;
-        } else if (TI == 21) {
-            float k2x, k2y;
-            velocity_st(a.psi0, s0, a.gp, bx, by, ex - dt * k1x, ey - dt * k1y, k2x, k2y);
-            Dx = dt * (k1x + k2x) * 0.5f;
-            Dy = dt * (k1y + k2y) * 0.5f;
-        } else {
-            float k2x, k2y, k3x, k3y;
-            velocity_st(a.psiB, sB, a.gp, bx, by, ex - 0.5f * dt * k1x, ey - 0.5f * dt * k1y, k2x, k2y);
-            velocity_st(a.psi0, s0, a.gp, bx, by, ex + dt * k1x - 2.0f * dt * k2x, ey + dt * k1y - 2.0f * dt * k2y,
-                        k3x, k3y);
-            Dx = dt * (k1x + 4.0f * k2x + k3x) * (1.0f / 6.0f);
-            Dy = dt * (k1y + 4.0f * k2y + k3y) * (1.0f / 6.0f);
-        }
-        float fx = ex - Dx, fy = ey - Dy;
-        float mx, my;
-        map_disp_st(a.map, sM, a.gm, iX, iY, fx, fy, n0.x, n0.y, mx, my);
-        gX = mx - Dx;
-        gY = my - Dy;
-    }
-    const int comp = k & 1, plane = (k >> 1) & 3;
-    float acc = 0.0f;
-    for (int kk = 0; kk < a.nfoot; ++kk) {
-        float vx = __shfl_sync(0xffffffffu, gX, kk, 8);
-        float vy = __shfl_sync(0xffffffffu, gY, kk, 8);
-        acc = fmaf(comp ? vy : vx, sc[plane][kk], acc);
-    }
-    if (plane == 0) acc += comp ? n0.y : n0.x;
-    reinterpret_cast<float*>(a.out)[8 * (long long)nd + k] = acc;
-}
-
-// ---------------------------------------------------------------------------
 // separable stream function psi = F(x) - h(v) (the Vlasov-Poisson potential):
 // characteristics in FP64.  The velocity u = (psi_y, -psi_x) = (-h'(v),
 // -F'(x)) is a pair of 1D cubic Hermite derivatives from FP64 tables
@@ -661,22 +526,6 @@ cudaError_t launch_advect_m(const AdvectMArgs& a, cudaStream_t s)
             default: return cudaErrorInvalidValue;
         }
         return cudaGetLastError();
-    }
-    const int ti = a.time_integration_num;
-    if ((ti == 10 || ti == 21 || ti == 30) && a.nfoot <= 8 && a.rp >= 1 && a.gm.NX % kTileNX == 0 &&
-        a.gm.NY % kTileNY == 0) {
-        // staged gathers (k_advect_ms) where the tile's copies fit the default shared memory
-        const int nf = ti == 10 ? 1 : (ti == 21 ? 2 : 3);
-        const long long pw = (long long)((kTileNX - 1) * a.rp + 2 * kPsiHalo + 2) * ((kTileNY - 1) * a.rp + 2 * kPsiHalo + 2);
-        const long long mw = 2ll * (kTileNX + 2 * kMapHalo + 1) * (kTileNY + 2 * kMapHalo + 1);
-        const size_t sm = sizeof(float4) * (size_t)(nf * pw + mw);
-        const long long tiles = (long long)(a.gm.NX / kTileNX) * (a.gm.NY / kTileNY);
-        if (sm <= 48 * 1024 && tiles < (1ll << 31)) {
-            if (ti == 10) k_advect_ms<10><<<(unsigned)tiles, 256, sm, s>>>(a);
-            else if (ti == 21) k_advect_ms<21><<<(unsigned)tiles, 256, sm, s>>>(a);
-            else k_advect_ms<30><<<(unsigned)tiles, 256, sm, s>>>(a);
-            return cudaGetLastError();
-        }
     }
     switch (a.time_integration_num) {
         case 10: k_advect_m<10><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
@@ -2025,21 +1874,10 @@ cudaError_t launch_ens(int kind, int TI, const EnsMember* mem, const int* cum, i
 }
 
 // ---------------------------------------------------------------------------
-// the fused psi solve of the mixed form (psi_solve.cuh): omega through the map on
-// the vorticity grid with k_sample_m4's arithmetic, the kept modes, the four psi
-// planes as FP32 nodes and, in the same pass, the Lagrange combinations of k_psi_nodes3
+// the psi solve of the mixed form on the library's FFT (psi_solve.cuh): omega through
+// the map on the vorticity grid (launch_sample_m), the kept modes, the four psi planes
+// as FP32 nodes and, in the same pass, the Lagrange combinations of k_psi_nodes3
 // ---------------------------------------------------------------------------
-struct SampleM4Src {
-    Grid gm, go, gf;
-    int rf;
-    const float4* map;
-    const float4* W;
-    __device__ __forceinline__ float value(int iX, int iY, bool) const
-    {
-        return sample_m4_value(gm, go, gf, rf, map, W, iX, iY);
-    }
-};
-
 struct NodesEpi {
     int nx;
     float4* out0;
@@ -2067,7 +1905,8 @@ struct NodesEpi {
 bool psi_solve_m_fits(const Grid& gm, const Grid& gv, const Grid& gp, double freq, const fft::Plan2D& pv,
                       const fft::Plan2D& pp, long long* w1_values, long long* w2_values)
 {
-    if (gv.NX != 4 * gm.NX || gv.NY != 4 * gm.NY || gv.NY > 65535) return false;
+    const int ro = gv.NX / gm.NX;
+    if (ro < 1 || ro > kMaxCheckRatio || ro * gm.NX != gv.NX || ro * gm.NY != gv.NY || gv.NY > 65535) return false;
     const psi::Layout L = psi::make_layout<float>(gv, gp, freq, pv, pp);
     if (!L.ok) return false;
     if (w1_values) *w1_values = L.w1_values;
@@ -2077,17 +1916,19 @@ bool psi_solve_m_fits(const Grid& gm, const Grid& gv, const Grid& gp, double fre
 
 void psi_solve_m_prepare()
 {
-    psi::prepare<float, SampleM4Src, NodesEpi>();
+    psi::prepare<float, NodesEpi>();
 }
 
 cudaError_t launch_psi_solve_m(const Grid& gm, const Grid& gv, const Grid& gf, const float4* map, const float4* W,
-                               const Grid& gp, double freq, const fft::Plan2D& pv, const fft::Plan2D& pp, float2* w1,
-                               float2* w2, float4* out0, const float4* l1, const float4* l2, const double* c1,
-                               const double* c2, const double* c3, float4* o1, float4* o2, float4* o3, cudaStream_t s)
+                               const Grid& gp, double freq, const fft::Plan2D& pv, const fft::Plan2D& pp, float* omega,
+                               float2* w1, float2* w2, float4* out0, const float4* l1, const float4* l2,
+                               const double* c1, const double* c2, const double* c3, float4* o1, float4* o2,
+                               float4* o3, cudaStream_t s)
 {
     if (!psi_solve_m_fits(gm, gv, gp, freq, pv, pp, nullptr, nullptr)) return cudaErrorInvalidValue;
     const psi::Layout L = psi::make_layout<float>(gv, gp, freq, pv, pp);
-    SampleM4Src src{gm, gv, gf, gf.NX / gv.NX, map, W};
+    cudaError_t e = launch_sample_m(gm, gv, gf, map, W, omega, nullptr, s);
+    if (e != cudaSuccess) return e;
     NodesEpi epi;
     epi.nx = gp.NX;
     epi.out0 = out0;
@@ -2098,7 +1939,7 @@ cudaError_t launch_psi_solve_m(const Grid& gm, const Grid& gv, const Grid& gf, c
         epi.cm.c[1][l] = c2 ? (float)c2[l] : 0.f;
         epi.cm.c[2][l] = c3 ? (float)c3[l] : 0.f;
     }
-    return psi::launch<float>(L, gv, gp, freq, pv, pp, w1, w2, src, epi, s);
+    return psi::launch<float>(L, gv, gp, freq, pv, pp, omega, w1, w2, epi, s);
 }
 
 }  // namespace cmm

@@ -1,6 +1,5 @@
-// psi_solve.cuh -- the psi solve of one time step as three fused kernels on the
-// library's FFT engine (fft.cuh), templated on the precision (FP64 plain form,
-// FP32 mixed form).
+// psi_solve.cuh -- the psi solve of one time step on the library's FFT engine
+// (fft.cuh), templated on the precision (FP64 plain form, FP32 mixed form).
 //
 // Reference: evaluate_stream_hermite (Cuda-CMM/src/simulation/cmm-simulation-host.cu:
 // 333-375): omega sampled through the map on the vorticity grid
@@ -8,22 +7,23 @@
 // grid, k_fft_cut_off_scale_h, k_fft_iLap_h (src/numerical/cmm-fft.cu:55-78,267-339), and
 // fourier_hermite (:398-429: the spectra of psi, d/dx, d/dy, d2/dxdy and four Z2D).
 //
-// Here:
-//   rows   (k_psi_rows)   one block per few vorticity-grid rows samples omega for the
-//                         whole row straight into shared memory, transforms the row and
-//                         writes only the columns kx the cut-off and the psi grid keep;
-//   cols   (k_psi_cols)   one block per (group of C kept columns, Hermite plane): the
-//                         column's forward transform over the vorticity grid, the
-//                         spectral steps (normalise, grid move, circular cut-off, inverse
-//                         Laplacian, the plane's derivative multiplier) and the inverse
-//                         column transform over the psi grid;
-//   inverse rows (k_psi_rows_inv)  one block per few psi rows: the row C2R of the four
-//                         planes (missing columns are zero) and an epilogue that writes
-//                         the Hermite nodes (and, in the mixed form, the Lagrange
-//                         combinations of the next step).
+// Here the sampled vorticity (its own full-occupancy kernel) goes through three passes:
+//   rows   (fft::rows_r2c)   the row R2C of every vorticity row, writing only the columns
+//                            kx the cut-off and the psi grid keep;
+//   cols   (k_psi_cols)      per (group of C kept columns, Hermite plane): the columns'
+//                            forward transform over the vorticity grid, the spectral steps
+//                            (normalise, grid move, circular cut-off, inverse Laplacian,
+//                            the plane's derivative multiplier) and the inverse column
+//                            transform over the psi grid;
+//   inverse rows (k_psi_rows_inv)  per few psi rows: the row C2R of the four planes
+//                            (missing columns are zero) and an epilogue that writes the
+//                            Hermite nodes (and, in the mixed form, the Lagrange
+//                            combinations of the next step).
 // Between them only the kept columns travel through global memory: at the metric's
 // sizes (vorticity 2048^2, psi 1024^2, cut-off 128) 2048 x 129 and 4 x 1024 x 129
-// complex values instead of the full half spectra.
+// complex values instead of the full half spectra.  The kernels are persistent (a block
+// copies its twiddle tables into shared memory once, then takes group after group) and
+// sized for occupancy: FP32 8 values per thread within 64 registers.
 #pragma once
 #include <algorithm>
 #include <cmath>
@@ -34,26 +34,26 @@
 namespace cmm {
 namespace psi {
 
-// block shapes: values per thread (VPT) and threads.  FP64 blocks hold 8 values per
-// thread (an FP64 radix-8 butterfly with its inputs fits the 128 registers of a 512-thread
-// block); FP32 blocks 16.  Every block holds up to 4096 complex values.
+// block shapes: values per thread (VPT, a template argument of the kernels) and the launch
+// bound (one block per SM at the bound gives 65536 / MAXT registers): FP32 4 values per
+// thread (8 for the longest lengths) within 64 registers, FP64 8 values within 128 (an FP64
+// radix-8 butterfly and its inputs)
 template <typename T> struct Shape;
-template <> struct Shape<float> { static constexpr int VPT = 16, ROWT = 256, COLC = 4; };
-template <> struct Shape<double> { static constexpr int VPT = 8, ROWT = 512, COLC = 2; };
-constexpr int kColThreads = 512;
-constexpr int kMaxValues = 4096;   // complex values a block transforms at once
+template <> struct Shape<float> { static constexpr int VPT = 4, VPT_LONG = 8, MAXT = 1024; };
+template <> struct Shape<double> { static constexpr int VPT = 8, VPT_LONG = 8, MAXT = 512; };
+constexpr int kBlockValues = 2048;   // values per group the launchers aim for
 
 struct ColsArgs {
     const void* w1;          // vorticity-grid row spectra: NYv rows, columns 0..kv-1, row stride ld1
     void* w2;                // the four psi-grid spectra: 4 x NYp rows, columns 0..ncols-1, row stride ld2
     long long ld1, ld2;
     int kv, ncols;
-    int C;                   // columns per block (32-byte row segments where they fit)
+    int C;                   // columns per group
     Grid gv, gp;
     double freq;
     fft::RadixPlan Pv, Pp;   // column lengths NYv, NYp
-    const void* twv;         // NYv entries exp(-2 pi i t / NYv)
-    const void* twp;         // NYp entries
+    const void* twv;         // the NYv column plan's pass twiddles
+    const void* twp;         // the NYp column plan's pass twiddles
 };
 
 // psi spectrum of plane q (0: psi, 1: d/dx, 2: d/dy, 3: d2/dxdy) at psi-grid column iXc, row
@@ -116,80 +116,42 @@ __device__ __forceinline__ float2 plane_mode<float2>(const float2* s, int off, i
     return q == 2 ? Py : make_float2(-Py.y * kx, Py.x * kx);
 }
 
-// grid (ceil(ncols / C), 4 planes); dynamic shared memory: padded(C NYv) + padded(C NYp) values
-template <typename T, int FAM>
-__global__ void __launch_bounds__(kColThreads, 1) k_psi_cols(ColsArgs a)
+// groups (C kept columns, plane q) grid-strided; dynamic shared memory: padded(C NYv) +
+// padded(C NYp) values + the two column plans' tables
+template <typename T, int FAM, int VPT>
+__global__ void __launch_bounds__(Shape<T>::MAXT, 1) k_psi_cols(ColsArgs a)
 {
     using V = typename fft::Cx<T>::V;
-    constexpr int VPT = Shape<T>::VPT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nv = a.gv.NY, np = a.gp.NY, C = a.C;
     V* A = reinterpret_cast<V*>(smem_raw);
     V* B = A + fft::padded_len<V>(C * nv);
-    const int col0 = blockIdx.x * C, q = blockIdx.y;
+    V* tv = B + fft::padded_len<V>(C * np);
+    V* tp = tv + a.Pv.tlen;
+    fft::load_table(tv, reinterpret_cast<const V*>(a.twv), a.Pv.tlen);
+    fft::load_table(tp, reinterpret_cast<const V*>(a.twp), a.Pp.tlen);
     const V* w1 = reinterpret_cast<const V*>(a.w1);
-    for (int e = threadIdx.x; e < C * nv; e += blockDim.x) {
-        const int c = e % C, r = e / C, col = col0 + c;
-        A[fft::pad<V>(c * nv + r)] = col < a.kv ? w1[r * a.ld1 + col] : fft::mk((T)0, (T)0);
-    }
-    __syncthreads();
-    fft::block_fft<VPT, FAM>(A, C, a.Pv, reinterpret_cast<const V*>(a.twv), 1, false);
-    for (int e = threadIdx.x; e < C * np; e += blockDim.x) {
-        const int c = e / np, r = e - c * np;
-        B[fft::pad<V>(e)] = plane_mode<V>(A, c * nv, q, col0 + c, r, a.gv, a.gp, a.freq);
-    }
-    __syncthreads();
-    fft::block_fft<VPT, FAM>(B, C, a.Pp, reinterpret_cast<const V*>(a.twp), 1, true);
-    V* w2 = reinterpret_cast<V*>(a.w2) + (long long)q * np * a.ld2;
-    for (int e = threadIdx.x; e < C * np; e += blockDim.x) {
-        const int c = e % C, r = e / C, col = col0 + c;
-        if (col < a.ncols) w2[r * a.ld2 + col] = B[fft::pad<V>(c * np + r)];
-    }
-}
-
-// ---------------------------------------------------------------- forward rows
-struct RowsArgs {
-    void* w1;                // output: row stride ld1, columns 0..kv-1
-    long long ld1;
-    int kv;
-    int nx, ny;              // vorticity grid
-    int nb;                  // rows per block
-    fft::RadixPlan P;        // packed length nx/2
-    const void* tw;          // nx entries
-};
-
-// Src::value(iX, iY, live) -> T: omega at vort node (iX, iY); every thread of a warp calls it
-// together (samplers may exchange values between lanes); `live` false for padding lanes
-template <typename T, int FAM, class Src>
-__global__ void __launch_bounds__(Shape<T>::ROWT, 1) k_psi_rows(RowsArgs a, Src src)
-{
-    using V = typename fft::Cx<T>::V;
-    constexpr int VPT = Shape<T>::VPT;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    V* s = reinterpret_cast<V*>(smem_raw);
-    T* sr = reinterpret_cast<T*>(smem_raw);
-    const int n = a.nx / 2;
-    const int row0 = blockIdx.x * a.nb;
-    const int nb = min(a.nb, a.ny - row0);
-    const int total = nb * a.nx;
-    const int iters = (a.nb * a.nx + blockDim.x - 1) / blockDim.x;
-    for (int j = 0; j < iters; ++j) {
-        const int e = threadIdx.x + j * blockDim.x;
-        const bool live = e < total;
-        const int ee = live ? e : total - 1;
-        const int b = ee / a.nx, iX = ee - b * a.nx;
-        const T v = src.value(iX, row0 + b, live);
-        if (live) {
-            const int m = b * n + (iX >> 1);
-            sr[2 * fft::pad<V>(m) + (iX & 1)] = v;
+    const int gx = (a.ncols + C - 1) / C;
+    for (int grp = blockIdx.x; grp < 4 * gx; grp += gridDim.x) {
+        const int q = grp / gx, col0 = (grp - q * gx) * C;
+        __syncthreads();   // tables in place, the previous group's outputs read
+        for (int e = threadIdx.x; e < C * nv; e += blockDim.x) {
+            const int c = e % C, r = e / C, col = col0 + c;
+            A[fft::pad<V>(c * nv + r)] = col < a.kv ? w1[r * a.ld1 + col] : fft::mk((T)0, (T)0);
         }
-    }
-    __syncthreads();
-    fft::block_fft<VPT, FAM>(s, nb, a.P, reinterpret_cast<const V*>(a.tw), 2, false);
-    V* w1 = reinterpret_cast<V*>(a.w1);
-    for (int e = threadIdx.x; e < nb * a.kv; e += blockDim.x) {
-        const int b = e / a.kv, k = e - b * a.kv;
-        w1[(row0 + b) * a.ld1 + k] = fft::r2c_bin(s, b * n, n, k, reinterpret_cast<const V*>(a.tw));
+        __syncthreads();
+        fft::block_fft<VPT, FAM>(A, C, a.Pv, tv, false);
+        for (int e = threadIdx.x; e < C * np; e += blockDim.x) {
+            const int c = e / np, r = e - c * np;
+            B[fft::pad<V>(e)] = plane_mode<V>(A, c * nv, q, col0 + c, r, a.gv, a.gp, a.freq);
+        }
+        __syncthreads();
+        fft::block_fft<VPT, FAM>(B, C, a.Pp, tp, true);
+        V* w2 = reinterpret_cast<V*>(a.w2) + (long long)q * np * a.ld2;
+        for (int e = threadIdx.x; e < C * np; e += blockDim.x) {
+            const int c = e % C, r = e / C, col = col0 + c;
+            if (col < a.ncols) w2[r * a.ld2 + col] = B[fft::pad<V>(c * np + r)];
+        }
     }
 }
 
@@ -199,42 +161,50 @@ struct RowsInvArgs {
     long long ld2;
     int kin;
     int nx, ny;              // psi grid
-    int nb;                  // rows per block
+    int nb;                  // rows per group
     fft::RadixPlan P;        // packed length nx/2
-    const void* tw;          // nx entries
+    const void* tw;          // the row plan's pass twiddles, then W^k for k <= nx/2
 };
 
-// Epi::store(iX, iY, f, fx, fy, fxy): the four Hermite planes' values at psi node (iX, iY)
-template <typename T, int FAM, class Epi>
-__global__ void __launch_bounds__(Shape<T>::ROWT, 1) k_psi_rows_inv(RowsInvArgs a, Epi epi)
+// Epi::store(iX, iY, f, fx, fy, fxy): the four Hermite planes' values at psi node (iX, iY);
+// groups of nb rows grid-strided; dynamic shared memory: padded(4 nb nx/2) values + the
+// row plan's table
+template <typename T, int FAM, int VPT, class Epi>
+__global__ void __launch_bounds__(Shape<T>::MAXT, 1) k_psi_rows_inv(RowsInvArgs a, Epi epi)
 {
     using V = typename fft::Cx<T>::V;
-    constexpr int VPT = Shape<T>::VPT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = a.nx / 2;
     V* s = reinterpret_cast<V*>(smem_raw);
     const T* sr = reinterpret_cast<const T*>(smem_raw);
-    const V* tw = reinterpret_cast<const V*>(a.tw);
-    const int n = a.nx / 2;
-    const int row0 = blockIdx.x * a.nb;
-    const int nb = min(a.nb, a.ny - row0);
+    V* tw = s + fft::padded_len<V>(4 * a.nb * n);
+    fft::load_table(tw, reinterpret_cast<const V*>(a.tw), a.P.tlen + n + 1);
+    const V* post = tw + a.P.tlen;
     const V zero = fft::mk((T)0, (T)0);
     const V* w2 = reinterpret_cast<const V*>(a.w2);
-    // transform t = 4 b + q: plane q of row row0 + b
-    for (int e = threadIdx.x; e < 4 * nb * n; e += blockDim.x) {
-        const int t = e / n, k = e - t * n, b = t >> 2, q = t & 3;
-        const V* src = w2 + ((long long)q * a.ny + row0 + b) * a.ld2;
-        V xk = k < a.kin ? src[k] : zero;
-        V xn = n - k < a.kin ? src[n - k] : zero;
-        if (k == 0) { xk.y = (T)0; xn.y = (T)0; }
-        s[fft::pad<V>(e)] = fft::c2r_pack(xk, xn, k, tw);
-    }
-    __syncthreads();
-    fft::block_fft<VPT, FAM>(s, 4 * nb, a.P, tw, 2, true);
-    for (int e = threadIdx.x; e < nb * a.nx; e += blockDim.x) {
-        const int b = e / a.nx, iX = e - b * a.nx;
-        const int base = 4 * b * n + (iX >> 1), c = iX & 1;
-        epi.store(iX, row0 + b, sr[2 * fft::pad<V>(base) + c], sr[2 * fft::pad<V>(base + n) + c],
-                  sr[2 * fft::pad<V>(base + 2 * n) + c], sr[2 * fft::pad<V>(base + 3 * n) + c]);
+    for (int row0 = blockIdx.x * a.nb; row0 < a.ny; row0 += gridDim.x * a.nb) {
+        const int nb = min(a.nb, a.ny - row0);
+        __syncthreads();
+        // transform t = 4 b + q: plane q of row row0 + b
+        for (int t = 0; t < 4 * nb; ++t) {
+            const int b = t >> 2, q = t & 3;
+            const V* src = w2 + ((long long)q * a.ny + row0 + b) * a.ld2;
+            for (int k = threadIdx.x; k < n; k += blockDim.x) {
+                V xk = k < a.kin ? src[k] : zero;
+                V xn = n - k < a.kin ? src[n - k] : zero;
+                if (k == 0) { xk.y = (T)0; xn.y = (T)0; }
+                s[fft::pad<V>(t * n + k)] = fft::c2r_pack(xk, xn, k, post);
+            }
+        }
+        __syncthreads();
+        fft::block_fft<VPT, FAM>(s, 4 * nb, a.P, tw, true);
+        for (int b = 0; b < nb; ++b) {
+            for (int iX = threadIdx.x; iX < a.nx; iX += blockDim.x) {
+                const int base = 4 * b * n + (iX >> 1), c = iX & 1;
+                epi.store(iX, row0 + b, sr[2 * fft::pad<V>(base) + c], sr[2 * fft::pad<V>(base + n) + c],
+                          sr[2 * fft::pad<V>(base + 2 * n) + c], sr[2 * fft::pad<V>(base + 3 * n) + c]);
+            }
+        }
     }
 }
 
@@ -245,15 +215,16 @@ namespace cmm {
 namespace psi {
 
 // ---------------------------------------------------------------- host side
-// the shape of one fused solve, or ok = false when the sizes need the unfused path
+// the shape of one solve on these kernels, or ok = false when the sizes need the 2D path
 struct Layout {
     bool ok = false;
     int fam = 0;
     int ncols = 0;           // psi-grid columns kept: 0 .. min(NXp/2, freq)
     int kv = 0;              // vorticity-row bins written: 0 .. min(NXv/2, ncols - 1)
     long long ld = 0;        // row stride of both intermediate arrays (complex values)
-    int nb_rows = 0, nb_inv = 0, C = 0;
-    size_t smem_rows = 0, smem_cols = 0, smem_inv = 0;
+    int nb_inv = 0, C = 0;   // psi rows per inverse-row group, columns per column group
+    int vpt = 0;             // values per thread of both kernels
+    size_t smem_cols = 0, smem_inv = 0;
     long long w1_values = 0, w2_values = 0;   // complex values of the intermediate arrays
 };
 
@@ -273,68 +244,82 @@ Layout make_layout(const Grid& gv, const Grid& gp, double freq, const fft::Plan2
     if (L.ncols < 1) return L;
     L.kv = std::min(gv.NX / 2, L.ncols - 1) + 1;
     L.ld = (L.ncols + 3) / 4 * 4;
-    const int cap = Shape<T>::VPT * Shape<T>::ROWT;   // values one row block transforms
-    const int nv = gv.NX / 2, np = gp.NX / 2;
-    if (nv > cap || 4 * np > cap) return L;
-    L.nb_rows = std::max(1, std::min(kMaxValues, cap) / nv);
-    L.nb_inv = std::max(1, std::min(kMaxValues, cap) / (4 * np));
-    L.C = Shape<T>::COLC;
-    const int ccap = Shape<T>::VPT * kColThreads;
-    auto col_smem = [&](int C) {
-        return sizeof(V) * ((size_t)fft::padded_len<V>(C * gv.NY) + (size_t)fft::padded_len<V>(C * gp.NY));
-    };
-    while (L.C > 1 && (L.C * std::max(gv.NY, gp.NY) > ccap || col_smem(L.C) > 200 * 1024)) L.C /= 2;
-    if (L.C * std::max(gv.NY, gp.NY) > ccap || col_smem(L.C) > 200 * 1024) return L;
-    L.smem_rows = sizeof(V) * (size_t)fft::padded_len<V>(L.nb_rows * nv);
-    L.smem_inv = sizeof(V) * (size_t)fft::padded_len<V>(4 * L.nb_inv * np);
-    L.smem_cols = col_smem(L.C);
+    const int np = gp.NX / 2;
+    const int need = std::max(4 * np, std::max(gv.NY, gp.NY));   // values of the largest group
+    L.vpt = need <= Shape<T>::VPT * Shape<T>::MAXT ? Shape<T>::VPT : Shape<T>::VPT_LONG;
+    if (need > L.vpt * Shape<T>::MAXT) return L;
+    L.nb_inv = std::max(1, kBlockValues / (4 * np));
+    L.C = 1;
+    while (2 * L.C * std::max(gv.NY, gp.NY) <= kBlockValues && L.C < 4) L.C *= 2;
+    L.smem_inv = sizeof(V) * ((size_t)fft::padded_len<V>(4 * L.nb_inv * np) + (size_t)pp.rx.tlen + (size_t)np + 1);
+    L.smem_cols = sizeof(V) * ((size_t)fft::padded_len<V>(L.C * gv.NY) + (size_t)fft::padded_len<V>(L.C * gp.NY) +
+                               (size_t)pv.ry.tlen + (size_t)pp.ry.tlen);
+    if (L.smem_cols > 200 * 1024 || L.smem_inv > 200 * 1024) return L;
     L.w1_values = (long long)gv.NY * L.ld;
     L.w2_values = 4ll * gp.NY * L.ld;
     L.ok = true;
     return L;
 }
 
-template <typename T, int FAM, class Src, class Epi>
+template <typename T, int FAM, int VPT, class Epi>
 void set_smem_limits()
 {
-    cudaFuncSetAttribute(k_psi_rows<T, FAM, Src>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_psi_cols<T, FAM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_psi_rows_inv<T, FAM, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_psi_cols<T, FAM, VPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_psi_rows_inv<T, FAM, VPT, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 }
 
 // raise the kernels' shared-memory limits (before any stream capture)
-template <typename T, class Src, class Epi>
+template <typename T, class Epi>
 void prepare()
 {
-    set_smem_limits<T, fft::kPow2, Src, Epi>();
-    set_smem_limits<T, fft::kPow2x3, Src, Epi>();
+    set_smem_limits<T, fft::kPow2, Shape<T>::VPT, Epi>();
+    set_smem_limits<T, fft::kPow2x3, Shape<T>::VPT, Epi>();
+    set_smem_limits<T, fft::kPow2, Shape<T>::VPT_LONG, Epi>();
+    set_smem_limits<T, fft::kPow2x3, Shape<T>::VPT_LONG, Epi>();
 }
 
-template <typename T, int FAM, class Src, class Epi>
-cudaError_t launch_fam(const Layout& L, const Grid& gv, const Grid& gp, double freq, const fft::Plan2D& pv,
-                       const fft::Plan2D& pp, void* w1, void* w2, const Src& src, const Epi& epi, cudaStream_t s)
+inline int threads_for(int values, int vpt)
 {
-    RowsArgs r;
-    r.w1 = w1; r.ld1 = L.ld; r.kv = L.kv; r.nx = gv.NX; r.ny = gv.NY; r.nb = L.nb_rows; r.P = pv.rx; r.tw = pv.twx;
-    k_psi_rows<T, FAM, Src><<<(unsigned)((gv.NY + L.nb_rows - 1) / L.nb_rows), Shape<T>::ROWT, L.smem_rows, s>>>(r, src);
+    int t = (values + vpt - 1) / vpt;
+    t = (t + 31) / 32 * 32;
+    return t < 32 ? 32 : t;
+}
+
+template <typename T, int FAM, int VPT, class Epi>
+cudaError_t launch_fam(const Layout& L, const Grid& gv, const Grid& gp, double freq, const fft::Plan2D& pv,
+                       const fft::Plan2D& pp, const void* omega, void* w1, void* w2, const Epi& epi, cudaStream_t s)
+{
+    cudaError_t e = fft::rows_r2c(pv, omega, gv.NX, gv.N, w1, L.ld, L.w1_values, gv.NY, 1, L.kv, s);
+    if (e != cudaSuccess) return e;
     ColsArgs c;
     c.w1 = w1; c.w2 = w2; c.ld1 = L.ld; c.ld2 = L.ld; c.kv = L.kv; c.ncols = L.ncols; c.C = L.C;
     c.gv = gv; c.gp = gp; c.freq = freq; c.Pv = pv.ry; c.Pp = pp.ry; c.twv = pv.twy; c.twp = pp.twy;
-    k_psi_cols<T, FAM><<<dim3((unsigned)((L.ncols + L.C - 1) / L.C), 4), kColThreads, L.smem_cols, s>>>(c);
+    const int tc = threads_for(L.C * std::max(gv.NY, gp.NY), VPT);
+    const long long gc = 4ll * ((L.ncols + L.C - 1) / L.C);
+    k_psi_cols<T, FAM, VPT><<<fft::resident_grid(reinterpret_cast<const void*>(k_psi_cols<T, FAM, VPT>), tc, L.smem_cols,
+                                                 gc), tc, L.smem_cols, s>>>(c);
     RowsInvArgs v;
     v.w2 = w2; v.ld2 = L.ld; v.kin = L.ncols; v.nx = gp.NX; v.ny = gp.NY; v.nb = L.nb_inv; v.P = pp.rx; v.tw = pp.twx;
-    k_psi_rows_inv<T, FAM, Epi><<<(unsigned)((gp.NY + L.nb_inv - 1) / L.nb_inv), Shape<T>::ROWT, L.smem_inv, s>>>(v, epi);
+    const int ti = threads_for(4 * L.nb_inv * (gp.NX / 2), VPT);
+    const long long gi = (gp.NY + L.nb_inv - 1) / L.nb_inv;
+    k_psi_rows_inv<T, FAM, VPT, Epi><<<fft::resident_grid(reinterpret_cast<const void*>(k_psi_rows_inv<T, FAM, VPT, Epi>),
+                                                          ti, L.smem_inv, gi), ti, L.smem_inv, s>>>(v, epi);
     return cudaGetLastError();
 }
 
-// the three kernels of one psi solve (3 launches); w1, w2 hold L.w1_values, L.w2_values
-template <typename T, class Src, class Epi>
+// the three transform passes of one psi solve from the sampled vorticity omega (gv rows,
+// FP32 or FP64); w1, w2 hold L.w1_values, L.w2_values complex values
+template <typename T, class Epi>
 cudaError_t launch(const Layout& L, const Grid& gv, const Grid& gp, double freq, const fft::Plan2D& pv,
-                   const fft::Plan2D& pp, void* w1, void* w2, const Src& src, const Epi& epi, cudaStream_t s)
+                   const fft::Plan2D& pp, const void* omega, void* w1, void* w2, const Epi& epi, cudaStream_t s)
 {
     if (!L.ok) return cudaErrorInvalidValue;
-    if (L.fam == fft::kPow2) return launch_fam<T, fft::kPow2>(L, gv, gp, freq, pv, pp, w1, w2, src, epi, s);
-    return launch_fam<T, fft::kPow2x3>(L, gv, gp, freq, pv, pp, w1, w2, src, epi, s);
+    constexpr int A = Shape<T>::VPT, B = Shape<T>::VPT_LONG;
+    if (L.fam == fft::kPow2)
+        return L.vpt == A ? launch_fam<T, fft::kPow2, A>(L, gv, gp, freq, pv, pp, omega, w1, w2, epi, s)
+                          : launch_fam<T, fft::kPow2, B>(L, gv, gp, freq, pv, pp, omega, w1, w2, epi, s);
+    return L.vpt == A ? launch_fam<T, fft::kPow2x3, A>(L, gv, gp, freq, pv, pp, omega, w1, w2, epi, s)
+                      : launch_fam<T, fft::kPow2x3, B>(L, gv, gp, freq, pv, pp, omega, w1, w2, epi, s);
 }
 
 }  // namespace psi

@@ -340,8 +340,9 @@ int EulerSim::alloc()
         if (!vlasov_) vcols_ = std::min(gv.NX_fft, (int)std::floor(s.freq_cut_psi) + 1);
     }
     if (!vlasov_) {
-        // the psi solve as three fused kernels where the sizes allow it (else sample, transform,
-        // spectral step, inverse transforms and node pass one after another)
+        // the psi solve as four kernels (sample, kept row modes, column transforms with the
+        // spectral step, inverse rows with the node pass) where the sizes allow it, else
+        // sample, 2D transform, spectral step, 2D inverse transforms and node pass
         long long n1 = 0, n2 = 0;
         psi_fused_ = mixed_ ? psi_solve_m_fits(gc, gv, gp, s.freq_cut_psi, fv_, fp_, &n1, &n2)
                             : psi_solve_fits(gv, gp, s.freq_cut_psi, pv_.p, pp_.p, &n1, &n2);
@@ -465,12 +466,12 @@ int EulerSim::evaluate_stream()
             int rc = learned_stream();
             if (rc) return rc;
         } else if (psi_fused_) {
-            // sample, transforms, spectral step and node pass in three kernels; with three
+            // sample, transforms, spectral step and node pass in four kernels; with three
             // Lagrange levels the node pass also writes the combinations below
             const bool combos = psi_lcl_ >= 0 && L == 3;
             fused_ = false;
             if (combos) predict_combinations();
-            CMM_LAUNCH(3, launch_psi_solve_m(gc, gv, gf, mapm_, wfm_, gp, s.freq_cut_psi, fv_, fp_,
+            CMM_LAUNCH(4, launch_psi_solve_m(gc, gv, gf, mapm_, wfm_, gp, s.freq_cut_psi, fv_, fp_, realf_,
                                              static_cast<float2*>(psw1_), static_cast<float2*>(psw2_), psim_[0],
                                              psim_[1], psim_[2], combos ? fusedLp_ : nullptr, fusedL1_, fusedL12_,
                                              psiP_, psiA_, psiB_, stream));
@@ -497,8 +498,9 @@ int EulerSim::evaluate_stream()
         return kOk;
     }
     if (psi_fused_) {
-        CMM_LAUNCH(3, launch_psi_solve(gc, gv, gf, ChiX, ChiY, wfine, s.molly_stencil, gp, s.freq_cut_psi, pv_.p, pp_.p,
-                                       static_cast<double2*>(psw1_), static_cast<double2*>(psw2_), psi[0], stream));
+        CMM_LAUNCH(4, launch_psi_solve(gc, gv, gf, ChiX, ChiY, wfine, s.molly_stencil, gp, s.freq_cut_psi, pv_.p, pp_.p,
+                                       real_buf_, static_cast<double2*>(psw1_), static_cast<double2*>(psw2_), psi[0],
+                                       stream));
         return kOk;
     }
     CMM_LAUNCH(1, launch_sample_vort(gc, gv, gf, ChiX, ChiY, wfine, s.molly_stencil, real_buf_, gv.NX, stream));

@@ -271,7 +271,7 @@ private:
     float2* spec4f_ = nullptr;       // 4 FP32 spectra
     fft::Plan2D fv_, fp_, ff_;   // FP32 transforms of the vort, psi and fine grids (mixed form)
     int vcols_ = 0;              // columns kx <= freq_cut_psi the psi solve keeps
-    bool psi_fused_ = false;     // the psi solve runs as the three fused kernels (psi_solve.cuh)
+    bool psi_fused_ = false;     // the psi solve runs on the kept-column kernels of psi_solve.cuh
     void* psw1_ = nullptr;       // their work arrays (kept columns of omega's and psi's spectra)
     void* psw2_ = nullptr;
     bool prof_ = false;

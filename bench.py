@@ -146,7 +146,11 @@ FP64_PEAK_TFLOPS = 1.10   # GB300 FP64 rate: `python bench.py --fp64-peak` (cuBL
 # ncu capture of the workload (profiles/k_particles_m_c2.md, k_advect_fp64_c2.md)
 # DRAM bytes (read + write) per launch of the roofline kernel, from the committed ncu
 # captures (profiles/k_advect_m_c2.md, profiles/k_advect_fp64_c2.md)
-NCU_TRAFFIC = {("mixed", "advect"): 58.74e6 + 1.05e6, ("fp64", "advect"): 127.4e6}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the roofline kernel,
+# from one ncu capture of the same kernel on this workload; the file named beside each figure
+# holds the command and the raw numbers
+NCU_TRAFFIC = {("mixed", "advect"): (58.74e6 + 1.05e6, "profiles/mixed_step_kernels_c2.md"),
+               ("fp64", "advect"): (127.4e6, "profiles/k_advect_fp64_c2.md")}
 
 
 def measure_fp64_peak():
@@ -792,18 +796,20 @@ def _report(args, world, rank, chosen, plain, clocks, e2e_line, ic):
     # the coarse vorticity is sampled only when read (not per step) in the 2D Euler form
     per.pop("coarse", None)
     # the roofline kernel: the single-kernel phase (advection, incompressibility check,
-    # tracers) with the largest measured time; the psi phase (sample, two cuFFT passes, the
-    # spectral step, the inverse cuFFT and the node pass) is reported in the breakdown
+    # tracers) with the largest measured time; the psi phase (sample, row transform, column
+    # transforms with the spectral step, inverse rows with the node pass) is reported in the
+    # breakdown with its own HBM fraction
     single = [k for k in ("advect", "incomp", "particles") if k in per and k in models]
     dom = max(single, key=lambda k: per[k])
     ms = per[dom]
     achieved = models[dom] / (ms / 1000.0) / 1e9
     kernels = {"advect": "k_advect (GALS map advection)", "incomp": "k_incomp (det grad X, max)",
-               "psi": "psi solve (k_sample + FFT + k_spec_psi)", "coarse": "k_sample (coarse omega)",
+               "psi": "psi solve (k_sample + k_rows_r2c + k_psi_cols + k_psi_rows_inv)", "coarse": "k_sample (coarse omega)",
                "particles": "k_particles (RK3 tracers)"}
     roof = {"kernel": kernels.get(dom, dom), "phase": dom, "bound": "hbm", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "peak_source": "of " + peak_kind,
-            "traffic": NCU_TRAFFIC.get((args.precision, dom)),
+            "traffic": NCU_TRAFFIC.get((args.precision, dom), (None, None))[0],
+            "traffic_source": NCU_TRAFFIC.get((args.precision, dom), (None, None))[1],
             "ms_per_launch": ms, "algorithmic_bytes": models[dom],
             "phases": {k: {"ms": per[k], "GBps": models[k] / (per[k] / 1000.0) / 1e9,
                            "frac": models[k] / (per[k] / 1000.0) / 1e9 / peak} for k in per if k in models}}

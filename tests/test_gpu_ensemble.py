@@ -2,7 +2,7 @@
 
 Each member of an ensemble runs the single-member kernels' device bodies on its own
 descriptor, and the psi solve transforms every member of a size class in one batched
-cuFFT call.  The batched kernels are separate instantiations of those bodies (their
+transform (the library's FFT).  The batched kernels are separate instantiations of those bodies (their
 arguments come from shared memory rather than the parameter space), so the compiler
 may contract and share FP32 products differently: a member agrees with its single run
 to FP32 rounding, not bit for bit (one step moves the map's cross-derivative plane, whose

@@ -121,7 +121,7 @@ def _net_case(blocks, seed, B=2, h=8, w=128):
 @pytest.mark.parametrize("blocks,cut", [(1, 0), (2, 0), (1, 5), (2, 3)])
 def test_network_loss_and_gradient_match_oracle(blocks, cut):
     """cut 0: mean squared error; cut > 0: the psi-space spectral loss of training (batched
-    cuFFT on the GPU, a direct DFT in the oracle)."""
+    transforms on the GPU, a direct DFT in the oracle)."""
     u, p, s_in, inputs, targets, layers = _net_case(blocks, 11 + blocks + cut)
     loss = u.loss_grad(inputs, targets, cut=cut)
     g = u.grads().astype(np.float64)

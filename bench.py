@@ -509,21 +509,32 @@ def run_ensemble(args):
         return time.perf_counter() - t0, a.elapsed_time(b) / 1e3
 
     res = {}
-    for graphs in ((True,) if args.ensemble_batched_only else (True, False)):
+    # (graphs, fused): the single-launch iteration (graph replay, then plain launches) and the
+    # two-phase iteration with its graphs
+    # (graphs, form): the autotuned form (the headline), the single launch alone and the two-phase
+    # iteration with host remaps (the earlier form), each with its CUDA graphs
+    variants = ((True, None),) if args.ensemble_batched_only else ((True, None), (True, True), (True, False))
+    for graphs, fused in variants:
         ens = m.Ensemble([ensemble_args(work, i, n) for i, (n, _) in enumerate(members)],
-                         stream=stream.cuda_stream, graphs=graphs)
+                         stream=stream.cuda_stream, graphs=graphs, fused=fused)
         for i, w in enumerate(ics):
             ens.set_initial_discrete(i, w)
         init_wall, _ = timed(ens.init)
         wall, dev = timed(ens.run)
         st = ens.stats()
-        res[graphs] = dict(st, init_s=init_wall, wall_s=wall, device_s=dev,
-                           member_steps_per_s=st["member_steps"] / wall,
-                           diag=[(ens.scalar(i, "energy"), ens.scalar(i, "enstrophy"),
-                                  int(ens.scalar(i, "map_counter"))) for i in range(len(members))])
+        info = ens.fused_info()
+        res[(graphs, fused)] = dict(st, init_s=init_wall, wall_s=wall, device_s=dev,
+                                    member_steps_per_s=st["member_steps"] / wall,
+                                    form="single launch" if info["fused"] else "two-phase",
+                                    register_budget=info["register_budget"],
+                                    fused_blocks=info["blocks"],
+                                    tiles_per_task=info["tiles_per_task"], why=info["why"],
+                                    tuning=[list(r) for r in ens.tuning()],
+                                    diag=[(ens.scalar(i, "energy"), ens.scalar(i, "enstrophy"),
+                                           int(ens.scalar(i, "map_counter"))) for i in range(len(members))])
         ens.close()
     if args.ensemble_batched_only:
-        b = res[True]
+        b = res[(True, None)]
         print(json.dumps({"batched_graphs": {k: v for k, v in b.items() if k != "diag"}}))
         return
     seq = {"mixed": dict(member_steps=0, wall_s=0.0, diag=[]), "fp64": dict(member_steps=0, wall_s=0.0, diag=[])}
@@ -541,17 +552,24 @@ def run_ensemble(args):
             seq[prec]["wall_s"] += wall
             seq[prec]["diag"].append((sim.scalar("energy"), sim.scalar("enstrophy"), int(sim.scalar("map_counter"))))
             sim.close()
-    b, plain = res[True], seq["fp64"]
+    b, plain = res[(True, None)], seq["fp64"]
     rel = [(abs(x[0] - y[0]) / abs(y[0]), abs(x[1] - y[1]) / abs(y[1])) for x, y in zip(b["diag"], plain["diag"])]
     counts = {str(s): sum(1 for n, _ in members if n == s) for s in ENSEMBLE["sizes"]}
     out = {"validation": "64-member ensemble of uneven sizes, batched vs one after another, vs plain FP64",
            "workload": "euler2d-ensemble 64 members N in {64,96,128,192,256} (mt19937_64 seed 0), fine 4N, psi 2N, "
                        "dt 1/(N/2), T=5, k0~U[4,16], remap 1e-3",
            "sizes": counts, "unit": "member-steps/s",
-           "batched_graphs": {k: b[k] for k in ("member_steps", "iterations", "launches", "advect_blocks",
-                                                "sample_blocks", "init_s", "wall_s", "device_s",
-                                                "member_steps_per_s")},
-           "batched_no_graphs": {k: res[False][k] for k in ("wall_s", "member_steps_per_s")},
+           "batched_graphs": {k: b[k] for k in ("member_steps", "iterations", "launches", "form", "register_budget",
+                                                "fused_blocks", "tiles_per_task", "tuning", "init_s", "wall_s",
+                                                "device_s", "member_steps_per_s")},
+           "single_launch_graphs": {k: res[(True, True)][k] for k in ("launches", "register_budget", "fused_blocks",
+                                                                      "tiles_per_task", "wall_s", "device_s",
+                                                                      "member_steps_per_s")},
+           "two_phase_host_remaps_graphs": {k: res[(True, False)][k] for k in ("launches", "advect_blocks",
+                                                                               "sample_blocks", "wall_s", "device_s",
+                                                                               "member_steps_per_s")},
+           "single_launch_equals_two_phase_maps": sum(1 for x, y in zip(res[(True, True)]["diag"],
+                                                                        res[(True, False)]["diag"]) if x[2] == y[2]),
            "sequential_mixed": {"member_steps": seq["mixed"]["member_steps"], "wall_s": seq["mixed"]["wall_s"],
                                 "member_steps_per_s": seq["mixed"]["member_steps"] / seq["mixed"]["wall_s"]},
            "sequential_fp64": {"member_steps": plain["member_steps"], "wall_s": plain["wall_s"],

@@ -21,6 +21,7 @@ CMM_ERR_SATURATED = -4
 CMM_ERR_STATE = -5
 CMM_ERR_UNSUPPORTED = -6
 CMM_ERR_NOT_FOUND = -7
+CMM_ERR_TIMEOUT = -8
 
 # every entry point declared in include/cmm_abi.h
 EXPORTS = [
@@ -33,6 +34,8 @@ EXPORTS = [
     "cmm_vlasov_diagnostics", "cmm_vlasov_destroy", "cmm_ensemble_create", "cmm_ensemble_set_initial_discrete",
     "cmm_ensemble_set_graphs", "cmm_ensemble_init", "cmm_ensemble_step", "cmm_ensemble_run",
     "cmm_ensemble_get_scalar", "cmm_ensemble_get_field", "cmm_ensemble_field_bytes", "cmm_ensemble_stats",
+    "cmm_ensemble_set_fused", "cmm_ensemble_set_wait_limit", "cmm_ensemble_fused_info", "cmm_ensemble_tuning",
+    "cmm_ensemble_set_profiling", "cmm_ensemble_profile",
     "cmm_ensemble_destroy", "cmm_upsampler_create", "cmm_upsampler_destroy", "cmm_upsampler_num_params",
     "cmm_upsampler_get_params", "cmm_upsampler_set_params", "cmm_upsampler_get_grads", "cmm_upsampler_set_scales",
     "cmm_upsampler_get_scales", "cmm_upsampler_collect", "cmm_upsampler_dataset_size", "cmm_upsampler_train",
@@ -119,6 +122,12 @@ def lib():
     L.cmm_ensemble_field_bytes.argtypes = [vp, ip, C.c_char_p]
     L.cmm_ensemble_field_bytes.restype = C.c_size_t
     L.cmm_ensemble_stats.argtypes = [vp, C.POINTER(C.c_longlong)]
+    L.cmm_ensemble_set_fused.argtypes = [vp, ip]
+    L.cmm_ensemble_set_wait_limit.argtypes = [vp, C.c_longlong]
+    L.cmm_ensemble_fused_info.argtypes = [vp, C.POINTER(C.c_longlong), C.c_char_p, C.c_size_t]
+    L.cmm_ensemble_tuning.argtypes = [vp, C.POINTER(C.c_longlong), ip]
+    L.cmm_ensemble_set_profiling.argtypes = [vp, ip]
+    L.cmm_ensemble_profile.argtypes = [vp, C.POINTER(C.c_ulonglong)]
     L.cmm_ensemble_destroy.argtypes = [vp]
     fp, u16p, llp = C.POINTER(C.c_float), C.POINTER(C.c_ushort), C.POINTER(C.c_longlong)
     L.cmm_upsampler_create.argtypes = [ip, ip, C.c_ulonglong, vp, C.POINTER(vp)]
@@ -361,7 +370,9 @@ class Ensemble:
     """Many mixed-form runs of uneven sizes advanced together (cmm_ensemble_*): members[i] is
     the argument list member i would get as a Simulation."""
 
-    def __init__(self, members, stream=None, graphs=True):
+    def __init__(self, members, stream=None, graphs=True, fused=None):
+        """fused: None (default) the autotuner's choice of iteration form, True the single launch,
+        False the two-phase iteration with the remaps on the host."""
         L = lib()
         flat, counts = [], []
         for argv in members:
@@ -375,6 +386,7 @@ class Ensemble:
         check(L.cmm_ensemble_create(len(counts), cnt, arr, stream, C.byref(h)))
         self.h, self.L, self.n = h, L, len(counts)
         check(L.cmm_ensemble_set_graphs(self.h, 1 if graphs else 0))
+        check(L.cmm_ensemble_set_fused(self.h, 2 if fused is None else (1 if fused else 0)))
 
     def close(self):
         if self.h:
@@ -418,6 +430,43 @@ class Ensemble:
         check(self.L.cmm_ensemble_stats(self.h, out))
         return dict(zip(("member_steps", "iterations", "launches", "members", "advect_blocks", "sample_blocks"),
                         list(out)))
+
+    def set_wait_limit(self, polls):
+        """Polls after which a grid barrier of the single-launch iteration gives up (CMM_ERR_TIMEOUT)."""
+        check(self.L.cmm_ensemble_set_wait_limit(self.h, C.c_longlong(int(polls))))
+
+    def fused_info(self):
+        """{available, fused, register_budget, blocks, tiles_per_task, waves, why}: whether the single
+        launch is available and in use, the shape in use (register_budget 0: the two-phase iteration),
+        or why it is unavailable."""
+        out = (C.c_longlong * 6)()
+        why = C.create_string_buffer(512)
+        check(self.L.cmm_ensemble_fused_info(self.h, out, why, C.c_size_t(512)))
+        return dict(available=bool(out[0]), fused=bool(out[1]), register_budget=out[2], blocks=out[3],
+                    tiles_per_task=out[4], waves=out[5], why=why.value.decode())
+
+    STAGES = ("precombine", "advect", "check", "compose", "fine_rows", "fine_columns", "fine_inverse_rows",
+              "sample", "psi_rows", "psi_columns", "psi_inverse_rows")
+
+    def set_profiling(self, on=True):
+        """Count block cycles and tasks per stage of the single-launch iteration (on zeroes them)."""
+        check(self.L.cmm_ensemble_set_profiling(self.h, 1 if on else 0))
+
+    def profile(self):
+        """{stage: (block cycles, tasks)}, barrier block cycles and ns per wave since profiling was switched on."""
+        out = (C.c_ulonglong * 56)()
+        check(self.L.cmm_ensemble_profile(self.h, out))
+        stages = {n: (out[k], out[16 + k]) for k, n in enumerate(self.STAGES)}
+        return dict(stages=stages, barrier_cycles=out[32], wave_ns=[out[40 + w] for w in range(16)])
+
+    def tuning(self):
+        """The autotuner's table: [(register_budget, blocks, tiles_per_task, median iteration ms), ...]
+        (empty until tuned)."""
+        out = (C.c_longlong * 128)()
+        n = self.L.cmm_ensemble_tuning(self.h, out, 32)
+        if n < 0:
+            check(n)
+        return [(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3] / 1e6) for k in range(min(n, 32))]
 
 
 

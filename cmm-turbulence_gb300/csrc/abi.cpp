@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <string>
@@ -20,6 +21,8 @@ struct cmm_ensemble {
     cmm::EnsembleSim* ens = nullptr;
     cudaStream_t stream = nullptr;
     bool graphs = true;
+    int fused = 2;
+    long long wait_limit = 1ll << 24;
 };
 
 struct cmm_poisson {
@@ -585,6 +588,8 @@ int cmm_ensemble_init(cmm_ensemble* e)
     if (!ens) return fail(CMM_ERR_PARAM, "out of host memory");
     ens->stream = e->stream;
     ens->use_graphs = e->graphs;
+    ens->fused_mode = e->fused;
+    ens->wait_limit = e->wait_limit;
     for (int i = 0; i < ens->size(); ++i) {
         const auto& d = e->discrete[(size_t)i];
         if (!d.empty() && ens->set_initial_discrete(i, d.data(), d.size())) {
@@ -656,6 +661,70 @@ int cmm_ensemble_stats(cmm_ensemble* e, long long* out6)
     out6[4] = x.blocks[cmm::kEnsAdvect];
     out6[5] = x.blocks[cmm::kEnsSampleVort];
     return CMM_OK;
+}
+
+int cmm_ensemble_set_fused(cmm_ensemble* e, int mode)
+{
+    if (!e) return fail(CMM_ERR_PARAM, "ensemble is NULL");
+    if (e->ens) return fail(CMM_ERR_STATE, "cmm_ensemble_set_fused after cmm_ensemble_init");
+    if (mode < 0 || mode > 2) return fail(CMM_ERR_PARAM, "iteration form 0 (two-phase), 1 (single launch) or 2 (tuned)");
+    e->fused = mode;
+    return CMM_OK;
+}
+
+int cmm_ensemble_set_wait_limit(cmm_ensemble* e, long long polls)
+{
+    if (!e) return fail(CMM_ERR_PARAM, "ensemble is NULL");
+    if (polls < 0) return fail(CMM_ERR_PARAM, "the wait limit is a number of polls (>= 0)");
+    e->wait_limit = polls;
+    if (e->ens) e->ens->set_wait_limit(polls);
+    return CMM_OK;
+}
+
+int cmm_ensemble_fused_info(cmm_ensemble* e, long long* out6, char* why, size_t why_cap)
+{
+    if (!e || !e->ens || !out6) return fail(CMM_ERR_STATE, "ensemble not initialised or NULL argument");
+    cmm::EnsembleSim& x = *e->ens;
+    out6[0] = x.fused_available() ? 1 : 0;
+    out6[1] = x.fused() ? 1 : 0;
+    out6[2] = x.fused_minb;
+    out6[3] = x.fused_blocks;
+    out6[4] = x.fused_g;
+    out6[5] = x.last_waves;
+    if (why && why_cap) {
+        const size_t n = std::min(why_cap - 1, x.fused_why.size());
+        std::memcpy(why, x.fused_why.data(), n);
+        why[n] = 0;
+    }
+    return CMM_OK;
+}
+
+int cmm_ensemble_tuning(cmm_ensemble* e, long long* out4, int cap)
+{
+    if (!e || !e->ens || (!out4 && cap > 0)) return fail(CMM_ERR_STATE, "ensemble not initialised or NULL argument");
+    const auto& t = e->ens->tuning;
+    const int n = std::min(cap, (int)t.size());
+    for (int k = 0; k < n; ++k) {
+        out4[4 * k] = t[(size_t)k].minb;
+        out4[4 * k + 1] = t[(size_t)k].blocks;
+        out4[4 * k + 2] = t[(size_t)k].g;
+        out4[4 * k + 3] = (long long)(t[(size_t)k].ms * 1e6);
+    }
+    return (int)t.size();
+}
+
+int cmm_ensemble_set_profiling(cmm_ensemble* e, int on)
+{
+    if (!e || !e->ens) return fail(CMM_ERR_STATE, "cmm_ensemble_set_profiling before cmm_ensemble_init");
+    int rc = e->ens->set_profiling(on != 0);
+    return rc ? fail(rc, e->ens->err) : CMM_OK;
+}
+
+int cmm_ensemble_profile(cmm_ensemble* e, unsigned long long* out56)
+{
+    if (!e || !e->ens || !out56) return fail(CMM_ERR_STATE, "ensemble not initialised or NULL argument");
+    int rc = e->ens->read_profile(out56);
+    return rc ? fail(rc, e->ens->err) : CMM_OK;
 }
 
 int cmm_ensemble_destroy(cmm_ensemble* e)

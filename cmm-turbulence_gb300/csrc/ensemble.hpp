@@ -3,19 +3,25 @@
 //
 // Every member is a full EulerSim (its own settings, maps, stack, initial condition,
 // remaps, saves).  One ensemble iteration advances each active member by one of its own
-// time steps; the per-step work of all members runs in a handful of launches:
-//   phase A: descriptors up, precombinations, map advection, incompressibility check,
-//            the members' E_inc down (one 8-byte value each, one copy);
-//   host:    remaps of the members whose E_inc asks for one, psi rotation;
-//   phase B: descriptors up, omega on the vort grids, one batched R2C per size class, the
-//            spectral psi, one batched C2R (4 planes) per size class, psi nodes and Lagrange
-//            combinations, coarse vorticity.
-// Members of one size class share contiguous FFT buffers, so each class transforms in one
-// batched transform (csrc/fft.hpp).  The batched kernels walk a work list of 256-thread tiles with a
-// persistent grid whose size per kernel is picked by timing the candidates on the first
-// iteration (every batched kernel is idempotent within a step, so the trials cost time but
-// change nothing).  From the second iteration on each phase is a CUDA graph, re-captured
-// when a size class finishes.
+// time steps.
+//
+// Single-launch iteration (the default where every member allows it, launch_ens_fused in
+// csrc/ens_fused.cuh): precombination, advection, incompressibility check, the remap
+// decision and the remaps (composition through the stack, fine-grid transforms, map push
+// and reset), the psi solve (sample, rows, columns, inverse rows with the Lagrange
+// combinations) and the coarse vorticity of every member run in one cooperative launch of
+// persistent blocks that take tasks from per-wave device work queues.  Around it: one copy
+// of the members' descriptors up, one memset of the launch's shared state and one copy of
+// the members' E_inc and remap flags down, all captured in one CUDA graph once the shape is
+// tuned.  The host then books each member's remap and does its particles and saves.  The
+// autotuner tries every (resident blocks per SM, tiles per task) shape on the first
+// iterations, round robin, and keeps the one with the lowest median iteration time.
+//
+// Two-phase iteration (the fallback): phase A (precombinations, advection, check) and phase
+// B (sample, batched transforms per size class, spectral psi, psi nodes, coarse vorticity)
+// in batched launches with the remaps one member at a time on the host between them; the
+// persistent grid of each batched kernel is picked by timing the candidates on the first
+// iteration, and each phase is a CUDA graph from the second on.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -45,6 +51,24 @@ public:
     std::string err;
     cudaStream_t stream = nullptr;
     bool use_graphs = true;
+    // iteration form (set before init): 0 the two-phase iteration with the remaps on the host,
+    // 1 the single launch, 2 (default) the autotuner's choice between the single launch in each of
+    // its shapes and the two-phase iteration with the remaps in one batched launch
+    int fused_mode = 2;
+    long long wait_limit = 1ll << 24;   // polls before a grid barrier of a batched launch gives up
+    bool fused_available() const { return fused_ok_; }
+    bool fused() const { return fused_ok_ && fused_minb != 0; }   // the form in use is the single launch
+    std::string fused_why;           // why the single-launch iteration is unavailable
+    int fused_minb = 0, fused_blocks = 0, fused_g = 0, last_waves = 0;
+    // register budget (blocks per SM; 0: the two-phase iteration with batched remaps), grid, tiles
+    // per task, median wall time of an iteration
+    struct Shape { int minb, blocks, g; double ms; };
+    std::vector<Shape> tuning;       // the autotuner's table
+    void set_wait_limit(long long polls);
+    // profiling counters of the single launch (kProfValues: cycles and tasks per stage, barrier
+    // cycles, nanoseconds per wave), summed over the iterations since profiling was switched on
+    int set_profiling(bool on);
+    int read_profile(unsigned long long* out);
     long long member_steps = 0;      // member time steps taken
     long long iterations = 0;
     long long launches = 0;          // batched launches + transform kernels + per-member remap work
@@ -61,6 +85,12 @@ private:
         long long real_stride = 0, spec_stride = 0, spec4_stride = 0;
         fft::Plan2D pv, pp;             // FP32 transforms of the vort and psi grids
         bool active = true;
+        // the single-launch iteration: fine-grid transforms and per-member work arrays
+        fft::Plan2D pf;
+        float* freal = nullptr;
+        float2* fw1 = nullptr;
+        float2* fw2 = nullptr;
+        long long freal_stride = 0, fw1_stride = 0, fw2_stride = 0;
     };
     int phase_a();
     int phase_b();
@@ -69,6 +99,11 @@ private:
     int capture(int which, cudaGraphExec_t* exec);
     void drop_graphs();
     int check(cudaError_t e, const char* what);
+    int init_fused();
+    int step_fused(const Shape& sh);
+    int step_two_phase(bool batched_remaps);
+    int fused_sequence(const Shape& sh);   // descriptors up, state zeroed, the launch, results down
+    int remap_launch();                     // the two-phase iteration's batched remaps (h_rem_)
 
     std::vector<std::unique_ptr<EulerSim>> m_;
     std::vector<SizeClass> cls_;
@@ -85,6 +120,20 @@ private:
     bool initialised_ = false, tuned_ = false, own_stream_ = false;
     cudaGraphExec_t graph_[2] = {nullptr, nullptr};
     std::vector<int> stepping_;              // members that took this iteration's step
+    // single-launch iteration
+    bool fused_ok_ = false, broken_ = false, fused_tuned_ = false, remap_pending_ = false;
+    EnsMember* h_rem_ = nullptr;             // remap descriptors of the two-phase iteration (pinned)
+    EnsMember* d_rem_ = nullptr;
+    EnsClass* d_cls_ = nullptr;
+    unsigned char* d_fsh_ = nullptr;         // EnsShared, then M E_inc (FP64 bits), then M remap flags
+    unsigned char* h_fsh_ = nullptr;         // pinned copy
+    size_t fsh_bytes_ = 0;
+    int tab_values_ = 0, work_values_ = 0, sms_ = 0;
+    std::vector<Shape> cands_;
+    std::vector<std::vector<float>> samples_;
+    int tune_iter_ = 0;
+    cudaGraphExec_t fgraph_ = nullptr;
+    unsigned long long* d_prof_ = nullptr;   // profiling counters (null: off)
 };
 
 }  // namespace cmm

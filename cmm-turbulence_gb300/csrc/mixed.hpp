@@ -58,18 +58,6 @@ cudaError_t launch_psi_solve_m(const Grid& gm, const Grid& gv, const Grid& gf, c
                                float2* w1, float2* w2, float4* out0, const float4* l1, const float4* l2,
                                const double* c1, const double* c2, const double* c3, float4* o1, float4* o2,
                                float4* o3, cudaStream_t s);
-cudaError_t launch_advect_m(const AdvectMArgs& a, cudaStream_t s);
-// the fused psi solve (omega through the map on gv, the kept modes, psi nodes on gp and, with
-// c1 != nullptr, the three Lagrange combinations of launch_psi_nodes3): three launches on the
-// library's FFT; runs when psi_solve_m_fits (vort grid = 4 x map grid, shapes the fused
-// kernels hold), which also gives the complex values the work arrays w1, w2 need
-bool psi_solve_m_fits(const Grid& gm, const Grid& gv, const Grid& gp, double freq, const fft::Plan2D& pv,
-                      const fft::Plan2D& pp, long long* w1_values, long long* w2_values);
-void psi_solve_m_prepare();
-cudaError_t launch_psi_solve_m(const Grid& gm, const Grid& gv, const Grid& gf, const float4* map, const float4* W,
-                               const Grid& gp, double freq, const fft::Plan2D& pv, const fft::Plan2D& pp, float2* w1,
-                               float2* w2, float4* out0, const float4* l1, const float4* l2, const double* c1,
-                               const double* c2, const double* c3, float4* o1, float4* o2, float4* o3, cudaStream_t s);
 // max |det grad X - 1| on the half-shifted check grid with r = Ncheck / Nmap points per cell and axis
 // (r * Nmap^2 < 2^31)
 cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_result, cudaStream_t s);
@@ -79,6 +67,9 @@ cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_
 cudaError_t launch_compose_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
                              const InitSource& src, const float4* disc, double* out, cudaStream_t s,
                              float* out_f = nullptr);
+// fixed-point constants of launch_compose_m: the target grid's node spacing, the map domain's scale
+void fix_constants(const Grid& gm, const Grid& gt, unsigned long long* stx, unsigned long long* sty, float2* scx,
+                   float2* scy);
 // FP32 Hermite spectra [F, i kx F, i ky F, -kx ky F] of an unnormalised R2C half spectrum
 cudaError_t launch_spec_hermite_f(const float2* F, const Grid& g, float2* out4, cudaStream_t s);
 // positions of the nodes of gt through the current map and the stack (fixed point), as FP64
@@ -171,8 +162,84 @@ struct EnsMember {
     float4* pa;
     float4* pb;
     float ca[3], cb[3];
+    // the single-launch iteration (launch_ens_fused)
+    int cls;                         // the member's size class (index into the EnsClass array)
+    int can_remap;                   // remapping on and room on the stack
+    double threshold;                // incomp_threshold
+    int n_maps;                      // maps on the stack
+    float inv_nf;                    // 1 / N of the fine grid (FP32)
+    const float4* stack;             // the stack (n_maps maps of 2 Nc float4)
+    float4* push_slot;               // where the advected map goes at a remap
+    InitSource src;                  // omega_0 (analytic, or the discrete field's nodes disc)
+    const float4* disc;
+    unsigned long long stx, sty;     // fixed-point spacing of the fine grid
+    float2 scx, scy;                 // fixed-point scale of the domain
+    float* real;                     // omega_0 on the fine grid at a remap, then omega on the vort grid
+    float2* w1;                      // row spectra (fine grid at a remap, then the psi solve's kept columns)
+    float2* w2;                      // the four Hermite spectra (fine grid, then psi grid)
+    float4* wfm_out;                 // the fine vorticity nodes a remap writes (= wfm)
+};
+
+// the transforms of one size class of the single-launch iteration (group shapes for
+// 256-thread blocks, 4 values per thread)
+struct EnsClass {
+    fft::RadixPlan v_rx, v_ry, p_rx, p_ry, f_rx, f_ry;   // vort, psi, fine grids: rows (n/2), columns
+    const float2* v_twx;             // row tables (pass twiddles, then W^k for k <= n)
+    const float2* v_twy;             // column tables
+    const float2* p_twx;
+    const float2* p_twy;
+    const float2* f_twx;
+    const float2* f_twy;
+    long long ld, f_ld;              // row strides of the work arrays: psi solve, fine grid
+    int kv, ncols;                   // psi solve: vort-row bins kept, psi columns kept
+    int C_p, C_f;                    // columns per group of the column passes (psi, fine)
+    int nb_prow, nb_pinv, nb_frow, nb_finv;   // rows per group of the row passes
+    int pow2;                        // every length a power of two (else 2^a 3^b)
     int pad_;
 };
+
+constexpr int kEnsFusedThreads = 256;
+constexpr int kEnsFusedMaxMembers = 512;
+constexpr int kEnsFusedMaxWaves = 16;
+
+// state one launch shares between its blocks (zeroed before the launch): the grid barrier,
+// one work-queue counter per wave, the members' check results and remap flags
+struct EnsShared {
+    unsigned int count;              // barrier arrivals
+    int status;                      // 0, or 1 + the wave after which a barrier gave up waiting
+    int waves;                       // waves the launch ran
+    int pad_;
+    unsigned int queue[kEnsFusedMaxWaves];
+};
+
+struct EnsFusedArgs {
+    const EnsMember* mem;
+    const EnsClass* cls;
+    int M;
+    int g;                           // 256-thread tiles per task of the elementwise stages
+    int lpn_log2;                    // advection lanes per node (log2)
+    int tab_values, work_values;     // dynamic shared memory: tables, then work (float2 units)
+    long long wait_limit;            // polls before a grid barrier gives up
+    EnsShared* sh;
+    unsigned long long* einc;        // M check results (FP64 bits), zeroed before the launch
+    int* remapped;                   // M flags, written by the launch
+    unsigned long long* prof;        // null, or kProfValues counters the launch adds to (profiling)
+    int remaps_only;                 // 1: only the remap stages of the members whose descriptors are active
+    int pad_;
+};
+
+// profiling counters of the single launch: block cycles and tasks per stage (11 stages),
+// block cycles in grid barriers, nanoseconds of each wave (block 0's clock)
+enum { kProfStage = 0, kProfTasks = 16, kProfBarrier = 32, kProfWave = 40, kProfValues = 40 + kEnsFusedMaxWaves };
+
+// shared-memory values (float2 units) the tables and the work of one class need
+void ens_fused_smem_values(const EnsClass& c, const Grid& gv, const Grid& gp, const Grid& gf, int* tab, int* work);
+// every member's whole step (precombination, advection, check, remap decision and remap, psi
+// solve, coarse vorticity) in one cooperative launch of `blocks` blocks; TI in {10, 21, 30}; minb
+// in {4, 6}: the register budget is that of minb resident blocks per SM (64 or 40 registers)
+cudaError_t launch_ens_fused(int TI, int minb, const EnsFusedArgs& a, int blocks, cudaStream_t s);
+// resident blocks per SM of the launch of that register budget (0: it cannot run)
+int ens_fused_blocks_per_sm(int TI, int minb, const EnsFusedArgs& a);
 
 enum { kEnsAdvect = 0, kEnsIncomp, kEnsSampleVort, kEnsSampleCoarse, kEnsSpec, kEnsNodes, kEnsPrecombine, kEnsKinds };
 // one batched launch of kernel kind over the work list cum (M members, cum[M] tiles) with

@@ -753,6 +753,15 @@ static unsigned long long fix_step(int n)
     return ~0ull / (unsigned long long)n;
 }
 
+void fix_constants(const Grid& gm, const Grid& gt, unsigned long long* stx, unsigned long long* sty, float2* scx,
+                   float2* scy)
+{
+    *stx = fix_step(gt.NX);
+    *sty = fix_step(gt.NY);
+    *scx = fix_scale(gm.Wx);
+    *scy = fix_scale(gm.Wy);
+}
+
 // ---------------------------------------------------------------------------
 // remap-time composition: every target node is chased through the current
 // map and all stacked maps (x <- x + d(x)) at 64-bit fixed-point positions;
@@ -760,14 +769,12 @@ static unsigned long long fix_step(int n)
 // Hermite nodes, an analytic one with its FP64 formula).  Target, map and
 // discrete grids span the same domain.
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(256) k_compose_m(Grid gm, Grid gt, unsigned long long stx, unsigned long long sty,
-                                                   float2 scx, float2 scy, const float4* __restrict__ map,
-                                                   const float4* __restrict__ stack, int n_maps, InitSource src,
-                                                   const float4* __restrict__ disc, T* __restrict__ out)
+// omega_0 at target node (iX, iY) (fixed-point spacing stx, sty)
+__device__ __forceinline__ double compose_value(const Grid& gm, unsigned long long stx, unsigned long long sty,
+                                                float2 scx, float2 scy, const float4* __restrict__ map,
+                                                const float4* __restrict__ stack, int n_maps, const InitSource& src,
+                                                const float4* __restrict__ disc, int iX, int iY)
 {
-    const int iX = blockIdx.x * blockDim.x + threadIdx.x, iY = blockIdx.y;
-    if (iX >= gt.NX) return;
     unsigned long long Px = (unsigned long long)iX * stx, Py = (unsigned long long)iY * sty;
     int cx, cy;
     float tx, ty, dx, dy;
@@ -796,7 +803,18 @@ __global__ void __launch_bounds__(256) k_compose_m(Grid gm, Grid gt, unsigned lo
         double y = gm.b2 + __ull2double_rn(Py) * (gm.Wy * 5.42101086242752217e-20);
         v = init_field(src.kind, x, y, src.ic_num, src.params, src.rand_table);
     }
-    out[(long long)iY * gt.NX + iX] = (T)v;
+    return v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_compose_m(Grid gm, Grid gt, unsigned long long stx, unsigned long long sty,
+                                                   float2 scx, float2 scy, const float4* __restrict__ map,
+                                                   const float4* __restrict__ stack, int n_maps, InitSource src,
+                                                   const float4* __restrict__ disc, T* __restrict__ out)
+{
+    const int iX = blockIdx.x * blockDim.x + threadIdx.x, iY = blockIdx.y;
+    if (iX >= gt.NX) return;
+    out[(long long)iY * gt.NX + iX] = (T)compose_value(gm, stx, sty, scx, scy, map, stack, n_maps, src, disc, iX, iY);
 }
 
 cudaError_t launch_compose_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
@@ -909,7 +927,8 @@ cudaError_t launch_compose_pos_m(const Grid& gm, const Grid& gt, const float4* m
 // y).  One thread per output point: the lanes of a warp sample consecutive points, so their
 // fine-grid gathers land on consecutive nodes (one 128-byte line per 8 lanes) instead of
 // nodes ro apart; the map cell's y-contraction is recomputed by each of its ro points.
-template <typename T, int RO = 0>
+// ZM: the map is the identity (its nodes are taken as zero, not read)
+template <typename T, int RO = 0, bool ZM = false>
 __device__ __forceinline__ void sample_m_point(const Grid& gm, const Grid& go, const Grid& gf, int ro_rt, int rf,
                                                float iro, const float4* __restrict__ map, const float4* __restrict__ W,
                                                T* __restrict__ out, int iX, int iY, const W4f* swx)
@@ -920,10 +939,11 @@ __device__ __forceinline__ void sample_m_point(const Grid& gm, const Grid& go, c
     const int my = iY / ro, sy = iY - my * ro;
     const int mx1 = mx + 1 == gm.NX ? 0 : mx + 1, my1 = my + 1 == gm.NY ? 0 : my + 1;
     const int i00 = my * gm.NX + mx, i10 = my * gm.NX + mx1, i01 = my1 * gm.NX + mx, i11 = my1 * gm.NX + mx1;
-    float4 a00 = __ldg(map + 2 * i00), b00 = __ldg(map + 2 * i00 + 1);
-    float4 a10 = __ldg(map + 2 * i10), b10 = __ldg(map + 2 * i10 + 1);
-    float4 a01 = __ldg(map + 2 * i01), b01 = __ldg(map + 2 * i01 + 1);
-    float4 a11 = __ldg(map + 2 * i11), b11 = __ldg(map + 2 * i11 + 1);
+    const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float4 a00 = ZM ? z4 : __ldg(map + 2 * i00), b00 = ZM ? z4 : __ldg(map + 2 * i00 + 1);
+    float4 a10 = ZM ? z4 : __ldg(map + 2 * i10), b10 = ZM ? z4 : __ldg(map + 2 * i10 + 1);
+    float4 a01 = ZM ? z4 : __ldg(map + 2 * i01), b01 = ZM ? z4 : __ldg(map + 2 * i01 + 1);
+    float4 a11 = ZM ? z4 : __ldg(map + 2 * i11), b11 = ZM ? z4 : __ldg(map + 2 * i11 + 1);
     const W4f wy = value_weights_f((float)sy * iro, gm.hyf);
     // y-contracted value (V) and x-slope (S) of each component at the two x-columns
     const float VX0 = fmaf(wy.w3, b01.x, fmaf(wy.w2, b00.x, fmaf(wy.w1, a01.x, wy.w0 * a00.x)));
@@ -960,6 +980,7 @@ __global__ void __launch_bounds__(256) k_sample_m(Grid gm, Grid go, Grid gf, int
 // multiple of 4) share the cell's y-contraction.  Lane k loads one component of the cell's
 // four nodes (X, X_x, Y, Y_x by k: 8 scalar loads) and contracts it in y (the same fmaf
 // chains as sample_m_point, so the values are identical); the quad exchanges the 8 values.
+template <bool ZM = false>
 __device__ __forceinline__ float sample_m4_value(const Grid& gm, const Grid& go, const Grid& gf, int rf,
                                                 const float4* __restrict__ map, const float4* __restrict__ W,
                                                 int iX0, int iY)
@@ -975,10 +996,10 @@ __device__ __forceinline__ float sample_m4_value(const Grid& gm, const Grid& go,
     // .x (VX), .z (SX), .y (VY), .w (SY)
     const int comp = k == 0 ? 0 : (k == 1 ? 2 : (k == 2 ? 1 : 3));
     const float* m = reinterpret_cast<const float*>(map);
-    const float a00 = __ldg(m + 8ll * i00 + comp), b00 = __ldg(m + 8ll * i00 + 4 + comp);
-    const float a10 = __ldg(m + 8ll * i10 + comp), b10 = __ldg(m + 8ll * i10 + 4 + comp);
-    const float a01 = __ldg(m + 8ll * i01 + comp), b01 = __ldg(m + 8ll * i01 + 4 + comp);
-    const float a11 = __ldg(m + 8ll * i11 + comp), b11 = __ldg(m + 8ll * i11 + 4 + comp);
+    const float a00 = ZM ? 0.0f : __ldg(m + 8ll * i00 + comp), b00 = ZM ? 0.0f : __ldg(m + 8ll * i00 + 4 + comp);
+    const float a10 = ZM ? 0.0f : __ldg(m + 8ll * i10 + comp), b10 = ZM ? 0.0f : __ldg(m + 8ll * i10 + 4 + comp);
+    const float a01 = ZM ? 0.0f : __ldg(m + 8ll * i01 + comp), b01 = ZM ? 0.0f : __ldg(m + 8ll * i01 + 4 + comp);
+    const float a11 = ZM ? 0.0f : __ldg(m + 8ll * i11 + comp), b11 = ZM ? 0.0f : __ldg(m + 8ll * i11 + 4 + comp);
     const float C0 = fmaf(wy.w3, b01, fmaf(wy.w2, b00, fmaf(wy.w1, a01, wy.w0 * a00)));
     const float C1 = fmaf(wy.w3, b11, fmaf(wy.w2, b10, fmaf(wy.w1, a11, wy.w0 * a10)));
     const unsigned full = 0xffffffffu;
@@ -1943,3 +1964,5 @@ cudaError_t launch_psi_solve_m(const Grid& gm, const Grid& gv, const Grid& gf, c
 }
 
 }  // namespace cmm
+
+#include "ens_fused.cuh"

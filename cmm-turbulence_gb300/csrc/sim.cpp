@@ -1596,7 +1596,7 @@ int EulerSim::ens_begin(EnsMember& e)
     return 0;
 }
 
-int EulerSim::ens_middle(double e_inc, EnsMember& e)
+int EulerSim::ens_middle(double e_inc, EnsMember& e, EnsMember* remap)
 {
     // step_once after the incompressibility check: the remap decision and remap, the
     // psi rotation, and the descriptor of the psi solve with its fused combinations
@@ -1609,6 +1609,20 @@ int EulerSim::ens_middle(double e_inc, EnsMember& e)
             if (s.verbose >= 0) log_.push("Stack Saturated : Exitting");
             ens_saturated_ = true;
             continue_ = false;
+        } else if (remap) {
+            // the remap runs in the ensemble's batched remap launch (launch_ens_fused, remaps
+            // only): its descriptor, the stack's room; the map moves to the stack there
+            old_ctr_ = loop_ctr_;
+            if ((rc = reserve_stack(n_maps_ + 1))) return rc;
+            *remap = EnsMember{};
+            remap_fields(*remap, true);
+            remap->active = 1;
+            remap->threshold = -1.0;   // decided here: every member in the launch remaps
+            remap->adv.gm = gc;
+            remap->adv.gp = gp;
+            remap->adv.out = mapm_;
+            n_maps_++;
+            kernel_launches++;
         } else {
             old_ctr_ = loop_ctr_;
             if ((rc = translate_ic())) return rc;
@@ -1672,6 +1686,124 @@ int EulerSim::ens_end()
     mon_buf_[kMonCounter].push_back(ens_counter_);
     if (mon_buf_[kMonTimeS].size() >= 1024) flush_monitor();
     return ens_saturated_ ? kErrSaturated : kOk;
+}
+
+int EulerSim::ens_fused_check(std::string* why) const
+{
+    auto no = [&](const char* w) { if (why) *why = w; return 0; };
+    if (s.save_map_stack) return no("the map stack is written at remaps (save_map_stack)");
+    if (gv.NX % gc.NX || gv.NY % gc.NY || gv.NX / gc.NX != gv.NY / gc.NY) return no("vort grid not a multiple of the map grid");
+    if (gf.NX % gv.NX || gf.NY % gv.NY) return no("fine grid not a multiple of the vort grid");
+    if (gf.b0 != gc.b0 || gf.b2 != gc.b2 || gf.Wx != gc.Wx || gf.Wy != gc.Wy) return no("fine and map grids span different domains");
+    if (s.initial_discrete && (gd.b0 != gc.b0 || gd.b2 != gc.b2 || gd.Wx != gc.Wx || gd.Wy != gc.Wy))
+        return no("discrete initial field on another domain");
+    return 1;
+}
+
+void EulerSim::ens_fused_bind(int cls, float* real, float2* w1, float2* w2)
+{
+    ens_cls_ = cls;
+    ens_real_ = real;
+    ens_w1_ = w1;
+    ens_w2_ = w2;
+}
+
+int EulerSim::ens_fused_prepare(EnsMember& e)
+{
+    // ens_middle's work that does not depend on the remap decision, done ahead of the launch:
+    // room on the stack for a push, the psi rotation, the predicted combinations, and the
+    // descriptor of the psi solve (on the advected map, mapm_new_ until the swap after it)
+    int rc;
+    const bool can = !s.skip_remapping && n_maps_ < max_maps;
+    if (can && (rc = reserve_stack(n_maps_ + 1))) return rc;
+    rotate_psi(L - 1);
+    const int lcl = ens_lcl_;
+    const double* t = t_vec_.data();
+    const double tn = t[lcl + 1];
+    double dtn = compute_next_timestep(tn);
+    if (tn + dtn > s.final_time) dtn = s.final_time - tn;
+    for (int i = 0; i < L; ++i) {
+        fusedLp_[i] = lagrange_coefficient(t, t[lcl] + dt_vec_[lcl + 1] / 2.0, lcl + 1, i, L);
+        fusedL1_[i] = lagrange_coefficient(t, tn + dtn, lcl + 1, i, L);
+        fusedL12_[i] = lagrange_coefficient(t, tn + dtn / 2.0, lcl + 1, i, L);
+    }
+    fused_ = true;
+    e.gv = gv;
+    e.gf = gf;
+    e.wfm = wfm_;
+    e.wfm_out = wfm_;
+    e.sample_out = ens_real_;
+    e.real = ens_real_;
+    e.w1 = ens_w1_;
+    e.w2 = ens_w2_;
+    e.freq = (float)s.freq_cut_psi;
+    e.inv_nv = (float)(1.0 / (double)gv.N);
+    e.inv_nf = (float)(1.0 / (double)gf.N);
+    e.psi_new = psim_[0];
+    e.lv1n = psim_[1];
+    e.lv2n = psim_[2];
+    e.o1 = psiP_; e.o2 = psiA_; e.o3 = psiB_;
+    for (int l = 0; l < 3; ++l) {
+        e.cm.c[0][l] = (float)fusedLp_[l];
+        e.cm.c[1][l] = (float)fusedL1_[l];
+        e.cm.c[2][l] = (float)fusedL12_[l];
+    }
+    e.fused = 1;
+    e.vort = vort;
+    remap_fields(e, can);
+    return kOk;
+}
+
+void EulerSim::remap_fields(EnsMember& e, bool can)
+{
+    // what the batched remap (compose, fine-grid transforms, push, reset) reads: the stack, the
+    // slot of the next map, omega_0 as translate_ic gives it to launch_compose_m, the work arrays
+    e.gf = gf;
+    e.wfm_out = wfm_;
+    e.real = ens_real_;
+    e.w1 = ens_w1_;
+    e.w2 = ens_w2_;
+    e.inv_nf = (float)(1.0 / (double)gf.N);
+    e.cls = ens_cls_;
+    e.can_remap = can ? 1 : 0;
+    e.threshold = s.incomp_threshold;
+    e.n_maps = n_maps_;
+    e.stack = stackm_;
+    e.push_slot = can ? stackm_ + 2 * (size_t)n_maps_ * gc.N : nullptr;
+    e.src = InitSource{};
+    e.src.kind = s.initial_discrete ? 3 : 0;
+    e.src.ic_num = s.initial_condition_num;
+    e.src.discrete = wdisc;
+    e.src.gd = gd;
+    e.src.params = d_params_;
+    e.src.rand_table = d_rand_;
+    e.disc = wdiscm_;
+    fix_constants(gc, gf, &e.stx, &e.sty, &e.scx, &e.scy);
+}
+
+int EulerSim::ens_fused_finish(double e_inc, bool remapped)
+{
+    // ens_middle's bookkeeping for the decision the device made with the same comparison
+    std::swap(mapm_, mapm_new_);
+    e_inc_ = e_inc;
+    ens_saturated_ = false;
+    const bool wants = e_inc_ > s.incomp_threshold && !s.skip_remapping;
+    if (remapped != (wants && n_maps_ < max_maps)) {
+        err = "remap decision of the batched iteration differs from the host's";
+        return kErrState;
+    }
+    if (wants && !remapped) {
+        if (s.verbose >= 0) log_.push("Stack Saturated : Exitting");
+        ens_saturated_ = true;
+        continue_ = false;
+    } else if (remapped) {
+        old_ctr_ = loop_ctr_;
+        n_maps_++;
+        kernel_launches++;
+    }
+    ens_gap_ = loop_ctr_ - old_ctr_;
+    ens_counter_ = n_maps_;
+    return kOk;
 }
 
 int EulerSim::finish()

@@ -22,7 +22,7 @@ namespace cmm {
 
 // status codes shared with the C-ABI
 enum Status { kOk = 0, kErrParam = -1, kErrIO = -2, kErrCuda = -3, kErrSaturated = -4, kErrState = -5,
-              kErrUnsupported = -6, kErrNotFound = -7 };
+              kErrUnsupported = -6, kErrNotFound = -7, kErrTimeout = -8 };
 
 struct EnsMember;
 namespace lrn { class Upsampler; }
@@ -51,8 +51,21 @@ public:
     int ens_check(std::string* why) const;
     void ens_bind(float* sample_out, const float2* spec_v, float2* spec4, const float* planes, unsigned long long* einc);
     int ens_begin(EnsMember& e);
-    int ens_middle(double e_inc, EnsMember& e);
+    // remap != nullptr (a member of the fused-path work arrays, ens_fused_bind): a remap is
+    // described in *remap for the ensemble's batched remap launch instead of run here
+    int ens_middle(double e_inc, EnsMember& e, EnsMember* remap = nullptr);
     int ens_end();
+    // the single-launch iteration (launch_ens_fused): the remap decision, the remap and the
+    // psi solve run on the device after ens_begin.  ens_fused_check: what that path needs
+    // beyond ens_check; ens_fused_bind: the member's size class and work arrays;
+    // ens_fused_prepare (after ens_begin): stack room, the psi rotation and the rest of the
+    // descriptor; ens_fused_finish (after the launch): the map swap and the bookkeeping of
+    // the remap the device decided (remapped), then ens_end as usual.
+    int ens_fused_check(std::string* why) const;
+    void ens_fused_bind(int cls, float* real, float2* w1, float2* w2);
+    int ens_fused_prepare(EnsMember& e);
+    int ens_fused_finish(double e_inc, bool remapped);
+    void remap_fields(EnsMember& e, bool can);
 
     // learned psi (precision=mixed, Euler; csrc/sim_learned.cpp).  With an upsampler attached,
     // every `every`-th step runs the exact vorticity-grid evaluation and judges the learned
@@ -223,6 +236,10 @@ private:
     float2* ens_spec4_ = nullptr;
     const float* ens_planes_ = nullptr;
     unsigned long long* ens_einc_ = nullptr;
+    int ens_cls_ = 0;
+    float* ens_real_ = nullptr;
+    float2* ens_w1_ = nullptr;
+    float2* ens_w2_ = nullptr;
     int ens_lcl_ = 0;
     double ens_dt_ = 0, ens_gap_ = 0, ens_counter_ = 0;
     bool ens_saturated_ = false;

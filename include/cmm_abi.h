@@ -39,6 +39,7 @@ extern "C" {
 #define CMM_ERR_STATE (-5)      /* call out of order (e.g. step before init) */
 #define CMM_ERR_UNSUPPORTED (-6)/* option of the reference not built in this library */
 #define CMM_ERR_NOT_FOUND (-7)  /* unknown field / scalar name */
+#define CMM_ERR_TIMEOUT (-8)    /* a bounded device wait gave up (grid barrier of a batched ensemble iteration) */
 
 typedef struct cmm_ctx cmm_ctx;
 
@@ -252,11 +253,15 @@ int cmm_diagnostics_noalloc(const cmm_grid* grid_psi, const double* psi, const c
 
 /* ---------------------------------------------------------------- ensembles
  * Many mixed-form 2D Euler runs of uneven sizes advanced together: one iteration
- * advances every member by one of its own time steps, with the advection,
- * incompressibility check, psi solve and coarse sample of all members in batched
- * launches (one batched transform per size class), captured as CUDA graphs.  Each member is
- * configured like cmm_create (argc[i] strings of argv, members one after another) and
- * must be precision=mixed, 2D Euler, three Lagrange levels, EulerExp / RK2 / RK3 maps.
+ * advances every member by one of its own time steps.  By default the whole iteration of
+ * every member -- advection, incompressibility check, remap decision and remap (composition
+ * through the stack, fine-grid transforms), psi solve and coarse sample -- runs in one
+ * cooperative launch of persistent blocks fed by device work queues, with its shape (resident
+ * blocks, tiles per task) picked by an autotuner on the first iterations and the iteration
+ * replayed from a CUDA graph.  Where a member does not allow that (see cmm_ensemble_fused_info)
+ * the iteration runs as two batched phases with the remaps on the host between them.  Each
+ * member is configured like cmm_create (argc[i] strings of argv, members one after another)
+ * and must be precision=mixed, 2D Euler, three Lagrange levels, EulerExp / RK2 / RK3 maps.
  * The reference has no ensemble driver; this is new API. */
 typedef struct cmm_ensemble cmm_ensemble;
 int cmm_ensemble_create(int n_members, const int* argc, const char* const* argv, void* stream, cmm_ensemble** out);
@@ -272,6 +277,31 @@ int cmm_ensemble_get_field(cmm_ensemble* e, int member, const char* name, void* 
 size_t cmm_ensemble_field_bytes(cmm_ensemble* e, int member, const char* name);
 /* out6 = {member time steps, iterations, batched launches, members, advection grid, sample grid} */
 int cmm_ensemble_stats(cmm_ensemble* e, long long* out6);
+/* before cmm_ensemble_init, the iteration form: 0 the two-phase iteration with the remaps on the
+ * host, 1 the single launch, 2 (default) the autotuner's choice between the single launch in each
+ * of its shapes and the two-phase iteration with the remaps in one batched launch.  1 and 2 fall
+ * back to 0 where a member does not allow the single launch (cmm_ensemble_fused_info). */
+int cmm_ensemble_set_fused(cmm_ensemble* e, int mode);
+/* polls (about 64 ns apart) after which a grid barrier of the single launch gives up: the
+ * launch ends, cmm_ensemble_step returns CMM_ERR_TIMEOUT and the ensemble refuses further
+ * steps (its members' states are partial); the CUDA context stays usable.  Default 2^24. */
+int cmm_ensemble_set_wait_limit(cmm_ensemble* e, long long polls);
+/* out6 = {single launch available (1) or not (0), in use (1: the single launch, 0: the two-phase
+ * iteration), the shape in use: register budget (resident blocks per SM the launch is compiled
+ * for: 4 -> 64 registers, 6 -> 40; 0 the two-phase iteration), blocks, tiles per task, waves of
+ * the last single launch}; why (if not NULL, why_cap bytes) receives the reason it is unavailable */
+int cmm_ensemble_fused_info(cmm_ensemble* e, long long* out6, char* why, size_t why_cap);
+/* the autotuner's table, up to cap entries of {register budget (0: the two-phase iteration with
+ * batched remaps), blocks, tiles per task, median iteration wall ns}; returns the number of
+ * entries (0 until tuning has finished) */
+int cmm_ensemble_tuning(cmm_ensemble* e, long long* out4, int cap);
+/* profiling of the single-launch iteration (after cmm_ensemble_init; on = 1 zeroes the counters).
+ * cmm_ensemble_profile fills out56: [0..10] block cycles per stage (precombine, advect, check,
+ * compose, fine rows, fine columns, fine inverse rows, sample, psi rows, psi columns, psi inverse
+ * rows), [16..26] tasks per stage, [32] block cycles waiting in grid barriers, [40..55] nanoseconds
+ * per wave, each summed over the iterations since profiling was switched on */
+int cmm_ensemble_set_profiling(cmm_ensemble* e, int on);
+int cmm_ensemble_profile(cmm_ensemble* e, unsigned long long* out56);
 int cmm_ensemble_destroy(cmm_ensemble* e);
 
 /* ---------------------------------------------------------------- learned psi

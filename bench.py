@@ -469,10 +469,11 @@ def ensemble_members(n=ENSEMBLE["members"], seed=ENSEMBLE["seed"]):
     return out
 
 
-def ensemble_args(work, i, n, precision="mixed"):
+def ensemble_args(work, i, n, precision="mixed", threshold=None):
     """N / 4N / 2N grids (map / fine = vort / psi), dt = 1/(N/2) (the metric workload's
-    CFL ratio), remaps at 1e-3 (FP32 rounding of E_inc is ~0.75/N^2, 1.8e-4 at N = 64)."""
-    e = ENSEMBLE
+    CFL ratio), remaps at 1e-3 (the run of record; at the metric workload's 1e-4 the small
+    members remap on most steps, in FP64 as in the mixed form: both are reported)."""
+    e = dict(ENSEMBLE, incomp_threshold=threshold or ENSEMBLE["incomp_threshold"])
     return ["workspace=%s/" % work, "sim_name=e%02d_%s" % (i, precision), "simulation_type=cmm_euler_2d",
             "grid_coarse=%d" % n, "grid_fine=%d" % (4 * n), "grid_vort=%d" % (4 * n), "grid_psi=%d" % (2 * n),
             "set_dt_by_steps=1", "steps_per_sec=%d" % (n // 2), "final_time=%r" % e["final_time"],
@@ -508,9 +509,31 @@ def run_ensemble(args):
         torch.cuda.synchronize()
         return time.perf_counter() - t0, a.elapsed_time(b) / 1e3
 
+    if args.ensemble_iterations or args.ensemble_profile:
+        ens = m.Ensemble([ensemble_args(work, i, n) for i, (n, _) in enumerate(members)],
+                         stream=stream.cuda_stream, graphs=not args.ensemble_iterations)
+        for i, w in enumerate(ics):
+            ens.set_initial_discrete(i, w)
+        ens.init()
+        if args.ensemble_profile:
+            ens.set_profiling(True)
+        wall, _ = timed((lambda: ens.step(args.ensemble_iterations)) if args.ensemble_iterations else ens.run)
+        st = ens.stats()
+        out = {"member_steps": st["member_steps"], "iterations": st["iterations"], "wall_s": wall,
+               "member_steps_per_s": st["member_steps"] / wall, "fused_info": ens.fused_info(),
+               "tuning": [list(r) for r in ens.tuning()]}
+        if args.ensemble_profile:
+            p = ens.profile()
+            tot = sum(c for c, _ in p["stages"].values()) + p["barrier_cycles"]
+            out["stages"] = {k: {"share": c / tot, "tasks": n, "cycles_per_task": c / max(n, 1)}
+                             for k, (c, n) in p["stages"].items()}
+            out["barrier_share"] = p["barrier_cycles"] / tot
+            out["wave_ms"] = [x / 1e6 for x in p["wave_ns"] if x]
+        ens.close()
+        print(json.dumps(out))
+        shutil.rmtree(work, ignore_errors=True)
+        return
     res = {}
-    # (graphs, fused): the single-launch iteration (graph replay, then plain launches) and the
-    # two-phase iteration with its graphs
     # (graphs, form): the autotuned form (the headline), the single launch alone and the two-phase
     # iteration with host remaps (the earlier form), each with its CUDA graphs
     variants = ((True, None),) if args.ensemble_batched_only else ((True, None), (True, True), (True, False))
@@ -552,6 +575,32 @@ def run_ensemble(args):
             seq[prec]["wall_s"] += wall
             seq[prec]["diag"].append((sim.scalar("energy"), sim.scalar("enstrophy"), int(sim.scalar("map_counter"))))
             sim.close()
+    # the whole ensemble again at the metric workload's remap threshold 1e-4: batched (the tuned
+    # form) against every member run alone in plain FP64
+    ens = m.Ensemble([ensemble_args(work, i, n, threshold=1e-4) for i, (n, _) in enumerate(members)],
+                     stream=stream.cuda_stream)
+    for i, w in enumerate(ics):
+        ens.set_initial_discrete(i, w)
+    ens.init()
+    wall4, _ = timed(ens.run)
+    st4 = ens.stats()
+    diag4 = [(ens.scalar(i, "energy"), ens.scalar(i, "enstrophy"), int(ens.scalar(i, "map_counter")))
+             for i in range(len(members))]
+    form4 = "single launch" if ens.fused_info()["fused"] else "two-phase"
+    ens.close()
+    fp4 = []
+    for i, (n, _) in enumerate(members):
+        sim = m.Simulation(ensemble_args(work, i, n, "fp64", threshold=1e-4), stream=stream.cuda_stream)
+        sim.set_initial_discrete(ics[i])
+        sim.init()
+        sim.run()
+        fp4.append((sim.scalar("energy"), sim.scalar("enstrophy"), int(sim.scalar("map_counter"))))
+        sim.close()
+    study = {"member_steps": st4["member_steps"], "wall_s": wall4, "member_steps_per_s": st4["member_steps"] / wall4,
+             "form": form4, "remaps_batched": sum(x[2] for x in diag4), "remaps_fp64": sum(y[2] for y in fp4),
+             "members_with_equal_remaps": sum(1 for x, y in zip(diag4, fp4) if x[2] == y[2]),
+             "max_energy_rel_err_vs_fp64": max(abs(x[0] - y[0]) / abs(y[0]) for x, y in zip(diag4, fp4)),
+             "max_enstrophy_rel_err_vs_fp64": max(abs(x[1] - y[1]) / abs(y[1]) for x, y in zip(diag4, fp4))}
     b, plain = res[(True, None)], seq["fp64"]
     rel = [(abs(x[0] - y[0]) / abs(y[0]), abs(x[1] - y[1]) / abs(y[1])) for x, y in zip(b["diag"], plain["diag"])]
     counts = {str(s): sum(1 for n, _ in members if n == s) for s in ENSEMBLE["sizes"]}
@@ -579,7 +628,8 @@ def run_ensemble(args):
            "max_energy_rel_err_vs_fp64": max(r[0] for r in rel),
            "max_enstrophy_rel_err_vs_fp64": max(r[1] for r in rel),
            "batched_equals_sequential_mixed_maps": sum(1 for x, y in zip(b["diag"], seq["mixed"]["diag"]) if x[2] == y[2]),
-           "remaps_batched": sum(x[2] for x in b["diag"]), "remaps_fp64": sum(y[2] for y in plain["diag"])}
+           "remaps_batched": sum(x[2] for x in b["diag"]), "remaps_fp64": sum(y[2] for y in plain["diag"]),
+           "threshold_1e-4": study}
     print(json.dumps(out))
     shutil.rmtree(work, ignore_errors=True)
 
@@ -887,6 +937,10 @@ def main():
     ap.add_argument("--vlasov-final", type=float, default=VLASOV["final_time"])
     ap.add_argument("--ensemble", action="store_true", help="run the 64-member ensemble batched and one by one")
     ap.add_argument("--ensemble-batched-only", action="store_true", help="with --ensemble: only the batched run")
+    ap.add_argument("--ensemble-profile", action="store_true",
+                    help="with --ensemble: the batched run with the single launch's per-stage counters")
+    ap.add_argument("--ensemble-iterations", type=int, default=0,
+                    help="with --ensemble: only this many batched iterations, without graphs (for an ncu capture)")
     ap.add_argument("--learned", action="store_true", help="train the psi upsampler and run the learned form")
     ap.add_argument("--learned-seeds", type=int, default=LEARNED["train_seeds"])
     ap.add_argument("--learned-iters", type=int, default=LEARNED["iters"])

@@ -268,6 +268,9 @@ void og_conv3x3_dw(const double* x, const double* dy, int B, int H, int W, int c
 double og_upsampler_loss_grad(const double* params, int nb, int C, const double* s_in, double s_out,
                               const float* inputs, const float* targets, int B, int h, int w, int emulate_bf16, int cut,
                               double* grad);
+double og_upsampler_loss_grad_sq(const double* params, int nb, int C, const double* s_in, double s_out,
+                                 const float* inputs, const float* targets, int B, int h, int w, int emu, int cut,
+                                 double* grad, double* dy_sq);
 
 #ifdef __cplusplus
 }

@@ -210,9 +210,29 @@ static void round_all(double* v, long n, int emu)
     for (long i = 0; i < n; ++i) v[i] = og_bf16_round(v[i]);
 }
 
+/* sum over pixels of dy^2 per output channel (the scale of a bias gradient's rounding noise) */
+static void sq_cols(const double* dy, long n, int cout, double* out)
+{
+    if (!out) return;
+    for (int co = 0; co < cout; ++co) {
+        double s = 0;
+        for (long p = 0; p < n; ++p) s += dy[p * cout + co] * dy[p * cout + co];
+        out[co] = s;
+    }
+}
+
 double og_upsampler_loss_grad(const double* params, int nb, int C, const double* s_in, double s_out,
                               const float* inputs, const float* targets, int B, int h, int w, int emu, int cut,
                               double* grad)
+{
+    return og_upsampler_loss_grad_sq(params, nb, C, s_in, s_out, inputs, targets, B, h, w, emu, cut, grad, NULL);
+}
+
+/* as og_upsampler_loss_grad; dy_sq (NULL or the size of params): at each layer's bias slots, the
+ * sum over pixels of the squared output gradient of that channel */
+double og_upsampler_loss_grad_sq(const double* params, int nb, int C, const double* s_in, double s_out,
+                                 const float* inputs, const float* targets, int B, int h, int w, int emu, int cut,
+                                 double* grad, double* dy_sq)
 {
     const int n_layers = 2 * nb + 2;
     long woff[130], boff[130];
@@ -344,14 +364,17 @@ double og_upsampler_loss_grad(const double* params, int nb, int C, const double*
     double* da2 = (double*)malloc(sizeof(double) * n * C);
     double* dh = (double*)malloc(sizeof(double) * n * C);
     og_conv3x3_dw(a[nb], dout, B, h, w, C, 16, grad + woff[lt], grad + boff[lt]);
+    sq_cols(dout, n, 16, dy_sq ? dy_sq + boff[lt] : NULL);
     og_conv3x3_t(dout, B, h, w, C, wq + woff[lt], 16, NULL, NULL, da);
     round_all(da, n * C, emu);
     for (int i = nb - 1; i >= 0; --i) {
         const int l1 = 1 + 2 * i, l2 = 2 + 2 * i;
         og_conv3x3_dw(hb[i], da, B, h, w, C, C, grad + woff[l2], grad + boff[l2]);
+        sq_cols(da, n, C, dy_sq ? dy_sq + boff[l2] : NULL);
         og_conv3x3_t(da, B, h, w, C, wq + woff[l2], C, hb[i], NULL, dh);
         round_all(dh, n * C, emu);
         og_conv3x3_dw(a[i], dh, B, h, w, C, C, grad + woff[l1], grad + boff[l1]);
+        sq_cols(dh, n, C, dy_sq ? dy_sq + boff[l1] : NULL);
         og_conv3x3_t(dh, B, h, w, C, wq + woff[l1], C, NULL, da, da2);
         round_all(da2, n * C, emu);
         double* t = da;
@@ -359,6 +382,7 @@ double og_upsampler_loss_grad(const double* params, int nb, int C, const double*
         da2 = t;
     }
     og_conv3x3_dw(x0, da, B, h, w, 16, C, grad + woff[0], grad + boff[0]);
+    sq_cols(da, n, C, dy_sq ? dy_sq + boff[0] : NULL);
     for (int i = 0; i <= nb; ++i) free(a[i]);
     for (int i = 0; i < nb; ++i) free(hb[i]);
     free(a);

@@ -581,6 +581,9 @@ def _learned_lib():
         L.og_upsampler_loss_grad.argtypes = [dp, C.c_int, C.c_int, dp, C.c_double, fp, fp, C.c_int, C.c_int, C.c_int,
                                              C.c_int, C.c_int, dp]
         L.og_upsampler_loss_grad.restype = C.c_double
+        L.og_upsampler_loss_grad_sq.argtypes = [dp, C.c_int, C.c_int, dp, C.c_double, fp, fp, C.c_int, C.c_int,
+                                                C.c_int, C.c_int, C.c_int, dp, dp]
+        L.og_upsampler_loss_grad_sq.restype = C.c_double
         L._learned = True
     return L
 
@@ -641,9 +644,12 @@ def conv3x3_weight_grad(x, dy):
     return dw, db
 
 
-def upsampler_loss_grad(params, blocks, channels, s_in, s_out, inputs, targets, emulate_bf16=True, cut=0):
+def upsampler_loss_grad(params, blocks, channels, s_in, s_out, inputs, targets, emulate_bf16=True, cut=0,
+                        dy_sq=False):
     """Loss and gradient of the upsampler: inputs[B, 7, h, w], targets[B, 2h, 2w] (float32);
-    cut > 0: the psi-space spectral loss (w = 1/|k|^4 on 0 < |k| <= cut)."""
+    cut > 0: the psi-space spectral loss (w = 1/|k|^4 on 0 < |k| <= cut).  dy_sq: also return,
+    at each layer's bias slots of the parameter layout, the sum over pixels of the squared
+    output gradient of that channel (the scale of the rounding noise in its bias gradient)."""
     L = _learned_lib()
     params = np.ascontiguousarray(params, dtype=np.float64)
     s_in = np.ascontiguousarray(s_in, dtype=np.float64)
@@ -652,10 +658,11 @@ def upsampler_loss_grad(params, blocks, channels, s_in, s_out, inputs, targets, 
     B, _, h, w = inputs.shape
     grad = np.zeros_like(params)
     fp = C.POINTER(C.c_float)
-    loss = L.og_upsampler_loss_grad(_dp(params), blocks, channels, _dp(s_in), float(s_out),
-                                    inputs.ctypes.data_as(fp), targets.ctypes.data_as(fp), B, h, w,
-                                    1 if emulate_bf16 else 0, int(cut), _dp(grad))
-    return loss, grad
+    sq = np.zeros_like(params)
+    loss = L.og_upsampler_loss_grad_sq(_dp(params), blocks, channels, _dp(s_in), float(s_out),
+                                       inputs.ctypes.data_as(fp), targets.ctypes.data_as(fp), B, h, w,
+                                       1 if emulate_bf16 else 0, int(cut), _dp(grad), _dp(sq))
+    return (loss, grad, sq) if dy_sq else (loss, grad)
 
 
 def upsampler_param_count(blocks, channels):

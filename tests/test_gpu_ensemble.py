@@ -42,8 +42,8 @@ def random_vorticity(n, seed, k0):
 
 
 def member_args(tmp, i, n, precision="mixed", final_time=0.5, threshold=1e-3):
-    # N / 4N / 2N grids (map / fine = vort / psi), dt = 1 / (N / 2).  The FP32 rounding of E_inc
-    # grows like dt h / eps^2 ~ 0.75 / N^2 (7e-4 at N = 32), so these small members remap at 1e-3
+    # N / 4N / 2N grids (map / fine = vort / psi), dt = 1 / (N / 2).  At 1e-4 members this small
+    # remap on most steps (in plain FP64 as in the mixed form); 1e-3 keeps a few remaps per run
     return ["workspace=%s/" % tmp, "sim_name=m%02d" % i, "simulation_type=cmm_euler_2d",
             "grid_coarse=%d" % n, "grid_fine=%d" % (4 * n), "grid_vort=%d" % (4 * n), "grid_psi=%d" % (2 * n),
             "set_dt_by_steps=1", "steps_per_sec=%d" % (n // 2), "final_time=%r" % final_time,

@@ -11,7 +11,8 @@ error and for the psi-space spectral loss training uses, against the oracle's ne
 BF16 rounding at the points where the product stores BF16 (weights, input, activations,
 output gradient, propagated gradients).  Where an FP32 sum lands on the other
 side of a BF16 rounding boundary the two round differently, so the gradients are compared
-in relative L2 per layer (2e-2) and the loss to 1e-3.
+in relative L2 per layer (2e-2), each bias gradient channel by channel against a bound derived
+from that rounding, and the loss to 1e-3.
 """
 import os
 import sys
@@ -125,23 +126,25 @@ def test_network_loss_and_gradient_match_oracle(blocks, cut):
     u, p, s_in, inputs, targets, layers = _net_case(blocks, 11 + blocks + cut)
     loss = u.loss_grad(inputs, targets, cut=cut)
     g = u.grads().astype(np.float64)
-    lo, go = O.upsampler_loss_grad(p, blocks, 32, s_in, 0.01, inputs, targets, emulate_bf16=True, cut=cut)
+    lo, go, dy_sq = O.upsampler_loss_grad(p, blocks, 32, s_in, 0.01, inputs, targets, emulate_bf16=True, cut=cut,
+                                          dy_sq=True)
     assert abs(loss - lo) <= 1e-3 * lo
     off = 0
     for li, (ci, co) in enumerate(layers):
-        # a layer's weights and bias together in relative L2.  A bias gradient is a sum over all
-        # pixels of the output gradient; under the spectral loss (k = 0 has no weight) that
-        # gradient has zero mean at the tail and nearly cancels inside, so the bias gradients
-        # alone are residues of BF16-rounded terms: they are checked separately for the mean
-        # squared error only
+        # a layer's weights and bias together in relative L2
         n_el = 9 * ci * co + co
         a, b = g[off:off + n_el], go[off:off + n_el]
         assert np.linalg.norm(a - b) <= 2e-2 * np.linalg.norm(b), (li, np.linalg.norm(a - b) / np.linalg.norm(b))
-        ab, bb = a[-co:], b[-co:]
-        if cut == 0 and np.linalg.norm(bb) > 0:
-            assert np.linalg.norm(ab - bb) <= 0.2 * np.linalg.norm(bb), (li, "bias")
-        elif cut == 0:
-            assert np.all(ab == 0), li
+        # each bias gradient, channel by channel: db_c = sum over pixels of the BF16 output
+        # gradient dy_c.  The product and the oracle round the same values, reached by sums in
+        # another order, so an element may land one BF16 step (at most 2^-7 of |dy|) on the other
+        # side; with independent signs the sum of n such steps stays within 6 sigma of
+        # 2^-7 sqrt(sum dy_c^2).  (A bias gradient under the spectral loss nearly cancels, so a
+        # relative bound on it would be meaningless; this one is absolute and holds for both losses.)
+        ab, bb, sq = a[-co:], b[-co:], dy_sq[off + n_el - co:off + n_el]
+        bound = 6.0 * 2.0 ** -7 * np.sqrt(sq) + 1e-6 * np.abs(bb)
+        assert np.all(np.abs(ab - bb) <= bound), (li, float(np.max(np.abs(ab - bb) / np.maximum(bound, 1e-300))))
+        assert np.all(ab[sq == 0] == 0), li
         off += n_el
     # unused channels carry no gradient: head inputs 7..15, tail outputs 4..15
     head = g[:9 * 16 * 32].reshape(9, 16, 32)

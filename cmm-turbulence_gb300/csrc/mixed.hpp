@@ -27,6 +27,8 @@ struct AdvectMArgs {
     const double2* tv;
     double coef64[4][kMaxFoot];
     double dt64, ep64;
+    double tau64;               // separable psi: the map's age (time since its identity), see SepDrift
+    const double2* drows;       // separable psi: SepDrift's per-row table
     float coef[4][kMaxFoot];
     float dt, ep;
     int time_integration_num;   // 10, 21, 20, 30, 40, 31, 41
@@ -34,6 +36,25 @@ struct AdvectMArgs {
     int rp;                     // psi cells per map cell (Npsi / Nmap, integer)
     int nx_log2;                // log2 of the map grid's NX when a power of two, else -1
 };
+
+// The Vlasov-Poisson mixed form stores its maps in the free-streaming frame: a map of age tau
+// (the time since it was the identity) is X = x + tau Phi(v) + d'(x, v), Y = v + d_v(x, v), where
+// Phi is the map grid's cubic Hermite interpolant of h' (u_x = -h'(v): free streaming; h the
+// velocity part of the separable psi) with node values h'(v_j) and slopes h''(v_j) (the mean of
+// the two sides at a node of h's table, as the GALS stencil's symmetric differences see it), and
+// only d' sits in the FP32 nodes.  Free streaming moves X by |v| tau, tens of length units
+// between remaps; d' holds what the electric field adds, so FP32 keeps it to 1e-7 of a small
+// number.  Because the drift is the map grid's own interpolant of its node data, X is exactly
+// the Hermite map of node data d' + (tau h'(v_j), 0, tau h''(v_j), 0) -- the map the plain form
+// would hold -- and every reader adds the drift in FP64 from the per-row table.
+struct SepDrift {
+    const double2* rows;        // (h'(v_j), h''(v_j)) for each map-grid row j
+    Grid gm;                    // the map grid
+    double tau;                 // the active map's age
+    const double* taus;         // the stacked maps' ages (compositions; null elsewhere)
+};
+// the per-row table of SepDrift from h's table tv (T[i] = (h(i+1) - h(i), h'(i)) on gp's v axis)
+cudaError_t launch_drift_rows(const double2* tv, const Grid& gp, const Grid& gm, double2* rows, cudaStream_t s);
 
 cudaError_t launch_init_map_m(float4* map, const Grid& g, cudaStream_t s);
 // outA = sum_l cA[l] levels[l], outB likewise (outB may be null)
@@ -60,13 +81,15 @@ cudaError_t launch_psi_solve_m(const Grid& gm, const Grid& gv, const Grid& gf, c
                                float4* o3, cudaStream_t s);
 // max |det grad X - 1| on the half-shifted check grid with r = Ncheck / Nmap points per cell and axis
 // (r * Nmap^2 < 2^31)
-cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_result, cudaStream_t s);
+cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_result, cudaStream_t s,
+                            const SepDrift* drift = nullptr);
 // omega_0 through current map + n stacked maps (n * 2*Nc float4), 64-bit fixed-point
 // positions; a discrete initial field (src.kind 3) is read from its FP32 Hermite nodes disc
 // (out_f != nullptr: FP32 output instead of out)
 cudaError_t launch_compose_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
                              const InitSource& src, const float4* disc, double* out, cudaStream_t s,
-                             float* out_f = nullptr);
+                             float* out_f = nullptr,
+                             const SepDrift* drift = nullptr);
 // fixed-point constants of launch_compose_m: the target grid's node spacing, the map domain's scale
 void fix_constants(const Grid& gm, const Grid& gt, unsigned long long* stx, unsigned long long* sty, float2* scx,
                    float2* scy);
@@ -74,10 +97,11 @@ void fix_constants(const Grid& gm, const Grid& gt, unsigned long long* stx, unsi
 cudaError_t launch_spec_hermite_f(const float2* F, const Grid& g, float2* out4, cudaStream_t s);
 // positions of the nodes of gt through the current map and the stack (fixed point), as FP64
 cudaError_t launch_compose_pos_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
-                                 double* px, double* py, cudaStream_t s);
+                                 double* px, double* py, cudaStream_t s, const SepDrift* drift = nullptr);
 // W(x + d(x)) on grid go (Ngo multiple of Nmap, Nf multiple of Ngo); out_f or out_d
 cudaError_t launch_sample_m(const Grid& gm, const Grid& go, const Grid& gf, const float4* map, const float4* W,
-                            float* out_f, double* out_d, cudaStream_t s);
+                            float* out_f, double* out_d, cudaStream_t s,
+                            const SepDrift* drift = nullptr);
 // tracers at 64-bit fixed-point positions P = (x - b0) / W * 2^64 (interleaved x, y)
 // (tA, tB, t0, tv: separable tables as in AdvectMArgs, used when tv != nullptr)
 // psiA = level t_n, psiB = the t_{n+1/2} combination, psi0 = t_{n+1}, psiC = t_{n-1} (RK3Mod);
@@ -123,7 +147,8 @@ cudaError_t launch_spec_psi_f(const float2* Fv, const Grid& gv, const Grid& gp, 
 cudaError_t launch_planes_to_float4(const float* planes, const double* planes_d, long long n, float4* out,
                                     cudaStream_t s);
 cudaError_t launch_float4_to_planes(const float4* in, long long n, double* planes, cudaStream_t s);
-cudaError_t launch_map_to_planes(const float4* map, const Grid& g, double* X, double* Y, cudaStream_t s);
+cudaError_t launch_map_to_planes(const float4* map, const Grid& g, double* X, double* Y, cudaStream_t s,
+                                 const SepDrift* drift = nullptr);
 cudaError_t launch_planes_to_map(const double* X, const double* Y, const Grid& g, float4* map, cudaStream_t s);
 // sum psi_x^2 + psi_y^2 (FP64 accumulation) -> out[0]
 cudaError_t launch_energy_m(const float4* psi, long long n, double* scratch, double* out, cudaStream_t s);

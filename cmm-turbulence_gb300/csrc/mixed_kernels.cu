@@ -432,6 +432,50 @@ __device__ __forceinline__ void velocity_sep64(const double2* __restrict__ TX, c
     ux = -sep_slope64(TV, y0, y1, ty, g.ihy);
 }
 
+// h'(v) and h''(v) (FP64) of the separable psi's velocity part from its 1D table (on gp's v
+// axis): the slope of the table's cubic Hermite piece (sep_slope64) and that slope's derivative
+__device__ __forceinline__ void sep_h12(const double2* __restrict__ tv, const Grid& gp, double v, double& h1, double& h2)
+{
+    int i0, i1;
+    double t;
+    locate64(0, (v - gp.b2) * gp.ihy, gp.NY, i0, i1, t);
+    const double ih = gp.ihy, s = 1.0 - t;
+    const double2 a0 = __ldg(tv + i0);
+    const double s1 = __ldg(&tv[i1].y);
+    h1 = fma(6.0 * s * t * ih, a0.x, fma(s * fma(3.0, s, -2.0), a0.y, t * fma(3.0, t, -2.0) * s1));
+    h2 = ih * fma(6.0 * (1.0 - 2.0 * t) * ih, a0.x, fma(6.0 * t - 4.0, a0.y, (6.0 * t - 2.0) * s1));
+}
+
+// SepDrift's per-row table: h' at each map row and h'' as the mean of its two sides
+__global__ void k_drift_rows(const double2* __restrict__ tv, Grid gp, Grid gm, double2* __restrict__ rows)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= gm.NY) return;
+    const double v = gm.b2 + j * gm.hy, e = 1e-9 * gp.hy;
+    double h1, h2l, h2r, g;
+    sep_h12(tv, gp, v, h1, g);
+    sep_h12(tv, gp, v - e, g, h2l);
+    sep_h12(tv, gp, v + e, g, h2r);
+    rows[j] = make_double2(h1, 0.5 * (h2l + h2r));
+}
+
+cudaError_t launch_drift_rows(const double2* tv, const Grid& gp, const Grid& gm, double2* rows, cudaStream_t s)
+{
+    k_drift_rows<<<(gm.NY + 127) / 128, 128, 0, s>>>(tv, gp, gm, rows);
+    return cudaGetLastError();
+}
+
+// Phi(v) of SepDrift: the map rows' cubic Hermite interpolant of h' (FP64)
+__device__ __forceinline__ double drift_phi(const double2* __restrict__ rows, const Grid& gm, double v)
+{
+    int j0, j1;
+    double t;
+    locate64(0, (v - gm.b2) * gm.ihy, gm.NY, j0, j1, t);
+    const double2 r0 = __ldg(rows + j0), r1 = __ldg(rows + j1);
+    const W4 w = value_weights(t, gm.hy);
+    return fma(w.w3, r1.y, fma(w.w2, r0.y, fma(w.w1, r1.x, w.w0 * r0.x)));
+}
+
 // FP64 interpolation of the FP32 displacement nodes, values taken relative to (rx, ry)
 __device__ __forceinline__ void map_disp64(const float4* __restrict__ M, const Grid& g, int bx, int by, double qx,
                                            double qy, double rx, double ry, double& dxo, double& dyo)
@@ -497,7 +541,13 @@ __global__ void __launch_bounds__(256) k_advect_sep(const AdvectMArgs a, int lpn
         }
         double mx, my;
         map_disp64(a.map, a.gm, iX, iY, (ex - Dx) * a.gm.ihx, (ey - Dy) * a.gm.ihy, n0.x, n0.y, mx, my);
-        gX = mx - Dx;
+        // free-streaming frame (SepDrift): X = x + tau Phi(v) + d'.  At the stencil point y = node +
+        // e_k the new map is X_old at its footpoint x_f = y - D, so d'_new(y) = d'_old(x_f) - D_x +
+        // tau (Phi(v_f) - Phi(v_y)) - dt Phi(v_y): free streaming alone (D_x = -dt h'(v_y), v_f =
+        // v_y) leaves d' unchanged up to Phi - h'
+        const double vy = a.gm.b2 + iY * a.gm.hy + ey;
+        const double sy = drift_phi(a.drows, a.gm, vy), sf = drift_phi(a.drows, a.gm, vy - Dy);
+        gX = mx - Dx + fma(a.tau64, sf - sy, -dt * sy);
         gY = my - Dy;
     }
     const int comp = k & 1, plane = (k >> 1) & 3;
@@ -626,7 +676,8 @@ __device__ __forceinline__ void incomp_tables(const Grid& gm, int r, float ir, W
 // R > 0 a compile-time r, nx_log2 >= 0 a power-of-two map width (shifts for the index split)
 template <int R = 0>
 __device__ __forceinline__ void incomp_item(const Grid& gm, int r_rt, float ir, const float4* __restrict__ M, int i,
-                                            const W4f* sw, const W4f* sd, F2& best, int nx_log2 = -1)
+                                            const W4f* sw, const W4f* sd, F2& best, int nx_log2 = -1,
+                                            const SepDrift* drift = nullptr)
 {
         const int r = R > 0 ? R : r_rt;
         int cell = i / r, sub_y = i - cell * r;
@@ -638,11 +689,19 @@ __device__ __forceinline__ void incomp_item(const Grid& gm, int r_rt, float ir, 
         float4 a10 = __ldg(M + 2 * i10), b10 = __ldg(M + 2 * i10 + 1);
         float4 a01 = __ldg(M + 2 * i01), b01 = __ldg(M + 2 * i01 + 1);
         float4 a11 = __ldg(M + 2 * i11), b11 = __ldg(M + 2 * i11 + 1);
+        float drow = 0.0f;   // free-streaming frame: the drift's value difference between the cell's rows
+        if (drift) {
+            // X as the map grid represents it: node data d' + (tau h'(v_j), 0, tau h''(v_j), 0)
+            const double2 r0 = __ldg(drift->rows + cy), r1 = __ldg(drift->rows + cy1);
+            const float s0 = (float)(r0.y * drift->tau), s1 = (float)(r1.y * drift->tau);
+            drow = (float)((r1.x - r0.x) * drift->tau);
+            b00.x += s0; b10.x += s0; b01.x += s1; b11.x += s1;
+        }
         float ty = ((float)sub_y + 0.5f) * ir;
         W4f wy = value_weights_f(ty, gm.hyf), dy = slope_weights_f(ty, gm.ihyf);
         // X: f = a.x, f_x = a.z, f_y = b.x, f_xy = b.z;  Y: f = a.y, f_x = a.w, f_y = b.y, f_xy = b.w
-        YCol cX = ycontract(0.0f, a10.x - a00.x, a01.x - a00.x, a11.x - a00.x, a00.z, a10.z, a01.z, a11.z,
-                            b00.x, b10.x, b01.x, b11.x, b00.z, b10.z, b01.z, b11.z, wy, dy);
+        YCol cX = ycontract(0.0f, a10.x - a00.x, a01.x - a00.x + drow, a11.x - a00.x + drow, a00.z, a10.z, a01.z,
+                            a11.z, b00.x, b10.x, b01.x, b11.x, b00.z, b10.z, b01.z, b11.z, wy, dy);
         YCol cY = ycontract(0.0f, a10.y - a00.y, a01.y - a00.y, a11.y - a00.y, a00.w, a10.w, a01.w, a11.w,
                             b00.y, b10.y, b01.y, b11.y, b00.w, b10.w, b01.w, b11.w, wy, dy);
         for (int sx = 0; sx < r; ++sx) {
@@ -688,7 +747,23 @@ __global__ void __launch_bounds__(256) k_incomp_m(Grid gm, int r, float ir, cons
     incomp_block_max(best, wmax, result);
 }
 
-cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_result, cudaStream_t s)
+// the same for a map in the free-streaming frame (SepDrift)
+__global__ void __launch_bounds__(256) k_incomp_m_drift(Grid gm, int r, float ir, const float4* __restrict__ M,
+                                                        unsigned long long* result, int nx_log2, SepDrift drift)
+{
+    __shared__ W4f sw[kMaxCheckRatio], sd[kMaxCheckRatio];
+    __shared__ F2 wmax[8];
+    incomp_tables(gm, r, ir, sw, sd);
+    __syncthreads();
+    F2 best = {0.0f, 0.0f};
+    const int total = (int)gm.N * r;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x)
+        incomp_item<0>(gm, r, ir, M, i, sw, sd, best, nx_log2, &drift);
+    incomp_block_max(best, wmax, result);
+}
+
+cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_result, cudaStream_t s,
+                            const SepDrift* drift)
 {
     if (r <= 0 || r > kMaxCheckRatio || gm.N * r > 0x7fffffffLL) return cudaErrorInvalidValue;
     cudaError_t e = cudaMemsetAsync(d_result, 0, sizeof(double), s);
@@ -699,6 +774,10 @@ cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_
     const int nx_log2 = (gm.NX & (gm.NX - 1)) == 0 ? __builtin_ctz((unsigned)gm.NX) : -1;
     unsigned long long* res = reinterpret_cast<unsigned long long*>(d_result);
     const float ir = 1.0f / (float)r;
+    if (drift) {
+        k_incomp_m_drift<<<blocks, 256, 0, s>>>(gm, r, ir, map, res, nx_log2, *drift);
+        return cudaGetLastError();
+    }
     switch (r) {
         case 2: k_incomp_m<2><<<blocks, 256, 0, s>>>(gm, r, ir, map, res, nx_log2); break;
         case 4: k_incomp_m<4><<<blocks, 256, 0, s>>>(gm, r, ir, map, res, nx_log2); break;
@@ -726,6 +805,24 @@ __device__ __forceinline__ unsigned long long fix_increment(float d, float2 sc)
     unsigned long long hi = (unsigned long long)(long long)__float2int_rn(n);   // saturates beyond W / 2
     unsigned long long lo = (unsigned long long)(long long)__float2int_rn(r * 2147483648.0f);
     return (hi << 32) + (lo << 1);
+}
+
+// FP64 coordinate -> 64-bit fixed point of the periodic domain [b, b + W)
+__device__ __forceinline__ unsigned long long fix_from(double x, double b, double W)
+{
+    double t = (x - b) / W;
+    t -= floor(t);
+    const double v = t * 18446744073709551616.0;
+    return v >= 18446744073709551616.0 ? 0ull : __double2ull_rn(v);
+}
+
+// the drift tau Phi(v) of a map in the free-streaming frame (SepDrift) at fixed-point v = Py, as a
+// fixed-point x increment (FP64: the drift is tens of domain lengths' worth of free streaming)
+__device__ __forceinline__ unsigned long long fix_drift(const SepDrift& d, const Grid& gm, unsigned long long Py,
+                                                        double tau)
+{
+    const double phi = drift_phi(d.rows, d.gm, gm.b2 + __ull2double_rn(Py) * (gm.Wy * 5.42101086242752217e-20));
+    return fix_from(phi * tau, 0.0, gm.Wx);
 }
 
 __device__ __forceinline__ void fix_cell(unsigned long long P, int n, int& cell, float& frac)
@@ -770,26 +867,40 @@ void fix_constants(const Grid& gm, const Grid& gt, unsigned long long* stx, unsi
 // discrete grids span the same domain.
 // ---------------------------------------------------------------------------
 // omega_0 at target node (iX, iY) (fixed-point spacing stx, sty)
-__device__ __forceinline__ double compose_value(const Grid& gm, unsigned long long stx, unsigned long long sty,
-                                                float2 scx, float2 scy, const float4* __restrict__ map,
-                                                const float4* __restrict__ stack, int n_maps, const InitSource& src,
-                                                const float4* __restrict__ disc, int iX, int iY)
+// the fixed-point position of a target node through the current map and the stack (drift: the
+// maps are in the free-streaming frame, drift->tau the current map's age, drift->taus the stack's)
+__device__ __forceinline__ void compose_chase(const Grid& gm, float2 scx, float2 scy, const float4* __restrict__ map,
+                                              const float4* __restrict__ stack, int n_maps, unsigned long long& Px,
+                                              unsigned long long& Py, const SepDrift* drift)
 {
-    unsigned long long Px = (unsigned long long)iX * stx, Py = (unsigned long long)iY * sty;
     int cx, cy;
     float tx, ty, dx, dy;
     fix_cell(Px, gm.NX, cx, tx);
     fix_cell(Py, gm.NY, cy, ty);
     map_disp_f(map, gm, locate_q(gm, cx, cy, tx, ty), 0.0f, 0.0f, dx, dy);
+    if (drift) Px += fix_drift(*drift, gm, Py, drift->tau);
     Px += fix_increment(dx, scx);
     Py += fix_increment(dy, scy);
     for (int m = n_maps - 1; m >= 0; --m) {
         fix_cell(Px, gm.NX, cx, tx);
         fix_cell(Py, gm.NY, cy, ty);
         map_disp_f(stack + 2 * (long long)m * gm.N, gm, locate_q(gm, cx, cy, tx, ty), 0.0f, 0.0f, dx, dy);
+        if (drift) Px += fix_drift(*drift, gm, Py, __ldg(drift->taus + m));
         Px += fix_increment(dx, scx);
         Py += fix_increment(dy, scy);
     }
+}
+
+__device__ __forceinline__ double compose_value(const Grid& gm, unsigned long long stx, unsigned long long sty,
+                                                float2 scx, float2 scy, const float4* __restrict__ map,
+                                                const float4* __restrict__ stack, int n_maps, const InitSource& src,
+                                                const float4* __restrict__ disc, int iX, int iY,
+                                                const SepDrift* drift = nullptr)
+{
+    unsigned long long Px = (unsigned long long)iX * stx, Py = (unsigned long long)iY * sty;
+    compose_chase(gm, scx, scy, map, stack, n_maps, Px, Py, drift);
+    int cx, cy;
+    float tx, ty;
     double v;
     if (src.kind == 3) {
         fix_cell(Px, src.gd.NX, cx, tx);
@@ -817,14 +928,33 @@ __global__ void __launch_bounds__(256) k_compose_m(Grid gm, Grid gt, unsigned lo
     out[(long long)iY * gt.NX + iX] = (T)compose_value(gm, stx, sty, scx, scy, map, stack, n_maps, src, disc, iX, iY);
 }
 
+// maps in the free-streaming frame (the Vlasov-Poisson mixed form)
+__global__ void __launch_bounds__(256) k_compose_m_drift(Grid gm, Grid gt, unsigned long long stx,
+                                                         unsigned long long sty, float2 scx, float2 scy,
+                                                         const float4* __restrict__ map,
+                                                         const float4* __restrict__ stack, int n_maps, InitSource src,
+                                                         const float4* __restrict__ disc, double* __restrict__ out,
+                                                         SepDrift drift)
+{
+    const int iX = blockIdx.x * blockDim.x + threadIdx.x, iY = blockIdx.y;
+    if (iX >= gt.NX) return;
+    out[(long long)iY * gt.NX + iX] = compose_value(gm, stx, sty, scx, scy, map, stack, n_maps, src, disc, iX, iY,
+                                                    &drift);
+}
+
 cudaError_t launch_compose_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
-                             const InitSource& src, const float4* disc, double* out, cudaStream_t s, float* out_f)
+                             const InitSource& src, const float4* disc, double* out, cudaStream_t s, float* out_f,
+                             const SepDrift* drift)
 {
     if (gt.b0 != gm.b0 || gt.b2 != gm.b2 || gt.Wx != gm.Wx || gt.Wy != gm.Wy || gt.NY > 65535) return cudaErrorInvalidValue;
     if (src.kind == 3 && (!disc || src.gd.b0 != gm.b0 || src.gd.b2 != gm.b2 || src.gd.Wx != gm.Wx || src.gd.Wy != gm.Wy))
         return cudaErrorInvalidValue;
     dim3 blocks((unsigned)((gt.NX + 255) / 256), (unsigned)gt.NY);
-    if (out_f)
+    if (drift) {
+        if (out_f || (n_maps > 0 && !drift->taus)) return cudaErrorInvalidValue;
+        k_compose_m_drift<<<blocks, 256, 0, s>>>(gm, gt, fix_step(gt.NX), fix_step(gt.NY), fix_scale(gm.Wx),
+                                                 fix_scale(gm.Wy), map, stack, n_maps, src, disc, out, *drift);
+    } else if (out_f)
         k_compose_m<float><<<blocks, 256, 0, s>>>(gm, gt, fix_step(gt.NX), fix_step(gt.NY), fix_scale(gm.Wx),
                                                   fix_scale(gm.Wy), map, stack, n_maps, src, disc, out_f);
     else
@@ -860,14 +990,6 @@ cudaError_t launch_spec_hermite_f(const float2* F, const Grid& g, float2* out4, 
     return cudaGetLastError();
 }
 
-// FP64 coordinate -> 64-bit fixed point of the periodic domain [b, b + W)
-__device__ __forceinline__ unsigned long long fix_from(double x, double b, double W)
-{
-    double t = (x - b) / W;
-    t -= floor(t);
-    const double v = t * 18446744073709551616.0;
-    return v >= 18446744073709551616.0 ? 0ull : __double2ull_rn(v);
-}
 
 // positions of the nodes of gt through the current map and the stack, at
 // fixed-point precision, returned as FP64 coordinates in [b0, b0 + W).  gt spans
@@ -876,7 +998,8 @@ __device__ __forceinline__ unsigned long long fix_from(double x, double b, doubl
 __global__ void __launch_bounds__(256) k_compose_pos_m(Grid gm, Grid gt, unsigned long long stx, unsigned long long sty,
                                                        float2 scx, float2 scy, const float4* __restrict__ map,
                                                        const float4* __restrict__ stack, int n_maps,
-                                                       double* __restrict__ px, double* __restrict__ py, bool window)
+                                                       double* __restrict__ px, double* __restrict__ py, bool window,
+                                                       SepDrift drift)
 {
     const int iX = blockIdx.x * blockDim.x + threadIdx.x, iY = blockIdx.y;
     if (iX >= gt.NX) return;
@@ -885,33 +1008,23 @@ __global__ void __launch_bounds__(256) k_compose_pos_m(Grid gm, Grid gt, unsigne
         Px = fix_from(gt.b0 + iX * gt.hx, gm.b0, gm.Wx);
         Py = fix_from(gt.b2 + iY * gt.hy, gm.b2, gm.Wy);
     }
-    int cx, cy;
-    float tx, ty, dx, dy;
-    fix_cell(Px, gm.NX, cx, tx);
-    fix_cell(Py, gm.NY, cy, ty);
-    map_disp_f(map, gm, locate_q(gm, cx, cy, tx, ty), 0.0f, 0.0f, dx, dy);
-    Px += fix_increment(dx, scx);
-    Py += fix_increment(dy, scy);
-    for (int m = n_maps - 1; m >= 0; --m) {
-        fix_cell(Px, gm.NX, cx, tx);
-        fix_cell(Py, gm.NY, cy, ty);
-        map_disp_f(stack + 2 * (long long)m * gm.N, gm, locate_q(gm, cx, cy, tx, ty), 0.0f, 0.0f, dx, dy);
-        Px += fix_increment(dx, scx);
-        Py += fix_increment(dy, scy);
-    }
+    compose_chase(gm, scx, scy, map, stack, n_maps, Px, Py, drift.rows ? &drift : nullptr);
     const long long i = (long long)iY * gt.NX + iX;
     px[i] = gm.b0 + __ull2double_rn(Px) * (gm.Wx * 5.42101086242752217e-20);
     py[i] = gm.b2 + __ull2double_rn(Py) * (gm.Wy * 5.42101086242752217e-20);
 }
 
 cudaError_t launch_compose_pos_m(const Grid& gm, const Grid& gt, const float4* map, const float4* stack, int n_maps,
-                                 double* px, double* py, cudaStream_t s)
+                                 double* px, double* py, cudaStream_t s, const SepDrift* drift)
 {
     if (gt.NY > 65535) return cudaErrorInvalidValue;
     const bool window = gt.b0 != gm.b0 || gt.b2 != gm.b2 || gt.Wx != gm.Wx || gt.Wy != gm.Wy;
     dim3 blocks((unsigned)((gt.NX + 255) / 256), (unsigned)gt.NY);
+    if (drift && n_maps > 0 && !drift->taus) return cudaErrorInvalidValue;
+    SepDrift d{};
+    if (drift) d = *drift;
     k_compose_pos_m<<<blocks, 256, 0, s>>>(gm, gt, fix_step(gt.NX), fix_step(gt.NY), fix_scale(gm.Wx), fix_scale(gm.Wy),
-                                           map, stack, n_maps, px, py, window);
+                                           map, stack, n_maps, px, py, window, d);
     return cudaGetLastError();
 }
 
@@ -1026,6 +1139,58 @@ __global__ void __launch_bounds__(256) k_sample_m4(Grid gm, Grid go, Grid gf, in
     if (iX < go.NX) out[(long long)iY * go.NX + iX] = (T)v;
 }
 
+// omega = W(X(x)) for a map in the free-streaming frame (SepDrift): the map's FP32 displacement
+// d' is contracted as in sample_m_point, the drift tau Phi(v) of the point's row is added in FP64
+// and the fine-grid cell is located in FP64 (the drift is tens of cells)
+template <typename T>
+__global__ void __launch_bounds__(256) k_sample_m_drift(Grid gm, Grid go, Grid gf, int ro, int rf, float iro,
+                                                        const float4* __restrict__ map, const float4* __restrict__ W,
+                                                        T* __restrict__ out, SepDrift drift)
+{
+    __shared__ W4f swx[kMaxCheckRatio];
+    __shared__ double sdrift;
+    const int iY = blockIdx.y;
+    if ((int)threadIdx.x < ro) swx[threadIdx.x] = value_weights_f((float)threadIdx.x * iro, gm.hxf);
+    if (threadIdx.x == 0) sdrift = drift_phi(drift.rows, drift.gm, go.b2 + iY * go.hy) * drift.tau;
+    __syncthreads();
+    const int iX = blockIdx.x * blockDim.x + threadIdx.x;
+    if (iX >= go.NX) return;
+    const int mx = iX / ro, k = iX - mx * ro;
+    const int my = iY / ro, sy = iY - my * ro;
+    const int mx1 = mx + 1 == gm.NX ? 0 : mx + 1, my1 = my + 1 == gm.NY ? 0 : my + 1;
+    const int i00 = my * gm.NX + mx, i10 = my * gm.NX + mx1, i01 = my1 * gm.NX + mx, i11 = my1 * gm.NX + mx1;
+    float4 a00 = __ldg(map + 2 * i00), b00 = __ldg(map + 2 * i00 + 1);
+    float4 a10 = __ldg(map + 2 * i10), b10 = __ldg(map + 2 * i10 + 1);
+    float4 a01 = __ldg(map + 2 * i01), b01 = __ldg(map + 2 * i01 + 1);
+    float4 a11 = __ldg(map + 2 * i11), b11 = __ldg(map + 2 * i11 + 1);
+    const W4f wy = value_weights_f((float)sy * iro, gm.hyf);
+    const float VX0 = fmaf(wy.w3, b01.x, fmaf(wy.w2, b00.x, fmaf(wy.w1, a01.x, wy.w0 * a00.x)));
+    const float VX1 = fmaf(wy.w3, b11.x, fmaf(wy.w2, b10.x, fmaf(wy.w1, a11.x, wy.w0 * a10.x)));
+    const float SX0 = fmaf(wy.w3, b01.z, fmaf(wy.w2, b00.z, fmaf(wy.w1, a01.z, wy.w0 * a00.z)));
+    const float SX1 = fmaf(wy.w3, b11.z, fmaf(wy.w2, b10.z, fmaf(wy.w1, a11.z, wy.w0 * a10.z)));
+    const float VY0 = fmaf(wy.w3, b01.y, fmaf(wy.w2, b00.y, fmaf(wy.w1, a01.y, wy.w0 * a00.y)));
+    const float VY1 = fmaf(wy.w3, b11.y, fmaf(wy.w2, b10.y, fmaf(wy.w1, a11.y, wy.w0 * a10.y)));
+    const float SY0 = fmaf(wy.w3, b01.w, fmaf(wy.w2, b00.w, fmaf(wy.w1, a01.w, wy.w0 * a00.w)));
+    const float SY1 = fmaf(wy.w3, b11.w, fmaf(wy.w2, b10.w, fmaf(wy.w1, a11.w, wy.w0 * a10.w)));
+    const W4f w = swx[k];
+    const float dx = fmaf(w.w3, SX1, fmaf(w.w2, SX0, fmaf(w.w1, VX1, w.w0 * VX0)));
+    const float dy = fmaf(w.w3, SY1, fmaf(w.w2, SY0, fmaf(w.w1, VY1, w.w0 * VY0)));
+    // the fine-grid cell of node (iX rf, iY rf) + (dx + drift, dy), located in FP64
+    const double qx = (double)(iX * rf) + ((double)dx + sdrift) * gf.ihx;
+    const double qy = (double)(iY * rf) + (double)dy * gf.ihy;
+    const double fx = floor(qx), fy = floor(qy);
+    CellF c;
+    c.tx = (float)(qx - fx);
+    c.ty = (float)(qy - fy);
+    const int ix0 = wrap_index((int)fx, gf.NX), iy0 = wrap_index((int)fy, gf.NY);
+    const int ix1 = ix0 + 1 == gf.NX ? 0 : ix0 + 1, iy1 = iy0 + 1 == gf.NY ? 0 : iy0 + 1;
+    c.i00 = iy0 * gf.NX + ix0; c.i10 = iy0 * gf.NX + ix1;
+    c.i01 = iy1 * gf.NX + ix0; c.i11 = iy1 * gf.NX + ix1;
+    Q4 q;
+    q.c00 = __ldg(W + c.i00); q.c10 = __ldg(W + c.i10); q.c01 = __ldg(W + c.i01); q.c11 = __ldg(W + c.i11);
+    out[(long long)iY * go.NX + iX] = (T)herm_value_f(q, value_weights_f(c.tx, gf.hxf), value_weights_f(c.ty, gf.hyf));
+}
+
 template <typename T>
 void sample_m_dispatch(dim3 blocks, cudaStream_t s, const Grid& gm, const Grid& go, const Grid& gf, int ro, int rf,
                        float iro, const float4* map, const float4* W, T* out)
@@ -1040,13 +1205,18 @@ void sample_m_dispatch(dim3 blocks, cudaStream_t s, const Grid& gm, const Grid& 
 }
 
 cudaError_t launch_sample_m(const Grid& gm, const Grid& go, const Grid& gf, const float4* map, const float4* W,
-                            float* out_f, double* out_d, cudaStream_t s)
+                            float* out_f, double* out_d, cudaStream_t s, const SepDrift* drift)
 {
     int ro = go.NX / gm.NX, rf = gf.NX / go.NX;
     if (ro < 1 || ro > kMaxCheckRatio || ro * gm.NX != go.NX || ro * gm.NY != go.NY || go.NY > 65535)
         return cudaErrorInvalidValue;
     dim3 blocks((unsigned)((go.NX + 255) / 256), (unsigned)go.NY);
     float iro = 1.0f / (float)ro;
+    if (drift) {
+        if (out_f) k_sample_m_drift<float><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out_f, *drift);
+        else k_sample_m_drift<double><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out_d, *drift);
+        return cudaGetLastError();
+    }
     if (out_f) sample_m_dispatch<float>(blocks, s, gm, go, gf, ro, rf, iro, map, W, out_f);
     else sample_m_dispatch<double>(blocks, s, gm, go, gf, ro, rf, iro, map, W, out_d);
     return cudaGetLastError();
@@ -1643,23 +1813,34 @@ cudaError_t launch_float4_to_planes(const float4* in, long long n, double* plane
     return cudaGetLastError();
 }
 
-// displacement map -> reference planar map X, Y (X = x + dX, X_x = 1 + dX_x, ...)
-__global__ void k_map_to_planes(const float4* __restrict__ M, Grid g, double* __restrict__ X, double* __restrict__ Y)
+// displacement map -> reference planar map X, Y (X = x + dX, X_x = 1 + dX_x, ...); a map in the
+// free-streaming frame (drift.rows) adds its drift's node data tau h'(v), tau h''(v) to X, X_y
+__global__ void k_map_to_planes(const float4* __restrict__ M, Grid g, double* __restrict__ X, double* __restrict__ Y,
+                                SepDrift drift)
 {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= g.N) return;
     int iX = (int)(i % g.NX), iY = (int)(i / g.NX);
     float4 a = M[2 * i], b = M[2 * i + 1];
-    X[i] = g.b0 + iX * g.hx + (double)a.x;
+    double h1 = 0.0, h2 = 0.0;
+    if (drift.rows) {
+        const double2 r = drift.rows[iY];   // the drift's node data on this row
+        h1 = r.x * drift.tau;
+        h2 = r.y * drift.tau;
+    }
+    X[i] = g.b0 + iX * g.hx + (double)a.x + h1;
     Y[i] = g.b2 + iY * g.hy + (double)a.y;
     X[g.N + i] = 1.0 + (double)a.z; Y[g.N + i] = (double)a.w;
-    X[2 * g.N + i] = (double)b.x; Y[2 * g.N + i] = 1.0 + (double)b.y;
+    X[2 * g.N + i] = (double)b.x + h2; Y[2 * g.N + i] = 1.0 + (double)b.y;
     X[3 * g.N + i] = (double)b.z; Y[3 * g.N + i] = (double)b.w;
 }
 
-cudaError_t launch_map_to_planes(const float4* map, const Grid& g, double* X, double* Y, cudaStream_t s)
+cudaError_t launch_map_to_planes(const float4* map, const Grid& g, double* X, double* Y, cudaStream_t s,
+                                 const SepDrift* drift)
 {
-    k_map_to_planes<<<(unsigned)((g.N + 255) / 256), 256, 0, s>>>(map, g, X, Y);
+    SepDrift d{};
+    if (drift) d = *drift;
+    k_map_to_planes<<<(unsigned)((g.N + 255) / 256), 256, 0, s>>>(map, g, X, Y, d);
     return cudaGetLastError();
 }
 

@@ -401,6 +401,8 @@ void EulerSim::release()
     destroy_vlasov_plans(vps_);
     smp_n_ = smp_plan_n_ = vsmp_plan_n_ = 0;
     f(mapm_); f(mapm_new_); f(psiA_); f(psiB_); f(psiP_); f(wfm_); f(stackm_); f(realf_); f(specf_); f(spec4f_);
+    f(d_stack_tau_); d_stack_tau_ = nullptr; stack_tau_cap_ = 0; stack_tau_.clear(); map_tau_ = 0.0;
+    f(drift_rows_); drift_rows_ = nullptr;
     psiP_ = nullptr;
     fused_ = false;
     for (int l = 0; l < kMaxLagrange; ++l) { f(psim_[l]); psim_[l] = nullptr; }
@@ -449,7 +451,10 @@ int EulerSim::translate_ic()
     }
     // plain form, and the Vlasov mixed form: there the kinetic energy weights f by v^2 over the
     // whole velocity range, where an FP32 transform's noise floor (~1e-7 of max f) would show
-    if (mixed_) CMM_LAUNCH(1, launch_compose_m(gc, gf, mapm_, stackm_, n_maps_, src, wdiscm_, real_buf_, stream));
+    SepDrift drift;
+    if (mixed_)
+        CMM_LAUNCH(1, launch_compose_m(gc, gf, mapm_, stackm_, n_maps_, src, wdiscm_, real_buf_, stream, nullptr,
+                                       sep_drift(drift, map_tau_)));
     else CMM_LAUNCH(1, launch_compose_sample(gc, gf, ChiX, ChiY, stack, n_maps_, src, real_buf_, stream));
     CMM_FFT(fft_d2z(pf_, real_buf_, spec_, stream));
     CMM_LAUNCH(1, launch_spec_hermite(spec_, gf, spec4_, stream));
@@ -571,7 +576,8 @@ int EulerSim::ensure_vort()
 int EulerSim::coarse_vort()
 {
     if (mixed_) {
-        CMM_LAUNCH(1, launch_sample_m(gc, gc, gf, mapm_, wfm_, nullptr, vort, stream));
+        SepDrift drift;
+        CMM_LAUNCH(1, launch_sample_m(gc, gc, gf, mapm_, wfm_, nullptr, vort, stream, sep_drift(drift, map_tau_)));
         return kOk;
     }
     CMM_LAUNCH(1, launch_sample_vort(gc, gc, gf, ChiX, ChiY, wfine, 0, vort, gc.NX, stream));
@@ -583,7 +589,8 @@ int EulerSim::sync_fp64_views()
     // mixed form: rebuild the reference-layout FP64 views (map planes, psi
     // levels, fine vorticity planes) used by the writers and cmm_get_field
     if (!mixed_) return kOk;
-    CMM_LAUNCH(1, launch_map_to_planes(mapm_, gc, ChiX, ChiY, stream));
+    SepDrift drift;
+    CMM_LAUNCH(1, launch_map_to_planes(mapm_, gc, ChiX, ChiY, stream, sep_drift(drift, map_tau_)));
     for (int l = 0; l < L; ++l) CMM_LAUNCH(1, launch_float4_to_planes(psim_[l], gp.N, psi[l], stream));
     CMM_LAUNCH(1, launch_float4_to_planes(wfm_, gf.N, wfine, stream));
     for (size_t i = 0; i < partfix_.size(); ++i) {
@@ -620,7 +627,8 @@ int EulerSim::evaluate_potential()
     // evaluate_potential_from_density_hermite (cmm-simulation-host.cu:385-415):
     // f on the vort grid, rho = int f dv - 1, phi from the 1D Poisson solve,
     // psi = phi(x) - h(v) (its Hermite planes written directly, psi is separable)
-    if (mixed_) CMM_LAUNCH(1, launch_sample_m(gc, gv, gf, mapm_, wfm_, realf_, nullptr, stream));
+    SepDrift drift;
+    if (mixed_) CMM_LAUNCH(1, launch_sample_m(gc, gv, gf, mapm_, wfm_, realf_, nullptr, stream, sep_drift(drift, map_tau_)));
     else CMM_LAUNCH(1, launch_sample_vort(gc, gv, gf, ChiX, ChiY, wfine, s.molly_stencil, real_buf_, gv.NX, stream));
     CMM_LAUNCH(2, launch_vlasov_rho(mixed_ ? nullptr : real_buf_, mixed_ ? realf_ : nullptr, gv, vl_part_, vl_rho_, stream));
     CMM_FFT(fft_d2z_1d(vp_.v, vl_rho_, vl_c_[0], stream));
@@ -656,6 +664,7 @@ int EulerSim::vlasov_mesure(double* out)
 
 int EulerSim::reset_map()
 {
+    map_tau_ = 0.0;
     if (mixed_) CMM_LAUNCH(1, launch_init_map_m(mapm_, gc, stream));
     else CMM_LAUNCH(1, launch_init_map(ChiX, ChiY, gc, stream));
     return kOk;
@@ -711,8 +720,39 @@ int EulerSim::advect_m(const double* t, const double* dtv, int lc, int ti_num, i
     a.time_integration_num = ti_num;
     a.rp = gp.NX / gc.NX;
     a.nx_log2 = (gc.NX & (gc.NX - 1)) == 0 ? __builtin_ctz((unsigned)gc.NX) : -1;
+    a.tau64 = map_tau_;
+    a.drows = drift_rows_;
     CMM_LAUNCH(1, launch_advect_m(a, stream));
     std::swap(mapm_, mapm_new_);
+    if (vlasov_) map_tau_ += a.dt64;   // the new map is one (signed) step older
+    return kOk;
+}
+
+const SepDrift* EulerSim::sep_drift(SepDrift& d, double tau) const
+{
+    if (!(mixed_ && vlasov_)) return nullptr;
+    d = SepDrift{};
+    d.rows = drift_rows_;
+    d.gm = gc;
+    d.tau = tau;
+    d.taus = d_stack_tau_;
+    return &d;
+}
+
+int EulerSim::upload_stack_taus()
+{
+    // the stacked maps' ages, for the compositions (Vlasov mixed form)
+    if (!(mixed_ && vlasov_)) return kOk;
+    const int need = std::max(1, (int)stack_tau_.size());
+    if (need > stack_tau_cap_) {
+        if (d_stack_tau_) CMM_CUDA(cudaFree(d_stack_tau_));
+        d_stack_tau_ = nullptr;
+        const int cap = std::max({need, 2 * stack_tau_cap_, 16});
+        CMM_CUDA(cudaMalloc((void**)&d_stack_tau_, sizeof(double) * cap));
+        stack_tau_cap_ = cap;
+    }
+    if (!stack_tau_.empty())
+        CMM_CUDA(cudaMemcpy(d_stack_tau_, stack_tau_.data(), sizeof(double) * stack_tau_.size(), cudaMemcpyHostToDevice));
     return kOk;
 }
 
@@ -819,7 +859,8 @@ int EulerSim::forwarded_positions(const double* frame, double* out)
 
 int EulerSim::incomp(double* out)
 {
-    if (mixed_) CMM_LAUNCH(1, launch_incomp_m(gc, gf.NX / gc.NX, mapm_, d_scal_, stream));
+    SepDrift drift;
+    if (mixed_) CMM_LAUNCH(1, launch_incomp_m(gc, gf.NX / gc.NX, mapm_, d_scal_, stream, sep_drift(drift, map_tau_)));
     else CMM_LAUNCH(1, launch_incomp(gf, gc, ChiX, ChiY, d_scal_, stream));
     CMM_CUDA(cudaMemcpyAsync(h_scal_, d_scal_, sizeof(double), cudaMemcpyDeviceToHost, stream));
     CMM_CUDA(cudaStreamSynchronize(stream));
@@ -893,6 +934,11 @@ int EulerSim::push_stack()
     if (mixed_) {
         size_t mapb = sizeof(float4) * 2 * (size_t)gc.N;
         CMM_CUDA(cudaMemcpyAsync(stackm_ + 2 * (size_t)n_maps_ * gc.N, mapm_, mapb, cudaMemcpyDeviceToDevice, stream));
+        if (vlasov_) {
+            stack_tau_.resize((size_t)n_maps_ + 1);
+            stack_tau_[(size_t)n_maps_] = map_tau_;
+            if ((rc = upload_stack_taus())) return rc;
+        }
     } else {
         double* slot = stack + (size_t)n_maps_ * 8 * gc.N;
         CMM_CUDA(cudaMemcpyAsync(slot, ChiX, sizeof(double) * 4 * gc.N, cudaMemcpyDeviceToDevice, stream));
@@ -927,7 +973,8 @@ int EulerSim::write_map_stack(int map_num, bool forward)
     // expects (its writer puts a forward sub-map under the next backward name at a remap,
     // cmm-euler2d.cu:848, which a later restart would read as a backward sub-map)
     const std::string fw = forward ? "_f" : "";
-    if (mixed_) CMM_LAUNCH(1, launch_map_to_planes(mapm_, gc, ChiX, ChiY, stream));
+    SepDrift drift;
+    if (mixed_) CMM_LAUNCH(1, launch_map_to_planes(mapm_, gc, ChiX, ChiY, stream, sep_drift(drift, map_tau_)));
     std::vector<double> h((size_t)8 * gc.N);
     const double* MX = forward ? ChiX_f : ChiX;
     const double* MY = forward ? ChiY_f : ChiY;
@@ -1026,6 +1073,8 @@ int EulerSim::restart_from_map_stack()
         if (rc) return rc;
     }
     n_maps_ = std::max(n, 0);
+    stack_tau_.assign((size_t)n_maps_, 0.0);   // stored maps are taken with age 0: X - x in full
+    if ((rc = upload_stack_taus())) return rc;
     if (!msg.empty()) { log_.push(msg + "Exitting .."); err = msg; return kErrIO; }
     if (s.verbose >= 2) log_.push("Loaded " + std::to_string(n_maps_) + " maps to map stack");
 
@@ -1245,6 +1294,10 @@ int EulerSim::init()
 
     if ((rc = reset_map())) return rc;
     if (vlasov_ && (rc = vlasov_setup_h())) return rc;
+    if (vlasov_ && mixed_) {   // the free-streaming frame's per-row drift table (SepDrift)
+        if (!drift_rows_) CMM_CUDA(cudaMalloc((void**)&drift_rows_, sizeof(double2) * gc.NY));
+        CMM_LAUNCH(1, launch_drift_rows(vtab_[3], gp, gc, drift_rows_, stream));
+    }
     if (s.forward_map) CMM_LAUNCH(1, launch_init_map(ChiX_f, ChiY_f, gc, stream));
     n_maps_f_ = 0;
     const bool restart = s.restart_time != 0;
@@ -1906,8 +1959,13 @@ int EulerSim::sample_outputs(double t_now, double dt_now)
                 if ((rc = out("Map_ChiX_f", X)) || (rc = out("Map_ChiY_f", Y))) return rc;
             if ((rc = write_forwarded(s.domain_bounds, "/Particle_data/Time_" + tname, false, var))) return rc;
         }
-        if (mixed_) CMM_LAUNCH(1, launch_compose_pos_m(gc, gs, mapm_, stackm_, n_maps_, X, Y, stream));
-        else CMM_LAUNCH(1, launch_compose_pos(gc, gs, ChiX, ChiY, stack, n_maps_, X, Y, stream));
+        if (mixed_) {
+            SepDrift drift;
+            CMM_LAUNCH(1, launch_compose_pos_m(gc, gs, mapm_, stackm_, n_maps_, X, Y, stream,
+                                               sep_drift(drift, map_tau_)));
+        } else {
+            CMM_LAUNCH(1, launch_compose_pos(gc, gs, ChiX, ChiY, stack, n_maps_, X, Y, stream));
+        }
         if (has(var, "Map_b") || has(var, "Chi_b") || all) {
             if ((rc = out("Map_ChiX", X)) || (rc = out("Map_ChiY", Y))) return rc;
         }
@@ -2009,8 +2067,13 @@ int EulerSim::vlasov_sample_outputs(double t_now, double dt_now)
             CMM_LAUNCH(1, launch_compose_fwd(gc, gs, ChiX_f, ChiY_f, stack_f, n_maps_f_, X, Y, stream));
             if ((rc = out("Map_ChiX_f", X)) || (rc = out("Map_ChiY_f", Y))) return rc;
         }
-        if (mixed_) CMM_LAUNCH(1, launch_compose_pos_m(gc, gs, mapm_, stackm_, n_maps_, X, Y, stream));
-        else CMM_LAUNCH(1, launch_compose_pos(gc, gs, ChiX, ChiY, stack, n_maps_, X, Y, stream));
+        if (mixed_) {
+            SepDrift drift;
+            CMM_LAUNCH(1, launch_compose_pos_m(gc, gs, mapm_, stackm_, n_maps_, X, Y, stream,
+                                               sep_drift(drift, map_tau_)));
+        } else {
+            CMM_LAUNCH(1, launch_compose_pos(gc, gs, ChiX, ChiY, stack, n_maps_, X, Y, stream));
+        }
         if (has(var, "Map_b") || has(var, "Chi_b") || all)
             if ((rc = out("Map_ChiX", X)) || (rc = out("Map_ChiY", Y))) return rc;
         InitSource src{};
@@ -2148,8 +2211,13 @@ int EulerSim::zoom_outputs(double t_now, double dt_now)
                     if ((rc = out("Map_ChiX_f", X)) || (rc = out("Map_ChiY_f", Y))) return rc;
                 if ((rc = write_forwarded(b, sub, true, var))) return rc;
             }
-            if (mixed_) CMM_LAUNCH(1, launch_compose_pos_m(gc, gz, mapm_, stackm_, n_maps_, X, Y, stream));
-            else CMM_LAUNCH(1, launch_compose_pos(gc, gz, ChiX, ChiY, stack, n_maps_, X, Y, stream));
+            if (mixed_) {
+                SepDrift drift;
+                CMM_LAUNCH(1, launch_compose_pos_m(gc, gz, mapm_, stackm_, n_maps_, X, Y, stream,
+                                                   sep_drift(drift, map_tau_)));
+            } else {
+                CMM_LAUNCH(1, launch_compose_pos(gc, gz, ChiX, ChiY, stack, n_maps_, X, Y, stream));
+            }
             if (has(var, "Map_b") || has(var, "Chi_b") || all)
                 if ((rc = out("Map_ChiX", X)) || (rc = out("Map_ChiY", Y))) return rc;
             InitSource src{};
@@ -2408,7 +2476,10 @@ int EulerSim::get_field(const std::string& n, void* dst, size_t bytes)
         // FP32 displacement maps -> the reference's planar X | Y layout, one map at a time
         size_t mb = sizeof(double) * 4 * gc.N;
         for (int m = 0; m < n_maps_ && !rc; ++m) {
-            rc = check(launch_map_to_planes(stackm_ + 2 * (size_t)m * gc.N, gc, ChiX_new, ChiY_new, stream), "map_to_planes");
+            SepDrift drift;
+            rc = check(launch_map_to_planes(stackm_ + 2 * (size_t)m * gc.N, gc, ChiX_new, ChiY_new, stream,
+                                            sep_drift(drift, m < (int)stack_tau_.size() ? stack_tau_[(size_t)m] : 0.0)),
+                       "map_to_planes");
             if (!rc) rc = check(cudaMemcpyAsync(d + 2 * m * mb, ChiX_new, mb, cudaMemcpyDeviceToHost, stream), "get_field");
             if (!rc) rc = check(cudaMemcpyAsync(d + (2 * m + 1) * mb, ChiY_new, mb, cudaMemcpyDeviceToHost, stream), "get_field");
         }

@@ -263,6 +263,15 @@ private:
     float4* wfm_ = nullptr;          // fine vorticity nodes
     float4* wdiscm_ = nullptr;       // discrete initial vorticity nodes (FP32 Hermite)
     float4* stackm_ = nullptr;       // n maps, 2*Nc float4 each
+    // Vlasov mixed form: the maps are stored in the free-streaming frame (SepDrift), which needs
+    // each map's age: the active map's, and every stacked map's (host and device copies)
+    double map_tau_ = 0.0;
+    double2* drift_rows_ = nullptr;  // SepDrift's per-row table (built once from h)
+    std::vector<double> stack_tau_;
+    double* d_stack_tau_ = nullptr;
+    int stack_tau_cap_ = 0;
+    const SepDrift* sep_drift(SepDrift& d, double tau) const;   // null unless the Vlasov mixed form
+    int upload_stack_taus();
     std::vector<unsigned long long*> partfix_;   // tracer positions, 64-bit fixed point (x, y interleaved)
     std::vector<float2*> velm_;                  // inertial velocity state (FP32), null for tracer sets
 

@@ -66,16 +66,20 @@ __device__ __forceinline__ void rows_prefetch(const RowsArgs& a, V* dst, int row
 // GTW: the twiddle table is read from global memory (too large to stage next to the data).
 // Otherwise two data buffers: while a group is transformed, the next group's rows arrive
 // by cp.async.
+// FP32 rows transform through a scratch buffer (block_fft_pp: one barrier per pass)
+template <typename T> struct RowsPP { static constexpr bool value = std::is_same<T, float>::value; };
+
 template <typename T, int FAM, int VPT, int MAXT, bool GTW>
 __global__ void __launch_bounds__(MAXT, 1) k_rows_r2c(RowsArgs a)
 {
     using V = typename Cx<T>::V;
-    constexpr bool DB = !GTW;
+    constexpr bool DB = !GTW, PP = RowsPP<T>::value;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = a.P.n;
     V* cur = reinterpret_cast<V*>(smem_raw);
-    V* nxt = cur + padded_len<V>(a.nb * n);
-    V* stw = nxt + padded_len<V>(a.nb * n);
+    V* nxt = cur + (DB ? padded_len<V>(a.nb * n) : 0);
+    V* tmp = nxt + padded_len<V>(a.nb * n);   // ping-pong scratch (PP)
+    V* stw = tmp + (PP ? padded_len<V>(a.nb * n) : 0);
     if (!GTW) load_table(stw, reinterpret_cast<const V*>(a.tw), a.P.tlen + n + 1);
     const V* tw = GTW ? reinterpret_cast<const V*>(a.tw) : stw;
     const V* post = tw + a.P.tlen;
@@ -99,11 +103,13 @@ __global__ void __launch_bounds__(MAXT, 1) k_rows_r2c(RowsArgs a)
             }
         }
         __syncthreads();
-        block_fft<VPT, FAM>(cur, nb, a.P, tw, false);
+        const V* res = cur;
+        if (PP) res = block_fft_pp<VPT, FAM>(cur, tmp, nb, a.P, tw, false);
+        else block_fft<VPT, FAM>(cur, nb, a.P, tw, false);
         for (int b = 0; b < nb; ++b) {
             const int g = row0 + b, item = g / a.rows_per_item, r = g - item * a.rows_per_item;
             V* dst = reinterpret_cast<V*>(a.out) + item * a.odist + r * a.old;
-            for (int k = threadIdx.x; k < a.kio; k += blockDim.x) dst[k] = r2c_bin(cur, b * n, n, k, post);
+            for (int k = threadIdx.x; k < a.kio; k += blockDim.x) dst[k] = r2c_bin(res, b * n, n, k, post);
         }
         if (DB) {
             V* t = cur;
@@ -417,11 +423,13 @@ static cudaError_t rows_launch(const Plan2D& p, bool forward, const void* in, lo
     const long long groups = (a.rows_total + a.nb - 1) / a.nb;
     // with its table staged the forward kernel double-buffers its rows (cp.async of the next
     // group); when that does not fit, one buffer and the table in global memory
+    // (the FP32 forward kernel adds a ping-pong scratch buffer: block_fft_pp)
     const int tl = p.rx.tlen + n + 1;
     const size_t data = p.dbl ? smem_bytes<double>(a.nb * n, 0) : smem_bytes<float>(a.nb * n, 0);
-    const size_t full = data * (forward ? 2 : 1) + (p.dbl ? sizeof(double2) : sizeof(float2)) * (size_t)tl;
+    const int pp = forward && !p.dbl ? 1 : 0;
+    const size_t full = data * (forward ? 2 + pp : 1) + (p.dbl ? sizeof(double2) : sizeof(float2)) * (size_t)tl;
     const bool gtw = full > (size_t)kMaxSmem;
-    const size_t sm = gtw ? data : full;
+    const size_t sm = gtw ? data * (1 + pp) : full;
     if (sm > (size_t)kMaxSmem) return cudaErrorInvalidValue;
     const bool ok = p.dbl ? launch_rows<double>(fam, sh, gtw, forward, groups, thr, sm, s, a)
                           : launch_rows<float>(fam, sh, gtw, forward, groups, thr, sm, s, a);

@@ -244,6 +244,82 @@ __device__ __forceinline__ void block_fft(V* s, int nb, const RadixPlan& P, cons
     }
 }
 
+// ---------------------------------------------------------------- ping-pong passes
+// The same Stockham pass from `in` to a second buffer `out`: no thread overwrites what
+// another still has to read, so a pass needs one barrier (after its writes) instead of two,
+// and each butterfly is stored as soon as it is computed (its values leave the registers).
+// Results are identical to pass().
+template <int R, int VPT, bool POW2, typename V>
+__device__ __forceinline__ void pass_pp(const V* in, V* out, int nb, int n, int p, int lnr, int lp, const V* ptw,
+                                        bool inv)
+{
+    constexpr int B = (VPT + R - 1) / R;
+    const int nR = n / R;
+    const int total = nb * nR;
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+        const int t = threadIdx.x + j * blockDim.x;
+        if (t < total) {
+            const int b = POW2 ? t >> lnr : t / nR;
+            const int i = t - b * nR;
+            const int k = POW2 ? i & ((1 << lp) - 1) : i % p;
+            const int base = b * n;
+            V v[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[r] = in[pad<V>(base + i + r * nR)];
+            if (k != 0) {
+                const V* tk = ptw + k * (R - 1);
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    V w = tk[r - 1];
+                    if (inv) w = cconj(w);
+                    v[r] = cmul(v[r], w);
+                }
+            }
+            if (R == 2) dft2(v);
+            else if (R == 4) dft4(v, inv);
+            else if (R == 8) dft8(v, inv);
+            else if (R == 3) dft3(v, inv);
+            else dft_generic<R>(v, inv, ptw + p * (R - 1));
+            const int dst = base + (i - k) * R + k;
+#pragma unroll
+            for (int r = 0; r < R; ++r) out[pad<V>(dst + r * p)] = v[r];
+        }
+    }
+    __syncthreads();
+}
+
+// block_fft with a second buffer: the transforms start in `a`, `b` is scratch; returns the
+// buffer that holds the results (a after an even number of passes, b after an odd one).
+// The caller synchronises after filling `a`; the last pass ends with a barrier.
+template <int VPT, int FAM, typename V>
+__device__ __forceinline__ V* block_fft_pp(V* a, V* b, int nb, const RadixPlan& P, const V* tw, bool inv)
+{
+    constexpr bool P2 = FAM == kPow2;
+    int p = 1;
+    V* src = a;
+    V* dst = b;
+    for (int q = 0; q < P.np; ++q) {
+        const int R = P.r[q], lnr = P.lnr[q], lp = P.lp[q];
+        const V* ptw = tw + P.toff[q];
+        if (R == 8) pass_pp<8, VPT, P2>(src, dst, nb, P.n, p, lnr, lp, ptw, inv);
+        else if (R == 4) pass_pp<4, VPT, P2>(src, dst, nb, P.n, p, lnr, lp, ptw, inv);
+        else if (R == 2) pass_pp<2, VPT, P2>(src, dst, nb, P.n, p, lnr, lp, ptw, inv);
+        else if (FAM >= kPow2x3 && R == 3) pass_pp<3, VPT, false>(src, dst, nb, P.n, p, lnr, lp, ptw, inv);
+        else if (FAM == kAny) {
+            if (R == 5) pass_pp<5, VPT, false>(src, dst, nb, P.n, p, lnr, lp, ptw, inv);
+            else if (R == 7) pass_pp<7, VPT, false>(src, dst, nb, P.n, p, lnr, lp, ptw, inv);
+            else if (R == 11) pass_pp<11, VPT, false>(src, dst, nb, P.n, p, lnr, lp, ptw, inv);
+            else pass_pp<13, VPT, false>(src, dst, nb, P.n, p, lnr, lp, ptw, inv);
+        }
+        p *= R;
+        V* t = src;
+        src = dst;
+        dst = t;
+    }
+    return src;
+}
+
 // the twiddle table (len entries) into shared memory
 template <typename V>
 __device__ __forceinline__ void load_table(V* dst, const V* __restrict__ src, int len)

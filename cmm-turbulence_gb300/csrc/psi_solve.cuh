@@ -116,17 +116,23 @@ __device__ __forceinline__ float2 plane_mode<float2>(const float2* s, int off, i
     return q == 2 ? Py : make_float2(-Py.y * kx, Py.x * kx);
 }
 
+// FP32: the transforms run through scratch buffers (fft::block_fft_pp, one barrier per pass)
+template <typename T> struct UsePP { static constexpr bool value = sizeof(T) == 4; };
+
 // groups (C kept columns, plane q) grid-strided; dynamic shared memory: padded(C NYv) +
-// padded(C NYp) values + the two column plans' tables
+// padded(C NYp) values (twice for FP32: the scratch buffers) + the two column plans' tables
 template <typename T, int FAM, int VPT>
 __global__ void __launch_bounds__(Shape<T>::MAXT, 1) k_psi_cols(ColsArgs a)
 {
     using V = typename fft::Cx<T>::V;
+    constexpr bool PP = UsePP<T>::value;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nv = a.gv.NY, np = a.gp.NY, C = a.C;
     V* A = reinterpret_cast<V*>(smem_raw);
     V* B = A + fft::padded_len<V>(C * nv);
-    V* tv = B + fft::padded_len<V>(C * np);
+    V* A2 = B + fft::padded_len<V>(C * np);                 // scratch (PP)
+    V* B2 = A2 + (PP ? fft::padded_len<V>(C * nv) : 0);
+    V* tv = B2 + (PP ? fft::padded_len<V>(C * np) : 0);
     V* tp = tv + a.Pv.tlen;
     fft::load_table(tv, reinterpret_cast<const V*>(a.twv), a.Pv.tlen);
     fft::load_table(tp, reinterpret_cast<const V*>(a.twp), a.Pp.tlen);
@@ -140,17 +146,21 @@ __global__ void __launch_bounds__(Shape<T>::MAXT, 1) k_psi_cols(ColsArgs a)
             A[fft::pad<V>(c * nv + r)] = col < a.kv ? w1[r * a.ld1 + col] : fft::mk((T)0, (T)0);
         }
         __syncthreads();
-        fft::block_fft<VPT, FAM>(A, C, a.Pv, tv, false);
+        const V* FA = A;
+        if (PP) FA = fft::block_fft_pp<VPT, FAM>(A, A2, C, a.Pv, tv, false);
+        else fft::block_fft<VPT, FAM>(A, C, a.Pv, tv, false);
         for (int e = threadIdx.x; e < C * np; e += blockDim.x) {
             const int c = e / np, r = e - c * np;
-            B[fft::pad<V>(e)] = plane_mode<V>(A, c * nv, q, col0 + c, r, a.gv, a.gp, a.freq);
+            B[fft::pad<V>(e)] = plane_mode<V>(FA, c * nv, q, col0 + c, r, a.gv, a.gp, a.freq);
         }
         __syncthreads();
-        fft::block_fft<VPT, FAM>(B, C, a.Pp, tp, true);
+        const V* FB = B;
+        if (PP) FB = fft::block_fft_pp<VPT, FAM>(B, B2, C, a.Pp, tp, true);
+        else fft::block_fft<VPT, FAM>(B, C, a.Pp, tp, true);
         V* w2 = reinterpret_cast<V*>(a.w2) + (long long)q * np * a.ld2;
         for (int e = threadIdx.x; e < C * np; e += blockDim.x) {
             const int c = e % C, r = e / C, col = col0 + c;
-            if (col < a.ncols) w2[r * a.ld2 + col] = B[fft::pad<V>(c * np + r)];
+            if (col < a.ncols) w2[r * a.ld2 + col] = FB[fft::pad<V>(c * np + r)];
         }
     }
 }
@@ -167,17 +177,18 @@ struct RowsInvArgs {
 };
 
 // Epi::store(iX, iY, f, fx, fy, fxy): the four Hermite planes' values at psi node (iX, iY);
-// groups of nb rows grid-strided; dynamic shared memory: padded(4 nb nx/2) values + the
-// row plan's table
+// groups of nb rows grid-strided; dynamic shared memory: padded(4 nb nx/2) values (twice for
+// FP32: the scratch buffer) + the row plan's table
 template <typename T, int FAM, int VPT, class Epi>
 __global__ void __launch_bounds__(Shape<T>::MAXT, 1) k_psi_rows_inv(RowsInvArgs a, Epi epi)
 {
     using V = typename fft::Cx<T>::V;
+    constexpr bool PP = UsePP<T>::value;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = a.nx / 2;
     V* s = reinterpret_cast<V*>(smem_raw);
-    const T* sr = reinterpret_cast<const T*>(smem_raw);
-    V* tw = s + fft::padded_len<V>(4 * a.nb * n);
+    V* s2 = s + fft::padded_len<V>(4 * a.nb * n);          // scratch (PP)
+    V* tw = s2 + (PP ? fft::padded_len<V>(4 * a.nb * n) : 0);
     fft::load_table(tw, reinterpret_cast<const V*>(a.tw), a.P.tlen + n + 1);
     const V* post = tw + a.P.tlen;
     const V zero = fft::mk((T)0, (T)0);
@@ -197,7 +208,10 @@ __global__ void __launch_bounds__(Shape<T>::MAXT, 1) k_psi_rows_inv(RowsInvArgs 
             }
         }
         __syncthreads();
-        fft::block_fft<VPT, FAM>(s, 4 * nb, a.P, tw, true);
+        const V* res = s;
+        if (PP) res = fft::block_fft_pp<VPT, FAM>(s, s2, 4 * nb, a.P, tw, true);
+        else fft::block_fft<VPT, FAM>(s, 4 * nb, a.P, tw, true);
+        const T* sr = reinterpret_cast<const T*>(res);
         for (int b = 0; b < nb; ++b) {
             for (int iX = threadIdx.x; iX < a.nx; iX += blockDim.x) {
                 const int base = 4 * b * n + (iX >> 1), c = iX & 1;
@@ -251,8 +265,9 @@ Layout make_layout(const Grid& gv, const Grid& gp, double freq, const fft::Plan2
     L.nb_inv = std::max(1, kBlockValues / (4 * np));
     L.C = 1;
     while (2 * L.C * std::max(gv.NY, gp.NY) <= kBlockValues && L.C < 4) L.C *= 2;
-    L.smem_inv = sizeof(V) * ((size_t)fft::padded_len<V>(4 * L.nb_inv * np) + (size_t)pp.rx.tlen + (size_t)np + 1);
-    L.smem_cols = sizeof(V) * ((size_t)fft::padded_len<V>(L.C * gv.NY) + (size_t)fft::padded_len<V>(L.C * gp.NY) +
+    const size_t pp2 = UsePP<T>::value ? 2 : 1;   // FP32: ping-pong scratch buffers
+    L.smem_inv = sizeof(V) * (pp2 * (size_t)fft::padded_len<V>(4 * L.nb_inv * np) + (size_t)pp.rx.tlen + (size_t)np + 1);
+    L.smem_cols = sizeof(V) * (pp2 * ((size_t)fft::padded_len<V>(L.C * gv.NY) + (size_t)fft::padded_len<V>(L.C * gp.NY)) +
                                (size_t)pv.ry.tlen + (size_t)pp.ry.tlen);
     if (L.smem_cols > 200 * 1024 || L.smem_inv > 200 * 1024) return L;
     L.w1_values = (long long)gv.NY * L.ld;

@@ -120,6 +120,79 @@ __global__ void __launch_bounds__(MAXT, 1) k_rows_r2c(RowsArgs a)
     if (DB) asm volatile("cp.async.wait_group 0;");
 }
 
+// FP32 rows of a compile-time power-of-two packed length N (block_fft_s: constant index
+// arithmetic), kStaticThreads threads of kStaticVPT values, nb = kStaticThreads kStaticVPT / N
+// rows per group.  The rows arrive unpadded by 16-byte cp.async.cg (past L1, into the
+// second of two row buffers while the first is transformed) and the first pass reads them
+// so; GT: the twiddle tables are read from global memory through L1, else staged in
+// shared memory.  Needs 16-byte aligned rows.
+constexpr int kStaticThreads = 256, kStaticVPT = 8;
+
+template <int N>
+__device__ __forceinline__ void rows_prefetch_s(const RowsArgs& a, float2* dst, int row0)
+{
+    const int nb = min(a.nb, a.rows_total - row0);
+    for (int b = 0; b < nb; ++b) {
+        const int g = row0 + b, item = g / a.rows_per_item, r = g - item * a.rows_per_item;
+        const float* src = reinterpret_cast<const float*>(a.in) + item * a.idist + r * a.ild;
+        for (int m = threadIdx.x; m < N / 2; m += kStaticThreads) {
+            const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + b * N + 2 * m);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(src + 4 * m));
+        }
+    }
+}
+
+template <int N, bool GT>
+__global__ void __launch_bounds__(kStaticThreads, GT ? 4 : 3) k_rows_r2c_s(RowsArgs a)
+{
+    using V = float2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int len = (padded_len<V>(a.nb * N) + 1) & ~1;   // even: the buffers stay 16-byte aligned
+    V* cur = reinterpret_cast<V*>(smem_raw);
+    V* nxt = cur + len;
+    V* tmp = nxt + len;
+    const V* tw = reinterpret_cast<const V*>(a.tw);
+    if (!GT) {
+        V* stw = tmp + len;
+        load_table(stw, tw, sp::tlen(N) + N + 1);
+        tw = stw;
+    }
+    const V* post = tw + sp::tlen(N);
+    const int stride = gridDim.x * a.nb;
+    if (blockIdx.x * a.nb < a.rows_total) rows_prefetch_s<N>(a, cur, blockIdx.x * a.nb);
+    asm volatile("cp.async.commit_group;");
+    for (int row0 = blockIdx.x * a.nb; row0 < a.rows_total; row0 += stride) {
+        const int nb = min(a.nb, a.rows_total - row0);
+        __syncthreads();   // the previous group's bins are read: its buffers may be refilled
+        if (row0 + stride < a.rows_total) rows_prefetch_s<N>(a, nxt, row0 + stride);
+        asm volatile("cp.async.commit_group;");
+        asm volatile("cp.async.wait_group 1;");
+        __syncthreads();
+        const V* res = block_fft_s<N, kStaticVPT, false, GT, true>(cur, tmp, nb, tw);
+        for (int b = 0; b < nb; ++b) {
+            const int g = row0 + b, item = g / a.rows_per_item, r = g - item * a.rows_per_item;
+            V* dst = reinterpret_cast<V*>(a.out) + item * a.odist + r * a.old;
+            for (int k = threadIdx.x; k < a.kio; k += kStaticThreads) dst[k] = r2c_bin(res, b * N, N, k, post);
+        }
+        V* t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+    asm volatile("cp.async.wait_group 0;");
+}
+
+// packed lengths with a static kernel
+#define CMM_FFT_STATIC_ROWS(X) X(128) X(256) X(512) X(1024) X(2048)
+constexpr bool kStaticGT = false;   // tables staged in shared memory
+// table length of the power-of-two plan of length n (host side of sp::tlen)
+inline int sp_tlen_pow2(int n)
+{
+#define X(N) if (n == N) return sp::tlen(N);
+    CMM_FFT_STATIC_ROWS(X)
+#undef X
+    return 0;
+}
+
 template <typename T, int FAM, int VPT, int MAXT, bool GTW>
 __global__ void __launch_bounds__(MAXT, 1) k_rows_c2r(RowsArgs a)
 {
@@ -229,6 +302,39 @@ void configure()
 #define X(T, F, V, M, G) configure_one<T, F, V, M, G>();
     CMM_FFT_SHAPES(X)
 #undef X
+#define X(N)                                                                                        \
+    cudaFuncSetAttribute(k_rows_r2c_s<N, kStaticGT>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
+    CMM_FFT_STATIC_ROWS(X)
+#undef X
+}
+
+// shared memory of k_rows_r2c_s<N, GT> with nb rows per group
+size_t static_rows_smem(int n, int nb, bool gt)
+{
+    const size_t len = (size_t)((padded_len<float2>(nb * n) + 1) & ~1);
+    return sizeof(float2) * (3 * len + (gt ? 0 : (size_t)sp_tlen_pow2(n) + (size_t)n + 1));
+}
+
+// the static FP32 R2C kernel of packed length n, or false when there is none
+bool launch_rows_static(int n, long long groups, size_t sm, cudaStream_t s, const RowsArgs& a)
+{
+#define X(N)                                                                                           \
+    if (n == N) {                                                                                      \
+        const void* f = reinterpret_cast<const void*>(k_rows_r2c_s<N, kStaticGT>);                     \
+        k_rows_r2c_s<N, kStaticGT><<<resident_grid(f, kStaticThreads, sm, groups), kStaticThreads, sm, s>>>(a); \
+        return true;                                                                                   \
+    }
+    CMM_FFT_STATIC_ROWS(X)
+#undef X
+    return false;
+}
+
+bool has_static_rows(int n)
+{
+#define X(N) if (n == N) return true;
+    CMM_FFT_STATIC_ROWS(X)
+#undef X
+    return false;
 }
 
 template <typename T>
@@ -411,6 +517,15 @@ static cudaError_t rows_launch(const Plan2D& p, bool forward, const void* in, lo
     a.rows_per_item = rows_per_item;
     a.rows_total = rows_per_item * items;
     a.kio = kio;
+    if (forward && !p.dbl && has_static_rows(n) && p.rx.tlen == sp_tlen_pow2(n) && aligned(in, 16) && ild % 4 == 0 &&
+        idist % 4 == 0) {
+        a.nb = kStaticThreads * kStaticVPT / n;
+        a.P = p.rx;
+        a.tw = p.twx;
+        const long long groups = (a.rows_total + a.nb - 1) / a.nb;
+        return launch_rows_static(n, groups, static_rows_smem(n, a.nb, kStaticGT), s, a) ? cudaGetLastError()
+                                                                                        : cudaErrorInvalidValue;
+    }
     // rows per group: about kBlockValues values, at least one row
     const int fam = family_of(p.rx);
     a.nb = n >= kBlockValues ? 1 : kBlockValues / n;

@@ -320,6 +320,120 @@ __device__ __forceinline__ V* block_fft_pp(V* a, V* b, int nb, const RadixPlan& 
     return src;
 }
 
+// ---------------------------------------------------------------- compile-time plans
+// The radix sequence, spans and table offsets of make_radix_plan for a length known at
+// compile time (power of two: 8s, then a 4, or 4 4 in place of a trailing 8 2, or a 2).
+namespace sp {
+constexpr int radix(int n, int q)
+{
+    int rs[kMaxPasses] = {};
+    int c = 0, m = n;
+    while (m % 8 == 0) { rs[c++] = 8; m /= 8; }
+    if (m % 4 == 0) { rs[c++] = 4; m /= 4; }
+    if (m % 2 == 0) {
+        if (c > 0 && rs[c - 1] == 8) { rs[c - 1] = 4; rs[c++] = 4; }
+        else rs[c++] = 2;
+        m /= 2;
+    }
+    return q < c ? rs[q] : 1;
+}
+constexpr int npass(int n) { int c = 0; while (radix(n, c) > 1) ++c; return c; }
+constexpr int span(int n, int q) { int s = 1; for (int i = 0; i < q; ++i) s *= radix(n, i); return s; }
+constexpr int toff(int n, int q) { int o = 0; for (int i = 0; i < q; ++i) o += span(n, i) * (radix(n, i) - 1); return o; }
+constexpr int tlen(int n) { return toff(n, npass(n)); }
+constexpr bool pow2(int n) { return n >= 2 && (n & (n - 1)) == 0; }
+// true when (x + c) >> S = (x >> S) + (c >> S) for every first index x and offset c of the
+// butterflies of pass q of length n (see padc), over enough transforms b to cycle b n mod 2^S
+constexpr bool pad_linear(int n, int q, int S)
+{
+    const int R = radix(n, q), P = span(n, q), nR = n / R;
+    const int nbt = n >= (1 << S) ? 2 : 2 * ((1 << S) / n) + 1;
+    for (int t = 0; t < nbt * nR; ++t) {
+        const int b = t / nR, i = t % nR, k = i % P;
+        const int x0 = b * n + i, d0 = b * n + (i - k) * R + k;
+        for (int r = 0; r < R; ++r) {
+            if (((x0 + r * nR) >> S) != (x0 >> S) + ((r * nR) >> S)) return false;
+            if (((d0 + r * P) >> S) != (d0 >> S) + ((r * P) >> S)) return false;
+        }
+    }
+    return true;
+}
+}  // namespace sp
+
+template <typename V> struct PadShift;
+template <> struct PadShift<float2> { static constexpr int value = 5; };
+template <> struct PadShift<double2> { static constexpr int value = 3; };
+
+// Offsets inside a pass.  pad(x) = x + (x >> S) is not linear, but for the accesses of one
+// butterfly of a power-of-two pass it is: a butterfly reads x0 + r n/R and writes
+// d0 + r p (r < R), where x0 = b n + i (i < n/R) and d0 = b n + (i - k) R + k (k < p).  With
+// L = 2^S: a stride (n/R or p) of at least L makes every offset a multiple of L; a smaller
+// stride divides L, the offsets' low S bits are multiples of it, and the low S bits of x0
+// (d0) leave room for them below L.  Either way no carry crosses bit S, (x0 + c) >> S =
+// (x0 >> S) + (c >> S) and pad(x0 + c) = pad(x0) + padc(c): one address register per
+// butterfly and an immediate per value.  sp::pad_linear checks this for every instantiated
+// pass at compile time.
+template <typename V> __host__ __device__ constexpr int padc(int c) { return c + (c >> PadShift<V>::value); }
+
+// pass Q of the length-N plan from `in` to `out` (ping-pong, one barrier), nb transforms,
+// VPT values per thread of the block (nb N <= VPT blockDim.x).  Every index is a shift or
+// mask by a constant.  The k = 0 twiddles (exactly 1) are applied like the others: the
+// values equal those of pass_pp up to the sign of zeros.
+// GT: the table is in global memory (read through the L1 cache), else in shared memory.
+// UIN: `in` holds the transforms unpadded (x at in[b n + i]): the first pass may read a
+// buffer filled by 16-byte copies (its reads, consecutive i per warp, need no padding).
+template <int N, int Q, int VPT, bool INV, bool GT, bool UIN = false, typename V>
+__device__ __forceinline__ void spass(const V* __restrict__ in, V* __restrict__ out, int nb, const V* tw)
+{
+    constexpr int R = sp::radix(N, Q), P = sp::span(N, Q), nR = N / R, B = (VPT + R - 1) / R;
+    static_assert(sp::pow2(N), "static passes are for power-of-two lengths");
+    static_assert(sp::pad_linear(N, Q, PadShift<V>::value), "padded offsets of this pass are not constants");
+    const int total = nb * nR;
+    const V* ptw = tw + sp::toff(N, Q);
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+        const int t = threadIdx.x + j * blockDim.x;
+        if (t < total) {
+            const int b = t / nR, i = t % nR, k = i % P;
+            const int x0 = b * N + i, d0 = b * N + (i - k) * R + k;
+            const V* src = in + (UIN ? x0 : pad<V>(x0));
+            V v[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[r] = src[UIN ? r * nR : padc<V>(r * nR)];
+            if (P > 1) {
+                const V* tk = ptw + k * (R - 1);
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    V w = GT ? __ldg(tk + r - 1) : tk[r - 1];
+                    if (INV) w = cconj(w);
+                    v[r] = cmul(v[r], w);
+                }
+            }
+            if (R == 2) dft2(v);
+            else if (R == 4) dft4(v, INV);
+            else dft8(v, INV);
+            V* dst = out + pad<V>(d0);
+#pragma unroll
+            for (int r = 0; r < R; ++r) dst[padc<V>(r * P)] = v[r];
+        }
+    }
+    __syncthreads();
+}
+
+// every pass of nb length-N transforms (N a power of two) between a and b (both of
+// padded_len(nb N) values); returns the buffer holding the results.  UIN0: a holds the
+// input unpadded.  The caller synchronises after filling a.
+template <int N, int VPT, bool INV, bool GT, bool UIN0 = false, int Q = 0, typename V>
+__device__ __forceinline__ V* block_fft_s(V* a, V* b, int nb, const V* tw)
+{
+    if constexpr (Q == sp::npass(N)) {
+        return a;
+    } else {
+        spass<N, Q, VPT, INV, GT, UIN0 && Q == 0>(a, b, nb, tw);
+        return block_fft_s<N, VPT, INV, GT, false, Q + 1>(b, a, nb, tw);
+    }
+}
+
 // the twiddle table (len entries) into shared memory
 template <typename V>
 __device__ __forceinline__ void load_table(V* dst, const V* __restrict__ src, int len)

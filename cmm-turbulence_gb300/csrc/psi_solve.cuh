@@ -89,11 +89,10 @@ __device__ __forceinline__ double2 plane_mode<double2>(const double2* s, int off
     return q == 2 ? Py : make_double2(-Py.y * kx, Py.x * kx);
 }
 
-template <>
-__device__ __forceinline__ float2 plane_mode<float2>(const float2* s, int off, int q, int iXc, int iYc, const Grid& gv,
-                                                     const Grid& gp, double freqd)
+// FP32 form with 1 / N_v and the cut-off already rounded to float
+__device__ __forceinline__ float2 plane_mode_f(const float2* s, int off, int q, int iXc, int iYc, const Grid& gv,
+                                               const Grid& gp, float freq, float inv_nv)
 {
-    const float freq = (float)freqd, inv_nv = (float)(1.0 / (double)gv.N);
     const bool hx = 2 * iXc > gp.NX, hy = 2 * iYc > gp.NY;
     const int fX = hx ? gp.NX - iXc : iXc, fY = hy ? gp.NY - iYc : iYc;
     float2 P = make_float2(0.f, 0.f);
@@ -114,6 +113,13 @@ __device__ __forceinline__ float2 plane_mode<float2>(const float2* s, int off, i
     if (q == 1) return make_float2(-P.y * kx, P.x * kx);
     const float2 Py = make_float2(-P.y * ky, P.x * ky);
     return q == 2 ? Py : make_float2(-Py.y * kx, Py.x * kx);
+}
+
+template <>
+__device__ __forceinline__ float2 plane_mode<float2>(const float2* s, int off, int q, int iXc, int iYc, const Grid& gv,
+                                                     const Grid& gp, double freqd)
+{
+    return plane_mode_f(s, off, q, iXc, iYc, gv, gp, (float)freqd, (float)(1.0 / (double)gv.N));
 }
 
 // FP32: the transforms run through scratch buffers (fft::block_fft_pp, one barrier per pass)
@@ -222,6 +228,119 @@ __global__ void __launch_bounds__(Shape<T>::MAXT, 1) k_psi_rows_inv(RowsInvArgs 
     }
 }
 
+// ---------------------------------------------------------------- static FP32 kernels
+// The same two passes for power-of-two lengths known at compile time (fft::block_fft_s:
+// every index a constant shift or mask), kStaticThreads threads.  GT: the twiddle tables
+// are read from global memory through L1 (shared memory holds only the data), else they
+// are staged in shared memory.
+constexpr int kStaticThreads = 256;
+
+// groups (kept column, block of PQ planes), the column's PQ plane groups adjacent; the
+// forward column transform (length NV) once per group, the PQ inverse transforms (length
+// NP) as one batch.  Shared memory: padded(NV) twice, padded(PQ NP) twice (and the tables).
+template <int NV, int NP, int PQ, bool GT>
+__host__ __device__ constexpr size_t cols_s_smem()
+{
+    return sizeof(float2) * (2 * (size_t)fft::padded_len<float2>(NV) + 2 * (size_t)fft::padded_len<float2>(PQ * NP) +
+                             (GT ? 0 : (size_t)fft::sp::tlen(NV) + (size_t)fft::sp::tlen(NP)));
+}
+
+template <int NV, int NP, int PQ, bool GT>
+__global__ void __launch_bounds__(kStaticThreads, 3) k_psi_cols_s(ColsArgs a)
+{
+    using V = float2;
+    constexpr int VF = (NV + kStaticThreads - 1) / kStaticThreads, VI = (PQ * NP + kStaticThreads - 1) / kStaticThreads;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    V* A = reinterpret_cast<V*>(smem_raw);
+    V* A2 = A + fft::padded_len<V>(NV);
+    V* B = A2 + fft::padded_len<V>(NV);
+    V* B2 = B + fft::padded_len<V>(PQ * NP);
+    const V* tv = reinterpret_cast<const V*>(a.twv);
+    const V* tp = reinterpret_cast<const V*>(a.twp);
+    if (!GT) {
+        V* stv = B2 + fft::padded_len<V>(PQ * NP);
+        V* stp = stv + fft::sp::tlen(NV);
+        fft::load_table(stv, tv, fft::sp::tlen(NV));
+        fft::load_table(stp, tp, fft::sp::tlen(NP));
+        tv = stv;
+        tp = stp;
+    }
+    const V* w1 = reinterpret_cast<const V*>(a.w1);
+    const float freq = (float)a.freq, inv_nv = (float)(1.0 / (double)a.gv.N);
+    constexpr int nq = 4 / PQ;
+    for (int grp = blockIdx.x; grp < nq * a.ncols; grp += gridDim.x) {
+        const int col = grp / nq, q0 = (grp - col * nq) * PQ;
+        __syncthreads();   // the previous group's outputs are read
+        for (int r = threadIdx.x; r < NV; r += kStaticThreads)
+            A[fft::pad<V>(r)] = col < a.kv ? w1[r * a.ld1 + col] : fft::mk(0.f, 0.f);
+        __syncthreads();
+        const V* FA = fft::block_fft_s<NV, VF, false, GT>(A, A2, 1, tv);
+        for (int e = threadIdx.x; e < PQ * NP; e += kStaticThreads) {
+            const int qq = e / NP, r = e % NP;
+            B[fft::pad<V>(e)] = plane_mode_f(FA, 0, q0 + qq, col, r, a.gv, a.gp, freq, inv_nv);
+        }
+        __syncthreads();
+        const V* FB = fft::block_fft_s<NP, VI, true, GT>(B, B2, PQ, tp);
+        V* w2 = reinterpret_cast<V*>(a.w2) + (long long)q0 * NP * a.ld2 + col;
+        for (int e = threadIdx.x; e < PQ * NP; e += kStaticThreads) w2[e * a.ld2] = FB[fft::pad<V>(e)];
+    }
+}
+
+// groups of NBR psi rows (the four planes of each as one batch of 4 NBR transforms of the
+// packed length N = nx / 2).  Shared memory: padded(4 NBR N) twice (and the table).
+template <int N, int NBR, bool GT>
+__host__ __device__ constexpr size_t rows_inv_s_smem()
+{
+    return sizeof(float2) * (2 * (size_t)fft::padded_len<float2>(4 * NBR * N) + (GT ? 0 : (size_t)fft::sp::tlen(N) + N + 1));
+}
+
+template <int N, int NBR, bool GT, class Epi>
+__global__ void __launch_bounds__(kStaticThreads, 4) k_psi_rows_inv_s(RowsInvArgs a, Epi epi)
+{
+    using V = float2;
+    constexpr int VPT = (4 * NBR * N + kStaticThreads - 1) / kStaticThreads;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    V* s = reinterpret_cast<V*>(smem_raw);
+    V* s2 = s + fft::padded_len<V>(4 * NBR * N);
+    const V* tw = reinterpret_cast<const V*>(a.tw);
+    if (!GT) {
+        V* stw = s2 + fft::padded_len<V>(4 * NBR * N);
+        fft::load_table(stw, tw, fft::sp::tlen(N) + N + 1);
+        tw = stw;
+    }
+    const V* post = tw + fft::sp::tlen(N);
+    const V zero = fft::mk(0.f, 0.f);
+    const V* w2 = reinterpret_cast<const V*>(a.w2);
+    for (int row0 = blockIdx.x * NBR; row0 < a.ny; row0 += gridDim.x * NBR) {
+        const int nb = min(NBR, a.ny - row0);
+        __syncthreads();
+        // transform t = 4 b + q: plane q of row row0 + b
+        for (int e = threadIdx.x; e < 4 * nb * N; e += kStaticThreads) {
+            const int t = e / N, k = e % N, b = t >> 2, q = t & 3;
+            const V* src = w2 + ((long long)q * a.ny + row0 + b) * a.ld2;
+            V xk = k < a.kin ? src[k] : zero;
+            V xn = N - k < a.kin ? src[N - k] : zero;
+            if (k == 0) { xk.y = 0.f; xn.y = 0.f; }
+            s[fft::pad<V>(e)] = fft::c2r_pack(xk, xn, k, post);
+        }
+        __syncthreads();
+        const float* sr = reinterpret_cast<const float*>(fft::block_fft_s<N, VPT, true, GT>(s, s2, 4 * nb, tw));
+        for (int e = threadIdx.x; e < nb * 2 * N; e += kStaticThreads) {
+            const int b = e / (2 * N), iX = e % (2 * N);
+            const int base = 4 * b * N + (iX >> 1), c = iX & 1;
+            epi.store(iX, row0 + b, sr[2 * fft::pad<V>(base) + c], sr[2 * fft::pad<V>(base + N) + c],
+                      sr[2 * fft::pad<V>(base + 2 * N) + c], sr[2 * fft::pad<V>(base + 3 * N) + c]);
+        }
+    }
+}
+
+// (vorticity column length, psi column length = psi row length) with a static kernel set,
+// and the shape those kernels run: planes per column group, rows per inverse-row group,
+// tables in global memory
+#define CMM_PSI_STATIC(X) X(512, 256) X(1024, 512) X(2048, 1024) X(4096, 2048)
+constexpr int kStaticPQ = 2, kStaticNBR = 1;
+constexpr bool kStaticGT = false;
+
 }  // namespace psi
 }  // namespace cmm
 
@@ -238,6 +357,7 @@ struct Layout {
     long long ld = 0;        // row stride of both intermediate arrays (complex values)
     int nb_inv = 0, C = 0;   // psi rows per inverse-row group, columns per column group
     int vpt = 0;             // values per thread of both kernels
+    bool stat = false;       // FP32 power-of-two sizes with a static kernel set (CMM_PSI_STATIC)
     size_t smem_cols = 0, smem_inv = 0;
     long long w1_values = 0, w2_values = 0;   // complex values of the intermediate arrays
 };
@@ -273,6 +393,17 @@ Layout make_layout(const Grid& gv, const Grid& gp, double freq, const fft::Plan2
     L.w1_values = (long long)gv.NY * L.ld;
     L.w2_values = 4ll * gp.NY * L.ld;
     L.ok = true;
+    if (sizeof(T) == 4 && gp.NX == gp.NY) {
+#define X(NV, NP)                                                                                       \
+        if (gv.NY == NV && gp.NY == NP && pv.ry.tlen == fft::sp::tlen(NV) && pp.ry.tlen == fft::sp::tlen(NP) && \
+            pp.rx.tlen == fft::sp::tlen(NP / 2)) {                                                      \
+            L.stat = true;                                                                              \
+            L.smem_cols = cols_s_smem<NV, NP, kStaticPQ, kStaticGT>();                                  \
+            L.smem_inv = rows_inv_s_smem<NP / 2, kStaticNBR, kStaticGT>();                              \
+        }
+        CMM_PSI_STATIC(X)
+#undef X
+    }
     return L;
 }
 
@@ -291,6 +422,28 @@ void prepare()
     set_smem_limits<T, fft::kPow2x3, Shape<T>::VPT, Epi>();
     set_smem_limits<T, fft::kPow2, Shape<T>::VPT_LONG, Epi>();
     set_smem_limits<T, fft::kPow2x3, Shape<T>::VPT_LONG, Epi>();
+    if (sizeof(T) == 4) {
+#define X(NV, NP)                                                                                       \
+        cudaFuncSetAttribute(k_psi_cols_s<NV, NP, kStaticPQ, kStaticGT>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                             200 * 1024);                                                               \
+        cudaFuncSetAttribute(k_psi_rows_inv_s<NP / 2, kStaticNBR, kStaticGT, Epi>,                       \
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        CMM_PSI_STATIC(X)
+#undef X
+    }
+}
+
+// the static column and inverse-row kernels (FP32, L.stat) of one shape
+template <int NV, int NP, int PQ, int NBR, bool GT, class Epi>
+void launch_static(const ColsArgs& c, const RowsInvArgs& v, const Epi& epi, cudaStream_t s)
+{
+    constexpr size_t smc = cols_s_smem<NV, NP, PQ, GT>(), smi = rows_inv_s_smem<NP / 2, NBR, GT>();
+    const void* fc = reinterpret_cast<const void*>(k_psi_cols_s<NV, NP, PQ, GT>);
+    k_psi_cols_s<NV, NP, PQ, GT><<<fft::resident_grid(fc, kStaticThreads, smc, (4 / PQ) * (long long)c.ncols),
+                                   kStaticThreads, smc, s>>>(c);
+    const void* fi = reinterpret_cast<const void*>(k_psi_rows_inv_s<NP / 2, NBR, GT, Epi>);
+    k_psi_rows_inv_s<NP / 2, NBR, GT, Epi><<<fft::resident_grid(fi, kStaticThreads, smi, (v.ny + NBR - 1) / NBR),
+                                             kStaticThreads, smi, s>>>(v, epi);
 }
 
 inline int threads_for(int values, int vpt)
@@ -309,6 +462,19 @@ cudaError_t launch_fam(const Layout& L, const Grid& gv, const Grid& gp, double f
     ColsArgs c;
     c.w1 = w1; c.w2 = w2; c.ld1 = L.ld; c.ld2 = L.ld; c.kv = L.kv; c.ncols = L.ncols; c.C = L.C;
     c.gv = gv; c.gp = gp; c.freq = freq; c.Pv = pv.ry; c.Pp = pp.ry; c.twv = pv.twy; c.twp = pp.twy;
+    if (L.stat) {
+        RowsInvArgs v;
+        v.w2 = w2; v.ld2 = L.ld; v.kin = L.ncols; v.nx = gp.NX; v.ny = gp.NY; v.nb = kStaticNBR; v.P = pp.rx;
+        v.tw = pp.twx;
+#define X(NV, NP)                                                                                       \
+        if (gv.NY == NV && gp.NY == NP) {                                                               \
+            launch_static<NV, NP, kStaticPQ, kStaticNBR, kStaticGT>(c, v, epi, s);                      \
+            return cudaGetLastError();                                                                  \
+        }
+        CMM_PSI_STATIC(X)
+#undef X
+        return cudaErrorInvalidValue;
+    }
     const int tc = threads_for(L.C * std::max(gv.NY, gp.NY), VPT);
     const long long gc = 4ll * ((L.ncols + L.C - 1) / L.C);
     k_psi_cols<T, FAM, VPT><<<fft::resident_grid(reinterpret_cast<const void*>(k_psi_cols<T, FAM, VPT>), tc, L.smem_cols,

@@ -9,7 +9,8 @@ Tolerances: relative L-infinity against the largest output magnitude,
 2e-15 * log2(N) in FP64 (rounding of a Stockham FFT grows like log N) and
 3e-7 * log2(N) in FP32.  Lengths cover the radix families (powers of two,
 3 * 2^k of the ensemble sizes, factors 5, 7, 11, 13), the longest rows (16384
-reals) and columns (8192), batches, and the psi solve's sizes.
+reals) and columns (8192), batches, and the psi solve's sizes; FP32 rows of 256 to
+4096 reals run the compile-time-length kernel.
 """
 import numpy as np
 import pytest
@@ -20,7 +21,7 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 SHAPES = [(64, 64), (128, 96), (96, 128), (256, 256), (384, 192), (1024, 1024), (2048, 2048), (60, 40),
-          (154, 52), (70, 26), (16384, 4), (8, 8192), (4, 4096)]
+          (154, 52), (70, 26), (16384, 4), (8, 8192), (4, 4096), (4096, 16), (512, 8)]
 
 
 def tol(nx, ny, prec):

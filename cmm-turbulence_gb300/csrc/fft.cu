@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "fft.hpp"
+#include "pdl.cuh"
 
 namespace cmm {
 namespace fft {
@@ -159,6 +160,8 @@ __global__ void __launch_bounds__(kStaticThreads, GT ? 4 : 3) k_rows_r2c_s(RowsA
     }
     const V* post = tw + sp::tlen(N);
     const int stride = gridDim.x * a.nb;
+    pdl_launch();
+    pdl_wait();   // the rows come from the previous kernel
     if (blockIdx.x * a.nb < a.rows_total) rows_prefetch_s<N>(a, cur, blockIdx.x * a.nb);
     asm volatile("cp.async.commit_group;");
     for (int row0 = blockIdx.x * a.nb; row0 < a.rows_total; row0 += stride) {
@@ -321,8 +324,8 @@ bool launch_rows_static(int n, long long groups, size_t sm, cudaStream_t s, cons
 #define X(N)                                                                                           \
     if (n == N) {                                                                                      \
         const void* f = reinterpret_cast<const void*>(k_rows_r2c_s<N, kStaticGT>);                     \
-        k_rows_r2c_s<N, kStaticGT><<<resident_grid(f, kStaticThreads, sm, groups), kStaticThreads, sm, s>>>(a); \
-        return true;                                                                                   \
+        return launch_pdl(k_rows_r2c_s<N, kStaticGT>, resident_grid(f, kStaticThreads, sm, groups), kStaticThreads, \
+                          sm, s, a) == cudaSuccess;                                                    \
     }
     CMM_FFT_STATIC_ROWS(X)
 #undef X

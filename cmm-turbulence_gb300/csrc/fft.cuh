@@ -321,8 +321,8 @@ __device__ __forceinline__ V* block_fft_pp(V* a, V* b, int nb, const RadixPlan& 
 }
 
 // ---------------------------------------------------------------- compile-time plans
-// The radix sequence, spans and table offsets of make_radix_plan for a length known at
-// compile time (power of two: 8s, then a 4, or 4 4 in place of a trailing 8 2, or a 2).
+// The radix sequence, spans and table offsets of make_radix_plan for a length 2^a 3^b known
+// at compile time (8s, then a 4, or 4 4 in place of a trailing 8 2, or a 2; then 3s).
 namespace sp {
 constexpr int radix(int n, int q)
 {
@@ -335,8 +335,19 @@ constexpr int radix(int n, int q)
         else rs[c++] = 2;
         m /= 2;
     }
+    while (m % 3 == 0) { rs[c++] = 3; m /= 3; }
     return q < c ? rs[q] : 1;
 }
+// n = 2^a 3^b >= 2
+constexpr bool supported(int n)
+{
+    if (n < 2) return false;
+    int m = n;
+    while (m % 2 == 0) m /= 2;
+    while (m % 3 == 0) m /= 3;
+    return m == 1;
+}
+constexpr int gcd(int a, int b) { return b == 0 ? a : gcd(b, a % b); }
 constexpr int npass(int n) { int c = 0; while (radix(n, c) > 1) ++c; return c; }
 constexpr int span(int n, int q) { int s = 1; for (int i = 0; i < q; ++i) s *= radix(n, i); return s; }
 constexpr int toff(int n, int q) { int o = 0; for (int i = 0; i < q; ++i) o += span(n, i) * (radix(n, i) - 1); return o; }
@@ -347,7 +358,7 @@ constexpr bool pow2(int n) { return n >= 2 && (n & (n - 1)) == 0; }
 constexpr bool pad_linear(int n, int q, int S)
 {
     const int R = radix(n, q), P = span(n, q), nR = n / R;
-    const int nbt = n >= (1 << S) ? 2 : 2 * ((1 << S) / n) + 1;
+    const int nbt = (1 << S) / gcd(n, 1 << S) + 1;   // b n mod 2^S repeats with this period
     for (int t = 0; t < nbt * nR; ++t) {
         const int b = t / nR, i = t % nR, k = i % P;
         const int x0 = b * n + i, d0 = b * n + (i - k) * R + k;
@@ -371,56 +382,91 @@ template <> struct PadShift<double2> { static constexpr int value = 3; };
 // stride divides L, the offsets' low S bits are multiples of it, and the low S bits of x0
 // (d0) leave room for them below L.  Either way no carry crosses bit S, (x0 + c) >> S =
 // (x0 >> S) + (c >> S) and pad(x0 + c) = pad(x0) + padc(c): one address register per
-// butterfly and an immediate per value.  sp::pad_linear checks this for every instantiated
-// pass at compile time.
+// butterfly and an immediate per value.  sp::pad_linear checks this at compile time for each
+// pass (it holds for every power-of-two pass); a pass where it fails (lengths with a factor
+// 3) computes the padded index of each value.
 template <typename V> __host__ __device__ constexpr int padc(int c) { return c + (c >> PadShift<V>::value); }
 
+// The butterfly of pass Q of the length-N plan whose first input is x0 = b N + i (k = i mod
+// p): reads the R inputs (from `in`, unpadded when UIN), twiddles, transforms; d0: the first
+// output index.  LIN (sp::pad_linear): the padded offsets are immediates.  The k = 0
+// twiddles (exactly 1) are applied like the others: values equal those of the plan-driven
+// passes up to the sign of zeros.  GT: the table is in global memory (read through the L1
+// cache), else in shared memory.
+template <int N, int Q, bool INV, bool GT, bool UIN, typename V>
+__device__ __forceinline__ void sbutterfly(const V* __restrict__ in, int t, const V* tw, V* v, int& d0)
+{
+    constexpr int R = sp::radix(N, Q), P = sp::span(N, Q), nR = N / R;
+    constexpr bool LIN = sp::pad_linear(N, Q, PadShift<V>::value);
+    const int b = t / nR, i = t % nR, k = i % P;
+    const int x0 = b * N + i;
+    d0 = b * N + (i - k) * R + k;
+    if (UIN) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = in[x0 + r * nR];
+    } else if (LIN) {
+        const V* src = in + pad<V>(x0);
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = src[padc<V>(r * nR)];
+    } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = in[pad<V>(x0 + r * nR)];
+    }
+    if (P > 1) {
+        const V* tk = tw + sp::toff(N, Q) + k * (R - 1);
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+            V w = GT ? __ldg(tk + r - 1) : tk[r - 1];
+            if (INV) w = cconj(w);
+            v[r] = cmul(v[r], w);
+        }
+    }
+    if (R == 2) dft2(v);
+    else if (R == 4) dft4(v, INV);
+    else if (R == 8) dft8(v, INV);
+    else dft3(v, INV);
+}
+
+// the R outputs of a butterfly from d0
+template <int N, int Q, typename V>
+__device__ __forceinline__ void sstore(V* __restrict__ out, int d0, const V* v)
+{
+    constexpr int R = sp::radix(N, Q), P = sp::span(N, Q);
+    if (sp::pad_linear(N, Q, PadShift<V>::value)) {
+        V* dst = out + pad<V>(d0);
+#pragma unroll
+        for (int r = 0; r < R; ++r) dst[padc<V>(r * P)] = v[r];
+    } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) out[pad<V>(d0 + r * P)] = v[r];
+    }
+}
+
 // pass Q of the length-N plan from `in` to `out` (ping-pong, one barrier), nb transforms,
-// VPT values per thread of the block (nb N <= VPT blockDim.x).  Every index is a shift or
-// mask by a constant.  The k = 0 twiddles (exactly 1) are applied like the others: the
-// values equal those of pass_pp up to the sign of zeros.
-// GT: the table is in global memory (read through the L1 cache), else in shared memory.
-// UIN: `in` holds the transforms unpadded (x at in[b n + i]): the first pass may read a
-// buffer filled by 16-byte copies (its reads, consecutive i per warp, need no padding).
+// VPT values per thread of the block (nb N <= VPT blockDim.x).  Every index is a constant
+// shift, mask or division.  UIN: `in` holds the transforms unpadded (x at in[b n + i]): the
+// first pass may read a buffer filled by 16-byte copies (its reads, consecutive i per warp,
+// need no padding).
 template <int N, int Q, int VPT, bool INV, bool GT, bool UIN = false, typename V>
 __device__ __forceinline__ void spass(const V* __restrict__ in, V* __restrict__ out, int nb, const V* tw)
 {
-    constexpr int R = sp::radix(N, Q), P = sp::span(N, Q), nR = N / R, B = (VPT + R - 1) / R;
-    static_assert(sp::pow2(N), "static passes are for power-of-two lengths");
-    static_assert(sp::pad_linear(N, Q, PadShift<V>::value), "padded offsets of this pass are not constants");
+    constexpr int R = sp::radix(N, Q), nR = N / R, B = (VPT + R - 1) / R;
+    static_assert(sp::supported(N), "static passes are for lengths 2^a 3^b");
     const int total = nb * nR;
-    const V* ptw = tw + sp::toff(N, Q);
 #pragma unroll
     for (int j = 0; j < B; ++j) {
         const int t = threadIdx.x + j * blockDim.x;
         if (t < total) {
-            const int b = t / nR, i = t % nR, k = i % P;
-            const int x0 = b * N + i, d0 = b * N + (i - k) * R + k;
-            const V* src = in + (UIN ? x0 : pad<V>(x0));
             V v[R];
-#pragma unroll
-            for (int r = 0; r < R; ++r) v[r] = src[UIN ? r * nR : padc<V>(r * nR)];
-            if (P > 1) {
-                const V* tk = ptw + k * (R - 1);
-#pragma unroll
-                for (int r = 1; r < R; ++r) {
-                    V w = GT ? __ldg(tk + r - 1) : tk[r - 1];
-                    if (INV) w = cconj(w);
-                    v[r] = cmul(v[r], w);
-                }
-            }
-            if (R == 2) dft2(v);
-            else if (R == 4) dft4(v, INV);
-            else dft8(v, INV);
-            V* dst = out + pad<V>(d0);
-#pragma unroll
-            for (int r = 0; r < R; ++r) dst[padc<V>(r * P)] = v[r];
+            int d0;
+            sbutterfly<N, Q, INV, GT, UIN>(in, t, tw, v, d0);
+            sstore<N, Q>(out, d0, v);
         }
     }
     __syncthreads();
 }
 
-// every pass of nb length-N transforms (N a power of two) between a and b (both of
+// every pass of nb length-N transforms (N = 2^a 3^b) between a and b (both of
 // padded_len(nb N) values); returns the buffer holding the results.  UIN0: a holds the
 // input unpadded.  The caller synchronises after filling a.
 template <int N, int VPT, bool INV, bool GT, bool UIN0 = false, int Q = 0, typename V>

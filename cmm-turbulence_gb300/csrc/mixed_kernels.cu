@@ -18,6 +18,7 @@
 
 #include "init_conditions.cuh"
 #include "mixed.hpp"
+#include "pdl.cuh"
 #include "psi_solve.cuh"
 
 namespace cmm {
@@ -387,9 +388,11 @@ template <int TI>
 __global__ void __launch_bounds__(256) k_advect_m(const AdvectMArgs a, int lpn_log2)
 {
     __shared__ float sc[4][kMaxFoot];
+    pdl_launch();
     if (threadIdx.x < 4 * kMaxFoot) sc[threadIdx.x / kMaxFoot][threadIdx.x % kMaxFoot] =
         a.coef[threadIdx.x / kMaxFoot][threadIdx.x % kMaxFoot];
     __syncthreads();
+    pdl_wait();
     advect_m_tile<TI>(a, lpn_log2, blockIdx.x * (long long)blockDim.x + threadIdx.x, sc);
 }
 
@@ -577,17 +580,18 @@ cudaError_t launch_advect_m(const AdvectMArgs& a, cudaStream_t s)
         }
         return cudaGetLastError();
     }
+    cudaError_t e;
     switch (a.time_integration_num) {
-        case 10: k_advect_m<10><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
-        case 21: k_advect_m<21><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
-        case 30: k_advect_m<30><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
-        case 20: k_advect_m<20><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
-        case 40: k_advect_m<40><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
-        case 31: k_advect_m<31><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
-        case 41: k_advect_m<41><<<blocks, 256, 0, s>>>(a, lpn_log2); break;
+        case 10: e = launch_pdl(k_advect_m<10>, blocks, 256, 0, s, a, lpn_log2); break;
+        case 21: e = launch_pdl(k_advect_m<21>, blocks, 256, 0, s, a, lpn_log2); break;
+        case 30: e = launch_pdl(k_advect_m<30>, blocks, 256, 0, s, a, lpn_log2); break;
+        case 20: e = launch_pdl(k_advect_m<20>, blocks, 256, 0, s, a, lpn_log2); break;
+        case 40: e = launch_pdl(k_advect_m<40>, blocks, 256, 0, s, a, lpn_log2); break;
+        case 31: e = launch_pdl(k_advect_m<31>, blocks, 256, 0, s, a, lpn_log2); break;
+        case 41: e = launch_pdl(k_advect_m<41>, blocks, 256, 0, s, a, lpn_log2); break;
         default: return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -1134,6 +1138,8 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_sample_m4(Grid gm, Grid go, Grid gf, int rf, const float4* __restrict__ map,
                                                    const float4* __restrict__ W, T* __restrict__ out)
 {
+    pdl_launch();
+    pdl_wait();
     const int iX = blockIdx.x * blockDim.x + threadIdx.x, iY = blockIdx.y;
     const float v = sample_m4_value(gm, go, gf, rf, map, W, iX, iY);
     if (iX < go.NX) out[(long long)iY * go.NX + iX] = (T)v;
@@ -1198,7 +1204,7 @@ void sample_m_dispatch(dim3 blocks, cudaStream_t s, const Grid& gm, const Grid& 
     switch (ro) {
         case 1: k_sample_m<T, 1><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out); break;
         case 2: k_sample_m<T, 2><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out); break;
-        case 4: k_sample_m4<T><<<blocks, 256, 0, s>>>(gm, go, gf, rf, map, W, out); break;
+        case 4: launch_pdl(k_sample_m4<T>, blocks, 256, 0, s, gm, go, gf, rf, map, W, out); break;
         case 8: k_sample_m<T, 8><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out); break;
         default: k_sample_m<T, 0><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out); break;
     }
@@ -1369,6 +1375,8 @@ __device__ __forceinline__ void inertial_step_m(const StageVel& V, float dt, flo
 template <int TI, bool INERT>
 __global__ void __launch_bounds__(256) k_particles_m(const PartM a)
 {
+    pdl_launch();
+    pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.num) return;
     ulonglong2 P = a.pos[i];
@@ -1462,8 +1470,8 @@ cudaError_t launch_particles_m(const Grid& gp, unsigned long long* pos, int num,
     PartM a{gp, P, vel, num, psiA, psi0, psiC, psiB, (float)dt, (float)tau, sx, sy};
 #define CMM_PM(TT)                                                         \
     do {                                                                   \
-        if (inert) k_particles_m<TT, true><<<blocks, 256, 0, s>>>(a);      \
-        else k_particles_m<TT, false><<<blocks, 256, 0, s>>>(a);           \
+        if (inert) launch_pdl(k_particles_m<TT, true>, blocks, 256, 0, s, a);  \
+        else launch_pdl(k_particles_m<TT, false>, blocks, 256, 0, s, a);       \
     } while (0)
     switch (ti) {
         case 10: CMM_PM(10); break;

@@ -30,6 +30,7 @@
 
 #include "cmm_common.cuh"
 #include "fft.hpp"
+#include "pdl.cuh"
 
 namespace cmm {
 namespace psi {
@@ -265,6 +266,8 @@ __global__ void __launch_bounds__(kStaticThreads, 3) k_psi_cols_s(ColsArgs a)
         tv = stv;
         tp = stp;
     }
+    pdl_launch();
+    pdl_wait();   // the row spectra come from the previous kernel
     const V* w1 = reinterpret_cast<const V*>(a.w1);
     const float freq = (float)a.freq, inv_nv = (float)(1.0 / (double)a.gv.N);
     constexpr int nq = 4 / PQ;
@@ -308,6 +311,8 @@ __global__ void __launch_bounds__(kStaticThreads, 4) k_psi_rows_inv_s(RowsInvArg
         fft::load_table(stw, tw, fft::sp::tlen(N) + N + 1);
         tw = stw;
     }
+    pdl_launch();
+    pdl_wait();   // the column spectra come from the previous kernel
     const V* post = tw + fft::sp::tlen(N);
     const V zero = fft::mk(0.f, 0.f);
     const V* w2 = reinterpret_cast<const V*>(a.w2);
@@ -439,11 +444,11 @@ void launch_static(const ColsArgs& c, const RowsInvArgs& v, const Epi& epi, cuda
 {
     constexpr size_t smc = cols_s_smem<NV, NP, PQ, GT>(), smi = rows_inv_s_smem<NP / 2, NBR, GT>();
     const void* fc = reinterpret_cast<const void*>(k_psi_cols_s<NV, NP, PQ, GT>);
-    k_psi_cols_s<NV, NP, PQ, GT><<<fft::resident_grid(fc, kStaticThreads, smc, (4 / PQ) * (long long)c.ncols),
-                                   kStaticThreads, smc, s>>>(c);
+    launch_pdl(k_psi_cols_s<NV, NP, PQ, GT>, fft::resident_grid(fc, kStaticThreads, smc, (4 / PQ) * (long long)c.ncols),
+               kStaticThreads, smc, s, c);
     const void* fi = reinterpret_cast<const void*>(k_psi_rows_inv_s<NP / 2, NBR, GT, Epi>);
-    k_psi_rows_inv_s<NP / 2, NBR, GT, Epi><<<fft::resident_grid(fi, kStaticThreads, smi, (v.ny + NBR - 1) / NBR),
-                                             kStaticThreads, smi, s>>>(v, epi);
+    launch_pdl(k_psi_rows_inv_s<NP / 2, NBR, GT, Epi>, fft::resident_grid(fi, kStaticThreads, smi, (v.ny + NBR - 1) / NBR),
+               kStaticThreads, smi, s, v, epi);
 }
 
 inline int threads_for(int values, int vpt)

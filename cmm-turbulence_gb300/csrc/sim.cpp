@@ -263,6 +263,9 @@ int EulerSim::alloc()
         return rc;
     CMM_CUDA(cudaMallocHost((void**)&h_scal_, sizeof(double) * 16));
     CMM_CUDA(cudaEventCreateWithFlags(&einc_ev_, cudaEventDisableTiming));
+    CMM_CUDA(cudaEventCreateWithFlags(&fork_ev_, cudaEventDisableTiming));
+    CMM_CUDA(cudaEventCreateWithFlags(&join_ev_, cudaEventDisableTiming));
+    CMM_CUDA(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
     for (auto& p : s.particles_advected) {
         double* d = nullptr;
         if ((rc = dalloc(&d, 2ll * std::max(p.num, 1)))) return rc;
@@ -418,6 +421,11 @@ void EulerSim::release()
     h_scal_ = nullptr;
     if (einc_ev_) cudaEventDestroy(einc_ev_);
     einc_ev_ = nullptr;
+    if (fork_ev_) cudaEventDestroy(fork_ev_);
+    if (join_ev_) cudaEventDestroy(join_ev_);
+    fork_ev_ = join_ev_ = nullptr;
+    if (side_) cudaStreamDestroy(side_);
+    side_ = nullptr;
     if (step_graph_) cudaGraphExecDestroy(step_graph_);
     step_graph_ = nullptr;
     destroy_plans(pf_); destroy_plans(pv_); destroy_plans(pp_); destroy_plans(pc_); destroy_plans(pd_);
@@ -1415,7 +1423,16 @@ int EulerSim::step_once()
     const bool spec = mixed_ && !vlasov_ && !ups_ && !s.forward_map;
     bool capturing = spec && use_graphs_ && !prof_ &&
                      cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    bool forked = false;   // the E_inc readback went to side_
+    auto join = [&]() -> int {
+        if (!forked) return kOk;
+        forked = false;
+        return check(cudaEventRecord(join_ev_, side_), "cudaEventRecord") ||
+               check(cudaStreamWaitEvent(stream, join_ev_, 0), "cudaStreamWaitEvent");
+    };
     auto end_capture = [&](int rc_in) -> int {
+        const int rj = join();
+        if (!rc_in) rc_in = rj;
         if (!capturing) return rc_in;
         capturing = false;
         cudaGraph_t g = nullptr;
@@ -1448,9 +1465,13 @@ int EulerSim::step_once()
     if (spec) {
         kernel_launches++;
         if ((rc = check(launch_incomp_m(gc, gf.NX / gc.NX, mapm_, d_scal_, stream), "launch_incomp_m")) ||
-            (rc = check(cudaMemcpyAsync(h_scal_, d_scal_, sizeof(double), cudaMemcpyDeviceToHost, stream), "cudaMemcpyAsync")) ||
-            (rc = check(capturing ? cudaEventRecordWithFlags(einc_ev_, stream, cudaEventRecordExternal)
-                                  : cudaEventRecord(einc_ev_, stream),
+            (rc = check(cudaEventRecord(fork_ev_, stream), "cudaEventRecord")) ||
+            (rc = check(cudaStreamWaitEvent(side_, fork_ev_, 0), "cudaStreamWaitEvent")))
+            return end_capture(rc);
+        forked = true;
+        if ((rc = check(cudaMemcpyAsync(h_scal_, d_scal_, sizeof(double), cudaMemcpyDeviceToHost, side_), "cudaMemcpyAsync")) ||
+            (rc = check(capturing ? cudaEventRecordWithFlags(einc_ev_, side_, cudaEventRecordExternal)
+                                  : cudaEventRecord(einc_ev_, side_),
                         "cudaEventRecord")))
             return end_capture(rc);
     } else if ((rc = incomp(&e_inc_))) {

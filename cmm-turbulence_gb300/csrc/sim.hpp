@@ -187,6 +187,10 @@ private:
     void rotate_psi(int n);
     void unrotate_psi(int n);
     cudaEvent_t einc_ev_ = nullptr;    // E_inc's readback (speculative psi evaluation)
+    // the readback runs on a side stream forked after the check (fork_ev_) and joined at the
+    // end of the step's front (join_ev_), so the psi solve's kernels follow the check directly
+    cudaStream_t side_ = nullptr;
+    cudaEvent_t fork_ev_ = nullptr, join_ev_ = nullptr;
     cudaGraphExec_t step_graph_ = nullptr;   // the captured front of a mixed Euler step
     bool use_graphs_ = true;
     long long graph_launches_ = 0;

@@ -83,6 +83,11 @@ cudaError_t launch_psi_solve_m(const Grid& gm, const Grid& gv, const Grid& gf, c
 // (r * Nmap^2 < 2^31)
 cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_result, cudaStream_t s,
                             const SepDrift* drift = nullptr);
+// the same check writing d_result, which must be zero on entry, and zeroing d_clear for the
+// next check (two slots used alternately: no clearing memset between the map advection and
+// the check); launched as a programmatic dependent of the previous kernel
+cudaError_t launch_incomp_m_pp(const Grid& gm, int r, const float4* map, double* d_result, double* d_clear,
+                               cudaStream_t s);
 // omega_0 through current map + n stacked maps (n * 2*Nc float4), 64-bit fixed-point
 // positions; a discrete initial field (src.kind 3) is read from its FP32 Hermite nodes disc
 // (out_f != nullptr: FP32 output instead of out)

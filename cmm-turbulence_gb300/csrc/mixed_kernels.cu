@@ -736,14 +736,19 @@ __device__ __forceinline__ void incomp_block_max(F2 best, F2* wmax, unsigned lon
     }
 }
 
+// clear (optional): a second result slot zeroed for the next check
 template <int R>
 __global__ void __launch_bounds__(256) k_incomp_m(Grid gm, int r, float ir, const float4* __restrict__ M,
-                                                  unsigned long long* result, int nx_log2)
+                                                  unsigned long long* result, int nx_log2,
+                                                  unsigned long long* clear = nullptr)
 {
     __shared__ W4f sw[kMaxCheckRatio], sd[kMaxCheckRatio];
     __shared__ F2 wmax[8];
+    pdl_launch();
     incomp_tables(gm, r, ir, sw, sd);
     __syncthreads();
+    pdl_wait();
+    if (clear && blockIdx.x == 0 && threadIdx.x == 0) *clear = 0ull;
     F2 best = {0.0f, 0.0f};
     const int total = (int)gm.N * r;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x)
@@ -764,6 +769,24 @@ __global__ void __launch_bounds__(256) k_incomp_m_drift(Grid gm, int r, float ir
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x)
         incomp_item<0>(gm, r, ir, M, i, sw, sd, best, nx_log2, &drift);
     incomp_block_max(best, wmax, result);
+}
+
+cudaError_t launch_incomp_m_pp(const Grid& gm, int r, const float4* map, double* d_result, double* d_clear,
+                               cudaStream_t s)
+{
+    if (r <= 0 || r > kMaxCheckRatio || gm.N * r > 0x7fffffffLL || d_result == d_clear) return cudaErrorInvalidValue;
+    const long long need = (gm.N * r + 255) / 256;
+    const unsigned blocks = (unsigned)(need < 152 * 8 ? need : 152 * 8);
+    const int nx_log2 = (gm.NX & (gm.NX - 1)) == 0 ? __builtin_ctz((unsigned)gm.NX) : -1;
+    unsigned long long* res = reinterpret_cast<unsigned long long*>(d_result);
+    unsigned long long* clr = reinterpret_cast<unsigned long long*>(d_clear);
+    const float ir = 1.0f / (float)r;
+    switch (r) {
+        case 2: return launch_pdl(k_incomp_m<2>, blocks, 256, 0, s, gm, r, ir, map, res, nx_log2, clr);
+        case 4: return launch_pdl(k_incomp_m<4>, blocks, 256, 0, s, gm, r, ir, map, res, nx_log2, clr);
+        case 8: return launch_pdl(k_incomp_m<8>, blocks, 256, 0, s, gm, r, ir, map, res, nx_log2, clr);
+        default: return launch_pdl(k_incomp_m<0>, blocks, 256, 0, s, gm, r, ir, map, res, nx_log2, clr);
+    }
 }
 
 cudaError_t launch_incomp_m(const Grid& gm, int r, const float4* map, double* d_result, cudaStream_t s,
@@ -1134,15 +1157,49 @@ __device__ __forceinline__ float sample_m4_value(const Grid& gm, const Grid& go,
     return herm_value_f(q, value_weights_f(c.tx, gf.hxf), value_weights_f(c.ty, gf.hyf));
 }
 
+// The kernel: a thread takes its column's four points of one map-cell row (vorticity rows
+// 4 my .. 4 my + 3), so the 8 map loads of the cell serve four points; each point's
+// contractions are those of sample_m4_value (identical values).
 template <typename T>
 __global__ void __launch_bounds__(256) k_sample_m4(Grid gm, Grid go, Grid gf, int rf, const float4* __restrict__ map,
                                                    const float4* __restrict__ W, T* __restrict__ out)
 {
     pdl_launch();
     pdl_wait();
-    const int iX = blockIdx.x * blockDim.x + threadIdx.x, iY = blockIdx.y;
-    const float v = sample_m4_value(gm, go, gf, rf, map, W, iX, iY);
-    if (iX < go.NX) out[(long long)iY * go.NX + iX] = (T)v;
+    const int iX0 = blockIdx.x * blockDim.x + threadIdx.x, my = blockIdx.y;
+    const bool live = iX0 < go.NX;
+    const int iX = live ? iX0 : go.NX - 1;        // dead lanes still take part in the quad exchange
+    const int mx = iX >> 2, k = iX & 3;
+    const int mx1 = mx + 1 == gm.NX ? 0 : mx + 1, my1 = my + 1 == gm.NY ? 0 : my + 1;
+    const int i00 = my * gm.NX + mx, i10 = my * gm.NX + mx1, i01 = my1 * gm.NX + mx, i11 = my1 * gm.NX + mx1;
+    const int comp = k == 0 ? 0 : (k == 1 ? 2 : (k == 2 ? 1 : 3));
+    const float* m = reinterpret_cast<const float*>(map);
+    const float a00 = __ldg(m + 8ll * i00 + comp), b00 = __ldg(m + 8ll * i00 + 4 + comp);
+    const float a10 = __ldg(m + 8ll * i10 + comp), b10 = __ldg(m + 8ll * i10 + 4 + comp);
+    const float a01 = __ldg(m + 8ll * i01 + comp), b01 = __ldg(m + 8ll * i01 + 4 + comp);
+    const float a11 = __ldg(m + 8ll * i11 + comp), b11 = __ldg(m + 8ll * i11 + 4 + comp);
+    const W4f w = value_weights_f((float)k * 0.25f, gm.hxf);   // sub-point k of the cell at k / 4
+    const unsigned full = 0xffffffffu;
+#pragma unroll 2
+    for (int sy = 0; sy < 4; ++sy) {
+        const W4f wy = value_weights_f((float)sy * 0.25f, gm.hyf);
+        const float C0 = fmaf(wy.w3, b01, fmaf(wy.w2, b00, fmaf(wy.w1, a01, wy.w0 * a00)));
+        const float C1 = fmaf(wy.w3, b11, fmaf(wy.w2, b10, fmaf(wy.w1, a11, wy.w0 * a10)));
+        const float VX0 = __shfl_sync(full, C0, 0, 4), VX1 = __shfl_sync(full, C1, 0, 4);
+        const float SX0 = __shfl_sync(full, C0, 1, 4), SX1 = __shfl_sync(full, C1, 1, 4);
+        const float VY0 = __shfl_sync(full, C0, 2, 4), VY1 = __shfl_sync(full, C1, 2, 4);
+        const float SY0 = __shfl_sync(full, C0, 3, 4), SY1 = __shfl_sync(full, C1, 3, 4);
+        if (live) {
+            const int iY = 4 * my + sy;
+            const float dx = fmaf(w.w3, SX1, fmaf(w.w2, SX0, fmaf(w.w1, VX1, w.w0 * VX0)));
+            const float dy = fmaf(w.w3, SY1, fmaf(w.w2, SY0, fmaf(w.w1, VY1, w.w0 * VY0)));
+            const CellF c = locate_rel(gf, iX * rf, iY * rf, dx, dy);
+            Q4 q;
+            q.c00 = __ldg(W + c.i00); q.c10 = __ldg(W + c.i10); q.c01 = __ldg(W + c.i01); q.c11 = __ldg(W + c.i11);
+            out[(long long)iY * go.NX + iX] =
+                (T)herm_value_f(q, value_weights_f(c.tx, gf.hxf), value_weights_f(c.ty, gf.hyf));
+        }
+    }
 }
 
 // omega = W(X(x)) for a map in the free-streaming frame (SepDrift): the map's FP32 displacement
@@ -1204,7 +1261,7 @@ void sample_m_dispatch(dim3 blocks, cudaStream_t s, const Grid& gm, const Grid& 
     switch (ro) {
         case 1: k_sample_m<T, 1><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out); break;
         case 2: k_sample_m<T, 2><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out); break;
-        case 4: launch_pdl(k_sample_m4<T>, blocks, 256, 0, s, gm, go, gf, rf, map, W, out); break;
+        case 4: launch_pdl(k_sample_m4<T>, dim3(blocks.x, blocks.y / 4), 256, 0, s, gm, go, gf, rf, map, W, out); break;
         case 8: k_sample_m<T, 8><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out); break;
         default: k_sample_m<T, 0><<<blocks, 256, 0, s>>>(gm, go, gf, ro, rf, iro, map, W, out); break;
     }

@@ -258,9 +258,12 @@ int EulerSim::alloc()
     if ((rc = dalloc(&real_buf_, rmax))) return rc;
     CMM_CUDA(cudaMalloc((void**)&spec_, sizeof(double2) * (size_t)cmax));
     CMM_CUDA(cudaMalloc((void**)&spec4_, sizeof(double2) * 4 * (size_t)cmax));
-    if ((rc = dalloc(&red_, 3 * kReduceBlocks)) || (rc = dalloc(&d_scal_, 16)) || (rc = dalloc(&d_params_, 10)) ||
+    if ((rc = dalloc(&red_, 3 * kReduceBlocks)) || (rc = dalloc(&d_scal_, 16)) || (rc = dalloc(&d_einc2_, 2)) ||
+        (rc = dalloc(&d_params_, 10)) ||
         (rc = dalloc(&d_rand_, kInitTable)))
         return rc;
+    CMM_CUDA(cudaMemsetAsync(d_einc2_, 0, sizeof(double) * 2, stream));
+    einc_slot_ = 0;
     CMM_CUDA(cudaMallocHost((void**)&h_scal_, sizeof(double) * 16));
     CMM_CUDA(cudaEventCreateWithFlags(&einc_ev_, cudaEventDisableTiming));
     CMM_CUDA(cudaEventCreateWithFlags(&fork_ev_, cudaEventDisableTiming));
@@ -378,7 +381,7 @@ void EulerSim::release()
     for (auto p : fparts_) f(p);
     fparts_.clear();
     for (int l = 0; l < kMaxLagrange; ++l) f(psi[l]);
-    f(real_buf_); f(spec_); f(spec4_); f(red_); f(d_scal_); f(d_params_); f(d_rand_);
+    f(real_buf_); f(spec_); f(spec4_); f(red_); f(d_scal_); f(d_einc2_); f(d_params_); f(d_rand_);
     for (auto p : parts) f(p);
     parts.clear();
     for (auto p : vels) f(p);
@@ -431,7 +434,7 @@ void EulerSim::release()
     destroy_plans(pf_); destroy_plans(pv_); destroy_plans(pp_); destroy_plans(pc_); destroy_plans(pd_);
     ChiX = ChiY = ChiX_new = ChiY_new = vort = wfine = wdisc = stack = nullptr;
     for (int l = 0; l < kMaxLagrange; ++l) psi[l] = nullptr;
-    real_buf_ = nullptr; spec_ = nullptr; spec4_ = nullptr; red_ = d_scal_ = d_params_ = d_rand_ = nullptr;
+    real_buf_ = nullptr; spec_ = nullptr; spec4_ = nullptr; red_ = d_scal_ = d_einc2_ = d_params_ = d_rand_ = nullptr;
     if (own_stream_ && stream) cudaStreamDestroy(stream);
     stream = nullptr;
     own_stream_ = false;
@@ -1464,12 +1467,15 @@ int EulerSim::step_once()
     ph_begin(kPhIncomp);
     if (spec) {
         kernel_launches++;
-        if ((rc = check(launch_incomp_m(gc, gf.NX / gc.NX, mapm_, d_scal_, stream), "launch_incomp_m")) ||
+        double* slot = d_einc2_ + einc_slot_;
+        if ((rc = check(launch_incomp_m_pp(gc, gf.NX / gc.NX, mapm_, slot, d_einc2_ + (1 - einc_slot_), stream),
+                        "launch_incomp_m")) ||
             (rc = check(cudaEventRecord(fork_ev_, stream), "cudaEventRecord")) ||
             (rc = check(cudaStreamWaitEvent(side_, fork_ev_, 0), "cudaStreamWaitEvent")))
             return end_capture(rc);
+        einc_slot_ = 1 - einc_slot_;
         forked = true;
-        if ((rc = check(cudaMemcpyAsync(h_scal_, d_scal_, sizeof(double), cudaMemcpyDeviceToHost, side_), "cudaMemcpyAsync")) ||
+        if ((rc = check(cudaMemcpyAsync(h_scal_, slot, sizeof(double), cudaMemcpyDeviceToHost, side_), "cudaMemcpyAsync")) ||
             (rc = check(capturing ? cudaEventRecordWithFlags(einc_ev_, side_, cudaEventRecordExternal)
                                   : cudaEventRecord(einc_ev_, side_),
                         "cudaEventRecord")))

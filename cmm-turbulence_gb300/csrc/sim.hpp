@@ -191,6 +191,8 @@ private:
     // end of the step's front (join_ev_), so the psi solve's kernels follow the check directly
     cudaStream_t side_ = nullptr;
     cudaEvent_t fork_ev_ = nullptr, join_ev_ = nullptr;
+    double* d_einc2_ = nullptr;   // the check's two result slots (zero when taken), used alternately
+    int einc_slot_ = 0;
     cudaGraphExec_t step_graph_ = nullptr;   // the captured front of a mixed Euler step
     bool use_graphs_ = true;
     long long graph_launches_ = 0;

@@ -34,6 +34,7 @@ struct RowsArgs {
     int rows_per_item, rows_total;
     int kio;                            // R2C: bins written; C2R: bins read (the rest zero)
     int nb;                             // rows per group
+    int tout;                           // R2C (static kernel): bin k of row r at out[k old + r]
     RadixPlan P;                        // packed complex length nx/2
     const void* tw;                     // P.tlen pass twiddles, then W^k for k <= nx/2
 };
@@ -172,10 +173,24 @@ __global__ void __launch_bounds__(kStaticThreads, GT ? 4 : 3) k_rows_r2c_s(RowsA
         asm volatile("cp.async.wait_group 1;");
         __syncthreads();
         const V* res = block_fft_s<N, kStaticVPT, false, GT, true>(cur, tmp, nb, tw);
-        for (int b = 0; b < nb; ++b) {
-            const int g = row0 + b, item = g / a.rows_per_item, r = g - item * a.rows_per_item;
-            V* dst = reinterpret_cast<V*>(a.out) + item * a.odist + r * a.old;
-            for (int k = threadIdx.x; k < a.kio; k += kStaticThreads) dst[k] = r2c_bin(res, b * N, N, k, post);
+        if (a.tout) {
+            // column-major bins (one item): rows row0 + b and row0 + b + 1 of bin k are adjacent,
+            // one 16-byte store per pair
+            V* out = reinterpret_cast<V*>(a.out);
+            for (int b = 0; b + 1 < nb; b += 2)
+                for (int k = threadIdx.x; k < a.kio; k += kStaticThreads) {
+                    const V u = r2c_bin(res, b * N, N, k, post), w = r2c_bin(res, (b + 1) * N, N, k, post);
+                    *reinterpret_cast<float4*>(out + k * a.old + row0 + b) = make_float4(u.x, u.y, w.x, w.y);
+                }
+            if (nb & 1)
+                for (int k = threadIdx.x; k < a.kio; k += kStaticThreads)
+                    out[k * a.old + row0 + nb - 1] = r2c_bin(res, (nb - 1) * N, N, k, post);
+        } else {
+            for (int b = 0; b < nb; ++b) {
+                const int g = row0 + b, item = g / a.rows_per_item, r = g - item * a.rows_per_item;
+                V* dst = reinterpret_cast<V*>(a.out) + item * a.odist + r * a.old;
+                for (int k = threadIdx.x; k < a.kio; k += kStaticThreads) dst[k] = r2c_bin(res, b * N, N, k, post);
+            }
         }
         V* t = cur;
         cur = nxt;
@@ -504,7 +519,8 @@ void plan_destroy(Plan2D& p)
 }
 
 static cudaError_t rows_launch(const Plan2D& p, bool forward, const void* in, long long ild, long long idist, void* out,
-                               long long old, long long odist, int rows_per_item, int items, int kio, cudaStream_t s)
+                               long long old, long long odist, int rows_per_item, int items, int kio, cudaStream_t s,
+                               bool tout = false)
 {
     if (!p.ok() || rows_per_item < 1 || items < 1 || kio < 0 || kio > p.nx / 2 + 1) return cudaErrorInvalidValue;
     const int n = p.nx / 2;
@@ -520,8 +536,14 @@ static cudaError_t rows_launch(const Plan2D& p, bool forward, const void* in, lo
     a.rows_per_item = rows_per_item;
     a.rows_total = rows_per_item * items;
     a.kio = kio;
-    if (forward && !p.dbl && has_static_rows(n) && p.rx.tlen == sp_tlen_pow2(n) && aligned(in, 16) && ild % 4 == 0 &&
-        idist % 4 == 0) {
+    a.tout = 0;
+    const bool stat = forward && !p.dbl && has_static_rows(n) && p.rx.tlen == sp_tlen_pow2(n) && aligned(in, 16) &&
+                      ild % 4 == 0 && idist % 4 == 0;
+    // column-major output: the static kernel, one item, 16-byte aligned row pairs
+    if (tout && (!stat || items != 1 || old % 2 != 0 || old < rows_per_item || !aligned(out, 16)))
+        return cudaErrorInvalidValue;
+    if (stat) {
+        a.tout = tout ? 1 : 0;
         a.nb = kStaticThreads * kStaticVPT / n;
         a.P = p.rx;
         a.tw = p.twx;
@@ -558,6 +580,18 @@ cudaError_t rows_r2c(const Plan2D& p, const void* in, long long ild, long long i
                      long long odist, int rows_per_item, int items, int kout, cudaStream_t s)
 {
     return rows_launch(p, true, in, ild, idist, out, old, odist, rows_per_item, items, kout, s);
+}
+
+cudaError_t rows_r2c_t(const Plan2D& p, const void* in, long long ild, void* out, long long ocol, int rows, int kout,
+                       cudaStream_t s)
+{
+    return rows_launch(p, true, in, ild, 0, out, ocol, 0, rows, 1, kout, s, true);
+}
+
+bool rows_r2c_t_supported(const Plan2D& p)
+{
+    const int n = p.nx / 2;
+    return p.ok() && !p.dbl && has_static_rows(n) && p.rx.tlen == sp_tlen_pow2(n);
 }
 
 cudaError_t rows_c2r(const Plan2D& p, const void* in, long long ild, long long idist, int kin, void* out,

@@ -51,6 +51,13 @@ cudaError_t c2r(const Plan2D& p, void* in, void* out, int batch, cudaStream_t s,
 // writing bins 0..kout-1 (row stride old, item stride odist)
 cudaError_t rows_r2c(const Plan2D& p, const void* in, long long ild, long long idist, void* out, long long old,
                      long long odist, int rows_per_item, int items, int kout, cudaStream_t s);
+// rows: R2C of one item of `rows` FP32 rows (16-byte aligned, row stride ild a multiple of 4
+// floats) writing bins 0..kout-1 column-major: bin k of row r at out[k ocol + r] (ocol even,
+// at least rows; out 16-byte aligned).  Only the compile-time power-of-two kernels
+// (rows_r2c_t_supported); cudaErrorInvalidValue otherwise
+cudaError_t rows_r2c_t(const Plan2D& p, const void* in, long long ild, void* out, long long ocol, int rows, int kout,
+                       cudaStream_t s);
+bool rows_r2c_t_supported(const Plan2D& p);
 // rows: C2R reading bins 0..kin-1 (the rest zero) of each row
 cudaError_t rows_c2r(const Plan2D& p, const void* in, long long ild, long long idist, int kin, void* out,
                      long long old, long long odist, int rows_per_item, int items, cudaStream_t s);

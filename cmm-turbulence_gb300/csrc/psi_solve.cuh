@@ -238,7 +238,9 @@ constexpr int kStaticThreads = 256;
 
 // groups (kept column, block of PQ planes), the column's PQ plane groups adjacent; the
 // forward column transform (length NV) once per group, the PQ inverse transforms (length
-// NP) as one batch.  Shared memory: padded(NV) twice, padded(PQ NP) twice (and the tables).
+// NP) as one batch.  The row spectra arrive column-major (fft::rows_r2c_t: bin col of row r
+// at w1[col ld1 + r]), so a column is one contiguous read.  Shared memory: padded(NV) twice,
+// padded(PQ NP) twice (and the tables).
 template <int NV, int NP, int PQ, bool GT>
 __host__ __device__ constexpr size_t cols_s_smem()
 {
@@ -275,7 +277,7 @@ __global__ void __launch_bounds__(kStaticThreads, 3) k_psi_cols_s(ColsArgs a)
         const int col = grp / nq, q0 = (grp - col * nq) * PQ;
         __syncthreads();   // the previous group's outputs are read
         for (int r = threadIdx.x; r < NV; r += kStaticThreads)
-            A[fft::pad<V>(r)] = col < a.kv ? w1[r * a.ld1 + col] : fft::mk(0.f, 0.f);
+            A[fft::pad<V>(r)] = col < a.kv ? w1[col * a.ld1 + r] : fft::mk(0.f, 0.f);
         __syncthreads();
         const V* FA = fft::block_fft_s<NV, VF, false, GT>(A, A2, 1, tv);
         for (int e = threadIdx.x; e < PQ * NP; e += kStaticThreads) {
@@ -401,7 +403,7 @@ Layout make_layout(const Grid& gv, const Grid& gp, double freq, const fft::Plan2
     if (sizeof(T) == 4 && gp.NX == gp.NY) {
 #define X(NV, NP)                                                                                       \
         if (gv.NY == NV && gp.NY == NP && pv.ry.tlen == fft::sp::tlen(NV) && pp.ry.tlen == fft::sp::tlen(NP) && \
-            pp.rx.tlen == fft::sp::tlen(NP / 2)) {                                                      \
+            pp.rx.tlen == fft::sp::tlen(NP / 2) && fft::rows_r2c_t_supported(pv)) {                     \
             L.stat = true;                                                                              \
             L.smem_cols = cols_s_smem<NV, NP, kStaticPQ, kStaticGT>();                                  \
             L.smem_inv = rows_inv_s_smem<NP / 2, kStaticNBR, kStaticGT>();                              \
@@ -462,10 +464,12 @@ template <typename T, int FAM, int VPT, class Epi>
 cudaError_t launch_fam(const Layout& L, const Grid& gv, const Grid& gp, double freq, const fft::Plan2D& pv,
                        const fft::Plan2D& pp, const void* omega, void* w1, void* w2, const Epi& epi, cudaStream_t s)
 {
-    cudaError_t e = fft::rows_r2c(pv, omega, gv.NX, gv.N, w1, L.ld, L.w1_values, gv.NY, 1, L.kv, s);
+    // static kernels: the kept bins column-major (kv columns of NY values: within w1_values)
+    cudaError_t e = L.stat ? fft::rows_r2c_t(pv, omega, gv.NX, w1, gv.NY, gv.NY, L.kv, s)
+                           : fft::rows_r2c(pv, omega, gv.NX, gv.N, w1, L.ld, L.w1_values, gv.NY, 1, L.kv, s);
     if (e != cudaSuccess) return e;
     ColsArgs c;
-    c.w1 = w1; c.w2 = w2; c.ld1 = L.ld; c.ld2 = L.ld; c.kv = L.kv; c.ncols = L.ncols; c.C = L.C;
+    c.w1 = w1; c.w2 = w2; c.ld1 = L.stat ? gv.NY : L.ld; c.ld2 = L.ld; c.kv = L.kv; c.ncols = L.ncols; c.C = L.C;
     c.gv = gv; c.gp = gp; c.freq = freq; c.Pv = pv.ry; c.Pp = pp.ry; c.twv = pv.twy; c.twp = pp.twy;
     if (L.stat) {
         RowsInvArgs v;

@@ -231,9 +231,10 @@ __global__ void __launch_bounds__(Shape<T>::MAXT, 1) k_psi_rows_inv(RowsInvArgs 
 
 // ---------------------------------------------------------------- static FP32 kernels
 // The same two passes for power-of-two lengths known at compile time (fft::block_fft_s:
-// every index a constant shift or mask), kStaticThreads threads.  GT: the twiddle tables
-// are read from global memory through L1 (shared memory holds only the data), else they
-// are staged in shared memory.
+// every index a constant shift or mask), kStaticThreads threads, launched as programmatic
+// dependents (each loads its tables, then waits for the previous kernel).  GT: the twiddle
+// tables are read from global memory through L1 (shared memory holds only the data), else
+// they are staged in shared memory.
 constexpr int kStaticThreads = 256;
 
 // groups (kept column, block of PQ planes), the column's PQ plane groups adjacent; the
@@ -342,8 +343,9 @@ __global__ void __launch_bounds__(kStaticThreads, 4) k_psi_rows_inv_s(RowsInvArg
 }
 
 // (vorticity column length, psi column length = psi row length) with a static kernel set,
-// and the shape those kernels run: planes per column group, rows per inverse-row group,
-// tables in global memory
+// and the shape those kernels run (chosen by timing at the metric's sizes): planes per
+// column group, rows per inverse-row group, tables in global memory (false: staged in
+// shared memory)
 #define CMM_PSI_STATIC(X) X(512, 256) X(1024, 512) X(2048, 1024) X(4096, 2048)
 constexpr int kStaticPQ = 2, kStaticNBR = 1;
 constexpr bool kStaticGT = false;

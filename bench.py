@@ -634,7 +634,7 @@ def run_ensemble(args):
     shutil.rmtree(work, ignore_errors=True)
 
 
-LEARNED = dict(blocks=6, channels=32, train_seeds=8, collect_every=32, iters=1200, batch=8, lr=1e-3,
+LEARNED = dict(blocks=6, channels=32, train_seeds=100, pairs_per_seed=200, passes=2, batch=8, lr=1e-3,
                exact_every=8, tol=1e-4)
 
 
@@ -650,11 +650,13 @@ def conv_flops_per_pixel(blocks, C=32):
 
 
 def run_learned(args):
-    """The learned psi on the metric workload: training pairs from seeded runs (seeds 1..S,
-    every 32 steps to T = 10), on-GPU training of the 6-block network, then the held-out
-    seed 0 to T = 10 three ways (exact mixed form, learned form with exact evaluation every
-    8 steps at psi tolerance 1e-4, plain FP64) plus the psi errors of the cheap, learned and
-    psi-grid evaluations along an exact run."""
+    """The learned psi on the metric workload: training pairs streamed from seeded runs
+    (seeds 1..S to T = 10, P pairs per run at evenly spaced steps: 100 x 200 = 20 000 pairs
+    by default, the size of the learned-psi configuration; the metric's seed 0 is held out),
+    each run's pairs trained on (`passes` epochs of batches) and dropped before the next run,
+    then the held-out seed 0 to T = 10 three ways (exact mixed form, learned form with exact
+    evaluation every 8 steps at psi tolerance 1e-4, plain FP64) plus the psi errors of the
+    cheap, learned and psi-grid evaluations along an exact run."""
     import __graft_entry__ as ge
     ge.build()
     m = ge.package()
@@ -668,24 +670,28 @@ def run_learned(args):
     stream = torch.cuda.Stream()
     u = m.Upsampler(blocks=L["blocks"], channels=L["channels"], seed=1, stream=stream.cuda_stream)
     t0 = time.perf_counter()
-    for seed in range(1, 1 + args.learned_seeds):
+    S, P = args.learned_seeds, args.learned_pairs_per_seed
+    steps_run = int(round(args.t10_final * WORKLOAD["steps_per_sec"]))
+    iters = max(1, L["passes"] * P // L["batch"])   # Adam steps on each run's pairs
+    losses, train_s, pairs, iterations = [], 0.0, 0, 0
+    for r, seed in enumerate(range(1, 1 + S)):
         sim = m.Simulation(["param_file=" + pf, "final_time=%g" % args.t10_final], stream=stream.cuda_stream)
         sim.set_initial_discrete(initial_vorticity(WORKLOAD["grid_fine"], seed, WORKLOAD["k0"]))
         sim.init()
         k = 0
         while sim.step(1) != 1:
             k += 1
-            if k % L["collect_every"] == 0:
+            if (k * P) // steps_run != ((k - 1) * P) // steps_run:   # P evenly spaced steps of the run
                 u.collect(sim)
         sim.close()
-    torch.cuda.synchronize()
-    gen_s = time.perf_counter() - t0
-    rounds = max(1, args.learned_iters // 100)
-    losses, train_s = [], 0.0
-    for r in range(rounds):
-        loss, sec = u.train(100, batch=L["batch"], lr=L["lr"] if r < 0.8 * rounds else L["lr"] / 5, seed=r)
+        pairs += u.dataset_size()
+        loss, sec = u.train(iters, batch=L["batch"], lr=L["lr"] if r < 0.8 * S else L["lr"] / 5, seed=r)
         losses.append(loss)
         train_s += sec
+        iterations += iters
+        u.clear_dataset()
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0 - train_s
     fwd_pp, train_pp = conv_flops_per_pixel(L["blocks"], L["channels"])
     px = WORKLOAD["grid_coarse"] ** 2
     ic = initial_vorticity(WORKLOAD["grid_fine"], WORKLOAD["seed"], WORKLOAD["k0"])
@@ -714,10 +720,11 @@ def run_learned(args):
            "network": {"blocks": L["blocks"], "channels": L["channels"], "params": u.num_params(),
                        "inputs": "psi, psi_x, psi_y, psi_xy (cheap), omega, omega_x, omega_y on 512^2",
                        "output": "sub-grid vorticity on the 1024^2 psi grid"},
-           "training": {"pairs": u.dataset_size(), "seeds": args.learned_seeds, "collect_every_steps": L["collect_every"],
-                        "pair_generation_s": gen_s, "iterations": rounds * 100, "batch": L["batch"],
-                        "device_s": train_s, "samples_per_s": rounds * 100 * L["batch"] / train_s,
-                        "conv_tflops": rounds * 100 * L["batch"] * px * train_pp / train_s / 1e12,
+           "training": {"pairs": pairs, "seeds": "1..%d (seed 0 held out)" % S, "pairs_per_run": P,
+                        "streamed": "each run's pairs trained on (%d Adam steps) and dropped" % iters,
+                        "pair_generation_s": gen_s, "iterations": iterations, "batch": L["batch"],
+                        "device_s": train_s, "samples_per_s": iterations * L["batch"] / train_s,
+                        "conv_tflops": iterations * L["batch"] * px * train_pp / train_s / 1e12,
                         "loss_first_last": [losses[0], losses[-1]], "loss": "mean relative psi-space error"},
            "exact_mixed": {k: exact[k] for k in keep},
            "learned": {k: learned[k] for k in keep + ("learned_steps", "cheap_steps", "exact_steps", "learned_checks",
@@ -943,7 +950,7 @@ def main():
                     help="with --ensemble: only this many batched iterations, without graphs (for an ncu capture)")
     ap.add_argument("--learned", action="store_true", help="train the psi upsampler and run the learned form")
     ap.add_argument("--learned-seeds", type=int, default=LEARNED["train_seeds"])
-    ap.add_argument("--learned-iters", type=int, default=LEARNED["iters"])
+    ap.add_argument("--learned-pairs-per-seed", type=int, default=LEARNED["pairs_per_seed"])
     ap.add_argument("--learned-profile", choices=["infer", "train"], help="small learned-psi runs for ncu captures")
     args = ap.parse_args()
     if args.fp64_peak:

@@ -38,7 +38,8 @@ EXPORTS = [
     "cmm_ensemble_set_profiling", "cmm_ensemble_profile",
     "cmm_ensemble_destroy", "cmm_upsampler_create", "cmm_upsampler_destroy", "cmm_upsampler_num_params",
     "cmm_upsampler_get_params", "cmm_upsampler_set_params", "cmm_upsampler_get_grads", "cmm_upsampler_set_scales",
-    "cmm_upsampler_get_scales", "cmm_upsampler_collect", "cmm_upsampler_dataset_size", "cmm_upsampler_train",
+    "cmm_upsampler_get_scales", "cmm_upsampler_collect", "cmm_upsampler_dataset_size", "cmm_upsampler_clear_dataset",
+    "cmm_upsampler_train",
     "cmm_upsampler_loss_grad", "cmm_upsampler_infer", "cmm_upsampler_evaluate", "cmm_upsampler_save",
     "cmm_upsampler_load", "cmm_attach_upsampler", "cmm_conv3x3", "cmm_conv3x3_weight_grad", "cmm_upsampler_time_infer",
     "cmm_fft_create", "cmm_fft_r2c", "cmm_fft_c2r", "cmm_fft_destroy",
@@ -140,6 +141,7 @@ def lib():
     L.cmm_upsampler_get_scales.argtypes = [vp, dp, dp]
     L.cmm_upsampler_collect.argtypes = [vp, vp]
     L.cmm_upsampler_dataset_size.argtypes = [vp]
+    L.cmm_upsampler_clear_dataset.argtypes = [vp]
     L.cmm_upsampler_train.argtypes = [vp, ip, ip, C.c_double, C.c_ulonglong, dp, dp]
     L.cmm_upsampler_loss_grad.argtypes = [vp, fp, fp, ip, ip, ip, ip, dp]
     L.cmm_upsampler_infer.argtypes = [vp, fp, ip, ip, fp]
@@ -522,6 +524,10 @@ class Upsampler:
 
     def dataset_size(self):
         return int(self.L.cmm_upsampler_dataset_size(self.h))
+
+    def clear_dataset(self):
+        """Drop the collected pairs (streamed training: collect, train, clear)."""
+        check(self.L.cmm_upsampler_clear_dataset(self.h))
 
     def train(self, iters, batch=8, lr=1e-3, seed=0):
         """-> (mean loss of the last steps, device seconds)"""

@@ -151,6 +151,13 @@ int cmm_upsampler_collect(cmm_upsampler* u, cmm_ctx* c)
 
 int cmm_upsampler_dataset_size(const cmm_upsampler* u) { return u ? u->u->dataset_size() : 0; }
 
+int cmm_upsampler_clear_dataset(cmm_upsampler* u)
+{
+    if (!u) return fail(CMM_ERR_PARAM, "upsampler is NULL");
+    u->u->clear_dataset();
+    return CMM_OK;
+}
+
 int cmm_upsampler_train(cmm_upsampler* u, int iters, int batch, double lr, unsigned long long seed, double* loss,
                         double* seconds)
 {

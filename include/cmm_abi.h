@@ -341,6 +341,10 @@ int cmm_upsampler_get_scales(const cmm_upsampler* u, double* s_in7, double* s_ou
 /* one training pair from the context's current state (its last psi must be exact) */
 int cmm_upsampler_collect(cmm_upsampler* u, cmm_ctx* c);
 int cmm_upsampler_dataset_size(const cmm_upsampler* u);
+/* drop every collected pair (their device buffers are freed, after the work queued on the
+ * device), so that training can stream pairs: collect a chunk, train on it, clear, collect
+ * the next */
+int cmm_upsampler_clear_dataset(cmm_upsampler* u);
 /* iters Adam steps (lr) on batches of `batch` pairs drawn with mt19937_64(seed); mean loss
  * of the last min(iters, 16) steps and the device seconds of the call */
 int cmm_upsampler_train(cmm_upsampler* u, int iters, int batch, double lr, unsigned long long seed, double* loss,

@@ -111,3 +111,27 @@ def test_learned_form_judge_and_fallback(trained):
     # a run of learned steps conserves like the exact one
     for q in ("enstrophy", "energy"):
         assert abs(l_[q] - s[q]) <= 1e-4 * abs(s[q]), q
+
+
+def test_dataset_clear_streams_pairs(tmp_path):
+    """Streamed training collects a run's pairs, trains on them and drops them: after
+    cmm_upsampler_clear_dataset the set is empty, collection starts again, and training
+    on the new pairs runs."""
+    m = cmm()
+    u = m.Upsampler(blocks=1, seed=2)
+    sim = m.Simulation(_args(tmp_path, "clr", final=0.25))
+    sim.set_initial_discrete(bench.initial_vorticity(4 * N, seed=5, k0=8.0))
+    sim.init()
+    for _ in range(2):
+        sim.step(1)
+        u.collect(sim)
+    assert u.dataset_size() == 2
+    u.clear_dataset()
+    assert u.dataset_size() == 0
+    sim.step(1)
+    u.collect(sim)
+    assert u.dataset_size() == 1
+    loss, sec = u.train(2, batch=1)
+    assert np.isfinite(loss) and sec > 0
+    sim.close()
+    u.close()

@@ -90,30 +90,39 @@ __device__ __forceinline__ double2 plane_mode<double2>(const double2* s, int off
     return q == 2 ? Py : make_double2(-Py.y * kx, Py.x * kx);
 }
 
-// FP32 form with 1 / N_v and the cut-off already rounded to float
-__device__ __forceinline__ float2 plane_mode_f(const float2* s, int off, int q, int iXc, int iYc, const Grid& gv,
-                                               const Grid& gp, float freq, float inv_nv)
+// FP32 form with 1 / N_v and the cut-off already rounded to float, in two parts: the mode
+// -F/(N_v k^2) of psi-grid column iXc, row iYc shared by the four planes (zero outside the
+// vorticity grid's spectrum, beyond the cut-off and at k = 0, where no division is done) and
+// the plane's derivative multiplier
+__device__ __forceinline__ float2 plane_base_f(const float2* s, int off, int iXc, int iYc, const Grid& gv,
+                                               const Grid& gp, float freq, float inv_nv, float& kx, float& ky)
 {
     const bool hx = 2 * iXc > gp.NX, hy = 2 * iYc > gp.NY;
     const int fX = hx ? gp.NX - iXc : iXc, fY = hy ? gp.NY - iYc : iYc;
-    float2 P = make_float2(0.f, 0.f);
-    if (!(2 * fX > gv.NX || 2 * fY > gv.NY)) {
-        const int iYs = iYc + (hy ? gv.NY - gp.NY : 0);
-        const float2 f = s[fft::pad<float2>(off + iYs)];
-        P = make_float2(f.x * inv_nv, f.y * inv_nv);
-    }
-    if ((float)(fX * fX + fY * fY) > freq * freq || (iXc == 0 && iYc == 0)) P = make_float2(0.f, 0.f);
-    const float kx = gp.kfxf * (float)(hx ? iXc - gp.NX : iXc);
-    const float ky = gp.kfyf * (float)(hy ? iYc - gp.NY : iYc);
-    if (iXc == 0 && iYc == 0) P = make_float2(0.f, 0.f);
-    else {
-        const float ik2 = 1.0f / (kx * kx + ky * ky);
-        P = make_float2(-P.x * ik2, -P.y * ik2);
-    }
+    kx = gp.kfxf * (float)(hx ? iXc - gp.NX : iXc);
+    ky = gp.kfyf * (float)(hy ? iYc - gp.NY : iYc);
+    if (2 * fX > gv.NX || 2 * fY > gv.NY || (float)(fX * fX + fY * fY) > freq * freq || (iXc == 0 && iYc == 0))
+        return make_float2(0.f, 0.f);
+    const int iYs = iYc + (hy ? gv.NY - gp.NY : 0);
+    const float2 f = s[fft::pad<float2>(off + iYs)];
+    const float ik2 = 1.0f / (kx * kx + ky * ky);
+    return make_float2(-(f.x * inv_nv) * ik2, -(f.y * inv_nv) * ik2);
+}
+
+__device__ __forceinline__ float2 plane_mul_f(float2 P, int q, float kx, float ky)
+{
     if (q == 0) return P;
     if (q == 1) return make_float2(-P.y * kx, P.x * kx);
     const float2 Py = make_float2(-P.y * ky, P.x * ky);
     return q == 2 ? Py : make_float2(-Py.y * kx, Py.x * kx);
+}
+
+__device__ __forceinline__ float2 plane_mode_f(const float2* s, int off, int q, int iXc, int iYc, const Grid& gv,
+                                               const Grid& gp, float freq, float inv_nv)
+{
+    float kx, ky;
+    const float2 P = plane_base_f(s, off, iXc, iYc, gv, gp, freq, inv_nv, kx, ky);
+    return plane_mul_f(P, q, kx, ky);
 }
 
 template <>
@@ -261,11 +270,16 @@ __global__ void __launch_bounds__(kStaticThreads, 3) k_psi_cols_s(ColsArgs a)
     V* B2 = B + fft::padded_len<V>(PQ * NP);
     const V* tv = reinterpret_cast<const V*>(a.twv);
     const V* tp = reinterpret_cast<const V*>(a.twp);
+    // the tables and each group's column arrive by 8-byte cp.async: their latencies overlap
+    auto copy8 = [](V* dst, const V* src) {
+        const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(src));
+    };
     if (!GT) {
         V* stv = B2 + fft::padded_len<V>(PQ * NP);
         V* stp = stv + fft::sp::tlen(NV);
-        fft::load_table(stv, tv, fft::sp::tlen(NV));
-        fft::load_table(stp, tp, fft::sp::tlen(NP));
+        for (int i = threadIdx.x; i < fft::sp::tlen(NV); i += kStaticThreads) copy8(stv + i, tv + i);
+        for (int i = threadIdx.x; i < fft::sp::tlen(NP); i += kStaticThreads) copy8(stp + i, tp + i);
         tv = stv;
         tp = stp;
     }
@@ -277,13 +291,20 @@ __global__ void __launch_bounds__(kStaticThreads, 3) k_psi_cols_s(ColsArgs a)
     for (int grp = blockIdx.x; grp < nq * a.ncols; grp += gridDim.x) {
         const int col = grp / nq, q0 = (grp - col * nq) * PQ;
         __syncthreads();   // the previous group's outputs are read
-        for (int r = threadIdx.x; r < NV; r += kStaticThreads)
-            A[fft::pad<V>(r)] = col < a.kv ? w1[col * a.ld1 + r] : fft::mk(0.f, 0.f);
+        for (int r = threadIdx.x; r < NV; r += kStaticThreads) {
+            if (col < a.kv) copy8(A + fft::pad<V>(r), w1 + col * a.ld1 + r);
+            else A[fft::pad<V>(r)] = fft::mk(0.f, 0.f);
+        }
+        asm volatile("cp.async.commit_group;");
+        asm volatile("cp.async.wait_group 0;");
         __syncthreads();
         const V* FA = fft::block_fft_s<NV, VF, false, GT>(A, A2, 1, tv);
-        for (int e = threadIdx.x; e < PQ * NP; e += kStaticThreads) {
-            const int qq = e / NP, r = e % NP;
-            B[fft::pad<V>(e)] = plane_mode_f(FA, 0, q0 + qq, col, r, a.gv, a.gp, freq, inv_nv);
+        // each row's mode once, then the PQ planes' multipliers
+        for (int r = threadIdx.x; r < NP; r += kStaticThreads) {
+            float kx, ky;
+            const V P = plane_base_f(FA, 0, col, r, a.gv, a.gp, freq, inv_nv, kx, ky);
+#pragma unroll
+            for (int qq = 0; qq < PQ; ++qq) B[fft::pad<V>(qq * NP + r)] = plane_mul_f(P, q0 + qq, kx, ky);
         }
         __syncthreads();
         const V* FB = fft::block_fft_s<NP, VI, true, GT>(B, B2, PQ, tp);

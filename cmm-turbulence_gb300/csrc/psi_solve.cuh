@@ -340,15 +340,29 @@ __global__ void __launch_bounds__(kStaticThreads, 4) k_psi_rows_inv_s(RowsInvArg
     const V* post = tw + fft::sp::tlen(N);
     const V zero = fft::mk(0.f, 0.f);
     const V* w2 = reinterpret_cast<const V*>(a.w2);
+    const int kin = a.kin;   // at most N + 1: the 4 NBR rows' bins fit s2
+    static_assert(4 * NBR * (N + 1) <= fft::padded_len<float2>(4 * NBR * N), "kept bins do not fit the scratch buffer");
     for (int row0 = blockIdx.x * NBR; row0 < a.ny; row0 += gridDim.x * NBR) {
         const int nb = min(NBR, a.ny - row0);
+        __syncthreads();   // the previous group's results (in s or s2) are read
+        // transform t = 4 b + q: plane q of row row0 + b.  Its kin kept bins go to s2 by 8-byte
+        // cp.async (one round trip for all of them; s2 is the transform's scratch, free until
+        // then), and the packing reads them there
+        for (int t = 0; t < 4 * nb; ++t) {
+            const V* src = w2 + ((long long)(t & 3) * a.ny + row0 + (t >> 2)) * a.ld2;
+            for (int k = threadIdx.x; k < kin; k += kStaticThreads) {
+                const unsigned sa = (unsigned)__cvta_generic_to_shared(s2 + t * kin + k);
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(src + k));
+            }
+        }
+        asm volatile("cp.async.commit_group;");
+        asm volatile("cp.async.wait_group 0;");
         __syncthreads();
-        // transform t = 4 b + q: plane q of row row0 + b
         for (int e = threadIdx.x; e < 4 * nb * N; e += kStaticThreads) {
-            const int t = e / N, k = e % N, b = t >> 2, q = t & 3;
-            const V* src = w2 + ((long long)q * a.ny + row0 + b) * a.ld2;
-            V xk = k < a.kin ? src[k] : zero;
-            V xn = N - k < a.kin ? src[N - k] : zero;
+            const int t = e / N, k = e % N;
+            const V* sb = s2 + t * kin;
+            V xk = k < kin ? sb[k] : zero;
+            V xn = N - k < kin ? sb[N - k] : zero;
             if (k == 0) { xk.y = 0.f; xn.y = 0.f; }
             s[fft::pad<V>(e)] = fft::c2r_pack(xk, xn, k, post);
         }

@@ -1,6 +1,6 @@
 // ens_fused.cuh -- one ensemble iteration in one cooperative launch (sm_103a).
 // Included at the end of mixed_kernels.cu: its stages run that file's device bodies
-// (advect_m_tile, incomp_item, compose_value, sample_m4_value / sample_m_point) and the
+// (advect_m_tile, incomp_item, compose_value, sample_m4_rows / sample_m_point) and the
 // library's FFT pieces (fft.cuh: block_fft, r2c_bin, c2r_pack; psi_solve.cuh: plane_mode),
 // so a member of the batched iteration computes what it computes alone.
 //
@@ -94,7 +94,7 @@ __device__ __forceinline__ int stage_tasks(const EnsMember& e, const EnsClass& c
         case kStFrow: return cdiv(e.gf.NY, c.nb_frow) + cdiv(2 * gm.N, kCopyChunk);
         case kStFcol: return (split ? 4 : 1) * cdiv(e.gf.NX / 2 + 1, c.C_f);
         case kStFinv: return cdiv(e.gf.NY, c.nb_finv);
-        case kStSmp: return cdiv(cdiv(e.gv.N, kT), g) + cdiv(cdiv(gm.N, kT), g);
+        case kStSmp: return cdiv(cdiv(e.gv.NX == 4 * gm.NX ? e.gv.N / 4 : e.gv.N, kT), g) + cdiv(cdiv(gm.N, kT), g);
         case kStProw: return cdiv(e.gv.NY, c.nb_prow);
         case kStPcol: return (split ? 4 : 1) * cdiv(c.ncols, c.C_p);
         case kStPinv: return cdiv(e.adv.gp.NY, c.nb_pinv);
@@ -539,31 +539,24 @@ __device__ __noinline__ void st_smp(const EnsMember& e, int t, int g, bool ident
     const Grid& gm = e.adv.gm;
     const Grid& gv = e.gv;
     const int ro = gv.NX / gm.NX, rf = e.gf.NX / gv.NX, rfc = e.gf.NX / gm.NX;
-    const int ntv = cdiv(cdiv(gv.N, kT), g);
+    // ro = 4: a tile is kT consecutive (map-cell row, vorticity column) pairs, each thread's
+    // four points the column's rows in that map-cell row (sample_m4_rows); else kT points
+    const long long nq = ro == 4 ? gv.N / 4 : gv.N;
+    const int ntv = cdiv(cdiv(nq, kT), g);
     const float iro = 1.0f / (float)ro;
     __syncthreads();   // the previous task's weight tables are read
     if (tid < ro) g_S.swx[tid] = value_weights_f((float)tid * iro, gm.hxf);   // k_ens_sample's tables
     if (tid == 0) g_S.swc = value_weights_f(0.0f * 1.0f, gm.hxf);
     __syncthreads();
     if (t < ntv && ro == 4) {
-        // two tiles at a time: their gathers are independent, so both are in flight together
-        for (int j = 0; j < g; j += 2) {
-            const long long i0 = ((long long)t * g + j) * kT;
-            if (i0 >= gv.N) break;   // block-uniform
-            const long long ia = i0 + tid, ib = ia + (j + 1 < g ? kT : gv.N);   // ib: past the end when there is no second tile
-            const bool la = ia < gv.N, lb = ib < gv.N;
-            const int yA = la ? (int)(ia / gv.NX) : gv.NY - 1, xA = la ? (int)(ia - (long long)yA * gv.NX) : gv.NX;
-            const int yB = lb ? (int)(ib / gv.NX) : gv.NY - 1, xB = lb ? (int)(ib - (long long)yB * gv.NX) : gv.NX;
-            float va, vb;
-            if (ident) {
-                va = sample_m4_value<true>(gm, gv, e.gf, rf, e.adv.out, e.wfm, xA, yA);
-                vb = sample_m4_value<true>(gm, gv, e.gf, rf, e.adv.out, e.wfm, xB, yB);
-            } else {
-                va = sample_m4_value<false>(gm, gv, e.gf, rf, e.adv.out, e.wfm, xA, yA);
-                vb = sample_m4_value<false>(gm, gv, e.gf, rf, e.adv.out, e.wfm, xB, yB);
-            }
-            if (la) e.real[ia] = va;
-            if (lb) e.real[ib] = vb;
+        for (int j = 0; j < g; ++j) {
+            const long long q0 = ((long long)t * g + j) * kT;
+            if (q0 >= nq) break;   // block-uniform
+            const long long q = q0 + tid;
+            const bool live = q < nq;   // the quad of a dead lane is dead too (nq and q0 are multiples of 4)
+            const int my = live ? (int)(q / gv.NX) : gm.NY - 1, x = live ? (int)(q - (long long)my * gv.NX) : gv.NX;
+            if (ident) sample_m4_rows<true>(gm, gv, e.gf, rf, e.adv.out, e.wfm, x, my, e.real);
+            else sample_m4_rows<false>(gm, gv, e.gf, rf, e.adv.out, e.wfm, x, my, e.real);
         }
     } else if (t < ntv) {
         for (int j = 0; j < g; ++j) {

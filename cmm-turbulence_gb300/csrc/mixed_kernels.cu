@@ -1116,68 +1116,30 @@ __global__ void __launch_bounds__(256) k_sample_m(Grid gm, Grid go, Grid gf, int
                           swx);
 }
 
-// ro = 4: the four lanes of a map cell (one quad of the warp: 256-thread blocks, go.NX a
-// multiple of 4) share the cell's y-contraction.  Lane k loads one component of the cell's
-// four nodes (X, X_x, Y, Y_x by k: 8 scalar loads) and contracts it in y (the same fmaf
-// chains as sample_m_point, so the values are identical); the quad exchanges the 8 values.
-template <bool ZM = false>
-__device__ __forceinline__ float sample_m4_value(const Grid& gm, const Grid& go, const Grid& gf, int rf,
-                                                const float4* __restrict__ map, const float4* __restrict__ W,
-                                                int iX0, int iY)
+// ro = 4.  The four lanes of a map cell (one quad of the warp: 256-thread blocks, go.NX a
+// multiple of 4) share the cell's y-contraction: lane k loads one component of the cell's four
+// nodes (X, X_x, Y, Y_x by k: 8 scalar loads), contracts it in y (the fmaf chains of
+// sample_m_point, so the values are identical) and the quad exchanges the results.  A thread
+// takes the four points of vorticity column iX0 in map-cell row my (vorticity rows 4 my ..
+// 4 my + 3), so the 8 map loads of the cell serve four points.  Lanes with iX0 >= go.NX still
+// take part in the quad exchange and write nothing.  ZM: the map is the identity (zero
+// displacement).
+template <bool ZM, typename T>
+__device__ __forceinline__ void sample_m4_rows(const Grid& gm, const Grid& go, const Grid& gf, int rf,
+                                               const float4* __restrict__ map, const float4* __restrict__ W,
+                                               int iX0, int my, T* __restrict__ out)
 {
     const bool live = iX0 < go.NX;
-    const int iX = live ? iX0 : go.NX - 1;        // dead lanes still take part in the quad exchange
+    const int iX = live ? iX0 : go.NX - 1;
     const int mx = iX >> 2, k = iX & 3;
-    const int my = iY >> 2, sy = iY & 3;
     const int mx1 = mx + 1 == gm.NX ? 0 : mx + 1, my1 = my + 1 == gm.NY ? 0 : my + 1;
     const int i00 = my * gm.NX + mx, i10 = my * gm.NX + mx1, i01 = my1 * gm.NX + mx, i11 = my1 * gm.NX + mx1;
-    const W4f wy = value_weights_f((float)sy * 0.25f, gm.hyf);
-    // component k of a = (X, Y, X_x, Y_x) and b = (X_y, Y_y, X_xy, Y_xy): lanes 0..3 take
-    // .x (VX), .z (SX), .y (VY), .w (SY)
     const int comp = k == 0 ? 0 : (k == 1 ? 2 : (k == 2 ? 1 : 3));
     const float* m = reinterpret_cast<const float*>(map);
     const float a00 = ZM ? 0.0f : __ldg(m + 8ll * i00 + comp), b00 = ZM ? 0.0f : __ldg(m + 8ll * i00 + 4 + comp);
     const float a10 = ZM ? 0.0f : __ldg(m + 8ll * i10 + comp), b10 = ZM ? 0.0f : __ldg(m + 8ll * i10 + 4 + comp);
     const float a01 = ZM ? 0.0f : __ldg(m + 8ll * i01 + comp), b01 = ZM ? 0.0f : __ldg(m + 8ll * i01 + 4 + comp);
     const float a11 = ZM ? 0.0f : __ldg(m + 8ll * i11 + comp), b11 = ZM ? 0.0f : __ldg(m + 8ll * i11 + 4 + comp);
-    const float C0 = fmaf(wy.w3, b01, fmaf(wy.w2, b00, fmaf(wy.w1, a01, wy.w0 * a00)));
-    const float C1 = fmaf(wy.w3, b11, fmaf(wy.w2, b10, fmaf(wy.w1, a11, wy.w0 * a10)));
-    const unsigned full = 0xffffffffu;
-    const float VX0 = __shfl_sync(full, C0, 0, 4), VX1 = __shfl_sync(full, C1, 0, 4);
-    const float SX0 = __shfl_sync(full, C0, 1, 4), SX1 = __shfl_sync(full, C1, 1, 4);
-    const float VY0 = __shfl_sync(full, C0, 2, 4), VY1 = __shfl_sync(full, C1, 2, 4);
-    const float SY0 = __shfl_sync(full, C0, 3, 4), SY1 = __shfl_sync(full, C1, 3, 4);
-    if (!live) return 0.0f;
-    const W4f w = value_weights_f((float)k * 0.25f, gm.hxf);   // sub-point k of the cell at k / 4
-    const float dx = fmaf(w.w3, SX1, fmaf(w.w2, SX0, fmaf(w.w1, VX1, w.w0 * VX0)));
-    const float dy = fmaf(w.w3, SY1, fmaf(w.w2, SY0, fmaf(w.w1, VY1, w.w0 * VY0)));
-    const CellF c = locate_rel(gf, iX * rf, iY * rf, dx, dy);
-    Q4 q;
-    q.c00 = __ldg(W + c.i00); q.c10 = __ldg(W + c.i10); q.c01 = __ldg(W + c.i01); q.c11 = __ldg(W + c.i11);
-    return herm_value_f(q, value_weights_f(c.tx, gf.hxf), value_weights_f(c.ty, gf.hyf));
-}
-
-// The kernel: a thread takes its column's four points of one map-cell row (vorticity rows
-// 4 my .. 4 my + 3), so the 8 map loads of the cell serve four points; each point's
-// contractions are those of sample_m4_value (identical values).
-template <typename T>
-__global__ void __launch_bounds__(256) k_sample_m4(Grid gm, Grid go, Grid gf, int rf, const float4* __restrict__ map,
-                                                   const float4* __restrict__ W, T* __restrict__ out)
-{
-    pdl_launch();
-    pdl_wait();
-    const int iX0 = blockIdx.x * blockDim.x + threadIdx.x, my = blockIdx.y;
-    const bool live = iX0 < go.NX;
-    const int iX = live ? iX0 : go.NX - 1;        // dead lanes still take part in the quad exchange
-    const int mx = iX >> 2, k = iX & 3;
-    const int mx1 = mx + 1 == gm.NX ? 0 : mx + 1, my1 = my + 1 == gm.NY ? 0 : my + 1;
-    const int i00 = my * gm.NX + mx, i10 = my * gm.NX + mx1, i01 = my1 * gm.NX + mx, i11 = my1 * gm.NX + mx1;
-    const int comp = k == 0 ? 0 : (k == 1 ? 2 : (k == 2 ? 1 : 3));
-    const float* m = reinterpret_cast<const float*>(map);
-    const float a00 = __ldg(m + 8ll * i00 + comp), b00 = __ldg(m + 8ll * i00 + 4 + comp);
-    const float a10 = __ldg(m + 8ll * i10 + comp), b10 = __ldg(m + 8ll * i10 + 4 + comp);
-    const float a01 = __ldg(m + 8ll * i01 + comp), b01 = __ldg(m + 8ll * i01 + 4 + comp);
-    const float a11 = __ldg(m + 8ll * i11 + comp), b11 = __ldg(m + 8ll * i11 + 4 + comp);
     const W4f w = value_weights_f((float)k * 0.25f, gm.hxf);   // sub-point k of the cell at k / 4
     const unsigned full = 0xffffffffu;
 #pragma unroll 2
@@ -1200,6 +1162,16 @@ __global__ void __launch_bounds__(256) k_sample_m4(Grid gm, Grid go, Grid gf, in
                 (T)herm_value_f(q, value_weights_f(c.tx, gf.hxf), value_weights_f(c.ty, gf.hyf));
         }
     }
+}
+
+// the kernel: one thread per vorticity column and map-cell row
+template <typename T>
+__global__ void __launch_bounds__(256) k_sample_m4(Grid gm, Grid go, Grid gf, int rf, const float4* __restrict__ map,
+                                                   const float4* __restrict__ W, T* __restrict__ out)
+{
+    pdl_launch();
+    pdl_wait();
+    sample_m4_rows<false>(gm, go, gf, rf, map, W, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y, out);
 }
 
 // omega = W(X(x)) for a map in the free-streaming frame (SepDrift): the map's FP32 displacement

@@ -612,6 +612,7 @@ __device__ __noinline__ void st_pcol(const EnsMember& e, const EnsClass& c, int 
     float2* B = A + fft::padded_len<float2>(C * nv);
     const float2* tv = g_dyn;
     const float2* tp = g_dyn + g_S.plan[0].tlen;
+    const float freq = (float)(double)e.freq, inv_nv = (float)(1.0 / (double)gv.N);
     for (int j = 0; j < g; ++j) {
         const int col0 = (t * g + j) * C;
         if (col0 >= c.ncols) break;
@@ -624,9 +625,12 @@ __device__ __noinline__ void st_pcol(const EnsMember& e, const EnsClass& c, int 
         fft_run(A, C, g_S.plan[0], tv, false, c.pow2);
         for (int qa = q0; qa < q1; qa += P) {
             const int nq = min(P, q1 - qa);   // planes in this call
-            for (int x = tid; x < nq * C * np; x += kT) {
-                const int qq = x / (C * np), y = x - qq * C * np, cc = y / np, r = y - cc * np;
-                B[fft::pad<float2>(x)] = psi::plane_mode<float2>(A, cc * nv, qa + qq, col0 + cc, r, gv, gp, (double)e.freq);
+            // each (column, row) mode once, then the call's planes' multipliers
+            for (int y = tid; y < C * np; y += kT) {
+                const int cc = y / np, r = y - cc * np;
+                float kx, ky;
+                const float2 M = psi::plane_base_f(A, cc * nv, col0 + cc, r, gv, gp, freq, inv_nv, kx, ky);
+                for (int qq = 0; qq < nq; ++qq) B[fft::pad<float2>(qq * C * np + y)] = psi::plane_mul_f(M, qa + qq, kx, ky);
             }
             __syncthreads();
             fft_run(B, nq * C, g_S.plan[1], tp, true, c.pow2);

@@ -776,16 +776,20 @@ cudaError_t launch_incomp_m_pp(const Grid& gm, int r, const float4* map, double*
 {
     if (r <= 0 || r > kMaxCheckRatio || gm.N * r > 0x7fffffffLL || d_result == d_clear) return cudaErrorInvalidValue;
     const long long need = (gm.N * r + 255) / 256;
-    const unsigned blocks = (unsigned)(need < 152 * 8 ? need : 152 * 8);
     const int nx_log2 = (gm.NX & (gm.NX - 1)) == 0 ? __builtin_ctz((unsigned)gm.NX) : -1;
     unsigned long long* res = reinterpret_cast<unsigned long long*>(d_result);
     unsigned long long* clr = reinterpret_cast<unsigned long long*>(d_clear);
     const float ir = 1.0f / (float)r;
+    // one resident wave of blocks over the grid-strided items: no tail wave
+    auto go = [&](auto kernel) {
+        const int blocks = fft::resident_grid(reinterpret_cast<const void*>(kernel), 256, 0, need);
+        return launch_pdl(kernel, (unsigned)blocks, 256, 0, s, gm, r, ir, map, res, nx_log2, clr);
+    };
     switch (r) {
-        case 2: return launch_pdl(k_incomp_m<2>, blocks, 256, 0, s, gm, r, ir, map, res, nx_log2, clr);
-        case 4: return launch_pdl(k_incomp_m<4>, blocks, 256, 0, s, gm, r, ir, map, res, nx_log2, clr);
-        case 8: return launch_pdl(k_incomp_m<8>, blocks, 256, 0, s, gm, r, ir, map, res, nx_log2, clr);
-        default: return launch_pdl(k_incomp_m<0>, blocks, 256, 0, s, gm, r, ir, map, res, nx_log2, clr);
+        case 2: return go(k_incomp_m<2>);
+        case 4: return go(k_incomp_m<4>);
+        case 8: return go(k_incomp_m<8>);
+        default: return go(k_incomp_m<0>);
     }
 }
 

@@ -142,10 +142,6 @@ def load_peaks():
 
 FP64_PEAK_TFLOPS = 1.10   # GB300 FP64 rate: `python bench.py --fp64-peak` (cuBLAS DGEMM), profiles/fp64_peak.md
 
-# DRAM bytes (read + write) per launch of a phase's dominant kernel, from one
-# ncu capture of the workload (profiles/k_particles_m_c2.md, k_advect_fp64_c2.md)
-# DRAM bytes (read + write) per launch of the roofline kernel, from the committed ncu
-# captures (profiles/k_advect_m_c2.md, profiles/k_advect_fp64_c2.md)
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the roofline kernel,
 # from one ncu capture of the same kernel on this workload; the file named beside each figure
 # holds the command and the raw numbers

@@ -537,7 +537,7 @@ static cudaError_t rows_launch(const Plan2D& p, bool forward, const void* in, lo
     a.rows_total = rows_per_item * items;
     a.kio = kio;
     a.tout = 0;
-    const bool stat = forward && !p.dbl && has_static_rows(n) && p.rx.tlen == sp_tlen_pow2(n) && aligned(in, 16) &&
+    const bool stat = forward && !p.dbl && has_static_rows(n) && sp::matches(n, p.rx) && aligned(in, 16) &&
                       ild % 4 == 0 && idist % 4 == 0;
     // column-major output: the static kernel, one item, 16-byte aligned row pairs
     if (tout && (!stat || items != 1 || old % 2 != 0 || old < rows_per_item || !aligned(out, 16)))
@@ -591,7 +591,7 @@ cudaError_t rows_r2c_t(const Plan2D& p, const void* in, long long ild, void* out
 bool rows_r2c_t_supported(const Plan2D& p)
 {
     const int n = p.nx / 2;
-    return p.ok() && !p.dbl && has_static_rows(n) && p.rx.tlen == sp_tlen_pow2(n);
+    return p.ok() && !p.dbl && has_static_rows(n) && sp::matches(n, p.rx);
 }
 
 cudaError_t rows_c2r(const Plan2D& p, const void* in, long long ild, long long idist, int kin, void* out,

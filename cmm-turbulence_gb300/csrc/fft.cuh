@@ -369,6 +369,15 @@ constexpr bool pad_linear(int n, int q, int S)
     }
     return true;
 }
+// true when the runtime plan P has the passes, spans and table offsets of the compile-time
+// plan of length n (the static kernels read P's tables with sp:: offsets)
+inline bool matches(int n, const RadixPlan& P)
+{
+    if (P.n != n || P.np != npass(n) || P.tlen != tlen(n)) return false;
+    for (int q = 0; q < P.np; ++q)
+        if (P.r[q] != radix(n, q) || P.toff[q] != toff(n, q)) return false;
+    return true;
+}
 }  // namespace sp
 
 template <typename V> struct PadShift;

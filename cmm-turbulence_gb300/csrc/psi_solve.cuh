@@ -439,8 +439,8 @@ Layout make_layout(const Grid& gv, const Grid& gp, double freq, const fft::Plan2
     L.ok = true;
     if (sizeof(T) == 4 && gp.NX == gp.NY) {
 #define X(NV, NP)                                                                                       \
-        if (gv.NY == NV && gp.NY == NP && pv.ry.tlen == fft::sp::tlen(NV) && pp.ry.tlen == fft::sp::tlen(NP) && \
-            pp.rx.tlen == fft::sp::tlen(NP / 2) && fft::rows_r2c_t_supported(pv)) {                     \
+        if (gv.NY == NV && gp.NY == NP && fft::sp::matches(NV, pv.ry) && fft::sp::matches(NP, pp.ry) &&   \
+            fft::sp::matches(NP / 2, pp.rx) && fft::rows_r2c_t_supported(pv)) {                         \
             L.stat = true;                                                                              \
             L.smem_cols = cols_s_smem<NV, NP, kStaticPQ, kStaticGT>();                                  \
             L.smem_inv = rows_inv_s_smem<NP / 2, kStaticNBR, kStaticGT>();                              \

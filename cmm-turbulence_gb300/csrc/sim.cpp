@@ -1430,8 +1430,9 @@ int EulerSim::step_once()
     auto join = [&]() -> int {
         if (!forked) return kOk;
         forked = false;
-        return check(cudaEventRecord(join_ev_, side_), "cudaEventRecord") ||
-               check(cudaStreamWaitEvent(stream, join_ev_, 0), "cudaStreamWaitEvent");
+        int rj = check(cudaEventRecord(join_ev_, side_), "cudaEventRecord");
+        if (!rj) rj = check(cudaStreamWaitEvent(stream, join_ev_, 0), "cudaStreamWaitEvent");
+        return rj;
     };
     auto end_capture = [&](int rc_in) -> int {
         const int rj = join();

@@ -333,18 +333,18 @@ size_t static_rows_smem(int n, int nb, bool gt)
     return sizeof(float2) * (3 * len + (gt ? 0 : (size_t)sp_tlen_pow2(n) + (size_t)n + 1));
 }
 
-// the static FP32 R2C kernel of packed length n, or false when there is none
-bool launch_rows_static(int n, long long groups, size_t sm, cudaStream_t s, const RowsArgs& a)
+// the static FP32 R2C kernel of packed length n (cudaErrorInvalidValue when there is none)
+cudaError_t launch_rows_static(int n, long long groups, size_t sm, cudaStream_t s, const RowsArgs& a)
 {
 #define X(N)                                                                                           \
     if (n == N) {                                                                                      \
         const void* f = reinterpret_cast<const void*>(k_rows_r2c_s<N, kStaticGT>);                     \
         return launch_pdl(k_rows_r2c_s<N, kStaticGT>, resident_grid(f, kStaticThreads, sm, groups), kStaticThreads, \
-                          sm, s, a) == cudaSuccess;                                                    \
+                          sm, s, a);                                                                   \
     }
     CMM_FFT_STATIC_ROWS(X)
 #undef X
-    return false;
+    return cudaErrorInvalidValue;
 }
 
 bool has_static_rows(int n)
@@ -548,8 +548,7 @@ static cudaError_t rows_launch(const Plan2D& p, bool forward, const void* in, lo
         a.P = p.rx;
         a.tw = p.twx;
         const long long groups = (a.rows_total + a.nb - 1) / a.nb;
-        return launch_rows_static(n, groups, static_rows_smem(n, a.nb, kStaticGT), s, a) ? cudaGetLastError()
-                                                                                        : cudaErrorInvalidValue;
+        return launch_rows_static(n, groups, static_rows_smem(n, a.nb, kStaticGT), s, a);
     }
     // rows per group: about kBlockValues values, at least one row
     const int fam = family_of(p.rx);

@@ -479,15 +479,17 @@ void prepare()
 
 // the static column and inverse-row kernels (FP32, L.stat) of one shape
 template <int NV, int NP, int PQ, int NBR, bool GT, class Epi>
-void launch_static(const ColsArgs& c, const RowsInvArgs& v, const Epi& epi, cudaStream_t s)
+cudaError_t launch_static(const ColsArgs& c, const RowsInvArgs& v, const Epi& epi, cudaStream_t s)
 {
     constexpr size_t smc = cols_s_smem<NV, NP, PQ, GT>(), smi = rows_inv_s_smem<NP / 2, NBR, GT>();
     const void* fc = reinterpret_cast<const void*>(k_psi_cols_s<NV, NP, PQ, GT>);
-    launch_pdl(k_psi_cols_s<NV, NP, PQ, GT>, fft::resident_grid(fc, kStaticThreads, smc, (4 / PQ) * (long long)c.ncols),
-               kStaticThreads, smc, s, c);
+    cudaError_t e = launch_pdl(k_psi_cols_s<NV, NP, PQ, GT>,
+                               fft::resident_grid(fc, kStaticThreads, smc, (4 / PQ) * (long long)c.ncols), kStaticThreads,
+                               smc, s, c);
+    if (e != cudaSuccess) return e;
     const void* fi = reinterpret_cast<const void*>(k_psi_rows_inv_s<NP / 2, NBR, GT, Epi>);
-    launch_pdl(k_psi_rows_inv_s<NP / 2, NBR, GT, Epi>, fft::resident_grid(fi, kStaticThreads, smi, (v.ny + NBR - 1) / NBR),
-               kStaticThreads, smi, s, v, epi);
+    return launch_pdl(k_psi_rows_inv_s<NP / 2, NBR, GT, Epi>,
+                      fft::resident_grid(fi, kStaticThreads, smi, (v.ny + NBR - 1) / NBR), kStaticThreads, smi, s, v, epi);
 }
 
 inline int threads_for(int values, int vpt)
@@ -513,10 +515,7 @@ cudaError_t launch_fam(const Layout& L, const Grid& gv, const Grid& gp, double f
         v.w2 = w2; v.ld2 = L.ld; v.kin = L.ncols; v.nx = gp.NX; v.ny = gp.NY; v.nb = kStaticNBR; v.P = pp.rx;
         v.tw = pp.twx;
 #define X(NV, NP)                                                                                       \
-        if (gv.NY == NV && gp.NY == NP) {                                                               \
-            launch_static<NV, NP, kStaticPQ, kStaticNBR, kStaticGT>(c, v, epi, s);                      \
-            return cudaGetLastError();                                                                  \
-        }
+        if (gv.NY == NV && gp.NY == NP) return launch_static<NV, NP, kStaticPQ, kStaticNBR, kStaticGT>(c, v, epi, s);
         CMM_PSI_STATIC(X)
 #undef X
         return cudaErrorInvalidValue;

@@ -174,3 +174,26 @@ def test_mixed_captured_and_plain_launches_agree(tmp_path):
     assert np.array_equal(e0, e1)
     for k in f0:
         assert np.array_equal(f0[k], f1[k]), k
+
+
+@pytest.mark.parametrize("coarse,fine,psi", [(256, 1024, 512), (1024, 4096, 2048)])
+def test_mixed_psi_solve_sizes_match_plain_fp64(tmp_path, coarse, fine, psi):
+    """The FP32 psi solve's compile-time kernels at the vorticity / psi sizes the other tests
+    do not reach (1024^2 / 512^2 and 4096^2 / 2048^2): the psi of the mixed form after its
+    initialisation and two steps against plain FP64 (relative L-infinity per Hermite plane,
+    FP32 rounding of the vorticity sample and transforms: 1e-4)."""
+    import bench
+    m = cmm()
+    ic = bench.initial_vorticity(fine, seed=2, k0=8.0)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        sim = m.Simulation(_args(tmp_path, prec, coarse, fine, psi, 256, 2.0 / 256, 1e-4, discrete=True))
+        sim.set_initial_discrete(ic)
+        sim.init()
+        sim.step(2)
+        out[prec] = sim.field("Stream_function_Psi_H_psi").reshape(4, psi, psi)
+        sim.close()
+    for q in range(4):
+        ref = out["fp64"][q]
+        err = np.max(np.abs(out["mixed"][q] - ref)) / np.max(np.abs(ref))
+        assert err < 1e-4, (q, err)
